@@ -1,0 +1,392 @@
+"""CPU oracle for Piranha's party-local share arithmetic (test infrastructure).
+
+This package is the checker. Only ``tests/``, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` may import it; the ``piranha_gb300`` product
+never does. The arithmetic lives in ``oracle.hpp`` (C++17, restating
+``src/mpc/RSS.inl`` and the ``src/gpu`` kernels of Piranha); this module only
+builds ``_build/liboracle.so`` on demand and wraps its C entry points for numpy.
+
+Array conventions
+-----------------
+* an RSS tensor of n elements is a numpy array of shape ``(3, 2, n)``:
+  ``[party A/B/C][shareA/shareB][element]``;
+* per-party public data (the output of ``reconstruct``) has shape ``(3, n)``;
+* ``Comm`` accumulates the bytes each party sends/receives and the rounds.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lock = threading.Lock()
+_lib = None
+
+FP_DEFAULT = 26
+
+FPROP, DGRAD, WGRAD = 0, 1, 2
+
+_SUF = {np.uint64: "u64", np.uint32: "u32", np.uint8: "u8"}
+_CT = {np.uint64: ctypes.c_uint64, np.uint32: ctypes.c_uint32, np.uint8: ctypes.c_uint8}
+
+
+def build() -> str:
+    """Compile the oracle with its Makefile (idempotent); return the .so path."""
+    srcs = [os.path.join(_HERE, f) for f in ("capi.cpp", "oracle.hpp")]
+    if os.path.exists(_LIB_PATH) and all(os.path.getmtime(_LIB_PATH) >= os.path.getmtime(s) for s in srcs):
+        return _LIB_PATH
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            _lib = ctypes.CDLL(build())
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Comm:
+    """Per-party byte counters and the round counter (one round per protocol step)."""
+
+    def __init__(self):
+        self.buf = np.zeros(9, dtype=np.uint64)
+
+    @property
+    def tx(self):
+        return [int(x) for x in self.buf[:3]]
+
+    @property
+    def rx(self):
+        return [int(x) for x in self.buf[4:7]]
+
+    @property
+    def rounds(self):
+        return int(self.buf[8])
+
+    def ptr(self):
+        return _p(self.buf)
+
+
+def _ring(dtype):
+    dt = np.dtype(dtype).type
+    if dt not in (np.uint64, np.uint32):
+        raise TypeError("ring must be uint64 or uint32")
+    return dt, _SUF[dt]
+
+
+def _views(a, dtype, n=None):
+    a = np.ascontiguousarray(a, dtype=dtype)
+    if a.ndim != 3 or a.shape[:2] != (3, 2) or (n is not None and a.shape[2] != n):
+        raise ValueError(f"expected RSS views of shape (3, 2, {n}), got {a.shape}")
+    return a
+
+
+# ------------------------------------------------------------------ encoding
+
+def encode(vals, dtype=np.uint64, fp=FP_DEFAULT):
+    dt, suf = _ring(dtype)
+    v = np.ascontiguousarray(vals, dtype=np.float64).ravel()
+    out = np.empty(v.size, dtype=dt)
+    getattr(lib(), f"or_encode_{suf}")(_p(v), ctypes.c_size_t(v.size), _p(out), fp)
+    return out
+
+
+def decode(x, fp=FP_DEFAULT):
+    x = np.asarray(x)
+    s = x.view(np.int64 if x.dtype == np.uint64 else np.int32)
+    return s.astype(np.float64) / float(1 << fp)
+
+
+def set_public(vals, dtype=np.uint64, fp=FP_DEFAULT, ref_compat=True):
+    """RSSBase::setPublic (RSS.inl:123-142); ref_compat keeps the PARTY_B fall-through."""
+    dt, suf = _ring(dtype)
+    v = np.ascontiguousarray(vals, dtype=np.float64).ravel()
+    out = np.zeros((3, 2, v.size), dtype=dt)
+    getattr(lib(), f"or_rss_set_public_{suf}")(_p(v), ctypes.c_size_t(v.size), _p(out), fp, int(ref_compat))
+    return out
+
+
+def from_list(vals, dtype=np.uint64, fp=FP_DEFAULT, to_fixed=True):
+    """The RSS initializer-list constructor (RSS.inl:389-414)."""
+    dt, suf = _ring(dtype)
+    v = np.ascontiguousarray(vals, dtype=np.float64).ravel()
+    out = np.zeros((3, 2, v.size), dtype=dt)
+    getattr(lib(), f"or_rss_from_list_{suf}")(_p(v), ctypes.c_size_t(v.size), _p(out), fp, int(to_fixed))
+    return out
+
+
+def share_random(secret, dtype=np.uint64, seed=0):
+    """A consistent 3-party RSS sharing of ring values with seeded random masks."""
+    dt, _ = _ring(dtype)
+    secret = np.asarray(secret, dtype=dt).ravel()
+    rng = np.random.default_rng(seed)
+    info = np.iinfo(dt)
+    x1 = rng.integers(0, info.max, size=secret.size, dtype=dt, endpoint=True)
+    x2 = rng.integers(0, info.max, size=secret.size, dtype=dt, endpoint=True)
+    with np.errstate(over="ignore"):
+        x0 = secret - x1 - x2
+    sh = [x0, x1, x2]
+    out = np.empty((3, 2, secret.size), dtype=dt)
+    for p in range(3):
+        out[p, 0] = sh[p]
+        out[p, 1] = sh[(p + 1) % 3]
+    return out
+
+
+def random_views(n, dtype=np.uint64, seed=0):
+    """Independent uniform ring values in all six share slots (arbitrary party views)."""
+    dt, _ = _ring(dtype)
+    rng = np.random.default_rng(seed)
+    return rng.integers(0, np.iinfo(dt).max, size=(3, 2, n), dtype=dt, endpoint=True)
+
+
+# ------------------------------------------------------------------ protocol
+
+def reconstruct(a, comm=None):
+    dt, suf = _ring(np.asarray(a).dtype)
+    a = _views(a, dt)
+    n = a.shape[2]
+    out = np.empty((3, n), dtype=dt)
+    comm = comm or Comm()
+    getattr(lib(), f"or_rss_reconstruct_{suf}")(_p(a), ctypes.c_size_t(n), _p(out), comm.ptr())
+    return out
+
+
+def reshare(c, comm=None):
+    dt, suf = _ring(np.asarray(c).dtype)
+    c = np.ascontiguousarray(c, dtype=dt)
+    n = c.shape[1]
+    out = np.empty((3, 2, n), dtype=dt)
+    comm = comm or Comm()
+    getattr(lib(), f"or_rss_reshare_{suf}")(_p(c), ctypes.c_size_t(n), _p(out), comm.ptr())
+    return out
+
+
+def matmul(a, b, M, N, K, tA, tB, tC, trunc, comm=None):
+    """RSS matmul (RSS.inl:482-540): localMatMul + dividePublic3out3."""
+    dt, suf = _ring(np.asarray(a).dtype)
+    a = _views(a, dt, M * K)
+    b = _views(b, dt, K * N)
+    c = np.empty((3, 2, M * N), dtype=dt)
+    comm = comm or Comm()
+    getattr(lib(), f"or_rss_matmul_{suf}")(_p(a), _p(b), _p(c), M, N, K, int(tA), int(tB), int(tC), trunc,
+                                           comm.ptr())
+    return c
+
+
+def conv_out_size(op, batch, H, W, f, Din, Dout, stride, pad):
+    P = (H + 2 * pad - f) // stride + 1
+    Q = (W + 2 * pad - f) // stride + 1
+    if op == FPROP:
+        return batch * P * Q * Dout
+    if op == DGRAD:
+        return batch * H * W * Din
+    return Dout * f * f * Din
+
+
+def convolution(a, b, op, batch, H, W, f, Din, Dout, stride, pad, trunc, comm=None):
+    """RSS convolution (RSS.inl:706-803)."""
+    dt, suf = _ring(np.asarray(a).dtype)
+    a = _views(a, dt)
+    b = _views(b, dt)
+    n_out = conv_out_size(op, batch, H, W, f, Din, Dout, stride, pad)
+    c = np.empty((3, 2, n_out), dtype=dt)
+    comm = comm or Comm()
+    getattr(lib(), f"or_rss_conv_{suf}")(_p(a), ctypes.c_size_t(a.shape[2]), _p(b), ctypes.c_size_t(b.shape[2]),
+                                         _p(c), op, batch, H, W, f, Din, Dout, stride, pad, trunc, comm.ptr())
+    return c
+
+
+def divide_public(a, d, comm=None):
+    """dividePublic (RSS.inl:423-455); d is a scalar or a per-element array."""
+    dt, suf = _ring(np.asarray(a).dtype)
+    a = _views(a, dt).copy()
+    n = a.shape[2]
+    dv = np.ascontiguousarray(np.atleast_1d(np.asarray(d, dtype=dt)))
+    vec = dv.size > 1 or (np.ndim(d) > 0)
+    if vec and dv.size != n:
+        raise ValueError("denominator vector size mismatch")
+    comm = comm or Comm()
+    getattr(lib(), f"or_rss_divide_public_{suf}")(_p(a), ctypes.c_size_t(n), _p(dv), int(vec), comm.ptr())
+    return a
+
+
+def divide_3of3(z, d, comm=None):
+    dt, suf = _ring(np.asarray(z).dtype)
+    z = np.ascontiguousarray(z, dtype=dt)
+    n = z.shape[1]
+    out = np.zeros((3, 2, n), dtype=dt)
+    comm = comm or Comm()
+    getattr(lib(), f"or_rss_divide_3of3_{suf}")(_p(z), ctypes.c_size_t(n), _CT[dt](int(d)), _p(out), comm.ptr())
+    return out
+
+
+def mul(a, b, comm=None):
+    dt, suf = _ring(np.asarray(a).dtype)
+    a = _views(a, dt).copy()
+    b = _views(b, dt, a.shape[2])
+    comm = comm or Comm()
+    getattr(lib(), f"or_rss_mul_{suf}")(_p(a), _p(b), ctypes.c_size_t(a.shape[2]), comm.ptr())
+    return a
+
+
+def and_(a, b, comm=None):
+    dt, suf = _ring(np.asarray(a).dtype)
+    a = _views(a, dt).copy()
+    b = _views(b, dt, a.shape[2])
+    comm = comm or Comm()
+    getattr(lib(), f"or_rss_and_{suf}")(_p(a), _p(b), ctypes.c_size_t(a.shape[2]), comm.ptr())
+    return a
+
+
+def _bits_suffix(dt, udt):
+    return f"{_SUF[dt]}_{_SUF[np.dtype(udt).type]}"
+
+
+def drelu(x, udtype=np.uint8, comm=None):
+    dt, _ = _ring(np.asarray(x).dtype)
+    x = _views(x, dt)
+    n = x.shape[2]
+    out = np.empty((3, 2, n), dtype=udtype)
+    comm = comm or Comm()
+    getattr(lib(), f"or_rss_drelu_{_bits_suffix(dt, udtype)}")(_p(x), ctypes.c_size_t(n), _p(out), comm.ptr())
+    return out
+
+
+def relu(x, udtype=np.uint8, comm=None):
+    dt, _ = _ring(np.asarray(x).dtype)
+    x = _views(x, dt)
+    n = x.shape[2]
+    out = np.empty((3, 2, n), dtype=dt)
+    dout = np.empty((3, 2, n), dtype=udtype)
+    comm = comm or Comm()
+    getattr(lib(), f"or_rss_relu_{_bits_suffix(dt, udtype)}")(_p(x), ctypes.c_size_t(n), _p(out), _p(dout),
+                                                              comm.ptr())
+    return out, dout
+
+
+def select_share(x, y, b, comm=None):
+    dt, _ = _ring(np.asarray(x).dtype)
+    x = _views(x, dt)
+    n = x.shape[2]
+    y = _views(y, dt, n)
+    b = np.ascontiguousarray(b)
+    z = np.empty((3, 2, n), dtype=dt)
+    comm = comm or Comm()
+    getattr(lib(), f"or_rss_select_share_{_bits_suffix(dt, b.dtype)}")(_p(x), _p(y), _p(b), _p(z),
+                                                                       ctypes.c_size_t(n), comm.ptr())
+    return z
+
+
+def maxpool(x, k, udtype=np.uint8, comm=None):
+    """RSS maxpool tournament (RSS.inl:868-1017) over rows of k (padded) values."""
+    dt, _ = _ring(np.asarray(x).dtype)
+    x = _views(x, dt)
+    n = x.shape[2]
+    out = np.empty((3, 2, n // k), dtype=dt)
+    dout = np.empty((3, 2, n), dtype=udtype)
+    comm = comm or Comm()
+    getattr(lib(), f"or_rss_maxpool_{_bits_suffix(dt, udtype)}")(_p(x), ctypes.c_size_t(n), _p(out), _p(dout), k,
+                                                                 comm.ptr())
+    return out, dout
+
+
+def maxpool_layer(x, H, W, C, pool, stride, batch, fp=FP_DEFAULT, udtype=np.uint8, comm=None):
+    """MaxpoolLayer::forward (MaxpoolLayer.cu:52-131) for RSS."""
+    dt, _ = _ring(np.asarray(x).dtype)
+    x = _views(x, dt, batch * H * W * C)
+    oh = (H - pool) // stride + 1
+    ow = (W - pool) // stride + 1
+    out = np.empty((3, 2, batch * oh * ow * C), dtype=dt)
+    dout = np.empty((3, 2, batch * oh * ow * C * pool * pool), dtype=udtype)
+    comm = comm or Comm()
+    getattr(lib(), f"or_maxpool_layer_{_bits_suffix(dt, udtype)}")(_p(x), _p(out), _p(dout), H, W, C, pool,
+                                                                   stride, batch, fp, comm.ptr())
+    return out, dout
+
+
+# -------------------------------------------------------- single-array kernels
+
+def gemm(M, N, K, A, tA, B, tB, tC, dtype=np.uint64):
+    dt, suf = _ring(dtype)
+    A = np.ascontiguousarray(A, dtype=dt)
+    B = np.ascontiguousarray(B, dtype=dt)
+    C = np.empty(M * N, dtype=dt)
+    getattr(lib(), f"or_gemm_{suf}")(M, N, K, _p(A), int(tA), _p(B), int(tB), _p(C), int(tC))
+    return C
+
+
+def conv(op, N, H, W, C, K, R, S, pad, stride, a, b, dtype=np.uint64):
+    dt, suf = _ring(dtype)
+    a = np.ascontiguousarray(a, dtype=dt)
+    b = np.ascontiguousarray(b, dtype=dt)
+    P = (H + 2 * pad - R) // stride + 1
+    Q = (W + 2 * pad - S) // stride + 1
+    n_out = {FPROP: N * P * Q * K, DGRAD: N * H * W * C, WGRAD: K * R * S * C}[op]
+    out = np.empty(n_out, dtype=dt)
+    getattr(lib(), f"or_conv_{suf}")(op, N, H, W, C, K, R, S, pad, stride, _p(a), _p(b), _p(out))
+    return out
+
+
+def maxpool_im2row(im, H, W, f, Din, batch, stride, pad, pad_val, dtype=np.uint64):
+    dt, suf = _ring(dtype)
+    im = np.ascontiguousarray(im, dtype=dt)
+    fn = getattr(lib(), f"or_maxpool_im2row_{suf}")
+    fn.restype = ctypes.c_size_t
+    n = fn(_p(im), None, ctypes.c_size_t(0), H, W, f, Din, batch, stride, pad, _CT[dt](int(pad_val) % (1 << 64)))
+    out = np.empty(n, dtype=dt)
+    fn(_p(im), _p(out), ctypes.c_size_t(n), H, W, f, Din, batch, stride, pad, _CT[dt](int(pad_val) % (1 << 64)))
+    return out
+
+
+def element_vector_add(a, b, rowwise, rows, cols, dtype=np.uint64):
+    dt, suf = _ring(dtype)
+    a = np.ascontiguousarray(a, dtype=dt).copy()
+    b = np.ascontiguousarray(b, dtype=dt)
+    getattr(lib(), f"or_element_vector_add_{suf}")(_p(a), _p(b), int(rowwise), rows, cols)
+    return a
+
+
+def reduce_sum(a, b, reduce_rows, rows, cols, dtype=np.uint64):
+    dt, suf = _ring(dtype)
+    a = np.ascontiguousarray(a, dtype=dt)
+    b = np.ascontiguousarray(b, dtype=dt).copy()
+    getattr(lib(), f"or_reduce_sum_{suf}")(_p(a), _p(b), int(reduce_rows), rows, cols)
+    return b
+
+
+def bitexpand(a, dtype=np.uint64):
+    dt, suf = _ring(dtype)
+    a = np.ascontiguousarray(a, dtype=dt)
+    bits = np.empty(a.size * np.dtype(dt).itemsize * 8, dtype=dt)
+    getattr(lib(), f"or_bitexpand_{suf}")(_p(a), ctypes.c_size_t(a.size), _p(bits))
+    return bits
+
+
+def expand_compare(b, nb, out_n):
+    b = np.ascontiguousarray(b, dtype=np.uint8)
+    nb = np.ascontiguousarray(nb, dtype=np.uint8)
+    out = np.empty(out_n, dtype=np.uint8)
+    lib().or_expand_compare_u8(_p(b), _p(nb), ctypes.c_size_t(b.size), _p(out), ctypes.c_size_t(out_n))
+    return out
+
+
+def div_public_values(x, d, dtype=np.uint64):
+    """The ring division functor alone (functors.cuh:33-45,94-105)."""
+    dt, suf = _ring(dtype)
+    x = np.ascontiguousarray(x, dtype=dt).ravel()
+    dv = np.ascontiguousarray(np.atleast_1d(np.asarray(d, dtype=dt)))
+    out = np.empty_like(x)
+    getattr(lib(), f"or_div_public_scalar_{suf}")(_p(x), ctypes.c_size_t(x.size), _p(dv), int(dv.size > 1), _p(out))
+    return out

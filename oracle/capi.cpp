@@ -1,0 +1,229 @@
+// capi.cpp — C entry points of the CPU oracle (test infrastructure only).
+//
+// Every RSS tensor crosses this boundary as one flat array laid out
+// [party(3)][share(2)][n]; per-party public data as [party(3)][n]. The comm
+// argument points at 9 uint64 counters {tx[4], rx[4], rounds} that each call
+// adds to (DeviceData.h:87-118 byte accounting, one round per protocol step).
+#include "oracle.hpp"
+
+using namespace oracle;
+
+namespace {
+
+template <typename T> void load(RSSV<T>& r, const T* flat, size_t n) {
+    r.resize(n);
+    for (int p = 0; p < 3; p++)
+        for (int s = 0; s < 2; s++) std::memcpy(r.v[p][s].data(), flat + ((size_t)p * 2 + s) * n, n * sizeof(T));
+}
+template <typename T> void store(const RSSV<T>& r, T* flat) {
+    size_t n = r.n;
+    for (int p = 0; p < 3; p++)
+        for (int s = 0; s < 2; s++) std::memcpy(flat + ((size_t)p * 2 + s) * n, r.v[p][s].data(), n * sizeof(T));
+}
+struct CommIO {
+    uint64_t* out;
+    Comm c;
+    explicit CommIO(uint64_t* o) : out(o) {}
+    ~CommIO() {
+        if (!out) return;
+        for (int p = 0; p < 4; p++) { out[p] += c.tx[p]; out[4 + p] += c.rx[p]; }
+        out[8] += c.rounds;
+    }
+};
+
+}  // namespace
+
+#define OR_RING(T, SUF)                                                                                      \
+    extern "C" int or_rss_matmul_##SUF(const T* a, const T* b, T* c, int M, int N, int K, int tA, int tB,     \
+                                       int tC, int trunc, uint64_t* comm) {                                  \
+        RSSV<T> A, B, C;                                                                                     \
+        load(A, a, (size_t)M * K);                                                                           \
+        load(B, b, (size_t)K * N);                                                                           \
+        CommIO io(comm);                                                                                     \
+        rss_matmul<T>(A, B, C, M, N, K, tA, tB, tC, trunc, io.c);                                            \
+        store(C, c);                                                                                         \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_rss_conv_##SUF(const T* a, size_t na, const T* b, size_t nb, T* c, int op, int batch,   \
+                                     int H, int W, int f, int Din, int Dout, int stride, int pad, int trunc,  \
+                                     uint64_t* comm) {                                                       \
+        RSSV<T> A, B, C;                                                                                     \
+        load(A, a, na);                                                                                      \
+        load(B, b, nb);                                                                                      \
+        CommIO io(comm);                                                                                     \
+        rss_convolution<T>(A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc, io.c);                \
+        store(C, c);                                                                                         \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_rss_divide_public_##SUF(T* a, size_t n, const T* d, int vector_d, uint64_t* comm) {     \
+        RSSV<T> A;                                                                                           \
+        load(A, a, n);                                                                                       \
+        CommIO io(comm);                                                                                     \
+        rss_divide_public<T>(A, d, vector_d != 0, io.c);                                                     \
+        store(A, a);                                                                                         \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_rss_divide_3of3_##SUF(const T* z, size_t n, T d, T* out, uint64_t* comm) {             \
+        std::vector<T> zz[3];                                                                                \
+        for (int p = 0; p < 3; p++) zz[p].assign(z + (size_t)p * n, z + (size_t)(p + 1) * n);                \
+        RSSV<T> O;                                                                                           \
+        CommIO io(comm);                                                                                     \
+        rss_divide_public_3of3<T>(zz, d, O, io.c);                                                           \
+        store(O, out);                                                                                       \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_rss_reconstruct_##SUF(const T* a, size_t n, T* out, uint64_t* comm) {                  \
+        RSSV<T> A;                                                                                           \
+        load(A, a, n);                                                                                       \
+        std::vector<T> o[3];                                                                                 \
+        CommIO io(comm);                                                                                     \
+        rss_reconstruct<T>(A, whole(n), o, io.c);                                                            \
+        for (int p = 0; p < 3; p++) std::memcpy(out + (size_t)p * n, o[p].data(), n * sizeof(T));            \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_rss_reshare_##SUF(const T* c, size_t n, T* out, uint64_t* comm) {                      \
+        std::vector<T> cc[3];                                                                                \
+        for (int p = 0; p < 3; p++) cc[p].assign(c + (size_t)p * n, c + (size_t)(p + 1) * n);               \
+        RSSV<T> O(n);                                                                                        \
+        CommIO io(comm);                                                                                     \
+        reshare_into<T>(cc, O, whole(n), io.c);                                                              \
+        store(O, out);                                                                                       \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_rss_mul_##SUF(T* a, const T* b, size_t n, uint64_t* comm) {                            \
+        RSSV<T> A, B;                                                                                        \
+        load(A, a, n);                                                                                       \
+        load(B, b, n);                                                                                       \
+        CommIO io(comm);                                                                                     \
+        rss_mul_assign<T>(A, B, io.c);                                                                       \
+        store(A, a);                                                                                         \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_rss_and_##SUF(T* a, const T* b, size_t n, uint64_t* comm) {                            \
+        RSSV<T> A, B;                                                                                        \
+        load(A, a, n);                                                                                       \
+        load(B, b, n);                                                                                       \
+        CommIO io(comm);                                                                                     \
+        rss_and_assign<T>(A, whole(n), B, whole(n), io.c);                                                   \
+        store(A, a);                                                                                         \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_rss_set_public_##SUF(const double* vals, size_t n, T* out, int fp, int ref_compat) {   \
+        RSSV<T> A(n);                                                                                        \
+        rss_set_public<T>(A, vals, fp, ref_compat != 0);                                                     \
+        store(A, out);                                                                                       \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_rss_from_list_##SUF(const double* vals, size_t n, T* out, int fp, int to_fixed) {      \
+        RSSV<T> A(n);                                                                                        \
+        rss_from_list<T>(A, vals, fp, to_fixed != 0);                                                        \
+        store(A, out);                                                                                       \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" void or_encode_##SUF(const double* vals, size_t n, T* out, int fp) {                          \
+        for (size_t i = 0; i < n; i++) out[i] = encode_fixed<T>(vals[i], fp);                                \
+    }                                                                                                        \
+    extern "C" void or_div_public_scalar_##SUF(const T* x, size_t n, const T* d, int vector_d, T* out) {     \
+        for (size_t i = 0; i < n; i++) out[i] = div_public<T>(x[i], vector_d ? d[i] : d[0]);                 \
+    }                                                                                                        \
+    extern "C" int or_gemm_##SUF(int M, int N, int K, const T* A, int tA, const T* B, int tB, T* C, int tC) { \
+        gemm<T>(M, N, K, A, tA, B, tB, C, tC);                                                               \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_conv_##SUF(int op, int N, int H, int W, int C, int K, int R, int S, int pad,           \
+                                 int stride, const T* a, const T* b, T* out) {                               \
+        ConvShape sh{N, H, W, C, K, R, S, pad, stride};                                                      \
+        conv_any<T>(op, sh, a, b, out);                                                                      \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" size_t or_maxpool_im2row_##SUF(const T* im, T* out, size_t cap, int H, int W, int f, int Din, \
+                                              int batch, int stride, int pad, T pad_val) {                   \
+        std::vector<T> o;                                                                                    \
+        maxpool_im2row<T>(im, o, H, W, f, Din, batch, stride, pad, pad_val);                                 \
+        if (out && cap >= o.size()) std::memcpy(out, o.data(), o.size() * sizeof(T));                        \
+        return o.size();                                                                                     \
+    }                                                                                                        \
+    extern "C" void or_element_vector_add_##SUF(T* a, const T* b, int rowwise, int rows, int cols) {         \
+        element_vector_add<T>(a, b, rowwise != 0, rows, cols);                                               \
+    }                                                                                                        \
+    extern "C" void or_reduce_sum_##SUF(const T* a, T* b, int reduceRows, int rows, int cols) {              \
+        reduce_sum<T>(a, b, reduceRows != 0, rows, cols);                                                    \
+    }                                                                                                        \
+    extern "C" void or_bitexpand_##SUF(const T* a, size_t n, T* bits) {                                      \
+        std::vector<T> av(a, a + n), b;                                                                      \
+        bitexpand<T, T>(av, b);                                                                              \
+        std::memcpy(bits, b.data(), b.size() * sizeof(T));                                                   \
+    }
+
+OR_RING(uint64_t, u64)
+OR_RING(uint32_t, u32)
+
+#define OR_BITS(T, TS, U, US)                                                                                \
+    extern "C" int or_rss_drelu_##TS##_##US(const T* in, size_t n, U* out, uint64_t* comm) {                 \
+        RSSV<T> A;                                                                                           \
+        load(A, in, n);                                                                                      \
+        RSSV<U> R(n);                                                                                        \
+        CommIO io(comm);                                                                                     \
+        rss_drelu<T, U>(A, whole(n), R, io.c);                                                               \
+        store(R, out);                                                                                       \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_rss_relu_##TS##_##US(const T* in, size_t n, T* out, U* dout, uint64_t* comm) {         \
+        RSSV<T> A, O;                                                                                        \
+        load(A, in, n);                                                                                      \
+        RSSV<U> D(n);                                                                                        \
+        CommIO io(comm);                                                                                     \
+        rss_relu<T, U>(A, O, D, io.c);                                                                       \
+        store(O, out);                                                                                       \
+        store(D, dout);                                                                                      \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_rss_select_share_##TS##_##US(const T* x, const T* y, const U* b, T* z, size_t n,       \
+                                                   uint64_t* comm) {                                         \
+        RSSV<T> X, Y, Z(n);                                                                                  \
+        RSSV<U> B;                                                                                           \
+        load(X, x, n);                                                                                       \
+        load(Y, y, n);                                                                                       \
+        load(B, b, n);                                                                                       \
+        CommIO io(comm);                                                                                     \
+        rss_select_share<T, U>(X, whole(n), Y, whole(n), B, Z, whole(n), io.c);                              \
+        store(Z, z);                                                                                         \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_rss_maxpool_##TS##_##US(const T* in, size_t n, T* out, U* dout, int k,                 \
+                                              uint64_t* comm) {                                              \
+        RSSV<T> A, O;                                                                                        \
+        load(A, in, n);                                                                                      \
+        RSSV<U> D(n);                                                                                        \
+        CommIO io(comm);                                                                                     \
+        rss_maxpool<T, U>(A, O, D, k, io.c);                                                                 \
+        store(O, out);                                                                                       \
+        store(D, dout);                                                                                      \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_maxpool_layer_##TS##_##US(const T* in, T* out, U* maxprime, int H, int W, int C,       \
+                                                int pool, int stride, int batch, int fp, uint64_t* comm) {   \
+        RSSV<T> A, O;                                                                                        \
+        load(A, in, (size_t)batch * H * W * C);                                                              \
+        RSSV<U> D;                                                                                           \
+        CommIO io(comm);                                                                                     \
+        maxpool_layer_forward<T, U>(A, O, D, H, W, C, pool, stride, batch, fp, io.c);                        \
+        store(O, out);                                                                                       \
+        store(D, maxprime);                                                                                  \
+        return 0;                                                                                            \
+    }
+
+OR_BITS(uint64_t, u64, uint8_t, u8)
+OR_BITS(uint64_t, u64, uint64_t, u64)
+OR_BITS(uint32_t, u32, uint8_t, u8)
+OR_BITS(uint32_t, u32, uint32_t, u32)
+
+extern "C" void or_expand_compare_u8(const uint8_t* b, const uint8_t* nb, size_t n, uint8_t* out, size_t out_n) {
+    std::vector<uint8_t> bv(b, b + n), nv(nb, nb + n), o(out_n);
+    expand_compare<uint8_t>(bv, nv, o);
+    std::memcpy(out, o.data(), out_n);
+}
+
+extern "C" void or_truncate_cols_u8(const uint8_t* a, uint8_t* b, size_t rows, int start_cols, int end_cols) {
+    truncate_cols<uint8_t>(a, b, rows, start_cols, end_cols);
+}

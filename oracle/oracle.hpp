@@ -1,0 +1,685 @@
+// oracle.hpp — CPU restatement of Piranha's party-local secret-share arithmetic.
+//
+// TEST INFRASTRUCTURE ONLY. This file is the checker: the pytest suite, the
+// smoke check and the CPU-baseline leg of bench.py call it to produce the
+// expected shares. Nothing in the piranha_gb300 product links or calls it.
+//
+// What it restates (paths relative to the Piranha source tree):
+//   * src/mpc/RSS.inl      — the 3-party replicated-secret-sharing protocol,
+//                            step by step, for every simulated party
+//   * src/gpu/functors.cuh — ring operators, including division through double
+//   * src/gpu/gemm.cuh     — the 8-layout ring GEMM (column-major default)
+//   * src/gpu/conv.cuh     — CUTLASS fprop/dgrad/wgrad problem semantics
+//   * src/gpu/bitwise.cuh, convolution.cuh, matrix.cuh — bit/maxpool/bias glue
+//   * src/mpc/Precompute.h — the constant "randomness" (r = 1, r' = d)
+//   * src/util/util.cuh    — fixed-point encode/decode
+//
+// Simulation model. Piranha runs one process per party; every DeviceData op
+// runs at each party on that party's own view. Here the three parties live in
+// one process: an RSS tensor of n elements is held as views[party][share][n]
+// (party A=0, B=1, C=2; share 0 = "shareA", share 1 = "shareB"). Per-party
+// public data (the result of a reconstruct, bit expansions) is pub[party][n].
+// A message "sent" by one party is read directly from the sender's view; the
+// bytes and rounds a socket would carry are added to a Comm counter with the
+// accounting of DeviceData::transmit/receive (DeviceData.h:87-118) and
+// Profiler::add_comm_round.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <limits>
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <type_traits>
+#include <vector>
+
+namespace oracle {
+
+enum { PA = 0, PB = 1, PC = 2 };
+static inline int next_party(int p) { return (p + 1) % 3; }  // RSS.inl:348-357
+static inline int prev_party(int p) { return (p + 2) % 3; }  // RSS.inl:360-369
+
+struct Comm {
+    uint64_t tx[4] = {0, 0, 0, 0};
+    uint64_t rx[4] = {0, 0, 0, 0};
+    uint64_t rounds = 0;
+    void msg(int nparties, uint64_t bytes_tx, uint64_t bytes_rx) {
+        for (int p = 0; p < nparties; p++) { tx[p] += bytes_tx; rx[p] += bytes_rx; }
+    }
+};
+
+// ---------------------------------------------------------------- ring ops --
+
+template <typename T> using S_t = typename std::make_signed<T>::type;
+
+// Saturating double -> signed conversion with PTX cvt.rzi semantics
+// (truncate toward zero, clamp to range, NaN -> 0). The reference runs its
+// division functor on the device, so these are the semantics it sees.
+template <typename S> static inline S cvt_rzi_sat(double q) {
+    if (std::isnan(q)) return 0;
+    const double hi = std::ldexp(1.0, int(sizeof(S) * 8 - 1));
+    if (q >= hi) return std::numeric_limits<S>::max();
+    if (q <= -hi) return std::numeric_limits<S>::min();
+    return (S)q;  // in range: C++ truncates toward zero
+}
+
+// functors.cuh:33-45 (scalar) and :94-105 (vector): (T)(S)((double)(S)x / (double)(S)d)
+template <typename T> static inline T div_public(T x, T d) {
+    using S = S_t<T>;
+    double q = (double)(S)x / (double)(S)d;
+    return (T)cvt_rzi_sat<S>(q);
+}
+
+// util.cuh:28-33 / RSS.inl:126: (T)(f * (1 << FP)). A negative double must go
+// through a signed integer first: that is what x86-64 hosts did for the
+// reference; aarch64's unsigned conversion would saturate to 0 instead.
+template <typename T> static inline T encode_fixed(double f, int fp) {
+    double v = f * (double)(1 << fp);
+    return (T)(int64_t)v;
+}
+// util.cuh:46-53
+template <typename T> static inline double decode_fixed(T v, int fp) {
+    return (double)(S_t<T>)v / (double)(1 << fp);
+}
+
+// ------------------------------------------------------------ share views --
+
+// views[p][s] is an n-element array; a strided view (StridedRange.cuh:11-52)
+// is expressed by (offset, stride, size) over the parent array.
+template <typename T> struct RSSV {
+    size_t n = 0;
+    std::vector<T> v[3][2];
+    RSSV() {}
+    explicit RSSV(size_t n_) { resize(n_); }
+    void resize(size_t n_) {
+        n = n_;
+        for (int p = 0; p < 3; p++)
+            for (int s = 0; s < 2; s++) v[p][s].assign(n, (T)0);
+    }
+    void zero() { for (int p = 0; p < 3; p++) for (int s = 0; s < 2; s++) std::fill(v[p][s].begin(), v[p][s].end(), (T)0); }
+};
+
+template <typename T> using Pub = std::vector<T>[3];
+
+struct Strided {
+    size_t offset, stride, size;
+};
+static inline Strided strided(size_t parent_n, size_t offset, size_t stride) {
+    // StridedRange.cuh:44-46: size = ((last - first) + (stride - 1)) / stride
+    size_t span = parent_n > offset ? parent_n - offset : 0;
+    return Strided{offset, stride, (span + stride - 1) / stride};
+}
+static inline Strided whole(size_t n) { return Strided{0, 1, n}; }
+
+// RSS.inl:117-120: fill puts val into party A's shareA and party C's shareB.
+template <typename T> void rss_fill(RSSV<T>& a, T val) {
+    for (int p = 0; p < 3; p++) {
+        std::fill(a.v[p][0].begin(), a.v[p][0].end(), p == PA ? val : (T)0);
+        std::fill(a.v[p][1].begin(), a.v[p][1].end(), p == PC ? val : (T)0);
+    }
+}
+
+// RSS.inl:123-142. With ref_compat the missing `break` after case PARTY_B is
+// reproduced: party B also receives the public values in its shareB.
+template <typename T> void rss_set_public(RSSV<T>& a, const double* vals, int fp, bool ref_compat) {
+    for (size_t i = 0; i < a.n; i++) {
+        T x = encode_fixed<T>(vals[i], fp);
+        a.v[PA][0][i] = x; a.v[PA][1][i] = 0;
+        a.v[PB][0][i] = 0; a.v[PB][1][i] = ref_compat ? x : (T)0;
+        a.v[PC][0][i] = 0; a.v[PC][1][i] = x;
+    }
+}
+
+// RSS.inl:389-414: the initializer-list constructor (no fall-through).
+template <typename T> void rss_from_list(RSSV<T>& a, const double* vals, int fp, bool to_fixed) {
+    for (size_t i = 0; i < a.n; i++) {
+        T x = to_fixed ? encode_fixed<T>(vals[i], fp) : (T)(int64_t)vals[i];
+        a.v[PA][0][i] = x; a.v[PA][1][i] = 0;
+        a.v[PB][0][i] = 0; a.v[PB][1][i] = 0;
+        a.v[PC][0][i] = 0; a.v[PC][1][i] = x;
+    }
+}
+
+// reshare (RSS.inl:1053-1074): out = (c_p, c_next). Applied to strided views.
+template <typename T> void reshare_into(const std::vector<T> (&c)[3], RSSV<T>& out, Strided w, Comm& comm) {
+    for (int p = 0; p < 3; p++)
+        for (size_t i = 0; i < w.size; i++) {
+            size_t j = w.offset + i * w.stride;
+            out.v[p][0][j] = c[p][i];
+            out.v[p][1][j] = c[next_party(p)][i];
+        }
+    comm.msg(3, w.size * sizeof(T), w.size * sizeof(T));
+    comm.rounds++;
+}
+
+// RSS &= RSS on (strided) views (RSS.inl:331-345):
+//   z = (a0 & (b0 ^ b1)) ^ (a1 & b0), then reshare.
+template <typename T> void rss_and_assign(RSSV<T>& a, Strided wa, const RSSV<T>& b, Strided wb, Comm& comm) {
+    std::vector<T> c[3];
+    for (int p = 0; p < 3; p++) {
+        c[p].resize(wa.size);
+        for (size_t i = 0; i < wa.size; i++) {
+            size_t ia = wa.offset + i * wa.stride, ib = wb.offset + i * wb.stride;
+            T b0 = b.v[p][0][ib], b1 = b.v[p][1][ib];
+            c[p][i] = (T)((a.v[p][0][ia] & (T)(b0 ^ b1)) ^ (a.v[p][1][ia] & b0));
+        }
+    }
+    reshare_into(c, a, wa, comm);
+}
+
+// RSS *= RSS (RSS.inl:284-320): z = a0*(b0+b1) + a1*b0, then reshare.
+template <typename T> void rss_mul_assign(RSSV<T>& a, const RSSV<T>& b, Comm& comm) {
+    std::vector<T> c[3];
+    for (int p = 0; p < 3; p++) {
+        c[p].resize(a.n);
+        for (size_t i = 0; i < a.n; i++) {
+            T b0 = b.v[p][0][i], b1 = b.v[p][1][i];
+            c[p][i] = (T)(a.v[p][0][i] * (T)(b0 + b1) + a.v[p][1][i] * b0);
+        }
+    }
+    reshare_into(c, a, whole(a.n), comm);
+}
+
+// RSS ^= RSS (RSS.inl:324-328), on views.
+template <typename T> void rss_xor_assign(RSSV<T>& a, Strided wa, const RSSV<T>& b, Strided wb) {
+    for (int p = 0; p < 3; p++)
+        for (int s = 0; s < 2; s++)
+            for (size_t i = 0; i < wa.size; i++)
+                a.v[p][s][wa.offset + i * wa.stride] ^= b.v[p][s][wb.offset + i * wb.stride];
+}
+
+// reconstruct (RSS.inl:458-479): out_p = a_p0 + a_p1 + (prev party's a0).
+template <typename T> void rss_reconstruct(const RSSV<T>& a, Strided w, std::vector<T> (&out)[3], Comm& comm) {
+    for (int p = 0; p < 3; p++) {
+        out[p].resize(w.size);
+        int q = prev_party(p);
+        for (size_t i = 0; i < w.size; i++) {
+            size_t j = w.offset + i * w.stride;
+            out[p][i] = (T)(a.v[p][0][j] + a.v[p][1][j] + a.v[q][0][j]);
+        }
+    }
+    comm.msg(3, w.size * sizeof(T), w.size * sizeof(T));
+    comm.rounds++;
+}
+
+// dividePublic(RSS, T) (RSS.inl:423-436) and the vector form (:439-455), with
+// Precompute::getDividedShares r = fill(1), r' = fill(d) (Precompute.h:107-134).
+template <typename T> void rss_divide_public(RSSV<T>& a, const T* d, bool vector_d, Comm& comm) {
+    // a -= r'  (RSS -= RSS): r' holds d in A.shareA and C.shareB
+    for (size_t i = 0; i < a.n; i++) {
+        T di = vector_d ? d[i] : d[0];
+        a.v[PA][0][i] -= di;
+        a.v[PC][1][i] -= di;
+    }
+    std::vector<T> rec[3];
+    rss_reconstruct(a, whole(a.n), rec, comm);
+    for (int p = 0; p < 3; p++)
+        for (size_t i = 0; i < a.n; i++) rec[p][i] = div_public<T>(rec[p][i], vector_d ? d[i] : d[0]);
+    // a.zero(); a += r; a += reconstructed
+    for (size_t i = 0; i < a.n; i++) {
+        a.v[PA][0][i] = (T)(1 + rec[PA][i]); a.v[PA][1][i] = 0;
+        a.v[PB][0][i] = 0;                    a.v[PB][1][i] = 0;
+        a.v[PC][0][i] = 0;                    a.v[PC][1][i] = (T)(1 + rec[PC][i]);
+    }
+}
+
+// dividePublic3out3 (RSS.inl:1077-1094) + reconstruct3out3 (:1020-1050).
+// z[p] is party p's 3-out-of-3 share; output is an RSS tensor.
+template <typename T> void rss_divide_public_3of3(std::vector<T> (&z)[3], T d, RSSV<T>& out, Comm& comm) {
+    size_t n = z[0].size();
+    for (size_t i = 0; i < n; i++) z[PA][i] -= d;  // a -= rPrime.shareA (only A holds d)
+    out.resize(n);
+    for (size_t i = 0; i < n; i++) {
+        T rec[3];
+        for (int p = 0; p < 3; p++) rec[p] = (T)(z[p][i] + z[prev_party(p)][i] + z[next_party(p)][i]);
+        out.v[PA][0][i] = (T)(1 + div_public<T>(rec[PA], d));
+        out.v[PC][1][i] = (T)(1 + div_public<T>(rec[PC], d));
+    }
+    comm.msg(3, 2 * n * sizeof(T), 2 * n * sizeof(T));
+    comm.rounds++;
+}
+
+// ---------------------------------------------------------------- GEMM ----
+
+// gpu::gemm (gemm.cuh:64-100): C(MxN) = A(MxK) * B(KxN) mod 2^w; each operand
+// is row-major when its transpose flag is set, column-major otherwise.
+template <typename T>
+void gemm(int M, int N, int K, const T* A, bool tA, const T* B, bool tB, T* C, bool tC) {
+    #pragma omp parallel for schedule(static)
+    for (int m = 0; m < M; m++) {
+        for (int n = 0; n < N; n++) {
+            T acc = 0;
+            for (int k = 0; k < K; k++) {
+                T a = tA ? A[(size_t)m * K + k] : A[m + (size_t)k * M];
+                T b = tB ? B[(size_t)k * N + n] : B[k + (size_t)n * K];
+                acc = (T)(acc + a * b);
+            }
+            if (tC) C[(size_t)m * N + n] = acc; else C[m + (size_t)n * M] = acc;
+        }
+    }
+}
+
+// localMatMul (RSS.inl:1097-1110): z_p = A_p0*B_p0 + A_p0*B_p1 + A_p1*B_p0.
+// Computed in the fused form A_p0*(B_p0+B_p1) + A_p1*B_p0 (identical mod 2^w).
+template <typename T>
+void local_matmul(const RSSV<T>& a, const RSSV<T>& b, std::vector<T> (&z)[3], int M, int N, int K,
+                  bool tA, bool tB, bool tC) {
+    std::vector<T> bs((size_t)K * N), t1((size_t)M * N), t2((size_t)M * N);
+    for (int p = 0; p < 3; p++) {
+        for (size_t i = 0; i < bs.size(); i++) bs[i] = (T)(b.v[p][0][i] + b.v[p][1][i]);
+        gemm<T>(M, N, K, a.v[p][0].data(), tA, bs.data(), tB, t1.data(), tC);
+        gemm<T>(M, N, K, a.v[p][1].data(), tA, b.v[p][0].data(), tB, t2.data(), tC);
+        z[p].resize((size_t)M * N);
+        for (size_t i = 0; i < z[p].size(); i++) z[p][i] = (T)(t1[i] + t2[i]);
+    }
+}
+
+// matmul (RSS.inl:482-540)
+template <typename T>
+void rss_matmul(const RSSV<T>& a, const RSSV<T>& b, RSSV<T>& c, int M, int N, int K, bool tA, bool tB,
+                bool tC, int trunc, Comm& comm) {
+    std::vector<T> z[3];
+    local_matmul(a, b, z, M, N, K, tA, tB, tC);
+    rss_divide_public_3of3(z, (T)((T)1 << trunc), c, comm);
+}
+
+// ---------------------------------------------------------------- conv ----
+
+// CUTLASS Conv2d problem semantics as used by conv.cuh:84-91,359-490:
+// NHWC activations, KRSC filters, cross-correlation, symmetric padding,
+// P = (H + 2*pad - R)/stride + 1.
+struct ConvShape {
+    int N, H, W, C, K, R, S, pad, stride;
+    int P() const { return (H + 2 * pad - R) / stride + 1; }
+    int Q() const { return (W + 2 * pad - S) / stride + 1; }
+};
+
+// fprop: Y[n,p,q,k] = sum_{r,s,c} X[n, p*st-pad+r, q*st-pad+s, c] * F[k,r,s,c]
+template <typename T> void conv_fprop(const ConvShape& sh, const T* X, const T* F, T* Y) {
+    int P = sh.P(), Q = sh.Q();
+    #pragma omp parallel for collapse(2) schedule(static)
+    for (int n = 0; n < sh.N; n++)
+        for (int p = 0; p < P; p++)
+            for (int q = 0; q < Q; q++)
+                for (int k = 0; k < sh.K; k++) {
+                    T acc = 0;
+                    for (int r = 0; r < sh.R; r++) {
+                        int h = p * sh.stride - sh.pad + r;
+                        if (h < 0 || h >= sh.H) continue;
+                        for (int s = 0; s < sh.S; s++) {
+                            int w = q * sh.stride - sh.pad + s;
+                            if (w < 0 || w >= sh.W) continue;
+                            const T* x = X + (((size_t)n * sh.H + h) * sh.W + w) * sh.C;
+                            const T* f = F + (((size_t)k * sh.R + r) * sh.S + s) * sh.C;
+                            for (int c = 0; c < sh.C; c++) acc = (T)(acc + x[c] * f[c]);
+                        }
+                    }
+                    Y[(((size_t)n * P + p) * Q + q) * sh.K + k] = acc;
+                }
+}
+
+// dgrad: dX[n,h,w,c] = sum_{k,r,s : h = p*st-pad+r, w = q*st-pad+s} dY[n,p,q,k] * F[k,r,s,c]
+template <typename T> void conv_dgrad(const ConvShape& sh, const T* dY, const T* F, T* dX) {
+    int P = sh.P(), Q = sh.Q();
+    #pragma omp parallel for collapse(2) schedule(static)
+    for (int n = 0; n < sh.N; n++)
+        for (int h = 0; h < sh.H; h++)
+            for (int w = 0; w < sh.W; w++)
+                for (int c = 0; c < sh.C; c++) {
+                    T acc = 0;
+                    for (int r = 0; r < sh.R; r++) {
+                        int ph = h + sh.pad - r;
+                        if (ph < 0 || ph % sh.stride) continue;
+                        int p = ph / sh.stride;
+                        if (p >= P) continue;
+                        for (int s = 0; s < sh.S; s++) {
+                            int qw = w + sh.pad - s;
+                            if (qw < 0 || qw % sh.stride) continue;
+                            int q = qw / sh.stride;
+                            if (q >= Q) continue;
+                            const T* dy = dY + (((size_t)n * P + p) * Q + q) * sh.K;
+                            for (int k = 0; k < sh.K; k++)
+                                acc = (T)(acc + dy[k] * F[(((size_t)k * sh.R + r) * sh.S + s) * sh.C + c]);
+                        }
+                    }
+                    dX[(((size_t)n * sh.H + h) * sh.W + w) * sh.C + c] = acc;
+                }
+}
+
+// wgrad: dF[k,r,s,c] = sum_{n,p,q} dY[n,p,q,k] * X[n, p*st-pad+r, q*st-pad+s, c]
+template <typename T> void conv_wgrad(const ConvShape& sh, const T* dY, const T* X, T* dF) {
+    int P = sh.P(), Q = sh.Q();
+    #pragma omp parallel for collapse(2) schedule(static)
+    for (int k = 0; k < sh.K; k++)
+        for (int r = 0; r < sh.R; r++)
+            for (int s = 0; s < sh.S; s++)
+                for (int c = 0; c < sh.C; c++) {
+                    T acc = 0;
+                    for (int n = 0; n < sh.N; n++)
+                        for (int p = 0; p < P; p++) {
+                            int h = p * sh.stride - sh.pad + r;
+                            if (h < 0 || h >= sh.H) continue;
+                            for (int q = 0; q < Q; q++) {
+                                int w = q * sh.stride - sh.pad + s;
+                                if (w < 0 || w >= sh.W) continue;
+                                acc = (T)(acc + dY[(((size_t)n * P + p) * Q + q) * sh.K + k] *
+                                                    X[(((size_t)n * sh.H + h) * sh.W + w) * sh.C + c]);
+                            }
+                        }
+                    dF[(((size_t)k * sh.R + r) * sh.S + s) * sh.C + c] = acc;
+                }
+}
+
+enum ConvOp { CONV_FPROP = 0, CONV_DGRAD = 1, CONV_WGRAD = 2 };
+
+// One party-local conv of the given kind between two single arrays.
+template <typename T> void conv_any(int op, const ConvShape& sh, const T* a, const T* b, T* out) {
+    if (op == CONV_FPROP) conv_fprop(sh, a, b, out);
+    else if (op == CONV_DGRAD) conv_dgrad(sh, a, b, out);
+    else conv_wgrad(sh, a, b, out);
+}
+
+// convolution (RSS.inl:706-803) with localFprop/Dgrad/Wgrad (:614-703):
+// three convs summed per party, then dividePublic3out3.
+// A and B follow the reference argument roles: fprop (im, filter), dgrad
+// (delta, filter), wgrad (delta, forward input).
+template <typename T>
+void rss_convolution(const RSSV<T>& A, const RSSV<T>& B, RSSV<T>& C, int op, int batch, int H, int W,
+                     int f, int Din, int Dout, int stride, int pad, int trunc, Comm& comm) {
+    ConvShape sh{batch, H, W, Din, Dout, f, f, pad, stride};
+    size_t out_n = op == CONV_FPROP ? (size_t)batch * sh.P() * sh.Q() * Dout
+                 : op == CONV_DGRAD ? (size_t)batch * H * W * Din
+                                    : (size_t)Dout * f * f * Din;
+    std::vector<T> z[3], t(out_n);
+    for (int p = 0; p < 3; p++) {
+        z[p].assign(out_n, 0);
+        const T* a0 = A.v[p][0].data(); const T* a1 = A.v[p][1].data();
+        const T* b0 = B.v[p][0].data(); const T* b1 = B.v[p][1].data();
+        const T* pairs[3][2] = {{a0, b0}, {a0, b1}, {a1, b0}};
+        for (auto& pr : pairs) {
+            // wgrad's first operand is the delta (NPQK) and second the input (NHWC)
+            conv_any<T>(op, sh, pr[0], pr[1], t.data());
+            for (size_t i = 0; i < out_n; i++) z[p][i] = (T)(z[p][i] + t[i]);
+        }
+    }
+    rss_divide_public_3of3(z, (T)((T)1 << trunc), C, comm);
+}
+
+// --------------------------------------------------------- bit kernels ----
+
+// bitexpand (bitwise.cuh:10-21): bits[v*W + b] = (a[v] >> b) & 1 (in-bounds part)
+template <typename T, typename U> void bitexpand(const std::vector<T>& a, std::vector<U>& bits) {
+    const int W = sizeof(T) * 8;
+    bits.assign(a.size() * W, 0);
+    for (size_t v = 0; v < a.size(); v++)
+        for (int b = 0; b < W; b++) bits[v * W + b] = (U)((a[v] >> b) & 1);
+}
+
+// setCarryOutMSB (bitwise.cuh:41-64)
+template <typename U>
+void set_carry_out_msb(std::vector<U>& rbits, std::vector<U>& abits, std::vector<U>& msb, int W, bool xor_msb) {
+    for (size_t i = 0; i < msb.size(); i++) {
+        size_t bi = i * W + (W - 1);
+        msb[i] = rbits[bi];
+        if (xor_msb) msb[i] ^= abits[bi];
+        abits[bi] = 1;
+        rbits[bi] = 0;
+    }
+}
+
+// carryOut (RSS.inl:1113-1209): log-depth generate/propagate tree over
+// strided views of the bit arrays; 2 AND-reshares per level.
+template <typename U> void carry_out(RSSV<U>& p, RSSV<U>& g, int k, RSSV<U>& out, Comm& comm) {
+    size_t N = p.n;
+    size_t stride = 2, offset = 1;
+    Strided pEven = strided(N, 0, stride), pOdd = strided(N, offset, stride);
+    Strided gEven = strided(N, 0, stride), gOdd = strided(N, offset, stride);
+    while (k > 1) {
+        rss_and_assign(g, gEven, p, pOdd, comm);
+        rss_and_assign(p, pEven, p, pOdd, comm);
+        rss_xor_assign(g, gOdd, g, gEven);
+        gEven = strided(N, offset, stride * 2);
+        offset += stride;
+        gOdd = strided(N, offset, stride * 2);
+        stride *= 2;
+        pEven = strided(N, 0, stride);
+        pOdd = strided(N, stride / 2, stride);
+        k /= 2;
+    }
+    Strided oE = strided(out.n, 0, 2), oO = strided(out.n, 1, 2);
+    for (int q = 0; q < 3; q++)
+        for (int s = 0; s < 2; s++) {
+            for (size_t i = 0; i < gEven.size && i < oE.size; i++)
+                out.v[q][s][oE.offset + i * 2] = g.v[q][s][gEven.offset + i * gEven.stride];
+            for (size_t i = 0; i < gOdd.size && i < oO.size; i++)
+                out.v[q][s][oO.offset + i * 2] = g.v[q][s][gOdd.offset + i * gOdd.stride];
+        }
+}
+
+// dReLU (RSS.inl:807-852) over a strided view of the input.
+template <typename T, typename U>
+void rss_drelu(const RSSV<T>& in, Strided w, RSSV<U>& result, Comm& comm) {
+    const int W = sizeof(T) * 8;
+    size_t n = w.size;
+    RSSV<U> rbits(n * W);
+    rss_fill<U>(rbits, 1);
+    std::vector<T> a[3];
+    rss_reconstruct(in, w, a, comm);  // r = input; reconstruct(r, a)
+    std::vector<U> abits[3];
+    for (int p = 0; p < 3; p++) {
+        for (auto& x : a[p]) x = (T)(x + 1);
+        bitexpand<T, U>(a[p], abits[p]);
+    }
+    RSSV<U> msb(n);
+    for (int p = 0; p < 3; p++) {
+        std::vector<U>& r0 = rbits.v[p][0];
+        std::vector<U>& r1 = rbits.v[p][1];
+        if (p != PC) {
+            set_carry_out_msb<U>(r0, abits[p], msb.v[p][0], W, p == PA);
+            set_carry_out_msb<U>(r1, abits[p], msb.v[p][1], W, p == PC);
+        } else {
+            set_carry_out_msb<U>(r1, abits[p], msb.v[p][1], W, p == PC);
+            set_carry_out_msb<U>(r0, abits[p], msb.v[p][0], W, p == PA);
+        }
+    }
+    RSSV<U> g(n * W), pp(n * W);
+    for (int p = 0; p < 3; p++)
+        for (size_t i = 0; i < n * W; i++) {
+            // g = rbits & abits (RSS &= DeviceData: both shares)
+            g.v[p][0][i] = rbits.v[p][0][i] & abits[p][i];
+            g.v[p][1][i] = rbits.v[p][1][i] & abits[p][i];
+            // p = rbits ^ abits (RSS ^= DeviceData: A.shareA, C.shareB)
+            pp.v[p][0][i] = rbits.v[p][0][i] ^ (p == PA ? abits[p][i] : (U)0);
+            pp.v[p][1][i] = rbits.v[p][1][i] ^ (p == PC ? abits[p][i] : (U)0);
+        }
+    RSSV<U> pre(result.n);
+    carry_out(pp, g, W, pre, comm);
+    rss_xor_assign(pre, whole(pre.n), msb, whole(msb.n));
+    // result.fill(1); result -= preResult
+    for (int p = 0; p < 3; p++)
+        for (size_t i = 0; i < result.n; i++) {
+            result.v[p][0][i] = (U)((p == PA ? 1 : 0) - pre.v[p][0][i]);
+            result.v[p][1][i] = (U)((p == PC ? 1 : 0) - pre.v[p][1][i]);
+        }
+}
+
+// convex_comb (RSS.inl:1322-1333 with rss_convex_comb_functor :33-61)
+template <typename T, typename U>
+void convex_comb(RSSV<T>& d, const RSSV<T>& c, const std::vector<U> (&e)[3]) {
+    for (int p = 0; p < 3; p++)
+        for (size_t i = 0; i < d.n; i++) {
+            T c0 = c.v[p][0][i], c1 = c.v[p][1][i];
+            if (e[p][i] == 1) {
+                if (p == PA) { d.v[p][0][i] = (T)(1 - c0); d.v[p][1][i] = (T)(0 - c1); }
+                else if (p == PB) { d.v[p][0][i] = (T)(0 - c0); d.v[p][1][i] = (T)(0 - c1); }
+                else { d.v[p][0][i] = (T)(0 - c0); d.v[p][1][i] = (T)(1 - c1); }
+            } else {
+                d.v[p][0][i] = c0; d.v[p][1][i] = c1;
+            }
+        }
+}
+
+// selectShare (RSS.inl:543-569): z = (y - x) * d + x with d from the revealed b.
+// x, y, z may be strided views of larger tensors (maxpool uses that).
+template <typename T, typename U>
+void rss_select_share(const RSSV<T>& x, Strided wx, const RSSV<T>& y, Strided wy, const RSSV<U>& b,
+                      RSSV<T>& z, Strided wz, Comm& comm) {
+    size_t n = wx.size;
+    RSSV<T> c(n);
+    std::vector<U> e[3];
+    rss_reconstruct(b, whole(b.n), e, comm);  // cbits = 0 ^ b; reconstruct(cbits, e)
+    RSSV<T> d(n);
+    convex_comb(d, c, e);
+    RSSV<T> res(n);
+    for (int p = 0; p < 3; p++)
+        for (int s = 0; s < 2; s++)
+            for (size_t i = 0; i < n; i++)
+                res.v[p][s][i] = (T)(y.v[p][s][wy.offset + i * wy.stride] - x.v[p][s][wx.offset + i * wx.stride]);
+    rss_mul_assign(res, d, comm);
+    for (int p = 0; p < 3; p++)
+        for (int s = 0; s < 2; s++)
+            for (size_t i = 0; i < n; i++)
+                z.v[p][s][wz.offset + i * wz.stride] = (T)(res.v[p][s][i] + x.v[p][s][wx.offset + i * wx.stride]);
+}
+
+// ReLU (RSS.inl:855-865)
+template <typename T, typename U> void rss_relu(const RSSV<T>& in, RSSV<T>& out, RSSV<U>& dout, Comm& comm) {
+    rss_drelu<T, U>(in, whole(in.n), dout, comm);
+    RSSV<T> zeros(in.n);
+    out.resize(in.n);
+    rss_select_share<T, U>(zeros, whole(in.n), in, whole(in.n), dout, out, whole(in.n), comm);
+}
+
+// expandCompare (bitwise.cuh:66-92), in-bounds part
+template <typename U>
+void expand_compare(const std::vector<U>& b, const std::vector<U>& nb, std::vector<U>& expanded) {
+    size_t f = (expanded.size() / b.size()) / 2;
+    for (size_t i = 0; i < b.size(); i++)
+        for (size_t e = 0; e < 2 * f; e++) expanded[i * 2 * f + e] = e < f ? b[i] : nb[i];
+}
+
+// maxpool (RSS.inl:868-1017): tournament over strided even/odd views of the
+// (padded) pool rows; dresult tracks the argmax one-hot.
+template <typename T, typename U>
+void rss_maxpool(RSSV<T>& input, RSSV<T>& result, RSSV<U>& dresult, int k, Comm& comm) {
+    size_t N = input.n;
+    rss_fill<U>(dresult, 1);
+    size_t stride = 2;
+    Strided even = strided(N, 0, stride), odd = strided(N, 1, stride);
+    auto level = [&](bool last) {
+        RSSV<T> diff(even.size);
+        for (int p = 0; p < 3; p++)
+            for (int s = 0; s < 2; s++)
+                for (size_t i = 0; i < even.size; i++)
+                    diff.v[p][s][i] = (T)(input.v[p][s][even.offset + i * even.stride] -
+                                          input.v[p][s][odd.offset + i * odd.stride]);
+        RSSV<U> b(even.size);
+        rss_drelu<T, U>(diff, whole(diff.n), b, comm);
+        rss_select_share<T, U>(input, odd, input, even, b, input, even, comm);
+        if (!last) {
+            stride *= 2;
+            even = strided(N, 0, stride);
+            odd = strided(N, stride / 2, stride);
+        } else {
+            result.resize(even.size);
+            for (int p = 0; p < 3; p++)
+                for (int s = 0; s < 2; s++)
+                    for (size_t i = 0; i < even.size; i++)
+                        result.v[p][s][i] = input.v[p][s][even.offset + i * even.stride];
+        }
+        RSSV<U> neg(b.n);
+        rss_fill<U>(neg, 1);
+        for (int p = 0; p < 3; p++)
+            for (int s = 0; s < 2; s++)
+                for (size_t i = 0; i < b.n; i++) neg.v[p][s][i] = (U)(neg.v[p][s][i] - b.v[p][s][i]);
+        RSSV<U> expanded(N);
+        for (int p = 0; p < 3; p++)
+            for (int s = 0; s < 2; s++) expand_compare<U>(b.v[p][s], neg.v[p][s], expanded.v[p][s]);
+        rss_and_assign(dresult, whole(N), expanded, whole(N), comm);
+    };
+    while (k > 2) {
+        level(false);
+        k /= 2;
+    }
+    level(true);
+}
+
+// maxpool_im2row + stride_pad (convolution.cuh:56-108,175-191,252-304).
+// Input is read with the reference's (batch, x=col, y=row, channel) indexing.
+template <typename T>
+void maxpool_im2row(const T* im, std::vector<T>& out, int H, int W, int f, int Din, int batch, int stride,
+                    int pad, T pad_val) {
+    int wK = (W - f + 2 * pad) / stride + 1, hK = (H - f + 2 * pad) / stride + 1;
+    int pool = f * f;
+    std::vector<T> unpadded((size_t)pool * wK * hK * batch * Din, 0);
+    for (int ic = 0; ic < batch * Din; ic++)
+        for (int win = 0; win < wK * hK; win++) {
+            int b = ic / Din, ch = ic % Din;
+            int baseCol = (win / hK) * stride - pad, baseRow = (win % hK) * stride - pad;
+            size_t o = (size_t)b * (wK * hK * Din * pool) + (size_t)win * (Din * pool) + (size_t)ch * pool;
+            for (int c = 0; c < f; c++)
+                for (int r = 0; r < f; r++) {
+                    int y = baseRow + r, x = baseCol + c;
+                    if (y < 0 || y >= H || x < 0 || x >= W) continue;  // slot left untouched
+                    unpadded[o++] = im[(size_t)b * H * W * Din + (size_t)x * H * Din + (size_t)y * Din + ch];
+                }
+        }
+    int padded = (int)std::pow(std::ceil(std::log2((double)pool)), 2);
+    out.assign((size_t)padded * wK * hK * batch * Din, 0);
+    if (padded == pool) {
+        out = unpadded;
+    } else {
+        size_t npools = (size_t)wK * hK * batch * Din;
+        for (size_t q = 0; q < npools; q++) {
+            for (int j = 0; j < pool; j++) out[q * padded + j] = unpadded[q * pool + j];
+            for (int j = pool; j < padded; j++) out[q * padded + j] = pad_val;
+        }
+    }
+}
+
+// truncate_cols (matrix.cuh:141-154)
+template <typename T> void truncate_cols(const T* a, T* b, size_t rows, int start_cols, int end_cols) {
+    for (size_t r = 0; r < rows; r++)
+        for (int i = 0; i < end_cols; i++) b[r * end_cols + i] = a[r * start_cols + i];
+}
+
+// elementVectorAdd (matrix.cuh:75-84): a[col*rows + row] += b[rowwise ? col : row]
+template <typename T> void element_vector_add(T* a, const T* b, bool rowwise, int rows, int cols) {
+    for (int r = 0; r < rows; r++)
+        for (int c = 0; c < cols; c++) a[(size_t)c * rows + r] = (T)(a[(size_t)c * rows + r] + b[rowwise ? c : r]);
+}
+
+// reduceSum (matrix.cuh:109-126); b accumulates (+=) like the reference.
+template <typename T> void reduce_sum(const T* a, T* b, bool reduceRows, int rows, int cols) {
+    int outn = reduceRows ? cols : rows;
+    for (int c = 0; c < outn; c++)
+        for (int i = 0; i < (reduceRows ? rows : cols); i++)
+            b[c] = (T)(b[c] + (reduceRows ? a[(size_t)cols * i + c] : a[(size_t)cols * c + i]));
+}
+
+// MaxpoolLayer::forward (MaxpoolLayer.cu:52-131) for RSS (numShares() == 2,
+// so every share of every party is padded with -10 * 2^FP).
+template <typename T, typename U>
+void maxpool_layer_forward(const RSSV<T>& in, RSSV<T>& act, RSSV<U>& maxPrime, int H, int W, int C, int pool,
+                           int stride, int batch, int fp, Comm& comm) {
+    int padded = (int)std::pow(std::ceil(std::log2((double)(pool * pool))), 2);
+    T pad_val = (T)(int64_t)(-10 * (1 << fp));
+    RSSV<T> pools;
+    for (int p = 0; p < 3; p++)
+        for (int s = 0; s < 2; s++) {
+            std::vector<T> o;
+            maxpool_im2row<T>(in.v[p][s].data(), o, H, W, pool, C, batch, stride, 0, pad_val);
+            if (p == 0 && s == 0) pools.resize(o.size());
+            pools.v[p][s] = o;
+        }
+    RSSV<U> expMax(pools.n);
+    rss_maxpool<T, U>(pools, act, expMax, padded, comm);
+    size_t rows = pools.n / padded;
+    maxPrime.resize(rows * pool * pool);
+    for (int p = 0; p < 3; p++)
+        for (int s = 0; s < 2; s++)
+            truncate_cols<U>(expMax.v[p][s].data(), maxPrime.v[p][s].data(), rows, padded, pool * pool);
+}
+
+}  // namespace oracle

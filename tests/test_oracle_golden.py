@@ -1,0 +1,323 @@
+"""Pin the CPU oracle against Piranha's own known-answer tests and fixtures.
+
+The cases come from src/test/GPU.cu, src/test/Func.cu and src/test/Layer.cu
+(extracted into tests/golden by make_golden.py). Ring-level kernels (GEMM,
+conv, bitexpand, im2row, ...) must match exactly. Protocol-level cases are
+compared the way the reference compares them: the value revealed at a party,
+decoded from fixed point, within eps = 1e-3 (util.cuh:19), or exactly for the
+integer (convertFixed=false) checks. Reveals are taken at party A and C; with
+the setPublic fall-through (RSS.inl:129-141) party B's view of a public-loaded
+tensor is inconsistent, so the reference's own assertions only hold at A and C
+for those cases.
+"""
+import numpy as np
+import pytest
+
+import oracle as orc
+
+FP = 26
+EPS = 1e-3
+U64 = np.uint64
+
+
+def u64(vals):
+    return np.array([int(v) % (1 << 64) for v in vals], dtype=U64)
+
+
+def s64(x):
+    return np.asarray(x, dtype=U64).view(np.int64)
+
+
+def reveal(views, party=0):
+    return orc.reconstruct(views)[party]
+
+
+# ------------------------------------------------------------- GPU.cu cases
+
+def test_gemm_kats(golden):
+    kat, _ = golden
+    c = kat["CutlassGemm"]
+    a, b = c["arrays"]["a"], c["arrays"]["b"]
+    M, N, K, tA, tB, tC = c["params"]["calls"][0]
+    assert list(orc.gemm(M, N, K, u64(a), tA, u64(b), tB, tC)) == list(u64(c["arrays"]["expected"]))
+
+    c = kat["CutlassGemmTranspose"]
+    a, d = u64(c["arrays"]["a"]), u64(c["arrays"]["d"])
+    outs = ["expected", "expected2", "expected3"]
+    rhs = [a, a, d]
+    for (M, N, K, tA, tB, tC), o, r in zip(c["params"]["calls"], outs, rhs):
+        assert list(orc.gemm(M, N, K, a, tA, r, tB, tC)) == list(u64(c["arrays"][o]))
+
+    c = kat["CutlassGemmTranspose2"]
+    M, N, K, tA, tB, tC = c["params"]["calls"][0]
+    got = orc.gemm(M, N, K, u64(c["arrays"]["a"]), tA, u64(c["arrays"]["b"]), tB, tC)
+    assert list(got) == list(u64(c["arrays"]["expected"]))
+
+
+@pytest.mark.parametrize("name,op,a,b", [
+    ("CutlassConvFprop", orc.FPROP, "im", "f"),
+    ("CutlassConvDgrad", orc.DGRAD, "delta", "f"),
+    ("CutlassConvDgrad2", orc.DGRAD, "delta", "filters"),
+    ("CutlassConvWgrad", orc.WGRAD, "delta", "im"),
+    ("CutlassConvWgrad2", orc.WGRAD, "delta", "input"),
+])
+def test_conv_kats(golden, name, op, a, b):
+    kat, _ = golden
+    c = kat[name]
+    p = c["params"]
+    got = orc.conv(op, p["N"], p["H"], p["W"], p["C"], p["K"], p["R"], p["R"], p["pad"], p["stride"],
+                   u64(c["arrays"][a]), u64(c["arrays"][b]))
+    assert list(got) == list(u64(c["arrays"]["expected"]))
+
+
+def test_element_vector_add_and_reduce(golden):
+    kat, _ = golden
+    c = kat["ElementwiseVectorAdd"]
+    a = orc.element_vector_add(u64(c["arrays"]["a"]), u64(c["arrays"]["row_b"]), True, 2, 3)
+    assert list(a) == list(u64(c["arrays"]["expected"]))
+    a = orc.element_vector_add(a, u64(c["arrays"]["col_b"]), False, 2, 3)
+    assert list(a) == list(u64(c["arrays"]["expected@2"]))
+    c = kat["ReduceSum"]
+    b = orc.reduce_sum(u64(c["arrays"]["a"]), u64(c["arrays"]["b"]), True, 2, 4)
+    assert list(b) == list(u64(c["arrays"]["expected"]))
+
+
+def test_bitexpand_kat(golden):
+    kat, _ = golden
+    c = kat["BitExpand64"]
+    assert list(orc.bitexpand(u64(c["arrays"]["a"]))) == list(u64(c["arrays"]["expected"]))
+
+
+def test_expand_compare_kat(golden):
+    kat, _ = golden
+    c = kat["ExpandCompare"]
+    b = np.array(c["arrays"]["b"], dtype=np.uint8)
+    nb = np.array(c["arrays"]["negb"], dtype=np.uint8)
+    # RSS<uint8_t>(list, false): party A shareA / party C shareB hold the values
+    outs = np.zeros((3, 2, 8), dtype=np.uint8)
+    zero = np.zeros(4, dtype=np.uint8)
+    for p, s in ((0, 0), (2, 1)):
+        outs[p, s] = orc.expand_compare(b, nb, 8)
+    for p, s in ((0, 1), (1, 0), (1, 1), (2, 0)):
+        outs[p, s] = orc.expand_compare(zero, zero, 8)
+    rec = (outs[0, 0].astype(int) + outs[0, 1] + outs[2, 0]) % 256
+    assert list(rec) == [int(v) for v in c["arrays"]["expected"]]
+
+
+def test_maxpool_im2row_kat(golden):
+    kat, _ = golden
+    c = kat["Maxpool_Im2Row"]
+    p = c["params"]
+    got = orc.maxpool_im2row(u64(c["arrays"]["im"]), p["H"], p["W"], p["f"], p["Din"], p["batch"], p["stride"],
+                             p["pad"], p["pad_val"])
+    # the reference compares (double)(int64) values (util.cuh:55-70,317-328)
+    assert np.array_equal(s64(got).astype(np.float64), np.array(c["arrays"]["expected"]))
+
+
+# ------------------------------------------------------------ Func.cu cases
+
+def enc_list(vals, fixed=True):
+    return orc.from_list(vals, U64, FP, to_fixed=fixed)
+
+
+def assert_reveal(views, expected, fixed=True, parties=(0, 1, 2)):
+    rec = orc.reconstruct(views)
+    for p in parties:
+        got = orc.decode(rec[p], FP) if fixed else s64(rec[p]).astype(np.float64)
+        assert np.max(np.abs(got - np.asarray(expected, dtype=np.float64))) <= EPS, (p, got, expected)
+
+
+def test_func_reconstruct(golden):
+    c = golden[0]["Reconstruct"]["arrays"]
+    assert_reveal(enc_list(c["a"]), c["expected"])
+
+
+@pytest.mark.parametrize("name", ["MatMul", "MatMul2"])
+def test_func_matmul(golden, name):
+    c = golden[0][name]
+    p, a = c["params"], c["arrays"]
+    comm = orc.Comm()
+    out = orc.matmul(enc_list(a["a"]), enc_list(a["b"]), p["M"], p["N"], p["K"], p["tA"], p["tB"], p["tC"], FP, comm)
+    assert_reveal(out, a["expected"])
+    mn = p["M"] * p["N"]
+    assert comm.rounds == 1 and comm.tx == [2 * mn * 8] * 3 and comm.rx == [2 * mn * 8] * 3
+
+
+def test_func_mult(golden):
+    a = golden[0]["Mult"]["arrays"]
+    out = orc.mul(enc_list(a["b"], False), enc_list(a["a"], False))
+    assert_reveal(out, a["expected"], fixed=False)
+
+
+@pytest.mark.parametrize("name", ["Truncate", "Truncate2"])
+def test_func_truncate(golden, name):
+    c = golden[0][name]
+    out = orc.divide_public(enc_list(c["arrays"]["a"]), c["params"]["d"])
+    assert_reveal(out, c["arrays"]["expected"])
+
+
+def test_func_truncate_vec(golden):
+    a = golden[0]["TruncateVec"]["arrays"]
+    d = np.array([1 << int(x) for x in a["pows"]], dtype=U64)
+    assert_reveal(orc.divide_public(enc_list(a["a"]), d), a["expected"])
+
+
+def test_func_select_share(golden):
+    a = golden[0]["SelectShare"]["arrays"]
+    z = orc.select_share(enc_list(a["x"]), enc_list(a["y"]), enc_list(a["b"], False))
+    assert_reveal(z, a["expected"])
+
+
+def test_func_convolution(golden):
+    c = golden[0]["Convolution"]
+    p, a = c["params"], c["arrays"]
+    out = orc.convolution(enc_list(a["im"]), enc_list(a["filters"]), orc.FPROP, p["batch"], p["H"], p["W"], p["f"],
+                          p["Din"], p["Dout"], p["stride"], p["pad"], FP)
+    assert_reveal(out, a["expected"])
+
+
+@pytest.mark.parametrize("name", ["DRELU", "DRELU2"])
+def test_func_drelu(golden, name):
+    a = golden[0][name]["arrays"]
+    comm = orc.Comm()
+    res = orc.drelu(enc_list(a["input"]), udtype=U64, comm=comm)
+    assert_reveal(res, a["expected"], fixed=False)
+    n = len(a["input"])
+    assert comm.rounds == 13  # 1 reveal + 6 carry levels x 2 AND-reshares
+    assert comm.tx == [n * 8 + 2 * n * (32 + 16 + 8 + 4 + 2 + 1) * 8] * 3  # u64 bit words
+
+
+def test_func_drelu3(golden):
+    a = golden[0]["DRELU3"]["arrays"]
+    x = enc_list(a["input"])
+    add = u64(a["add"])
+    x = (x + add[None, None, :]).astype(U64)  # every share of every party += add
+    res = orc.drelu(x, udtype=U64)
+    assert_reveal(res, a["expected"], fixed=False)
+
+
+def test_func_relu(golden):
+    a = golden[0]["RELU"]["arrays"]
+    comm = orc.Comm()
+    out, dout = orc.relu(enc_list(a["input"]), udtype=U64, comm=comm)
+    assert_reveal(out, a["expected"])
+    assert_reveal(dout, a["dexpected"], fixed=False)
+    assert comm.rounds == 15
+
+
+def test_func_maxpool(golden):
+    a = golden[0]["Maxpool"]["arrays"]
+    out, dout = orc.maxpool(enc_list(a["input"]), 4, udtype=U64)
+    assert_reveal(out, a["expected"])
+    assert_reveal(dout, a["dexpected"], fixed=False)
+
+
+def test_func_maxpool2(golden):
+    a = golden[0]["Maxpool2"]["arrays"]
+    x = enc_list(a["input"])
+    pools = np.stack([np.stack([orc.maxpool_im2row(x[p, s], 3, 3, 3, 1, 1, 1, 0, -10) for s in range(2)])
+                      for p in range(3)])
+    out, dexp = orc.maxpool(pools, 16, udtype=U64)
+    dres = dexp[:, :, :9]  # truncate_cols(16 -> 9) for the single pool row
+    assert_reveal(out, a["expected"])
+    assert_reveal(dres, a["dexpected"], fixed=False)
+
+
+# ----------------------------------------------------------- Layer.cu cases
+
+def test_layer_relu_basic(golden):
+    a = golden[0]["ReLUForwardBasic"]["arrays"]
+    out, _ = orc.relu(enc_list(a["input"]))
+    assert_reveal(out, a["expected"])
+
+
+def test_layer_maxpool_basic(golden):
+    c = golden[0]["MaxpoolForwardBasic"]
+    p, a = c["params"], c["arrays"]
+    out, _ = orc.maxpool_layer(enc_list(a["inputImage"]), p["H"], p["W"], p["C"], p["pool"], p["stride"], p["batch"])
+    assert_reveal(out, a["expected"])
+
+
+@pytest.mark.parametrize("name", ["CNNForwardBasic", "CNNForwardStride", "CNNForwardInputChannels",
+                                  "CNNForwardAllDims"])
+def test_layer_cnn_inline(golden, name):
+    c = golden[0][name]
+    p, a = c["params"], c["arrays"]
+    out = orc.convolution(enc_list(a["im"]), enc_list(a["filter"]), orc.FPROP, p["batch"], p["H"], p["W"], p["f"],
+                          p["Din"], p["Dout"], p["stride"], p["pad"], FP)
+    assert_reveal(out, a["expected"])
+
+
+def fc_forward(x, w, b, batch, din, dout):
+    """FCLayer::forward (FCLayer.cu:78-130): matmul(tA=tB=tC=1) + per-share bias add."""
+    act = orc.matmul(x, w, batch, dout, din, 1, 1, 1, FP)
+    for p in range(3):
+        for s in range(2):
+            act[p, s] = orc.element_vector_add(act[p, s], b[p, s], False, dout, batch)
+    return act
+
+
+def test_layer_fc_mnist(golden):
+    L = golden[1]
+    x = orc.set_public(L["fc_mnist_input"])
+    w = orc.set_public(L["fc_mnist_weight"])
+    b = orc.set_public(L["fc_mnist_bias"])
+    act = fc_forward(x, w, b, 128, 16, 10)
+    assert_reveal(act, L["fc_mnist_output"], parties=(0, 2))
+
+
+def test_layer_relu_mnist(golden):
+    L = golden[1]
+    out, _ = orc.relu(orc.set_public(L["relu_mnist_input"]))
+    assert_reveal(out, L["relu_mnist_output"], parties=(0, 2))
+
+
+def test_layer_maxpool_mnist(golden):
+    L = golden[1]
+    out, _ = orc.maxpool_layer(orc.set_public(L["maxpool_mnist_input"]), 9, 9, 2, 3, 2, 128)
+    assert_reveal(out, L["maxpool_mnist_output"], parties=(0, 2))
+
+
+def test_layer_cnn_mnist(golden):
+    L = golden[1]
+    out = orc.convolution(orc.set_public(L["cnn_mnist_input"]), orc.set_public(L["cnn_mnist_weight"]), orc.FPROP,
+                          128, 9, 9, 3, 2, 3, 2, 1, FP)
+    assert_reveal(out, L["cnn_mnist_output"], parties=(0, 2))
+
+
+def test_layer_secureml_chain(golden):
+    """SecureML forward (files/test/secureml): FC-ReLU-FC-ReLU-FC-ReLU, every intermediate output."""
+    L = golden[1]
+    x = orc.set_public(L["secureml_input"])
+    dims = [(784, 128), (128, 128), (128, 10)]
+    outs = []
+    for li, (din, dout) in zip((0, 2, 4), dims):
+        w = orc.set_public(L[f"secureml_weight{li}"])
+        b = orc.set_public(L[f"secureml_bias{li}"])
+        x = fc_forward(x, w, b, 128, din, dout)
+        outs.append(x)
+        x, _ = orc.relu(x)
+        outs.append(x)
+    for i, o in enumerate(outs):
+        assert_reveal(o, L[f"secureml_output{i}"], parties=(0,))
+
+
+# --------------------------------------------------------- ring semantics
+
+def test_division_semantics():
+    """functors.cuh:33-45: truncation toward zero of the rounded double."""
+    x = np.array([7, (-7) % (1 << 64), (1 << 60) + 1, (1 << 63) - 1, 1 << 63], dtype=U64)
+    got = s64(orc.div_public_values(x, 2))
+    exp = [3, -3, 1 << 59, 1 << 62, -(1 << 62)]
+    assert list(got) == exp
+    # |x| > 2^53: the int64 -> double rounding is visible
+    x = np.array([(1 << 54) + 3], dtype=U64)
+    assert int(s64(orc.div_public_values(x, 1))[0]) == (1 << 54) + 4
+    # d = 1 and x rounding up to 2^63 saturates like cvt.rzi.s64.f64
+    x = np.array([(1 << 63) - 1], dtype=U64)
+    assert int(s64(orc.div_public_values(x, 1))[0]) == (1 << 63) - 1
+
+
+def test_encode_negative_two_complement():
+    got = orc.encode([-1.5, 2.25, -0.0000001], U64, FP)
+    assert list(s64(got)) == [-(3 << 25), 9 << 24, int(-0.0000001 * (1 << 26))]
