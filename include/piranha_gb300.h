@@ -1,0 +1,203 @@
+/*
+ * piranha_gb300.h — C ABI of the GB300-native implementation of Piranha's
+ * party-local secret-share arithmetic (3-party RSS over Z_2^64 / Z_2^32).
+ *
+ * All three parties are simulated on one GPU. An RSS tensor of n elements is
+ * passed as SIX device pointers, index [party * 2 + share] with party A=0,
+ * B=1, C=2 and share 0 = the reference's "shareA", 1 = "shareB" (RSS.h:74-75).
+ * Each pointer addresses n contiguous elements. Per-party public data (the
+ * output of a reconstruct) is THREE device pointers, one per party.
+ *
+ * Every call is enqueued on the context's stream and returns an int status
+ * (PG_OK = 0). Nothing here exits or asserts: size mismatches and unsupported
+ * shapes return PG_ERR_*, and pg_last_error() gives a message. Calls do not
+ * synchronize; pg_sync() does. Inter-party messages become reads of the
+ * sender's buffer inside the fused kernels; the bytes and rounds a socket
+ * would carry are added to the context's counters with the accounting of
+ * DeviceData::transmit/receive (src/gpu/DeviceData.h:87-118) and
+ * Profiler::add_comm_round (src/util/Profiler.cpp:95-99).
+ *
+ * Citations point at the Piranha (ucbrise/piranha) source each entry point
+ * replaces; paths are relative to that project.
+ */
+#ifndef PIRANHA_GB300_H
+#define PIRANHA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status codes */
+#define PG_OK 0
+#define PG_ERR_INVALID_ARG 1   /* null pointer, negative size, bad enum */
+#define PG_ERR_SIZE 2          /* sizes that do not describe a valid problem */
+#define PG_ERR_CUDA 3          /* a CUDA runtime call failed */
+#define PG_ERR_UNSUPPORTED 4   /* shape outside what a kernel implements */
+#define PG_ERR_TIMEOUT 5       /* a bounded device-side wait gave up */
+#define PG_ERR_NO_MEMORY 6     /* context scratch could not be allocated */
+
+/* share-GEMM / conv implementation forms */
+#define PG_FORM_U64 0          /* plain 64-bit integer CUDA-core kernels */
+#define PG_FORM_LIMB_TC 1      /* 8-bit limbs on tcgen05 tensor cores, exact */
+
+/* cutlass::conv::Operator (used by RSS.inl:706-803), redefined locally */
+#define PG_CONV_FPROP 0
+#define PG_CONV_DGRAD 1
+#define PG_CONV_WGRAD 2
+
+typedef struct pg_ctx pg_ctx;
+
+/* ------------------------------------------------------------------ context
+ * Replaces the reference's process-global state (partyNum, PrecomputeObject,
+ * comm_profiler/func_profiler; src/main.cu:34-38) with an explicit handle. */
+int pg_ctx_create(pg_ctx **out, int device);
+int pg_ctx_destroy(pg_ctx *ctx);
+int pg_ctx_set_stream(pg_ctx *ctx, void *cuda_stream);
+void *pg_ctx_get_stream(pg_ctx *ctx);
+int pg_ctx_set_form(pg_ctx *ctx, int form);
+int pg_ctx_get_form(pg_ctx *ctx);
+const char *pg_last_error(pg_ctx *ctx);
+int pg_sync(pg_ctx *ctx);
+/* counters: out[0..3] = bytes sent by party 0..3, out[4..7] = bytes received,
+ * out[8] = communication rounds (src/util/Profiler.cpp:95-128) */
+int pg_comm_get(pg_ctx *ctx, uint64_t out[9]);
+int pg_comm_reset(pg_ctx *ctx);
+/* number of kernels this library launched through ctx (all streams) */
+uint64_t pg_kernel_launches(pg_ctx *ctx);
+
+/* -------------------------------------------- single-array ring kernels
+ * gpu::gemm (src/gpu/gemm.cuh:102-112): C = A*B mod 2^w, A MxK, B KxN, C MxN;
+ * an operand is row-major when its transpose flag is set, column-major
+ * otherwise (gemm.cuh:64-100). */
+int pg_gemm_u64(pg_ctx *ctx, int M, int N, int K, const uint64_t *A, int tA, const uint64_t *B, int tB,
+                uint64_t *C, int tC);
+int pg_gemm_u32(pg_ctx *ctx, int M, int N, int K, const uint32_t *A, int tA, const uint32_t *B, int tB,
+                uint32_t *C, int tC);
+/* gpu::conv_fprop / conv_dgrad / conv_wgrad (src/gpu/conv.cuh:359-490):
+ * NHWC activations, KRSC filters, cross-correlation, symmetric padding.
+ * fprop: a = X (N,H,W,C), b = F (K,R,S,C), out = Y (N,P,Q,K)
+ * dgrad: a = dY (N,P,Q,K), b = F (K,R,S,C), out = dX (N,H,W,C)
+ * wgrad: a = dY (N,P,Q,K), b = X (N,H,W,C), out = dF (K,R,S,C) */
+int pg_conv_u64(pg_ctx *ctx, int op, int N, int H, int W, int C, int K, int R, int S, int pad, int stride,
+                const uint64_t *a, const uint64_t *b, uint64_t *out);
+
+/* --------------------------------------------------------- RSS protocol
+ * matmul (src/mpc/RSS.inl:482-540 with localMatMul :1097-1110 and
+ * dividePublic3out3 :1077-1094): per party z = A0*(B0+B1) + A1*B0 computed
+ * as one contraction over the concatenated K of all three parties, revealed
+ * 3-out-of-3 and truncated by 2^trunc in the epilogue. */
+int pg_rss_matmul_u64(pg_ctx *ctx, const uint64_t *const a[6], const uint64_t *const b[6], uint64_t *const c[6],
+                      int M, int N, int K, int tA, int tB, int tC, int trunc);
+int pg_rss_matmul_u32(pg_ctx *ctx, const uint32_t *const a[6], const uint32_t *const b[6], uint32_t *const c[6],
+                      int M, int N, int K, int tA, int tB, int tC, int trunc);
+/* FCLayer::forward (src/nn/FCLayer.cu:78-130): matmul(tA=tB=tC=1, FP) followed
+ * by elementVectorAdd of the bias shares, fused into one launch. bias may be
+ * NULL (no bias). */
+int pg_rss_fc_forward_u64(pg_ctx *ctx, const uint64_t *const x[6], const uint64_t *const w[6],
+                          const uint64_t *const bias[6], uint64_t *const out[6], int batch, int din, int dout,
+                          int fp);
+/* convolution (src/mpc/RSS.inl:706-803): the three party-local convolutions
+ * (localFprop/Dgrad/Wgrad :614-703) fused as one implicit GEMM over the
+ * concatenated K, then the 3-out-of-3 truncation. Argument roles follow the
+ * reference: fprop (im, filter), dgrad (delta, filter), wgrad (delta, input). */
+int pg_rss_conv_u64(pg_ctx *ctx, const uint64_t *const A[6], const uint64_t *const B[6], uint64_t *const C[6],
+                    int op, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad, int trunc);
+/* dividePublic(RSS&, T) and dividePublic(RSS&, DeviceData&) (RSS.inl:423-455) */
+int pg_rss_divide_public_u64(pg_ctx *ctx, uint64_t *const a[6], size_t n, uint64_t d);
+int pg_rss_divide_public_vec_u64(pg_ctx *ctx, uint64_t *const a[6], size_t n, const uint64_t *d);
+int pg_rss_divide_public_u32(pg_ctx *ctx, uint32_t *const a[6], size_t n, uint32_t d);
+/* reconstruct (RSS.inl:458-479): out[p] = a_p0 + a_p1 + a_{prev(p)}0 */
+int pg_rss_reconstruct_u64(pg_ctx *ctx, const uint64_t *const a[6], size_t n, uint64_t *const out[3]);
+int pg_rss_reconstruct_u8(pg_ctx *ctx, const uint8_t *const a[6], size_t n, uint8_t *const out[3]);
+/* reshare (RSS.inl:1053-1074): out_p = (c_p, c_{next(p)}) */
+int pg_rss_reshare_u64(pg_ctx *ctx, const uint64_t *const c[3], size_t n, uint64_t *const out[6]);
+/* RSS *= RSS and RSS &= RSS (RSS.inl:284-345), in place on a */
+int pg_rss_mul_u64(pg_ctx *ctx, uint64_t *const a[6], const uint64_t *const b[6], size_t n);
+int pg_rss_and_u64(pg_ctx *ctx, uint64_t *const a[6], const uint64_t *const b[6], size_t n);
+int pg_rss_and_u8(pg_ctx *ctx, uint8_t *const a[6], const uint8_t *const b[6], size_t n);
+/* dReLU (RSS.inl:807-852): result bit shares; carries of the bit-decomposition
+ * circuit (carryOut :1113-1209) evaluated on bit-packed 64-bit words */
+int pg_rss_drelu_u64_u8(pg_ctx *ctx, const uint64_t *const in[6], size_t n, uint8_t *const out[6]);
+int pg_rss_drelu_u64_u64(pg_ctx *ctx, const uint64_t *const in[6], size_t n, uint64_t *const out[6]);
+/* ReLU (RSS.inl:855-865) = dReLU + selectShare(0, x, d), one fused launch */
+int pg_rss_relu_u64_u8(pg_ctx *ctx, const uint64_t *const in[6], size_t n, uint64_t *const out[6],
+                       uint8_t *const dout[6]);
+int pg_rss_relu_u64_u64(pg_ctx *ctx, const uint64_t *const in[6], size_t n, uint64_t *const out[6],
+                        uint64_t *const dout[6]);
+int pg_rss_relu_u32_u8(pg_ctx *ctx, const uint32_t *const in[6], size_t n, uint32_t *const out[6],
+                       uint8_t *const dout[6]);
+/* selectShare (RSS.inl:543-569): z = b ? y : x via the revealed bit */
+int pg_rss_select_share_u64_u8(pg_ctx *ctx, const uint64_t *const x[6], const uint64_t *const y[6],
+                               const uint8_t *const b[6], uint64_t *const z[6], size_t n);
+int pg_rss_select_share_u64_u64(pg_ctx *ctx, const uint64_t *const x[6], const uint64_t *const y[6],
+                                const uint64_t *const b[6], uint64_t *const z[6], size_t n);
+/* maxpool (RSS.inl:868-1017) over rows of k contiguous values (k = 4 or 16);
+ * in is n = rows * k values, out rows values, dout n bit shares */
+int pg_rss_maxpool_u64_u8(pg_ctx *ctx, const uint64_t *const in[6], size_t n, int k, uint64_t *const out[6],
+                          uint8_t *const dout[6]);
+int pg_rss_maxpool_u64_u64(pg_ctx *ctx, const uint64_t *const in[6], size_t n, int k, uint64_t *const out[6],
+                           uint64_t *const dout[6]);
+/* MaxpoolLayer::forward (src/nn/MaxpoolLayer.cu:52-131): maxpool_im2row
+ * windows (reference N,W,H,C indexing), power-of-two padding with
+ * -10 * 2^fp, tournament, truncate_cols; one fused launch. out has
+ * batch*P*Q*C values, maxprime batch*P*Q*C*pool*pool bit shares. */
+int pg_rss_maxpool_layer_u64_u8(pg_ctx *ctx, const uint64_t *const in[6], uint64_t *const out[6],
+                                uint8_t *const maxprime[6], int H, int W, int C, int pool, int stride, int batch,
+                                int fp);
+
+/* ------------------------------------------------------- glue kernels
+ * elementVectorAdd (src/gpu/matrix.cuh:75-84), reduceSum (:109-126),
+ * truncate_cols (:141-154), bitexpand (src/gpu/bitwise.cuh:10-21),
+ * expandCompare (:66-92), maxpool_im2row + stride_pad
+ * (src/gpu/convolution.cuh:56-108,175-191,252-304) */
+int pg_element_vector_add_u64(pg_ctx *ctx, uint64_t *a, const uint64_t *b, int rowwise, int rows, int cols);
+int pg_reduce_sum_u64(pg_ctx *ctx, const uint64_t *a, uint64_t *b, int reduce_rows, int rows, int cols);
+int pg_truncate_cols_u8(pg_ctx *ctx, const uint8_t *a, uint8_t *b, size_t rows, int start_cols, int end_cols);
+int pg_bitexpand_u64(pg_ctx *ctx, const uint64_t *a, size_t n, uint64_t *bits);
+int pg_expand_compare_u8(pg_ctx *ctx, const uint8_t *b, const uint8_t *nb, size_t n, uint8_t *out,
+                         size_t out_n);
+int pg_maxpool_im2row_u64(pg_ctx *ctx, const uint64_t *im, uint64_t *out, int H, int W, int f, int Din,
+                          int batch, int stride, int pad, uint64_t pad_val);
+
+/* ------------------------------------------------------ network executor
+ * NeuralNetwork::forward (src/nn/NeuralNetwork.cu:109-133) for FC / CNN /
+ * ReLU / Maxpool stacks: layers run in order on preallocated share buffers
+ * and the whole forward can be captured as one CUDA graph. */
+#define PG_LAYER_FC 1      /* p = {din, dout} */
+#define PG_LAYER_CNN 2     /* p = {H, W, Din, Dout, f, stride, pad} */
+#define PG_LAYER_RELU 3    /* p = {n per image} */
+#define PG_LAYER_MAXPOOL 4 /* p = {H, W, C, pool, stride} */
+
+typedef struct pg_net pg_net;
+/* spec: nlayers records of 8 ints {type, p0..p6}. Weight/bias shares are
+ * copied in later with pg_net_set_params. */
+int pg_net_create(pg_ctx *ctx, pg_net **out, const int *spec, int nlayers, int batch, int fp);
+int pg_net_destroy(pg_net *net);
+/* layer i's weights (and FC bias, may be NULL) as six device pointers each;
+ * copies on the context stream and waits for the copies to finish */
+int pg_net_set_params(pg_net *net, int layer, const uint64_t *const w[6], const uint64_t *const bias[6]);
+size_t pg_net_input_size(pg_net *net);   /* elements per share buffer */
+size_t pg_net_output_size(pg_net *net);
+/* forward on device-resident shares (six pointers each) */
+int pg_net_forward(pg_net *net, const uint64_t *const in[6], uint64_t *const out[6]);
+/* the same with host buffers: in_host/out_host are [6][n] contiguous
+ * (pinned memory recommended); copies are on the context stream */
+int pg_net_forward_host(pg_net *net, const uint64_t *in_host, uint64_t *out_host);
+/* capture the forward (on the network's own input/output buffers) as a CUDA
+ * graph, recorded on a private stream; later forwards replay it on the
+ * context stream (which may be the legacy default stream) */
+int pg_net_capture(pg_net *net);
+/* forward on the network's own input buffers (filled by the caller through
+ * pg_net_input_shares), replaying the captured graph when there is one */
+int pg_net_forward_resident(pg_net *net);
+int pg_net_input_shares(pg_net *net, uint64_t *out[6]);
+/* device pointers (owned by the network) of layer i's output shares */
+int pg_net_layer_output(pg_net *net, int layer, uint64_t *const out[6], size_t *n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PIRANHA_GB300_H */

@@ -1,0 +1,470 @@
+"""piranha_gb300 — GB300-native party-local secret-share arithmetic (Piranha's hot path).
+
+The compute lives in ``libpiranha_gb300.so`` (hand-written sm_103a CUDA behind
+the C ABI of ``include/piranha_gb300.h``). This module is the Python host
+mirror of the reference's operator surface (``src/mpc/RSS.h:105-145``,
+``src/gpu/gemm.cuh``, ``src/gpu/conv.cuh``): the same operation names and
+argument meanings, operating on all three simulated parties at once.
+
+Share tensors are torch CUDA tensors of shape ``(3, 2, n)`` —
+``[party A/B/C][shareA/shareB][element]`` — holding ring elements
+(uint64 stored as ``torch.int64`` bit patterns, uint32 as ``torch.int32``,
+bit shares as ``torch.uint8``). PyTorch only provides device memory and
+streams here; every operation below is one or more launches of this
+library's own kernels. There is no CPU fallback: if the library cannot be
+built or loaded, importing the ops raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+PG_OK = 0
+FORM_U64, FORM_LIMB_TC = 0, 1
+FPROP, DGRAD, WGRAD = 0, 1, 2
+LAYER_FC, LAYER_CNN, LAYER_RELU, LAYER_MAXPOOL = 1, 2, 3, 4
+FLOAT_PRECISION = 26
+
+_lib = None
+_lock = threading.Lock()
+
+
+class PiranhaError(RuntimeError):
+    pass
+
+
+_P6 = ctypes.c_void_p * 6
+_P3 = ctypes.c_void_p * 3
+
+
+def _declare(lib):
+    vp, i, sz, u64, u32 = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_uint32
+    sig = {
+        "pg_ctx_create": [ctypes.POINTER(vp), i],
+        "pg_ctx_destroy": [vp],
+        "pg_ctx_set_stream": [vp, vp],
+        "pg_ctx_set_form": [vp, i],
+        "pg_ctx_get_form": [vp],
+        "pg_sync": [vp],
+        "pg_comm_get": [vp, vp],
+        "pg_comm_reset": [vp],
+        "pg_gemm_u64": [vp, i, i, i, vp, i, vp, i, vp, i],
+        "pg_gemm_u32": [vp, i, i, i, vp, i, vp, i, vp, i],
+        "pg_conv_u64": [vp, i, i, i, i, i, i, i, i, i, i, vp, vp, vp],
+        "pg_rss_matmul_u64": [vp, _P6, _P6, _P6, i, i, i, i, i, i, i],
+        "pg_rss_matmul_u32": [vp, _P6, _P6, _P6, i, i, i, i, i, i, i],
+        "pg_rss_fc_forward_u64": [vp, _P6, _P6, vp, _P6, i, i, i, i],
+        "pg_rss_conv_u64": [vp, _P6, _P6, _P6, i, i, i, i, i, i, i, i, i, i],
+        "pg_rss_divide_public_u64": [vp, _P6, sz, u64],
+        "pg_rss_divide_public_vec_u64": [vp, _P6, sz, vp],
+        "pg_rss_divide_public_u32": [vp, _P6, sz, u32],
+        "pg_rss_reconstruct_u64": [vp, _P6, sz, _P3],
+        "pg_rss_reconstruct_u8": [vp, _P6, sz, _P3],
+        "pg_rss_reshare_u64": [vp, _P3, sz, _P6],
+        "pg_rss_mul_u64": [vp, _P6, _P6, sz],
+        "pg_rss_and_u64": [vp, _P6, _P6, sz],
+        "pg_rss_and_u8": [vp, _P6, _P6, sz],
+        "pg_rss_drelu_u64_u8": [vp, _P6, sz, _P6],
+        "pg_rss_drelu_u64_u64": [vp, _P6, sz, _P6],
+        "pg_rss_relu_u64_u8": [vp, _P6, sz, _P6, _P6],
+        "pg_rss_relu_u64_u64": [vp, _P6, sz, _P6, _P6],
+        "pg_rss_relu_u32_u8": [vp, _P6, sz, _P6, _P6],
+        "pg_rss_select_share_u64_u8": [vp, _P6, _P6, _P6, _P6, sz],
+        "pg_rss_select_share_u64_u64": [vp, _P6, _P6, _P6, _P6, sz],
+        "pg_rss_maxpool_u64_u8": [vp, _P6, sz, i, _P6, _P6],
+        "pg_rss_maxpool_u64_u64": [vp, _P6, sz, i, _P6, _P6],
+        "pg_rss_maxpool_layer_u64_u8": [vp, _P6, _P6, _P6, i, i, i, i, i, i, i],
+        "pg_element_vector_add_u64": [vp, vp, vp, i, i, i],
+        "pg_reduce_sum_u64": [vp, vp, vp, i, i, i],
+        "pg_truncate_cols_u8": [vp, vp, vp, sz, i, i],
+        "pg_bitexpand_u64": [vp, vp, sz, vp],
+        "pg_expand_compare_u8": [vp, vp, vp, sz, vp, sz],
+        "pg_maxpool_im2row_u64": [vp, vp, vp, i, i, i, i, i, i, i, u64],
+        "pg_net_create": [vp, ctypes.POINTER(vp), vp, i, i, i],
+        "pg_net_destroy": [vp],
+        "pg_net_set_params": [vp, i, _P6, vp],
+        "pg_net_forward": [vp, _P6, _P6],
+        "pg_net_forward_host": [vp, vp, vp],
+        "pg_net_forward_resident": [vp],
+        "pg_net_capture": [vp],
+        "pg_net_input_shares": [vp, _P6],
+        "pg_net_layer_output": [vp, i, _P6, ctypes.POINTER(sz)],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    lib.pg_last_error.argtypes = [vp]
+    lib.pg_last_error.restype = ctypes.c_char_p
+    lib.pg_kernel_launches.argtypes = [vp]
+    lib.pg_kernel_launches.restype = ctypes.c_uint64
+    lib.pg_ctx_get_stream.argtypes = [vp]
+    lib.pg_ctx_get_stream.restype = vp
+    lib.pg_net_input_size.argtypes = [vp]
+    lib.pg_net_input_size.restype = sz
+    lib.pg_net_output_size.argtypes = [vp]
+    lib.pg_net_output_size.restype = sz
+
+
+def lib():
+    """Load (building first when stale) the CUDA library. Raises on failure."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = _build.build()
+            _lib = ctypes.CDLL(path)
+            _declare(_lib)
+    return _lib
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+# ------------------------------------------------------------------ context
+
+class Context:
+    """pg_ctx: stream, implementation form and per-party comm counters."""
+
+    def __init__(self, device: int = 0, stream=None, form: int = FORM_U64):
+        import torch
+
+        self.torch = torch
+        self.device = device
+        torch.cuda.set_device(device)
+        self._h = ctypes.c_void_p()
+        self._check(lib().pg_ctx_create(ctypes.byref(self._h), device))
+        # default: torch's current stream, so that torch's allocator and
+        # uploads are ordered with this library's kernels
+        self.stream = stream if stream is not None else torch.cuda.current_stream(device)
+        lib().pg_ctx_set_stream(self._h, ctypes.c_void_p(self.stream.cuda_stream))
+        self.set_form(form)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, st):
+        if st != PG_OK:
+            msg = lib().pg_last_error(self._h).decode() if getattr(self, "_h", None) else ""
+            raise PiranhaError(f"piranha_gb300 status {st}: {msg}")
+
+    def set_form(self, form: int):
+        self._check(lib().pg_ctx_set_form(self._h, form))
+
+    @property
+    def form(self):
+        return lib().pg_ctx_get_form(self._h)
+
+    def sync(self):
+        self._check(lib().pg_sync(self._h))
+
+    def comm(self):
+        buf = (ctypes.c_uint64 * 9)()
+        self._check(lib().pg_comm_get(self._h, buf))
+        return {"tx": list(buf[0:3]), "rx": list(buf[4:7]), "rounds": buf[8]}
+
+    def reset_comm(self):
+        self._check(lib().pg_comm_reset(self._h))
+
+    def kernel_launches(self) -> int:
+        return int(lib().pg_kernel_launches(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.stream.synchronize()
+            lib().pg_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------- share tensors
+
+def _torch():
+    import torch
+
+    return torch
+
+
+_TDT = {"u64": "int64", "u32": "int32", "u8": "uint8"}
+
+
+def empty_shares(n: int, ring: str = "u64", device="cuda"):
+    torch = _torch()
+    return torch.empty((3, 2, n), dtype=getattr(torch, _TDT[ring]), device=device)
+
+
+def zeros_shares(n: int, ring: str = "u64", device="cuda"):
+    torch = _torch()
+    return torch.zeros((3, 2, n), dtype=getattr(torch, _TDT[ring]), device=device)
+
+
+def to_device(views: np.ndarray, device="cuda"):
+    """numpy (3, 2, n) uint64/uint32/uint8 -> torch device tensor (bit-identical)."""
+    torch = _torch()
+    v = np.ascontiguousarray(views)
+    view_as = {np.dtype(np.uint64): np.int64, np.dtype(np.uint32): np.int32, np.dtype(np.uint8): np.uint8}
+    return torch.from_numpy(v.view(view_as[v.dtype])).to(device)
+
+
+def to_host(t, ring: str = "u64") -> np.ndarray:
+    a = t.detach().cpu().numpy()
+    return a.view({"u64": np.uint64, "u32": np.uint32, "u8": np.uint8}[ring])
+
+
+def _p6(t):
+    if t.dim() != 3 or t.shape[0] != 3 or t.shape[1] != 2 or not t.is_cuda:
+        raise PiranhaError("expected a CUDA share tensor of shape (3, 2, n)")
+    if not t.is_contiguous():
+        raise PiranhaError("share tensor must be contiguous")
+    return _P6(*[t[p, s].data_ptr() for p in range(3) for s in range(2)])
+
+
+def _p3(t):
+    return _P3(*[t[p].data_ptr() for p in range(3)])
+
+
+def _ring(t):
+    torch = _torch()
+    return {torch.int64: "u64", torch.int32: "u32", torch.uint8: "u8"}[t.dtype]
+
+
+# --------------------------------------------------------- RSS protocol ops
+# Names and argument meanings follow src/mpc/RSS.h:105-145.
+
+def matmul(ctx: Context, a, b, c, M, N, K, transpose_a, transpose_b, transpose_c, truncation):
+    """RSS matmul (RSS.inl:482-540): c = trunc(a @ b) as shares of all parties."""
+    fn = lib().pg_rss_matmul_u64 if _ring(a) == "u64" else lib().pg_rss_matmul_u32
+    ctx._check(fn(ctx.handle, _p6(a), _p6(b), _p6(c), M, N, K, int(transpose_a), int(transpose_b), int(transpose_c),
+                  int(truncation)))
+    return c
+
+
+def fc_forward(ctx: Context, x, w, bias, out, batch, din, dout, fp=FLOAT_PRECISION):
+    """FCLayer::forward (FCLayer.cu:78-130): matmul + per-share bias add."""
+    bp = ctypes.cast(_p6(bias), ctypes.c_void_p) if bias is not None else None
+    ctx._check(lib().pg_rss_fc_forward_u64(ctx.handle, _p6(x), _p6(w), bp, _p6(out), batch, din, dout, fp))
+    return out
+
+
+def convolution(ctx: Context, A, B, C, op, batchSize, imageHeight, imageWidth, filterSize, Din, Dout, stride,
+                padding, truncation):
+    """RSS convolution (RSS.inl:706-803)."""
+    ctx._check(lib().pg_rss_conv_u64(ctx.handle, _p6(A), _p6(B), _p6(C), op, batchSize, imageHeight, imageWidth,
+                                     filterSize, Din, Dout, stride, padding, truncation))
+    return C
+
+
+def dividePublic(ctx: Context, a, denominator):
+    """dividePublic (RSS.inl:423-455), scalar or per-element device vector, in place."""
+    n = a.shape[2]
+    torch = _torch()
+    if isinstance(denominator, torch.Tensor):
+        ctx._check(lib().pg_rss_divide_public_vec_u64(ctx.handle, _p6(a), n, ctypes.c_void_p(denominator.data_ptr())))
+    elif _ring(a) == "u32":
+        ctx._check(lib().pg_rss_divide_public_u32(ctx.handle, _p6(a), n, int(denominator) & 0xFFFFFFFF))
+    else:
+        ctx._check(lib().pg_rss_divide_public_u64(ctx.handle, _p6(a), n, int(denominator) & 0xFFFFFFFFFFFFFFFF))
+    return a
+
+
+def reconstruct(ctx: Context, a, out=None):
+    """reconstruct (RSS.inl:458-479): returns (3, n) — the value each party reveals."""
+    torch = _torch()
+    n = a.shape[2]
+    if out is None:
+        out = torch.empty((3, n), dtype=a.dtype, device=a.device)
+    fn = lib().pg_rss_reconstruct_u8 if _ring(a) == "u8" else lib().pg_rss_reconstruct_u64
+    ctx._check(fn(ctx.handle, _p6(a), n, _p3(out)))
+    return out
+
+
+def reshare(ctx: Context, c, out):
+    ctx._check(lib().pg_rss_reshare_u64(ctx.handle, _p3(c), c.shape[1], _p6(out)))
+    return out
+
+
+def mul_(ctx: Context, a, b):
+    """RSS *= RSS (RSS.inl:284-320), in place on a."""
+    ctx._check(lib().pg_rss_mul_u64(ctx.handle, _p6(a), _p6(b), a.shape[2]))
+    return a
+
+
+def and_(ctx: Context, a, b):
+    """RSS &= RSS (RSS.inl:331-345), in place on a."""
+    fn = lib().pg_rss_and_u8 if _ring(a) == "u8" else lib().pg_rss_and_u64
+    ctx._check(fn(ctx.handle, _p6(a), _p6(b), a.shape[2]))
+    return a
+
+
+def dReLU(ctx: Context, input, result):
+    """dReLU (RSS.inl:807-852); result is uint8 or uint64 bit shares."""
+    fn = lib().pg_rss_drelu_u64_u8 if _ring(result) == "u8" else lib().pg_rss_drelu_u64_u64
+    ctx._check(fn(ctx.handle, _p6(input), input.shape[2], _p6(result)))
+    return result
+
+
+def ReLU(ctx: Context, input, result, dresult):
+    """ReLU (RSS.inl:855-865)."""
+    if _ring(input) == "u32":
+        fn = lib().pg_rss_relu_u32_u8
+    else:
+        fn = lib().pg_rss_relu_u64_u8 if _ring(dresult) == "u8" else lib().pg_rss_relu_u64_u64
+    ctx._check(fn(ctx.handle, _p6(input), input.shape[2], _p6(result), _p6(dresult)))
+    return result, dresult
+
+
+def selectShare(ctx: Context, x, y, b, z):
+    """selectShare (RSS.inl:543-569): z = b ? y : x."""
+    fn = lib().pg_rss_select_share_u64_u8 if _ring(b) == "u8" else lib().pg_rss_select_share_u64_u64
+    ctx._check(fn(ctx.handle, _p6(x), _p6(y), _p6(b), _p6(z), x.shape[2]))
+    return z
+
+
+def maxpool(ctx: Context, input, result, dresult, k):
+    """maxpool (RSS.inl:868-1017) over rows of k (4 or 16) contiguous values."""
+    fn = lib().pg_rss_maxpool_u64_u8 if _ring(dresult) == "u8" else lib().pg_rss_maxpool_u64_u64
+    ctx._check(fn(ctx.handle, _p6(input), input.shape[2], k, _p6(result), _p6(dresult)))
+    return result, dresult
+
+
+def maxpool_layer(ctx: Context, input, out, maxprime, H, W, C, pool, stride, batch, fp=FLOAT_PRECISION):
+    """MaxpoolLayer::forward (MaxpoolLayer.cu:52-131)."""
+    ctx._check(lib().pg_rss_maxpool_layer_u64_u8(ctx.handle, _p6(input), _p6(out), _p6(maxprime), H, W, C, pool,
+                                                  stride, batch, fp))
+    return out, maxprime
+
+
+# --------------------------------------------------------------- gpu:: ops
+
+class gpu:
+    """Single-array kernels of src/gpu (gemm.cuh, conv.cuh, matrix.cuh, bitwise.cuh, convolution.cuh)."""
+
+    @staticmethod
+    def gemm(ctx: Context, M, N, K, A, transpose_a, B, transpose_b, C, transpose_c):
+        fn = lib().pg_gemm_u64 if A.dtype == _torch().int64 else lib().pg_gemm_u32
+        ctx._check(fn(ctx.handle, M, N, K, ctypes.c_void_p(A.data_ptr()), int(transpose_a),
+                      ctypes.c_void_p(B.data_ptr()), int(transpose_b), ctypes.c_void_p(C.data_ptr()),
+                      int(transpose_c)))
+        return C
+
+    @staticmethod
+    def conv(ctx: Context, op, N, H, W, C, K, R, S, pad, stride, a, b, out):
+        ctx._check(lib().pg_conv_u64(ctx.handle, op, N, H, W, C, K, R, S, pad, stride, ctypes.c_void_p(a.data_ptr()),
+                                     ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(out.data_ptr())))
+        return out
+
+    @staticmethod
+    def elementVectorAdd(ctx: Context, a, b, rowwise, rows, cols):
+        ctx._check(lib().pg_element_vector_add_u64(ctx.handle, ctypes.c_void_p(a.data_ptr()),
+                                                   ctypes.c_void_p(b.data_ptr()), int(rowwise), rows, cols))
+        return a
+
+    @staticmethod
+    def reduceSum(ctx: Context, a, b, reduceRows, rows, cols):
+        ctx._check(lib().pg_reduce_sum_u64(ctx.handle, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()),
+                                           int(reduceRows), rows, cols))
+        return b
+
+    @staticmethod
+    def truncate_cols(ctx: Context, a, b, rows, start_cols, end_cols):
+        ctx._check(lib().pg_truncate_cols_u8(ctx.handle, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()),
+                                             rows, start_cols, end_cols))
+        return b
+
+    @staticmethod
+    def bitexpand(ctx: Context, a, bits):
+        ctx._check(lib().pg_bitexpand_u64(ctx.handle, ctypes.c_void_p(a.data_ptr()), a.numel(),
+                                          ctypes.c_void_p(bits.data_ptr())))
+        return bits
+
+    @staticmethod
+    def expandCompare(ctx: Context, b, nb, out):
+        ctx._check(lib().pg_expand_compare_u8(ctx.handle, ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(nb.data_ptr()),
+                                              b.numel(), ctypes.c_void_p(out.data_ptr()), out.numel()))
+        return out
+
+    @staticmethod
+    def maxpool_im2row(ctx: Context, im, out, imageHeight, imageWidth, filterSize, Din, batchSize, stride, padding,
+                       pad_val):
+        ctx._check(lib().pg_maxpool_im2row_u64(ctx.handle, ctypes.c_void_p(im.data_ptr()),
+                                               ctypes.c_void_p(out.data_ptr()), imageHeight, imageWidth, filterSize,
+                                               Din, batchSize, stride, padding, int(pad_val) % (1 << 64)))
+        return out
+
+
+# ------------------------------------------------------------------ network
+
+class Network:
+    """Secure-inference executor (NeuralNetwork::forward, NeuralNetwork.cu:109-133).
+
+    ``layers`` is a list of tuples: ("fc", din, dout), ("cnn", H, W, Din, Dout, f, stride, pad),
+    ("relu", n_per_image), ("maxpool", H, W, C, pool, stride).
+    """
+
+    _CODES = {"fc": LAYER_FC, "cnn": LAYER_CNN, "relu": LAYER_RELU, "maxpool": LAYER_MAXPOOL}
+
+    def __init__(self, ctx: Context, layers, batch: int, fp: int = FLOAT_PRECISION):
+        self.ctx = ctx
+        self.layers = list(layers)
+        self.batch = batch
+        spec = np.zeros((len(self.layers), 8), dtype=np.int32)
+        for i, L in enumerate(self.layers):
+            spec[i, 0] = self._CODES[L[0]]
+            spec[i, 1:1 + len(L) - 1] = L[1:]
+        self._spec = spec
+        self._h = ctypes.c_void_p()
+        ctx._check(lib().pg_net_create(ctx.handle, ctypes.byref(self._h), spec.ctypes.data_as(ctypes.c_void_p),
+                                       len(self.layers), batch, fp))
+        self.in_n = int(lib().pg_net_input_size(self._h))
+        self.out_n = int(lib().pg_net_output_size(self._h))
+
+    def set_params(self, layer: int, w, bias=None):
+        bp = ctypes.cast(_p6(bias), ctypes.c_void_p) if bias is not None else None
+        self.ctx._check(lib().pg_net_set_params(self._h, layer, _p6(w), bp))
+
+    def forward(self, x, out):
+        self.ctx._check(lib().pg_net_forward(self._h, _p6(x), _p6(out)))
+        return out
+
+    def capture(self):
+        self.ctx._check(lib().pg_net_capture(self._h))
+
+    def forward_resident(self):
+        self.ctx._check(lib().pg_net_forward_resident(self._h))
+
+    def input_buffers(self):
+        arr = _P6()
+        self.ctx._check(lib().pg_net_input_shares(self._h, arr))
+        return [int(x) for x in arr]
+
+    def forward_host(self, in_host_ptr: int, out_host_ptr: int):
+        self.ctx._check(lib().pg_net_forward_host(self._h, ctypes.c_void_p(in_host_ptr), ctypes.c_void_p(out_host_ptr)))
+
+    def layer_output_ptrs(self, layer: int):
+        arr = _P6()
+        n = ctypes.c_size_t()
+        self.ctx._check(lib().pg_net_layer_output(self._h, layer, arr, ctypes.byref(n)))
+        return [int(x) for x in arr], int(n.value)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.ctx.stream.synchronize()
+            lib().pg_net_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,302 @@
+// pg_abi.cu — the extern "C" surface declared in include/piranha_gb300.h:
+// context lifetime, status/error reporting, communication counters, and thin
+// wrappers that forward to the templated kernels of the other translation
+// units.
+#include <cstring>
+
+#include "pg_common.cuh"
+
+namespace pg {
+
+int set_error(Ctx *c, int code, const char *fmt, ...) {
+    if (!c) return code;
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    c->err = buf;
+    return code;
+}
+
+int launch_status(Ctx *c, const char *what) {
+    cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(c, PG_ERR_CUDA, "%s launch: %s", what, cudaGetErrorString(e));
+    }
+    return PG_OK;
+}
+
+void *scratch(Ctx *c, size_t bytes) {
+    if (bytes <= c->scratch_bytes) return c->scratch;
+    if (c->scratch) {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(c->scratch);
+        c->scratch = nullptr;
+        c->scratch_bytes = 0;
+    }
+    size_t want = bytes + (bytes >> 3);
+    if (cudaMalloc(&c->scratch, want) != cudaSuccess) {
+        cudaGetLastError();
+        set_error(c, PG_ERR_NO_MEMORY, "scratch allocation of %zu bytes failed", want);
+        return nullptr;
+    }
+    c->scratch_bytes = want;
+    return c->scratch;
+}
+
+// kernels in other translation units
+template <typename T>
+int rss_matmul(Ctx *, const T *const *, const T *const *, T *const *, const T *const *, int, int, int, int, int, int,
+               int);
+template <typename T>
+int rss_conv(Ctx *, const T *const *, const T *const *, T *const *, int, int, int, int, int, int, int, int, int, int);
+template <typename T> int plain_gemm(Ctx *, int, int, int, const T *, int, const T *, int, T *, int);
+int plain_conv_u64(Ctx *, int, int, int, int, int, int, int, int, int, int, const uint64_t *, const uint64_t *,
+                   uint64_t *);
+template <typename T, typename U> int rss_drelu(Ctx *, const T *const *, size_t, U *const *);
+template <typename T, typename U> int rss_relu(Ctx *, const T *const *, size_t, T *const *, U *const *);
+template <typename T, typename U>
+int rss_select(Ctx *, const T *const *, const T *const *, const U *const *, T *const *, size_t);
+template <typename T, typename U> int rss_maxpool(Ctx *, const T *const *, size_t, int, T *const *, U *const *);
+template <typename T, typename U>
+int rss_maxpool_layer(Ctx *, const T *const *, T *const *, U *const *, int, int, int, int, int, int, int);
+template <typename T> int rss_reconstruct(Ctx *, const T *const *, size_t, T *const *);
+template <typename T> int rss_reshare(Ctx *, const T *const *, size_t, T *const *);
+template <typename T, bool AND> int rss_mul(Ctx *, T *const *, const T *const *, size_t);
+template <typename T> int rss_divide_public(Ctx *, T *const *, size_t, T, const T *);
+int element_vector_add_u64(Ctx *, uint64_t *, const uint64_t *, int, int, int);
+int reduce_sum_u64(Ctx *, const uint64_t *, uint64_t *, int, int, int);
+int truncate_cols_u8(Ctx *, const uint8_t *, uint8_t *, size_t, int, int);
+int bitexpand_u64(Ctx *, const uint64_t *, size_t, uint64_t *);
+int expand_compare_u8(Ctx *, const uint8_t *, const uint8_t *, size_t, uint8_t *, size_t);
+int maxpool_im2row_u64(Ctx *, const uint64_t *, uint64_t *, int, int, int, int, int, int, int, uint64_t);
+int limb_rss_matmul_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *,
+                        const uint64_t *const *, int, int, int, int, int, int, int);
+int limb_rss_conv_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *, int, int, int, int,
+                      int, int, int, int, int, int);
+
+}  // namespace pg
+
+using namespace pg;
+
+#define CTX_OR_FAIL(c) \
+    if (!(c)) return PG_ERR_INVALID_ARG
+
+extern "C" {
+
+int pg_ctx_create(pg_ctx **out, int device) {
+    if (!out) return PG_ERR_INVALID_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return PG_ERR_CUDA;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return PG_ERR_CUDA;
+    pg_ctx *c = new pg_ctx();
+    c->device = device;
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    *out = c;
+    return PG_OK;
+}
+
+int pg_ctx_destroy(pg_ctx *c) {
+    CTX_OR_FAIL(c);
+    if (c->scratch) {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(c->scratch);
+    }
+    delete c;
+    return PG_OK;
+}
+
+int pg_ctx_set_stream(pg_ctx *c, void *s) {
+    CTX_OR_FAIL(c);
+    c->stream = (cudaStream_t)s;
+    return PG_OK;
+}
+void *pg_ctx_get_stream(pg_ctx *c) { return c ? (void *)c->stream : nullptr; }
+int pg_ctx_set_form(pg_ctx *c, int form) {
+    CTX_OR_FAIL(c);
+    if (form != PG_FORM_U64 && form != PG_FORM_LIMB_TC) return set_error(c, PG_ERR_INVALID_ARG, "bad form %d", form);
+    c->form = form;
+    return PG_OK;
+}
+int pg_ctx_get_form(pg_ctx *c) { return c ? c->form : -1; }
+const char *pg_last_error(pg_ctx *c) { return c ? c->err.c_str() : "null context"; }
+int pg_sync(pg_ctx *c) {
+    CTX_OR_FAIL(c);
+    PG_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PG_OK;
+}
+int pg_comm_get(pg_ctx *c, uint64_t out[9]) {
+    CTX_OR_FAIL(c);
+    if (!out) return PG_ERR_INVALID_ARG;
+    memcpy(out, c->comm, sizeof(c->comm));
+    return PG_OK;
+}
+int pg_comm_reset(pg_ctx *c) {
+    CTX_OR_FAIL(c);
+    memset(c->comm, 0, sizeof(c->comm));
+    return PG_OK;
+}
+uint64_t pg_kernel_launches(pg_ctx *c) { return c ? c->launches.load() : 0; }
+
+int pg_gemm_u64(pg_ctx *c, int M, int N, int K, const uint64_t *A, int tA, const uint64_t *B, int tB, uint64_t *C,
+                int tC) {
+    CTX_OR_FAIL(c);
+    return plain_gemm<uint64_t>(c, M, N, K, A, tA, B, tB, C, tC);
+}
+int pg_gemm_u32(pg_ctx *c, int M, int N, int K, const uint32_t *A, int tA, const uint32_t *B, int tB, uint32_t *C,
+                int tC) {
+    CTX_OR_FAIL(c);
+    return plain_gemm<uint32_t>(c, M, N, K, A, tA, B, tB, C, tC);
+}
+int pg_conv_u64(pg_ctx *c, int op, int N, int H, int W, int C, int K, int R, int S, int pad, int stride,
+                const uint64_t *a, const uint64_t *b, uint64_t *out) {
+    CTX_OR_FAIL(c);
+    return plain_conv_u64(c, op, N, H, W, C, K, R, S, pad, stride, a, b, out);
+}
+
+int pg_rss_matmul_u64(pg_ctx *c, const uint64_t *const a[6], const uint64_t *const b[6], uint64_t *const out[6],
+                      int M, int N, int K, int tA, int tB, int tC, int trunc) {
+    CTX_OR_FAIL(c);
+    if (c->form == PG_FORM_LIMB_TC) return limb_rss_matmul_u64(c, a, b, out, nullptr, M, N, K, tA, tB, tC, trunc);
+    return rss_matmul<uint64_t>(c, a, b, out, nullptr, M, N, K, tA, tB, tC, trunc);
+}
+int pg_rss_matmul_u32(pg_ctx *c, const uint32_t *const a[6], const uint32_t *const b[6], uint32_t *const out[6],
+                      int M, int N, int K, int tA, int tB, int tC, int trunc) {
+    CTX_OR_FAIL(c);
+    return rss_matmul<uint32_t>(c, a, b, out, nullptr, M, N, K, tA, tB, tC, trunc);
+}
+int pg_rss_fc_forward_u64(pg_ctx *c, const uint64_t *const x[6], const uint64_t *const w[6],
+                          const uint64_t *const bias[6], uint64_t *const out[6], int batch, int din, int dout, int fp) {
+    CTX_OR_FAIL(c);
+    if (bias)
+        for (int i = 0; i < 6; i++)
+            if (!bias[i]) return set_error(c, PG_ERR_INVALID_ARG, "null bias share");
+    if (c->form == PG_FORM_LIMB_TC) return limb_rss_matmul_u64(c, x, w, out, bias, batch, dout, din, 1, 1, 1, fp);
+    return rss_matmul<uint64_t>(c, x, w, out, bias, batch, dout, din, 1, 1, 1, fp);
+}
+int pg_rss_conv_u64(pg_ctx *c, const uint64_t *const A[6], const uint64_t *const B[6], uint64_t *const C[6], int op,
+                    int batch, int H, int W, int f, int Din, int Dout, int stride, int pad, int trunc) {
+    CTX_OR_FAIL(c);
+    if (c->form == PG_FORM_LIMB_TC && op == PG_CONV_FPROP)
+        return limb_rss_conv_u64(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc);
+    return rss_conv<uint64_t>(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc);
+}
+int pg_rss_divide_public_u64(pg_ctx *c, uint64_t *const a[6], size_t n, uint64_t d) {
+    CTX_OR_FAIL(c);
+    return rss_divide_public<uint64_t>(c, a, n, d, nullptr);
+}
+int pg_rss_divide_public_vec_u64(pg_ctx *c, uint64_t *const a[6], size_t n, const uint64_t *d) {
+    CTX_OR_FAIL(c);
+    if (!d) return set_error(c, PG_ERR_INVALID_ARG, "null denominators");
+    return rss_divide_public<uint64_t>(c, a, n, 0, d);
+}
+int pg_rss_divide_public_u32(pg_ctx *c, uint32_t *const a[6], size_t n, uint32_t d) {
+    CTX_OR_FAIL(c);
+    return rss_divide_public<uint32_t>(c, a, n, d, nullptr);
+}
+int pg_rss_reconstruct_u64(pg_ctx *c, const uint64_t *const a[6], size_t n, uint64_t *const out[3]) {
+    CTX_OR_FAIL(c);
+    return rss_reconstruct<uint64_t>(c, a, n, out);
+}
+int pg_rss_reconstruct_u8(pg_ctx *c, const uint8_t *const a[6], size_t n, uint8_t *const out[3]) {
+    CTX_OR_FAIL(c);
+    return rss_reconstruct<uint8_t>(c, a, n, out);
+}
+int pg_rss_reshare_u64(pg_ctx *c, const uint64_t *const cin[3], size_t n, uint64_t *const out[6]) {
+    CTX_OR_FAIL(c);
+    return rss_reshare<uint64_t>(c, cin, n, out);
+}
+int pg_rss_mul_u64(pg_ctx *c, uint64_t *const a[6], const uint64_t *const b[6], size_t n) {
+    CTX_OR_FAIL(c);
+    return rss_mul<uint64_t, false>(c, a, b, n);
+}
+int pg_rss_and_u64(pg_ctx *c, uint64_t *const a[6], const uint64_t *const b[6], size_t n) {
+    CTX_OR_FAIL(c);
+    return rss_mul<uint64_t, true>(c, a, b, n);
+}
+int pg_rss_and_u8(pg_ctx *c, uint8_t *const a[6], const uint8_t *const b[6], size_t n) {
+    CTX_OR_FAIL(c);
+    return rss_mul<uint8_t, true>(c, a, b, n);
+}
+int pg_rss_drelu_u64_u8(pg_ctx *c, const uint64_t *const in[6], size_t n, uint8_t *const out[6]) {
+    CTX_OR_FAIL(c);
+    return rss_drelu<uint64_t, uint8_t>(c, in, n, out);
+}
+int pg_rss_drelu_u64_u64(pg_ctx *c, const uint64_t *const in[6], size_t n, uint64_t *const out[6]) {
+    CTX_OR_FAIL(c);
+    return rss_drelu<uint64_t, uint64_t>(c, in, n, out);
+}
+int pg_rss_relu_u64_u8(pg_ctx *c, const uint64_t *const in[6], size_t n, uint64_t *const out[6],
+                       uint8_t *const dout[6]) {
+    CTX_OR_FAIL(c);
+    return rss_relu<uint64_t, uint8_t>(c, in, n, out, dout);
+}
+int pg_rss_relu_u64_u64(pg_ctx *c, const uint64_t *const in[6], size_t n, uint64_t *const out[6],
+                        uint64_t *const dout[6]) {
+    CTX_OR_FAIL(c);
+    return rss_relu<uint64_t, uint64_t>(c, in, n, out, dout);
+}
+int pg_rss_relu_u32_u8(pg_ctx *c, const uint32_t *const in[6], size_t n, uint32_t *const out[6],
+                       uint8_t *const dout[6]) {
+    CTX_OR_FAIL(c);
+    return rss_relu<uint32_t, uint8_t>(c, in, n, out, dout);
+}
+int pg_rss_select_share_u64_u8(pg_ctx *c, const uint64_t *const x[6], const uint64_t *const y[6],
+                               const uint8_t *const b[6], uint64_t *const z[6], size_t n) {
+    CTX_OR_FAIL(c);
+    return rss_select<uint64_t, uint8_t>(c, x, y, b, z, n);
+}
+int pg_rss_select_share_u64_u64(pg_ctx *c, const uint64_t *const x[6], const uint64_t *const y[6],
+                                const uint64_t *const b[6], uint64_t *const z[6], size_t n) {
+    CTX_OR_FAIL(c);
+    return rss_select<uint64_t, uint64_t>(c, x, y, b, z, n);
+}
+int pg_rss_maxpool_u64_u8(pg_ctx *c, const uint64_t *const in[6], size_t n, int k, uint64_t *const out[6],
+                          uint8_t *const dout[6]) {
+    CTX_OR_FAIL(c);
+    return rss_maxpool<uint64_t, uint8_t>(c, in, n, k, out, dout);
+}
+int pg_rss_maxpool_u64_u64(pg_ctx *c, const uint64_t *const in[6], size_t n, int k, uint64_t *const out[6],
+                           uint64_t *const dout[6]) {
+    CTX_OR_FAIL(c);
+    return rss_maxpool<uint64_t, uint64_t>(c, in, n, k, out, dout);
+}
+int pg_rss_maxpool_layer_u64_u8(pg_ctx *c, const uint64_t *const in[6], uint64_t *const out[6],
+                                uint8_t *const maxprime[6], int H, int W, int C, int pool, int stride, int batch,
+                                int fp) {
+    CTX_OR_FAIL(c);
+    return rss_maxpool_layer<uint64_t, uint8_t>(c, in, out, maxprime, H, W, C, pool, stride, batch, fp);
+}
+int pg_element_vector_add_u64(pg_ctx *c, uint64_t *a, const uint64_t *b, int rowwise, int rows, int cols) {
+    CTX_OR_FAIL(c);
+    return element_vector_add_u64(c, a, b, rowwise, rows, cols);
+}
+int pg_reduce_sum_u64(pg_ctx *c, const uint64_t *a, uint64_t *b, int reduce_rows, int rows, int cols) {
+    CTX_OR_FAIL(c);
+    return reduce_sum_u64(c, a, b, reduce_rows, rows, cols);
+}
+int pg_truncate_cols_u8(pg_ctx *c, const uint8_t *a, uint8_t *b, size_t rows, int start_cols, int end_cols) {
+    CTX_OR_FAIL(c);
+    return truncate_cols_u8(c, a, b, rows, start_cols, end_cols);
+}
+int pg_bitexpand_u64(pg_ctx *c, const uint64_t *a, size_t n, uint64_t *bits) {
+    CTX_OR_FAIL(c);
+    return bitexpand_u64(c, a, n, bits);
+}
+int pg_expand_compare_u8(pg_ctx *c, const uint8_t *b, const uint8_t *nb, size_t n, uint8_t *out, size_t out_n) {
+    CTX_OR_FAIL(c);
+    return expand_compare_u8(c, b, nb, n, out, out_n);
+}
+int pg_maxpool_im2row_u64(pg_ctx *c, const uint64_t *im, uint64_t *out, int H, int W, int f, int Din, int batch,
+                          int stride, int pad, uint64_t pad_val) {
+    CTX_OR_FAIL(c);
+    return maxpool_im2row_u64(c, im, out, H, W, f, Din, batch, stride, pad, pad_val);
+}
+
+}  // extern "C"

@@ -1,0 +1,360 @@
+// pg_gemm_u64.cu — the plain 64/32-bit integer CUDA-core form of the ring
+// GEMM and implicit-GEMM convolutions, with the RSS truncation epilogue.
+//
+// One kernel covers gpu::gemm (src/gpu/gemm.cuh:64-112), gpu::conv_fprop /
+// conv_dgrad / conv_wgrad (src/gpu/conv.cuh:359-490) and, through K
+// segments, RSS localMatMul (src/mpc/RSS.inl:1097-1110) and
+// localFprop/Dgrad/Wgrad (:614-703): for the three simulated parties the six
+// segments are [x_p0 | x_p1] x [y_p0 + y_p1 ; y_p0], so one contraction over
+// the concatenated K accumulates sum_p z_p, which is exactly what
+// reconstruct3out3 (:1020-1050) reveals. The epilogue then applies
+// dividePublic3out3 (:1077-1094) and writes all six output shares (plus the
+// FC bias shares of FCLayer.cu:110-116 when given).
+#include "pg_common.cuh"
+
+namespace pg {
+
+enum GemmKind { K_GEMM = 0, K_FPROP = 1, K_DGRAD = 2, K_WGRAD = 3 };
+enum Epi { EPI_RAW = 0, EPI_RSS = 1 };
+
+// unsigned 32-bit division by a runtime constant (round-up multiply-high)
+struct FastDiv {
+    uint32_t d, m;
+    int s;
+    __host__ void init(uint32_t dd) {
+        d = dd;
+        if (dd <= 1) { m = 0; s = 0; return; }
+        s = 0;
+        while ((1ull << s) < dd) s++;
+        m = (uint32_t)((((1ull << 32) * ((1ull << s) - dd)) / dd) + 1);
+    }
+    __device__ __forceinline__ uint32_t div(uint32_t x) const {
+        if (d == 1) return x;
+        uint32_t hi = __umulhi(x, m);
+        return (hi + ((x - hi) >> 1)) >> (s - 1);
+    }
+};
+
+template <typename T> struct GemmArgs {
+    int M, N, K;  // K per segment
+    int nseg;
+    const T *a[6];
+    const T *b0[6];
+    const T *b1[6];  // added to b0 when not null
+    int tA, tB, tC;
+    // conv geometry
+    int cn, ch, cw, cc, ck, cr, cs, cp, cq, pad, stride;
+    FastDiv dQ, dP, dW, dH, dC, dS, dK, dRSC;
+    // epilogue
+    int epi;
+    T *c_raw;
+    T *out[6];
+    const T *bias[6];
+    T d;
+    int dshift;
+};
+
+constexpr int BM = 128, BN = 64, BK = 16, NT = 256, TM = 8, TN = 4;
+constexpr int APAD = 2, BPAD = 2;
+
+// Which index of a loaded element varies fastest across threads.
+template <int KIND> struct Layout {
+    // A: true = m-fastest (M-contiguous operand), false = k-fastest
+    static __device__ __forceinline__ bool a_mfast(const void *) { return KIND == K_WGRAD; }
+};
+
+template <typename T, int KIND> struct Loader {
+    // A[m][k] of segment s
+    static __device__ __forceinline__ T load_a(const GemmArgs<T> &g, const T *a, int m, int k) {
+        if (m >= g.M || k >= g.K) return 0;
+        if (KIND == K_GEMM) {
+            return g.tA ? a[(size_t)m * g.K + k] : a[(size_t)m + (size_t)k * g.M];
+        } else if (KIND == K_FPROP) {
+            // m = (n, p, q); k = (r, s, c)
+            uint32_t nq = g.dQ.div(m), q = m - nq * g.cq;
+            uint32_t n = g.dP.div(nq), p = nq - n * g.cp;
+            uint32_t rs = g.dC.div(k), c = k - rs * g.cc;
+            uint32_t r = g.dS.div(rs), s = rs - r * g.cs;
+            int h = (int)(p * g.stride) - g.pad + (int)r, w = (int)(q * g.stride) - g.pad + (int)s;
+            if (h < 0 || h >= g.ch || w < 0 || w >= g.cw) return 0;
+            return a[(((size_t)n * g.ch + h) * g.cw + w) * g.cc + c];
+        } else if (KIND == K_DGRAD) {
+            // m = (n, h, w); k = (r, s, kk); value dY[n][p][q][kk] with h = p*st - pad + r
+            uint32_t nh = g.dW.div(m), w = m - nh * g.cw;
+            uint32_t n = g.dH.div(nh), h = nh - n * g.ch;
+            uint32_t rs = g.dK.div(k), kk = k - rs * g.ck;
+            uint32_t r = g.dS.div(rs), s = rs - r * g.cs;
+            int ph = (int)h + g.pad - (int)r, qw = (int)w + g.pad - (int)s;
+            if (ph < 0 || qw < 0 || ph % g.stride || qw % g.stride) return 0;
+            int p = ph / g.stride, q = qw / g.stride;
+            if (p >= g.cp || q >= g.cq) return 0;
+            return a[(((size_t)n * g.cp + p) * g.cq + q) * g.ck + kk];
+        } else {  // K_WGRAD: m = kk, k = (n, p, q): dY[k][m]
+            return a[(size_t)k * g.ck + m];
+        }
+    }
+    static __device__ __forceinline__ T load_b1(const GemmArgs<T> &g, const T *b, int k, int n) {
+        if (KIND == K_GEMM) {
+            return g.tB ? b[(size_t)k * g.N + n] : b[(size_t)k + (size_t)n * g.K];
+        } else if (KIND == K_FPROP) {
+            return b[(size_t)n * g.K + k];  // F[co][r][s][c], k = (r,s,c)
+        } else if (KIND == K_DGRAD) {
+            uint32_t rs = g.dK.div(k), kk = k - rs * g.ck;  // k = (r, s, kk), n = c
+            return b[((size_t)kk * g.cr * g.cs + rs) * g.cc + n];
+        } else {  // K_WGRAD: k = (n, p, q), n_out = (r, s, c): X[n][p*st-pad+r][q*st-pad+s][c]
+            uint32_t nq = g.dQ.div(k), q = k - nq * g.cq;
+            uint32_t nn = g.dP.div(nq), p = nq - nn * g.cp;
+            uint32_t rs = g.dC.div(n), c = n - rs * g.cc;
+            uint32_t r = g.dS.div(rs), s = rs - r * g.cs;
+            int h = (int)(p * g.stride) - g.pad + (int)r, w = (int)(q * g.stride) - g.pad + (int)s;
+            if (h < 0 || h >= g.ch || w < 0 || w >= g.cw) return 0;
+            return b[(((size_t)nn * g.ch + h) * g.cw + w) * g.cc + c];
+        }
+    }
+    static __device__ __forceinline__ T load_b(const GemmArgs<T> &g, int seg, int k, int n) {
+        if (k >= g.K || n >= g.N) return 0;
+        T v = load_b1(g, g.b0[seg], k, n);
+        if (g.b1[seg]) v = (T)(v + load_b1(g, g.b1[seg], k, n));
+        return v;
+    }
+    // B k-fastest for K-contiguous B operands
+    static constexpr bool b_kfast = (KIND == K_FPROP);
+};
+
+template <typename T, int KIND>
+__global__ void __launch_bounds__(NT) ring_gemm_kernel(const GemmArgs<T> g) {
+    __shared__ T As[2][BK][BM + APAD];
+    __shared__ T Bs[2][BK][BN + BPAD];
+    using L = Loader<T, KIND>;
+    const int tid = threadIdx.x;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const bool a_mfast = (KIND == K_WGRAD) || (KIND == K_GEMM && !g.tA);
+    const bool b_kfast = (KIND == K_FPROP) || (KIND == K_GEMM && !g.tB);
+
+    T acc[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; i++)
+#pragma unroll
+        for (int j = 0; j < TN; j++) acc[i][j] = 0;
+
+    T ra[BM * BK / NT], rb[BN * BK / NT];
+    const int ksteps = (g.K + BK - 1) / BK;
+    const int total = ksteps * g.nseg;
+
+    auto gload = [&](int step) {
+        int seg = step / ksteps, k0 = (step - seg * ksteps) * BK;
+        const T *a = g.a[seg];
+#pragma unroll
+        for (int i = 0; i < BM * BK / NT; i++) {
+            int e = tid + i * NT;
+            int mm = a_mfast ? (e % BM) : (e / BK), kk = a_mfast ? (e / BM) : (e % BK);
+            ra[i] = L::load_a(g, a, m0 + mm, k0 + kk);
+        }
+#pragma unroll
+        for (int i = 0; i < BN * BK / NT; i++) {
+            int e = tid + i * NT;
+            int kk = b_kfast ? (e % BK) : (e / BN), nn = b_kfast ? (e / BK) : (e % BN);
+            rb[i] = L::load_b(g, seg, k0 + kk, n0 + nn);
+        }
+    };
+    auto sstore = [&](int buf) {
+#pragma unroll
+        for (int i = 0; i < BM * BK / NT; i++) {
+            int e = tid + i * NT;
+            int mm = a_mfast ? (e % BM) : (e / BK), kk = a_mfast ? (e / BM) : (e % BK);
+            As[buf][kk][mm] = ra[i];
+        }
+#pragma unroll
+        for (int i = 0; i < BN * BK / NT; i++) {
+            int e = tid + i * NT;
+            int kk = b_kfast ? (e % BK) : (e / BN), nn = b_kfast ? (e / BK) : (e % BN);
+            Bs[buf][kk][nn] = rb[i];
+        }
+    };
+
+    const int tm = tid / (BN / TN), tn = tid % (BN / TN);
+    if (total > 0) {
+        gload(0);
+        sstore(0);
+    }
+    __syncthreads();
+    for (int step = 0; step < total; step++) {
+        int buf = step & 1;
+        if (step + 1 < total) gload(step + 1);
+#pragma unroll
+        for (int kk = 0; kk < BK; kk++) {
+            T av[TM], bv[TN];
+#pragma unroll
+            for (int i = 0; i < TM; i++) av[i] = As[buf][kk][tm * TM + i];
+#pragma unroll
+            for (int j = 0; j < TN; j++) bv[j] = Bs[buf][kk][tn * TN + j];
+#pragma unroll
+            for (int i = 0; i < TM; i++)
+#pragma unroll
+                for (int j = 0; j < TN; j++) acc[i][j] = (T)(acc[i][j] + av[i] * bv[j]);
+        }
+        if (step + 1 < total) sstore(buf ^ 1);
+        __syncthreads();
+    }
+
+    // epilogue
+#pragma unroll
+    for (int i = 0; i < TM; i++) {
+        int m = m0 + tm * TM + i;
+        if (m >= g.M) continue;
+#pragma unroll
+        for (int j = 0; j < TN; j++) {
+            int n = n0 + tn * TN + j;
+            if (n >= g.N) continue;
+            size_t idx = (KIND == K_GEMM && !g.tC) ? (size_t)m + (size_t)n * g.M : (size_t)m * g.N + n;
+            T z = acc[i][j];
+            if (g.epi == EPI_RAW) {
+                g.c_raw[idx] = z;
+            } else {
+                // dividePublic3out3: reveal sum_p z_p - d, divide, r = 1 at A.shareA / C.shareB
+                T v = (T)(1 + div_public<T>((T)(z - g.d), g.d, g.dshift));
+#pragma unroll
+                for (int ps = 0; ps < 6; ps++) {
+                    T base = (ps == 0 || ps == 5) ? v : (T)0;
+                    if (g.bias[ps]) base = (T)(base + g.bias[ps][n]);
+                    g.out[ps][idx] = base;
+                }
+            }
+        }
+    }
+}
+
+template <typename T> static void setup_conv(GemmArgs<T> &g, int op, int N, int H, int W, int C, int K, int R,
+                                            int S, int pad, int stride) {
+    int P = (H + 2 * pad - R) / stride + 1, Q = (W + 2 * pad - S) / stride + 1;
+    g.cn = N; g.ch = H; g.cw = W; g.cc = C; g.ck = K; g.cr = R; g.cs = S; g.cp = P; g.cq = Q;
+    g.pad = pad; g.stride = stride;
+    g.dQ.init(Q); g.dP.init(P); g.dW.init(W); g.dH.init(H); g.dC.init(C); g.dS.init(S); g.dK.init(K);
+    g.dRSC.init(R * S * C);
+    if (op == PG_CONV_FPROP) { g.M = N * P * Q; g.N = K; g.K = R * S * C; }
+    else if (op == PG_CONV_DGRAD) { g.M = N * H * W; g.N = C; g.K = R * S * K; }
+    else { g.M = K; g.N = R * S * C; g.K = N * P * Q; }
+}
+
+template <typename T> static int launch_gemm(Ctx *c, GemmArgs<T> &g, int kind) {
+    if (g.M <= 0 || g.N <= 0 || g.K < 0) return set_error(c, PG_ERR_SIZE, "ring gemm: bad sizes M=%d N=%d K=%d", g.M, g.N, g.K);
+    dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM);
+    if (grid.y > 65535) return set_error(c, PG_ERR_UNSUPPORTED, "ring gemm: M=%d too large", g.M);
+    switch (kind) {
+        case K_GEMM: ring_gemm_kernel<T, K_GEMM><<<grid, NT, 0, c->stream>>>(g); break;
+        case K_FPROP: ring_gemm_kernel<T, K_FPROP><<<grid, NT, 0, c->stream>>>(g); break;
+        case K_DGRAD: ring_gemm_kernel<T, K_DGRAD><<<grid, NT, 0, c->stream>>>(g); break;
+        default: ring_gemm_kernel<T, K_WGRAD><<<grid, NT, 0, c->stream>>>(g); break;
+    }
+    c->launches++;
+    return launch_status(c, "ring_gemm_kernel");
+}
+
+// --------------------------------------------------------------- entry glue
+
+template <typename T> static void zero_args(GemmArgs<T> &g) { memset(&g, 0, sizeof(g)); }
+
+// Fill the six RSS segments: seg 2p = (x_p0, y_p0 + y_p1), seg 2p+1 = (x_p1, y_p0).
+template <typename T> static void rss_segments(GemmArgs<T> &g, const T *const *a, const T *const *b) {
+    g.nseg = 6;
+    for (int p = 0; p < 3; p++) {
+        g.a[2 * p] = a[2 * p];
+        g.b0[2 * p] = b[2 * p];
+        g.b1[2 * p] = b[2 * p + 1];
+        g.a[2 * p + 1] = a[2 * p + 1];
+        g.b0[2 * p + 1] = b[2 * p];
+        g.b1[2 * p + 1] = nullptr;
+    }
+}
+
+template <typename T> static int rss_epilogue(Ctx *c, GemmArgs<T> &g, T *const *out, int trunc) {
+    if (trunc < 0 || trunc >= (int)(sizeof(T) * 8)) return set_error(c, PG_ERR_INVALID_ARG, "bad truncation %d", trunc);
+    g.epi = EPI_RSS;
+    for (int i = 0; i < 6; i++) g.out[i] = out[i];
+    g.d = (T)((T)1 << trunc);
+    g.dshift = pow2_shift<T>(g.d);
+    return PG_OK;
+}
+
+template <typename T>
+int rss_matmul(Ctx *c, const T *const a[6], const T *const b[6], T *const out[6], const T *const bias[6], int M,
+               int N, int K, int tA, int tB, int tC, int trunc) {
+    CSh6<T> ca, cb;
+    Sh6<T> co;
+    if (!load6(ca, a) || !load6(cb, b) || !load6(co, out)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    if (M <= 0 || N <= 0 || K <= 0) return set_error(c, PG_ERR_SIZE, "matmul: bad sizes");
+    GemmArgs<T> g;
+    zero_args(g);
+    g.M = M; g.N = N; g.K = K; g.tA = tA; g.tB = tB; g.tC = tC;
+    rss_segments(g, a, b);
+    int st = rss_epilogue(c, g, out, trunc);
+    if (st) return st;
+    if (bias)
+        for (int i = 0; i < 6; i++) g.bias[i] = bias[i];
+    st = launch_gemm(c, g, K_GEMM);
+    if (st) return st;
+    comm_msg(c, 2ull * M * N * sizeof(T), 2ull * M * N * sizeof(T));  // reconstruct3out3
+    comm_round(c);
+    return PG_OK;
+}
+
+template <typename T>
+int rss_conv(Ctx *c, const T *const A[6], const T *const B[6], T *const C[6], int op, int batch, int H, int W, int f,
+             int Din, int Dout, int stride, int pad, int trunc) {
+    CSh6<T> ca, cb;
+    Sh6<T> co;
+    if (!load6(ca, A) || !load6(cb, B) || !load6(co, C)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    if (op < 0 || op > 2) return set_error(c, PG_ERR_INVALID_ARG, "bad conv operator %d", op);
+    if (batch <= 0 || H <= 0 || W <= 0 || f <= 0 || Din <= 0 || Dout <= 0 || stride <= 0 || pad < 0 ||
+        H + 2 * pad < f || W + 2 * pad < f)
+        return set_error(c, PG_ERR_SIZE, "conv: bad geometry");
+    GemmArgs<T> g;
+    zero_args(g);
+    setup_conv(g, op, batch, H, W, Din, Dout, f, f, pad, stride);
+    rss_segments(g, A, B);
+    int st = rss_epilogue(c, g, C, trunc);
+    if (st) return st;
+    st = launch_gemm(c, g, op == PG_CONV_FPROP ? K_FPROP : op == PG_CONV_DGRAD ? K_DGRAD : K_WGRAD);
+    if (st) return st;
+    uint64_t n_out = (uint64_t)g.M * g.N;
+    comm_msg(c, 2 * n_out * sizeof(T), 2 * n_out * sizeof(T));
+    comm_round(c);
+    return PG_OK;
+}
+
+template <typename T>
+int plain_gemm(Ctx *c, int M, int N, int K, const T *A, int tA, const T *B, int tB, T *C, int tC) {
+    if (!A || !B || !C) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+    if (M <= 0 || N <= 0 || K <= 0) return set_error(c, PG_ERR_SIZE, "gemm: bad sizes");
+    GemmArgs<T> g;
+    zero_args(g);
+    g.M = M; g.N = N; g.K = K; g.tA = tA; g.tB = tB; g.tC = tC;
+    g.nseg = 1; g.a[0] = A; g.b0[0] = B; g.b1[0] = nullptr;
+    g.epi = EPI_RAW; g.c_raw = C;
+    return launch_gemm(c, g, K_GEMM);
+}
+
+int plain_conv_u64(Ctx *c, int op, int N, int H, int W, int C, int K, int R, int S, int pad, int stride,
+                   const uint64_t *a, const uint64_t *b, uint64_t *out) {
+    if (!a || !b || !out) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+    if (op < 0 || op > 2 || N <= 0 || H <= 0 || W <= 0 || C <= 0 || K <= 0 || R <= 0 || S <= 0 || stride <= 0 ||
+        pad < 0 || H + 2 * pad < R || W + 2 * pad < S)
+        return set_error(c, PG_ERR_SIZE, "conv: bad geometry");
+    GemmArgs<uint64_t> g;
+    zero_args(g);
+    setup_conv(g, op, N, H, W, C, K, R, S, pad, stride);
+    g.nseg = 1; g.a[0] = a; g.b0[0] = b; g.b1[0] = nullptr;
+    g.epi = EPI_RAW; g.c_raw = out;
+    return launch_gemm(c, g, op == PG_CONV_FPROP ? K_FPROP : op == PG_CONV_DGRAD ? K_DGRAD : K_WGRAD);
+}
+
+template int rss_matmul<uint64_t>(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *,
+                                  const uint64_t *const *, int, int, int, int, int, int, int);
+template int rss_matmul<uint32_t>(Ctx *, const uint32_t *const *, const uint32_t *const *, uint32_t *const *,
+                                  const uint32_t *const *, int, int, int, int, int, int, int);
+template int rss_conv<uint64_t>(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *, int, int,
+                                int, int, int, int, int, int, int, int);
+template int plain_gemm<uint64_t>(Ctx *, int, int, int, const uint64_t *, int, const uint64_t *, int, uint64_t *, int);
+template int plain_gemm<uint32_t>(Ctx *, int, int, int, const uint32_t *, int, const uint32_t *, int, uint32_t *, int);
+
+}  // namespace pg

@@ -1,0 +1,211 @@
+// pg_maxpool.cu — fused RSS maxpool: window gather + tournament + argmax bits.
+//
+// Restates MaxpoolLayer::forward (src/nn/MaxpoolLayer.cu:52-131) and maxpool
+// (src/mpc/RSS.inl:868-1017). The reference materialises the pool rows with
+// maxpool_im2row + stride_pad (src/gpu/convolution.cuh:56-108,175-191), then
+// runs a tournament over strided even/odd views of the whole row array: per
+// level a dReLU of even - odd, a selectShare that keeps the larger value in
+// the even slot, and dresult &= expandCompare(b, 1 - b). Pairs never cross a
+// pool row (the padded row length is a power of two), so one thread can own
+// one pool row for all three parties and run every level in registers.
+#include "pg_relu_value.cuh"
+
+namespace pg {
+
+template <typename T, typename U, int K>
+__device__ __forceinline__ void tournament(T (&v)[K][3][2], U (&dr)[K][3][2]) {
+#pragma unroll
+    for (int i = 0; i < K; i++)
+#pragma unroll
+        for (int p = 0; p < 3; p++) {
+            dr[i][p][0] = (p == 0) ? 1 : 0;  // dresult.fill(1)
+            dr[i][p][1] = (p == 2) ? 1 : 0;
+        }
+#pragma unroll
+    for (int s = 2; s <= K; s *= 2) {
+        const int half = s / 2;
+        U ex[K][3][2];
+#pragma unroll
+        for (int j = 0; j < K / s; j++) {
+            const int e = s * j, o = s * j + half;
+            T diff[3][2];
+            U b[3][2];
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int q = 0; q < 2; q++) diff[p][q] = (T)(v[e][p][q] - v[o][p][q]);
+            drelu_value<T, U>(diff, b);
+            T z[3][2];
+            select_value<T, U>(v[o], v[e], b, z);  // selectShare(odd, even, b, even)
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int q = 0; q < 2; q++) v[e][p][q] = z[p][q];
+            // negated = fill(1) - b; expandCompare(b, negated)
+#pragma unroll
+            for (int i = 0; i < s; i++)
+#pragma unroll
+                for (int p = 0; p < 3; p++) {
+                    if (i < half) {
+                        ex[e + i][p][0] = b[p][0];
+                        ex[e + i][p][1] = b[p][1];
+                    } else {
+                        ex[e + i][p][0] = (U)((p == 0 ? 1 : 0) - b[p][0]);
+                        ex[e + i][p][1] = (U)((p == 2 ? 1 : 0) - b[p][1]);
+                    }
+                }
+        }
+        // dresult &= expandedB (RSS AND with reshare)
+#pragma unroll
+        for (int i = 0; i < K; i++) {
+            U c[3];
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+                c[p] = (U)((dr[i][p][0] & (U)(ex[i][p][0] ^ ex[i][p][1])) ^ (dr[i][p][1] & ex[i][p][0]));
+#pragma unroll
+            for (int p = 0; p < 3; p++) {
+                dr[i][p][0] = c[p];
+                dr[i][p][1] = c[next_party(p)];
+            }
+        }
+    }
+}
+
+template <typename T, typename U, int K>
+__global__ void maxpool_rows_kernel(CSh6<T> in, size_t rows, Sh6<T> out, Sh6<U> dout) {
+    for (size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x; r < rows; r += (size_t)gridDim.x * blockDim.x) {
+        T v[K][3][2];
+        U dr[K][3][2];
+#pragma unroll
+        for (int i = 0; i < K; i++)
+#pragma unroll
+            for (int k = 0; k < 6; k++) v[i][k >> 1][k & 1] = in.p[k][r * K + i];
+        tournament<T, U, K>(v, dr);
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            out.p[k][r] = v[0][k >> 1][k & 1];
+#pragma unroll
+            for (int i = 0; i < K; i++) dout.p[k][r * K + i] = dr[i][k >> 1][k & 1];
+        }
+    }
+}
+
+struct PoolGeom {
+    int H, W, C, f, stride, batch, wK, hK;
+    uint64_t pad_val;
+};
+
+// One thread per (image, window, channel) pool row in the reference's order:
+// row = (b * (wK*hK) + win) * C + ch, window elements gathered with the
+// (batch, x=col, y=row, channel) indexing of maxpool_im2row.
+template <typename T, typename U, int K>
+__global__ void maxpool_layer_kernel(CSh6<T> in, PoolGeom g, size_t rows, Sh6<T> out, Sh6<U> maxprime) {
+    const int pool = g.f * g.f;
+    for (size_t row = blockIdx.x * (size_t)blockDim.x + threadIdx.x; row < rows;
+         row += (size_t)gridDim.x * blockDim.x) {
+        int ch = (int)(row % g.C);
+        size_t t = row / g.C;
+        int win = (int)(t % ((size_t)g.wK * g.hK));
+        int b = (int)(t / ((size_t)g.wK * g.hK));
+        int baseCol = (win / g.hK) * g.stride, baseRow = (win % g.hK) * g.stride;
+        T v[K][3][2];
+        U dr[K][3][2];
+#pragma unroll
+        for (int i = 0; i < K; i++) {
+            if (i < pool) {
+                int c = i / g.f, r = i - c * g.f;
+                size_t src = (size_t)b * g.H * g.W * g.C + (size_t)(baseCol + c) * g.H * g.C +
+                             (size_t)(baseRow + r) * g.C + ch;
+#pragma unroll
+                for (int k = 0; k < 6; k++) v[i][k >> 1][k & 1] = in.p[k][src];
+            } else {
+#pragma unroll
+                for (int k = 0; k < 6; k++) v[i][k >> 1][k & 1] = (T)g.pad_val;  // stride_pad value
+            }
+        }
+        tournament<T, U, K>(v, dr);
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            out.p[k][row] = v[0][k >> 1][k & 1];
+            for (int i = 0; i < pool; i++) maxprime.p[k][row * pool + i] = dr[i][k >> 1][k & 1];
+        }
+    }
+}
+
+template <typename T, typename U> void count_drelu(Ctx *c, size_t n);
+template <typename T, typename U> void count_select(Ctx *c, size_t n);
+
+template <typename T, typename U> static void count_maxpool(Ctx *c, size_t n, int k) {
+    for (int s = 2; s <= k; s *= 2) {
+        size_t pairs = n / s;
+        count_drelu<T, U>(c, pairs);
+        count_select<T, U>(c, pairs);
+        comm_msg(c, n * sizeof(U), n * sizeof(U));  // dresult &= expandedB
+        comm_round(c);
+    }
+}
+
+static unsigned pool_grid(Ctx *c, size_t n) {
+    size_t b = (n + 127) / 128;
+    size_t cap = (size_t)(c->sm_count > 0 ? c->sm_count : 148) * 16;
+    if (b > cap) b = cap;
+    return (unsigned)(b ? b : 1);
+}
+
+template <typename T, typename U>
+int rss_maxpool(Ctx *c, const T *const in[6], size_t n, int k, T *const out[6], U *const dout[6]) {
+    CSh6<T> a;
+    Sh6<T> o;
+    Sh6<U> d;
+    if (!load6(a, in) || !load6(o, out) || !load6(d, dout)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    if (k != 4 && k != 16) return set_error(c, PG_ERR_UNSUPPORTED, "maxpool: k=%d (supported: 4, 16)", k);
+    if (n % k) return set_error(c, PG_ERR_SIZE, "maxpool: n=%zu not a multiple of k=%d", n, k);
+    size_t rows = n / k;
+    if (rows == 0) return PG_OK;
+    if (k == 4) maxpool_rows_kernel<T, U, 4><<<pool_grid(c, rows), 128, 0, c->stream>>>(a, rows, o, d);
+    else maxpool_rows_kernel<T, U, 16><<<pool_grid(c, rows), 128, 0, c->stream>>>(a, rows, o, d);
+    c->launches++;
+    int st = launch_status(c, "maxpool_rows_kernel");
+    if (st) return st;
+    count_maxpool<T, U>(c, n, k);
+    return PG_OK;
+}
+
+template <typename T, typename U>
+int rss_maxpool_layer(Ctx *c, const T *const in[6], T *const out[6], U *const maxprime[6], int H, int W, int C,
+                      int pool, int stride, int batch, int fp) {
+    CSh6<T> a;
+    Sh6<T> o;
+    Sh6<U> d;
+    if (!load6(a, in) || !load6(o, out) || !load6(d, maxprime)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    if (H <= 0 || W <= 0 || C <= 0 || pool <= 0 || stride <= 0 || batch <= 0 || pool > H || pool > W)
+        return set_error(c, PG_ERR_SIZE, "maxpool layer: bad geometry");
+    // padded pool size pow(ceil(log2(pool^2)), 2) (MaxpoolLayer.cu:69)
+    int l2 = 0;
+    while ((1 << l2) < pool * pool) l2++;
+    int padded = l2 * l2;
+    if (padded != 4 && padded != 16)
+        return set_error(c, PG_ERR_UNSUPPORTED, "maxpool layer: pool %d pads to %d (supported: 4, 16)", pool, padded);
+    PoolGeom g;
+    g.H = H; g.W = W; g.C = C; g.f = pool; g.stride = stride; g.batch = batch;
+    g.wK = (W - pool) / stride + 1;
+    g.hK = (H - pool) / stride + 1;
+    g.pad_val = (uint64_t)(T)(int64_t)(-10 * (1 << fp));
+    size_t rows = (size_t)batch * g.wK * g.hK * C;
+    if (padded == 4) maxpool_layer_kernel<T, U, 4><<<pool_grid(c, rows), 128, 0, c->stream>>>(a, g, rows, o, d);
+    else maxpool_layer_kernel<T, U, 16><<<pool_grid(c, rows), 128, 0, c->stream>>>(a, g, rows, o, d);
+    c->launches++;
+    int st = launch_status(c, "maxpool_layer_kernel");
+    if (st) return st;
+    count_maxpool<T, U>(c, rows * padded, padded);
+    return PG_OK;
+}
+
+template int rss_maxpool<uint64_t, uint8_t>(Ctx *, const uint64_t *const *, size_t, int, uint64_t *const *,
+                                            uint8_t *const *);
+template int rss_maxpool<uint64_t, uint64_t>(Ctx *, const uint64_t *const *, size_t, int, uint64_t *const *,
+                                             uint64_t *const *);
+template int rss_maxpool_layer<uint64_t, uint8_t>(Ctx *, const uint64_t *const *, uint64_t *const *,
+                                                  uint8_t *const *, int, int, int, int, int, int, int);
+
+}  // namespace pg

@@ -1,0 +1,117 @@
+"""Network-level parity: the GPU executor against the oracle, layer by layer, bit for bit."""
+import numpy as np
+import pytest
+
+import oracle as orc
+from tests import netref
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pg():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import piranha_gb300 as pg
+
+    pg.lib()
+    return pg
+
+
+def _wrap_device(ptr, n):
+    """A torch view of n int64 elements of existing device memory."""
+    import torch
+
+    class _A:
+        __cuda_array_interface__ = {"shape": (n,), "typestr": "<i8", "data": (ptr, False), "version": 3}
+
+    return torch.as_tensor(_A(), device="cuda")
+
+
+def run_net(pg, layers, params, x, batch, capture=False, form=0):
+    ctx = pg.Context(0, form=form)
+    net = pg.Network(ctx, layers, batch)
+    for i, prm in enumerate(params):
+        if prm is not None:
+            net.set_params(i, pg.to_device(prm[0]), pg.to_device(prm[1]) if prm[1] is not None else None)
+    if capture:
+        net.capture()
+        # the network's input buffers are one contiguous [6][n] block
+        ptrs = net.input_buffers()
+        dst = _wrap_device(ptrs[0], 6 * net.in_n)
+        dst.copy_(pg.to_device(x).reshape(-1))
+        import torch
+
+        torch.cuda.synchronize()
+        net.forward_resident()
+        ctx.sync()
+        optrs, n = net.layer_output_ptrs(len(layers) - 1)
+        res = gather(pg, optrs, n)
+    else:
+        out = pg.empty_shares(net.out_n)
+        net.forward(pg.to_device(x), out)
+        ctx.sync()
+        res = pg.to_host(out)
+    outs = []
+    for i in range(len(layers)):
+        optrs, n = net.layer_output_ptrs(i)
+        outs.append(gather(pg, optrs, n))
+    comm = ctx.comm()
+    net.close()
+    ctx.close()
+    return res, outs, comm
+
+
+def gather(pg, ptrs, n):
+    out = np.empty((3, 2, n), dtype=np.uint64)
+    for k, ptr in enumerate(ptrs):
+        t = _wrap_device(ptr, n)
+        out[k // 2, k % 2] = t.cpu().numpy().view(np.uint64)
+    return out
+
+
+def test_secureml_fixture_forward(pg, golden):
+    L = golden[1]
+    layers = netref.secureml_layers()
+    params = []
+    for li in (0, 2, 4):
+        params.append((orc.set_public(L[f"secureml_weight{li}"]), orc.set_public(L[f"secureml_bias{li}"])))
+        params.append(None)
+    x = orc.set_public(L["secureml_input"])
+    comm = orc.Comm()
+    want, want_outs = netref.forward(layers, params, x, 128, comm=comm, keep=True)
+    got, got_outs, gcomm = run_net(pg, layers, params, x, 128)
+    for i, (g, w) in enumerate(zip(got_outs, want_outs)):
+        assert np.array_equal(g, w), f"layer {i}"
+    assert np.array_equal(got, want)
+    # the reference's own fixture values, decoded at party A (eps 1e-3)
+    for i, o in enumerate(got_outs):
+        rec = orc.reconstruct(o)[0]
+        assert np.max(np.abs(orc.decode(rec) - L[f"secureml_output{i}"])) <= 1e-3
+    assert gcomm["tx"] == comm.tx and gcomm["rounds"] == comm.rounds
+
+
+def test_lenet_forward_random_shares(pg):
+    layers = netref.lenet_layers()
+    params = netref.kaiming_uniform_params(layers, 7)
+    batch = 4
+    rng = np.random.default_rng(8)
+    x = orc.share_random(orc.encode(rng.uniform(0, 1, batch * 784)), seed=9)
+    want, want_outs = netref.forward(layers, params, x, batch, keep=True)
+    got, got_outs, _ = run_net(pg, layers, params, x, batch)
+    for i, (g, w) in enumerate(zip(got_outs, want_outs)):
+        assert np.array_equal(g, w), f"layer {i} {layers[i]}"
+
+
+def test_vgg16_forward_batch2(pg):
+    layers = netref.vgg16_layers()
+    params = netref.kaiming_uniform_params(layers, 11)
+    batch = 2
+    rng = np.random.default_rng(12)
+    x = orc.share_random(orc.encode(rng.uniform(0, 1, batch * 3072)), seed=13)
+    want = netref.forward(layers, params, x, batch)
+    got, got_outs, _ = run_net(pg, layers, params, x, batch)
+    assert np.array_equal(got, want)
+    got2, _, _ = run_net(pg, layers, params, x, batch, capture=True)
+    assert np.array_equal(got2, want)
