@@ -194,6 +194,11 @@ int pg_net_capture(pg_net *net);
  * pg_net_input_shares), replaying the captured graph when there is one */
 int pg_net_forward_resident(pg_net *net);
 int pg_net_input_shares(pg_net *net, uint64_t *out[6]);
+/* per-layer CUDA-event timing (events are recorded into a captured graph
+ * too); pg_net_layer_times gives each layer's milliseconds of the last
+ * completed forward */
+int pg_net_enable_timing(pg_net *net, int on);
+int pg_net_layer_times(pg_net *net, float *ms);
 /* device pointers (owned by the network) of layer i's output shares */
 int pg_net_layer_output(pg_net *net, int layer, uint64_t *const out[6], size_t *n);
 

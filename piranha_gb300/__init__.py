@@ -94,6 +94,8 @@ def _declare(lib):
         "pg_net_capture": [vp],
         "pg_net_input_shares": [vp, _P6],
         "pg_net_layer_output": [vp, i, _P6, ctypes.POINTER(sz)],
+        "pg_net_enable_timing": [vp, i],
+        "pg_net_layer_times": [vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -450,6 +452,14 @@ class Network:
 
     def forward_host(self, in_host_ptr: int, out_host_ptr: int):
         self.ctx._check(lib().pg_net_forward_host(self._h, ctypes.c_void_p(in_host_ptr), ctypes.c_void_p(out_host_ptr)))
+
+    def enable_timing(self, on: bool = True):
+        self.ctx._check(lib().pg_net_enable_timing(self._h, int(on)))
+
+    def layer_times_ms(self):
+        buf = (ctypes.c_float * len(self.layers))()
+        self.ctx._check(lib().pg_net_layer_times(self._h, buf))
+        return list(buf)
 
     def layer_output_ptrs(self, layer: int):
         arr = _P6()

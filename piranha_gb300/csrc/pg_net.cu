@@ -47,13 +47,16 @@ struct pg_net {
     cudaGraphExec_t exec = nullptr;
     uint64_t comm_per_fwd[9] = {0};  // accounting of one forward, replayed with the graph
     uint64_t launches_per_fwd = 0;
+    std::vector<cudaEvent_t> ev;  // 2 per layer when per-layer timing is on (recorded into graphs too)
 };
 
 static int net_run(pg_net *net, const uint64_t *const in[6]) {
     Ctx *c = net->ctx;
     const uint64_t *const *cur = in;
-    for (auto &L : net->layers) {
+    for (size_t li = 0; li < net->layers.size(); li++) {
+        NetLayer &L = net->layers[li];
         int st = PG_OK;
+        if (!net->ev.empty()) cudaEventRecordWithFlags(net->ev[2 * li], c->stream, cudaEventRecordExternal);
         switch (L.type) {
             case PG_LAYER_FC: {
                 const uint64_t *const *bias = L.b_n ? (const uint64_t *const *)L.b : nullptr;
@@ -79,6 +82,7 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
             default: st = set_error(c, PG_ERR_INVALID_ARG, "bad layer type %d", L.type);
         }
         if (st) return st;
+        if (!net->ev.empty()) cudaEventRecordWithFlags(net->ev[2 * li + 1], c->stream, cudaEventRecordExternal);
         cur = L.out;
     }
     return PG_OK;
@@ -175,6 +179,7 @@ int pg_net_create(pg_ctx *c, pg_net **out, const int *spec, int nlayers, int bat
 
 int pg_net_destroy(pg_net *net) {
     if (!net) return PG_ERR_INVALID_ARG;
+    for (auto e : net->ev) cudaEventDestroy(e);
     if (net->exec) cudaGraphExecDestroy(net->exec);
     if (net->graph) cudaGraphDestroy(net->graph);
     if (net->arena) {
@@ -293,6 +298,26 @@ int pg_net_forward_resident(pg_net *net) {
 int pg_net_input_shares(pg_net *net, uint64_t *out[6]) {
     if (!net || !out) return PG_ERR_INVALID_ARG;
     for (int k = 0; k < 6; k++) out[k] = net->in[k];
+    return PG_OK;
+}
+
+int pg_net_enable_timing(pg_net *net, int on) {
+    if (!net) return PG_ERR_INVALID_ARG;
+    if (net->exec) return set_error(net->ctx, PG_ERR_INVALID_ARG, "enable timing before capturing the graph");
+    for (auto e : net->ev) cudaEventDestroy(e);
+    net->ev.clear();
+    if (on) {
+        net->ev.resize(2 * net->layers.size());
+        for (auto &e : net->ev) PG_CHECK_CUDA(net->ctx, cudaEventCreate(&e));
+    }
+    return PG_OK;
+}
+
+int pg_net_layer_times(pg_net *net, float *ms) {
+    if (!net || !ms) return PG_ERR_INVALID_ARG;
+    if (net->ev.empty()) return set_error(net->ctx, PG_ERR_INVALID_ARG, "per-layer timing is off");
+    for (size_t i = 0; i < net->layers.size(); i++)
+        PG_CHECK_CUDA(net->ctx, cudaEventElapsedTime(&ms[i], net->ev[2 * i], net->ev[2 * i + 1]));
     return PG_OK;
 }
 
