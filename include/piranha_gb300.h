@@ -67,6 +67,12 @@ int pg_comm_get(pg_ctx *ctx, uint64_t out[9]);
 int pg_comm_reset(pg_ctx *ctx);
 /* number of kernels this library launched through ctx (all streams) */
 uint64_t pg_kernel_launches(pg_ctx *ctx);
+/* synchronize, then report (and clear) the device error word that bounded
+ * device-side waits set when they give up: PG_ERR_TIMEOUT with *code != 0 */
+int pg_device_errors(pg_ctx *ctx, int *code);
+/* diagnostic: one 128x64x16 tcgen05 MMA of fp16 operands (A 128x16 and B
+ * 64x16 row-major halves), D = A * B^T as 128x64 fp32 row-major */
+int pg_tc_selftest(pg_ctx *ctx, const uint16_t *A, const uint16_t *B, float *D);
 
 /* -------------------------------------------- single-array ring kernels
  * gpu::gemm (src/gpu/gemm.cuh:102-112): C = A*B mod 2^w, A MxK, B KxN, C MxN;

@@ -19,6 +19,7 @@ from __future__ import annotations
 import ctypes
 import os
 import threading
+import weakref
 
 import numpy as np
 
@@ -95,6 +96,8 @@ def _declare(lib):
         "pg_net_input_shares": [vp, _P6],
         "pg_net_layer_output": [vp, i, _P6, ctypes.POINTER(sz)],
         "pg_net_enable_timing": [vp, i],
+        "pg_device_errors": [vp, ctypes.POINTER(i)],
+        "pg_tc_selftest": [vp, vp, vp, vp],
         "pg_net_layer_times": [vp, vp],
     }
     for name, args in sig.items():
@@ -138,6 +141,7 @@ class Context:
 
         self.torch = torch
         self.device = device
+        self._children = weakref.WeakSet()  # networks created on this context
         torch.cuda.set_device(device)
         self._h = ctypes.c_void_p()
         self._check(lib().pg_ctx_create(ctypes.byref(self._h), device))
@@ -174,11 +178,18 @@ class Context:
     def reset_comm(self):
         self._check(lib().pg_comm_reset(self._h))
 
+    def check_device_errors(self):
+        """Synchronize and raise if a bounded device-side wait gave up."""
+        code = ctypes.c_int(0)
+        self._check(lib().pg_device_errors(self._h, ctypes.byref(code)))
+
     def kernel_launches(self) -> int:
         return int(lib().pg_kernel_launches(self._h))
 
     def close(self):
         if getattr(self, "_h", None):
+            for child in list(self._children):
+                child.close()
             self.stream.synchronize()
             lib().pg_ctx_destroy(self._h)
             self._h = None
@@ -428,6 +439,7 @@ class Network:
         self._h = ctypes.c_void_p()
         ctx._check(lib().pg_net_create(ctx.handle, ctypes.byref(self._h), spec.ctypes.data_as(ctypes.c_void_p),
                                        len(self.layers), batch, fp))
+        ctx._children.add(self)
         self.in_n = int(lib().pg_net_input_size(self._h))
         self.out_n = int(lib().pg_net_output_size(self._h))
 
@@ -468,10 +480,11 @@ class Network:
         return [int(x) for x in arr], int(n.value)
 
     def close(self):
-        if getattr(self, "_h", None):
+        # a network must be destroyed before its context (Context.close does this first)
+        if getattr(self, "_h", None) and getattr(self.ctx, "_h", None):
             self.ctx.stream.synchronize()
             lib().pg_net_destroy(self._h)
-            self._h = None
+        self._h = None
 
     def __del__(self):
         try:

@@ -28,6 +28,8 @@ int launch_status(Ctx *c, const char *what) {
     return PG_OK;
 }
 
+int *device_error_word(Ctx *c) { return c->dev_err; }
+
 void *scratch(Ctx *c, size_t bytes) {
     if (bytes <= c->scratch_bytes) return c->scratch;
     if (c->scratch) {
@@ -76,6 +78,7 @@ int limb_rss_matmul_u64(Ctx *, const uint64_t *const *, const uint64_t *const *,
                         const uint64_t *const *, int, int, int, int, int, int, int);
 int limb_rss_conv_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *, int, int, int, int,
                       int, int, int, int, int, int);
+int limb_selftest(Ctx *, const uint16_t *, const uint16_t *, float *);
 
 }  // namespace pg
 
@@ -98,16 +101,20 @@ int pg_ctx_create(pg_ctx **out, int device) {
     pg_ctx *c = new pg_ctx();
     c->device = device;
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (cudaMalloc(&c->dev_err, 256) != cudaSuccess || cudaMemset(c->dev_err, 0, 256) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return PG_ERR_CUDA;
+    }
     *out = c;
     return PG_OK;
 }
 
 int pg_ctx_destroy(pg_ctx *c) {
     CTX_OR_FAIL(c);
-    if (c->scratch) {
-        cudaStreamSynchronize(c->stream);
-        cudaFree(c->scratch);
-    }
+    cudaStreamSynchronize(c->stream);
+    if (c->scratch) cudaFree(c->scratch);
+    if (c->dev_err) cudaFree(c->dev_err);
     delete c;
     return PG_OK;
 }
@@ -143,6 +150,20 @@ int pg_comm_reset(pg_ctx *c) {
     return PG_OK;
 }
 uint64_t pg_kernel_launches(pg_ctx *c) { return c ? c->launches.load() : 0; }
+
+int pg_device_errors(pg_ctx *c, int *out) {
+    CTX_OR_FAIL(c);
+    if (!out) return PG_ERR_INVALID_ARG;
+    PG_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    PG_CHECK_CUDA(c, cudaMemcpy(out, c->dev_err, sizeof(int), cudaMemcpyDeviceToHost));
+    PG_CHECK_CUDA(c, cudaMemset(c->dev_err, 0, sizeof(int)));
+    return *out ? set_error(c, PG_ERR_TIMEOUT, "device wait timed out (code 0x%x)", *out) : PG_OK;
+}
+
+int pg_tc_selftest(pg_ctx *c, const uint16_t *A, const uint16_t *B, float *D) {
+    CTX_OR_FAIL(c);
+    return limb_selftest(c, A, B, D);
+}
 
 int pg_gemm_u64(pg_ctx *c, int M, int N, int K, const uint64_t *A, int tA, const uint64_t *B, int tB, uint64_t *C,
                 int tC) {

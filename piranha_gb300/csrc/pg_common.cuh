@@ -29,6 +29,7 @@ struct Ctx {
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
     int sm_count = 0;
+    int *dev_err = nullptr;  // device word that bounded waits set on timeout
 };
 
 int set_error(Ctx *c, int code, const char *fmt, ...);

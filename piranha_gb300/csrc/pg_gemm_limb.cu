@@ -1,13 +1,631 @@
-// pg_gemm_limb.cu — placeholder for the limb tensor-core form.
+// pg_gemm_limb.cu — the 8-bit-limb tensor-core form of the RSS share-GEMM and
+// implicit-GEMM convolution (tcgen05, fp16 operands, fp32 accumulators in
+// tensor memory), exact modulo 2^64.
+//
+// Arithmetic. Every 64-bit operand v is written as eight signed digits
+// d_i = byte_i(v) - 128 in [-128, 127], so v = sum_i d_i 2^(8i) + C with
+// C = 0x8080808080808080 (mod 2^64). A digit is exact in fp16 and a digit
+// product has magnitude <= 2^14. For a contraction over K' terms
+//   sum a*b = sum_s 2^(8s) D_s + C*(sum a) + C*(sum b) - K'*C^2   (mod 2^64)
+// with D_s = sum_{i+j=s} sum_k d_i(a_k) d_j(b_k) for the 36 digit pairs with
+// i+j < 8 (pairs with i+j >= 8 vanish mod 2^64). One tcgen05.mma per pair and
+// K step of 16 accumulates D_s in fp32 tensor memory; an accumulator holds at
+// most (s+1)*128 products per chunk of 128 K' terms, so |D_s| <= 2^24 and
+// every fp32 sum is an exact integer. After each chunk the epilogue warps move
+// the eight accumulators into 64-bit registers. The row sums of A and column
+// sums of B are accumulated by the producer warps while they convert tiles.
+//
+// Protocol. The K' dimension is the concatenation of the six RSS segments
+// [x_p0 | x_p1] x [y_p0 + y_p1 ; y_p0] of the three parties (localMatMul,
+// src/mpc/RSS.inl:1097-1110; localFprop :614-639), so Z = sum_p z_p, which
+// the epilogue truncates with dividePublic3out3 (:1077-1094).
+//
+// Roles (384 threads): warps 0-2 load u64 tiles (implicit im2col for conv),
+// convert them to limb planes in the UMMA core-matrix layout and accumulate
+// row/column sums; warp 3 owns the tensor memory and one lane issues the
+// MMAs; warps 4-11 drain tensor memory (two warps per 32-lane quarter, 32
+// columns each) and run the epilogue. Every mbarrier wait is
+// bounded; on a timeout the kernel records an error word, stops issuing work,
+// waits for its own MMAs and frees tensor memory before returning.
+#include <cuda_fp16.h>
+
+#include <cstring>
+
 #include "pg_common.cuh"
+#include "pg_tcgen05.cuh"
 
 namespace pg {
-int limb_rss_matmul_u64(Ctx *c, const uint64_t *const *, const uint64_t *const *, uint64_t *const *,
-                        const uint64_t *const *, int, int, int, int, int, int, int) {
-    return set_error(c, PG_ERR_UNSUPPORTED, "limb tensor-core form not built");
+
+namespace limb {
+
+constexpr int BM = 128, BN = 64, BK = 16, STAGES = 4, CHUNK_STAGES = 8;  // 8 stages = 128 K' per chunk
+constexpr int A_LIMB_BYTES = BM * BK * 2;                               // 4096
+constexpr int B_LIMB_BYTES = BN * BK * 2;                               // 2048
+constexpr int STAGE_BYTES = 8 * (A_LIMB_BYTES + B_LIMB_BYTES);          // 49152
+constexpr int NTHREADS = 384;  // 12 warps: 0-2 producers, 3 MMA, 4-11 epilogue
+constexpr int NPRODUCERS = 96;
+constexpr uint32_t TMEM_COLS = 512;  // 8 diagonals x 64 columns
+constexpr uint64_t CDIG = 0x8080808080808080ull;
+constexpr uint64_t WAIT_NS = 2000000000ull;  // 2 s bound on any single wait
+
+enum { KIND_GEMM = 0, KIND_FPROP = 1 };
+
+struct FastDivL {
+    uint32_t d, m;
+    int s;
+    __host__ void init(uint32_t dd) {
+        d = dd;
+        if (dd <= 1) { m = 0; s = 0; return; }
+        s = 0;
+        while ((1ull << s) < dd) s++;
+        m = (uint32_t)((((1ull << 32) * ((1ull << s) - dd)) / dd) + 1);
+    }
+    __device__ __forceinline__ uint32_t div(uint32_t x) const {
+        if (d == 1) return x;
+        uint32_t hi = __umulhi(x, m);
+        return (hi + ((x - hi) >> 1)) >> (s - 1);
+    }
+};
+
+struct Args {
+    int M, N, Kseg, nseg;
+    const uint64_t *a[6];
+    const uint64_t *b0[6];
+    const uint64_t *b1[6];
+    int kind, tA, tB;
+    // conv fprop geometry
+    int ch, cw, cc, cs, cp, cq, pad, stride;
+    FastDivL dQ, dP, dC, dS;
+    // K' split: chunks [z*chunks_per_split, ...) of the total
+    int total_stages, chunks_per_split;
+    // epilogue
+    int direct;           // 1: RSS epilogue here; 0: write the slice's Z to partial
+    uint64_t *partial;    // [gridDim.z][M][N]
+    uint64_t *out[6];
+    const uint64_t *bias[6];
+    int tC;
+    uint64_t d;
+    int dshift;
+    int *err;
+};
+
+struct __align__(8) Smem {
+    uint8_t stage[STAGES][STAGE_BYTES];
+    Args args;  // kernel arguments, copied here so that dynamic indexing stays out of local memory
+    uint64_t full[STAGES], empty[STAGES], acc_full, acc_empty, done;
+    uint64_t rowsum[BM], colsum[BN];
+    uint32_t tmem_base;
+    int abort;
+};
+
+// ---------------------------------------------------------------- loaders
+
+// 8 consecutive K' values of row m of A (K' offset k of segment seg)
+__device__ __forceinline__ void load_a8(const Args &g, int seg, int m, int k, uint64_t (&v)[8]) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) v[i] = 0;
+    if (m >= g.M) return;
+    const uint64_t *a = g.a[seg];
+    if (g.kind == KIND_FPROP) {
+        uint32_t nq = g.dQ.div(m), q = m - nq * g.cq;
+        uint32_t n = g.dP.div(nq), p = nq - n * g.cp;
+        uint32_t rs = g.dC.div(k), c = k - rs * g.cc;
+        uint32_t r = g.dS.div(rs), s = rs - r * g.cs;
+        int h = (int)(p * g.stride) - g.pad + (int)r, w = (int)(q * g.stride) - g.pad + (int)s;
+        if (h < 0 || h >= g.ch || w < 0 || w >= g.cw) return;
+        const ulonglong2 *src = (const ulonglong2 *)(a + ((((size_t)n * g.ch + h) * g.cw + w) * g.cc + c));
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            ulonglong2 t = __ldg(src + i);
+            v[2 * i] = t.x;
+            v[2 * i + 1] = t.y;
+        }
+    } else if (g.tA) {
+        const ulonglong2 *src = (const ulonglong2 *)(a + (size_t)m * g.Kseg + k);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            ulonglong2 t = __ldg(src + i);
+            v[2 * i] = t.x;
+            v[2 * i + 1] = t.y;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 8; i++) v[i] = __ldg(a + (size_t)m + (size_t)(k + i) * g.M);
+    }
 }
-int limb_rss_conv_u64(Ctx *c, const uint64_t *const *, const uint64_t *const *, uint64_t *const *, int, int, int, int,
-                      int, int, int, int, int, int) {
-    return set_error(c, PG_ERR_UNSUPPORTED, "limb tensor-core form not built");
+
+// 8 consecutive K' values of column n of B (b0 + b1 when b1 is given)
+__device__ __forceinline__ void load_b8_one(const Args &g, const uint64_t *b, int n, int k, uint64_t (&v)[8]) {
+    if (g.kind == KIND_FPROP || !g.tB) {
+        const ulonglong2 *src = (const ulonglong2 *)(b + (size_t)n * g.Kseg + k);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            ulonglong2 t = __ldg(src + i);
+            v[2 * i] = t.x;
+            v[2 * i + 1] = t.y;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 8; i++) v[i] = __ldg(b + (size_t)(k + i) * g.N + n);
+    }
 }
+
+__device__ __forceinline__ void load_b8(const Args &g, int seg, int n, int k, uint64_t (&v)[8]) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) v[i] = 0;
+    if (n >= g.N) return;
+    load_b8_one(g, g.b0[seg], n, k, v);
+    if (g.b1[seg]) {
+        uint64_t w[8];
+        load_b8_one(g, g.b1[seg], n, k, w);
+#pragma unroll
+        for (int i = 0; i < 8; i++) v[i] += w[i];
+    }
+}
+
+// byte i of each of v[k], v[k+1] as fp16 (byte - 128), packed in one half2 word
+__device__ __forceinline__ uint32_t digit_pair(uint32_t wk, uint32_t wk1, uint32_t sel) {
+    uint32_t d;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(wk), "r"(wk1), "r"(sel));
+    d = (d & 0x00FF00FFu) | 0x64006400u;  // fp16 1024 + byte
+    __half2 h = *reinterpret_cast<__half2 *>(&d);
+    h = __hsub2(h, __halves2half2(__ushort_as_half(0x6480), __ushort_as_half(0x6480)));  // - 1152
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+// Convert 8 u64 values (consecutive K' of one row) into the 8 limb planes:
+// limb i goes to plane_base + i*plane_bytes at core-matrix offset off.
+__device__ __forceinline__ void store_limbs(uint8_t *plane_base, int plane_bytes, uint32_t off,
+                                            const uint64_t (&v)[8]) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        uint32_t w[4];
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            uint32_t a = i < 4 ? (uint32_t)v[2 * p] : (uint32_t)(v[2 * p] >> 32);
+            uint32_t b = i < 4 ? (uint32_t)v[2 * p + 1] : (uint32_t)(v[2 * p + 1] >> 32);
+            // prmt selector: d.byte0 = a.byte(i&3), d.byte2 = b.byte(i&3) (bytes 1, 3 masked off)
+            const uint32_t sel = (uint32_t)(i & 3) | ((uint32_t)(i & 3) << 4) | ((uint32_t)(4 + (i & 3)) << 8) |
+                                 ((uint32_t)(4 + (i & 3)) << 12);
+            w[p] = digit_pair(a, b, sel);
+        }
+        uint4 q = make_uint4(w[0], w[1], w[2], w[3]);
+        *reinterpret_cast<uint4 *>(plane_base + i * plane_bytes + off) = q;
+    }
+}
+
+// core-matrix offset of (row, 8-element chunk kc) inside a limb plane
+__device__ __forceinline__ uint32_t cm_off(int row, int kc) {
+    return (uint32_t)((row >> 3) * 256 + kc * 128 + (row & 7) * 16);
+}
+
+__device__ __forceinline__ void flag_error(Smem &sm, const Args &g, int code) {
+    sm.abort = 1;
+    if (g.err) atomicCAS(g.err, 0, code);
+}
+
+// Move the eight diagonal accumulators of 32 columns (col0..col0+31) of this
+// thread's TMEM lane into the 64-bit running sums. Diagonals 0-3 are added as
+// sign-extended 64-bit values shifted by 8s; diagonals 4-7 only matter modulo
+// 2^32 (they are shifted by >= 32), so they are combined in 32-bit registers.
+__device__ __forceinline__ void drain32(uint32_t taddr, uint64_t (&run)[32]) {
+#pragma unroll
+    for (int d = 0; d < 8; d++) {
+        uint32_t r[32];
+        tc::tmem_ld32(taddr + (uint32_t)(d * BN), r);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            int v = __float2int_rz(__uint_as_float(r[j]));  // exact: |v| <= 2^24
+            if (d < 4) run[j] += (uint64_t)(int64_t)v << (8 * d);
+            else run[j] += (uint64_t)((uint32_t)v << (8 * (d - 4))) << 32;  // needed mod 2^32 only
+        }
+    }
+}
+
+// Final epilogue for 32 columns of one row: add the digit-offset correction,
+// then either store the slice's partial Z or apply dividePublic3out3 and
+// write the six output shares (+ bias shares).
+__device__ __forceinline__ void finish32(const Args &g, const Smem &sm, int z, int m, int row, int nbase, int cbase,
+                                         uint64_t kc2, uint64_t (&run)[32]) {
+    const uint64_t rs = sm.rowsum[row];
+#pragma unroll
+    for (int j = 0; j < 32; j++) run[j] += CDIG * (rs + sm.colsum[cbase + j]) - kc2;
+    const int ncols = g.N - nbase < 32 ? g.N - nbase : 32;
+    if (!g.direct) {
+        uint64_t *dst = g.partial + ((size_t)z * g.M + m) * g.N + nbase;
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+            if (j < ncols) dst[j] = run[j];
+        return;
+    }
+#pragma unroll
+    for (int j = 0; j < 32; j++) run[j] = 1 + div_public<uint64_t>(run[j] - g.d, g.d, g.dshift);
+    const bool colmajor = (g.kind == KIND_GEMM && !g.tC);
+#pragma unroll 1
+    for (int ps = 0; ps < 6; ps++) {
+        uint64_t *o = g.out[ps];
+        const uint64_t *b = g.bias[ps];
+        const bool val = (ps == 0 || ps == 5);
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            if (j < ncols) {
+                const int n = nbase + j;
+                uint64_t base = val ? run[j] : 0;
+                if (b) base += b[n];
+                o[colmajor ? (size_t)m + (size_t)n * g.M : (size_t)m * g.N + n] = base;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ kernel
+
+__global__ void __launch_bounds__(NTHREADS, 1) limb_gemm_kernel(const __grid_constant__ Args gp) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    Smem &sm = *reinterpret_cast<Smem *>(smem_raw);
+    {
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(&gp);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(&sm.args);
+        for (int i = threadIdx.x; i < (int)(sizeof(Args) / 4); i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const Args &g = sm.args;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const int z = blockIdx.z;
+    const int stage_begin = z * g.chunks_per_split * CHUNK_STAGES;
+    int stage_end = stage_begin + g.chunks_per_split * CHUNK_STAGES;
+    if (stage_end > g.total_stages) stage_end = g.total_stages;
+    const int nst = stage_end > stage_begin ? stage_end - stage_begin : 0;
+    const int nchunks = (nst + CHUNK_STAGES - 1) / CHUNK_STAGES;
+    const int stages_per_seg = g.Kseg / BK;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            tc::mbar_init(tc::smem_u32(&sm.full[s]), NPRODUCERS);
+            tc::mbar_init(tc::smem_u32(&sm.empty[s]), 1);
+        }
+        tc::mbar_init(tc::smem_u32(&sm.acc_full), 1);
+        tc::mbar_init(tc::smem_u32(&sm.acc_empty), 256);
+        tc::mbar_init(tc::smem_u32(&sm.done), 1);
+        sm.abort = 0;
+        tc::fence_mbar_init();
+    }
+    for (int i = threadIdx.x; i < BM + BN; i += blockDim.x) {
+        if (i < BM) sm.rowsum[i] = 0;
+        else sm.colsum[i - BM] = 0;
+    }
+    if (warp == 3) {
+        tc::tmem_alloc(tc::smem_u32(&sm.tmem_base), TMEM_COLS);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = sm.tmem_base;
+
+    if (warp < 3) {
+        // ------------------------------------------------------- producers
+        // units of 8 consecutive K' values per stage: A rows 0..127 x 2, then B rows 0..63 x 2
+        const int t = threadIdx.x;
+        for (int it = 0; it < nst; it++) {
+            const int s = it % STAGES;
+            const uint32_t ph = (uint32_t)(it / STAGES) & 1;
+            if (!tc::mbar_wait(tc::smem_u32(&sm.empty[s]), ph ^ 1, &sm.abort, WAIT_NS)) {
+                flag_error(sm, g, 0x100 + s);
+                break;
+            }
+            const int gst = stage_begin + it;
+            const int seg = gst / stages_per_seg;
+            const int k = (gst - seg * stages_per_seg) * BK;
+            uint8_t *stA = sm.stage[s];
+            uint8_t *stB = sm.stage[s] + 8 * A_LIMB_BYTES;
+#pragma unroll 1
+            for (int u4 = 0; u4 < 4; u4++) {
+                const int u = t + u4 * NPRODUCERS;
+                uint64_t v[8];
+                uint64_t sum = 0;
+                if (u < 2 * BM) {
+                    const int row = u >> 1, kc = u & 1;
+                    load_a8(g, seg, m0 + row, k + kc * 8, v);
+#pragma unroll
+                    for (int i = 0; i < 8; i++) sum += v[i];
+                    store_limbs(stA, A_LIMB_BYTES, cm_off(row, kc), v);
+                    atomicAdd((unsigned long long *)&sm.rowsum[row], (unsigned long long)sum);
+                } else {
+                    const int row = (u - 2 * BM) >> 1, kc = u & 1;
+                    load_b8(g, seg, n0 + row, k + kc * 8, v);
+#pragma unroll
+                    for (int i = 0; i < 8; i++) sum += v[i];
+                    store_limbs(stB, B_LIMB_BYTES, cm_off(row, kc), v);
+                    atomicAdd((unsigned long long *)&sm.colsum[row], (unsigned long long)sum);
+                }
+            }
+            tc::fence_proxy_async_smem();
+            tc::mbar_arrive(tc::smem_u32(&sm.full[s]));
+        }
+        asm volatile("bar.sync 1, 352;" ::: "memory");  // producers + epilogue
+    } else if (warp == 3) {
+        // ------------------------------------------------------------- MMA
+        if (lane == 0) {
+            const uint32_t idesc = tc::idesc_f16_f32(BM, BN);
+            int it = 0;
+            for (int c = 0; c < nchunks && !sm.abort; c++) {
+                if (c > 0 && !tc::mbar_wait(tc::smem_u32(&sm.acc_empty), (uint32_t)(c - 1) & 1, &sm.abort, WAIT_NS)) {
+                    flag_error(sm, g, 0x200);
+                    break;
+                }
+                tc::tc_fence_after();
+                const int cst = (nst - c * CHUNK_STAGES) < CHUNK_STAGES ? nst - c * CHUNK_STAGES : CHUNK_STAGES;
+                bool ok = true;
+                for (int st = 0; st < cst; st++, it++) {
+                    const int s = it % STAGES;
+                    const uint32_t ph = (uint32_t)(it / STAGES) & 1;
+                    if (!tc::mbar_wait(tc::smem_u32(&sm.full[s]), ph, &sm.abort, WAIT_NS)) {
+                        flag_error(sm, g, 0x300 + s);
+                        ok = false;
+                        break;
+                    }
+                    tc::tc_fence_after();
+                    const uint32_t a0 = tc::smem_u32(sm.stage[s]);
+                    const uint32_t b0 = a0 + 8 * A_LIMB_BYTES;
+#pragma unroll
+                    for (int i = 0; i < 8; i++) {
+                        const uint64_t ad = tc::smem_desc(a0 + i * A_LIMB_BYTES, 128, 256);
+#pragma unroll
+                        for (int j = 0; j < 8 - i; j++) {
+                            const uint64_t bd = tc::smem_desc(b0 + j * B_LIMB_BYTES, 128, 256);
+                            tc::mma_f16(tmem + (uint32_t)((i + j) * BN), ad, bd, idesc, (st > 0 || i > 0) ? 1u : 0u);
+                        }
+                    }
+                    tc::mma_commit(tc::smem_u32(&sm.empty[s]));
+                }
+                if (!ok) break;
+                tc::mma_commit(tc::smem_u32(&sm.acc_full));
+            }
+            // all MMAs this thread issued are complete once `done` fires
+            tc::mma_commit(tc::smem_u32(&sm.done));
+            if (!tc::mbar_wait(tc::smem_u32(&sm.done), 0, &sm.abort, WAIT_NS) && g.err) atomicCAS(g.err, 0, 0x400);
+        }
+        __syncwarp();
+    } else {
+        // -------------------------------------------------------- epilogue
+        const int q = warp & 3;               // TMEM lane quarter
+        const int colh = (warp - 4) >> 2;     // which 32 of the 64 columns
+        const int row = q * 32 + lane;        // tile row = TMEM lane
+        uint64_t run[32];
+#pragma unroll
+        for (int j = 0; j < 32; j++) run[j] = 0;
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(colh * 32);
+        for (int c = 0; c < nchunks; c++) {
+            if (!tc::mbar_wait(tc::smem_u32(&sm.acc_full), (uint32_t)c & 1, &sm.abort, WAIT_NS)) {
+                flag_error(sm, g, 0x500);
+                break;
+            }
+            tc::tc_fence_after();
+            drain32(taddr, run);
+            tc::tc_fence_before();
+            tc::mbar_arrive(tc::smem_u32(&sm.acc_empty));
+        }
+        asm volatile("bar.sync 1, 352;" ::: "memory");
+        const int m = m0 + row;
+        if (!sm.abort && m < g.M) {
+            const uint64_t kc2 = (uint64_t)nst * BK * (CDIG * CDIG);
+            finish32(g, sm, z, m, row, n0 + colh * 32, colh * 32, kc2, run);
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 3) {
+        tc::tc_fence_after();
+        tc::tmem_dealloc(tmem, TMEM_COLS);
+    }
+}
+
+// sum the split-K partials and apply dividePublic3out3 (+ bias)
+__global__ void limb_reduce_kernel(const Args g, int nsplit) {
+    size_t total = (size_t)g.M * g.N;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        uint64_t zv = 0;
+        for (int s = 0; s < nsplit; s++) zv += g.partial[(size_t)s * total + e];
+        int m = (int)(e / g.N), n = (int)(e % g.N);
+        size_t idx = (g.kind == KIND_GEMM && !g.tC) ? (size_t)m + (size_t)n * g.M : e;
+        uint64_t vv = 1 + div_public<uint64_t>(zv - g.d, g.d, g.dshift);
+#pragma unroll
+        for (int ps = 0; ps < 6; ps++) {
+            uint64_t base = (ps == 0 || ps == 5) ? vv : 0;
+            if (g.bias[ps]) base += g.bias[ps][n];
+            g.out[ps][idx] = base;
+        }
+    }
+}
+
+// ------------------------------------------------------------- self test
+
+// One 128x64x16 MMA of fp16 integers: D = A * B^T with A, B given K-major
+// (row-major 128x16 and 64x16 halves). Checks descriptors, instruction
+// descriptor and the TMEM lane/column layout against a host reference.
+__global__ void __launch_bounds__(128, 1) selftest_kernel(const uint16_t *A, const uint16_t *B, float *D, int *err) {
+    __shared__ __align__(1024) uint8_t sa[A_LIMB_BYTES];
+    __shared__ __align__(1024) uint8_t sb[B_LIMB_BYTES];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tbase;
+    __shared__ int abort_flag;
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    for (int kc = 0; kc < 2; kc++) {
+        *reinterpret_cast<uint4 *>(sa + cm_off(t, kc)) = *reinterpret_cast<const uint4 *>(A + t * 16 + kc * 8);
+        if (t < 64) *reinterpret_cast<uint4 *>(sb + cm_off(t, kc)) = *reinterpret_cast<const uint4 *>(B + t * 16 + kc * 8);
+    }
+    if (t == 0) {
+        tc::mbar_init(tc::smem_u32(&bar), 1);
+        abort_flag = 0;
+        tc::fence_mbar_init();
+    }
+    tc::fence_proxy_async_smem();
+    if (warp == 0) {
+        tc::tmem_alloc(tc::smem_u32(&tbase), 64);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tm = tbase;
+    if (t == 0) {
+        tc::mma_f16(tm, tc::smem_desc(tc::smem_u32(sa), 128, 256), tc::smem_desc(tc::smem_u32(sb), 128, 256),
+                    tc::idesc_f16_f32(128, 64), 0u);
+        tc::mma_commit(tc::smem_u32(&bar));
+    }
+    __syncwarp();
+    bool ok = tc::mbar_wait(tc::smem_u32(&bar), 0, &abort_flag, WAIT_NS);
+    if (!ok && err) atomicCAS(err, 0, 0x600);
+    tc::tc_fence_after();
+    if (ok) {
+        for (int half = 0; half < 2; half++) {
+            uint32_t r[32];
+            tc::tmem_ld32(tm + ((uint32_t)(warp * 32) << 16) + (uint32_t)(half * 32), r);
+            tc::tmem_wait_ld();
+            for (int j = 0; j < 32; j++) D[(warp * 32 + lane) * 64 + half * 32 + j] = __uint_as_float(r[j]);
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc::tc_fence_after();
+        tc::tmem_dealloc(tm, 64);
+    }
+}
+
+static size_t smem_bytes() { return sizeof(Smem) + 1024; }
+
+}  // namespace limb
+
+int *device_error_word(Ctx *c);
+template <typename T>
+int rss_matmul(Ctx *, const T *const *, const T *const *, T *const *, const T *const *, int, int, int, int, int, int,
+               int);
+template <typename T>
+int rss_conv(Ctx *, const T *const *, const T *const *, T *const *, int, int, int, int, int, int, int, int, int, int);
+
+static int limb_launch(Ctx *c, limb::Args &g, int total_stages) {
+    using namespace limb;
+    static bool attr_set = false;
+    if (!attr_set) {
+        PG_CHECK_CUDA(c, cudaFuncSetAttribute(limb_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem_bytes()));
+        attr_set = true;
+    }
+    const int tiles_m = (g.M + BM - 1) / BM, tiles_n = (g.N + BN - 1) / BN;
+    const int tiles = tiles_m * tiles_n;
+    const int chunks = (total_stages + CHUNK_STAGES - 1) / CHUNK_STAGES;
+    int sms = c->sm_count > 0 ? c->sm_count : 148;
+    int split = tiles >= sms ? 1 : sms / tiles;
+    if (split > chunks) split = chunks;
+    if (split < 1) split = 1;
+    int cps = (chunks + split - 1) / split;
+    split = (chunks + cps - 1) / cps;
+    g.total_stages = total_stages;
+    g.chunks_per_split = cps;
+    g.err = device_error_word(c);
+    if (split > 1) {
+        uint64_t *part = (uint64_t *)scratch(c, (size_t)split * g.M * g.N * 8);
+        if (!part) return PG_ERR_NO_MEMORY;
+        g.partial = part;
+        g.direct = 0;
+    } else {
+        g.direct = 1;
+    }
+    dim3 grid(tiles_n, tiles_m, split);
+    limb_gemm_kernel<<<grid, NTHREADS, smem_bytes(), c->stream>>>(g);
+    c->launches++;
+    int st = launch_status(c, "limb_gemm_kernel");
+    if (st) return st;
+    if (split > 1) {
+        size_t total = (size_t)g.M * g.N;
+        unsigned blocks = (unsigned)((total + 255) / 256);
+        if (blocks > (unsigned)sms * 8) blocks = sms * 8;
+        limb_reduce_kernel<<<blocks, 256, 0, c->stream>>>(g, split);
+        c->launches++;
+        st = launch_status(c, "limb_reduce_kernel");
+        if (st) return st;
+    }
+    return PG_OK;
+}
+
+static void limb_segments(limb::Args &g, const uint64_t *const *a, const uint64_t *const *b) {
+    g.nseg = 6;
+    for (int p = 0; p < 3; p++) {
+        g.a[2 * p] = a[2 * p];
+        g.b0[2 * p] = b[2 * p];
+        g.b1[2 * p] = b[2 * p + 1];
+        g.a[2 * p + 1] = a[2 * p + 1];
+        g.b0[2 * p + 1] = b[2 * p];
+        g.b1[2 * p + 1] = nullptr;
+    }
+}
+
+static bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
+
+int limb_rss_matmul_u64(Ctx *c, const uint64_t *const a[6], const uint64_t *const b[6], uint64_t *const out[6],
+                        const uint64_t *const bias[6], int M, int N, int K, int tA, int tB, int tC, int trunc) {
+    CSh6<uint64_t> ca, cb;
+    Sh6<uint64_t> co;
+    if (!load6(ca, a) || !load6(cb, b) || !load6(co, out)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    if (M <= 0 || N <= 0 || K <= 0) return set_error(c, PG_ERR_SIZE, "matmul: bad sizes");
+    if (trunc < 0 || trunc > 63) return set_error(c, PG_ERR_INVALID_ARG, "bad truncation %d", trunc);
+    bool ok = (K % limb::BK) == 0;
+    for (int i = 0; i < 6 && ok; i++) ok = aligned16(a[i]) && aligned16(b[i]);
+    if (tA && (K % 2)) ok = false;
+    if (!ok)  // shapes the limb tiles do not cover run on the integer CUDA cores
+        return rss_matmul<uint64_t>(c, a, b, out, bias, M, N, K, tA, tB, tC, trunc);
+    limb::Args g;
+    memset(&g, 0, sizeof(g));
+    g.M = M; g.N = N; g.Kseg = K; g.kind = limb::KIND_GEMM; g.tA = tA; g.tB = tB; g.tC = tC;
+    limb_segments(g, a, b);
+    for (int i = 0; i < 6; i++) { g.out[i] = out[i]; g.bias[i] = bias ? bias[i] : nullptr; }
+    g.d = 1ull << trunc;
+    g.dshift = pow2_shift<uint64_t>(g.d);
+    int st = limb_launch(c, g, 6 * K / limb::BK);
+    if (st) return st;
+    comm_msg(c, 2ull * M * N * 8, 2ull * M * N * 8);
+    comm_round(c);
+    return PG_OK;
+}
+
+int limb_rss_conv_u64(Ctx *c, const uint64_t *const A[6], const uint64_t *const B[6], uint64_t *const C[6], int op,
+                      int batch, int H, int W, int f, int Din, int Dout, int stride, int pad, int trunc) {
+    CSh6<uint64_t> ca, cb;
+    Sh6<uint64_t> co;
+    if (!load6(ca, A) || !load6(cb, B) || !load6(co, C)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    bool ok = op == PG_CONV_FPROP && (Din % 16) == 0;
+    for (int i = 0; i < 6 && ok; i++) ok = aligned16(A[i]) && aligned16(B[i]);
+    if (!ok || batch <= 0 || H <= 0 || W <= 0 || f <= 0 || Dout <= 0 || stride <= 0 || pad < 0 || H + 2 * pad < f ||
+        W + 2 * pad < f)
+        return rss_conv<uint64_t>(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc);
+    if (trunc < 0 || trunc > 63) return set_error(c, PG_ERR_INVALID_ARG, "bad truncation %d", trunc);
+    limb::Args g;
+    memset(&g, 0, sizeof(g));
+    int P = (H + 2 * pad - f) / stride + 1, Q = (W + 2 * pad - f) / stride + 1;
+    g.M = batch * P * Q; g.N = Dout; g.Kseg = f * f * Din; g.kind = limb::KIND_FPROP; g.tC = 1;
+    g.ch = H; g.cw = W; g.cc = Din; g.cs = f; g.cp = P; g.cq = Q; g.pad = pad; g.stride = stride;
+    g.dQ.init(Q); g.dP.init(P); g.dC.init(Din); g.dS.init(f);
+    limb_segments(g, A, B);
+    for (int i = 0; i < 6; i++) { g.out[i] = C[i]; g.bias[i] = nullptr; }
+    g.d = 1ull << trunc;
+    g.dshift = pow2_shift<uint64_t>(g.d);
+    int st = limb_launch(c, g, 6 * g.Kseg / limb::BK);
+    if (st) return st;
+    uint64_t n_out = (uint64_t)g.M * g.N;
+    comm_msg(c, 2 * n_out * 8, 2 * n_out * 8);
+    comm_round(c);
+    return PG_OK;
+}
+
+int limb_selftest(Ctx *c, const uint16_t *A, const uint16_t *B, float *D) {
+    if (!A || !B || !D) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+    limb::selftest_kernel<<<1, 128, 0, c->stream>>>(A, B, D, device_error_word(c));
+    c->launches++;
+    return launch_status(c, "selftest_kernel");
+}
+
 }  // namespace pg

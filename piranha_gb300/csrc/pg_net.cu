@@ -50,13 +50,23 @@ struct pg_net {
     std::vector<cudaEvent_t> ev;  // 2 per layer when per-layer timing is on (recorded into graphs too)
 };
 
+// Per-layer timing events: inside a stream capture they must be external
+// event nodes so that graph replays record them; outside, a plain record.
+static int record_event(Ctx *c, cudaEvent_t e) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    PG_CHECK_CUDA(c, cudaStreamIsCapturing(c->stream, &cs));
+    if (cs == cudaStreamCaptureStatusActive) PG_CHECK_CUDA(c, cudaEventRecordWithFlags(e, c->stream, cudaEventRecordExternal));
+    else PG_CHECK_CUDA(c, cudaEventRecord(e, c->stream));
+    return PG_OK;
+}
+
 static int net_run(pg_net *net, const uint64_t *const in[6]) {
     Ctx *c = net->ctx;
     const uint64_t *const *cur = in;
     for (size_t li = 0; li < net->layers.size(); li++) {
         NetLayer &L = net->layers[li];
         int st = PG_OK;
-        if (!net->ev.empty()) cudaEventRecordWithFlags(net->ev[2 * li], c->stream, cudaEventRecordExternal);
+        if (!net->ev.empty() && (st = record_event(c, net->ev[2 * li]))) return st;
         switch (L.type) {
             case PG_LAYER_FC: {
                 const uint64_t *const *bias = L.b_n ? (const uint64_t *const *)L.b : nullptr;
@@ -82,7 +92,7 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
             default: st = set_error(c, PG_ERR_INVALID_ARG, "bad layer type %d", L.type);
         }
         if (st) return st;
-        if (!net->ev.empty()) cudaEventRecordWithFlags(net->ev[2 * li + 1], c->stream, cudaEventRecordExternal);
+        if (!net->ev.empty() && (st = record_event(c, net->ev[2 * li + 1]))) return st;
         cur = L.out;
     }
     return PG_OK;
@@ -232,6 +242,18 @@ int pg_net_capture(pg_net *net) {
     if (net->graph) {
         cudaGraphDestroy(net->graph);
         net->graph = nullptr;
+    }
+    // One eager forward first: it sizes the context scratch (split-K
+    // partials), which cannot be allocated while a stream is capturing.
+    {
+        uint64_t comm_save[9];
+        memcpy(comm_save, c->comm, sizeof(comm_save));
+        uint64_t launches_save = c->launches.load();
+        int st0 = net_run(net, (const uint64_t *const *)net->in);
+        memcpy(c->comm, comm_save, sizeof(comm_save));
+        c->launches = launches_save;
+        if (st0) return st0;
+        PG_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     }
     // Capture on a private stream (the context stream may be the legacy
     // default stream, which cannot be captured); replays go to ctx->stream.

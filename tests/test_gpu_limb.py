@@ -1,0 +1,130 @@
+"""The 8-bit-limb tensor-core form (tcgen05) against the CPU oracle, bit for bit.
+
+Covers the single-MMA self test (descriptor and tensor-memory layout), the
+fused share-GEMM and implicit-GEMM conv at several shapes (including split-K
+and tile-ragged edges), the digit-magnitude worst case (every product at
+2^14, so every fp32 accumulator reaches exactly 2^24 per chunk), and a full
+VGG16 forward in the limb form.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle as orc
+from tests import netref
+
+pytestmark = pytest.mark.gpu
+
+U64 = np.uint64
+
+
+@pytest.fixture(scope="module")
+def pg():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import piranha_gb300 as pg
+
+    pg.lib()
+    return pg
+
+
+@pytest.fixture()
+def ctx(pg):
+    c = pg.Context(0, form=pg.FORM_LIMB_TC)
+    yield c
+    c.check_device_errors()
+    c.close()
+
+
+def test_tc_selftest(pg, ctx):
+    import torch
+
+    rng = np.random.default_rng(1)
+    A = rng.integers(-128, 128, size=(128, 16)).astype(np.float16)
+    B = rng.integers(-128, 128, size=(64, 16)).astype(np.float16)
+    ta = torch.from_numpy(A.view(np.int16)).cuda()
+    tb = torch.from_numpy(B.view(np.int16)).cuda()
+    D = torch.zeros((128, 64), dtype=torch.float32, device="cuda")
+    st = pg.lib().pg_tc_selftest(ctx.handle, ctypes.c_void_p(ta.data_ptr()), ctypes.c_void_p(tb.data_ptr()),
+                                 ctypes.c_void_p(D.data_ptr()))
+    ctx._check(st)
+    ctx.check_device_errors()
+    want = A.astype(np.float64) @ B.astype(np.float64).T
+    assert np.array_equal(D.cpu().numpy().astype(np.float64), want)
+
+
+@pytest.mark.parametrize("M,N,K,tA,tB,tC", [
+    (128, 64, 16, 1, 1, 1),     # one tile, one stage
+    (128, 128, 512, 1, 1, 1),   # FC-like
+    (200, 70, 144, 1, 0, 1),    # ragged tiles, B column-major
+    (64, 256, 256, 0, 1, 0),    # A column-major, C column-major
+    (32, 32, 2048, 1, 1, 1),    # split-K over many chunks
+    (128, 10, 784, 1, 1, 1),    # SecureML-like output layer
+])
+def test_limb_matmul(pg, ctx, M, N, K, tA, tB, tC):
+    a, b = orc.random_views(M * K, U64, 3), orc.random_views(K * N, U64, 4)
+    comm = orc.Comm()
+    want = orc.matmul(a, b, M, N, K, tA, tB, tC, 26, comm)
+    c = pg.empty_shares(M * N)
+    pg.matmul(ctx, pg.to_device(a), pg.to_device(b), c, M, N, K, tA, tB, tC, 26)
+    ctx.check_device_errors()
+    assert np.array_equal(pg.to_host(c), want)
+    cc = ctx.comm()
+    assert cc["tx"] == comm.tx and cc["rounds"] == comm.rounds
+
+
+def test_limb_matmul_fallback_shape(pg, ctx):
+    M, N, K = 20, 30, 25  # K not a multiple of 16: runs on the integer CUDA cores
+    a, b = orc.random_views(M * K, U64, 5), orc.random_views(K * N, U64, 6)
+    want = orc.matmul(a, b, M, N, K, 1, 1, 1, 20)
+    c = pg.empty_shares(M * N)
+    pg.matmul(ctx, pg.to_device(a), pg.to_device(b), c, M, N, K, 1, 1, 1, 20)
+    ctx.sync()
+    assert np.array_equal(pg.to_host(c), want)
+
+
+@pytest.mark.parametrize("fill", [0, (1 << 64) - 1, 0x8080808080808080, 0x7F7F7F7F7F7F7F7F])
+def test_limb_digit_extremes(pg, ctx, fill):
+    """Constant operands put every digit at an extreme: 0 -> all digits -128 (products 2^14)."""
+    M, N, K = 128, 64, 1024
+    a = np.full((3, 2, M * K), fill, dtype=U64)
+    b = np.full((3, 2, K * N), fill, dtype=U64)
+    want = orc.matmul(a, b, M, N, K, 1, 1, 1, 13)
+    c = pg.empty_shares(M * N)
+    pg.matmul(ctx, pg.to_device(a), pg.to_device(b), c, M, N, K, 1, 1, 1, 13)
+    ctx.check_device_errors()
+    assert np.array_equal(pg.to_host(c), want)
+
+
+@pytest.mark.parametrize("batch,H,W,f,Din,Dout,stride,pad", [
+    (2, 8, 8, 3, 16, 64, 1, 1),
+    (3, 5, 5, 3, 32, 70, 2, 1),
+    (2, 4, 4, 3, 64, 128, 1, 1),
+    (1, 2, 2, 3, 128, 64, 1, 1),
+    (2, 6, 6, 1, 16, 16, 1, 0),
+])
+def test_limb_conv(pg, ctx, batch, H, W, f, Din, Dout, stride, pad):
+    A = orc.random_views(batch * H * W * Din, U64, 7)
+    B = orc.random_views(Dout * f * f * Din, U64, 8)
+    want = orc.convolution(A, B, orc.FPROP, batch, H, W, f, Din, Dout, stride, pad, 26)
+    C = pg.empty_shares(want.shape[2])
+    pg.convolution(ctx, pg.to_device(A), pg.to_device(B), C, orc.FPROP, batch, H, W, f, Din, Dout, stride, pad, 26)
+    ctx.check_device_errors()
+    assert np.array_equal(pg.to_host(C), want)
+
+
+def test_limb_vgg16_forward(pg):
+    from tests.test_gpu_network import run_net
+
+    layers = netref.vgg16_layers()
+    params = netref.kaiming_uniform_params(layers, 21)
+    batch = 2
+    rng = np.random.default_rng(22)
+    x = orc.share_random(orc.encode(rng.uniform(0, 1, batch * 3072)), seed=23)
+    want, want_outs = netref.forward(layers, params, x, batch, keep=True)
+    got, got_outs, _ = run_net(pg, layers, params, x, batch, capture=True, form=pg.FORM_LIMB_TC)
+    for i, (g, w) in enumerate(zip(got_outs, want_outs)):
+        assert np.array_equal(g, w), f"layer {i} {layers[i]}"
+    assert np.array_equal(got, want)

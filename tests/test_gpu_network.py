@@ -115,3 +115,35 @@ def test_vgg16_forward_batch2(pg):
     assert np.array_equal(got, want)
     got2, _, _ = run_net(pg, layers, params, x, batch, capture=True)
     assert np.array_equal(got2, want)
+
+
+def test_capture_with_layer_timing_on_side_stream(pg):
+    """The bench path: a non-default stream, per-layer events recorded inside the graph."""
+    import torch
+
+    layers = netref.secureml_layers()
+    params = netref.kaiming_uniform_params(layers, 31)
+    batch = 16
+    x = orc.share_random(orc.encode(np.random.default_rng(32).uniform(0, 1, batch * 784)), seed=33)
+    want = netref.forward(layers, params, x, batch)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        for form in (pg.FORM_U64, pg.FORM_LIMB_TC):
+            ctx = pg.Context(0, stream=stream, form=form)
+            net = pg.Network(ctx, layers, batch)
+            for i, prm in enumerate(params):
+                if prm is not None:
+                    net.set_params(i, pg.to_device(prm[0]), pg.to_device(prm[1]))
+            net.enable_timing(True)
+            net.capture()
+            ptrs = net.input_buffers()
+            _wrap_device(ptrs[0], 6 * net.in_n).copy_(pg.to_device(x).reshape(-1))
+            net.forward_resident()
+            ctx.sync()
+            times = net.layer_times_ms()
+            assert len(times) == len(layers) and all(t >= 0 for t in times) and sum(times) > 0
+            optrs, n = net.layer_output_ptrs(len(layers) - 1)
+            assert np.array_equal(gather(pg, optrs, n), want)
+            ctx.check_device_errors()
+            net.close()
+            ctx.close()
