@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain-u64-form comparison run")
     return ap.parse_args()
 
 
@@ -180,6 +181,12 @@ def run_ours(args, rank, world, local_rank):
                 if form == forms[-1]:
                     raise
                 print(f"[bench] form {form} unavailable: {e}", file=sys.stderr)
+        if result and result["form"] == "limb_tc" and not args.no_compare:
+            # the same workload on the plain 64-bit integer CUDA-core form, for the limb/u64 ratio
+            u = bench_form(args, pg, torch, stream, dev, pg.FORM_U64, layers, params, x, macs, batch, world)
+            result["compare_u64"] = {"value": u["value"], "ms_per_step": u["ms_per_step"],
+                                     "conv_tflops_equiv": u["roofline"]["achieved"],
+                                     "limb_over_u64": result["value"] / u["value"]}
     return result, (layers, params, x)
 
 
@@ -345,6 +352,8 @@ def main():
         "comm_per_party_per_forward": res["comm_per_party_per_forward"],
         "layer_ms": res["layer_ms"],
     }
+    if "compare_u64" in res:
+        line["compare_u64_form"] = res["compare_u64"]
     print(json.dumps(line))
 
 

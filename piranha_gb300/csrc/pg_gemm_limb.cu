@@ -20,11 +20,18 @@
 // src/mpc/RSS.inl:1097-1110; localFprop :614-639), so Z = sum_p z_p, which
 // the epilogue truncates with dividePublic3out3 (:1077-1094).
 //
-// Roles (384 threads): warps 0-2 load u64 tiles (implicit im2col for conv),
-// convert them to limb planes in the UMMA core-matrix layout and accumulate
-// row/column sums; warp 3 owns the tensor memory and one lane issues the
-// MMAs; warps 4-11 drain tensor memory (two warps per 32-lane quarter, 32
-// columns each) and run the epilogue. Every mbarrier wait is
+// Operands. B (weights, y_p0 + y_p1 and y_p0 per party) is converted once per
+// call by pack_b_kernel into limb planes laid out exactly as the kernel's
+// shared-memory stages (16 KB per segment, K block of 16 and N tile of 64), with
+// its column sums; the GEMM streams it in with one bulk async copy per stage.
+// A (activations, implicit im2col for conv) is converted on chip.
+//
+// Roles (448 threads): warps 0-3 load A rows (one row per thread, two
+// 8-value units per stage, loads for the next stage in flight while the
+// current one is converted) and accumulate the row sums; warp 4 issues the B
+// bulk copies; warp 5 owns the tensor memory and one lane issues the MMAs;
+// warps 6-13 drain tensor memory (two warps per 32-lane quarter, 32 columns
+// each) and run the epilogue. Every mbarrier wait is
 // bounded; on a timeout the kernel records an error word, stops issuing work,
 // waits for its own MMAs and frees tensor memory before returning.
 #include <cuda_fp16.h>
@@ -41,9 +48,10 @@ namespace limb {
 constexpr int BM = 128, BN = 64, BK = 16, STAGES = 4, CHUNK_STAGES = 8;  // 8 stages = 128 K' per chunk
 constexpr int A_LIMB_BYTES = BM * BK * 2;                               // 4096
 constexpr int B_LIMB_BYTES = BN * BK * 2;                               // 2048
-constexpr int STAGE_BYTES = 8 * (A_LIMB_BYTES + B_LIMB_BYTES);          // 49152
-constexpr int NTHREADS = 384;  // 12 warps: 0-2 producers, 3 MMA, 4-11 epilogue
-constexpr int NPRODUCERS = 96;
+constexpr int B_STAGE_BYTES = 8 * B_LIMB_BYTES;                         // 16384
+constexpr int STAGE_BYTES = 8 * A_LIMB_BYTES + B_STAGE_BYTES;           // 49152
+constexpr int NTHREADS = 448;
+constexpr int W_BPROD = 4, W_MMA = 5, W_EPI0 = 6;
 constexpr uint32_t TMEM_COLS = 512;  // 8 diagonals x 64 columns
 constexpr uint64_t CDIG = 0x8080808080808080ull;
 constexpr uint64_t WAIT_NS = 2000000000ull;  // 2 s bound on any single wait
@@ -70,9 +78,10 @@ struct FastDivL {
 struct Args {
     int M, N, Kseg, nseg;
     const uint64_t *a[6];
-    const uint64_t *b0[6];
-    const uint64_t *b1[6];
-    int kind, tA, tB;
+    const uint8_t *packB;      // [seg][kb][ntile][16 KB] limb planes of B
+    const uint64_t *colsum;    // [split][ntiles*64] column sums of B over each K' slice
+    int kind, tA, tC;
+    int ntiles_n, kblocks;     // kblocks = Kseg / 16
     // conv fprop geometry
     int ch, cw, cc, cs, cp, cq, pad, stride;
     FastDivL dQ, dP, dC, dS;
@@ -83,13 +92,12 @@ struct Args {
     uint64_t *partial;    // [gridDim.z][M][N]
     uint64_t *out[6];
     const uint64_t *bias[6];
-    int tC;
     uint64_t d;
     int dshift;
     int *err;
 };
 
-struct __align__(8) Smem {
+struct __align__(16) Smem {
     uint8_t stage[STAGES][STAGE_BYTES];
     Args args;  // kernel arguments, copied here so that dynamic indexing stays out of local memory
     uint64_t full[STAGES], empty[STAGES], acc_full, acc_empty, done;
@@ -134,35 +142,6 @@ __device__ __forceinline__ void load_a8(const Args &g, int seg, int m, int k, ui
     }
 }
 
-// 8 consecutive K' values of column n of B (b0 + b1 when b1 is given)
-__device__ __forceinline__ void load_b8_one(const Args &g, const uint64_t *b, int n, int k, uint64_t (&v)[8]) {
-    if (g.kind == KIND_FPROP || !g.tB) {
-        const ulonglong2 *src = (const ulonglong2 *)(b + (size_t)n * g.Kseg + k);
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            ulonglong2 t = __ldg(src + i);
-            v[2 * i] = t.x;
-            v[2 * i + 1] = t.y;
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < 8; i++) v[i] = __ldg(b + (size_t)(k + i) * g.N + n);
-    }
-}
-
-__device__ __forceinline__ void load_b8(const Args &g, int seg, int n, int k, uint64_t (&v)[8]) {
-#pragma unroll
-    for (int i = 0; i < 8; i++) v[i] = 0;
-    if (n >= g.N) return;
-    load_b8_one(g, g.b0[seg], n, k, v);
-    if (g.b1[seg]) {
-        uint64_t w[8];
-        load_b8_one(g, g.b1[seg], n, k, w);
-#pragma unroll
-        for (int i = 0; i < 8; i++) v[i] += w[i];
-    }
-}
-
 // byte i of each of v[k], v[k+1] as fp16 (byte - 128), packed in one half2 word
 __device__ __forceinline__ uint32_t digit_pair(uint32_t wk, uint32_t wk1, uint32_t sel) {
     uint32_t d;
@@ -195,7 +174,7 @@ __device__ __forceinline__ void store_limbs(uint8_t *plane_base, int plane_bytes
 }
 
 // core-matrix offset of (row, 8-element chunk kc) inside a limb plane
-__device__ __forceinline__ uint32_t cm_off(int row, int kc) {
+__host__ __device__ __forceinline__ uint32_t cm_off(int row, int kc) {
     return (uint32_t)((row >> 3) * 256 + kc * 128 + (row & 7) * 16);
 }
 
@@ -204,10 +183,10 @@ __device__ __forceinline__ void flag_error(Smem &sm, const Args &g, int code) {
     if (g.err) atomicCAS(g.err, 0, code);
 }
 
-// Move the eight diagonal accumulators of 32 columns (col0..col0+31) of this
-// thread's TMEM lane into the 64-bit running sums. Diagonals 0-3 are added as
+// Move the eight diagonal accumulators of 32 columns of this thread's TMEM
+// lane into the 64-bit running sums. Diagonals 0-3 are added as
 // sign-extended 64-bit values shifted by 8s; diagonals 4-7 only matter modulo
-// 2^32 (they are shifted by >= 32), so they are combined in 32-bit registers.
+// 2^32 (they are shifted by >= 32), so only the high word is touched.
 __device__ __forceinline__ void drain32(uint32_t taddr, uint64_t (&run)[32]) {
 #pragma unroll
     for (int d = 0; d < 8; d++) {
@@ -239,21 +218,25 @@ __device__ __forceinline__ void finish32(const Args &g, const Smem &sm, int z, i
             if (j < ncols) dst[j] = run[j];
         return;
     }
-#pragma unroll
-    for (int j = 0; j < 32; j++) run[j] = 1 + div_public<uint64_t>(run[j] - g.d, g.d, g.dshift);
     const bool colmajor = (g.kind == KIND_GEMM && !g.tC);
-#pragma unroll 1
-    for (int ps = 0; ps < 6; ps++) {
-        uint64_t *o = g.out[ps];
-        const uint64_t *b = g.bias[ps];
-        const bool val = (ps == 0 || ps == 5);
 #pragma unroll
-        for (int j = 0; j < 32; j++) {
-            if (j < ncols) {
-                const int n = nbase + j;
-                uint64_t base = val ? run[j] : 0;
-                if (b) base += b[n];
-                o[colmajor ? (size_t)m + (size_t)n * g.M : (size_t)m * g.N + n] = base;
+    for (int j8 = 0; j8 < 32; j8 += 8) {
+        uint64_t v[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) v[j] = 1 + div_public<uint64_t>(run[j8 + j] - g.d, g.d, g.dshift);
+#pragma unroll 1
+        for (int ps = 0; ps < 6; ps++) {
+            uint64_t *o = g.out[ps];
+            const uint64_t *b = g.bias[ps];
+            const bool val = (ps == 0 || ps == 5);
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                if (j8 + j < ncols) {
+                    const int n = nbase + j8 + j;
+                    uint64_t base = val ? v[j] : 0;
+                    if (b) base += b[n];
+                    o[colmajor ? (size_t)m + (size_t)n * g.M : (size_t)m * g.N + n] = base;
+                }
             }
         }
     }
@@ -269,21 +252,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) limb_gemm_kernel(const __grid_con
         uint32_t *dst = reinterpret_cast<uint32_t *>(&sm.args);
         for (int i = threadIdx.x; i < (int)(sizeof(Args) / 4); i += blockDim.x) dst[i] = src[i];
     }
-    __syncthreads();
-    const Args &g = sm.args;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
     const int z = blockIdx.z;
-    const int stage_begin = z * g.chunks_per_split * CHUNK_STAGES;
-    int stage_end = stage_begin + g.chunks_per_split * CHUNK_STAGES;
-    if (stage_end > g.total_stages) stage_end = g.total_stages;
-    const int nst = stage_end > stage_begin ? stage_end - stage_begin : 0;
-    const int nchunks = (nst + CHUNK_STAGES - 1) / CHUNK_STAGES;
-    const int stages_per_seg = g.Kseg / BK;
-
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
-            tc::mbar_init(tc::smem_u32(&sm.full[s]), NPRODUCERS);
+            tc::mbar_init(tc::smem_u32(&sm.full[s]), 128 + 1);  // A producers + the B bulk-copy arrive
             tc::mbar_init(tc::smem_u32(&sm.empty[s]), 1);
         }
         tc::mbar_init(tc::smem_u32(&sm.acc_full), 1);
@@ -292,61 +266,79 @@ __global__ void __launch_bounds__(NTHREADS, 1) limb_gemm_kernel(const __grid_con
         sm.abort = 0;
         tc::fence_mbar_init();
     }
-    for (int i = threadIdx.x; i < BM + BN; i += blockDim.x) {
-        if (i < BM) sm.rowsum[i] = 0;
-        else sm.colsum[i - BM] = 0;
-    }
-    if (warp == 3) {
+    if (warp == W_MMA) {
         tc::tmem_alloc(tc::smem_u32(&sm.tmem_base), TMEM_COLS);
         tc::tmem_relinquish();
     }
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
+    const Args &g = sm.args;
     const uint32_t tmem = sm.tmem_base;
+    const int stage_begin = z * g.chunks_per_split * CHUNK_STAGES;
+    int stage_end = stage_begin + g.chunks_per_split * CHUNK_STAGES;
+    if (stage_end > g.total_stages) stage_end = g.total_stages;
+    const int nst = stage_end > stage_begin ? stage_end - stage_begin : 0;
+    const int nchunks = (nst + CHUNK_STAGES - 1) / CHUNK_STAGES;
+    const int stages_per_seg = g.kblocks;
 
-    if (warp < 3) {
-        // ------------------------------------------------------- producers
-        // units of 8 consecutive K' values per stage: A rows 0..127 x 2, then B rows 0..63 x 2
-        const int t = threadIdx.x;
-        for (int it = 0; it < nst; it++) {
+    if (warp < 4) {
+        // ----------------------------------------------------- A producers
+        const int row = threadIdx.x;  // tile row; units (row, chunk 0) and (row, chunk 1) per stage
+        uint64_t rsum = 0;
+        uint64_t bufA[2][8], bufB[2][8];
+        auto load_stage = [&](int it, uint64_t (&buf)[2][8]) {
+            const int gst = stage_begin + it;
+            const int seg = gst / stages_per_seg;
+            const int k0 = (gst - seg * stages_per_seg) * BK;
+            load_a8(g, seg, m0 + row, k0, buf[0]);
+            load_a8(g, seg, m0 + row, k0 + 8, buf[1]);
+        };
+        auto step = [&](int it, uint64_t (&cur)[2][8], uint64_t (&nxt)[2][8]) -> bool {
             const int s = it % STAGES;
             const uint32_t ph = (uint32_t)(it / STAGES) & 1;
             if (!tc::mbar_wait(tc::smem_u32(&sm.empty[s]), ph ^ 1, &sm.abort, WAIT_NS)) {
                 flag_error(sm, g, 0x100 + s);
-                break;
+                return false;
             }
-            const int gst = stage_begin + it;
-            const int seg = gst / stages_per_seg;
-            const int k = (gst - seg * stages_per_seg) * BK;
-            uint8_t *stA = sm.stage[s];
-            uint8_t *stB = sm.stage[s] + 8 * A_LIMB_BYTES;
-#pragma unroll 1
-            for (int u4 = 0; u4 < 4; u4++) {
-                const int u = t + u4 * NPRODUCERS;
-                uint64_t v[8];
-                uint64_t sum = 0;
-                if (u < 2 * BM) {
-                    const int row = u >> 1, kc = u & 1;
-                    load_a8(g, seg, m0 + row, k + kc * 8, v);
+            if (it + 1 < nst) load_stage(it + 1, nxt);
 #pragma unroll
-                    for (int i = 0; i < 8; i++) sum += v[i];
-                    store_limbs(stA, A_LIMB_BYTES, cm_off(row, kc), v);
-                    atomicAdd((unsigned long long *)&sm.rowsum[row], (unsigned long long)sum);
-                } else {
-                    const int row = (u - 2 * BM) >> 1, kc = u & 1;
-                    load_b8(g, seg, n0 + row, k + kc * 8, v);
+            for (int kc = 0; kc < 2; kc++) {
 #pragma unroll
-                    for (int i = 0; i < 8; i++) sum += v[i];
-                    store_limbs(stB, B_LIMB_BYTES, cm_off(row, kc), v);
-                    atomicAdd((unsigned long long *)&sm.colsum[row], (unsigned long long)sum);
-                }
+                for (int i = 0; i < 8; i++) rsum += cur[kc][i];
+                store_limbs(sm.stage[s], A_LIMB_BYTES, cm_off(row, kc), cur[kc]);
             }
             tc::fence_proxy_async_smem();
             tc::mbar_arrive(tc::smem_u32(&sm.full[s]));
+            return true;
+        };
+        if (nst > 0) load_stage(0, bufA);
+        for (int it = 0; it < nst; it += 2) {
+            if (!step(it, bufA, bufB)) break;
+            if (it + 1 < nst && !step(it + 1, bufB, bufA)) break;
         }
-        asm volatile("bar.sync 1, 352;" ::: "memory");  // producers + epilogue
-    } else if (warp == 3) {
+        sm.rowsum[row] = rsum;
+        if (row < BN) sm.colsum[row] = g.colsum[(size_t)z * g.ntiles_n * BN + n0 + row];
+        asm volatile("bar.sync 1, 384;" ::: "memory");  // A producers + epilogue
+    } else if (warp == W_BPROD) {
+        // ------------------------------------------------ B bulk copies
+        if (lane == 0) {
+            for (int it = 0; it < nst; it++) {
+                const int s = it % STAGES;
+                const uint32_t ph = (uint32_t)(it / STAGES) & 1;
+                if (!tc::mbar_wait(tc::smem_u32(&sm.empty[s]), ph ^ 1, &sm.abort, WAIT_NS)) {
+                    flag_error(sm, g, 0x180 + s);
+                    break;
+                }
+                const int gst = stage_begin + it;  // = seg * kblocks + kb
+                const uint8_t *src = g.packB + ((size_t)gst * g.ntiles_n + blockIdx.x) * B_STAGE_BYTES;
+                const uint32_t bar = tc::smem_u32(&sm.full[s]);
+                tc::mbar_arrive_expect_tx(bar, B_STAGE_BYTES);
+                tc::bulk_g2s(tc::smem_u32(sm.stage[s] + 8 * A_LIMB_BYTES), src, B_STAGE_BYTES, bar);
+            }
+        }
+        __syncwarp();
+    } else if (warp == W_MMA) {
         // ------------------------------------------------------------- MMA
         if (lane == 0) {
             const uint32_t idesc = tc::idesc_f16_f32(BM, BN);
@@ -391,9 +383,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) limb_gemm_kernel(const __grid_con
         __syncwarp();
     } else {
         // -------------------------------------------------------- epilogue
-        const int q = warp & 3;               // TMEM lane quarter
-        const int colh = (warp - 4) >> 2;     // which 32 of the 64 columns
-        const int row = q * 32 + lane;        // tile row = TMEM lane
+        const int q = warp & 3;                  // TMEM lane quarter this warp may access
+        const int colh = (warp - W_EPI0) >> 2;   // which 32 of the 64 columns
+        const int row = q * 32 + lane;           // tile row = TMEM lane
         uint64_t run[32];
 #pragma unroll
         for (int j = 0; j < 32; j++) run[j] = 0;
@@ -408,7 +400,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) limb_gemm_kernel(const __grid_con
             tc::tc_fence_before();
             tc::mbar_arrive(tc::smem_u32(&sm.acc_empty));
         }
-        asm volatile("bar.sync 1, 352;" ::: "memory");
+        asm volatile("bar.sync 1, 384;" ::: "memory");
         const int m = m0 + row;
         if (!sm.abort && m < g.M) {
             const uint64_t kc2 = (uint64_t)nst * BK * (CDIG * CDIG);
@@ -417,9 +409,53 @@ __global__ void __launch_bounds__(NTHREADS, 1) limb_gemm_kernel(const __grid_con
     }
     tc::tc_fence_before();
     __syncthreads();
-    if (warp == 3) {
+    if (warp == W_MMA) {
         tc::tc_fence_after();
         tc::tmem_dealloc(tmem, TMEM_COLS);
+    }
+}
+
+// Convert B (segment seg: y_p0 + y_p1 for even seg, y_p0 for odd) into the
+// stage image layout and accumulate the column sums. One thread per
+// (segment, column, K block of 16, chunk of 8).
+struct PackArgs {
+    const uint64_t *b[6];
+    int N, Kseg, ntiles_n, kblocks, tB, kind;
+    int stages_per_split;  // column sums are kept per K' slice of this many stages
+    uint8_t *packB;
+    uint64_t *colsum;
+};
+
+__global__ void pack_b_kernel(const __grid_constant__ PackArgs pa) {
+    const size_t total = (size_t)6 * pa.ntiles_n * BN * pa.kblocks * 2;
+    for (size_t u = blockIdx.x * (size_t)blockDim.x + threadIdx.x; u < total; u += (size_t)gridDim.x * blockDim.x) {
+        const int kc = (int)(u & 1);
+        size_t t = u >> 1;
+        const int kb = (int)(t % pa.kblocks);
+        t /= pa.kblocks;
+        const int n = (int)(t % ((size_t)pa.ntiles_n * BN));
+        const int seg = (int)(t / ((size_t)pa.ntiles_n * BN));
+        const int p = seg >> 1;
+        const int k = kb * BK + kc * 8;
+        uint64_t v[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) v[i] = 0;
+        if (n < pa.N) {
+            const uint64_t *b0 = pa.b[2 * p], *b1 = (seg & 1) ? nullptr : pa.b[2 * p + 1];
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                size_t idx = (pa.kind == KIND_FPROP || !pa.tB) ? (size_t)n * pa.Kseg + k + i : (size_t)(k + i) * pa.N + n;
+                v[i] = b0[idx] + (b1 ? b1[idx] : 0);
+            }
+            uint64_t sum = 0;
+#pragma unroll
+            for (int i = 0; i < 8; i++) sum += v[i];
+            const int slice = (seg * pa.kblocks + kb) / pa.stages_per_split;
+            atomicAdd((unsigned long long *)&pa.colsum[(size_t)slice * pa.ntiles_n * BN + n], (unsigned long long)sum);
+        }
+        const int nt = n / BN, nr = n % BN;
+        uint8_t *dst = pa.packB + (((size_t)seg * pa.kblocks + kb) * pa.ntiles_n + nt) * B_STAGE_BYTES;
+        store_limbs(dst, B_LIMB_BYTES, cm_off(nr, kc), v);
     }
 }
 
@@ -507,7 +543,8 @@ int rss_matmul(Ctx *, const T *const *, const T *const *, T *const *, const T *c
 template <typename T>
 int rss_conv(Ctx *, const T *const *, const T *const *, T *const *, int, int, int, int, int, int, int, int, int, int);
 
-static int limb_launch(Ctx *c, limb::Args &g, int total_stages) {
+// b: the six B share pointers (layout per g.kind / tB)
+static int limb_launch(Ctx *c, limb::Args &g, int tB, const uint64_t *const *b) {
     using namespace limb;
     static bool attr_set = false;
     if (!attr_set) {
@@ -517,6 +554,9 @@ static int limb_launch(Ctx *c, limb::Args &g, int total_stages) {
     }
     const int tiles_m = (g.M + BM - 1) / BM, tiles_n = (g.N + BN - 1) / BN;
     const int tiles = tiles_m * tiles_n;
+    g.ntiles_n = tiles_n;
+    g.kblocks = g.Kseg / BK;
+    const int total_stages = 6 * g.kblocks;
     const int chunks = (total_stages + CHUNK_STAGES - 1) / CHUNK_STAGES;
     int sms = c->sm_count > 0 ? c->sm_count : 148;
     int split = tiles >= sms ? 1 : sms / tiles;
@@ -527,10 +567,34 @@ static int limb_launch(Ctx *c, limb::Args &g, int total_stages) {
     g.total_stages = total_stages;
     g.chunks_per_split = cps;
     g.err = device_error_word(c);
+    // scratch: packed B stages, column sums, then [split][M][N] partials (all 256-byte aligned)
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t pack_bytes = (size_t)total_stages * tiles_n * B_STAGE_BYTES;
+    const size_t col_bytes = al((size_t)split * tiles_n * BN * 8);
+    const size_t part_bytes = split > 1 ? (size_t)split * g.M * g.N * 8 : 0;
+    uint8_t *scr = (uint8_t *)scratch(c, pack_bytes + col_bytes + part_bytes);
+    if (!scr) return PG_ERR_NO_MEMORY;
+    g.packB = scr;
+    g.colsum = (uint64_t *)(scr + pack_bytes);
+    PG_CHECK_CUDA(c, cudaMemsetAsync((void *)g.colsum, 0, col_bytes, c->stream));
+    {
+        PackArgs pa;
+        memset(&pa, 0, sizeof(pa));
+        for (int i = 0; i < 6; i++) pa.b[i] = b[i];
+        pa.N = g.N; pa.Kseg = g.Kseg; pa.ntiles_n = tiles_n; pa.kblocks = g.kblocks; pa.tB = tB; pa.kind = g.kind;
+        pa.stages_per_split = cps * CHUNK_STAGES;
+        pa.packB = scr;
+        pa.colsum = (uint64_t *)(scr + pack_bytes);
+        size_t units = (size_t)6 * tiles_n * BN * g.kblocks * 2;
+        unsigned blocks = (unsigned)((units + 255) / 256);
+        if (blocks > (unsigned)sms * 16) blocks = sms * 16;
+        pack_b_kernel<<<blocks, 256, 0, c->stream>>>(pa);
+        c->launches++;
+        int st = launch_status(c, "pack_b_kernel");
+        if (st) return st;
+    }
     if (split > 1) {
-        uint64_t *part = (uint64_t *)scratch(c, (size_t)split * g.M * g.N * 8);
-        if (!part) return PG_ERR_NO_MEMORY;
-        g.partial = part;
+        g.partial = (uint64_t *)(scr + pack_bytes + col_bytes);
         g.direct = 0;
     } else {
         g.direct = 1;
@@ -552,16 +616,9 @@ static int limb_launch(Ctx *c, limb::Args &g, int total_stages) {
     return PG_OK;
 }
 
-static void limb_segments(limb::Args &g, const uint64_t *const *a, const uint64_t *const *b) {
+static void limb_segments(limb::Args &g, const uint64_t *const *a) {
     g.nseg = 6;
-    for (int p = 0; p < 3; p++) {
-        g.a[2 * p] = a[2 * p];
-        g.b0[2 * p] = b[2 * p];
-        g.b1[2 * p] = b[2 * p + 1];
-        g.a[2 * p + 1] = a[2 * p + 1];
-        g.b0[2 * p + 1] = b[2 * p];
-        g.b1[2 * p + 1] = nullptr;
-    }
+    for (int i = 0; i < 6; i++) g.a[i] = a[i];  // segment 2p: x_p0, segment 2p+1: x_p1
 }
 
 static bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
@@ -580,12 +637,12 @@ int limb_rss_matmul_u64(Ctx *c, const uint64_t *const a[6], const uint64_t *cons
         return rss_matmul<uint64_t>(c, a, b, out, bias, M, N, K, tA, tB, tC, trunc);
     limb::Args g;
     memset(&g, 0, sizeof(g));
-    g.M = M; g.N = N; g.Kseg = K; g.kind = limb::KIND_GEMM; g.tA = tA; g.tB = tB; g.tC = tC;
-    limb_segments(g, a, b);
+    g.M = M; g.N = N; g.Kseg = K; g.kind = limb::KIND_GEMM; g.tA = tA; g.tC = tC;
+    limb_segments(g, a);
     for (int i = 0; i < 6; i++) { g.out[i] = out[i]; g.bias[i] = bias ? bias[i] : nullptr; }
     g.d = 1ull << trunc;
     g.dshift = pow2_shift<uint64_t>(g.d);
-    int st = limb_launch(c, g, 6 * K / limb::BK);
+    int st = limb_launch(c, g, tB, b);
     if (st) return st;
     comm_msg(c, 2ull * M * N * 8, 2ull * M * N * 8);
     comm_round(c);
@@ -609,11 +666,11 @@ int limb_rss_conv_u64(Ctx *c, const uint64_t *const A[6], const uint64_t *const 
     g.M = batch * P * Q; g.N = Dout; g.Kseg = f * f * Din; g.kind = limb::KIND_FPROP; g.tC = 1;
     g.ch = H; g.cw = W; g.cc = Din; g.cs = f; g.cp = P; g.cq = Q; g.pad = pad; g.stride = stride;
     g.dQ.init(Q); g.dP.init(P); g.dC.init(Din); g.dS.init(f);
-    limb_segments(g, A, B);
+    limb_segments(g, A);
     for (int i = 0; i < 6; i++) { g.out[i] = C[i]; g.bias[i] = nullptr; }
     g.d = 1ull << trunc;
     g.dshift = pow2_shift<uint64_t>(g.d);
-    int st = limb_launch(c, g, 6 * g.Kseg / limb::BK);
+    int st = limb_launch(c, g, 0, B);
     if (st) return st;
     uint64_t n_out = (uint64_t)g.M * g.N;
     comm_msg(c, 2 * n_out * 8, 2 * n_out * 8);
