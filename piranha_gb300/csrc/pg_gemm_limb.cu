@@ -9,11 +9,14 @@
 //   sum a*b = sum_s 2^(8s) D_s + C*(sum a) + C*(sum b) - K'*C^2   (mod 2^64)
 // with D_s = sum_{i+j=s} sum_k d_i(a_k) d_j(b_k) for the 36 digit pairs with
 // i+j < 8 (pairs with i+j >= 8 vanish mod 2^64). One tcgen05.mma per pair and
-// K step of 16 accumulates D_s in fp32 tensor memory; an accumulator holds at
-// most (s+1)*128 products per chunk of 128 K' terms, so |D_s| <= 2^24 and
-// every fp32 sum is an exact integer. After each chunk the epilogue warps move
-// the eight accumulators into 64-bit registers. The row sums of A and column
-// sums of B are accumulated by the producer warps while they convert tiles.
+// K step of 16 accumulates D_s in fp32 tensor memory. Each output tile runs
+// two passes over K': the high pass (diagonals 4-7, 26 pairs, needed only
+// modulo 2^32) and the low pass (diagonals 0-3, 10 pairs, digits 0-3 only).
+// A pass keeps four accumulators and two tensor-memory buffers, so the
+// epilogue warps drain one buffer into 64-bit registers while the MMAs fill
+// the other; chunk lengths keep every |D_s| <= 2^24, so every fp32 sum is an
+// exact integer. The row sums of A are accumulated by the producer warps and
+// the column sums of B by the packing kernel.
 //
 // Protocol. The K' dimension is the concatenation of the six RSS segments
 // [x_p0 | x_p1] x [y_p0 + y_p1 ; y_p0] of the three parties (localMatMul,
@@ -45,14 +48,18 @@ namespace pg {
 
 namespace limb {
 
-constexpr int BM = 128, BN = 64, BK = 16, STAGES = 4, CHUNK_STAGES = 8;  // 8 stages = 128 K' per chunk
+constexpr int BM = 128, BN = 64, BK = 16, STAGES = 4;
+// K' per fp32 accumulation chunk: the high pass (diagonals 4-7, up to 8 pairs
+// per diagonal) drains every 128 K' (8 stages), the low pass (diagonals 0-3,
+// up to 4 pairs) every 256 K' (16 stages): |D_s| <= (pairs * K'chunk) * 2^14 <= 2^24.
+constexpr int CHUNK_STAGES = 8, CHUNK_STAGES_LO = 16;
 constexpr int A_LIMB_BYTES = BM * BK * 2;                               // 4096
 constexpr int B_LIMB_BYTES = BN * BK * 2;                               // 2048
 constexpr int B_STAGE_BYTES = 8 * B_LIMB_BYTES;                         // 16384
 constexpr int STAGE_BYTES = 8 * A_LIMB_BYTES + B_STAGE_BYTES;           // 49152
 constexpr int NTHREADS = 448;
 constexpr int W_BPROD = 4, W_MMA = 5, W_EPI0 = 6;
-constexpr uint32_t TMEM_COLS = 512;  // 8 diagonals x 64 columns
+constexpr uint32_t TMEM_COLS = 512;  // 2 buffers x 4 diagonals x 64 columns
 constexpr uint64_t CDIG = 0x8080808080808080ull;
 constexpr uint64_t WAIT_NS = 2000000000ull;  // 2 s bound on any single wait
 
@@ -100,7 +107,7 @@ struct Args {
 struct __align__(16) Smem {
     uint8_t stage[STAGES][STAGE_BYTES];
     Args args;  // kernel arguments, copied here so that dynamic indexing stays out of local memory
-    uint64_t full[STAGES], empty[STAGES], acc_full, acc_empty, done;
+    uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], done;
     uint64_t rowsum[BM], colsum[BN];
     uint32_t tmem_base;
     int abort;
@@ -173,6 +180,21 @@ __device__ __forceinline__ void store_limbs(uint8_t *plane_base, int plane_bytes
     }
 }
 
+// Limbs 0-3 only (the low 32 bits of each value), for the low-digit pass.
+__device__ __forceinline__ void store_limbs_lo(uint8_t *plane_base, int plane_bytes, uint32_t off,
+                                               const uint64_t (&v)[8]) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        uint32_t w[4];
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            const uint32_t sel = (uint32_t)i | ((uint32_t)i << 4) | ((uint32_t)(4 + i) << 8) | ((uint32_t)(4 + i) << 12);
+            w[p] = digit_pair((uint32_t)v[2 * p], (uint32_t)v[2 * p + 1], sel);
+        }
+        *reinterpret_cast<uint4 *>(plane_base + i * plane_bytes + off) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
+
 // core-matrix offset of (row, 8-element chunk kc) inside a limb plane
 __host__ __device__ __forceinline__ uint32_t cm_off(int row, int kc) {
     return (uint32_t)((row >> 3) * 256 + kc * 128 + (row & 7) * 16);
@@ -183,21 +205,22 @@ __device__ __forceinline__ void flag_error(Smem &sm, const Args &g, int code) {
     if (g.err) atomicCAS(g.err, 0, code);
 }
 
-// Move the eight diagonal accumulators of 32 columns of this thread's TMEM
-// lane into the 64-bit running sums. Diagonals 0-3 are added as
-// sign-extended 64-bit values shifted by 8s; diagonals 4-7 only matter modulo
-// 2^32 (they are shifted by >= 32), so only the high word is touched.
-__device__ __forceinline__ void drain32(uint32_t taddr, uint64_t (&run)[32]) {
+// Move four diagonal accumulators (32 columns of this thread's TMEM lane)
+// into the 64-bit running sums. HI: diagonals 4-7, which matter only modulo
+// 2^32 (shift >= 32), so only the high word is touched; LO: diagonals 0-3,
+// added as sign-extended 64-bit values shifted by 8s.
+template <bool HI>
+__device__ __forceinline__ void drain4(uint32_t taddr, uint64_t (&run)[32]) {
 #pragma unroll
-    for (int d = 0; d < 8; d++) {
+    for (int a = 0; a < 4; a++) {
         uint32_t r[32];
-        tc::tmem_ld32(taddr + (uint32_t)(d * BN), r);
+        tc::tmem_ld32(taddr + (uint32_t)(a * BN), r);
         tc::tmem_wait_ld();
 #pragma unroll
         for (int j = 0; j < 32; j++) {
             int v = __float2int_rz(__uint_as_float(r[j]));  // exact: |v| <= 2^24
-            if (d < 4) run[j] += (uint64_t)(int64_t)v << (8 * d);
-            else run[j] += (uint64_t)((uint32_t)v << (8 * (d - 4))) << 32;  // needed mod 2^32 only
+            if (HI) run[j] += (uint64_t)((uint32_t)v << (8 * a)) << 32;
+            else run[j] += (uint64_t)(int64_t)v << (8 * a);
         }
     }
 }
@@ -242,6 +265,29 @@ __device__ __forceinline__ void finish32(const Args &g, const Smem &sm, int z, i
     }
 }
 
+// All MMAs of one stage for the diagonals D0..D0+3. For a fixed A digit
+// plane i, the pairs (i, j) with i + j in the pass's range use consecutive B
+// digit planes j = jlo..jhi, which sit in shared memory exactly as one
+// (64*cnt)-row operand, and land in consecutive 64-column accumulators
+// d - D0 = i + jlo - D0 ... So one MMA with N = 64*cnt covers them all: 8
+// MMAs per stage for the high pass (N = 256 x5, 192, 128, 64) and 4 for the
+// low pass (N = 256, 192, 128, 64).
+template <int D0>
+__device__ __forceinline__ void issue_stage(uint32_t acc, uint64_t adesc, uint64_t bdesc, bool first_stage) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int jlo = D0 - i > 0 ? D0 - i : 0;
+        const int jhi = D0 + 3 - i;  // inclusive
+        const int cnt = jhi - jlo + 1;
+        if (cnt <= 0) continue;
+        const uint64_t ad = adesc + (uint64_t)((i * A_LIMB_BYTES) >> 4);
+        const uint64_t bd = bdesc + (uint64_t)((jlo * B_LIMB_BYTES) >> 4);
+        const uint32_t d = acc + (uint32_t)((i + jlo - D0) * BN);
+        const uint32_t accum = (!first_stage || i > 0) ? 1u : 0u;  // i = 0 writes all four accumulators first
+        tc::mma_f16(d, ad, bd, tc::idesc_f16_f32(BM, BN * cnt), accum);
+    }
+}
+
 // ------------------------------------------------------------------ kernel
 
 __global__ void __launch_bounds__(NTHREADS, 1) limb_gemm_kernel(const __grid_constant__ Args gp) {
@@ -260,8 +306,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) limb_gemm_kernel(const __grid_con
             tc::mbar_init(tc::smem_u32(&sm.full[s]), 128 + 1);  // A producers + the B bulk-copy arrive
             tc::mbar_init(tc::smem_u32(&sm.empty[s]), 1);
         }
-        tc::mbar_init(tc::smem_u32(&sm.acc_full), 1);
-        tc::mbar_init(tc::smem_u32(&sm.acc_empty), 256);
+        for (int b = 0; b < 2; b++) {
+            tc::mbar_init(tc::smem_u32(&sm.acc_full[b]), 1);
+            tc::mbar_init(tc::smem_u32(&sm.acc_empty[b]), 256);
+        }
         tc::mbar_init(tc::smem_u32(&sm.done), 1);
         sm.abort = 0;
         tc::fence_mbar_init();
@@ -279,7 +327,6 @@ __global__ void __launch_bounds__(NTHREADS, 1) limb_gemm_kernel(const __grid_con
     int stage_end = stage_begin + g.chunks_per_split * CHUNK_STAGES;
     if (stage_end > g.total_stages) stage_end = g.total_stages;
     const int nst = stage_end > stage_begin ? stage_end - stage_begin : 0;
-    const int nchunks = (nst + CHUNK_STAGES - 1) / CHUNK_STAGES;
     const int stages_per_seg = g.kblocks;
 
     if (warp < 4) {
@@ -294,28 +341,46 @@ __global__ void __launch_bounds__(NTHREADS, 1) limb_gemm_kernel(const __grid_con
             load_a8(g, seg, m0 + row, k0, buf[0]);
             load_a8(g, seg, m0 + row, k0 + 8, buf[1]);
         };
-        auto step = [&](int it, uint64_t (&cur)[2][8], uint64_t (&nxt)[2][8]) -> bool {
-            const int s = it % STAGES;
-            const uint32_t ph = (uint32_t)(it / STAGES) & 1;
+        // global ring position: pass 0 (high digits) stages 0..nst-1, pass 1 (low) nst..2*nst-1
+        auto step = [&](int it, bool lo_pass, uint64_t (&cur)[2][8], uint64_t (&nxt)[2][8]) -> bool {
+            const int git = it + (lo_pass ? nst : 0);
+            const int s = git % STAGES;
+            const uint32_t ph = (uint32_t)(git / STAGES) & 1;
             if (!tc::mbar_wait(tc::smem_u32(&sm.empty[s]), ph ^ 1, &sm.abort, WAIT_NS)) {
                 flag_error(sm, g, 0x100 + s);
                 return false;
             }
             if (it + 1 < nst) load_stage(it + 1, nxt);
+            else if (!lo_pass) load_stage(0, nxt);  // first stage of the low pass
 #pragma unroll
             for (int kc = 0; kc < 2; kc++) {
+                if (!lo_pass) {
 #pragma unroll
-                for (int i = 0; i < 8; i++) rsum += cur[kc][i];
-                store_limbs(sm.stage[s], A_LIMB_BYTES, cm_off(row, kc), cur[kc]);
+                    for (int i = 0; i < 8; i++) rsum += cur[kc][i];
+                    store_limbs(sm.stage[s], A_LIMB_BYTES, cm_off(row, kc), cur[kc]);
+                } else {
+                    store_limbs_lo(sm.stage[s], A_LIMB_BYTES, cm_off(row, kc), cur[kc]);
+                }
             }
             tc::fence_proxy_async_smem();
             tc::mbar_arrive(tc::smem_u32(&sm.full[s]));
             return true;
         };
+        bool ok = true;
         if (nst > 0) load_stage(0, bufA);
-        for (int it = 0; it < nst; it += 2) {
-            if (!step(it, bufA, bufB)) break;
-            if (it + 1 < nst && !step(it + 1, bufB, bufA)) break;
+        // both passes together have 2*nst stages; nst parity decides which buffer starts the low pass
+        for (int pass = 0; pass < 2 && ok; pass++) {
+            const bool lo = pass == 1;
+            const bool startA = !lo || (nst % 2 == 0);
+            for (int it = 0; it < nst && ok; it += 2) {
+                if (startA) {
+                    ok = step(it, lo, bufA, bufB);
+                    if (ok && it + 1 < nst) ok = step(it + 1, lo, bufB, bufA);
+                } else {
+                    ok = step(it, lo, bufB, bufA);
+                    if (ok && it + 1 < nst) ok = step(it + 1, lo, bufA, bufB);
+                }
+            }
         }
         sm.rowsum[row] = rsum;
         if (row < BN) sm.colsum[row] = g.colsum[(size_t)z * g.ntiles_n * BN + n0 + row];
@@ -323,9 +388,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) limb_gemm_kernel(const __grid_con
     } else if (warp == W_BPROD) {
         // ------------------------------------------------ B bulk copies
         if (lane == 0) {
-            for (int it = 0; it < nst; it++) {
-                const int s = it % STAGES;
-                const uint32_t ph = (uint32_t)(it / STAGES) & 1;
+            for (int git = 0; git < 2 * nst; git++) {
+                const bool lo = git >= nst;
+                const int it = lo ? git - nst : git;
+                const int s = git % STAGES;
+                const uint32_t ph = (uint32_t)(git / STAGES) & 1;
                 if (!tc::mbar_wait(tc::smem_u32(&sm.empty[s]), ph ^ 1, &sm.abort, WAIT_NS)) {
                     flag_error(sm, g, 0x180 + s);
                     break;
@@ -333,48 +400,51 @@ __global__ void __launch_bounds__(NTHREADS, 1) limb_gemm_kernel(const __grid_con
                 const int gst = stage_begin + it;  // = seg * kblocks + kb
                 const uint8_t *src = g.packB + ((size_t)gst * g.ntiles_n + blockIdx.x) * B_STAGE_BYTES;
                 const uint32_t bar = tc::smem_u32(&sm.full[s]);
-                tc::mbar_arrive_expect_tx(bar, B_STAGE_BYTES);
-                tc::bulk_g2s(tc::smem_u32(sm.stage[s] + 8 * A_LIMB_BYTES), src, B_STAGE_BYTES, bar);
+                const uint32_t bytes = lo ? B_STAGE_BYTES / 2 : B_STAGE_BYTES;  // limbs 0-3 lead the image
+                tc::mbar_arrive_expect_tx(bar, bytes);
+                tc::bulk_g2s(tc::smem_u32(sm.stage[s] + 8 * A_LIMB_BYTES), src, bytes, bar);
             }
         }
         __syncwarp();
     } else if (warp == W_MMA) {
         // ------------------------------------------------------------- MMA
         if (lane == 0) {
-            const uint32_t idesc = tc::idesc_f16_f32(BM, BN);
-            int it = 0;
-            for (int c = 0; c < nchunks && !sm.abort; c++) {
-                if (c > 0 && !tc::mbar_wait(tc::smem_u32(&sm.acc_empty), (uint32_t)(c - 1) & 1, &sm.abort, WAIT_NS)) {
-                    flag_error(sm, g, 0x200);
-                    break;
-                }
-                tc::tc_fence_after();
-                const int cst = (nst - c * CHUNK_STAGES) < CHUNK_STAGES ? nst - c * CHUNK_STAGES : CHUNK_STAGES;
-                bool ok = true;
-                for (int st = 0; st < cst; st++, it++) {
-                    const int s = it % STAGES;
-                    const uint32_t ph = (uint32_t)(it / STAGES) & 1;
-                    if (!tc::mbar_wait(tc::smem_u32(&sm.full[s]), ph, &sm.abort, WAIT_NS)) {
-                        flag_error(sm, g, 0x300 + s);
+            const uint64_t desc0 = tc::smem_desc(tc::smem_u32(sm.stage[0]), 128, 256);
+            int git = 0, gc = 0;  // ring position, global chunk (buffer = gc & 1)
+            bool ok = true;
+            for (int pass = 0; pass < 2 && ok; pass++) {
+                const bool lo = pass == 1;
+                const int cstages = lo ? CHUNK_STAGES_LO : CHUNK_STAGES;
+                const int nch = (nst + cstages - 1) / cstages;
+                for (int c = 0; c < nch && ok; c++, gc++) {
+                    const int buf = gc & 1;
+                    if (gc >= 2 && !tc::mbar_wait(tc::smem_u32(&sm.acc_empty[buf]), (uint32_t)((gc - 2) >> 1) & 1,
+                                                  &sm.abort, WAIT_NS)) {
+                        flag_error(sm, g, 0x200 + buf);
                         ok = false;
                         break;
                     }
                     tc::tc_fence_after();
-                    const uint32_t a0 = tc::smem_u32(sm.stage[s]);
-                    const uint32_t b0 = a0 + 8 * A_LIMB_BYTES;
-#pragma unroll
-                    for (int i = 0; i < 8; i++) {
-                        const uint64_t ad = tc::smem_desc(a0 + i * A_LIMB_BYTES, 128, 256);
-#pragma unroll
-                        for (int j = 0; j < 8 - i; j++) {
-                            const uint64_t bd = tc::smem_desc(b0 + j * B_LIMB_BYTES, 128, 256);
-                            tc::mma_f16(tmem + (uint32_t)((i + j) * BN), ad, bd, idesc, (st > 0 || i > 0) ? 1u : 0u);
+                    const uint32_t acc = tmem + (uint32_t)(buf * 4 * BN);
+                    const int cst = (nst - c * cstages) < cstages ? nst - c * cstages : cstages;
+                    for (int st = 0; st < cst; st++, git++) {
+                        const int s = git % STAGES;
+                        const uint32_t ph = (uint32_t)(git / STAGES) & 1;
+                        if (!tc::mbar_wait(tc::smem_u32(&sm.full[s]), ph, &sm.abort, WAIT_NS)) {
+                            flag_error(sm, g, 0x300 + s);
+                            ok = false;
+                            break;
                         }
+                        tc::tc_fence_after();
+                        const uint64_t ad = desc0 + (uint64_t)((s * STAGE_BYTES) >> 4);
+                        const uint64_t bd = ad + (uint64_t)((8 * A_LIMB_BYTES) >> 4);
+                        if (lo) issue_stage<0>(acc, ad, bd, st == 0);
+                        else issue_stage<4>(acc, ad, bd, st == 0);
+                        tc::mma_commit(tc::smem_u32(&sm.empty[s]));
                     }
-                    tc::mma_commit(tc::smem_u32(&sm.empty[s]));
+                    if (!ok) break;
+                    tc::mma_commit(tc::smem_u32(&sm.acc_full[buf]));
                 }
-                if (!ok) break;
-                tc::mma_commit(tc::smem_u32(&sm.acc_full));
             }
             // all MMAs this thread issued are complete once `done` fires
             tc::mma_commit(tc::smem_u32(&sm.done));
@@ -390,15 +460,19 @@ __global__ void __launch_bounds__(NTHREADS, 1) limb_gemm_kernel(const __grid_con
 #pragma unroll
         for (int j = 0; j < 32; j++) run[j] = 0;
         const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(colh * 32);
-        for (int c = 0; c < nchunks; c++) {
-            if (!tc::mbar_wait(tc::smem_u32(&sm.acc_full), (uint32_t)c & 1, &sm.abort, WAIT_NS)) {
+        const int nch_hi = (nst + CHUNK_STAGES - 1) / CHUNK_STAGES;
+        const int nch_lo = (nst + CHUNK_STAGES_LO - 1) / CHUNK_STAGES_LO;
+        for (int gc = 0; gc < nch_hi + nch_lo; gc++) {
+            const int buf = gc & 1;
+            if (!tc::mbar_wait(tc::smem_u32(&sm.acc_full[buf]), (uint32_t)(gc >> 1) & 1, &sm.abort, WAIT_NS)) {
                 flag_error(sm, g, 0x500);
                 break;
             }
             tc::tc_fence_after();
-            drain32(taddr, run);
+            if (gc < nch_hi) drain4<true>(taddr + (uint32_t)(buf * 4 * BN), run);
+            else drain4<false>(taddr + (uint32_t)(buf * 4 * BN), run);
             tc::tc_fence_before();
-            tc::mbar_arrive(tc::smem_u32(&sm.acc_empty));
+            tc::mbar_arrive(tc::smem_u32(&sm.acc_empty[buf]));
         }
         asm volatile("bar.sync 1, 384;" ::: "memory");
         const int m = m0 + row;
