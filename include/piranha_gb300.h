@@ -168,6 +168,34 @@ int pg_expand_compare_u8(pg_ctx *ctx, const uint8_t *b, const uint8_t *nb, size_
 int pg_maxpool_im2row_u64(pg_ctx *ctx, const uint64_t *im, uint64_t *out, int H, int W, int f, int Din,
                           int batch, int stride, int pad, uint64_t pad_val);
 
+/* ---------------------------------------------- share-GEMM without allocation
+ * No counterpart in the reference. The same result as pg_rss_matmul_u64, bit
+ * for bit, computed by the limb tensor-core kernels, for callers that must not
+ * allocate device memory while they run: a host that hands out all device
+ * memory from its own pool, a serving loop that cannot stall its other
+ * streams on cudaFree's device-wide wait, or one that must not fail with
+ * out-of-memory halfway through a request. pg_rss_matmul_u64 grows the
+ * context's scratch with cudaMalloc/cudaFree; this call allocates nothing and
+ * takes its scratch from one fixed device array of PG_NOALLOC_SCRATCH_BYTES,
+ * which the CUDA runtime reserves when it loads the library module that holds
+ * it.
+ *  - The first call on a device does set-up (finds the array's address and
+ *    sets the kernel's shared-memory limit) and needs the context's device
+ *    current. Make it before any stream capture on that device.
+ *  - The scratch need is 96 * K * (N rounded up to 64) bytes of packed
+ *    weights plus the column sums (and split-K partial sums, used only when
+ *    they fit). A problem that does not fit returns PG_ERR_SIZE; pg_last_error
+ *    gives the need and the limit.
+ *  - K must be a multiple of 16 and the twelve input pointers 16-byte
+ *    aligned; other shapes return PG_ERR_UNSUPPORTED.
+ *  - All calls on a device, from every context and thread, share the one
+ *    array. Calls that can run at the same time on the device (streams with
+ *    no ordering between them) corrupt each other's results: order them on
+ *    one stream or with events. */
+#define PG_NOALLOC_SCRATCH_BYTES ((size_t)128 << 20)
+int pg_rss_matmul_u64_noalloc(pg_ctx *ctx, const uint64_t *const a[6], const uint64_t *const b[6],
+                              uint64_t *const c[6], int M, int N, int K, int tA, int tB, int tC, int trunc);
+
 /* ------------------------------------------------------ network executor
  * NeuralNetwork::forward (src/nn/NeuralNetwork.cu:109-133) for FC / CNN /
  * ReLU / Maxpool stacks: layers run in order on preallocated share buffers

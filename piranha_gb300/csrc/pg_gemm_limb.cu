@@ -759,4 +759,114 @@ int limb_selftest(Ctx *c, const uint16_t *A, const uint16_t *B, float *D) {
     return launch_status(c, "selftest_kernel");
 }
 
+// ------------------------------------------------ fixed-scratch share-GEMM
+
+// Raise the GEMM kernel's dynamic shared-memory limit on the current device.
+int limb_prepare_current_device(Ctx *c) {
+    PG_CHECK_CUDA(c, cudaFuncSetAttribute(limb::limb_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)limb::smem_bytes()));
+    return PG_OK;
+}
+
+// The limb-form RSS share-GEMM of limb_rss_matmul_u64 (no bias), with every
+// scratch byte taken from [scr, scr + cap) instead of the context's scratch.
+// It allocates nothing. Split-K is used only when its partial sums fit too;
+// a problem whose unsplit need exceeds cap is refused with PG_ERR_SIZE, and
+// shapes the limb tiles do not cover with PG_ERR_UNSUPPORTED. The column
+// sums are zeroed on the stream before use; the packed weights and the
+// partial sums are written in full by their producers before they are read.
+int limb_rss_matmul_u64_fixed(Ctx *c, uint8_t *scr, size_t cap, const uint64_t *const a[6],
+                              const uint64_t *const b[6], uint64_t *const out[6], int M, int N, int K, int tA, int tB,
+                              int tC, int trunc) {
+    using namespace limb;
+    CSh6<uint64_t> ca, cb;
+    Sh6<uint64_t> co;
+    if (!load6(ca, a) || !load6(cb, b) || !load6(co, out)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    if (M <= 0 || N <= 0 || K <= 0) return set_error(c, PG_ERR_SIZE, "matmul: bad sizes");
+    if (trunc < 0 || trunc > 63) return set_error(c, PG_ERR_INVALID_ARG, "bad truncation %d", trunc);
+    if (K % BK) return set_error(c, PG_ERR_UNSUPPORTED, "K = %d is not a multiple of %d", K, BK);
+    for (int i = 0; i < 6; i++)
+        if (!aligned16(a[i]) || !aligned16(b[i]))
+            return set_error(c, PG_ERR_UNSUPPORTED, "share pointers must be 16-byte aligned");
+    if (!scr || ((uintptr_t)scr & 255)) return set_error(c, PG_ERR_INVALID_ARG, "scratch must be 256-byte aligned");
+
+    Args g;
+    memset(&g, 0, sizeof(g));
+    g.M = M; g.N = N; g.Kseg = K; g.kind = KIND_GEMM; g.tA = tA; g.tC = tC;
+    limb_segments(g, a);
+    for (int i = 0; i < 6; i++) { g.out[i] = out[i]; g.bias[i] = nullptr; }
+    g.d = 1ull << trunc;
+    g.dshift = pow2_shift<uint64_t>(g.d);
+
+    const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
+    const int tiles = tiles_m * tiles_n;
+    g.ntiles_n = tiles_n;
+    g.kblocks = K / BK;
+    const int total_stages = 6 * g.kblocks;
+    const int chunks = (total_stages + CHUNK_STAGES - 1) / CHUNK_STAGES;
+    const int sms = c->sm_count > 0 ? c->sm_count : 148;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t pack_bytes = (size_t)total_stages * tiles_n * B_STAGE_BYTES;
+    auto need = [&](int split) {
+        return pack_bytes + al((size_t)split * tiles_n * BN * 8) + (split > 1 ? (size_t)split * M * N * 8 : 0);
+    };
+    int split = tiles >= sms ? 1 : sms / tiles;
+    if (split > chunks) split = chunks;
+    if (split < 1) split = 1;
+    int cps = (chunks + split - 1) / split;
+    split = (chunks + cps - 1) / cps;
+    if (need(split) > cap) {
+        split = 1;
+        cps = chunks;
+    }
+    if (need(split) > cap)
+        return set_error(c, PG_ERR_SIZE,
+                         "M=%d N=%d K=%d needs %zu bytes of scratch; the fixed scratch holds %zu (the packed "
+                         "weights alone take 96 * K * (N rounded up to 64) bytes)",
+                         M, N, K, need(split), cap);
+    g.total_stages = total_stages;
+    g.chunks_per_split = cps;
+    g.err = device_error_word(c);
+    const size_t col_bytes = al((size_t)split * tiles_n * BN * 8);
+    uint64_t *colsum = (uint64_t *)(scr + pack_bytes);
+    g.packB = scr;
+    g.colsum = colsum;
+    PG_CHECK_CUDA(c, cudaMemsetAsync((void *)colsum, 0, col_bytes, c->stream));
+    {
+        PackArgs pa;
+        memset(&pa, 0, sizeof(pa));
+        for (int i = 0; i < 6; i++) pa.b[i] = b[i];
+        pa.N = N; pa.Kseg = K; pa.ntiles_n = tiles_n; pa.kblocks = g.kblocks; pa.tB = tB; pa.kind = KIND_GEMM;
+        pa.stages_per_split = cps * CHUNK_STAGES;
+        pa.packB = scr;
+        pa.colsum = colsum;
+        size_t units = (size_t)6 * tiles_n * BN * g.kblocks * 2;
+        unsigned blocks = (unsigned)((units + 255) / 256);
+        if (blocks > (unsigned)sms * 16) blocks = sms * 16;
+        pack_b_kernel<<<blocks, 256, 0, c->stream>>>(pa);
+        c->launches++;
+        int st = launch_status(c, "pack_b_kernel");
+        if (st) return st;
+    }
+    g.direct = split > 1 ? 0 : 1;
+    if (split > 1) g.partial = (uint64_t *)(scr + pack_bytes + col_bytes);
+    dim3 grid(tiles_n, tiles_m, split);
+    limb_gemm_kernel<<<grid, NTHREADS, smem_bytes(), c->stream>>>(g);
+    c->launches++;
+    int st = launch_status(c, "limb_gemm_kernel");
+    if (st) return st;
+    if (split > 1) {
+        size_t total = (size_t)M * N;
+        unsigned blocks = (unsigned)((total + 255) / 256);
+        if (blocks > (unsigned)sms * 8) blocks = sms * 8;
+        limb_reduce_kernel<<<blocks, 256, 0, c->stream>>>(g, split);
+        c->launches++;
+        st = launch_status(c, "limb_reduce_kernel");
+        if (st) return st;
+    }
+    comm_msg(c, 2ull * M * N * 8, 2ull * M * N * 8);
+    comm_round(c);
+    return PG_OK;
+}
+
 }  // namespace pg

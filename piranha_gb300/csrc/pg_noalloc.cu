@@ -1,0 +1,82 @@
+// pg_noalloc.cu — pg_rss_matmul_u64_noalloc: the limb tensor-core RSS
+// share-GEMM with its scratch in one fixed device array, for callers that
+// must not allocate device memory once they are running.
+//
+// The regular entry point grows the context's scratch with cudaMalloc and
+// releases the old block with cudaFree, which waits for the whole device.
+// A host that owns all device memory through its own pool, a serving loop
+// that must not stall its other streams on that wait, or one that must not
+// meet an out-of-memory error halfway through a request cannot allow either.
+// This entry point takes its scratch from `noalloc_scratch` below instead,
+// which the CUDA runtime reserves when it loads this file's module.
+//
+// Set-up: the first call on a device, with the context's device current,
+// looks up the array's device address with cudaGetSymbolAddress (which also
+// loads the module) and raises the GEMM kernel's shared-memory limit; later
+// calls on that device reuse the address. Make that first call before any
+// stream capture on the device.
+//
+// Sharing: every call on a device, from every context and thread, uses the
+// same array. Calls whose execution can overlap on the device (different
+// streams with no ordering between them) corrupt each other's results;
+// order them on one stream or with events.
+#include <mutex>
+
+#include "pg_common.cuh"
+
+namespace pg {
+int limb_prepare_current_device(Ctx *c);
+int limb_rss_matmul_u64_fixed(Ctx *c, uint8_t *scr, size_t cap, const uint64_t *const a[6],
+                              const uint64_t *const b[6], uint64_t *const out[6], int M, int N, int K, int tA, int tB,
+                              int tC, int trunc);
+}  // namespace pg
+
+using namespace pg;
+
+namespace {
+
+static __device__ __align__(256) uint8_t noalloc_scratch[PG_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+std::mutex setup_mutex;
+uint8_t *scratch_addr[kMaxDevices];  // per device, set once by set-up
+
+int setup_device(Ctx *c, uint8_t **out) {
+    int cur = -1;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(c, PG_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+    }
+    if (cur != c->device)
+        return set_error(c, PG_ERR_INVALID_ARG, "the context's device %d must be current (device %d is)", c->device,
+                         cur);
+    if (cur < 0 || cur >= kMaxDevices)
+        return set_error(c, PG_ERR_UNSUPPORTED, "device ordinal %d is above %d", cur, kMaxDevices - 1);
+    std::lock_guard<std::mutex> lock(setup_mutex);
+    if (!scratch_addr[cur]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return set_error(c, PG_ERR_CUDA, "cudaGetSymbolAddress of the fixed scratch: %s", cudaGetErrorString(e));
+        }
+        int st = limb_prepare_current_device(c);
+        if (st) return st;
+        scratch_addr[cur] = (uint8_t *)p;
+    }
+    *out = scratch_addr[cur];
+    return PG_OK;
+}
+
+}  // namespace
+
+extern "C" int pg_rss_matmul_u64_noalloc(pg_ctx *c, const uint64_t *const a[6], const uint64_t *const b[6],
+                                         uint64_t *const out[6], int M, int N, int K, int tA, int tB, int tC,
+                                         int trunc) {
+    if (!c) return PG_ERR_INVALID_ARG;
+    uint8_t *scr = nullptr;
+    int st = setup_device(c, &scr);
+    if (st) return st;
+    return limb_rss_matmul_u64_fixed(c, scr, PG_NOALLOC_SCRATCH_BYTES, a, b, out, M, N, K, tA, tB, tC, trunc);
+}
