@@ -74,9 +74,9 @@ int truncate_cols_u8(Ctx *, const uint8_t *, uint8_t *, size_t, int, int);
 int bitexpand_u64(Ctx *, const uint64_t *, size_t, uint64_t *);
 int expand_compare_u8(Ctx *, const uint8_t *, const uint8_t *, size_t, uint8_t *, size_t);
 int maxpool_im2row_u64(Ctx *, const uint64_t *, uint64_t *, int, int, int, int, int, int, int, uint64_t);
-int limb_rss_matmul_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *,
+int limb3_rss_matmul_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *,
                         const uint64_t *const *, int, int, int, int, int, int, int);
-int limb_rss_conv_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *, int, int, int, int,
+int limb3_rss_conv_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *, int, int, int, int,
                       int, int, int, int, int, int);
 int limb_selftest(Ctx *, const uint16_t *, const uint16_t *, float *);
 
@@ -184,7 +184,7 @@ int pg_conv_u64(pg_ctx *c, int op, int N, int H, int W, int C, int K, int R, int
 int pg_rss_matmul_u64(pg_ctx *c, const uint64_t *const a[6], const uint64_t *const b[6], uint64_t *const out[6],
                       int M, int N, int K, int tA, int tB, int tC, int trunc) {
     CTX_OR_FAIL(c);
-    if (c->form == PG_FORM_LIMB_TC) return limb_rss_matmul_u64(c, a, b, out, nullptr, M, N, K, tA, tB, tC, trunc);
+    if (c->form == PG_FORM_LIMB_TC) return limb3_rss_matmul_u64(c, a, b, out, nullptr, M, N, K, tA, tB, tC, trunc);
     return rss_matmul<uint64_t>(c, a, b, out, nullptr, M, N, K, tA, tB, tC, trunc);
 }
 int pg_rss_matmul_u32(pg_ctx *c, const uint32_t *const a[6], const uint32_t *const b[6], uint32_t *const out[6],
@@ -198,14 +198,14 @@ int pg_rss_fc_forward_u64(pg_ctx *c, const uint64_t *const x[6], const uint64_t 
     if (bias)
         for (int i = 0; i < 6; i++)
             if (!bias[i]) return set_error(c, PG_ERR_INVALID_ARG, "null bias share");
-    if (c->form == PG_FORM_LIMB_TC) return limb_rss_matmul_u64(c, x, w, out, bias, batch, dout, din, 1, 1, 1, fp);
+    if (c->form == PG_FORM_LIMB_TC) return limb3_rss_matmul_u64(c, x, w, out, bias, batch, dout, din, 1, 1, 1, fp);
     return rss_matmul<uint64_t>(c, x, w, out, bias, batch, dout, din, 1, 1, 1, fp);
 }
 int pg_rss_conv_u64(pg_ctx *c, const uint64_t *const A[6], const uint64_t *const B[6], uint64_t *const C[6], int op,
                     int batch, int H, int W, int f, int Din, int Dout, int stride, int pad, int trunc) {
     CTX_OR_FAIL(c);
     if (c->form == PG_FORM_LIMB_TC && op == PG_CONV_FPROP)
-        return limb_rss_conv_u64(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc);
+        return limb3_rss_conv_u64(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc);
     return rss_conv<uint64_t>(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc);
 }
 int pg_rss_divide_public_u64(pg_ctx *c, uint64_t *const a[6], size_t n, uint64_t d) {

@@ -1,0 +1,884 @@
+// pg_limb_tma.cu — the 8-bit-limb tensor-core RSS share-GEMM and implicit
+// convolution, fed by TMA (tcgen05, fp16 digits, fp32 accumulators in tensor
+// memory), exact modulo 2^64.
+//
+// Digits. Every 64-bit operand v is written with eight signed digits
+//   e_i = byte_i(v + 0x8080808080808080) - 128  in [-128, 127],
+// for which v = sum_i e_i 2^(8i) (mod 2^64) holds exactly (adding 128 to
+// every byte and removing it again digit by digit leaves the value). So a
+// contraction over K' terms is
+//   sum_k a_k b_k = sum_s 2^(8s) D_s (mod 2^64),  D_s = sum_{i+j=s} sum_k e_i(a_k) e_j(b_k),
+// with no correction terms, and only the 36 digit pairs with i+j < 8 matter.
+// The value 0 has all digits 0, so zero padding (tensor-map out-of-bounds
+// fill, ragged tiles) stands for the value 0. A digit product is at most 2^14
+// in magnitude; a diagonal has at most 8 pairs, so draining the fp32
+// accumulators every 128 K' (diagonals 4-7) or 256 K' (diagonals 0-3, at most
+// 4 pairs) keeps every partial sum an integer of magnitude <= 2^24, exact in
+// fp32.
+//
+// Operands. A (activations, or the GEMM's left operand) is first written by
+// image_kernel as an image of digit planes in global memory,
+//   img[seg][plane][C/8][pixel][8]  (fp16),
+// so that for a tile of output pixels and one conv tap, the 16 channels of a
+// K block are one 4-D tensor-map box: (8 channels x Wt pixels, as one
+// contiguous line of 16*Wt bytes) x Ht rows x Nt images x 2 channel groups.
+// A tap is a shift of the box (16 bytes per pixel along the line), and
+// padding is the box running out of bounds. The GEMM case reads lines of 32
+// consecutive image rows instead. B (weights, with
+// y_p0 + y_p1 precomputed) is packed once by pack_kernel into the exact
+// shared-memory stage image and streamed with bulk async copies.
+//
+// Protocol. The K' dimension concatenates the six RSS segments
+// [x_p0 | x_p1] x [y_p0 + y_p1 ; y_p0] of the three parties (localMatMul,
+// src/mpc/RSS.inl:1097-1110; localFprop :614-639); the epilogue truncates
+// Z = sum_p z_p with dividePublic3out3 (:1077-1094).
+//
+// Roles (320 threads): warp 0 issues the TMA and bulk copies of each stage,
+// warp 1 owns tensor memory and one lane issues the MMAs, warps 2-9 drain the
+// accumulators (two warps per 32-lane quarter, 32 columns each) and run the
+// epilogue. Each output tile runs two passes over K' (high digit diagonals
+// 4-7, needed modulo 2^32, then 0-3 with digits 0-3 only), each pass with two
+// tensor-memory buffers of four 64-column accumulators. Every mbarrier wait
+// is bounded; on a timeout the kernel records an error word, stops issuing,
+// waits for its own copies and MMAs, and frees tensor memory.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_fp16.h>
+
+#include <cstring>
+#include <mutex>
+
+#include "pg_common.cuh"
+#include "pg_limb_tma.cuh"
+#include "pg_tcgen05.cuh"
+
+namespace pg {
+int *device_error_word(Ctx *c);
+namespace lt {
+
+constexpr int BM = 128, BN = 64, BK = 16, STAGES = 4;
+constexpr int CHUNK_STAGES = 8, CHUNK_STAGES_LO = 16;
+constexpr int A_PLANE_BYTES = BM * BK * 2;                      // 4096
+constexpr int B_PLANE_BYTES = BN * BK * 2;                      // 2048
+constexpr int B_STAGE_BYTES = 8 * B_PLANE_BYTES;                // 16384
+constexpr int STAGE_BYTES = 8 * A_PLANE_BYTES + B_STAGE_BYTES;  // 49152
+constexpr int NTHREADS = 320;
+constexpr int W_PROD = 0, W_MMA = 1, W_EPI0 = 2;
+constexpr uint32_t TMEM_COLS = 512;  // 2 buffers x 4 diagonals x 64 columns
+constexpr uint64_t DIGIT_OFFSET = 0x8080808080808080ull;
+constexpr uint64_t WAIT_NS = 2000000000ull;  // 2 s bound on any single wait
+
+struct Args {
+    int M, N;
+    int kblocks, cblocks, C8, f, pad;
+    int Wt, Ht, Nt, R, tiles_w, tiles_h, P, Q, Nimg;
+    int rows_mode;  // 1: the image holds one row per output row (GEMM, im2col)
+    int ntiles_n, total_stages, chunks_per_split;
+    int direct, colmajor;
+    uint32_t a_box_bytes;  // bytes of one digit plane of a stage (16 * 2 * Wt * Ht * Nt)
+    const uint8_t *packB;
+    uint64_t *partial;
+    uint64_t *out[6];
+    const uint64_t *bias[6];
+    uint64_t d;
+    int dshift;
+    int *err;
+};
+
+struct __align__(16) Smem {
+    uint8_t stage[STAGES][STAGE_BYTES];
+    Args args;
+    uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], done;
+    uint32_t tmem_base;
+    int abort;
+    int never;  // stays 0: a wait that must not be cut short by the abort flag
+};
+
+static size_t smem_bytes() { return sizeof(Smem) + 1024; }
+
+// ------------------------------------------------------------------ digits
+
+// fp16 digits of byte b of two words, packed in one half2 word:
+// low half from x, high half from y, each (1024 + byte) - 1152 = byte - 128.
+__device__ __forceinline__ uint32_t digit_pair(uint32_t x, uint32_t y, uint32_t b) {
+    const uint32_t sel = b | (b << 4) | ((4 + b) << 8) | ((4 + b) << 12);
+    uint32_t d;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(x), "r"(y), "r"(sel));
+    d = (d & 0x00FF00FFu) | 0x64006400u;
+    __half2 h = *reinterpret_cast<__half2 *>(&d);
+    h = __hsub2(h, __halves2half2(__ushort_as_half(0x6480), __ushort_as_half(0x6480)));
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+// The digit planes (8 fp16 each, one uint4 per plane) of 8 values.
+template <int NPL>
+__device__ __forceinline__ void digits8(const uint64_t (&v)[8], uint4 (&pl)[NPL]) {
+    uint32_t lo[8], hi[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const uint64_t u = v[k] + DIGIT_OFFSET;
+        lo[k] = (uint32_t)u;
+        hi[k] = (uint32_t)(u >> 32);
+    }
+#pragma unroll
+    for (int i = 0; i < NPL; i++) {
+        uint32_t w[4];
+#pragma unroll
+        for (int p = 0; p < 4; p++)
+            w[p] = i < 4 ? digit_pair(lo[2 * p], lo[2 * p + 1], (uint32_t)(i & 3))
+                         : digit_pair(hi[2 * p], hi[2 * p + 1], (uint32_t)(i & 3));
+        pl[i] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
+
+// ------------------------------------------------------------ image kernel
+
+enum { SRC_ROWS = 0, SRC_COLS = 1, SRC_IM2COL = 2 };
+
+struct ImageArgs {
+    const uint64_t *a[6];
+    int mode;
+    long long pixels;  // image rows written (source rows, then zero rows up to a whole line)
+    long long pixels_src;  // image rows that come from A
+    int C8;            // image channel groups of 8
+    int Kreal;         // values at k >= Kreal are 0
+    long long ld;      // ROWS: row stride; COLS: column stride
+    int vec;           // ROWS: rows are 16-byte aligned and Kreal is a multiple of 8
+    int H, W, Din, f, stride, pad, P, Q;
+    uint4 *img;
+};
+
+// One thread per (segment, 8-channel group, pixel); consecutive threads take
+// consecutive pixels, so the plane stores are coalesced.
+__global__ void image_kernel(const __grid_constant__ ImageArgs ia) {
+    const long long total = 6ll * ia.C8 * ia.pixels;
+    for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < total;
+         u += (long long)gridDim.x * blockDim.x) {
+        const long long pix = u % ia.pixels;
+        const long long t = u / ia.pixels;
+        const int cb = (int)(t % ia.C8);
+        const int seg = (int)(t / ia.C8);
+        const uint64_t *a = ia.a[seg];
+        const int k0 = cb * 8;
+        uint64_t v[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) v[i] = 0;
+        if (pix >= ia.pixels_src) {
+            // zero row padding the image to whole lines
+        } else if (ia.mode == SRC_ROWS) {
+            const uint64_t *src = a + pix * ia.ld + k0;
+            if (ia.vec && k0 < ia.Kreal) {
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const ulonglong2 q = __ldg(reinterpret_cast<const ulonglong2 *>(src) + i);
+                    v[2 * i] = q.x;
+                    v[2 * i + 1] = q.y;
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; i++)
+                    if (k0 + i < ia.Kreal) v[i] = __ldg(src + i);
+            }
+        } else if (ia.mode == SRC_COLS) {
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+                if (k0 + i < ia.Kreal) v[i] = __ldg(a + (long long)(k0 + i) * ia.ld + pix);
+        } else {
+            const int q = (int)(pix % ia.Q);
+            const long long np = pix / ia.Q;
+            const int p = (int)(np % ia.P);
+            const long long n = np / ia.P;
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const int k = k0 + i;
+                if (k >= ia.Kreal) continue;
+                const int c = k % ia.Din, rs = k / ia.Din;
+                const int s = rs % ia.f, r = rs / ia.f;
+                const int h = p * ia.stride - ia.pad + r, w = q * ia.stride - ia.pad + s;
+                if (h < 0 || h >= ia.H || w < 0 || w >= ia.W) continue;
+                v[i] = __ldg(a + ((n * ia.H + h) * ia.W + w) * (long long)ia.Din + c);
+            }
+        }
+        uint4 pl[8];
+        digits8<8>(v, pl);
+#pragma unroll
+        for (int i = 0; i < 8; i++) ia.img[((long long)(seg * 8 + i) * ia.C8 + cb) * ia.pixels + pix] = pl[i];
+    }
+}
+
+// ------------------------------------------------------------- B packing
+
+struct PackArgs {
+    const uint64_t *b[6];
+    int N, Kreal, kblocks, ntiles_n;
+    int kn;  // 1: b[k * N + n]; 0: b[n * Kreal + k]
+    uint8_t *packB;
+};
+
+// core-matrix offset of (row, 8-element K chunk kc) inside a B digit plane:
+// 8 rows x 16 bytes per core matrix, K-adjacent core matrices 128 bytes
+// apart, 8-row groups 256 bytes apart
+__host__ __device__ __forceinline__ uint32_t b_off(int row, int kc) {
+    return (uint32_t)((row >> 3) * 256 + kc * 128 + (row & 7) * 16);
+}
+
+// One thread per (segment, column, K block, chunk of 8). Segment 2p holds
+// y_p0 + y_p1 and segment 2p+1 holds y_p0 of party p.
+__global__ void pack_kernel(const __grid_constant__ PackArgs pa) {
+    const long long total = 6ll * pa.ntiles_n * BN * pa.kblocks * 2;
+    for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < total;
+         u += (long long)gridDim.x * blockDim.x) {
+        const int kc = (int)(u & 1);
+        long long t = u >> 1;
+        const int kb = (int)(t % pa.kblocks);
+        t /= pa.kblocks;
+        const int n = (int)(t % ((long long)pa.ntiles_n * BN));
+        const int seg = (int)(t / ((long long)pa.ntiles_n * BN));
+        const int p = seg >> 1;
+        const int k0 = kb * BK + kc * 8;
+        uint64_t v[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) v[i] = 0;
+        if (n < pa.N) {
+            const uint64_t *b0 = pa.b[2 * p], *b1 = (seg & 1) ? nullptr : pa.b[2 * p + 1];
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const int k = k0 + i;
+                if (k < pa.Kreal) {
+                    const long long idx = pa.kn ? (long long)k * pa.N + n : (long long)n * pa.Kreal + k;
+                    v[i] = b0[idx] + (b1 ? b1[idx] : 0);
+                }
+            }
+        }
+        uint4 pl[8];
+        digits8<8>(v, pl);
+        uint8_t *dst = pa.packB + (((long long)seg * pa.kblocks + kb) * pa.ntiles_n + n / BN) * B_STAGE_BYTES;
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+            *reinterpret_cast<uint4 *>(dst + i * B_PLANE_BYTES + b_off(n % BN, kc)) = pl[i];
+    }
+}
+
+// ------------------------------------------------------------- GEMM kernel
+
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void flag_error(Smem &sm, const Args &g, int code) {
+    sm.abort = 1;
+    if (g.err) atomicCAS(g.err, 0, code);
+}
+
+// All MMAs of one stage for diagonals D0..D0+3: for A digit plane i, the B
+// planes j = jlo..jhi with i + j in range are adjacent in shared memory and
+// their products go to adjacent accumulators, so one MMA with N = 64 * cnt
+// covers them (8 MMAs per stage in the high pass, 4 in the low pass).
+template <int D0>
+__device__ __forceinline__ void issue_stage(uint32_t acc, uint64_t adesc, uint64_t bdesc, bool first_stage) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int jlo = D0 - i > 0 ? D0 - i : 0;
+        const int jhi = D0 + 3 - i;
+        const int cnt = jhi - jlo + 1;
+        if (cnt <= 0) continue;
+        const uint64_t ad = adesc + (uint64_t)((i * A_PLANE_BYTES) >> 4);
+        const uint64_t bd = bdesc + (uint64_t)((jlo * B_PLANE_BYTES) >> 4);
+        const uint32_t d = acc + (uint32_t)((i + jlo - D0) * BN);
+        const uint32_t accum = (!first_stage || i > 0) ? 1u : 0u;  // i = 0 writes all four accumulators first
+        tc::mma_f16(d, ad, bd, tc::idesc_f16_f32(BM, BN * cnt), accum);
+    }
+}
+
+__device__ __forceinline__ int f2i(uint32_t x) { return __float2int_rz(__uint_as_float(x)); }
+
+// Diagonals 4-7 (shift >= 32) matter only modulo 2^32 of their sum
+// D4 + 2^8 D5 + 2^16 D6 + 2^24 D7, which goes to the high word of the
+// running 64-bit sum.
+__device__ __forceinline__ void drain_hi(uint32_t taddr, uint64_t (&acc)[32]) {
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        uint32_t r[32];
+        tc::tmem_ld32(taddr + (uint32_t)(a * BN), r);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 32; j++) acc[j] += (uint64_t)((uint32_t)f2i(r[j]) << (8 * a)) << 32;
+    }
+}
+
+// Diagonals 0-3 in full 64-bit precision, one accumulator at a time.
+__device__ __forceinline__ void drain_lo(uint32_t taddr, uint64_t (&acc)[32]) {
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        uint32_t r[32];
+        tc::tmem_ld32(taddr + (uint32_t)(a * BN), r);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            // acc += D * 2^(8a) as one widening multiply-add
+            const int32_t dv = f2i(r[j]);
+            uint64_t t;
+            asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(t) : "r"(dv), "r"(1 << (8 * a)), "l"(acc[j]));
+            acc[j] = t;
+        }
+    }
+}
+
+// 32 columns of one output row: store the slice's partial Z, or apply
+// dividePublic3out3 and write the six output shares (+ bias shares).
+__device__ __forceinline__ void finish32(const Args &g, int z, long long m, int nbase, const uint64_t (&zs)[32]) {
+    const int ncols = g.N - nbase < 32 ? g.N - nbase : 32;
+    if (!g.direct) {
+        uint64_t *dst = g.partial + ((long long)z * g.M + m) * g.N + nbase;
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+            if (j < ncols) dst[j] = zs[j];
+        return;
+    }
+#pragma unroll
+    for (int j8 = 0; j8 < 32; j8 += 8) {
+        uint64_t v[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            v[j] = 1 + div_public<uint64_t>(zs[j8 + j] - g.d, g.d, g.dshift);
+        }
+#pragma unroll 1
+        for (int ps = 0; ps < 6; ps++) {
+            uint64_t *o = g.out[ps];
+            const uint64_t *b = g.bias[ps];
+            const bool val = (ps == 0 || ps == 5);
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                if (j8 + j < ncols) {
+                    const int n = nbase + j8 + j;
+                    uint64_t base = val ? v[j] : 0;
+                    if (b) base += b[n];
+                    o[g.colmajor ? m + (long long)n * g.M : m * g.N + n] = base;
+                }
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+    limb_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ Args gp) {
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t pad = (1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u;
+    Smem &sm = *reinterpret_cast<Smem *>(smem_raw + pad);
+    {
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(&gp);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(&sm.args);
+        for (int i = threadIdx.x; i < (int)(sizeof(Args) / 4); i += blockDim.x) dst[i] = src[i];
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int z = blockIdx.z;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            tc::mbar_init(tc::smem_u32(&sm.full[s]), 1);
+            tc::mbar_init(tc::smem_u32(&sm.empty[s]), 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            tc::mbar_init(tc::smem_u32(&sm.acc_full[b]), 1);
+            tc::mbar_init(tc::smem_u32(&sm.acc_empty[b]), 256);
+        }
+        tc::mbar_init(tc::smem_u32(&sm.done), 1);
+        sm.abort = 0;
+        sm.never = 0;
+        tc::fence_mbar_init();
+    }
+    if (warp == W_MMA) {
+        tc::tmem_alloc(tc::smem_u32(&sm.tmem_base), TMEM_COLS);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const Args &g = sm.args;
+    const uint32_t tmem = sm.tmem_base;
+    const int stage_begin = z * g.chunks_per_split * CHUNK_STAGES;
+    int stage_end = stage_begin + g.chunks_per_split * CHUNK_STAGES;
+    if (stage_end > g.total_stages) stage_end = g.total_stages;
+    const int nst = stage_end > stage_begin ? stage_end - stage_begin : 0;
+    // output-pixel rectangle of this tile
+    const int tw = blockIdx.y % g.tiles_w, t2 = blockIdx.y / g.tiles_w;
+    const int th = t2 % g.tiles_h, tn = t2 / g.tiles_h;
+    const int w0 = tw * g.Wt, h0 = th * g.Ht, n0 = tn * g.Nt;
+
+    if (warp == W_PROD) {
+        // ------------------------------------------------ TMA + bulk copies
+        if (lane == 0) {
+            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
+            int issued = 0;
+            bool ok = true;
+            for (int git = 0; git < 2 * nst; git++) {
+                const bool lo = git >= nst;
+                const int it = lo ? git - nst : git;
+                const int s = git % STAGES;
+                const uint32_t ph = (uint32_t)(git / STAGES) & 1;
+                if (!tc::mbar_wait(tc::smem_u32(&sm.empty[s]), ph ^ 1, &sm.abort, WAIT_NS)) {
+                    flag_error(sm, g, 0x100 + s);
+                    ok = false;
+                    break;
+                }
+                const int gst = stage_begin + it;
+                const int seg = gst / g.kblocks, kb = gst - seg * g.kblocks;
+                const int tap = kb / g.cblocks, cb = kb - tap * g.cblocks;
+                const int r = tap / g.f, sx = tap - r * g.f;
+                const int nplanes = lo ? 4 : 8;
+                const uint32_t bar = tc::smem_u32(&sm.full[s]);
+                const uint32_t bbytes = lo ? B_STAGE_BYTES / 2 : B_STAGE_BYTES;  // digits 0-3 lead the image
+                tc::mbar_arrive_expect_tx(bar, nplanes * g.a_box_bytes + bbytes);
+                const uint32_t dst = tc::smem_u32(sm.stage[s]);
+                // line offset (16 bytes per pixel, so always 16-byte aligned), row, image
+                const int x = g.rows_mode ? 0 : 8 * (w0 + sx - g.pad);
+                const int y = g.rows_mode ? n0 >> 5 : h0 + r - g.pad;
+                const int zc = g.rows_mode ? 0 : n0;
+                for (int i = 0; i < nplanes; i++)
+                    tma_load_4d(dst + i * A_PLANE_BYTES, &tmA, x, y, zc, (seg * 8 + i) * g.C8 + 2 * cb, bar);
+                const uint8_t *src = g.packB + ((size_t)gst * g.ntiles_n + blockIdx.x) * B_STAGE_BYTES;
+                tc::bulk_g2s(dst + 8 * A_PLANE_BYTES, src, bbytes, bar);
+                issued = git + 1;
+            }
+            if (!ok) {
+                // wait (bounded, not cut short by the abort flag) for the copies still in flight
+                const int from = issued - STAGES > 0 ? issued - STAGES : 0;
+                for (int git = from; git < issued; git++)
+                    tc::mbar_wait(tc::smem_u32(&sm.full[git % STAGES]), (uint32_t)(git / STAGES) & 1, &sm.never,
+                                  WAIT_NS);
+            }
+        }
+        __syncwarp();
+    } else if (warp == W_MMA) {
+        // ------------------------------------------------------------- MMA
+        if (lane == 0) {
+            const uint32_t s0 = tc::smem_u32(sm.stage[0]);
+            const uint64_t adesc0 = tc::smem_desc(s0, g.a_box_bytes / 2, 128);  // K chunks one box half apart
+            const uint64_t bdesc0 = tc::smem_desc(s0 + 8 * A_PLANE_BYTES, 128, 256);
+            int git = 0, gc = 0;
+            bool ok = true;
+            for (int pass = 0; pass < 2 && ok; pass++) {
+                const bool lo = pass == 1;
+                const int cstages = lo ? CHUNK_STAGES_LO : CHUNK_STAGES;
+                const int nch = (nst + cstages - 1) / cstages;
+                for (int c = 0; c < nch && ok; c++, gc++) {
+                    const int buf = gc & 1;
+                    if (gc >= 2 && !tc::mbar_wait(tc::smem_u32(&sm.acc_empty[buf]), (uint32_t)((gc - 2) >> 1) & 1,
+                                                  &sm.abort, WAIT_NS)) {
+                        flag_error(sm, g, 0x200 + buf);
+                        ok = false;
+                        break;
+                    }
+                    tc::tc_fence_after();
+                    const uint32_t acc = tmem + (uint32_t)(buf * 4 * BN);
+                    const int cst = (nst - c * cstages) < cstages ? nst - c * cstages : cstages;
+                    for (int st = 0; st < cst; st++, git++) {
+                        const int s = git % STAGES;
+                        const uint32_t ph = (uint32_t)(git / STAGES) & 1;
+                        if (!tc::mbar_wait(tc::smem_u32(&sm.full[s]), ph, &sm.abort, WAIT_NS)) {
+                            flag_error(sm, g, 0x300 + s);
+                            ok = false;
+                            break;
+                        }
+                        tc::tc_fence_after();
+                        const uint64_t off = (uint64_t)((s * STAGE_BYTES) >> 4);
+                        if (lo) issue_stage<0>(acc, adesc0 + off, bdesc0 + off, st == 0);
+                        else issue_stage<4>(acc, adesc0 + off, bdesc0 + off, st == 0);
+                        tc::mma_commit(tc::smem_u32(&sm.empty[s]));
+                    }
+                    if (!ok) break;
+                    tc::mma_commit(tc::smem_u32(&sm.acc_full[buf]));
+                }
+            }
+            tc::mma_commit(tc::smem_u32(&sm.done));
+            if (!tc::mbar_wait(tc::smem_u32(&sm.done), 0, &sm.never, WAIT_NS) && g.err) atomicCAS(g.err, 0, 0x400);
+        }
+        __syncwarp();
+    } else {
+        // -------------------------------------------------------- epilogue
+        const int q = warp & 3;
+        const int colh = (warp - W_EPI0) >> 2;
+        const int row = q * 32 + lane;
+        uint64_t zs[32];  // running Z of this thread's 32 columns
+#pragma unroll
+        for (int j = 0; j < 32; j++) zs[j] = 0;
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(colh * 32);
+        const int nch_hi = (nst + CHUNK_STAGES - 1) / CHUNK_STAGES;
+        const int nch_lo = (nst + CHUNK_STAGES_LO - 1) / CHUNK_STAGES_LO;
+        // chunk gc uses tensor-memory buffer gc & 1; its (gc >> 1)-th fill
+        auto wait_chunk = [&](int gc) -> bool {
+            if (!tc::mbar_wait(tc::smem_u32(&sm.acc_full[gc & 1]), (uint32_t)(gc >> 1) & 1, &sm.abort, WAIT_NS)) {
+                flag_error(sm, g, 0x500);
+                return false;
+            }
+            tc::tc_fence_after();
+            return true;
+        };
+        auto release_chunk = [&](int gc) {
+            tc::tc_fence_before();
+            tc::mbar_arrive(tc::smem_u32(&sm.acc_empty[gc & 1]));
+        };
+        bool ok = true;
+#pragma unroll 1
+        for (int gc = 0; gc < nch_hi && ok; gc++) {
+            if (!(ok = wait_chunk(gc))) break;
+            drain_hi(taddr + (uint32_t)((gc & 1) * 4 * BN), zs);
+            release_chunk(gc);
+        }
+#pragma unroll 1
+        for (int gc = nch_hi; gc < nch_hi + nch_lo && ok; gc++) {
+            if (!(ok = wait_chunk(gc))) break;
+            drain_lo(taddr + (uint32_t)((gc & 1) * 4 * BN), zs);
+            release_chunk(gc);
+        }
+        if (!sm.abort && row < g.R) {
+            const int wh = g.Wt * g.Ht;
+            const int nn = row / wh, rem = row - nn * wh;
+            const int hh = rem / g.Wt, ww = rem - hh * g.Wt;
+            const int n = n0 + nn, h = h0 + hh, w = w0 + ww;
+            if (n < g.Nimg && h < g.P && w < g.Q) {
+                const long long m = ((long long)n * g.P + h) * g.Q + w;
+                const int nbase = blockIdx.x * BN + colh * 32;
+                if (nbase < g.N) finish32(g, z, m, nbase, zs);
+            }
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == W_MMA) {
+        tc::tc_fence_after();
+        tc::tmem_dealloc(tmem, TMEM_COLS);
+    }
+}
+
+// sum the split-K partials and apply dividePublic3out3 (+ bias)
+__global__ void reduce_kernel(const __grid_constant__ Args g, int nsplit) {
+    const long long total = (long long)g.M * g.N;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        uint64_t zv = 0;
+        for (int s = 0; s < nsplit; s++) zv += g.partial[(long long)s * total + e];
+        const long long m = e / g.N;
+        const int n = (int)(e - m * g.N);
+        const long long idx = g.colmajor ? m + (long long)n * g.M : e;
+        const uint64_t vv = 1 + div_public<uint64_t>(zv - g.d, g.d, g.dshift);
+#pragma unroll
+        for (int ps = 0; ps < 6; ps++) {
+            uint64_t base = (ps == 0 || ps == 5) ? vv : 0;
+            if (g.bias[ps]) base += g.bias[ps][n];
+            g.out[ps][idx] = base;
+        }
+    }
+}
+
+// ------------------------------------------------------------------- host
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn(Ctx *c) {
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+        else
+            cudaGetLastError();
+    });
+    if (!fn) set_error(c, PG_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    return fn;
+}
+
+static void tile_geometry(Plan &p) {
+    if (!p.implicit) {
+        // rows of the image, 32 per tensor-map line
+        p.Wt = 1;
+        p.Ht = 1;
+        const int r32 = (p.M + 31) / 32 * 32;
+        p.Nt = r32 < BM ? r32 : BM;
+        p.tiles_w = 1;
+        p.tiles_h = 1;
+    } else {
+        // up to 32 output columns per line; then rows, then whole images, up to 128 pixels
+        p.Wt = p.Q < 32 ? p.Q : 32;
+        p.tiles_w = (p.Q + p.Wt - 1) / p.Wt;
+        p.Ht = p.P < BM / p.Wt ? p.P : BM / p.Wt;
+        p.Nt = 1;
+        if (p.Ht == p.P && p.tiles_w == 1) {
+            const int per = BM / (p.P * p.Wt);
+            p.Nt = per < p.Nimg ? per : p.Nimg;
+        }
+        p.tiles_h = (p.P + p.Ht - 1) / p.Ht;
+    }
+    p.R = p.Wt * p.Ht * p.Nt;
+    p.tiles_m = p.tiles_w * p.tiles_h * ((p.Nimg + p.Nt - 1) / p.Nt);
+}
+
+static void finish_plan(Plan &p) {
+    p.kblocks = p.C / BK * (p.implicit ? p.f * p.f : 1);
+    p.cblocks = p.C / BK;
+    p.ntiles_n = (p.N + BN - 1) / BN;
+    // the GEMM / im2col image is padded with zero rows to whole 32-row lines
+    p.pixels_alloc = p.implicit ? p.pixels : (p.pixels + 31) / 32 * 32;
+    p.image_bytes = 96ull * (size_t)p.C * (size_t)p.pixels_alloc;
+    p.packB_bytes = (size_t)6 * p.kblocks * p.ntiles_n * B_STAGE_BYTES;
+    tile_geometry(p);
+}
+
+int plan_gemm(Ctx *c, Plan &p, int M, int N, int K, int tA, int tB, int tC) {
+    memset(&p, 0, sizeof(p));
+    if (M <= 0 || N <= 0 || K <= 0) return set_error(c, PG_ERR_SIZE, "matmul: bad sizes");
+    p.implicit = 0;
+    p.M = M; p.N = N; p.Kreal = K;
+    p.C = (K + BK - 1) / BK * BK;
+    p.pixels = M;
+    p.src_mode = tA ? SRC_ROWS : SRC_COLS;
+    p.ld = tA ? K : M;
+    p.tB_kn = tB;
+    p.colmajor = !tC;
+    p.f = 1; p.pad = 0;
+    p.Wimg = 1; p.Himg = 1; p.Nimg = M;
+    p.P = 1; p.Q = 1;
+    finish_plan(p);
+    return PG_OK;
+}
+
+int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad) {
+    memset(&p, 0, sizeof(p));
+    if (batch <= 0 || H <= 0 || W <= 0 || f <= 0 || Din <= 0 || Dout <= 0 || stride <= 0 || pad < 0 ||
+        H + 2 * pad < f || W + 2 * pad < f)
+        return set_error(c, PG_ERR_SIZE, "convolution: bad geometry");
+    const int P = (H + 2 * pad - f) / stride + 1, Q = (W + 2 * pad - f) / stride + 1;
+    p.M = batch * P * Q;
+    p.N = Dout;
+    p.tB_kn = 0;  // KRSC filters: b[n * f*f*Din + k]
+    p.colmajor = 0;
+    p.H = H; p.W = W; p.Din = Din; p.stride = stride;
+    if (stride == 1 && Din % BK == 0 && Q <= BM && P <= H && Q <= W) {
+        // implicit: the image is the activation tensor itself, taps are box shifts
+        p.implicit = 1;
+        p.Kreal = Din;
+        p.C = Din;
+        p.pixels = (long long)batch * H * W;
+        p.src_mode = SRC_ROWS;
+        p.ld = Din;
+        p.f = f; p.pad = pad;
+        p.Wimg = W; p.Himg = H; p.Nimg = batch;
+        p.P = P; p.Q = Q;
+    } else {
+        // explicit: the image holds the im2col rows (K = f*f*Din padded to 16)
+        p.implicit = 0;
+        p.Kreal = f * f * Din;
+        p.C = (p.Kreal + BK - 1) / BK * BK;
+        p.pixels = p.M;
+        p.src_mode = SRC_IM2COL;
+        p.f = 1; p.pad = 0;
+        p.cf = f; p.cpad = pad; p.cP = P; p.cQ = Q;
+        p.Wimg = 1; p.Himg = 1; p.Nimg = p.M;
+        p.P = 1; p.Q = 1;
+    }
+    finish_plan(p);
+    return PG_OK;
+}
+
+void choose_split(const Plan &p, int sms, int &split, int &cps) {
+    const int total_stages = 6 * p.kblocks;
+    const int chunks = (total_stages + CHUNK_STAGES - 1) / CHUNK_STAGES;
+    const int tiles = p.tiles_m * p.ntiles_n;
+    split = tiles >= sms ? 1 : sms / tiles;
+    if (split > chunks) split = chunks;
+    if (split < 1) split = 1;
+    cps = (chunks + split - 1) / split;
+    split = (chunks + cps - 1) / cps;
+}
+
+size_t partial_bytes(const Plan &p, int split) { return split > 1 ? (size_t)split * p.M * p.N * 8 : 0; }
+
+int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image) {
+    ImageArgs ia;
+    memset(&ia, 0, sizeof(ia));
+    bool vec = p.src_mode == SRC_ROWS && p.ld % 2 == 0;
+    for (int i = 0; i < 6; i++) {
+        if (!a[i]) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+        ia.a[i] = a[i];
+        if (((uintptr_t)a[i] & 15) != 0) vec = false;
+    }
+    ia.mode = p.src_mode;
+    ia.pixels = p.pixels_alloc;
+    ia.pixels_src = p.pixels;
+    ia.C8 = p.C / 8;
+    ia.Kreal = p.Kreal;
+    ia.ld = p.ld;
+    ia.vec = vec && p.Kreal % 8 == 0;
+    ia.H = p.H; ia.W = p.W; ia.Din = p.Din; ia.f = p.cf; ia.stride = p.stride; ia.pad = p.cpad;
+    ia.P = p.cP; ia.Q = p.cQ;
+    ia.img = (uint4 *)image;
+    const long long units = 6ll * ia.C8 * p.pixels_alloc;
+    const int sms = c->sm_count > 0 ? c->sm_count : 148;
+    long long blocks = (units + 255) / 256;
+    if (blocks > (long long)sms * 32) blocks = (long long)sms * 32;
+    image_kernel<<<(unsigned)blocks, 256, 0, c->stream>>>(ia);
+    c->launches++;
+    return launch_status(c, "image_kernel");
+}
+
+int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB) {
+    PackArgs pa;
+    memset(&pa, 0, sizeof(pa));
+    for (int i = 0; i < 6; i++) {
+        if (!b[i]) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+        pa.b[i] = b[i];
+    }
+    pa.N = p.N;
+    pa.Kreal = p.implicit ? p.f * p.f * p.Din : p.Kreal;
+    pa.kblocks = p.kblocks;
+    pa.ntiles_n = p.ntiles_n;
+    pa.kn = p.tB_kn;
+    pa.packB = (uint8_t *)packB;
+    const long long units = 6ll * p.ntiles_n * BN * p.kblocks * 2;
+    const int sms = c->sm_count > 0 ? c->sm_count : 148;
+    long long blocks = (units + 255) / 256;
+    if (blocks > (long long)sms * 16) blocks = (long long)sms * 16;
+    pack_kernel<<<(unsigned)blocks, 256, 0, c->stream>>>(pa);
+    c->launches++;
+    return launch_status(c, "pack_kernel");
+}
+
+int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial, int split, int cps,
+             uint64_t *const out[6], const uint64_t *const bias[6], int trunc) {
+    {
+        static std::mutex mu;
+        static bool attr_done[64];
+        std::lock_guard<std::mutex> lock(mu);
+        if (c->device < 0 || c->device >= 64) return set_error(c, PG_ERR_UNSUPPORTED, "device ordinal %d", c->device);
+        if (!attr_done[c->device]) {
+            PG_CHECK_CUDA(c, cudaFuncSetAttribute(limb_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)smem_bytes()));
+            attr_done[c->device] = true;
+        }
+    }
+    if (trunc < 0 || trunc > 63) return set_error(c, PG_ERR_INVALID_ARG, "bad truncation %d", trunc);
+    if (((uintptr_t)image & 15) || ((uintptr_t)packB & 15))
+        return set_error(c, PG_ERR_INVALID_ARG, "limb buffers must be 16-byte aligned");
+    if (p.tiles_m > 65535) return set_error(c, PG_ERR_UNSUPPORTED, "M = %d has too many row tiles", p.M);
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn(c);
+    if (!enc) return PG_ERR_CUDA;
+    // image dims (innermost first): a line of pixels x 8 channels, rows, images,
+    // (segment, plane, channel group of 8)
+    alignas(64) CUtensorMap tm;
+    cuuint64_t dims[4];
+    cuuint64_t strides[3];
+    cuuint32_t box[4];
+    const cuuint64_t plane_stride = (cuuint64_t)p.pixels_alloc * 16;
+    if (p.implicit) {
+        dims[0] = 8 * (cuuint64_t)p.Wimg; dims[1] = p.Himg; dims[2] = p.Nimg; dims[3] = 48 * (cuuint64_t)(p.C / 8);
+        strides[0] = (cuuint64_t)p.Wimg * 16; strides[1] = (cuuint64_t)p.Himg * p.Wimg * 16; strides[2] = plane_stride;
+        box[0] = 8 * p.Wt; box[1] = p.Ht; box[2] = p.Nt; box[3] = 2;
+    } else {
+        dims[0] = 256; dims[1] = p.pixels_alloc / 32; dims[2] = 1; dims[3] = 48 * (cuuint64_t)(p.C / 8);
+        strides[0] = 512; strides[1] = plane_stride; strides[2] = plane_stride;
+        box[0] = 256; box[1] = p.Nt / 32; box[2] = 1; box[3] = 2;
+    }
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = enc(&tm, CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, const_cast<void *>(image), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(c, PG_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    Args g;
+    memset(&g, 0, sizeof(g));
+    g.M = p.M; g.N = p.N;
+    g.kblocks = p.kblocks; g.cblocks = p.cblocks; g.C8 = p.C / 8; g.f = p.f; g.pad = p.pad;
+    g.Wt = p.Wt; g.Ht = p.Ht; g.Nt = p.Nt; g.R = p.R; g.tiles_w = p.tiles_w; g.tiles_h = p.tiles_h;
+    g.rows_mode = !p.implicit;
+    g.P = p.P; g.Q = p.Q; g.Nimg = p.Nimg;
+    g.ntiles_n = p.ntiles_n;
+    g.total_stages = 6 * p.kblocks;
+    g.chunks_per_split = cps;
+    g.direct = split > 1 ? 0 : 1;
+    g.colmajor = p.colmajor;
+    g.a_box_bytes = 32u * (uint32_t)p.R;
+    g.packB = (const uint8_t *)packB;
+    g.partial = partial;
+    for (int i = 0; i < 6; i++) {
+        g.out[i] = out[i];
+        g.bias[i] = bias ? bias[i] : nullptr;
+    }
+    g.d = 1ull << trunc;
+    g.dshift = pow2_shift<uint64_t>(g.d);
+    g.err = device_error_word(c);
+    if (split > 1 && !partial) return set_error(c, PG_ERR_INVALID_ARG, "split-K needs a partial buffer");
+    dim3 grid(p.ntiles_n, p.tiles_m, split);
+    limb_tma_kernel<<<grid, NTHREADS, smem_bytes(), c->stream>>>(tm, g);
+    c->launches++;
+    int st = launch_status(c, "limb_tma_kernel");
+    if (st) return st;
+    if (split > 1) {
+        const long long total = (long long)p.M * p.N;
+        const int sms = c->sm_count > 0 ? c->sm_count : 148;
+        long long blocks = (total + 255) / 256;
+        if (blocks > (long long)sms * 8) blocks = (long long)sms * 8;
+        reduce_kernel<<<(unsigned)blocks, 256, 0, c->stream>>>(g, split);
+        c->launches++;
+        st = launch_status(c, "reduce_kernel");
+    }
+    return st;
+}
+
+}  // namespace lt
+
+// --------------------------------------------------- standalone entry points
+
+static int run_with_scratch(Ctx *c, const lt::Plan &p, const uint64_t *const a[6], const uint64_t *const b[6],
+                            uint64_t *const out[6], const uint64_t *const bias[6], int trunc) {
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    int split, cps;
+    lt::choose_split(p, c->sm_count > 0 ? c->sm_count : 148, split, cps);
+    const size_t ib = al(p.image_bytes), pb = al(p.packB_bytes), qb = al(lt::partial_bytes(p, split));
+    uint8_t *scr = (uint8_t *)scratch(c, ib + pb + qb);
+    if (!scr) return PG_ERR_NO_MEMORY;
+    int st = lt::run_image(c, p, a, scr);
+    if (!st) st = lt::run_pack(c, p, b, scr + ib);
+    if (!st)
+        st = lt::run_gemm(c, p, scr, scr + ib, split > 1 ? (uint64_t *)(scr + ib + pb) : nullptr, split, cps, out,
+                          bias, trunc);
+    if (st) return st;
+    comm_msg(c, 2ull * p.M * p.N * 8, 2ull * p.M * p.N * 8);
+    comm_round(c);
+    return PG_OK;
+}
+
+int limb3_rss_matmul_u64(Ctx *c, const uint64_t *const a[6], const uint64_t *const b[6], uint64_t *const out[6],
+                         const uint64_t *const bias[6], int M, int N, int K, int tA, int tB, int tC, int trunc) {
+    CSh6<uint64_t> ca, cb;
+    Sh6<uint64_t> co;
+    if (!load6(ca, a) || !load6(cb, b) || !load6(co, out)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    if (trunc < 0 || trunc > 63) return set_error(c, PG_ERR_INVALID_ARG, "bad truncation %d", trunc);
+    lt::Plan p;
+    int st = lt::plan_gemm(c, p, M, N, K, tA, tB, tC);
+    if (st) return st;
+    return run_with_scratch(c, p, a, b, out, bias, trunc);
+}
+
+template <typename T>
+int rss_conv(Ctx *, const T *const *, const T *const *, T *const *, int, int, int, int, int, int, int, int, int, int);
+
+int limb3_rss_conv_u64(Ctx *c, const uint64_t *const A[6], const uint64_t *const B[6], uint64_t *const C[6], int op,
+                       int batch, int H, int W, int f, int Din, int Dout, int stride, int pad, int trunc) {
+    if (op != PG_CONV_FPROP)  // the data-gradient and weight-gradient convolutions run on the integer CUDA cores
+        return rss_conv<uint64_t>(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc);
+    CSh6<uint64_t> ca, cb;
+    Sh6<uint64_t> co;
+    if (!load6(ca, A) || !load6(cb, B) || !load6(co, C)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    if (trunc < 0 || trunc > 63) return set_error(c, PG_ERR_INVALID_ARG, "bad truncation %d", trunc);
+    lt::Plan p;
+    int st = lt::plan_conv(c, p, batch, H, W, f, Din, Dout, stride, pad);
+    if (st) return st;
+    return run_with_scratch(c, p, A, B, C, nullptr, trunc);
+}
+
+}  // namespace pg

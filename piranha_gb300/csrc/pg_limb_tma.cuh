@@ -1,0 +1,43 @@
+// pg_limb_tma.cuh — host-side plan of the TMA-fed limb tensor-core share-GEMM
+// (pg_limb_tma.cu): problem geometry, the digit-plane image of A, the packed
+// weights, the tile rectangle, and the three launches (image, pack, GEMM).
+#pragma once
+
+#include <stddef.h>
+#include <stdint.h>
+
+namespace pg {
+struct Ctx;
+namespace lt {
+
+struct Plan {
+    int implicit;       // 1: image = activation tensor (taps are box shifts); 0: one image row per output row
+    int src_mode;       // how the image kernel reads A (rows, columns, im2col gather)
+    long long ld;       // row / column stride of A for rows / columns
+    long long pixels;   // image rows that come from A
+    long long pixels_alloc;  // image rows stored (a whole number of 32-row lines for the GEMM form)
+    int C;              // image channels (multiple of 16)
+    int Kreal;          // real channels of A per image row (image channels >= Kreal are 0)
+    int Wimg, Himg, Nimg;  // image tensor extents (W, H, images) seen by the tensor map
+    int H, W, Din, stride; // input geometry of a convolution
+    int cf, cpad, cP, cQ;  // convolution taps, padding and output extents for the im2col gather
+    int f, pad, P, Q;      // taps and output extents the GEMM kernel iterates (1, 0, 1, 1 unless implicit)
+    int M, N, kblocks, cblocks, ntiles_n;
+    int Wt, Ht, Nt, R, tiles_w, tiles_h, tiles_m;  // output-pixel rectangle of a tile, rows used
+    int tB_kn;          // weights as b[k * N + n] (1) or b[n * Kb + k] (0)
+    int colmajor;       // output column-major (GEMM with tC = 0)
+    size_t image_bytes, packB_bytes;
+};
+
+int plan_gemm(Ctx *c, Plan &p, int M, int N, int K, int tA, int tB, int tC);
+int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad);
+void choose_split(const Plan &p, int sms, int &split, int &chunks_per_split);
+size_t partial_bytes(const Plan &p, int split);
+// A shares -> digit-plane image; weight shares -> packed stage images; then the GEMM (+ split-K reduction)
+int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image);
+int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB);
+int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial, int split,
+             int chunks_per_split, uint64_t *const out[6], const uint64_t *const bias[6], int trunc);
+
+}  // namespace lt
+}  // namespace pg

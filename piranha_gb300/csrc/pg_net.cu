@@ -19,9 +19,9 @@ int rss_conv(Ctx *, const T *const *, const T *const *, T *const *, int, int, in
 template <typename T, typename U> int rss_relu(Ctx *, const T *const *, size_t, T *const *, U *const *);
 template <typename T, typename U>
 int rss_maxpool_layer(Ctx *, const T *const *, T *const *, U *const *, int, int, int, int, int, int, int);
-int limb_rss_matmul_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *,
+int limb3_rss_matmul_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *,
                         const uint64_t *const *, int, int, int, int, int, int, int);
-int limb_rss_conv_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *, int, int, int, int,
+int limb3_rss_conv_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *, int, int, int, int,
                       int, int, int, int, int, int);
 }  // namespace pg
 
@@ -71,7 +71,7 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
             case PG_LAYER_FC: {
                 const uint64_t *const *bias = L.b_n ? (const uint64_t *const *)L.b : nullptr;
                 st = c->form == PG_FORM_LIMB_TC
-                         ? limb_rss_matmul_u64(c, cur, (const uint64_t *const *)L.w, L.out, bias, net->batch, L.p[1],
+                         ? limb3_rss_matmul_u64(c, cur, (const uint64_t *const *)L.w, L.out, bias, net->batch, L.p[1],
                                                L.p[0], 1, 1, 1, net->fp)
                          : rss_matmul<uint64_t>(c, cur, (const uint64_t *const *)L.w, L.out, bias, net->batch, L.p[1],
                                                 L.p[0], 1, 1, 1, net->fp);
@@ -79,7 +79,7 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
             }
             case PG_LAYER_CNN:
                 st = c->form == PG_FORM_LIMB_TC
-                         ? limb_rss_conv_u64(c, cur, (const uint64_t *const *)L.w, L.out, PG_CONV_FPROP, net->batch,
+                         ? limb3_rss_conv_u64(c, cur, (const uint64_t *const *)L.w, L.out, PG_CONV_FPROP, net->batch,
                                              L.p[0], L.p[1], L.p[4], L.p[2], L.p[3], L.p[5], L.p[6], net->fp)
                          : rss_conv<uint64_t>(c, cur, (const uint64_t *const *)L.w, L.out, PG_CONV_FPROP, net->batch,
                                               L.p[0], L.p[1], L.p[4], L.p[2], L.p[3], L.p[5], L.p[6], net->fp);

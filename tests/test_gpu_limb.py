@@ -62,6 +62,7 @@ def test_tc_selftest(pg, ctx):
     (64, 256, 256, 0, 1, 0),    # A column-major, C column-major
     (32, 32, 2048, 1, 1, 1),    # split-K over many chunks
     (128, 10, 784, 1, 1, 1),    # SecureML-like output layer
+    (300, 20, 16, 1, 1, 1),     # M not a multiple of 32: zero rows pad the last line
 ])
 def test_limb_matmul(pg, ctx, M, N, K, tA, tB, tC):
     a, b = orc.random_views(M * K, U64, 3), orc.random_views(K * N, U64, 4)
@@ -75,8 +76,8 @@ def test_limb_matmul(pg, ctx, M, N, K, tA, tB, tC):
     assert cc["tx"] == comm.tx and cc["rounds"] == comm.rounds
 
 
-def test_limb_matmul_fallback_shape(pg, ctx):
-    M, N, K = 20, 30, 25  # K not a multiple of 16: runs on the integer CUDA cores
+def test_limb_matmul_odd_k(pg, ctx):
+    M, N, K = 20, 30, 25  # K not a multiple of 16: zero digits pad the contraction
     a, b = orc.random_views(M * K, U64, 5), orc.random_views(K * N, U64, 6)
     want = orc.matmul(a, b, M, N, K, 1, 1, 1, 20)
     c = pg.empty_shares(M * N)
@@ -85,9 +86,10 @@ def test_limb_matmul_fallback_shape(pg, ctx):
     assert np.array_equal(pg.to_host(c), want)
 
 
-@pytest.mark.parametrize("fill", [0, (1 << 64) - 1, 0x8080808080808080, 0x7F7F7F7F7F7F7F7F])
+@pytest.mark.parametrize("fill", [0, (1 << 64) - 1, 0x8080808080808080, 0x7F7F7F7F7F7F7F7F, 0x7F7F7F7F7F7F7F80])
 def test_limb_digit_extremes(pg, ctx, fill):
-    """Constant operands put every digit at an extreme: 0 -> all digits -128 (products 2^14)."""
+    """Constant operands put every digit at an extreme: 0x7F..7F80 has all digits -128, so every
+    product is 2^14 and each accumulator reaches exactly 2^24 per chunk."""
     M, N, K = 128, 64, 1024
     a = np.full((3, 2, M * K), fill, dtype=U64)
     b = np.full((3, 2, K * N), fill, dtype=U64)
@@ -104,6 +106,13 @@ def test_limb_digit_extremes(pg, ctx, fill):
     (2, 4, 4, 3, 64, 128, 1, 1),
     (1, 2, 2, 3, 128, 64, 1, 1),
     (2, 6, 6, 1, 16, 16, 1, 0),
+    (2, 8, 8, 3, 3, 64, 1, 1),      # Din = 3: im2col image, K = 27 padded to 32
+    (9, 4, 4, 3, 16, 16, 1, 1),     # whole-image tiles, the last one ragged
+    (1, 4, 4, 3, 16, 16, 1, 2),     # padding wider than the kernel reach: im2col image
+    (2, 12, 12, 5, 20, 50, 1, 0),   # LeNet-like 5x5, Din = 20
+    (1, 32, 32, 3, 64, 64, 1, 1),   # one VGG row tile: 4 rows x 32 columns
+    (1, 5, 40, 3, 16, 16, 1, 1),    # wider than one 32-pixel line: tiles along w
+    (1, 3, 70, 1, 16, 8, 1, 0),     # ragged last w tile
 ])
 def test_limb_conv(pg, ctx, batch, H, W, f, Din, Dout, stride, pad):
     A = orc.random_views(batch * H * W * Din, U64, 7)
