@@ -12,9 +12,8 @@
 // The value 0 has all digits 0, so zero padding (tensor-map out-of-bounds
 // fill, ragged tiles) stands for the value 0. A digit product is at most 2^14
 // in magnitude; a diagonal has at most 8 pairs, so draining the fp32
-// accumulators every 128 K' (diagonals 4-7) or 256 K' (diagonals 0-3, at most
-// 4 pairs) keeps every partial sum an integer of magnitude <= 2^24, exact in
-// fp32.
+// accumulators every 128 K' keeps every partial sum an integer of magnitude
+// <= 2^24, exact in fp32.
 //
 // Operands. A (activations, or the GEMM's left operand) is first written by
 // image_kernel as an image of digit planes in global memory,
@@ -36,9 +35,11 @@
 // Roles (320 threads): warp 0 issues the TMA and bulk copies of each stage,
 // warp 1 owns tensor memory and one lane issues the MMAs, warps 2-9 drain the
 // accumulators (two warps per 32-lane quarter, 32 columns each) and run the
-// epilogue. Each output tile runs two passes over K' (high digit diagonals
-// 4-7, needed modulo 2^32, then 0-3 with digits 0-3 only), each pass with two
-// tensor-memory buffers of four 64-column accumulators. Every mbarrier wait
+// epilogue. Each output tile makes one pass over K' with all eight digit
+// diagonals in tensor memory (8 x 64 columns); every 128 K' the epilogue
+// drains them into 64-bit registers while the producer keeps loading the
+// next stages (loading, not the tensor pipe, bounds this kernel, so the MMA
+// waiting for the drain costs little). Every mbarrier wait
 // is bounded; on a timeout the kernel records an error word, stops issuing,
 // waits for its own copies and MMAs, and frees tensor memory.
 #include <cuda.h>
@@ -57,14 +58,14 @@ int *device_error_word(Ctx *c);
 namespace lt {
 
 constexpr int BM = 128, BN = 64, BK = 16, STAGES = 4;
-constexpr int CHUNK_STAGES = 8, CHUNK_STAGES_LO = 16;
+constexpr int CHUNK_STAGES = 8;  // K' of 128 per accumulator drain
 constexpr int A_PLANE_BYTES = BM * BK * 2;                      // 4096
 constexpr int B_PLANE_BYTES = BN * BK * 2;                      // 2048
 constexpr int B_STAGE_BYTES = 8 * B_PLANE_BYTES;                // 16384
 constexpr int STAGE_BYTES = 8 * A_PLANE_BYTES + B_STAGE_BYTES;  // 49152
 constexpr int NTHREADS = 320;
 constexpr int W_PROD = 0, W_MMA = 1, W_EPI0 = 2;
-constexpr uint32_t TMEM_COLS = 512;  // 2 buffers x 4 diagonals x 64 columns
+constexpr uint32_t TMEM_COLS = 512;  // 8 diagonals x 64 columns
 constexpr uint64_t DIGIT_OFFSET = 0x8080808080808080ull;
 constexpr uint64_t WAIT_NS = 2000000000ull;  // 2 s bound on any single wait
 
@@ -88,7 +89,7 @@ struct Args {
 struct __align__(16) Smem {
     uint8_t stage[STAGES][STAGE_BYTES];
     Args args;
-    uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], done;
+    uint64_t full[STAGES], empty[STAGES], acc_full, acc_empty, done;
     uint32_t tmem_base;
     int abort;
     int never;  // stays 0: a wait that must not be cut short by the abort flag
@@ -275,44 +276,30 @@ __device__ __forceinline__ void flag_error(Smem &sm, const Args &g, int code) {
     if (g.err) atomicCAS(g.err, 0, code);
 }
 
-// All MMAs of one stage for diagonals D0..D0+3: for A digit plane i, the B
-// planes j = jlo..jhi with i + j in range are adjacent in shared memory and
-// their products go to adjacent accumulators, so one MMA with N = 64 * cnt
-// covers them (8 MMAs per stage in the high pass, 4 in the low pass).
-template <int D0>
+// All MMAs of one stage. For A digit plane i, the B planes j = 0..7-i (the
+// pairs with i + j < 8) are adjacent in shared memory and their products go
+// to the adjacent accumulators of diagonals i..7, so at most two MMAs (N up
+// to 256 each) cover them: 12 MMAs per stage for the 36 pairs.
 __device__ __forceinline__ void issue_stage(uint32_t acc, uint64_t adesc, uint64_t bdesc, bool first_stage) {
 #pragma unroll
     for (int i = 0; i < 8; i++) {
-        const int jlo = D0 - i > 0 ? D0 - i : 0;
-        const int jhi = D0 + 3 - i;
-        const int cnt = jhi - jlo + 1;
-        if (cnt <= 0) continue;
         const uint64_t ad = adesc + (uint64_t)((i * A_PLANE_BYTES) >> 4);
-        const uint64_t bd = bdesc + (uint64_t)((jlo * B_PLANE_BYTES) >> 4);
-        const uint32_t d = acc + (uint32_t)((i + jlo - D0) * BN);
-        const uint32_t accum = (!first_stage || i > 0) ? 1u : 0u;  // i = 0 writes all four accumulators first
-        tc::mma_f16(d, ad, bd, tc::idesc_f16_f32(BM, BN * cnt), accum);
+        const uint32_t accum = (!first_stage || i > 0) ? 1u : 0u;  // i = 0 writes all eight accumulators first
+#pragma unroll
+        for (int j0 = 0; j0 < 8 - i; j0 += 4) {
+            const int cnt = (8 - i - j0) < 4 ? (8 - i - j0) : 4;
+            tc::mma_f16(acc + (uint32_t)((i + j0) * BN), ad, bdesc + (uint64_t)((j0 * B_PLANE_BYTES) >> 4),
+                        tc::idesc_f16_f32(BM, BN * cnt), accum);
+        }
     }
 }
 
 __device__ __forceinline__ int f2i(uint32_t x) { return __float2int_rz(__uint_as_float(x)); }
 
-// Diagonals 4-7 (shift >= 32) matter only modulo 2^32 of their sum
-// D4 + 2^8 D5 + 2^16 D6 + 2^24 D7, which goes to the high word of the
-// running 64-bit sum.
-__device__ __forceinline__ void drain_hi(uint32_t taddr, uint64_t (&acc)[32]) {
-#pragma unroll
-    for (int a = 0; a < 4; a++) {
-        uint32_t r[32];
-        tc::tmem_ld32(taddr + (uint32_t)(a * BN), r);
-        tc::tmem_wait_ld();
-#pragma unroll
-        for (int j = 0; j < 32; j++) acc[j] += (uint64_t)((uint32_t)f2i(r[j]) << (8 * a)) << 32;
-    }
-}
-
-// Diagonals 0-3 in full 64-bit precision, one accumulator at a time.
-__device__ __forceinline__ void drain_lo(uint32_t taddr, uint64_t (&acc)[32]) {
+// Move the eight diagonal accumulators of this thread's 32 columns into the
+// running 64-bit sums, one accumulator at a time: diagonals 0-3 in full
+// 64-bit precision, diagonals 4-7 (shift >= 32) only into the high word.
+__device__ __forceinline__ void drain8(uint32_t taddr, uint64_t (&acc)[32]) {
 #pragma unroll
     for (int a = 0; a < 4; a++) {
         uint32_t r[32];
@@ -326,6 +313,14 @@ __device__ __forceinline__ void drain_lo(uint32_t taddr, uint64_t (&acc)[32]) {
             asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(t) : "r"(dv), "r"(1 << (8 * a)), "l"(acc[j]));
             acc[j] = t;
         }
+    }
+#pragma unroll
+    for (int a = 4; a < 8; a++) {
+        uint32_t r[32];
+        tc::tmem_ld32(taddr + (uint32_t)(a * BN), r);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 32; j++) acc[j] += (uint64_t)((uint32_t)f2i(r[j]) << (8 * (a - 4))) << 32;
     }
 }
 
@@ -382,10 +377,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             tc::mbar_init(tc::smem_u32(&sm.full[s]), 1);
             tc::mbar_init(tc::smem_u32(&sm.empty[s]), 1);
         }
-        for (int b = 0; b < 2; b++) {
-            tc::mbar_init(tc::smem_u32(&sm.acc_full[b]), 1);
-            tc::mbar_init(tc::smem_u32(&sm.acc_empty[b]), 256);
-        }
+        tc::mbar_init(tc::smem_u32(&sm.acc_full), 1);
+        tc::mbar_init(tc::smem_u32(&sm.acc_empty), 256);
         tc::mbar_init(tc::smem_u32(&sm.done), 1);
         sm.abort = 0;
         sm.never = 0;
@@ -415,9 +408,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
             int issued = 0;
             bool ok = true;
-            for (int git = 0; git < 2 * nst; git++) {
-                const bool lo = git >= nst;
-                const int it = lo ? git - nst : git;
+            for (int git = 0; git < nst; git++) {
                 const int s = git % STAGES;
                 const uint32_t ph = (uint32_t)(git / STAGES) & 1;
                 if (!tc::mbar_wait(tc::smem_u32(&sm.empty[s]), ph ^ 1, &sm.abort, WAIT_NS)) {
@@ -425,23 +416,21 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     ok = false;
                     break;
                 }
-                const int gst = stage_begin + it;
+                const int gst = stage_begin + git;
                 const int seg = gst / g.kblocks, kb = gst - seg * g.kblocks;
                 const int tap = kb / g.cblocks, cb = kb - tap * g.cblocks;
                 const int r = tap / g.f, sx = tap - r * g.f;
-                const int nplanes = lo ? 4 : 8;
                 const uint32_t bar = tc::smem_u32(&sm.full[s]);
-                const uint32_t bbytes = lo ? B_STAGE_BYTES / 2 : B_STAGE_BYTES;  // digits 0-3 lead the image
-                tc::mbar_arrive_expect_tx(bar, nplanes * g.a_box_bytes + bbytes);
+                tc::mbar_arrive_expect_tx(bar, 8 * g.a_box_bytes + B_STAGE_BYTES);
                 const uint32_t dst = tc::smem_u32(sm.stage[s]);
                 // line offset (16 bytes per pixel, so always 16-byte aligned), row, image
                 const int x = g.rows_mode ? 0 : 8 * (w0 + sx - g.pad);
                 const int y = g.rows_mode ? n0 >> 5 : h0 + r - g.pad;
                 const int zc = g.rows_mode ? 0 : n0;
-                for (int i = 0; i < nplanes; i++)
+                for (int i = 0; i < 8; i++)
                     tma_load_4d(dst + i * A_PLANE_BYTES, &tmA, x, y, zc, (seg * 8 + i) * g.C8 + 2 * cb, bar);
                 const uint8_t *src = g.packB + ((size_t)gst * g.ntiles_n + blockIdx.x) * B_STAGE_BYTES;
-                tc::bulk_g2s(dst + 8 * A_PLANE_BYTES, src, bbytes, bar);
+                tc::bulk_g2s(dst + 8 * A_PLANE_BYTES, src, B_STAGE_BYTES, bar);
                 issued = git + 1;
             }
             if (!ok) {
@@ -459,40 +448,32 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const uint32_t s0 = tc::smem_u32(sm.stage[0]);
             const uint64_t adesc0 = tc::smem_desc(s0, g.a_box_bytes / 2, 128);  // K chunks one box half apart
             const uint64_t bdesc0 = tc::smem_desc(s0 + 8 * A_PLANE_BYTES, 128, 256);
-            int git = 0, gc = 0;
+            const int nch = (nst + CHUNK_STAGES - 1) / CHUNK_STAGES;
+            int git = 0;
             bool ok = true;
-            for (int pass = 0; pass < 2 && ok; pass++) {
-                const bool lo = pass == 1;
-                const int cstages = lo ? CHUNK_STAGES_LO : CHUNK_STAGES;
-                const int nch = (nst + cstages - 1) / cstages;
-                for (int c = 0; c < nch && ok; c++, gc++) {
-                    const int buf = gc & 1;
-                    if (gc >= 2 && !tc::mbar_wait(tc::smem_u32(&sm.acc_empty[buf]), (uint32_t)((gc - 2) >> 1) & 1,
-                                                  &sm.abort, WAIT_NS)) {
-                        flag_error(sm, g, 0x200 + buf);
+            for (int c = 0; c < nch && ok; c++) {
+                // the accumulators are free once the epilogue has drained chunk c - 1
+                if (c >= 1 && !tc::mbar_wait(tc::smem_u32(&sm.acc_empty), (uint32_t)(c - 1) & 1, &sm.abort, WAIT_NS)) {
+                    flag_error(sm, g, 0x200);
+                    break;
+                }
+                tc::tc_fence_after();
+                const int cst = (nst - c * CHUNK_STAGES) < CHUNK_STAGES ? nst - c * CHUNK_STAGES : CHUNK_STAGES;
+                for (int st = 0; st < cst; st++, git++) {
+                    const int s = git % STAGES;
+                    const uint32_t ph = (uint32_t)(git / STAGES) & 1;
+                    if (!tc::mbar_wait(tc::smem_u32(&sm.full[s]), ph, &sm.abort, WAIT_NS)) {
+                        flag_error(sm, g, 0x300 + s);
                         ok = false;
                         break;
                     }
                     tc::tc_fence_after();
-                    const uint32_t acc = tmem + (uint32_t)(buf * 4 * BN);
-                    const int cst = (nst - c * cstages) < cstages ? nst - c * cstages : cstages;
-                    for (int st = 0; st < cst; st++, git++) {
-                        const int s = git % STAGES;
-                        const uint32_t ph = (uint32_t)(git / STAGES) & 1;
-                        if (!tc::mbar_wait(tc::smem_u32(&sm.full[s]), ph, &sm.abort, WAIT_NS)) {
-                            flag_error(sm, g, 0x300 + s);
-                            ok = false;
-                            break;
-                        }
-                        tc::tc_fence_after();
-                        const uint64_t off = (uint64_t)((s * STAGE_BYTES) >> 4);
-                        if (lo) issue_stage<0>(acc, adesc0 + off, bdesc0 + off, st == 0);
-                        else issue_stage<4>(acc, adesc0 + off, bdesc0 + off, st == 0);
-                        tc::mma_commit(tc::smem_u32(&sm.empty[s]));
-                    }
-                    if (!ok) break;
-                    tc::mma_commit(tc::smem_u32(&sm.acc_full[buf]));
+                    const uint64_t off = (uint64_t)((s * STAGE_BYTES) >> 4);
+                    issue_stage(tmem, adesc0 + off, bdesc0 + off, st == 0);
+                    tc::mma_commit(tc::smem_u32(&sm.empty[s]));
                 }
+                if (!ok) break;
+                tc::mma_commit(tc::smem_u32(&sm.acc_full));
             }
             tc::mma_commit(tc::smem_u32(&sm.done));
             if (!tc::mbar_wait(tc::smem_u32(&sm.done), 0, &sm.never, WAIT_NS) && g.err) atomicCAS(g.err, 0, 0x400);
@@ -507,33 +488,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll
         for (int j = 0; j < 32; j++) zs[j] = 0;
         const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(colh * 32);
-        const int nch_hi = (nst + CHUNK_STAGES - 1) / CHUNK_STAGES;
-        const int nch_lo = (nst + CHUNK_STAGES_LO - 1) / CHUNK_STAGES_LO;
-        // chunk gc uses tensor-memory buffer gc & 1; its (gc >> 1)-th fill
-        auto wait_chunk = [&](int gc) -> bool {
-            if (!tc::mbar_wait(tc::smem_u32(&sm.acc_full[gc & 1]), (uint32_t)(gc >> 1) & 1, &sm.abort, WAIT_NS)) {
+        const int nch = (nst + CHUNK_STAGES - 1) / CHUNK_STAGES;
+#pragma unroll 1
+        for (int c = 0; c < nch; c++) {
+            if (!tc::mbar_wait(tc::smem_u32(&sm.acc_full), (uint32_t)c & 1, &sm.abort, WAIT_NS)) {
                 flag_error(sm, g, 0x500);
-                return false;
+                break;
             }
             tc::tc_fence_after();
-            return true;
-        };
-        auto release_chunk = [&](int gc) {
+            drain8(taddr, zs);
             tc::tc_fence_before();
-            tc::mbar_arrive(tc::smem_u32(&sm.acc_empty[gc & 1]));
-        };
-        bool ok = true;
-#pragma unroll 1
-        for (int gc = 0; gc < nch_hi && ok; gc++) {
-            if (!(ok = wait_chunk(gc))) break;
-            drain_hi(taddr + (uint32_t)((gc & 1) * 4 * BN), zs);
-            release_chunk(gc);
-        }
-#pragma unroll 1
-        for (int gc = nch_hi; gc < nch_hi + nch_lo && ok; gc++) {
-            if (!(ok = wait_chunk(gc))) break;
-            drain_lo(taddr + (uint32_t)((gc & 1) * 4 * BN), zs);
-            release_chunk(gc);
+            tc::mbar_arrive(tc::smem_u32(&sm.acc_empty));
         }
         if (!sm.abort && row < g.R) {
             const int wh = g.Wt * g.Ht;
