@@ -11,9 +11,9 @@
 // with no correction terms, and only the 36 digit pairs with i+j < 8 matter.
 // The value 0 has all digits 0, so zero padding (tensor-map out-of-bounds
 // fill, ragged tiles) stands for the value 0. A digit product is at most 2^14
-// in magnitude; a diagonal has at most 8 pairs, so draining the fp32
-// accumulators every 128 K' keeps every partial sum an integer of magnitude
-// <= 2^24, exact in fp32.
+// in magnitude; diagonals 4-7 have at most 8 pairs and are drained every
+// 128 K', diagonals 0-3 at most 4 pairs and are drained every 256 K', so
+// every partial sum is an integer of magnitude <= 2^24, exact in fp32.
 //
 // Operands. A (activations, or the GEMM's left operand) is first written by
 // image_kernel as an image of digit planes in global memory,
@@ -36,10 +36,10 @@
 // warp 1 owns tensor memory and one lane issues the MMAs, warps 2-9 drain the
 // accumulators (two warps per 32-lane quarter, 32 columns each) and run the
 // epilogue. Each output tile makes one pass over K' with all eight digit
-// diagonals in tensor memory (8 x 64 columns); every 128 K' the epilogue
-// drains them into 64-bit registers while the producer keeps loading the
-// next stages (loading, not the tensor pipe, bounds this kernel, so the MMA
-// waiting for the drain costs little). Every mbarrier wait
+// diagonals in tensor memory (8 x 64 columns) in two groups, diagonals 0-3
+// and 4-7, whose drains into 64-bit registers are staggered: while the
+// epilogue drains one group, the MMAs of the other group run ahead over the
+// stages already loaded. Every mbarrier wait
 // is bounded; on a timeout the kernel records an error word, stops issuing,
 // waits for its own copies and MMAs, and frees tensor memory.
 #include <cuda.h>
@@ -58,7 +58,12 @@ int *device_error_word(Ctx *c);
 namespace lt {
 
 constexpr int BM = 128, BN = 64, BK = 16, STAGES = 4;
-constexpr int CHUNK_STAGES = 8;  // K' of 128 per accumulator drain
+// Accumulator drains: diagonals 4-7 (up to 8 pairs) every 128 K', diagonals
+// 0-3 (up to 4 pairs) every 256 K', with the low group's boundaries falling
+// between the high group's (its first chunk is 192 K').
+constexpr int CHUNK_STAGES = 8;     // high group, and the split-K granule
+constexpr int CHUNK_STAGES_LO = 16;
+constexpr int LO_FIRST = 12;
 constexpr int A_PLANE_BYTES = BM * BK * 2;                      // 4096
 constexpr int B_PLANE_BYTES = BN * BK * 2;                      // 2048
 constexpr int B_STAGE_BYTES = 8 * B_PLANE_BYTES;                // 16384
@@ -89,7 +94,7 @@ struct Args {
 struct __align__(16) Smem {
     uint8_t stage[STAGES][STAGE_BYTES];
     Args args;
-    uint64_t full[STAGES], empty[STAGES], acc_full, acc_empty, done;
+    uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], done;  // [0] low group, [1] high group
     uint32_t tmem_base;
     int abort;
     int never;  // stays 0: a wait that must not be cut short by the abort flag
@@ -276,30 +281,36 @@ __device__ __forceinline__ void flag_error(Smem &sm, const Args &g, int code) {
     if (g.err) atomicCAS(g.err, 0, code);
 }
 
-// All MMAs of one stage. For A digit plane i, the B planes j = 0..7-i (the
-// pairs with i + j < 8) are adjacent in shared memory and their products go
-// to the adjacent accumulators of diagonals i..7, so at most two MMAs (N up
-// to 256 each) cover them: 12 MMAs per stage for the 36 pairs.
-__device__ __forceinline__ void issue_stage(uint32_t acc, uint64_t adesc, uint64_t bdesc, bool first_stage) {
+// The MMAs of one stage for the low diagonals 0-3 (columns 0-255): for A
+// digit plane i < 4 the B planes j = 0..3-i are adjacent in shared memory and
+// their products go to the adjacent accumulators of diagonals i..3, so one
+// MMA with N = 64 (4 - i) covers them. i = 0 writes all four accumulators.
+__device__ __forceinline__ void issue_lo(uint32_t acc, uint64_t adesc, uint64_t bdesc, bool first_stage) {
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+        tc::mma_f16(acc + (uint32_t)(i * BN), adesc + (uint64_t)((i * A_PLANE_BYTES) >> 4), bdesc,
+                    tc::idesc_f16_f32(BM, BN * (4 - i)), (!first_stage || i > 0) ? 1u : 0u);
+}
+
+// The MMAs of one stage for the high diagonals 4-7 (columns 256-511): for A
+// plane i the B planes j = max(0, 4-i)..7-i, one MMA each (8 per stage).
+__device__ __forceinline__ void issue_hi(uint32_t acc, uint64_t adesc, uint64_t bdesc, bool first_stage) {
 #pragma unroll
     for (int i = 0; i < 8; i++) {
-        const uint64_t ad = adesc + (uint64_t)((i * A_PLANE_BYTES) >> 4);
-        const uint32_t accum = (!first_stage || i > 0) ? 1u : 0u;  // i = 0 writes all eight accumulators first
-#pragma unroll
-        for (int j0 = 0; j0 < 8 - i; j0 += 4) {
-            const int cnt = (8 - i - j0) < 4 ? (8 - i - j0) : 4;
-            tc::mma_f16(acc + (uint32_t)((i + j0) * BN), ad, bdesc + (uint64_t)((j0 * B_PLANE_BYTES) >> 4),
-                        tc::idesc_f16_f32(BM, BN * cnt), accum);
-        }
+        const int jlo = 4 - i > 0 ? 4 - i : 0;
+        const int cnt = 8 - i < 4 ? 8 - i : 4;
+        tc::mma_f16(acc + (uint32_t)((i + jlo) * BN), adesc + (uint64_t)((i * A_PLANE_BYTES) >> 4),
+                    bdesc + (uint64_t)((jlo * B_PLANE_BYTES) >> 4), tc::idesc_f16_f32(BM, BN * cnt),
+                    (!first_stage || i > 0) ? 1u : 0u);
     }
 }
 
 __device__ __forceinline__ int f2i(uint32_t x) { return __float2int_rz(__uint_as_float(x)); }
 
-// Move the eight diagonal accumulators of this thread's 32 columns into the
-// running 64-bit sums, one accumulator at a time: diagonals 0-3 in full
-// 64-bit precision, diagonals 4-7 (shift >= 32) only into the high word.
-__device__ __forceinline__ void drain8(uint32_t taddr, uint64_t (&acc)[32]) {
+// Move accumulators into the running 64-bit sums of this thread's 32
+// columns, one accumulator at a time. Low group: diagonals 0-3 in full 64-bit
+// precision. High group: diagonals 4-7 (shift >= 32) only into the high word.
+__device__ __forceinline__ void drain_lo(uint32_t taddr, uint64_t (&acc)[32]) {
 #pragma unroll
     for (int a = 0; a < 4; a++) {
         uint32_t r[32];
@@ -314,6 +325,8 @@ __device__ __forceinline__ void drain8(uint32_t taddr, uint64_t (&acc)[32]) {
             acc[j] = t;
         }
     }
+}
+__device__ __forceinline__ void drain_hi(uint32_t taddr, uint64_t (&acc)[32]) {
 #pragma unroll
     for (int a = 4; a < 8; a++) {
         uint32_t r[32];
@@ -322,6 +335,11 @@ __device__ __forceinline__ void drain8(uint32_t taddr, uint64_t (&acc)[32]) {
 #pragma unroll
         for (int j = 0; j < 32; j++) acc[j] += (uint64_t)((uint32_t)f2i(r[j]) << (8 * (a - 4))) << 32;
     }
+}
+
+// number of low-group chunks of a K' range of nst stages
+__device__ __forceinline__ int lo_chunks(int nst) {
+    return nst <= 0 ? 0 : nst <= LO_FIRST ? 1 : 1 + (nst - LO_FIRST + CHUNK_STAGES_LO - 1) / CHUNK_STAGES_LO;
 }
 
 // 32 columns of one output row: store the slice's partial Z, or apply
@@ -377,8 +395,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             tc::mbar_init(tc::smem_u32(&sm.full[s]), 1);
             tc::mbar_init(tc::smem_u32(&sm.empty[s]), 1);
         }
-        tc::mbar_init(tc::smem_u32(&sm.acc_full), 1);
-        tc::mbar_init(tc::smem_u32(&sm.acc_empty), 256);
+        for (int b = 0; b < 2; b++) {
+            tc::mbar_init(tc::smem_u32(&sm.acc_full[b]), 1);
+            tc::mbar_init(tc::smem_u32(&sm.acc_empty[b]), 256);
+        }
         tc::mbar_init(tc::smem_u32(&sm.done), 1);
         sm.abort = 0;
         sm.never = 0;
@@ -448,32 +468,58 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const uint32_t s0 = tc::smem_u32(sm.stage[0]);
             const uint64_t adesc0 = tc::smem_desc(s0, g.a_box_bytes / 2, 128);  // K chunks one box half apart
             const uint64_t bdesc0 = tc::smem_desc(s0 + 8 * A_PLANE_BYTES, 128, 256);
-            const int nch = (nst + CHUNK_STAGES - 1) / CHUNK_STAGES;
-            int git = 0;
-            bool ok = true;
-            for (int c = 0; c < nch && ok; c++) {
-                // the accumulators are free once the epilogue has drained chunk c - 1
-                if (c >= 1 && !tc::mbar_wait(tc::smem_u32(&sm.acc_empty), (uint32_t)(c - 1) & 1, &sm.abort, WAIT_NS)) {
-                    flag_error(sm, g, 0x200);
-                    break;
+            // Two cursors over the stage ring, one per accumulator group. A group
+            // at a chunk boundary waits for the epilogue to drain it while the
+            // other group runs on over the stages already loaded; a stage is
+            // released once both groups have issued their MMAs for it.
+            int cur[2] = {0, 0};           // next stage per group (0 low, 1 high)
+            int cstart[2] = {0, 0};        // first stage of the group's current chunk
+            int cend[2] = {nst < LO_FIRST ? nst : LO_FIRST, nst < CHUNK_STAGES ? nst : CHUNK_STAGES};
+            int chunk[2] = {0, 0};         // chunks committed so far
+            bool drained[2] = {true, true};
+            int rel = 0;
+            uint64_t t_idle = 0;
+            while (cur[0] < nst || cur[1] < nst) {
+                bool prog = false;
+#pragma unroll
+                for (int gi = 0; gi < 2; gi++) {
+                    const int t = cur[gi];
+                    if (t >= nst) continue;
+                    if (!drained[gi]) {
+                        if (!tc::mbar_try_wait(tc::smem_u32(&sm.acc_empty[gi]), (uint32_t)(chunk[gi] - 1) & 1)) continue;
+                        drained[gi] = true;
+                    }
+                    if (!tc::mbar_try_wait(tc::smem_u32(&sm.full[t % STAGES]), (uint32_t)(t / STAGES) & 1)) continue;
+                    tc::tc_fence_after();
+                    const uint64_t off = (uint64_t)(((t % STAGES) * STAGE_BYTES) >> 4);
+                    if (gi == 0) issue_lo(tmem, adesc0 + off, bdesc0 + off, t == cstart[0]);
+                    else issue_hi(tmem, adesc0 + off, bdesc0 + off, t == cstart[1]);
+                    cur[gi] = t + 1;
+                    prog = true;
+                    if (cur[gi] == cend[gi]) {
+                        tc::mma_commit(tc::smem_u32(&sm.acc_full[gi]));
+                        chunk[gi]++;
+                        drained[gi] = false;
+                        cstart[gi] = cur[gi];
+                        const int len = gi == 0 ? CHUNK_STAGES_LO : CHUNK_STAGES;
+                        cend[gi] = nst < cur[gi] + len ? nst : cur[gi] + len;
+                    }
                 }
-                tc::tc_fence_after();
-                const int cst = (nst - c * CHUNK_STAGES) < CHUNK_STAGES ? nst - c * CHUNK_STAGES : CHUNK_STAGES;
-                for (int st = 0; st < cst; st++, git++) {
-                    const int s = git % STAGES;
-                    const uint32_t ph = (uint32_t)(git / STAGES) & 1;
-                    if (!tc::mbar_wait(tc::smem_u32(&sm.full[s]), ph, &sm.abort, WAIT_NS)) {
-                        flag_error(sm, g, 0x300 + s);
-                        ok = false;
+                // release the stages both groups are done with (only stages that are reloaded)
+                const int done_both = cur[0] < cur[1] ? cur[0] : cur[1];
+                for (; rel < done_both; rel++)
+                    if (rel < nst - STAGES) tc::mma_commit(tc::smem_u32(&sm.empty[rel % STAGES]));
+                if (prog) {
+                    t_idle = 0;
+                } else {
+                    if (sm.abort) break;
+                    const uint64_t now = tc::globaltimer();
+                    if (t_idle == 0) t_idle = now;
+                    else if (now - t_idle > WAIT_NS) {
+                        flag_error(sm, g, 0x300);
                         break;
                     }
-                    tc::tc_fence_after();
-                    const uint64_t off = (uint64_t)((s * STAGE_BYTES) >> 4);
-                    issue_stage(tmem, adesc0 + off, bdesc0 + off, st == 0);
-                    tc::mma_commit(tc::smem_u32(&sm.empty[s]));
                 }
-                if (!ok) break;
-                tc::mma_commit(tc::smem_u32(&sm.acc_full));
             }
             tc::mma_commit(tc::smem_u32(&sm.done));
             if (!tc::mbar_wait(tc::smem_u32(&sm.done), 0, &sm.never, WAIT_NS) && g.err) atomicCAS(g.err, 0, 0x400);
@@ -488,17 +534,32 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll
         for (int j = 0; j < 32; j++) zs[j] = 0;
         const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(colh * 32);
-        const int nch = (nst + CHUNK_STAGES - 1) / CHUNK_STAGES;
-#pragma unroll 1
-        for (int c = 0; c < nch; c++) {
-            if (!tc::mbar_wait(tc::smem_u32(&sm.acc_full), (uint32_t)c & 1, &sm.abort, WAIT_NS)) {
-                flag_error(sm, g, 0x500);
-                break;
+        // drain each group's chunks in order, whichever group is ready first
+        const int nch[2] = {lo_chunks(nst), (nst + CHUNK_STAGES - 1) / CHUNK_STAGES};
+        int done_ch[2] = {0, 0};
+        uint64_t t_idle = 0;
+        while (done_ch[0] < nch[0] || done_ch[1] < nch[1]) {
+            int gi = -1;
+            if (done_ch[1] < nch[1] && tc::mbar_try_wait(tc::smem_u32(&sm.acc_full[1]), (uint32_t)done_ch[1] & 1)) gi = 1;
+            else if (done_ch[0] < nch[0] && tc::mbar_try_wait(tc::smem_u32(&sm.acc_full[0]), (uint32_t)done_ch[0] & 1))
+                gi = 0;
+            if (gi < 0) {
+                if (sm.abort) break;
+                const uint64_t now = tc::globaltimer();
+                if (t_idle == 0) t_idle = now;
+                else if (now - t_idle > WAIT_NS) {
+                    flag_error(sm, g, 0x500);
+                    break;
+                }
+                continue;
             }
+            t_idle = 0;
             tc::tc_fence_after();
-            drain8(taddr, zs);
+            if (gi == 0) drain_lo(taddr, zs);
+            else drain_hi(taddr, zs);
             tc::tc_fence_before();
-            tc::mbar_arrive(tc::smem_u32(&sm.acc_empty));
+            tc::mbar_arrive(tc::smem_u32(&sm.acc_empty[gi]));
+            done_ch[gi]++;
         }
         if (!sm.abort && row < g.R) {
             const int wh = g.Wt * g.Ht;

@@ -63,6 +63,7 @@ def test_tc_selftest(pg, ctx):
     (32, 32, 2048, 1, 1, 1),    # split-K over many chunks
     (128, 10, 784, 1, 1, 1),    # SecureML-like output layer
     (300, 20, 16, 1, 1, 1),     # M not a multiple of 32: zero rows pad the last line
+    (256, 128, 512, 1, 1, 1),   # two row and two column tiles with split-K
 ])
 def test_limb_matmul(pg, ctx, M, N, K, tA, tB, tC):
     a, b = orc.random_views(M * K, U64, 3), orc.random_views(K * N, U64, 4)
@@ -113,6 +114,8 @@ def test_limb_digit_extremes(pg, ctx, fill):
     (1, 32, 32, 3, 64, 64, 1, 1),   # one VGG row tile: 4 rows x 32 columns
     (1, 5, 40, 3, 16, 16, 1, 1),    # wider than one 32-pixel line: tiles along w
     (1, 3, 70, 1, 16, 8, 1, 0),     # ragged last w tile
+    (2, 16, 16, 3, 64, 128, 1, 1),  # two N tiles, four row tiles of 8 x 16 pixels
+    (4, 32, 32, 3, 64, 64, 1, 1),   # 32 row tiles of 4 x 32 pixels
 ])
 def test_limb_conv(pg, ctx, batch, H, W, f, Din, Dout, stride, pad):
     A = orc.random_views(batch * H * W * Din, U64, 7)
