@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "pg_common.cuh"
+#include "pg_limb_tma.cuh"
 
 namespace pg {
 template <typename T>
@@ -19,10 +20,6 @@ int rss_conv(Ctx *, const T *const *, const T *const *, T *const *, int, int, in
 template <typename T, typename U> int rss_relu(Ctx *, const T *const *, size_t, T *const *, U *const *);
 template <typename T, typename U>
 int rss_maxpool_layer(Ctx *, const T *const *, T *const *, U *const *, int, int, int, int, int, int, int);
-int limb3_rss_matmul_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *,
-                        const uint64_t *const *, int, int, int, int, int, int, int);
-int limb3_rss_conv_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *, int, int, int, int,
-                      int, int, int, int, int, int);
 }  // namespace pg
 
 using namespace pg;
@@ -33,6 +30,10 @@ struct NetLayer {
     size_t in_n, out_n, w_n, b_n, d_n;  // elements per share buffer (activations include the batch)
     uint64_t *w[6], *b[6], *out[6];
     uint8_t *d[6];
+    // limb tensor-core form (FC and CNN layers): plan, split-K, packed weights
+    lt::Plan plan;
+    int split, cps;
+    uint8_t *packB;
 };
 
 struct pg_net {
@@ -48,7 +49,72 @@ struct pg_net {
     uint64_t comm_per_fwd[9] = {0};  // accounting of one forward, replayed with the graph
     uint64_t launches_per_fwd = 0;
     std::vector<cudaEvent_t> ev;  // 2 per layer when per-layer timing is on (recorded into graphs too)
+    // Buffers of the limb tensor-core form, owned by the network (so that a
+    // captured graph never points into the context's growable scratch):
+    // packed weights of every FC / CNN layer, one digit-plane image and one
+    // split-K partial buffer shared by the layers. Set up by the first
+    // limb-form forward, which is always eager (capture runs one first).
+    void *limb_arena = nullptr;
+    uint8_t *limb_image = nullptr;
+    uint64_t *limb_partial = nullptr;
 };
+
+// Plans, buffer sizes and weight packing of the limb form.
+static int net_limb_setup(pg_net *net) {
+    Ctx *c = net->ctx;
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    size_t image = 0, partial = 0, packs = 0;
+    const int sms = c->sm_count > 0 ? c->sm_count : 148;
+    for (auto &L : net->layers) {
+        int st = PG_OK;
+        if (L.type == PG_LAYER_FC) st = lt::plan_gemm(c, L.plan, net->batch, L.p[1], L.p[0], 1, 1, 1);
+        else if (L.type == PG_LAYER_CNN)
+            st = lt::plan_conv(c, L.plan, net->batch, L.p[0], L.p[1], L.p[4], L.p[2], L.p[3], L.p[5], L.p[6]);
+        else continue;
+        if (st) return st;
+        lt::choose_split(L.plan, sms, L.split, L.cps);
+        image = image > L.plan.image_bytes ? image : L.plan.image_bytes;
+        const size_t pb = lt::partial_bytes(L.plan, L.split);
+        partial = partial > pb ? partial : pb;
+        packs += al(L.plan.packB_bytes);
+    }
+    const size_t bytes = al(image) + al(partial) + packs;
+    if (cudaMalloc(&net->limb_arena, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        net->limb_arena = nullptr;
+        return set_error(c, PG_ERR_NO_MEMORY, "limb-form buffers of %zu bytes", bytes);
+    }
+    uint8_t *ptr = (uint8_t *)net->limb_arena;
+    net->limb_image = ptr;
+    ptr += al(image);
+    net->limb_partial = partial ? (uint64_t *)ptr : nullptr;
+    ptr += al(partial);
+    for (auto &L : net->layers) {
+        if (L.type != PG_LAYER_FC && L.type != PG_LAYER_CNN) continue;
+        L.packB = ptr;
+        ptr += al(L.plan.packB_bytes);
+        int st = lt::run_pack(c, L.plan, (const uint64_t *const *)L.w, L.packB);
+        if (st) return st;
+    }
+    return PG_OK;
+}
+
+// One FC / CNN layer in the limb form: digit image of the input, GEMM over
+// the packed weights (+ split-K reduction), then the message accounting of
+// matmul / convolution (RSS.inl:517-538, :790-802).
+static int net_limb_layer(pg_net *net, NetLayer &L, const uint64_t *const *in) {
+    Ctx *c = net->ctx;
+    int st = lt::run_image(c, L.plan, in, net->limb_image);
+    if (st) return st;
+    const uint64_t *const *bias = L.b_n ? (const uint64_t *const *)L.b : nullptr;
+    st = lt::run_gemm(c, L.plan, net->limb_image, L.packB, L.split > 1 ? net->limb_partial : nullptr, L.split, L.cps,
+                      L.out, bias, net->fp);
+    if (st) return st;
+    const uint64_t n_out = (uint64_t)L.plan.M * L.plan.N;
+    comm_msg(c, 2 * n_out * 8, 2 * n_out * 8);
+    comm_round(c);
+    return PG_OK;
+}
 
 // Per-layer timing events: inside a stream capture they must be external
 // event nodes so that graph replays record them; outside, a plain record.
@@ -63,6 +129,14 @@ static int record_event(Ctx *c, cudaEvent_t e) {
 static int net_run(pg_net *net, const uint64_t *const in[6]) {
     Ctx *c = net->ctx;
     const uint64_t *const *cur = in;
+    if (c->form == PG_FORM_LIMB_TC && !net->limb_arena) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        PG_CHECK_CUDA(c, cudaStreamIsCapturing(c->stream, &cs));
+        if (cs != cudaStreamCaptureStatusNone)
+            return set_error(c, PG_ERR_INVALID_ARG, "limb-form buffers must be set up by an eager forward first");
+        int st = net_limb_setup(net);
+        if (st) return st;
+    }
     for (size_t li = 0; li < net->layers.size(); li++) {
         NetLayer &L = net->layers[li];
         int st = PG_OK;
@@ -71,16 +145,14 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
             case PG_LAYER_FC: {
                 const uint64_t *const *bias = L.b_n ? (const uint64_t *const *)L.b : nullptr;
                 st = c->form == PG_FORM_LIMB_TC
-                         ? limb3_rss_matmul_u64(c, cur, (const uint64_t *const *)L.w, L.out, bias, net->batch, L.p[1],
-                                               L.p[0], 1, 1, 1, net->fp)
+                         ? net_limb_layer(net, L, cur)
                          : rss_matmul<uint64_t>(c, cur, (const uint64_t *const *)L.w, L.out, bias, net->batch, L.p[1],
                                                 L.p[0], 1, 1, 1, net->fp);
                 break;
             }
             case PG_LAYER_CNN:
                 st = c->form == PG_FORM_LIMB_TC
-                         ? limb3_rss_conv_u64(c, cur, (const uint64_t *const *)L.w, L.out, PG_CONV_FPROP, net->batch,
-                                             L.p[0], L.p[1], L.p[4], L.p[2], L.p[3], L.p[5], L.p[6], net->fp)
+                         ? net_limb_layer(net, L, cur)
                          : rss_conv<uint64_t>(c, cur, (const uint64_t *const *)L.w, L.out, PG_CONV_FPROP, net->batch,
                                               L.p[0], L.p[1], L.p[4], L.p[2], L.p[3], L.p[5], L.p[6], net->fp);
                 break;
@@ -192,10 +264,9 @@ int pg_net_destroy(pg_net *net) {
     for (auto e : net->ev) cudaEventDestroy(e);
     if (net->exec) cudaGraphExecDestroy(net->exec);
     if (net->graph) cudaGraphDestroy(net->graph);
-    if (net->arena) {
-        cudaStreamSynchronize(net->ctx->stream);
-        cudaFree(net->arena);
-    }
+    if (net->arena || net->limb_arena) cudaStreamSynchronize(net->ctx->stream);
+    if (net->arena) cudaFree(net->arena);
+    if (net->limb_arena) cudaFree(net->limb_arena);
     delete net;
     return PG_OK;
 }
@@ -212,6 +283,11 @@ int pg_net_set_params(pg_net *net, int layer, const uint64_t *const w[6], const 
     if (L.b_n && bias)
         for (int k = 0; k < 6; k++)
             PG_CHECK_CUDA(c, cudaMemcpyAsync(L.b[k], bias[k], L.b_n * 8, cudaMemcpyDeviceToDevice, c->stream));
+    // the limb form keeps the weights packed: repack this layer's
+    if (net->limb_arena && L.packB) {
+        int st = lt::run_pack(c, L.plan, (const uint64_t *const *)L.w, L.packB);
+        if (st) return st;
+    }
     // a set-up call: the caller may release the source buffers on return
     PG_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
     return PG_OK;

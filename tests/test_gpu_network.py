@@ -147,3 +147,66 @@ def test_capture_with_layer_timing_on_side_stream(pg):
             ctx.check_device_errors()
             net.close()
             ctx.close()
+
+
+@pytest.mark.parametrize("capture", [False, True])
+def test_lenet_forward_limb_form(pg, capture):
+    """LeNet in the limb tensor-core form: im2col-image convs (Din = 1 and 20),
+    FC layers with bias and split-K, weights packed once by the network."""
+    layers = netref.lenet_layers()
+    params = netref.kaiming_uniform_params(layers, 17)
+    batch = 4
+    rng = np.random.default_rng(18)
+    x = orc.share_random(orc.encode(rng.uniform(0, 1, batch * 784)), seed=19)
+    want, want_outs = netref.forward(layers, params, x, batch, keep=True)
+    got, got_outs, _ = run_net(pg, layers, params, x, batch, capture=capture, form=pg.FORM_LIMB_TC)
+    for i, (g, w) in enumerate(zip(got_outs, want_outs)):
+        assert np.array_equal(g, w), f"layer {i} {layers[i]}"
+    assert np.array_equal(got, want)
+
+
+def test_secureml_fixture_forward_limb_form(pg, golden):
+    L = golden[1]
+    layers = netref.secureml_layers()
+    params = []
+    for li in (0, 2, 4):
+        params.append((orc.set_public(L[f"secureml_weight{li}"]), orc.set_public(L[f"secureml_bias{li}"])))
+        params.append(None)
+    x = orc.set_public(L["secureml_input"])
+    comm = orc.Comm()
+    want, want_outs = netref.forward(layers, params, x, 128, comm=comm, keep=True)
+    got, got_outs, gcomm = run_net(pg, layers, params, x, 128, form=pg.FORM_LIMB_TC)
+    for i, (g, w) in enumerate(zip(got_outs, want_outs)):
+        assert np.array_equal(g, w), f"layer {i}"
+    assert gcomm["tx"] == comm.tx and gcomm["rounds"] == comm.rounds
+
+
+def test_limb_weights_repacked_after_capture(pg):
+    """set_params after capture repacks the layer, and the replayed graph uses the new weights."""
+    import torch
+
+    layers = netref.secureml_layers()
+    p1 = netref.kaiming_uniform_params(layers, 41)
+    p2 = netref.kaiming_uniform_params(layers, 42)
+    batch = 8
+    x = orc.share_random(orc.encode(np.random.default_rng(43).uniform(0, 1, batch * 784)), seed=44)
+    ctx = pg.Context(0, form=pg.FORM_LIMB_TC)
+    net = pg.Network(ctx, layers, batch)
+    for i, prm in enumerate(p1):
+        if prm is not None:
+            net.set_params(i, pg.to_device(prm[0]), pg.to_device(prm[1]))
+    net.capture()
+    ptrs = net.input_buffers()
+    _wrap_device(ptrs[0], 6 * net.in_n).copy_(pg.to_device(x).reshape(-1))
+    torch.cuda.synchronize()
+    for params in (p1, p2):
+        for i, prm in enumerate(params):
+            if prm is not None:
+                net.set_params(i, pg.to_device(prm[0]), pg.to_device(prm[1]))
+        net.forward_resident()
+        ctx.sync()
+        optrs, n = net.layer_output_ptrs(len(layers) - 1)
+        assert np.array_equal(gather(pg, optrs, n), netref.forward(layers, params, x, batch))
+    ctx.check_device_errors()
+    net.close()
+    ctx.close()
