@@ -179,20 +179,20 @@ int pg_maxpool_im2row_u64(pg_ctx *ctx, const uint64_t *im, uint64_t *out, int H,
  * takes its scratch from one fixed device array of PG_NOALLOC_SCRATCH_BYTES,
  * which the CUDA runtime reserves when it loads the library module that holds
  * it.
- *  - The first call on a device does set-up (finds the array's address and
- *    sets the kernel's shared-memory limit) and needs the context's device
- *    current. Make it before any stream capture on that device.
- *  - The scratch need is 96 * K * (N rounded up to 64) bytes of packed
- *    weights plus the column sums (and split-K partial sums, used only when
- *    they fit). A problem that does not fit returns PG_ERR_SIZE; pg_last_error
- *    gives the need and the limit.
- *  - K must be a multiple of 16 and the twelve input pointers 16-byte
- *    aligned; other shapes return PG_ERR_UNSUPPORTED.
+ *  - The first call on a device does set-up (finds the array's address, sets
+ *    the kernel's shared-memory limit and looks up the tensor-map encoder)
+ *    and needs the context's device current. Make it before any stream
+ *    capture on that device.
+ *  - The scratch need is 96 * K16 * M32 bytes for the digit image of a plus
+ *    96 * K16 * N64 bytes for the packed weights (K16, M32, N64 = K, M, N
+ *    rounded up to 16, 32, 64), plus split-K partial sums when they fit too;
+ *    K = M = N = 1024 fits. A problem that does not fit returns PG_ERR_SIZE;
+ *    pg_last_error gives the need and the limit.
  *  - All calls on a device, from every context and thread, share the one
  *    array. Calls that can run at the same time on the device (streams with
  *    no ordering between them) corrupt each other's results: order them on
  *    one stream or with events. */
-#define PG_NOALLOC_SCRATCH_BYTES ((size_t)128 << 20)
+#define PG_NOALLOC_SCRATCH_BYTES ((size_t)256 << 20)
 int pg_rss_matmul_u64_noalloc(pg_ctx *ctx, const uint64_t *const a[6], const uint64_t *const b[6],
                               uint64_t *const c[6], int M, int N, int K, int tA, int tB, int tC, int trunc);
 

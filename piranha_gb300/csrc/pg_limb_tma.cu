@@ -601,6 +601,62 @@ __global__ void reduce_kernel(const __grid_constant__ Args g, int nsplit) {
     }
 }
 
+// ------------------------------------------------------------- self test
+
+// One 128x64x16 MMA of fp16 integers, D = A * B^T, with A and B given as
+// K-major row-major halves (128 x 16 and 64 x 16). Checks the shared-memory
+// descriptors, the instruction descriptor and the tensor-memory lane/column
+// layout against a host reference.
+__global__ void __launch_bounds__(128, 1) selftest_kernel(const uint16_t *A, const uint16_t *B, float *D, int *err) {
+    __shared__ __align__(1024) uint8_t sa[A_PLANE_BYTES];
+    __shared__ __align__(1024) uint8_t sb[B_PLANE_BYTES];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tbase;
+    __shared__ int abort_flag;
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    for (int kc = 0; kc < 2; kc++) {
+        *reinterpret_cast<uint4 *>(sa + b_off(t, kc)) = *reinterpret_cast<const uint4 *>(A + t * 16 + kc * 8);
+        if (t < 64) *reinterpret_cast<uint4 *>(sb + b_off(t, kc)) = *reinterpret_cast<const uint4 *>(B + t * 16 + kc * 8);
+    }
+    if (t == 0) {
+        tc::mbar_init(tc::smem_u32(&bar), 1);
+        abort_flag = 0;
+        tc::fence_mbar_init();
+    }
+    tc::fence_proxy_async_smem();
+    if (warp == 0) {
+        tc::tmem_alloc(tc::smem_u32(&tbase), 64);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tm = tbase;
+    if (t == 0) {
+        tc::mma_f16(tm, tc::smem_desc(tc::smem_u32(sa), 128, 256), tc::smem_desc(tc::smem_u32(sb), 128, 256),
+                    tc::idesc_f16_f32(128, 64), 0u);
+        tc::mma_commit(tc::smem_u32(&bar));
+    }
+    __syncwarp();
+    const bool ok = tc::mbar_wait(tc::smem_u32(&bar), 0, &abort_flag, WAIT_NS);
+    if (!ok && err) atomicCAS(err, 0, 0x700);
+    tc::tc_fence_after();
+    if (ok) {
+        for (int half = 0; half < 2; half++) {
+            uint32_t r[32];
+            tc::tmem_ld32(tm + ((uint32_t)(warp * 32) << 16) + (uint32_t)(half * 32), r);
+            tc::tmem_wait_ld();
+            for (int j = 0; j < 32; j++) D[(warp * 32 + lane) * 64 + half * 32 + j] = __uint_as_float(r[j]);
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc::tc_fence_after();
+        tc::tmem_dealloc(tm, 64);
+    }
+}
+
 // ------------------------------------------------------------------- host
 
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn(Ctx *c) {
@@ -618,6 +674,22 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn(Ctx *c) {
     });
     if (!fn) set_error(c, PG_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
     return fn;
+}
+
+// Once per device (with it current): the GEMM kernel's shared-memory limit
+// and the tensor-map encoder.
+int prepare_device(Ctx *c) {
+    static std::mutex mu;
+    static bool done[64];
+    std::lock_guard<std::mutex> lock(mu);
+    if (c->device < 0 || c->device >= 64) return set_error(c, PG_ERR_UNSUPPORTED, "device ordinal %d", c->device);
+    if (!done[c->device]) {
+        PG_CHECK_CUDA(c, cudaFuncSetAttribute(limb_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem_bytes()));
+        if (!encode_fn(c)) return PG_ERR_CUDA;
+        done[c->device] = true;
+    }
+    return PG_OK;
 }
 
 static void tile_geometry(Plan &p) {
@@ -778,15 +850,8 @@ int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB) {
 int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial, int split, int cps,
              uint64_t *const out[6], const uint64_t *const bias[6], int trunc) {
     {
-        static std::mutex mu;
-        static bool attr_done[64];
-        std::lock_guard<std::mutex> lock(mu);
-        if (c->device < 0 || c->device >= 64) return set_error(c, PG_ERR_UNSUPPORTED, "device ordinal %d", c->device);
-        if (!attr_done[c->device]) {
-            PG_CHECK_CUDA(c, cudaFuncSetAttribute(limb_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  (int)smem_bytes()));
-            attr_done[c->device] = true;
-        }
+        int st = prepare_device(c);
+        if (st) return st;
     }
     if (trunc < 0 || trunc > 63) return set_error(c, PG_ERR_INVALID_ARG, "bad truncation %d", trunc);
     if (((uintptr_t)image & 15) || ((uintptr_t)packB & 15))
@@ -905,6 +970,56 @@ int limb3_rss_conv_u64(Ctx *c, const uint64_t *const A[6], const uint64_t *const
     int st = lt::plan_conv(c, p, batch, H, W, f, Din, Dout, stride, pad);
     if (st) return st;
     return run_with_scratch(c, p, A, B, C, nullptr, trunc);
+}
+
+int limb_prepare_current_device(Ctx *c) { return lt::prepare_device(c); }
+
+// limb3_rss_matmul_u64 without a bias, with every scratch byte taken from
+// [scr, scr + cap): the digit image of A, the packed weights, and the split-K
+// partial sums (used only when they fit too). A problem whose unsplit need
+// exceeds cap is refused with PG_ERR_SIZE. It allocates nothing.
+int limb_rss_matmul_u64_fixed(Ctx *c, uint8_t *scr, size_t cap, const uint64_t *const a[6],
+                              const uint64_t *const b[6], uint64_t *const out[6], int M, int N, int K, int tA, int tB,
+                              int tC, int trunc) {
+    CSh6<uint64_t> ca, cb;
+    Sh6<uint64_t> co;
+    if (!load6(ca, a) || !load6(cb, b) || !load6(co, out)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    if (trunc < 0 || trunc > 63) return set_error(c, PG_ERR_INVALID_ARG, "bad truncation %d", trunc);
+    if (!scr || ((uintptr_t)scr & 255)) return set_error(c, PG_ERR_INVALID_ARG, "scratch must be 256-byte aligned");
+    lt::Plan p;
+    int st = lt::plan_gemm(c, p, M, N, K, tA, tB, tC);
+    if (st) return st;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    int split, cps;
+    lt::choose_split(p, c->sm_count > 0 ? c->sm_count : 148, split, cps);
+    const size_t ib = al(p.image_bytes), pb = al(p.packB_bytes);
+    if (ib + pb + al(lt::partial_bytes(p, split)) > cap) {
+        split = 1;
+        cps = (6 * p.kblocks + lt::CHUNK_STAGES - 1) / lt::CHUNK_STAGES;
+    }
+    const size_t need = ib + pb + al(lt::partial_bytes(p, split));
+    if (need > cap)
+        return set_error(c, PG_ERR_SIZE,
+                         "M=%d N=%d K=%d needs %zu bytes of scratch; the fixed scratch holds %zu (the operand image "
+                         "takes 96 * K16 * M32 bytes and the packed weights 96 * K16 * N64, with K16, M32 and N64 "
+                         "= K, M and N rounded up to 16, 32 and 64)",
+                         M, N, K, need, cap);
+    st = lt::run_image(c, p, a, scr);
+    if (!st) st = lt::run_pack(c, p, b, scr + ib);
+    if (!st)
+        st = lt::run_gemm(c, p, scr, scr + ib, split > 1 ? (uint64_t *)(scr + ib + pb) : nullptr, split, cps, out,
+                          nullptr, trunc);
+    if (st) return st;
+    comm_msg(c, 2ull * M * N * 8, 2ull * M * N * 8);
+    comm_round(c);
+    return PG_OK;
+}
+
+int limb_selftest(Ctx *c, const uint16_t *A, const uint16_t *B, float *D) {
+    if (!A || !B || !D) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+    lt::selftest_kernel<<<1, 128, 0, c->stream>>>(A, B, D, device_error_word(c));
+    c->launches++;
+    return launch_status(c, "selftest_kernel");
 }
 
 }  // namespace pg

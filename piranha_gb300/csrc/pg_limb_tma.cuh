@@ -29,6 +29,7 @@ struct Plan {
     size_t image_bytes, packB_bytes;
 };
 
+int prepare_device(Ctx *c);  // once per device, with it current (no allocation)
 int plan_gemm(Ctx *c, Plan &p, int M, int N, int K, int tA, int tB, int tC);
 int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad);
 void choose_split(const Plan &p, int sms, int &split, int &chunks_per_split);

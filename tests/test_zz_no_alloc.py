@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 
 U64 = np.uint64
 P6 = ctypes.c_void_p * 6
-PG_ERR_SIZE, PG_ERR_UNSUPPORTED = 2, 4
+PG_ERR_SIZE = 2
 
 
 @pytest.fixture(scope="module")
@@ -109,4 +109,13 @@ def test_noalloc_refuses_what_does_not_fit(pg, ctx):
     msg = pg.lib().pg_last_error(ctx.handle)
     msg = msg.decode() if isinstance(msg, bytes) else str(msg)
     assert "fixed scratch" in msg
-    assert _noalloc(pg, ctx, d, d, d, 8, 8, 24, 1, 1, 1, 26) == PG_ERR_UNSUPPORTED
+
+
+def test_noalloc_any_k(pg, ctx):
+    # K not a multiple of 16: zero digits pad the contraction
+    M, N, K = 40, 24, 25
+    a, b = orc.random_views(M * K, U64, 11), orc.random_views(K * N, U64, 12)
+    out = pg.zeros_shares(M * N)
+    ctx._check(_noalloc(pg, ctx, pg.to_device(a), pg.to_device(b), out, M, N, K, 1, 1, 1, 20))
+    ctx.check_device_errors()
+    assert np.array_equal(pg.to_host(out), orc.matmul(a, b, M, N, K, 1, 1, 1, 20))
