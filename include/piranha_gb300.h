@@ -168,6 +168,51 @@ int pg_expand_compare_u8(pg_ctx *ctx, const uint8_t *b, const uint8_t *nb, size_
 int pg_maxpool_im2row_u64(pg_ctx *ctx, const uint64_t *im, uint64_t *out, int H, int W, int f, int Din,
                           int batch, int stride, int pad, uint64_t pad_val);
 
+/* --------------------------------------------------------- TPC (2PC) protocol
+ * src/mpc/TPC.h, TPC.inl: two-party additive shares. A TPC tensor of n
+ * elements is TWO device pointers, [party A, party B], each n elements; its
+ * value is their sum. The reference's multiplications use constant Beaver
+ * triples (src/mpc/Precompute.h), and its results land in party A's share
+ * with party B's 0; these entry points produce the same shares bit for bit.
+ * Counters add the bytes and rounds of every reveal the reference makes. */
+/* matmul (TPC.inl:575-583, localMatMul :1060-1091): reveal a and b masked,
+ * multiply, dividePublic by 2^trunc */
+int pg_tpc_matmul_u64(pg_ctx *ctx, const uint64_t *const a[2], const uint64_t *const b[2], uint64_t *const c[2],
+                      int M, int N, int K, int tA, int tB, int tC, int trunc);
+int pg_tpc_matmul_u32(pg_ctx *ctx, const uint32_t *const a[2], const uint32_t *const b[2], uint32_t *const c[2],
+                      int M, int N, int K, int tA, int tB, int tC, int trunc);
+/* FCLayer::forward (src/nn/FCLayer.cu:78-130) for TPC: matmul(tA=tB=tC=1, FP)
+ * then each party adds its bias share; bias may be NULL */
+int pg_tpc_fc_forward_u64(pg_ctx *ctx, const uint64_t *const x[2], const uint64_t *const w[2],
+                          const uint64_t *const bias[2], uint64_t *const out[2], int batch, int din, int dout, int fp);
+int pg_tpc_fc_forward_u32(pg_ctx *ctx, const uint32_t *const x[2], const uint32_t *const w[2],
+                          const uint32_t *const bias[2], uint32_t *const out[2], int batch, int din, int dout, int fp);
+/* convolution (TPC.inl:789-827 with localFprop/Dgrad/Wgrad :645-787) */
+int pg_tpc_conv_u64(pg_ctx *ctx, const uint64_t *const A[2], const uint64_t *const B[2], uint64_t *const C[2],
+                    int op, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad, int trunc);
+/* dividePublic (TPC.inl:371-401), in place */
+int pg_tpc_divide_public_u64(pg_ctx *ctx, uint64_t *const a[2], size_t n, uint64_t d);
+int pg_tpc_divide_public_vec_u64(pg_ctx *ctx, uint64_t *const a[2], size_t n, const uint64_t *d);
+int pg_tpc_divide_public_u32(pg_ctx *ctx, uint32_t *const a[2], size_t n, uint32_t d);
+/* reconstruct (TPC.inl:552-572): out[p] = a_A + a_B for both parties */
+int pg_tpc_reconstruct_u64(pg_ctx *ctx, const uint64_t *const a[2], size_t n, uint64_t *const out[2]);
+int pg_tpc_reconstruct_u32(pg_ctx *ctx, const uint32_t *const a[2], size_t n, uint32_t *const out[2]);
+int pg_tpc_reconstruct_u8(pg_ctx *ctx, const uint8_t *const a[2], size_t n, uint8_t *const out[2]);
+/* TPC *= TPC (TPC.inl:242-272), in place on a */
+int pg_tpc_mul_u64(pg_ctx *ctx, uint64_t *const a[2], const uint64_t *const b[2], size_t n);
+/* dReLU (TPC.inl:829-868), ReLU (:871-884), selectShare (:586-610),
+ * maxpool over rows of k = 2, 4, 8 or 16 values (:887-1058) */
+int pg_tpc_drelu_u64_u8(pg_ctx *ctx, const uint64_t *const in[2], size_t n, uint8_t *const out[2]);
+int pg_tpc_drelu_u32_u8(pg_ctx *ctx, const uint32_t *const in[2], size_t n, uint8_t *const out[2]);
+int pg_tpc_relu_u64_u8(pg_ctx *ctx, const uint64_t *const in[2], size_t n, uint64_t *const out[2],
+                       uint8_t *const dout[2]);
+int pg_tpc_relu_u32_u8(pg_ctx *ctx, const uint32_t *const in[2], size_t n, uint32_t *const out[2],
+                       uint8_t *const dout[2]);
+int pg_tpc_select_share_u64_u8(pg_ctx *ctx, const uint64_t *const x[2], const uint64_t *const y[2],
+                               const uint8_t *const b[2], uint64_t *const z[2], size_t n);
+int pg_tpc_maxpool_u64_u8(pg_ctx *ctx, const uint64_t *const in[2], size_t n, int k, uint64_t *const out[2],
+                          uint8_t *const dout[2]);
+
 /* ---------------------------------------------- share-GEMM without allocation
  * No counterpart in the reference. The same result as pg_rss_matmul_u64, bit
  * for bit, computed by the limb tensor-core kernels, for callers that must not

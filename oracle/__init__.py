@@ -390,3 +390,139 @@ def div_public_values(x, d, dtype=np.uint64):
     out = np.empty_like(x)
     getattr(lib(), f"or_div_public_scalar_{suf}")(_p(x), ctypes.c_size_t(x.size), _p(dv), int(dv.size > 1), _p(out))
     return out
+
+
+# ------------------------------------------------------------------- TPC
+# A TPC tensor of n elements is a numpy array of shape (2, n): [party A/B][element]
+# (src/mpc/TPC.h: one additive share per party).
+
+def _tviews(a, dtype, n=None):
+    a = np.ascontiguousarray(a, dtype=dtype)
+    if a.ndim != 2 or a.shape[0] != 2 or (n is not None and a.shape[1] != n):
+        raise ValueError(f"expected TPC shares of shape (2, {n}), got {a.shape}")
+    return a
+
+
+def tpc_from_list(vals, dtype=np.uint64, fp=FP_DEFAULT, to_fixed=True):
+    """setPublic / initializer list (TPC.inl:109-123, :341-363): party A holds the values."""
+    dt, suf = _ring(dtype)
+    v = np.ascontiguousarray(vals, dtype=np.float64).ravel()
+    out = np.empty((2, v.size), dtype=dt)
+    getattr(lib(), f"or_tpc_from_list_{suf}")(_p(v), ctypes.c_size_t(v.size), fp, int(to_fixed), _p(out))
+    return out
+
+
+def tpc_share_random(secret, dtype=np.uint64, seed=0):
+    """A valid 2-party sharing of `secret` with a seeded random mask for party B."""
+    dt, _ = _ring(dtype)
+    s = np.ascontiguousarray(secret, dtype=dt).ravel()
+    rng = np.random.default_rng(seed)
+    mask = rng.integers(0, np.iinfo(dt).max, size=s.size, dtype=dt, endpoint=True)
+    return np.stack([(s - mask).astype(dt), mask])
+
+
+def tpc_reconstruct(a, comm=None):
+    """reconstruct (TPC.inl:552-572): both parties get share A + share B (uint64/uint32/uint8)."""
+    dt = np.asarray(a).dtype.type
+    suf = _SUF[dt]
+    a = _tviews(a, dt)
+    n = a.shape[1]
+    out = np.empty((2, n), dtype=dt)
+    comm = comm or Comm()
+    getattr(lib(), f"or_tpc_reconstruct_{suf}")(_p(a), ctypes.c_size_t(n), _p(out), comm.ptr())
+    return out
+
+
+def tpc_matmul(a, b, M, N, K, tA, tB, tC, trunc, comm=None):
+    """TPC matmul (TPC.inl:575-583): localMatMul with the matrix triple, then dividePublic."""
+    dt, suf = _ring(np.asarray(a).dtype)
+    a = _tviews(a, dt, M * K)
+    b = _tviews(b, dt, K * N)
+    c = np.empty((2, M * N), dtype=dt)
+    comm = comm or Comm()
+    getattr(lib(), f"or_tpc_matmul_{suf}")(_p(a), _p(b), _p(c), M, N, K, int(tA), int(tB), int(tC), trunc,
+                                           comm.ptr())
+    return c
+
+
+def tpc_convolution(a, b, op, batch, H, W, f, Din, Dout, stride, pad, trunc, comm=None):
+    """TPC convolution (TPC.inl:789-827)."""
+    dt, suf = _ring(np.asarray(a).dtype)
+    a = _tviews(a, dt)
+    b = _tviews(b, dt)
+    n_out = conv_out_size(op, batch, H, W, f, Din, Dout, stride, pad)
+    c = np.empty((2, n_out), dtype=dt)
+    comm = comm or Comm()
+    getattr(lib(), f"or_tpc_conv_{suf}")(_p(a), ctypes.c_size_t(a.shape[1]), _p(b), ctypes.c_size_t(b.shape[1]),
+                                         _p(c), op, batch, H, W, f, Din, Dout, stride, pad, trunc, comm.ptr())
+    return c
+
+
+def tpc_divide_public(a, d, comm=None):
+    dt, suf = _ring(np.asarray(a).dtype)
+    a = _tviews(a, dt).copy()
+    n = a.shape[1]
+    dv = np.ascontiguousarray(np.atleast_1d(np.asarray(d, dtype=dt)))
+    vec = dv.size > 1 or (np.ndim(d) > 0)
+    if vec and dv.size != n:
+        raise ValueError("denominator vector size mismatch")
+    comm = comm or Comm()
+    getattr(lib(), f"or_tpc_divide_public_{suf}")(_p(a), ctypes.c_size_t(n), _p(dv), int(vec), comm.ptr())
+    return a
+
+
+def tpc_mul(a, b, comm=None):
+    dt, suf = _ring(np.asarray(a).dtype)
+    a = _tviews(a, dt).copy()
+    b = _tviews(b, dt, a.shape[1])
+    comm = comm or Comm()
+    getattr(lib(), f"or_tpc_mul_{suf}")(_p(a), _p(b), ctypes.c_size_t(a.shape[1]), comm.ptr())
+    return a
+
+
+def tpc_drelu(x, udtype=np.uint8, comm=None):
+    dt, _ = _ring(np.asarray(x).dtype)
+    x = _tviews(x, dt)
+    n = x.shape[1]
+    out = np.empty((2, n), dtype=udtype)
+    comm = comm or Comm()
+    getattr(lib(), f"or_tpc_drelu_{_bits_suffix(dt, udtype)}")(_p(x), ctypes.c_size_t(n), _p(out), comm.ptr())
+    return out
+
+
+def tpc_relu(x, udtype=np.uint8, comm=None):
+    dt, _ = _ring(np.asarray(x).dtype)
+    x = _tviews(x, dt)
+    n = x.shape[1]
+    out = np.empty((2, n), dtype=dt)
+    dout = np.empty((2, n), dtype=udtype)
+    comm = comm or Comm()
+    getattr(lib(), f"or_tpc_relu_{_bits_suffix(dt, udtype)}")(_p(x), ctypes.c_size_t(n), _p(out), _p(dout),
+                                                              comm.ptr())
+    return out, dout
+
+
+def tpc_select_share(x, y, b, comm=None):
+    dt, _ = _ring(np.asarray(x).dtype)
+    x = _tviews(x, dt)
+    n = x.shape[1]
+    y = _tviews(y, dt, n)
+    b = np.ascontiguousarray(b)
+    z = np.empty((2, n), dtype=dt)
+    comm = comm or Comm()
+    getattr(lib(), f"or_tpc_select_share_{_bits_suffix(dt, b.dtype)}")(_p(x), _p(y), _p(b), ctypes.c_size_t(n),
+                                                                       _p(z), comm.ptr())
+    return z
+
+
+def tpc_maxpool(x, k, udtype=np.uint8, comm=None):
+    """TPC maxpool tournament (TPC.inl:887-1058) over rows of k (padded) values."""
+    dt, _ = _ring(np.asarray(x).dtype)
+    x = _tviews(x, dt)
+    n = x.shape[1]
+    out = np.empty((2, n // k), dtype=dt)
+    dout = np.empty((2, n), dtype=udtype)
+    comm = comm or Comm()
+    getattr(lib(), f"or_tpc_maxpool_{_bits_suffix(dt, udtype)}")(_p(x), ctypes.c_size_t(n), k, _p(out), _p(dout),
+                                                                 comm.ptr())
+    return out, dout

@@ -227,3 +227,130 @@ extern "C" void or_expand_compare_u8(const uint8_t* b, const uint8_t* nb, size_t
 extern "C" void or_truncate_cols_u8(const uint8_t* a, uint8_t* b, size_t rows, int start_cols, int end_cols) {
     truncate_cols<uint8_t>(a, b, rows, start_cols, end_cols);
 }
+
+// ------------------------------------------------------------------- TPC
+// A TPC tensor crosses as one flat array [party(2)][n].
+
+namespace {
+template <typename T> void tload(TPCV<T>& r, const T* flat, size_t n) {
+    r.resize(n);
+    for (int p = 0; p < 2; p++) std::memcpy(r.s[p].data(), flat + (size_t)p * n, n * sizeof(T));
+}
+template <typename T> void tstore(const TPCV<T>& r, T* flat) {
+    for (int p = 0; p < 2; p++) std::memcpy(flat + (size_t)p * r.n, r.s[p].data(), r.n * sizeof(T));
+}
+}  // namespace
+
+#define OR_TPC(T, SUF)                                                                                       \
+    extern "C" int or_tpc_matmul_##SUF(const T* a, const T* b, T* c, int M, int N, int K, int tA, int tB,     \
+                                       int tC, int trunc, uint64_t* comm) {                                  \
+        TPCV<T> A, B, C;                                                                                     \
+        tload(A, a, (size_t)M * K);                                                                          \
+        tload(B, b, (size_t)K * N);                                                                          \
+        CommIO io(comm);                                                                                     \
+        tpc_matmul<T>(A, B, C, M, N, K, tA, tB, tC, trunc, io.c);                                            \
+        tstore(C, c);                                                                                        \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_tpc_conv_##SUF(const T* a, size_t na, const T* b, size_t nb, T* c, int op, int batch,   \
+                                     int H, int W, int f, int Din, int Dout, int stride, int pad, int trunc,  \
+                                     uint64_t* comm) {                                                       \
+        TPCV<T> A, B, C;                                                                                     \
+        tload(A, a, na);                                                                                     \
+        tload(B, b, nb);                                                                                     \
+        CommIO io(comm);                                                                                     \
+        tpc_convolution<T>(A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc, io.c);                \
+        tstore(C, c);                                                                                        \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_tpc_divide_public_##SUF(T* a, size_t n, const T* d, int vector_d, uint64_t* comm) {     \
+        TPCV<T> A;                                                                                           \
+        tload(A, a, n);                                                                                      \
+        CommIO io(comm);                                                                                     \
+        tpc_divide_public<T>(A, d, vector_d != 0, io.c);                                                     \
+        tstore(A, a);                                                                                        \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_tpc_reconstruct_##SUF(const T* a, size_t n, T* out, uint64_t* comm) {                  \
+        TPCV<T> A;                                                                                           \
+        tload(A, a, n);                                                                                      \
+        std::vector<T> o[2];                                                                                 \
+        CommIO io(comm);                                                                                     \
+        tpc_reconstruct<T>(A, whole(n), o, io.c);                                                            \
+        for (int p = 0; p < 2; p++) std::memcpy(out + (size_t)p * n, o[p].data(), n * sizeof(T));            \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_tpc_mul_##SUF(T* a, const T* b, size_t n, uint64_t* comm) {                            \
+        TPCV<T> A, B;                                                                                        \
+        tload(A, a, n);                                                                                      \
+        tload(B, b, n);                                                                                      \
+        CommIO io(comm);                                                                                     \
+        tpc_mul_assign<T>(A, whole(n), B, whole(n), io.c);                                                   \
+        tstore(A, a);                                                                                        \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_tpc_from_list_##SUF(const double* v, size_t n, int fp, int to_fixed, T* out) {         \
+        TPCV<T> A(n);                                                                                        \
+        tpc_from_list<T>(A, v, fp, to_fixed != 0);                                                           \
+        tstore(A, out);                                                                                      \
+        return 0;                                                                                            \
+    }
+
+#define OR_TPC_BITS(T, U, SUF)                                                                               \
+    extern "C" int or_tpc_drelu_##SUF(const T* in, size_t n, U* out, uint64_t* comm) {                       \
+        TPCV<T> A;                                                                                           \
+        tload(A, in, n);                                                                                     \
+        TPCV<U> R;                                                                                           \
+        CommIO io(comm);                                                                                     \
+        tpc_drelu<T, U>(A, whole(n), R, io.c);                                                               \
+        tstore(R, out);                                                                                      \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_tpc_relu_##SUF(const T* in, size_t n, T* out, U* dout, uint64_t* comm) {               \
+        TPCV<T> A, O;                                                                                        \
+        tload(A, in, n);                                                                                     \
+        TPCV<U> D;                                                                                           \
+        CommIO io(comm);                                                                                     \
+        tpc_relu<T, U>(A, O, D, io.c);                                                                       \
+        tstore(O, out);                                                                                      \
+        tstore(D, dout);                                                                                     \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_tpc_select_share_##SUF(const T* x, const T* y, const U* b, size_t n, T* z,             \
+                                             uint64_t* comm) {                                               \
+        TPCV<T> X, Y, Z(n);                                                                                  \
+        tload(X, x, n);                                                                                      \
+        tload(Y, y, n);                                                                                      \
+        TPCV<U> B;                                                                                           \
+        tload(B, b, n);                                                                                      \
+        CommIO io(comm);                                                                                     \
+        tpc_select_share<T, U>(X, whole(n), Y, whole(n), B, Z, whole(n), io.c);                              \
+        tstore(Z, z);                                                                                        \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_tpc_maxpool_##SUF(const T* in, size_t n, int k, T* out, U* dout, uint64_t* comm) {     \
+        TPCV<T> A, O;                                                                                        \
+        tload(A, in, n);                                                                                     \
+        TPCV<U> D;                                                                                           \
+        CommIO io(comm);                                                                                     \
+        tpc_maxpool<T, U>(A, O, D, k, io.c);                                                                 \
+        tstore(O, out);                                                                                      \
+        tstore(D, dout);                                                                                     \
+        return 0;                                                                                            \
+    }
+
+OR_TPC(uint64_t, u64)
+OR_TPC(uint32_t, u32)
+OR_TPC_BITS(uint64_t, uint8_t, u64_u8)
+OR_TPC_BITS(uint64_t, uint64_t, u64_u64)
+OR_TPC_BITS(uint32_t, uint8_t, u32_u8)
+
+extern "C" int or_tpc_reconstruct_u8(const uint8_t* a, size_t n, uint8_t* out, uint64_t* comm) {
+    TPCV<uint8_t> A;
+    tload(A, a, n);
+    std::vector<uint8_t> o[2];
+    CommIO io(comm);
+    tpc_reconstruct<uint8_t>(A, whole(n), o, io.c);
+    for (int p = 0; p < 2; p++) std::memcpy(out + (size_t)p * n, o[p].data(), n);
+    return 0;
+}

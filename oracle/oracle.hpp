@@ -682,4 +682,321 @@ void maxpool_layer_forward(const RSSV<T>& in, RSSV<T>& act, RSSV<U>& maxPrime, i
             truncate_cols<U>(expMax.v[p][s].data(), maxPrime.v[p][s].data(), rows, padded, pool * pool);
 }
 
+
+// ========================================================================
+// TPC: 2-party additive sharing (src/mpc/TPC.h, TPC.inl). Each party holds
+// one share; x = x_A + x_B. Multiplications use the Beaver triples of
+// Precompute.h (constant: x = y = z = 1 elementwise, the matrix triple
+// x = y = 1 with z = K, the convolution triples x = y = z = 0). Adding public
+// DeviceData to a TPC share changes party A's share only (TPC.inl:175-189).
+// ========================================================================
+
+enum { TA = 0, TB = 1 };
+
+template <typename T> struct TPCV {
+    size_t n = 0;
+    std::vector<T> s[2];
+    TPCV() {}
+    explicit TPCV(size_t n_) { resize(n_); }
+    void resize(size_t n_) {
+        n = n_;
+        for (int p = 0; p < 2; p++) s[p].assign(n, (T)0);
+    }
+};
+
+// TPC.inl:104-106
+template <typename T> void tpc_fill(TPCV<T>& a, T val) {
+    std::fill(a.s[TA].begin(), a.s[TA].end(), val);
+    std::fill(a.s[TB].begin(), a.s[TB].end(), (T)0);
+}
+
+// TPC.inl:109-123 (setPublic) and :341-363 (initializer list): A holds the values
+template <typename T> void tpc_from_list(TPCV<T>& a, const double* vals, int fp, bool to_fixed) {
+    for (size_t i = 0; i < a.n; i++) {
+        a.s[TA][i] = to_fixed ? encode_fixed<T>(vals[i], fp) : (T)(int64_t)vals[i];
+        a.s[TB][i] = 0;
+    }
+}
+
+// reconstruct (TPC.inl:552-572): each party sends its share to the other;
+// out = own share + received share.
+template <typename T> void tpc_reconstruct(const TPCV<T>& in, Strided w, std::vector<T> (&out)[2], Comm& comm) {
+    for (int p = 0; p < 2; p++) {
+        out[p].resize(w.size);
+        for (size_t i = 0; i < w.size; i++) {
+            size_t j = w.offset + i * w.stride;
+            out[p][i] = (T)(in.s[p][j] + in.s[1 - p][j]);
+        }
+    }
+    comm.msg(2, w.size * sizeof(T), w.size * sizeof(T));
+    comm.rounds++;
+}
+
+template <typename T> static TPCV<T> tpc_gather(const TPCV<T>& a, Strided w) {
+    TPCV<T> r(w.size);
+    for (int p = 0; p < 2; p++)
+        for (size_t i = 0; i < w.size; i++) r.s[p][i] = a.s[p][w.offset + i * w.stride];
+    return r;
+}
+template <typename T> static void tpc_scatter(TPCV<T>& a, Strided w, const TPCV<T>& r) {
+    for (int p = 0; p < 2; p++)
+        for (size_t i = 0; i < w.size; i++) a.s[p][w.offset + i * w.stride] = r.s[p][i];
+}
+
+// TPC *= TPC (TPC.inl:242-272) on the view wa of a, with b viewed by wb.
+template <typename T> void tpc_mul_assign(TPCV<T>& a, Strided wa, const TPCV<T>& b, Strided wb, Comm& comm) {
+    size_t n = wb.size;
+    TPCV<T> self = tpc_gather(a, wa), rhs = tpc_gather(b, wb);
+    TPCV<T> x(n), y(n), z(n);
+    tpc_fill<T>(x, 1); tpc_fill<T>(y, 1); tpc_fill<T>(z, 1);
+    for (int p = 0; p < 2; p++)
+        for (size_t i = 0; i < n; i++) {
+            x.s[p][i] = (T)(x.s[p][i] + self.s[p][i]);
+            y.s[p][i] = (T)(y.s[p][i] + rhs.s[p][i]);
+        }
+    std::vector<T> e[2], f[2];
+    tpc_reconstruct(x, whole(n), e, comm);
+    tpc_reconstruct(y, whole(n), f, comm);
+    for (int p = 0; p < 2; p++)
+        for (size_t i = 0; i < n; i++) {
+            x.s[p][i] = (T)(x.s[p][i] - self.s[p][i]);
+            y.s[p][i] = (T)(y.s[p][i] - rhs.s[p][i]);
+        }
+    for (int p = 0; p < 2; p++)
+        for (size_t i = 0; i < n; i++) {
+            T v = z.s[p][i];                                                     // this = 0; this += z
+            if (p == TA) v = (T)(v + (T)((T)(f[p][i] - y.s[p][i]) * e[p][i]));  // += (f - y) * e  (A only)
+            if (p == TA) v = (T)(v + (T)((T)(0 - x.s[p][i]) * f[p][i]));        // += (-x) * f     (A only)
+            self.s[p][i] = v;
+        }
+    tpc_scatter(a, wa, self);
+}
+
+// TPC &= TPC (TPC.inl:281-312): the boolean Beaver triple, with reconstruct
+// still adding the two shares.
+template <typename U> void tpc_and_assign(TPCV<U>& a, Strided wa, const TPCV<U>& b, Strided wb, Comm& comm) {
+    size_t n = wb.size;
+    TPCV<U> self = tpc_gather(a, wa), rhs = tpc_gather(b, wb);
+    TPCV<U> x(n), y(n), z(n);
+    tpc_fill<U>(x, 1); tpc_fill<U>(y, 1); tpc_fill<U>(z, 1);
+    for (int p = 0; p < 2; p++)
+        for (size_t i = 0; i < n; i++) {
+            x.s[p][i] ^= self.s[p][i];
+            y.s[p][i] ^= rhs.s[p][i];
+        }
+    std::vector<U> e[2], f[2];
+    tpc_reconstruct(x, whole(n), e, comm);
+    tpc_reconstruct(y, whole(n), f, comm);
+    for (int p = 0; p < 2; p++)
+        for (size_t i = 0; i < n; i++) {
+            x.s[p][i] ^= self.s[p][i];
+            y.s[p][i] ^= rhs.s[p][i];
+        }
+    for (int p = 0; p < 2; p++)
+        for (size_t i = 0; i < n; i++) {
+            U v = z.s[p][i];
+            if (p == TA) v ^= (U)((U)(f[p][i] ^ y.s[p][i]) & e[p][i]);
+            if (p == TA) v ^= (U)(x.s[p][i] & f[p][i]);
+            self.s[p][i] = v;
+        }
+    tpc_scatter(a, wa, self);
+}
+
+// TPC ^= TPC: local (TPC.inl:276-279)
+template <typename U> void tpc_xor_assign(TPCV<U>& a, Strided wa, const TPCV<U>& b, Strided wb) {
+    for (int p = 0; p < 2; p++)
+        for (size_t i = 0; i < wb.size; i++) a.s[p][wa.offset + i * wa.stride] ^= b.s[p][wb.offset + i * wb.stride];
+}
+
+// dividePublic (TPC.inl:371-401) with getDividedShares (Precompute.h:112-134):
+// r = 1 and r' = d (scalar) or r' = d_i (vector), both held by party A.
+template <typename T> void tpc_divide_public(TPCV<T>& a, const T* d, bool vec, Comm& comm) {
+    for (size_t i = 0; i < a.n; i++) a.s[TA][i] = (T)(a.s[TA][i] - (vec ? d[i] : d[0]));  // a -= r'
+    std::vector<T> rec[2];
+    tpc_reconstruct(a, whole(a.n), rec, comm);
+    for (size_t i = 0; i < a.n; i++) {
+        T q = div_public<T>(rec[TA][i], vec ? d[i] : d[0]);
+        a.s[TA][i] = (T)(1 + q);  // a = 0; a += r (A: 1); a += reconstructed (A only)
+        a.s[TB][i] = 0;
+    }
+}
+
+// localMatMul (TPC.inl:1060-1091) with the matrix triple of Precompute.h:77-90,
+// then dividePublic by 2^trunc (matmul, TPC.inl:575-583).
+template <typename T>
+void tpc_matmul(const TPCV<T>& a, const TPCV<T>& b, TPCV<T>& c, int M, int N, int K, bool tA, bool tB, bool tC,
+                int trunc, Comm& comm) {
+    TPCV<T> x(a.n), y(b.n);
+    tpc_fill<T>(x, 1); tpc_fill<T>(y, 1);
+    for (int p = 0; p < 2; p++) {
+        for (size_t i = 0; i < a.n; i++) x.s[p][i] = (T)(x.s[p][i] + a.s[p][i]);
+        for (size_t i = 0; i < b.n; i++) y.s[p][i] = (T)(y.s[p][i] + b.s[p][i]);
+    }
+    std::vector<T> e[2], f[2];
+    tpc_reconstruct(x, whole(x.n), e, comm);
+    tpc_reconstruct(y, whole(y.n), f, comm);
+    for (int p = 0; p < 2; p++) {
+        for (size_t i = 0; i < a.n; i++) x.s[p][i] = (T)(x.s[p][i] - a.s[p][i]);
+        for (size_t i = 0; i < b.n; i++) y.s[p][i] = (T)(y.s[p][i] - b.s[p][i]);
+    }
+    size_t mn = (size_t)M * N;
+    c.resize(mn);
+    std::vector<T> t(mn);
+    for (int p = 0; p < 2; p++) {
+        for (size_t i = 0; i < mn; i++) c.s[p][i] = p == TA ? (T)K : (T)0;  // c = 0; c += z (z = K at A)
+        if (p != TA) continue;  // TPC += DeviceData: party A only
+        gemm<T>(M, N, K, e[p].data(), tA, f[p].data(), tB, t.data(), tC);
+        for (size_t i = 0; i < mn; i++) c.s[p][i] = (T)(c.s[p][i] + t[i]);
+        gemm<T>(M, N, K, e[p].data(), tA, y.s[p].data(), tB, t.data(), tC);
+        for (size_t i = 0; i < mn; i++) c.s[p][i] = (T)(c.s[p][i] - t[i]);
+        gemm<T>(M, N, K, x.s[p].data(), tA, f[p].data(), tB, t.data(), tC);
+        for (size_t i = 0; i < mn; i++) c.s[p][i] = (T)(c.s[p][i] - t[i]);
+    }
+    T d = (T)((T)1 << trunc);
+    tpc_divide_public(c, &d, false, comm);
+}
+
+// convolution (TPC.inl:789-827) with localFprop/Dgrad/Wgrad (:645-787): the
+// convolution triples are all zero, so party A's share becomes conv(A, B) of
+// the revealed operands and party B's 0; then dividePublic by 2^trunc.
+template <typename T>
+void tpc_convolution(const TPCV<T>& A, const TPCV<T>& B, TPCV<T>& C, int op, int batch, int H, int W, int f,
+                     int Din, int Dout, int stride, int pad, int trunc, Comm& comm) {
+    ConvShape sh{batch, H, W, Din, Dout, f, f, pad, stride};
+    size_t out_n = op == CONV_FPROP ? (size_t)batch * sh.P() * sh.Q() * Dout
+                 : op == CONV_DGRAD ? (size_t)batch * H * W * Din
+                                    : (size_t)Dout * f * f * Din;
+    std::vector<T> e[2], fr[2];
+    tpc_reconstruct(A, whole(A.n), e, comm);  // x = 0 + A
+    tpc_reconstruct(B, whole(B.n), fr, comm);
+    C.resize(out_n);
+    std::vector<T> t(out_n);
+    conv_any<T>(op, sh, e[TA].data(), fr[TA].data(), t.data());  // the e*y and x*f terms are 0
+    for (size_t i = 0; i < out_n; i++) C.s[TA][i] = t[i];
+    T d = (T)((T)1 << trunc);
+    tpc_divide_public(C, &d, false, comm);
+}
+
+// carryOut (TPC.inl:1093-1146): the RSS tree with TPC ANDs.
+template <typename U> void tpc_carry_out(TPCV<U>& p, TPCV<U>& g, int k, TPCV<U>& out, Comm& comm) {
+    size_t N = p.n;
+    size_t stride = 2, offset = 1;
+    Strided pEven = strided(N, 0, stride), pOdd = strided(N, offset, stride);
+    Strided gEven = strided(N, 0, stride), gOdd = strided(N, offset, stride);
+    while (k > 1) {
+        tpc_and_assign(g, gEven, p, pOdd, comm);
+        tpc_and_assign(p, pEven, p, pOdd, comm);
+        tpc_xor_assign(g, gOdd, g, gEven);
+        gEven = strided(N, offset, stride * 2);
+        offset += stride;
+        gOdd = strided(N, offset, stride * 2);
+        stride *= 2;
+        pEven = strided(N, 0, stride);
+        pOdd = strided(N, stride / 2, stride);
+        k /= 2;
+    }
+    Strided oE = strided(out.n, 0, 2), oO = strided(out.n, 1, 2);
+    for (int q = 0; q < 2; q++) {
+        for (size_t i = 0; i < gEven.size && i < oE.size; i++) out.s[q][oE.offset + i * 2] = g.s[q][gEven.offset + i * gEven.stride];
+        for (size_t i = 0; i < gOdd.size && i < oO.size; i++) out.s[q][oO.offset + i * 2] = g.s[q][gOdd.offset + i * gOdd.stride];
+    }
+}
+
+// dReLU (TPC.inl:829-868)
+template <typename T, typename U> void tpc_drelu(const TPCV<T>& in, Strided w, TPCV<U>& result, Comm& comm) {
+    const int W = sizeof(T) * 8;
+    size_t n = w.size;
+    TPCV<U> rbits(n * W);
+    tpc_fill<U>(rbits, 1);
+    std::vector<T> a[2];
+    tpc_reconstruct(in, w, a, comm);  // r = 0; r += input; reconstruct(r, a)
+    std::vector<U> abits[2];
+    for (int p = 0; p < 2; p++) {
+        for (auto& x : a[p]) x = (T)(x + 1);
+        bitexpand<T, U>(a[p], abits[p]);
+    }
+    TPCV<U> msb(n);
+    for (int p = 0; p < 2; p++) set_carry_out_msb<U>(rbits.s[p], abits[p], msb.s[p], W, p == TA);
+    TPCV<U> g(n * W), pp(n * W);
+    for (int p = 0; p < 2; p++)
+        for (size_t i = 0; i < n * W; i++) {
+            g.s[p][i] = rbits.s[p][i] & abits[p][i];                           // &= DeviceData: every party
+            pp.s[p][i] = rbits.s[p][i] ^ (p == TA ? abits[p][i] : (U)0);  // ^= DeviceData: party A
+        }
+    TPCV<U> pre(n);
+    tpc_carry_out(pp, g, W, pre, comm);
+    tpc_xor_assign(pre, whole(n), msb, whole(n));
+    result.resize(n);
+    for (int p = 0; p < 2; p++)
+        for (size_t i = 0; i < n; i++) result.s[p][i] = (U)((p == TA ? 1 : 0) - pre.s[p][i]);
+}
+
+// selectShare (TPC.inl:586-610) with convex_comb (:1282-1289, functor :31-53).
+template <typename T, typename U>
+void tpc_select_share(const TPCV<T>& x, Strided wx, const TPCV<T>& y, Strided wy, const TPCV<U>& b, TPCV<T>& z,
+                      Strided wz, Comm& comm) {
+    size_t n = wx.size;
+    std::vector<U> e[2];
+    tpc_reconstruct(b, whole(b.n), e, comm);  // cbits = 0 ^ b
+    TPCV<T> d(n);                             // c = 0
+    for (int p = 0; p < 2; p++)
+        for (size_t i = 0; i < n; i++) d.s[p][i] = e[p][i] == 1 ? (p == TA ? (T)1 : (T)0) : (T)0;
+    TPCV<T> res(n);
+    for (int p = 0; p < 2; p++)
+        for (size_t i = 0; i < n; i++)
+            res.s[p][i] = (T)(y.s[p][wy.offset + i * wy.stride] - x.s[p][wx.offset + i * wx.stride]);
+    tpc_mul_assign(res, whole(n), d, whole(n), comm);
+    for (int p = 0; p < 2; p++)
+        for (size_t i = 0; i < n; i++)
+            z.s[p][wz.offset + i * wz.stride] = (T)(res.s[p][i] + x.s[p][wx.offset + i * wx.stride]);
+}
+
+// ReLU (TPC.inl:871-884)
+template <typename T, typename U> void tpc_relu(const TPCV<T>& in, TPCV<T>& out, TPCV<U>& dout, Comm& comm) {
+    tpc_drelu<T, U>(in, whole(in.n), dout, comm);
+    TPCV<T> zeros(in.n);
+    out.resize(in.n);
+    tpc_select_share<T, U>(zeros, whole(in.n), in, whole(in.n), dout, out, whole(in.n), comm);
+}
+
+// maxpool (TPC.inl:887-1058)
+template <typename T, typename U>
+void tpc_maxpool(TPCV<T>& input, TPCV<T>& result, TPCV<U>& dresult, int k, Comm& comm) {
+    size_t N = input.n;
+    dresult.resize(N);
+    tpc_fill<U>(dresult, 1);
+    size_t stride = 2;
+    Strided even = strided(N, 0, stride), odd = strided(N, 1, stride);
+    auto level = [&](bool last) {
+        TPCV<T> diff(even.size);
+        for (int p = 0; p < 2; p++)
+            for (size_t i = 0; i < even.size; i++)
+                diff.s[p][i] = (T)(input.s[p][even.offset + i * even.stride] - input.s[p][odd.offset + i * odd.stride]);
+        TPCV<U> b(even.size);
+        tpc_drelu<T, U>(diff, whole(diff.n), b, comm);
+        tpc_select_share<T, U>(input, odd, input, even, b, input, even, comm);
+        if (!last) {
+            stride *= 2;
+            even = strided(N, 0, stride);
+            odd = strided(N, stride / 2, stride);
+        } else {
+            result.resize(even.size);
+            for (int p = 0; p < 2; p++)
+                for (size_t i = 0; i < even.size; i++) result.s[p][i] = input.s[p][even.offset + i * even.stride];
+        }
+        TPCV<U> neg(b.n);
+        tpc_fill<U>(neg, 1);
+        for (int p = 0; p < 2; p++)
+            for (size_t i = 0; i < b.n; i++) neg.s[p][i] = (U)(neg.s[p][i] - b.s[p][i]);
+        TPCV<U> expanded(N);
+        for (int p = 0; p < 2; p++) expand_compare<U>(b.s[p], neg.s[p], expanded.s[p]);
+        tpc_and_assign(dresult, whole(N), expanded, whole(N), comm);
+    };
+    while (k > 2) {
+        level(false);
+        k /= 2;
+    }
+    level(true);
+}
+
 }  // namespace oracle

@@ -41,6 +41,7 @@ class PiranhaError(RuntimeError):
 
 _P6 = ctypes.c_void_p * 6
 _P3 = ctypes.c_void_p * 3
+_P2 = ctypes.c_void_p * 2
 
 
 def _declare(lib):
@@ -99,6 +100,24 @@ def _declare(lib):
         "pg_device_errors": [vp, ctypes.POINTER(i)],
         "pg_tc_selftest": [vp, vp, vp, vp],
         "pg_net_layer_times": [vp, vp],
+        "pg_tpc_matmul_u64": [vp, _P2, _P2, _P2, i, i, i, i, i, i, i],
+        "pg_tpc_matmul_u32": [vp, _P2, _P2, _P2, i, i, i, i, i, i, i],
+        "pg_tpc_fc_forward_u64": [vp, _P2, _P2, vp, _P2, i, i, i, i],
+        "pg_tpc_fc_forward_u32": [vp, _P2, _P2, vp, _P2, i, i, i, i],
+        "pg_tpc_conv_u64": [vp, _P2, _P2, _P2, i, i, i, i, i, i, i, i, i, i],
+        "pg_tpc_divide_public_u64": [vp, _P2, sz, u64],
+        "pg_tpc_divide_public_vec_u64": [vp, _P2, sz, vp],
+        "pg_tpc_divide_public_u32": [vp, _P2, sz, u32],
+        "pg_tpc_reconstruct_u64": [vp, _P2, sz, _P2],
+        "pg_tpc_reconstruct_u32": [vp, _P2, sz, _P2],
+        "pg_tpc_reconstruct_u8": [vp, _P2, sz, _P2],
+        "pg_tpc_mul_u64": [vp, _P2, _P2, sz],
+        "pg_tpc_drelu_u64_u8": [vp, _P2, sz, _P2],
+        "pg_tpc_drelu_u32_u8": [vp, _P2, sz, _P2],
+        "pg_tpc_relu_u64_u8": [vp, _P2, sz, _P2, _P2],
+        "pg_tpc_relu_u32_u8": [vp, _P2, sz, _P2, _P2],
+        "pg_tpc_select_share_u64_u8": [vp, _P2, _P2, _P2, _P2, sz],
+        "pg_tpc_maxpool_u64_u8": [vp, _P2, sz, i, _P2, _P2],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -359,6 +378,110 @@ def maxpool_layer(ctx: Context, input, out, maxprime, H, W, C, pool, stride, bat
 
 
 # --------------------------------------------------------------- gpu:: ops
+
+class tpc:
+    """The 2-party protocol (src/mpc/TPC.h): a TPC tensor of n elements is a
+    CUDA tensor of shape (2, n), [party A, party B], whose value is the sum.
+    Names and argument meanings follow TPC.h's free functions."""
+
+    @staticmethod
+    def empty(n: int, ring: str = "u64", device="cuda"):
+        torch = _torch()
+        return torch.empty((2, n), dtype=getattr(torch, _TDT[ring]), device=device)
+
+    @staticmethod
+    def zeros(n: int, ring: str = "u64", device="cuda"):
+        torch = _torch()
+        return torch.zeros((2, n), dtype=getattr(torch, _TDT[ring]), device=device)
+
+    @staticmethod
+    def _p2(t):
+        if t.dim() != 2 or t.shape[0] != 2 or not t.is_cuda:
+            raise PiranhaError("expected a CUDA TPC tensor of shape (2, n)")
+        if not t.is_contiguous():
+            raise PiranhaError("TPC tensor must be contiguous")
+        return _P2(t[0].data_ptr(), t[1].data_ptr())
+
+    @staticmethod
+    def matmul(ctx: Context, a, b, c, M, N, K, transpose_a, transpose_b, transpose_c, truncation):
+        """matmul (TPC.inl:575-583)."""
+        fn = lib().pg_tpc_matmul_u64 if _ring(a) == "u64" else lib().pg_tpc_matmul_u32
+        ctx._check(fn(ctx.handle, tpc._p2(a), tpc._p2(b), tpc._p2(c), M, N, K, int(transpose_a), int(transpose_b),
+                      int(transpose_c), int(truncation)))
+        return c
+
+    @staticmethod
+    def fc_forward(ctx: Context, x, w, bias, out, batch, din, dout, fp=FLOAT_PRECISION):
+        """FCLayer::forward (FCLayer.cu:78-130) for TPC: matmul + per-party bias shares."""
+        fn = lib().pg_tpc_fc_forward_u64 if _ring(x) == "u64" else lib().pg_tpc_fc_forward_u32
+        bp = ctypes.cast(tpc._p2(bias), ctypes.c_void_p) if bias is not None else None
+        ctx._check(fn(ctx.handle, tpc._p2(x), tpc._p2(w), bp, tpc._p2(out), batch, din, dout, fp))
+        return out
+
+    @staticmethod
+    def convolution(ctx: Context, A, B, C, op, batchSize, imageHeight, imageWidth, filterSize, Din, Dout, stride,
+                    padding, truncation):
+        """convolution (TPC.inl:789-827)."""
+        ctx._check(lib().pg_tpc_conv_u64(ctx.handle, tpc._p2(A), tpc._p2(B), tpc._p2(C), int(op), batchSize,
+                                         imageHeight, imageWidth, filterSize, Din, Dout, stride, padding,
+                                         int(truncation)))
+        return C
+
+    @staticmethod
+    def dividePublic(ctx: Context, a, denominator):
+        """dividePublic (TPC.inl:371-401); the denominator is a scalar or a CUDA tensor."""
+        torch = _torch()
+        n = a.shape[1]
+        if isinstance(denominator, torch.Tensor):
+            ctx._check(lib().pg_tpc_divide_public_vec_u64(ctx.handle, tpc._p2(a), n,
+                                                          ctypes.c_void_p(denominator.data_ptr())))
+        elif _ring(a) == "u64":
+            ctx._check(lib().pg_tpc_divide_public_u64(ctx.handle, tpc._p2(a), n, int(denominator)))
+        else:
+            ctx._check(lib().pg_tpc_divide_public_u32(ctx.handle, tpc._p2(a), n, int(denominator)))
+        return a
+
+    @staticmethod
+    def reconstruct(ctx: Context, a, out):
+        """reconstruct (TPC.inl:552-572): out has shape (2, n), one row per party."""
+        fn = getattr(lib(), f"pg_tpc_reconstruct_{_ring(a)}")
+        ctx._check(fn(ctx.handle, tpc._p2(a), a.shape[1], tpc._p2(out)))
+        return out
+
+    @staticmethod
+    def mul_(ctx: Context, a, b):
+        """TPC *= TPC (TPC.inl:242-272), in place on a."""
+        ctx._check(lib().pg_tpc_mul_u64(ctx.handle, tpc._p2(a), tpc._p2(b), a.shape[1]))
+        return a
+
+    @staticmethod
+    def dReLU(ctx: Context, input, result):
+        """dReLU (TPC.inl:829-868): uint8 bit shares."""
+        fn = lib().pg_tpc_drelu_u64_u8 if _ring(input) == "u64" else lib().pg_tpc_drelu_u32_u8
+        ctx._check(fn(ctx.handle, tpc._p2(input), input.shape[1], tpc._p2(result)))
+        return result
+
+    @staticmethod
+    def ReLU(ctx: Context, input, result, dresult):
+        """ReLU (TPC.inl:871-884)."""
+        fn = lib().pg_tpc_relu_u64_u8 if _ring(input) == "u64" else lib().pg_tpc_relu_u32_u8
+        ctx._check(fn(ctx.handle, tpc._p2(input), input.shape[1], tpc._p2(result), tpc._p2(dresult)))
+        return result, dresult
+
+    @staticmethod
+    def selectShare(ctx: Context, x, y, b, z):
+        """selectShare (TPC.inl:586-610): z = b ? y : x."""
+        ctx._check(lib().pg_tpc_select_share_u64_u8(ctx.handle, tpc._p2(x), tpc._p2(y), tpc._p2(b), tpc._p2(z),
+                                                    x.shape[1]))
+        return z
+
+    @staticmethod
+    def maxpool(ctx: Context, input, result, dresult, k):
+        """maxpool (TPC.inl:887-1058) over rows of k values."""
+        ctx._check(lib().pg_tpc_maxpool_u64_u8(ctx.handle, tpc._p2(input), input.shape[1], int(k), tpc._p2(result),
+                                               tpc._p2(dresult)))
+        return result, dresult
+
 
 class gpu:
     """Single-array kernels of src/gpu (gemm.cuh, conv.cuh, matrix.cuh, bitwise.cuh, convolution.cuh)."""

@@ -223,6 +223,99 @@ def test_func_maxpool2(golden):
     assert_reveal(dres, a["dexpected"], fixed=False)
 
 
+# ---------------------------------------------- Func.cu cases, TPC (2PC)
+# The reference's Func tests are typed over RSS, TPC, FPC and OPC
+# (src/test/Func.cu:11), so the same expected values pin the TPC restatement.
+
+def tenc(vals, fixed=True):
+    return orc.tpc_from_list(vals, U64, FP, to_fixed=fixed)
+
+
+def assert_reveal_tpc(shares, expected, fixed=True):
+    rec = orc.tpc_reconstruct(shares)
+    for p in (0, 1):
+        got = orc.decode(rec[p], FP) if fixed else s64(rec[p].astype(U64)).astype(np.float64)
+        assert np.max(np.abs(got - np.asarray(expected, dtype=np.float64))) <= EPS, (p, got, expected)
+
+
+def test_tpc_func_reconstruct(golden):
+    c = golden[0]["Reconstruct"]["arrays"]
+    assert_reveal_tpc(tenc(c["a"]), c["expected"])
+
+
+@pytest.mark.parametrize("name", ["MatMul", "MatMul2"])
+def test_tpc_func_matmul(golden, name):
+    c = golden[0][name]
+    p, a = c["params"], c["arrays"]
+    comm = orc.Comm()
+    out = orc.tpc_matmul(tenc(a["a"]), tenc(a["b"]), p["M"], p["N"], p["K"], p["tA"], p["tB"], p["tC"], FP, comm)
+    assert_reveal_tpc(out, a["expected"])
+    # reveal e (M x K) and f (K x N), then the truncation's reveal (M x N)
+    n = p["M"] * p["K"] + p["K"] * p["N"] + p["M"] * p["N"]
+    assert comm.rounds == 3 and comm.tx[:2] == [n * 8] * 2
+
+
+def test_tpc_func_mult(golden):
+    a = golden[0]["Mult"]["arrays"]
+    assert_reveal_tpc(orc.tpc_mul(tenc(a["b"], False), tenc(a["a"], False)), a["expected"], fixed=False)
+
+
+@pytest.mark.parametrize("name", ["Truncate", "Truncate2"])
+def test_tpc_func_truncate(golden, name):
+    c = golden[0][name]
+    assert_reveal_tpc(orc.tpc_divide_public(tenc(c["arrays"]["a"]), c["params"]["d"]), c["arrays"]["expected"])
+
+
+def test_tpc_func_truncate_vec(golden):
+    a = golden[0]["TruncateVec"]["arrays"]
+    d = np.array([1 << int(x) for x in a["pows"]], dtype=U64)
+    assert_reveal_tpc(orc.tpc_divide_public(tenc(a["a"]), d), a["expected"])
+
+
+def test_tpc_func_select_share(golden):
+    a = golden[0]["SelectShare"]["arrays"]
+    z = orc.tpc_select_share(tenc(a["x"]), tenc(a["y"]), tenc(a["b"], False))
+    assert_reveal_tpc(z, a["expected"])
+
+
+@pytest.mark.parametrize("name", ["DRELU", "DRELU2"])
+def test_tpc_func_drelu(golden, name):
+    a = golden[0][name]["arrays"]
+    comm = orc.Comm()
+    res = orc.tpc_drelu(tenc(a["input"]), udtype=U64, comm=comm)
+    assert_reveal_tpc(res, a["expected"], fixed=False)
+    assert comm.rounds == 25  # 1 reveal + 6 carry levels x 2 ANDs x 2 reveals
+
+
+def test_tpc_func_drelu3(golden):
+    a = golden[0]["DRELU3"]["arrays"]
+    x = tenc(a["input"])
+    x = (x + u64(a["add"])[None, :]).astype(U64)  # the one share of each party += add
+    assert_reveal_tpc(orc.tpc_drelu(x, udtype=U64), a["expected"], fixed=False)
+
+
+def test_tpc_func_relu(golden):
+    a = golden[0]["RELU"]["arrays"]
+    out, dout = orc.tpc_relu(tenc(a["input"]), udtype=U64)
+    assert_reveal_tpc(out, a["expected"])
+    assert_reveal_tpc(dout, a["dexpected"], fixed=False)
+
+
+def test_tpc_func_maxpool(golden):
+    a = golden[0]["Maxpool"]["arrays"]
+    out, dout = orc.tpc_maxpool(tenc(a["input"]), 4, udtype=U64)
+    assert_reveal_tpc(out, a["expected"])
+    assert_reveal_tpc(dout, a["dexpected"], fixed=False)
+
+
+def test_tpc_func_convolution(golden):
+    c = golden[0]["Convolution"]
+    p, a = c["params"], c["arrays"]
+    out = orc.tpc_convolution(tenc(a["im"]), tenc(a["filters"]), orc.FPROP, p["batch"], p["H"], p["W"], p["f"],
+                              p["Din"], p["Dout"], p["stride"], p["pad"], FP)
+    assert_reveal_tpc(out, a["expected"])
+
+
 # ----------------------------------------------------------- Layer.cu cases
 
 def test_layer_relu_basic(golden):
