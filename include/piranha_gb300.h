@@ -213,6 +213,56 @@ int pg_tpc_select_share_u64_u8(pg_ctx *ctx, const uint64_t *const x[2], const ui
 int pg_tpc_maxpool_u64_u8(pg_ctx *ctx, const uint64_t *const in[2], size_t n, int k, uint64_t *const out[2],
                           uint8_t *const dout[2]);
 
+/* --------------------------------------------------------- FPC (4PC) protocol
+ * src/mpc/FPC.h, FPC.inl: four-party replicated shares. An FPC tensor of n
+ * elements is TWELVE device pointers, index party * 3 + share with parties
+ * A..D = 0..3 and shares shareA/shareB/shareC = 0..2; party p's share k holds
+ * component x_{(p+1+k) mod 4} of x = x0 + x1 + x2 + x3 (FPC.inl:948-953), and
+ * public values live in x0 (B.shareC, C.shareB, D.shareA: FPC.inl:120-155).
+ * Every party's arrays come out as the reference computes them at that party,
+ * including the reshare's per-party cross terms (reshareFPC, FPC.inl:1184-1259).
+ * Counters: reconstruct sends n elements from every party to the next (1
+ * round); each of a product's six reshares sends n elements from party I to
+ * party G (1 round each). */
+/* matmul (FPC.inl:636-670): local products, six reshares, dividePublic */
+int pg_fpc_matmul_u64(pg_ctx *ctx, const uint64_t *const a[12], const uint64_t *const b[12], uint64_t *const c[12],
+                      int M, int N, int K, int tA, int tB, int tC, int trunc);
+int pg_fpc_matmul_u32(pg_ctx *ctx, const uint32_t *const a[12], const uint32_t *const b[12], uint32_t *const c[12],
+                      int M, int N, int K, int tA, int tB, int tC, int trunc);
+/* FCLayer::forward (src/nn/FCLayer.cu:78-130) for FPC: matmul(tA=tB=tC=1, FP)
+ * then every share adds its bias share; bias may be NULL */
+int pg_fpc_fc_forward_u64(pg_ctx *ctx, const uint64_t *const x[12], const uint64_t *const w[12],
+                          const uint64_t *const bias[12], uint64_t *const out[12], int batch, int din, int dout, int fp);
+int pg_fpc_fc_forward_u32(pg_ctx *ctx, const uint32_t *const x[12], const uint32_t *const w[12],
+                          const uint32_t *const bias[12], uint32_t *const out[12], int batch, int din, int dout, int fp);
+/* convolution (FPC.inl:862-925 with localFprop/Dgrad/Wgrad :745-860) */
+int pg_fpc_conv_u64(pg_ctx *ctx, const uint64_t *const A[12], const uint64_t *const B[12], uint64_t *const C[12],
+                    int op, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad, int trunc);
+/* dividePublic (FPC.inl:576-608), in place */
+int pg_fpc_divide_public_u64(pg_ctx *ctx, uint64_t *const a[12], size_t n, uint64_t d);
+int pg_fpc_divide_public_vec_u64(pg_ctx *ctx, uint64_t *const a[12], size_t n, const uint64_t *d);
+int pg_fpc_divide_public_u32(pg_ctx *ctx, uint32_t *const a[12], size_t n, uint32_t d);
+/* reconstruct (FPC.inl:611-634): out[p] = party p's three shares plus the
+ * previous party's shareA, for the four parties */
+int pg_fpc_reconstruct_u64(pg_ctx *ctx, const uint64_t *const a[12], size_t n, uint64_t *const out[4]);
+int pg_fpc_reconstruct_u32(pg_ctx *ctx, const uint32_t *const a[12], size_t n, uint32_t *const out[4]);
+int pg_fpc_reconstruct_u8(pg_ctx *ctx, const uint8_t *const a[12], size_t n, uint8_t *const out[4]);
+/* FPC *= FPC (FPC.inl:322-364) and &= (:375-399), in place on a */
+int pg_fpc_mul_u64(pg_ctx *ctx, uint64_t *const a[12], const uint64_t *const b[12], size_t n);
+int pg_fpc_and_u8(pg_ctx *ctx, uint8_t *const a[12], const uint8_t *const b[12], size_t n);
+/* dReLU (FPC.inl:930-990), ReLU (:992-1003), selectShare (:672-711),
+ * maxpool over rows of k values, k a power of two (:1005-1177) */
+int pg_fpc_drelu_u64_u8(pg_ctx *ctx, const uint64_t *const in[12], size_t n, uint8_t *const out[12]);
+int pg_fpc_drelu_u32_u8(pg_ctx *ctx, const uint32_t *const in[12], size_t n, uint8_t *const out[12]);
+int pg_fpc_relu_u64_u8(pg_ctx *ctx, const uint64_t *const in[12], size_t n, uint64_t *const out[12],
+                       uint8_t *const dout[12]);
+int pg_fpc_relu_u32_u8(pg_ctx *ctx, const uint32_t *const in[12], size_t n, uint32_t *const out[12],
+                       uint8_t *const dout[12]);
+int pg_fpc_select_share_u64_u8(pg_ctx *ctx, const uint64_t *const x[12], const uint64_t *const y[12],
+                               const uint8_t *const b[12], uint64_t *const z[12], size_t n);
+int pg_fpc_maxpool_u64_u8(pg_ctx *ctx, const uint64_t *const in[12], size_t n, int k, uint64_t *const out[12],
+                          uint8_t *const dout[12]);
+
 /* ---------------------------------------------- share-GEMM without allocation
  * No counterpart in the reference. The same result as pg_rss_matmul_u64, bit
  * for bit, computed by the limb tensor-core kernels, for callers that must not

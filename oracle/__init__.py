@@ -11,7 +11,10 @@ Array conventions
 * an RSS tensor of n elements is a numpy array of shape ``(3, 2, n)``:
   ``[party A/B/C][shareA/shareB][element]``;
 * per-party public data (the output of ``reconstruct``) has shape ``(3, n)``;
-* ``Comm`` accumulates the bytes each party sends/receives and the rounds.
+* a TPC tensor has shape ``(2, n)`` and an FPC tensor ``(4, 3, n)``
+  (``[party A..D][shareA/shareB/shareC][element]``);
+* ``Comm`` accumulates the bytes each party sends/receives and the rounds
+  (``Comm(4)`` reports all four parties).
 """
 from __future__ import annotations
 
@@ -59,16 +62,17 @@ def _p(a):
 class Comm:
     """Per-party byte counters and the round counter (one round per protocol step)."""
 
-    def __init__(self):
+    def __init__(self, parties=3):
+        self.parties = parties
         self.buf = np.zeros(9, dtype=np.uint64)
 
     @property
     def tx(self):
-        return [int(x) for x in self.buf[:3]]
+        return [int(x) for x in self.buf[:self.parties]]
 
     @property
     def rx(self):
-        return [int(x) for x in self.buf[4:7]]
+        return [int(x) for x in self.buf[4:4 + self.parties]]
 
     @property
     def rounds(self):
@@ -524,5 +528,155 @@ def tpc_maxpool(x, k, udtype=np.uint8, comm=None):
     dout = np.empty((2, n), dtype=udtype)
     comm = comm or Comm()
     getattr(lib(), f"or_tpc_maxpool_{_bits_suffix(dt, udtype)}")(_p(x), ctypes.c_size_t(n), k, _p(out), _p(dout),
+                                                                 comm.ptr())
+    return out, dout
+
+
+# ------------------------------------------------------------------- FPC
+# An FPC tensor of n elements is a numpy array of shape (4, 3, n):
+# [party A/B/C/D][shareA/shareB/shareC][element]; party p's share k holds the
+# component x_{(p+1+k) mod 4} of x = x0 + x1 + x2 + x3 (src/mpc/FPC.inl:948-953).
+
+def _fviews(a, dtype, n=None):
+    a = np.ascontiguousarray(a, dtype=dtype)
+    if a.ndim != 3 or a.shape[:2] != (4, 3) or (n is not None and a.shape[2] != n):
+        raise ValueError(f"expected FPC views of shape (4, 3, {n}), got {a.shape}")
+    return a
+
+
+def fpc_from_list(vals, dtype=np.uint64, fp=FP_DEFAULT, to_fixed=True):
+    """setPublic / initializer list (FPC.inl:127-155, :528-565): component x0 holds the values."""
+    dt = np.dtype(dtype).type
+    v = np.ascontiguousarray(vals, dtype=np.float64).ravel()
+    out = np.empty((4, 3, v.size), dtype=dt)
+    getattr(lib(), f"or_fpc_from_list_{_SUF[dt]}")(_p(v), ctypes.c_size_t(v.size), fp, int(to_fixed), _p(out))
+    return out
+
+
+def fpc_share_random(secret, dtype=np.uint64, seed=0):
+    """A consistent 4-party replicated sharing of `secret` with seeded random x1, x2, x3."""
+    dt = np.dtype(dtype).type
+    s = np.ascontiguousarray(secret, dtype=dt).ravel()
+    rng = np.random.default_rng(seed)
+    comp = [None] + [rng.integers(0, np.iinfo(dt).max, size=s.size, dtype=dt, endpoint=True) for _ in range(3)]
+    comp[0] = (s - comp[1] - comp[2] - comp[3]).astype(dt)
+    out = np.empty((4, 3, s.size), dtype=dt)
+    for p in range(4):
+        for k in range(3):
+            out[p, k] = comp[(p + 1 + k) % 4]
+    return out
+
+
+def fpc_reconstruct(a, comm=None):
+    """reconstruct (FPC.inl:611-634): own three shares plus the previous party's shareA."""
+    dt = np.asarray(a).dtype.type
+    a = _fviews(a, dt)
+    n = a.shape[2]
+    out = np.empty((4, n), dtype=dt)
+    comm = comm or Comm(4)
+    getattr(lib(), f"or_fpc_reconstruct_{_SUF[dt]}")(_p(a), ctypes.c_size_t(n), _p(out), comm.ptr())
+    return out
+
+
+def fpc_matmul(a, b, M, N, K, tA, tB, tC, trunc, comm=None):
+    """FPC matmul (FPC.inl:636-670): local products, six reshares, dividePublic."""
+    dt, suf = _ring(np.asarray(a).dtype)
+    a = _fviews(a, dt, M * K)
+    b = _fviews(b, dt, K * N)
+    c = np.empty((4, 3, M * N), dtype=dt)
+    comm = comm or Comm(4)
+    getattr(lib(), f"or_fpc_matmul_{suf}")(_p(a), _p(b), _p(c), M, N, K, int(tA), int(tB), int(tC), trunc,
+                                           comm.ptr())
+    return c
+
+
+def fpc_convolution(a, b, op, batch, H, W, f, Din, Dout, stride, pad, trunc, comm=None):
+    """FPC convolution (FPC.inl:862-925)."""
+    dt, suf = _ring(np.asarray(a).dtype)
+    a = _fviews(a, dt)
+    b = _fviews(b, dt)
+    n_out = conv_out_size(op, batch, H, W, f, Din, Dout, stride, pad)
+    c = np.empty((4, 3, n_out), dtype=dt)
+    comm = comm or Comm(4)
+    getattr(lib(), f"or_fpc_conv_{suf}")(_p(a), ctypes.c_size_t(a.shape[2]), _p(b), ctypes.c_size_t(b.shape[2]),
+                                         _p(c), op, batch, H, W, f, Din, Dout, stride, pad, trunc, comm.ptr())
+    return c
+
+
+def fpc_divide_public(a, d, comm=None):
+    dt, suf = _ring(np.asarray(a).dtype)
+    a = _fviews(a, dt).copy()
+    n = a.shape[2]
+    dv = np.ascontiguousarray(np.atleast_1d(np.asarray(d, dtype=dt)))
+    vec = dv.size > 1 or (np.ndim(d) > 0)
+    if vec and dv.size != n:
+        raise ValueError("denominator vector size mismatch")
+    comm = comm or Comm(4)
+    getattr(lib(), f"or_fpc_divide_public_{suf}")(_p(a), ctypes.c_size_t(n), _p(dv), int(vec), comm.ptr())
+    return a
+
+
+def fpc_mul(a, b, comm=None):
+    dt, suf = _ring(np.asarray(a).dtype)
+    a = _fviews(a, dt).copy()
+    b = _fviews(b, dt, a.shape[2])
+    comm = comm or Comm(4)
+    getattr(lib(), f"or_fpc_mul_{suf}")(_p(a), _p(b), ctypes.c_size_t(a.shape[2]), comm.ptr())
+    return a
+
+
+def fpc_and(a, b, comm=None):
+    dt = np.asarray(a).dtype.type
+    a = _fviews(a, dt).copy()
+    b = _fviews(b, dt, a.shape[2])
+    comm = comm or Comm(4)
+    getattr(lib(), f"or_fpc_and_{_SUF[dt]}")(_p(a), _p(b), ctypes.c_size_t(a.shape[2]), comm.ptr())
+    return a
+
+
+def fpc_drelu(x, udtype=np.uint8, comm=None):
+    dt, _ = _ring(np.asarray(x).dtype)
+    x = _fviews(x, dt)
+    n = x.shape[2]
+    out = np.empty((4, 3, n), dtype=udtype)
+    comm = comm or Comm(4)
+    getattr(lib(), f"or_fpc_drelu_{_bits_suffix(dt, udtype)}")(_p(x), ctypes.c_size_t(n), _p(out), comm.ptr())
+    return out
+
+
+def fpc_relu(x, udtype=np.uint8, comm=None):
+    dt, _ = _ring(np.asarray(x).dtype)
+    x = _fviews(x, dt)
+    n = x.shape[2]
+    out = np.empty((4, 3, n), dtype=dt)
+    dout = np.empty((4, 3, n), dtype=udtype)
+    comm = comm or Comm(4)
+    getattr(lib(), f"or_fpc_relu_{_bits_suffix(dt, udtype)}")(_p(x), ctypes.c_size_t(n), _p(out), _p(dout),
+                                                              comm.ptr())
+    return out, dout
+
+
+def fpc_select_share(x, y, b, comm=None):
+    dt, _ = _ring(np.asarray(x).dtype)
+    x = _fviews(x, dt)
+    n = x.shape[2]
+    y = _fviews(y, dt, n)
+    b = np.ascontiguousarray(b)
+    z = np.empty((4, 3, n), dtype=dt)
+    comm = comm or Comm(4)
+    getattr(lib(), f"or_fpc_select_share_{_bits_suffix(dt, b.dtype)}")(_p(x), _p(y), _p(b), ctypes.c_size_t(n),
+                                                                       _p(z), comm.ptr())
+    return z
+
+
+def fpc_maxpool(x, k, udtype=np.uint8, comm=None):
+    """FPC maxpool tournament (FPC.inl:1005-1177) over rows of k (padded) values."""
+    dt, _ = _ring(np.asarray(x).dtype)
+    x = _fviews(x, dt)
+    n = x.shape[2]
+    out = np.empty((4, 3, n // k), dtype=dt)
+    dout = np.empty((4, 3, n), dtype=udtype)
+    comm = comm or Comm(4)
+    getattr(lib(), f"or_fpc_maxpool_{_bits_suffix(dt, udtype)}")(_p(x), ctypes.c_size_t(n), k, _p(out), _p(dout),
                                                                  comm.ptr())
     return out, dout

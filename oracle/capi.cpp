@@ -354,3 +354,132 @@ extern "C" int or_tpc_reconstruct_u8(const uint8_t* a, size_t n, uint8_t* out, u
     for (int p = 0; p < 2; p++) std::memcpy(out + (size_t)p * n, o[p].data(), n);
     return 0;
 }
+
+// ------------------------------------------------------------------- FPC
+// An FPC tensor crosses as one flat array [party(4)][share(3)][n].
+
+namespace {
+template <typename T> void fload(FPCV<T>& r, const T* flat, size_t n) {
+    r.resize(n);
+    for (int p = 0; p < 4; p++)
+        for (int k = 0; k < 3; k++) std::memcpy(r.s[p][k].data(), flat + ((size_t)p * 3 + k) * n, n * sizeof(T));
+}
+template <typename T> void fstore(const FPCV<T>& r, T* flat) {
+    for (int p = 0; p < 4; p++)
+        for (int k = 0; k < 3; k++) std::memcpy(flat + ((size_t)p * 3 + k) * r.n, r.s[p][k].data(), r.n * sizeof(T));
+}
+}  // namespace
+
+#define OR_FPC(T, SUF)                                                                                       \
+    extern "C" int or_fpc_matmul_##SUF(const T* a, const T* b, T* c, int M, int N, int K, int tA, int tB,     \
+                                       int tC, int trunc, uint64_t* comm) {                                  \
+        FPCV<T> A, B, C;                                                                                     \
+        fload(A, a, (size_t)M * K);                                                                          \
+        fload(B, b, (size_t)K * N);                                                                          \
+        CommIO io(comm);                                                                                     \
+        fpc_matmul<T>(A, B, C, M, N, K, tA, tB, tC, trunc, io.c);                                            \
+        fstore(C, c);                                                                                        \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_fpc_conv_##SUF(const T* a, size_t na, const T* b, size_t nb, T* c, int op, int batch,   \
+                                     int H, int W, int f, int Din, int Dout, int stride, int pad, int trunc,  \
+                                     uint64_t* comm) {                                                       \
+        FPCV<T> A, B, C;                                                                                     \
+        fload(A, a, na);                                                                                     \
+        fload(B, b, nb);                                                                                     \
+        CommIO io(comm);                                                                                     \
+        fpc_convolution<T>(A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc, io.c);                \
+        fstore(C, c);                                                                                        \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_fpc_divide_public_##SUF(T* a, size_t n, const T* d, int vector_d, uint64_t* comm) {     \
+        FPCV<T> A;                                                                                           \
+        fload(A, a, n);                                                                                      \
+        CommIO io(comm);                                                                                     \
+        fpc_divide_public<T>(A, d, vector_d != 0, io.c);                                                     \
+        fstore(A, a);                                                                                        \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_fpc_reconstruct_##SUF(const T* a, size_t n, T* out, uint64_t* comm) {                  \
+        FPCV<T> A;                                                                                           \
+        fload(A, a, n);                                                                                      \
+        std::vector<T> o[4];                                                                                 \
+        CommIO io(comm);                                                                                     \
+        fpc_reconstruct<T>(A, whole(n), o, io.c);                                                            \
+        for (int p = 0; p < 4; p++) std::memcpy(out + (size_t)p * n, o[p].data(), n * sizeof(T));            \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_fpc_mul_##SUF(T* a, const T* b, size_t n, uint64_t* comm) {                            \
+        FPCV<T> A, B;                                                                                        \
+        fload(A, a, n);                                                                                      \
+        fload(B, b, n);                                                                                      \
+        CommIO io(comm);                                                                                     \
+        fpc_mul_assign<T>(A, whole(n), B, whole(n), io.c);                                                   \
+        fstore(A, a);                                                                                        \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_fpc_and_##SUF(T* a, const T* b, size_t n, uint64_t* comm) {                            \
+        FPCV<T> A, B;                                                                                        \
+        fload(A, a, n);                                                                                      \
+        fload(B, b, n);                                                                                      \
+        CommIO io(comm);                                                                                     \
+        fpc_and_assign<T>(A, whole(n), B, whole(n), io.c);                                                   \
+        fstore(A, a);                                                                                        \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_fpc_from_list_##SUF(const double* v, size_t n, int fp, int to_fixed, T* out) {         \
+        FPCV<T> A(n);                                                                                        \
+        fpc_from_list<T>(A, v, fp, to_fixed != 0);                                                           \
+        fstore(A, out);                                                                                      \
+        return 0;                                                                                            \
+    }
+
+#define OR_FPC_BITS(T, U, SUF)                                                                               \
+    extern "C" int or_fpc_drelu_##SUF(const T* in, size_t n, U* out, uint64_t* comm) {                       \
+        FPCV<T> A;                                                                                           \
+        fload(A, in, n);                                                                                     \
+        FPCV<U> R;                                                                                           \
+        CommIO io(comm);                                                                                     \
+        fpc_drelu<T, U>(A, whole(n), R, io.c);                                                               \
+        fstore(R, out);                                                                                      \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_fpc_relu_##SUF(const T* in, size_t n, T* out, U* dout, uint64_t* comm) {               \
+        FPCV<T> A, O;                                                                                        \
+        fload(A, in, n);                                                                                     \
+        FPCV<U> D;                                                                                           \
+        CommIO io(comm);                                                                                     \
+        fpc_relu<T, U>(A, O, D, io.c);                                                                       \
+        fstore(O, out);                                                                                      \
+        fstore(D, dout);                                                                                     \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_fpc_select_share_##SUF(const T* x, const T* y, const U* b, size_t n, T* z,             \
+                                             uint64_t* comm) {                                               \
+        FPCV<T> X, Y, Z(n);                                                                                  \
+        fload(X, x, n);                                                                                      \
+        fload(Y, y, n);                                                                                      \
+        FPCV<U> B;                                                                                           \
+        fload(B, b, n);                                                                                      \
+        CommIO io(comm);                                                                                     \
+        fpc_select_share<T, U>(X, whole(n), Y, whole(n), B, Z, whole(n), io.c);                              \
+        fstore(Z, z);                                                                                        \
+        return 0;                                                                                            \
+    }                                                                                                        \
+    extern "C" int or_fpc_maxpool_##SUF(const T* in, size_t n, int k, T* out, U* dout, uint64_t* comm) {     \
+        FPCV<T> A, O;                                                                                        \
+        fload(A, in, n);                                                                                     \
+        FPCV<U> D;                                                                                           \
+        CommIO io(comm);                                                                                     \
+        fpc_maxpool<T, U>(A, O, D, k, io.c);                                                                 \
+        fstore(O, out);                                                                                      \
+        fstore(D, dout);                                                                                     \
+        return 0;                                                                                            \
+    }
+
+OR_FPC(uint64_t, u64)
+OR_FPC(uint32_t, u32)
+OR_FPC(uint8_t, u8)
+OR_FPC_BITS(uint64_t, uint8_t, u64_u8)
+OR_FPC_BITS(uint64_t, uint64_t, u64_u64)
+OR_FPC_BITS(uint32_t, uint8_t, u32_u8)

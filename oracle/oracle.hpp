@@ -999,4 +999,372 @@ void tpc_maxpool(TPCV<T>& input, TPCV<T>& result, TPCV<U>& dresult, int k, Comm&
     level(true);
 }
 
+
+// ========================================================================
+// FPC: 4-party replicated sharing (src/mpc/FPC.h, FPC.inl). x = x0+x1+x2+x3;
+// party p (A=0 .. D=3) holds the three components it is not named after,
+// share k = component (p+1+k) mod 4 (FPC.inl:948-953). Public values and
+// public DeviceData added, subtracted or XORed go into component x0 only,
+// held by B as shareC, C as shareB and D as shareA (FPC.inl:120-125,
+// :184-260); *=, &=, >>= and <<= by public data touch every share.
+// Products reshare their cross terms with reshareFPC (FPC.inl:1184-1259),
+// whose PRG masks are zero.
+// ========================================================================
+
+template <typename T> struct FPCV {
+    size_t n = 0;
+    std::vector<T> s[4][3];
+    FPCV() {}
+    explicit FPCV(size_t n_) { resize(n_); }
+    void resize(size_t n_) {
+        n = n_;
+        for (int p = 0; p < 4; p++)
+            for (int k = 0; k < 3; k++) s[p][k].assign(n, (T)0);
+    }
+};
+
+// the share index at which party p holds component c (c != p): FPC.inl:498-504
+static inline int fpc_share_of(int p, int c) { return (3 - p + c) % 4; }
+static inline int fpc_x0_share(int p) { return p == 0 ? -1 : fpc_share_of(p, 0); }
+
+// fill (FPC.inl:120-125)
+template <typename T> void fpc_fill(FPCV<T>& a, T val) {
+    for (int p = 0; p < 4; p++)
+        for (int k = 0; k < 3; k++) std::fill(a.s[p][k].begin(), a.s[p][k].end(), k == fpc_x0_share(p) ? val : (T)0);
+}
+
+// setPublic (FPC.inl:127-155) and the initializer list (:528-565)
+template <typename T> void fpc_from_list(FPCV<T>& a, const double* vals, int fp, bool to_fixed) {
+    fpc_fill<T>(a, 0);
+    for (int p = 1; p < 4; p++)
+        for (size_t i = 0; i < a.n; i++)
+            a.s[p][fpc_x0_share(p)][i] = to_fixed ? encode_fixed<T>(vals[i], fp) : (T)(int64_t)vals[i];
+}
+
+// reconstruct (FPC.inl:611-634): shareA goes to the next party; the result is
+// the own three shares plus the previous party's shareA.
+template <typename T> void fpc_reconstruct(const FPCV<T>& in, Strided w, std::vector<T> (&out)[4], Comm& comm) {
+    for (int p = 0; p < 4; p++) {
+        int prev = (p + 3) % 4;
+        out[p].resize(w.size);
+        for (size_t i = 0; i < w.size; i++) {
+            size_t j = w.offset + i * w.stride;
+            out[p][i] = (T)(in.s[p][0][j] + in.s[p][1][j] + in.s[p][2][j] + in.s[prev][0][j]);
+        }
+    }
+    comm.msg(4, w.size * sizeof(T), w.size * sizeof(T));
+    comm.rounds++;
+}
+
+template <typename T> static FPCV<T> fpc_gather(const FPCV<T>& a, Strided w) {
+    FPCV<T> r(w.size);
+    for (int p = 0; p < 4; p++)
+        for (int k = 0; k < 3; k++)
+            for (size_t i = 0; i < w.size; i++) r.s[p][k][i] = a.s[p][k][w.offset + i * w.stride];
+    return r;
+}
+template <typename T> static void fpc_scatter(FPCV<T>& a, Strided w, const FPCV<T>& r) {
+    for (int p = 0; p < 4; p++)
+        for (int k = 0; k < 3; k++)
+            for (size_t i = 0; i < w.size; i++) a.s[p][k][w.offset + i * w.stride] = r.s[p][k][i];
+}
+
+// partyG / partyH (FPC.inl:452-496)
+static inline int fpc_party_g(int i, int j) {
+    static const int g[4][4] = {{-1, 2, 1, 1}, {-1, -1, 3, 2}, {-1, -1, -1, 0}, {-1, -1, -1, -1}};
+    return g[i][j];
+}
+static inline int fpc_party_h(int i, int j) {
+    static const int h[4][4] = {{-1, 3, 3, 2}, {-1, -1, 0, 0}, {-1, -1, -1, 1}, {-1, -1, -1, -1}};
+    return h[i][j];
+}
+
+// reshareFPC (FPC.inl:1184-1259) of the per-party cross terms z / zPrime
+// (zPrime when I and J are opposites). Parties I and J add their own term to
+// the share holding component H; G adds the term I sent it; H does nothing.
+template <typename T>
+void fpc_reshare(const std::vector<T> (&z)[4], const std::vector<T> (&zp)[4], int I, int J, FPCV<T>& out, Comm& comm) {
+    int G = fpc_party_g(I, J), H = fpc_party_h(I, J);
+    bool opp = (I - J == 2) || (J - I == 2);
+    size_t n = out.n;
+    for (int p = 0; p < 4; p++) {
+        if (p == H) continue;
+        int src = p == G ? I : p;
+        const std::vector<T>& mask = opp ? zp[src] : z[src];
+        std::vector<T>& dst = out.s[p][fpc_share_of(p, H)];
+        for (size_t i = 0; i < n; i++) dst[i] = (T)(dst[i] + mask[i]);
+    }
+    comm.tx[I] += n * sizeof(T);
+    comm.rx[G] += n * sizeof(T);
+    comm.rounds++;
+}
+
+template <typename T> static void fpc_reshare_all(const std::vector<T> (&z)[4], const std::vector<T> (&zp)[4], FPCV<T>& out,
+                                                  Comm& comm) {
+    static const int pairs[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+    for (auto& pr : pairs) fpc_reshare<T>(z, zp, pr[0], pr[1], out, comm);
+}
+
+// FPC *= FPC (FPC.inl:322-364) and FPC &= FPC (:375-399, XOR for + and AND
+// for *; the reshare still adds) on the view wa of a, with b viewed by wb.
+template <typename T, bool BOOL>
+void fpc_mul_like(FPCV<T>& a, Strided wa, const FPCV<T>& b, Strided wb, Comm& comm) {
+    size_t n = wb.size;
+    FPCV<T> self = fpc_gather(a, wa), rhs = fpc_gather(b, wb);
+    auto mul = [](T x, T y) { return BOOL ? (T)(x & y) : (T)(x * y); };
+    auto add = [](T x, T y) { return BOOL ? (T)(x ^ y) : (T)(x + y); };
+    std::vector<T> z[4], zp[4];
+    for (int p = 0; p < 4; p++) {
+        z[p].resize(n);
+        zp[p].resize(n);
+        const auto& s = self.s[p];
+        const auto& r = rhs.s[p];
+        for (size_t i = 0; i < n; i++) {
+            z[p][i] = add(mul(s[0][i], r[1][i]), mul(s[1][i], r[0][i]));
+            zp[p][i] = add(mul(s[0][i], r[2][i]), mul(s[2][i], r[0][i]));
+        }
+        for (int k = 0; k < 3; k++)
+            for (size_t i = 0; i < n; i++) self.s[p][k][i] = mul(self.s[p][k][i], r[k][i]);
+    }
+    fpc_reshare_all<T>(z, zp, self, comm);
+    fpc_scatter(a, wa, self);
+}
+template <typename T> void fpc_mul_assign(FPCV<T>& a, Strided wa, const FPCV<T>& b, Strided wb, Comm& comm) {
+    fpc_mul_like<T, false>(a, wa, b, wb, comm);
+}
+template <typename U> void fpc_and_assign(FPCV<U>& a, Strided wa, const FPCV<U>& b, Strided wb, Comm& comm) {
+    fpc_mul_like<U, true>(a, wa, b, wb, comm);
+}
+
+// FPC ^= FPC: local (FPC.inl:366-372)
+template <typename U> void fpc_xor_assign(FPCV<U>& a, Strided wa, const FPCV<U>& b, Strided wb) {
+    for (int p = 0; p < 4; p++)
+        for (int k = 0; k < 3; k++)
+            for (size_t i = 0; i < wb.size; i++) a.s[p][k][wa.offset + i * wa.stride] ^= b.s[p][k][wb.offset + i * wb.stride];
+}
+
+// dividePublic (FPC.inl:576-608) with getDividedShares (Precompute.h:107-133):
+// r = fill(1) and r' = d (scalar or per element), both in component x0.
+template <typename T> void fpc_divide_public(FPCV<T>& a, const T* d, bool vec, Comm& comm) {
+    for (int p = 1; p < 4; p++) {
+        auto& x0 = a.s[p][fpc_x0_share(p)];
+        for (size_t i = 0; i < a.n; i++) x0[i] = (T)(x0[i] - (vec ? d[i] : d[0]));  // a -= r'
+    }
+    std::vector<T> rec[4];
+    fpc_reconstruct(a, whole(a.n), rec, comm);
+    for (int p = 0; p < 4; p++) {
+        for (int k = 0; k < 3; k++) std::fill(a.s[p][k].begin(), a.s[p][k].end(), (T)0);  // a.zero()
+        if (p == 0) continue;  // party A holds no x0: r and the quotient do not reach it
+        auto& x0 = a.s[p][fpc_x0_share(p)];
+        for (size_t i = 0; i < a.n; i++) x0[i] = (T)(1 + div_public<T>(rec[p][i], vec ? d[i] : d[0]));
+    }
+}
+
+// matmul (FPC.inl:636-670): diagonal products per share, cross terms into
+// z = a0 b1 + a1 b0 and z' = a0 b2 + a2 b0, six reshares, dividePublic.
+template <typename T>
+void fpc_matmul(const FPCV<T>& a, const FPCV<T>& b, FPCV<T>& c, int M, int N, int K, bool tA, bool tB, bool tC,
+                int trunc, Comm& comm) {
+    size_t mn = (size_t)M * N;
+    c.resize(mn);
+    std::vector<T> z[4], zp[4], t(mn);
+    for (int p = 0; p < 4; p++) {
+        const auto& A = a.s[p];
+        const auto& B = b.s[p];
+        for (int k = 0; k < 3; k++) gemm<T>(M, N, K, A[k].data(), tA, B[k].data(), tB, c.s[p][k].data(), tC);
+        z[p].assign(mn, 0);
+        zp[p].assign(mn, 0);
+        gemm<T>(M, N, K, A[0].data(), tA, B[1].data(), tB, t.data(), tC);
+        for (size_t i = 0; i < mn; i++) z[p][i] = (T)(z[p][i] + t[i]);
+        gemm<T>(M, N, K, A[1].data(), tA, B[0].data(), tB, t.data(), tC);
+        for (size_t i = 0; i < mn; i++) z[p][i] = (T)(z[p][i] + t[i]);
+        gemm<T>(M, N, K, A[0].data(), tA, B[2].data(), tB, t.data(), tC);
+        for (size_t i = 0; i < mn; i++) zp[p][i] = (T)(zp[p][i] + t[i]);
+        gemm<T>(M, N, K, A[2].data(), tA, B[0].data(), tB, t.data(), tC);
+        for (size_t i = 0; i < mn; i++) zp[p][i] = (T)(zp[p][i] + t[i]);
+    }
+    fpc_reshare_all<T>(z, zp, c, comm);
+    T d = (T)((T)1 << trunc);
+    fpc_divide_public(c, &d, false, comm);
+}
+
+// convolution (FPC.inl:862-925) with localFprop/Dgrad/Wgrad (:745-860).
+template <typename T>
+void fpc_convolution(const FPCV<T>& A, const FPCV<T>& B, FPCV<T>& C, int op, int batch, int H, int W, int f,
+                     int Din, int Dout, int stride, int pad, int trunc, Comm& comm) {
+    ConvShape sh{batch, H, W, Din, Dout, f, f, pad, stride};
+    size_t out_n = op == CONV_FPROP ? (size_t)batch * sh.P() * sh.Q() * Dout
+                 : op == CONV_DGRAD ? (size_t)batch * H * W * Din
+                                    : (size_t)Dout * f * f * Din;
+    C.resize(out_n);
+    std::vector<T> z[4], zp[4], t(out_n);
+    for (int p = 0; p < 4; p++) {
+        const auto& a = A.s[p];
+        const auto& b = B.s[p];
+        for (int k = 0; k < 3; k++) conv_any<T>(op, sh, a[k].data(), b[k].data(), C.s[p][k].data());
+        z[p].assign(out_n, 0);
+        zp[p].assign(out_n, 0);
+        conv_any<T>(op, sh, a[0].data(), b[1].data(), t.data());
+        for (size_t i = 0; i < out_n; i++) z[p][i] = (T)(z[p][i] + t[i]);
+        conv_any<T>(op, sh, a[1].data(), b[0].data(), t.data());
+        for (size_t i = 0; i < out_n; i++) z[p][i] = (T)(z[p][i] + t[i]);
+        conv_any<T>(op, sh, a[0].data(), b[2].data(), t.data());
+        for (size_t i = 0; i < out_n; i++) zp[p][i] = (T)(zp[p][i] + t[i]);
+        conv_any<T>(op, sh, a[2].data(), b[0].data(), t.data());
+        for (size_t i = 0; i < out_n; i++) zp[p][i] = (T)(zp[p][i] + t[i]);
+    }
+    fpc_reshare_all<T>(z, zp, C, comm);
+    T d = (T)((T)1 << trunc);
+    fpc_divide_public(C, &d, false, comm);
+}
+
+// carryOut (FPC.inl:1297-1416): the same tree with FPC ANDs.
+template <typename U> void fpc_carry_out(FPCV<U>& p, FPCV<U>& g, int k, FPCV<U>& out, Comm& comm) {
+    size_t N = p.n;
+    size_t stride = 2, offset = 1;
+    Strided pEven = strided(N, 0, stride), pOdd = strided(N, offset, stride);
+    Strided gEven = strided(N, 0, stride), gOdd = strided(N, offset, stride);
+    while (k > 1) {
+        fpc_and_assign(g, gEven, p, pOdd, comm);
+        fpc_and_assign(p, pEven, p, pOdd, comm);
+        fpc_xor_assign(g, gOdd, g, gEven);
+        gEven = strided(N, offset, stride * 2);
+        offset += stride;
+        gOdd = strided(N, offset, stride * 2);
+        stride *= 2;
+        pEven = strided(N, 0, stride);
+        pOdd = strided(N, stride / 2, stride);
+        k /= 2;
+    }
+    Strided oE = strided(out.n, 0, 2), oO = strided(out.n, 1, 2);
+    for (int q = 0; q < 4; q++)
+        for (int s = 0; s < 3; s++) {
+            for (size_t i = 0; i < gEven.size && i < oE.size; i++)
+                out.s[q][s][oE.offset + i * 2] = g.s[q][s][gEven.offset + i * gEven.stride];
+            for (size_t i = 0; i < gOdd.size && i < oO.size; i++)
+                out.s[q][s][oO.offset + i * 2] = g.s[q][s][gOdd.offset + i * gOdd.stride];
+        }
+}
+
+// dReLU (FPC.inl:930-990)
+template <typename T, typename U> void fpc_drelu(const FPCV<T>& in, Strided w, FPCV<U>& result, Comm& comm) {
+    const int W = sizeof(T) * 8;
+    size_t n = w.size;
+    FPCV<U> rbits(n * W);
+    fpc_fill<U>(rbits, 1);
+    std::vector<T> a[4];
+    fpc_reconstruct(in, w, a, comm);  // r = 0; r += input; reconstruct(r, a)
+    std::vector<U> abits[4];
+    FPCV<U> msb(n);
+    for (int p = 0; p < 4; p++) {
+        for (auto& x : a[p]) x = (T)(x + 1);
+        bitexpand<T, U>(a[p], abits[p]);
+        int x0 = fpc_x0_share(p);
+        for (size_t i = 0; i < n; i++) {
+            size_t bi = i * W + (W - 1);
+            for (int k = 0; k < 3; k++) {
+                msb.s[p][k][i] = rbits.s[p][k][bi];                 // getMSBs of every share
+                if (k == x0) msb.s[p][k][i] ^= abits[p][bi];        // msb ^= abits_msb: x0 only
+                rbits.s[p][k][bi] = 0;                              // setMSBs(rbits, 0)
+            }
+            abits[p][bi] = 1;                                       // setMSBs(abits, 1)
+        }
+    }
+    FPCV<U> g(n * W), pp(n * W);
+    for (int p = 0; p < 4; p++) {
+        int x0 = fpc_x0_share(p);
+        for (int k = 0; k < 3; k++)
+            for (size_t i = 0; i < n * W; i++) {
+                g.s[p][k][i] = rbits.s[p][k][i] & abits[p][i];                        // &= DeviceData: all shares
+                pp.s[p][k][i] = rbits.s[p][k][i] ^ (k == x0 ? abits[p][i] : (U)0);  // ^= DeviceData: x0
+            }
+    }
+    FPCV<U> pre(n);
+    fpc_carry_out(pp, g, W, pre, comm);
+    fpc_xor_assign(pre, whole(n), msb, whole(n));
+    result.resize(n);
+    fpc_fill<U>(result, 1);
+    for (int p = 0; p < 4; p++)
+        for (int k = 0; k < 3; k++)
+            for (size_t i = 0; i < n; i++) result.s[p][k][i] = (U)(result.s[p][k][i] - pre.s[p][k][i]);
+}
+
+// selectShare (FPC.inl:672-711) with convex_comb (:1528-1541, functor :31-66):
+// c = 0, so d holds 1 in component x0 where the party's opened e is 1.
+template <typename T, typename U>
+void fpc_select_share(const FPCV<T>& x, Strided wx, const FPCV<T>& y, Strided wy, const FPCV<U>& b, FPCV<T>& z,
+                      Strided wz, Comm& comm) {
+    size_t n = wx.size;
+    std::vector<U> e[4];
+    fpc_reconstruct(b, whole(b.n), e, comm);  // cbits = 0 ^ b
+    FPCV<T> d(n);
+    for (int p = 1; p < 4; p++) {
+        int x0 = fpc_x0_share(p);
+        for (size_t i = 0; i < n; i++) d.s[p][x0][i] = e[p][i] == 1 ? (T)1 : (T)0;
+    }
+    FPCV<T> res(n);
+    for (int p = 0; p < 4; p++)
+        for (int k = 0; k < 3; k++)
+            for (size_t i = 0; i < n; i++)
+                res.s[p][k][i] = (T)(y.s[p][k][wy.offset + i * wy.stride] - x.s[p][k][wx.offset + i * wx.stride]);
+    fpc_mul_assign(res, whole(n), d, whole(n), comm);
+    for (int p = 0; p < 4; p++)
+        for (int k = 0; k < 3; k++)
+            for (size_t i = 0; i < n; i++)
+                z.s[p][k][wz.offset + i * wz.stride] = (T)(res.s[p][k][i] + x.s[p][k][wx.offset + i * wx.stride]);
+}
+
+// ReLU (FPC.inl:992-1003)
+template <typename T, typename U> void fpc_relu(const FPCV<T>& in, FPCV<T>& out, FPCV<U>& dout, Comm& comm) {
+    fpc_drelu<T, U>(in, whole(in.n), dout, comm);
+    FPCV<T> zeros(in.n);
+    out.resize(in.n);
+    fpc_select_share<T, U>(zeros, whole(in.n), in, whole(in.n), dout, out, whole(in.n), comm);
+}
+
+// maxpool (FPC.inl:1005-1177)
+template <typename T, typename U>
+void fpc_maxpool(FPCV<T>& input, FPCV<T>& result, FPCV<U>& dresult, int k, Comm& comm) {
+    size_t N = input.n;
+    dresult.resize(N);
+    fpc_fill<U>(dresult, 1);
+    size_t stride = 2;
+    Strided even = strided(N, 0, stride), odd = strided(N, 1, stride);
+    auto level = [&](bool last) {
+        FPCV<T> diff(even.size);
+        for (int p = 0; p < 4; p++)
+            for (int s = 0; s < 3; s++)
+                for (size_t i = 0; i < even.size; i++)
+                    diff.s[p][s][i] = (T)(input.s[p][s][even.offset + i * even.stride] -
+                                          input.s[p][s][odd.offset + i * odd.stride]);
+        FPCV<U> b(even.size);
+        fpc_drelu<T, U>(diff, whole(diff.n), b, comm);
+        fpc_select_share<T, U>(input, odd, input, even, b, input, even, comm);
+        if (!last) {
+            stride *= 2;
+            even = strided(N, 0, stride);
+            odd = strided(N, stride / 2, stride);
+        } else {
+            result.resize(even.size);
+            for (int p = 0; p < 4; p++)
+                for (int s = 0; s < 3; s++)
+                    for (size_t i = 0; i < even.size; i++) result.s[p][s][i] = input.s[p][s][even.offset + i * even.stride];
+        }
+        FPCV<U> neg(b.n);
+        fpc_fill<U>(neg, 1);
+        for (int p = 0; p < 4; p++)
+            for (int s = 0; s < 3; s++)
+                for (size_t i = 0; i < b.n; i++) neg.s[p][s][i] = (U)(neg.s[p][s][i] - b.s[p][s][i]);
+        FPCV<U> expanded(N);
+        for (int p = 0; p < 4; p++)
+            for (int s = 0; s < 3; s++) expand_compare<U>(b.s[p][s], neg.s[p][s], expanded.s[p][s]);
+        fpc_and_assign(dresult, whole(N), expanded, whole(N), comm);
+    };
+    while (k > 2) {
+        level(false);
+        k /= 2;
+    }
+    level(true);
+}
+
 }  // namespace oracle

@@ -42,6 +42,8 @@ class PiranhaError(RuntimeError):
 _P6 = ctypes.c_void_p * 6
 _P3 = ctypes.c_void_p * 3
 _P2 = ctypes.c_void_p * 2
+_P4 = ctypes.c_void_p * 4
+_P12 = ctypes.c_void_p * 12
 
 
 def _declare(lib):
@@ -118,6 +120,25 @@ def _declare(lib):
         "pg_tpc_relu_u32_u8": [vp, _P2, sz, _P2, _P2],
         "pg_tpc_select_share_u64_u8": [vp, _P2, _P2, _P2, _P2, sz],
         "pg_tpc_maxpool_u64_u8": [vp, _P2, sz, i, _P2, _P2],
+        "pg_fpc_matmul_u64": [vp, _P12, _P12, _P12, i, i, i, i, i, i, i],
+        "pg_fpc_matmul_u32": [vp, _P12, _P12, _P12, i, i, i, i, i, i, i],
+        "pg_fpc_fc_forward_u64": [vp, _P12, _P12, vp, _P12, i, i, i, i],
+        "pg_fpc_fc_forward_u32": [vp, _P12, _P12, vp, _P12, i, i, i, i],
+        "pg_fpc_conv_u64": [vp, _P12, _P12, _P12, i, i, i, i, i, i, i, i, i, i],
+        "pg_fpc_divide_public_u64": [vp, _P12, sz, u64],
+        "pg_fpc_divide_public_vec_u64": [vp, _P12, sz, vp],
+        "pg_fpc_divide_public_u32": [vp, _P12, sz, u32],
+        "pg_fpc_reconstruct_u64": [vp, _P12, sz, _P4],
+        "pg_fpc_reconstruct_u32": [vp, _P12, sz, _P4],
+        "pg_fpc_reconstruct_u8": [vp, _P12, sz, _P4],
+        "pg_fpc_mul_u64": [vp, _P12, _P12, sz],
+        "pg_fpc_and_u8": [vp, _P12, _P12, sz],
+        "pg_fpc_drelu_u64_u8": [vp, _P12, sz, _P12],
+        "pg_fpc_drelu_u32_u8": [vp, _P12, sz, _P12],
+        "pg_fpc_relu_u64_u8": [vp, _P12, sz, _P12, _P12],
+        "pg_fpc_relu_u32_u8": [vp, _P12, sz, _P12, _P12],
+        "pg_fpc_select_share_u64_u8": [vp, _P12, _P12, _P12, _P12, sz],
+        "pg_fpc_maxpool_u64_u8": [vp, _P12, sz, i, _P12, _P12],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -189,10 +210,10 @@ class Context:
     def sync(self):
         self._check(lib().pg_sync(self._h))
 
-    def comm(self):
+    def comm(self, parties=3):
         buf = (ctypes.c_uint64 * 9)()
         self._check(lib().pg_comm_get(self._h, buf))
-        return {"tx": list(buf[0:3]), "rx": list(buf[4:7]), "rounds": buf[8]}
+        return {"tx": list(buf[0:parties]), "rx": list(buf[4:4 + parties]), "rounds": buf[8]}
 
     def reset_comm(self):
         self._check(lib().pg_comm_reset(self._h))
@@ -480,6 +501,123 @@ class tpc:
         """maxpool (TPC.inl:887-1058) over rows of k values."""
         ctx._check(lib().pg_tpc_maxpool_u64_u8(ctx.handle, tpc._p2(input), input.shape[1], int(k), tpc._p2(result),
                                                tpc._p2(dresult)))
+        return result, dresult
+
+
+class fpc:
+    """The 4-party protocol (src/mpc/FPC.h): an FPC tensor of n elements is a
+    CUDA tensor of shape (4, 3, n), [party A..D][shareA/shareB/shareC], party
+    p's share k holding component x_{(p+1+k) mod 4} of x = x0 + x1 + x2 + x3.
+    Names and argument meanings follow FPC.h's free functions."""
+
+    @staticmethod
+    def empty(n: int, ring: str = "u64", device="cuda"):
+        torch = _torch()
+        return torch.empty((4, 3, n), dtype=getattr(torch, _TDT[ring]), device=device)
+
+    @staticmethod
+    def zeros(n: int, ring: str = "u64", device="cuda"):
+        torch = _torch()
+        return torch.zeros((4, 3, n), dtype=getattr(torch, _TDT[ring]), device=device)
+
+    @staticmethod
+    def _p12(t):
+        if t.dim() != 3 or tuple(t.shape[:2]) != (4, 3) or not t.is_cuda:
+            raise PiranhaError("expected a CUDA FPC tensor of shape (4, 3, n)")
+        if not t.is_contiguous():
+            raise PiranhaError("FPC tensor must be contiguous")
+        return _P12(*[t[p, k].data_ptr() for p in range(4) for k in range(3)])
+
+    @staticmethod
+    def _p4(t):
+        if t.dim() != 2 or t.shape[0] != 4 or not t.is_cuda or not t.is_contiguous():
+            raise PiranhaError("expected a contiguous CUDA tensor of shape (4, n)")
+        return _P4(*[t[p].data_ptr() for p in range(4)])
+
+    @staticmethod
+    def matmul(ctx: Context, a, b, c, M, N, K, transpose_a, transpose_b, transpose_c, truncation):
+        """matmul (FPC.inl:636-670)."""
+        fn = lib().pg_fpc_matmul_u64 if _ring(a) == "u64" else lib().pg_fpc_matmul_u32
+        ctx._check(fn(ctx.handle, fpc._p12(a), fpc._p12(b), fpc._p12(c), M, N, K, int(transpose_a),
+                      int(transpose_b), int(transpose_c), int(truncation)))
+        return c
+
+    @staticmethod
+    def fc_forward(ctx: Context, x, w, bias, out, batch, din, dout, fp=FLOAT_PRECISION):
+        """FCLayer::forward (FCLayer.cu:78-130) for FPC: matmul + bias shares."""
+        fn = lib().pg_fpc_fc_forward_u64 if _ring(x) == "u64" else lib().pg_fpc_fc_forward_u32
+        bp = ctypes.cast(fpc._p12(bias), ctypes.c_void_p) if bias is not None else None
+        ctx._check(fn(ctx.handle, fpc._p12(x), fpc._p12(w), bp, fpc._p12(out), batch, din, dout, fp))
+        return out
+
+    @staticmethod
+    def convolution(ctx: Context, A, B, C, op, batchSize, imageHeight, imageWidth, filterSize, Din, Dout, stride,
+                    padding, truncation):
+        """convolution (FPC.inl:862-925)."""
+        ctx._check(lib().pg_fpc_conv_u64(ctx.handle, fpc._p12(A), fpc._p12(B), fpc._p12(C), int(op), batchSize,
+                                         imageHeight, imageWidth, filterSize, Din, Dout, stride, padding,
+                                         int(truncation)))
+        return C
+
+    @staticmethod
+    def dividePublic(ctx: Context, a, denominator):
+        """dividePublic (FPC.inl:576-608); the denominator is a scalar or a CUDA tensor."""
+        torch = _torch()
+        n = a.shape[2]
+        if isinstance(denominator, torch.Tensor):
+            ctx._check(lib().pg_fpc_divide_public_vec_u64(ctx.handle, fpc._p12(a), n,
+                                                          ctypes.c_void_p(denominator.data_ptr())))
+        elif _ring(a) == "u64":
+            ctx._check(lib().pg_fpc_divide_public_u64(ctx.handle, fpc._p12(a), n, int(denominator)))
+        else:
+            ctx._check(lib().pg_fpc_divide_public_u32(ctx.handle, fpc._p12(a), n, int(denominator)))
+        return a
+
+    @staticmethod
+    def reconstruct(ctx: Context, a, out):
+        """reconstruct (FPC.inl:611-634): out has shape (4, n), one row per party."""
+        fn = getattr(lib(), f"pg_fpc_reconstruct_{_ring(a)}")
+        ctx._check(fn(ctx.handle, fpc._p12(a), a.shape[2], fpc._p4(out)))
+        return out
+
+    @staticmethod
+    def mul_(ctx: Context, a, b):
+        """FPC *= FPC (FPC.inl:322-364), in place on a."""
+        ctx._check(lib().pg_fpc_mul_u64(ctx.handle, fpc._p12(a), fpc._p12(b), a.shape[2]))
+        return a
+
+    @staticmethod
+    def and_(ctx: Context, a, b):
+        """FPC &= FPC on uint8 bit shares (FPC.inl:375-399), in place on a."""
+        ctx._check(lib().pg_fpc_and_u8(ctx.handle, fpc._p12(a), fpc._p12(b), a.shape[2]))
+        return a
+
+    @staticmethod
+    def dReLU(ctx: Context, input, result):
+        """dReLU (FPC.inl:930-990): uint8 bit shares."""
+        fn = lib().pg_fpc_drelu_u64_u8 if _ring(input) == "u64" else lib().pg_fpc_drelu_u32_u8
+        ctx._check(fn(ctx.handle, fpc._p12(input), input.shape[2], fpc._p12(result)))
+        return result
+
+    @staticmethod
+    def ReLU(ctx: Context, input, result, dresult):
+        """ReLU (FPC.inl:992-1003)."""
+        fn = lib().pg_fpc_relu_u64_u8 if _ring(input) == "u64" else lib().pg_fpc_relu_u32_u8
+        ctx._check(fn(ctx.handle, fpc._p12(input), input.shape[2], fpc._p12(result), fpc._p12(dresult)))
+        return result, dresult
+
+    @staticmethod
+    def selectShare(ctx: Context, x, y, b, z):
+        """selectShare (FPC.inl:672-711): z = b ? y : x."""
+        ctx._check(lib().pg_fpc_select_share_u64_u8(ctx.handle, fpc._p12(x), fpc._p12(y), fpc._p12(b),
+                                                    fpc._p12(z), x.shape[2]))
+        return z
+
+    @staticmethod
+    def maxpool(ctx: Context, input, result, dresult, k):
+        """maxpool (FPC.inl:1005-1177) over rows of k values (k a power of two)."""
+        ctx._check(lib().pg_fpc_maxpool_u64_u8(ctx.handle, fpc._p12(input), input.shape[2], int(k),
+                                               fpc._p12(result), fpc._p12(dresult)))
         return result, dresult
 
 

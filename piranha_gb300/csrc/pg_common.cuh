@@ -87,6 +87,15 @@ template <typename T> inline bool load6(Sh6<T> &o, T *const *a) {
     return true;
 }
 
+// Operand segments of one fused ring GEMM: sum over i of A_i (B0_i + B1_i),
+// B1_i optional; every segment has the same shape and layout.
+template <typename T> struct SegList {
+    int nseg = 0;
+    const T *a[12];
+    const T *b0[12];
+    const T *b1[12];
+};
+
 // party helpers (RSS.inl:348-369)
 __host__ __device__ constexpr int next_party(int p) { return p == 2 ? 0 : p + 1; }
 __host__ __device__ constexpr int prev_party(int p) { return p == 0 ? 2 : p - 1; }

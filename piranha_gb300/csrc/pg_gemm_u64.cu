@@ -15,7 +15,7 @@
 namespace pg {
 
 enum GemmKind { K_GEMM = 0, K_FPROP = 1, K_DGRAD = 2, K_WGRAD = 3 };
-enum Epi { EPI_RAW = 0, EPI_RSS = 1 };
+enum Epi { EPI_RAW = 0, EPI_RSS = 1, EPI_FPC = 2 };
 
 // unsigned 32-bit division by a runtime constant (round-up multiply-high)
 struct FastDiv {
@@ -35,12 +35,14 @@ struct FastDiv {
     }
 };
 
+constexpr int kMaxSeg = 12;
+
 template <typename T> struct GemmArgs {
     int M, N, K;  // K per segment
     int nseg;
-    const T *a[6];
-    const T *b0[6];
-    const T *b1[6];  // added to b0 when not null
+    const T *a[kMaxSeg];
+    const T *b0[kMaxSeg];
+    const T *b1[kMaxSeg];  // added to b0 when not null (the same pointer twice doubles it)
     int tA, tB, tC;
     // conv geometry
     int cn, ch, cw, cc, ck, cr, cs, cp, cq, pad, stride;
@@ -52,6 +54,7 @@ template <typename T> struct GemmArgs {
     const T *bias[6];
     T d;
     int dshift;
+    int x0;  // EPI_FPC: the output share that holds component x0 (-1: none)
 };
 
 constexpr int BM = 128, BN = 64, BK = 16, NT = 256, TM = 8, TN = 4;
@@ -210,6 +213,15 @@ __global__ void __launch_bounds__(NT) ring_gemm_kernel(const GemmArgs<T> g) {
             T z = acc[i][j];
             if (g.epi == EPI_RAW) {
                 g.c_raw[idx] = z;
+            } else if (g.epi == EPI_FPC) {
+                // FPC dividePublic at one party: its reveal minus d, divided, plus r = 1 in x0
+                T v = (T)(1 + div_public<T>((T)(z - g.d), g.d, g.dshift));
+#pragma unroll
+                for (int ps = 0; ps < 3; ps++) {
+                    T base = ps == g.x0 ? v : (T)0;
+                    if (g.bias[ps]) base = (T)(base + g.bias[ps][n]);
+                    g.out[ps][idx] = base;
+                }
             } else {
                 // dividePublic3out3: reveal sum_p z_p - d, divide, r = 1 at A.shareA / C.shareB
                 T v = (T)(1 + div_public<T>((T)(z - g.d), g.d, g.dshift));
@@ -322,6 +334,46 @@ int rss_conv(Ctx *c, const T *const A[6], const T *const B[6], T *const C[6], in
     return PG_OK;
 }
 
+// One simulated FPC party's share-GEMM: the reveal of the party's product
+// shares after the six reshares is a sum of local products a_{u,i} b_{u,j};
+// the caller passes them as segments and the epilogue finishes dividePublic.
+template <typename T>
+int fpc_party_gemm(Ctx *c, const SegList<T> &s, int M, int N, int K, int tA, int tB, int tC, T *const out[3],
+                   const T *const bias[3], int x0, int trunc) {
+    if (s.nseg <= 0 || s.nseg > kMaxSeg) return set_error(c, PG_ERR_INVALID_ARG, "fpc gemm: %d segments", s.nseg);
+    if (M <= 0 || N <= 0 || K <= 0) return set_error(c, PG_ERR_SIZE, "matmul: bad sizes");
+    if (trunc < 0 || trunc > (int)(sizeof(T) * 8 - 2)) return set_error(c, PG_ERR_INVALID_ARG, "bad truncation %d", trunc);
+    GemmArgs<T> g;
+    zero_args(g);
+    g.M = M; g.N = N; g.K = K; g.tA = tA; g.tB = tB; g.tC = tC;
+    g.nseg = s.nseg;
+    for (int i = 0; i < s.nseg; i++) { g.a[i] = s.a[i]; g.b0[i] = s.b0[i]; g.b1[i] = s.b1[i]; }
+    g.epi = EPI_FPC;
+    for (int i = 0; i < 3; i++) { g.out[i] = out[i]; g.bias[i] = bias ? bias[i] : nullptr; }
+    g.x0 = x0;
+    g.d = (T)((T)1 << trunc);
+    g.dshift = pow2_shift<T>(g.d);
+    return launch_gemm(c, g, K_GEMM);
+}
+
+int fpc_party_conv_u64(Ctx *c, const SegList<uint64_t> &s, int op, int batch, int H, int W, int f, int Din,
+                       int Dout, int stride, int pad, uint64_t *const out[3], int x0, int trunc) {
+    if (s.nseg <= 0 || s.nseg > kMaxSeg) return set_error(c, PG_ERR_INVALID_ARG, "fpc conv: %d segments", s.nseg);
+    if (op < 0 || op > 2) return set_error(c, PG_ERR_INVALID_ARG, "bad conv operator %d", op);
+    if (trunc < 0 || trunc > 62) return set_error(c, PG_ERR_INVALID_ARG, "bad truncation %d", trunc);
+    GemmArgs<uint64_t> g;
+    zero_args(g);
+    setup_conv(g, op, batch, H, W, Din, Dout, f, f, pad, stride);
+    g.nseg = s.nseg;
+    for (int i = 0; i < s.nseg; i++) { g.a[i] = s.a[i]; g.b0[i] = s.b0[i]; g.b1[i] = s.b1[i]; }
+    g.epi = EPI_FPC;
+    for (int i = 0; i < 3; i++) g.out[i] = out[i];
+    g.x0 = x0;
+    g.d = 1ull << trunc;
+    g.dshift = trunc;
+    return launch_gemm(c, g, op == PG_CONV_FPROP ? K_FPROP : op == PG_CONV_DGRAD ? K_DGRAD : K_WGRAD);
+}
+
 template <typename T>
 int plain_gemm(Ctx *c, int M, int N, int K, const T *A, int tA, const T *B, int tB, T *C, int tC) {
     if (!A || !B || !C) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
@@ -354,6 +406,10 @@ template int rss_matmul<uint32_t>(Ctx *, const uint32_t *const *, const uint32_t
                                   const uint32_t *const *, int, int, int, int, int, int, int);
 template int rss_conv<uint64_t>(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *, int, int,
                                 int, int, int, int, int, int, int, int);
+template int fpc_party_gemm<uint64_t>(Ctx *, const SegList<uint64_t> &, int, int, int, int, int, int,
+                                      uint64_t *const *, const uint64_t *const *, int, int);
+template int fpc_party_gemm<uint32_t>(Ctx *, const SegList<uint32_t> &, int, int, int, int, int, int,
+                                      uint32_t *const *, const uint32_t *const *, int, int);
 template int plain_gemm<uint64_t>(Ctx *, int, int, int, const uint64_t *, int, const uint64_t *, int, uint64_t *, int);
 template int plain_gemm<uint32_t>(Ctx *, int, int, int, const uint32_t *, int, const uint32_t *, int, uint32_t *, int);
 

@@ -316,6 +316,129 @@ def test_tpc_func_convolution(golden):
     assert_reveal_tpc(out, a["expected"])
 
 
+# ---------------------------------------------- Func.cu cases, FPC (4PC)
+# The same typed Func vectors pin the 4-party restatement; every party's
+# reveal (own three shares plus the previous party's shareA) must match.
+
+def fenc(vals, fixed=True):
+    return orc.fpc_from_list(vals, U64, FP, to_fixed=fixed)
+
+
+def assert_reveal_fpc(shares, expected, fixed=True):
+    rec = orc.fpc_reconstruct(shares)
+    for p in range(4):
+        got = orc.decode(rec[p], FP) if fixed else s64(rec[p].astype(U64)).astype(np.float64)
+        assert np.max(np.abs(got - np.asarray(expected, dtype=np.float64))) <= EPS, (p, got, expected)
+
+
+def test_fpc_func_reconstruct(golden):
+    c = golden[0]["Reconstruct"]["arrays"]
+    comm = orc.Comm(4)
+    rec = orc.fpc_reconstruct(fenc(c["a"]), comm)
+    for p in range(4):
+        assert np.max(np.abs(orc.decode(rec[p], FP) - np.asarray(c["expected"]))) <= EPS
+    n = len(c["a"])
+    assert comm.rounds == 1 and comm.tx == [n * 8] * 4 and comm.rx == [n * 8] * 4
+
+
+@pytest.mark.parametrize("name", ["MatMul", "MatMul2"])
+def test_fpc_func_matmul(golden, name):
+    c = golden[0][name]
+    p, a = c["params"], c["arrays"]
+    comm = orc.Comm(4)
+    out = orc.fpc_matmul(fenc(a["a"]), fenc(a["b"]), p["M"], p["N"], p["K"], p["tA"], p["tB"], p["tC"], FP, comm)
+    assert_reveal_fpc(out, a["expected"])
+    # six reshares (sender I -> receiver G, M x N each), then the truncation's reveal
+    mn = p["M"] * p["N"]
+    assert comm.rounds == 7
+    assert comm.tx == [3 * mn * 8 + mn * 8, 2 * mn * 8 + mn * 8, mn * 8 + mn * 8, mn * 8]
+    assert comm.rx == [mn * 8 + mn * 8, 2 * mn * 8 + mn * 8, 2 * mn * 8 + mn * 8, mn * 8 + mn * 8]
+
+
+def test_fpc_func_mult(golden):
+    a = golden[0]["Mult"]["arrays"]
+    assert_reveal_fpc(orc.fpc_mul(fenc(a["b"], False), fenc(a["a"], False)), a["expected"], fixed=False)
+
+
+@pytest.mark.parametrize("name", ["Truncate", "Truncate2"])
+def test_fpc_func_truncate(golden, name):
+    c = golden[0][name]
+    assert_reveal_fpc(orc.fpc_divide_public(fenc(c["arrays"]["a"]), c["params"]["d"]), c["arrays"]["expected"])
+
+
+def test_fpc_func_truncate_vec(golden):
+    a = golden[0]["TruncateVec"]["arrays"]
+    d = np.array([1 << int(x) for x in a["pows"]], dtype=U64)
+    assert_reveal_fpc(orc.fpc_divide_public(fenc(a["a"]), d), a["expected"])
+
+
+def test_fpc_func_select_share(golden):
+    a = golden[0]["SelectShare"]["arrays"]
+    z = orc.fpc_select_share(fenc(a["x"]), fenc(a["y"]), fenc(a["b"], False))
+    assert_reveal_fpc(z, a["expected"])
+
+
+@pytest.mark.parametrize("name", ["DRELU", "DRELU2"])
+def test_fpc_func_drelu(golden, name):
+    a = golden[0][name]["arrays"]
+    comm = orc.Comm(4)
+    res = orc.fpc_drelu(fenc(a["input"]), udtype=U64, comm=comm)
+    assert_reveal_fpc(res, a["expected"], fixed=False)
+    assert comm.rounds == 73  # 1 reveal + 6 carry levels x 2 ANDs x 6 reshares
+
+
+def test_fpc_func_drelu3(golden):
+    a = golden[0]["DRELU3"]["arrays"]
+    x = fenc(a["input"])
+    x = (x + u64(a["add"])[None, None, :]).astype(U64)  # every share of every party += add
+    assert_reveal_fpc(orc.fpc_drelu(x, udtype=U64), a["expected"], fixed=False)
+
+
+def test_fpc_func_relu(golden):
+    a = golden[0]["RELU"]["arrays"]
+    out, dout = orc.fpc_relu(fenc(a["input"]), udtype=U64)
+    assert_reveal_fpc(out, a["expected"])
+    assert_reveal_fpc(dout, a["dexpected"], fixed=False)
+
+
+def test_fpc_func_maxpool(golden):
+    a = golden[0]["Maxpool"]["arrays"]
+    out, dout = orc.fpc_maxpool(fenc(a["input"]), 4, udtype=U64)
+    assert_reveal_fpc(out, a["expected"])
+    assert_reveal_fpc(dout, a["dexpected"], fixed=False)
+
+
+def test_fpc_func_convolution(golden):
+    c = golden[0]["Convolution"]
+    p, a = c["params"], c["arrays"]
+    out = orc.fpc_convolution(fenc(a["im"]), fenc(a["filters"]), orc.FPROP, p["batch"], p["H"], p["W"], p["f"],
+                              p["Din"], p["Dout"], p["stride"], p["pad"], FP)
+    assert_reveal_fpc(out, a["expected"])
+
+
+def test_fpc_random_sharing_product_is_not_the_product():
+    """A quirk the restatement keeps: reshareFPC's PRG masks are zero and party
+    J adds its own cross term where I and G add I's (FPC.inl:1184-1259), so a
+    product of two fully random 4-party sharings does not reveal x*y, while
+    the same values loaded through setPublic (x0 only) do."""
+    M, N, K = 4, 3, 5
+    rng = np.random.default_rng(3)
+    xv, wv = rng.normal(0, 1, M * K), rng.normal(0, 1, K * N)
+    ref = orc.decode(orc.gemm(M, N, K, orc.encode(xv), 1, orc.encode(wv), 1, 1), 2 * FP)
+    pub = orc.fpc_reconstruct(orc.fpc_matmul(fenc(xv), fenc(wv), M, N, K, 1, 1, 1, FP))
+    assert all(np.max(np.abs(orc.decode(pub[p], FP) - ref)) < EPS for p in range(4))
+    a, b = orc.fpc_share_random(orc.encode(xv), seed=4), orc.fpc_share_random(orc.encode(wv), seed=5)
+    rnd = orc.fpc_reconstruct(orc.fpc_matmul(a, b, M, N, K, 1, 1, 1, FP))
+    assert any(np.max(np.abs(orc.decode(rnd[p], FP) - ref)) > 1.0 for p in range(4))
+
+
+def test_fpc_share_random_reconstructs():
+    rng = np.random.default_rng(5)
+    v = rng.integers(0, 1 << 63, 100, dtype=U64)
+    rec = orc.fpc_reconstruct(orc.fpc_share_random(v, seed=6))
+    assert all(np.array_equal(rec[p], v) for p in range(4))
+
+
 # ----------------------------------------------------------- Layer.cu cases
 
 def test_layer_relu_basic(golden):
