@@ -396,6 +396,85 @@ def div_public_values(x, d, dtype=np.uint64):
     return out
 
 
+# ------------------------------------------------------- training step (RSS)
+
+def vector_expand(a, f):
+    """vectorExpand (matrix.cuh:129-139)."""
+    a = np.ascontiguousarray(a, dtype=np.uint64)
+    b = np.empty(a.size * f, dtype=np.uint64)
+    lib().or_vector_expand_u64(_p(a), ctypes.c_size_t(a.size), _p(b), ctypes.c_size_t(f))
+    return b
+
+
+def maxpool_row2im(rows, out, image_height, image_width, f, Din, batch, stride):
+    """maxpool_row2im (convolution.cuh:111-152): adds into a copy of out."""
+    rows = np.ascontiguousarray(rows, dtype=np.uint64)
+    out = np.ascontiguousarray(out, dtype=np.uint64).copy()
+    lib().or_maxpool_row2im_u64(_p(rows), _p(out), image_height, image_width, f, Din, batch, stride)
+    return out
+
+
+def relu_layer_backward(delta, relu_prime, comm=None):
+    """ReLULayer::backward (ReLULayer.cu:90-124)."""
+    delta = _views(delta, np.uint64)
+    n = delta.shape[2]
+    b = np.ascontiguousarray(relu_prime, dtype=np.uint8)
+    out = np.empty((3, 2, n), dtype=np.uint64)
+    comm = comm or Comm()
+    lib().or_relu_layer_backward_u64_u8(_p(delta), ctypes.c_size_t(n), _p(b), _p(out), comm.ptr())
+    return out
+
+
+def maxpool_layer_backward(delta, max_prime, H, W, C, pool, stride, batch, comm=None):
+    """MaxpoolLayer::backward (MaxpoolLayer.cu:133-185)."""
+    delta = _views(delta, np.uint64)
+    n = delta.shape[2]
+    mp = np.ascontiguousarray(max_prime, dtype=np.uint8)
+    if mp.shape != (3, 2, n * pool * pool):
+        raise ValueError("maxPrime must have shape (3, 2, n * pool^2)")
+    out = np.empty((3, 2, batch * H * W * C), dtype=np.uint64)
+    comm = comm or Comm()
+    lib().or_maxpool_layer_backward_u64_u8(_p(delta), ctypes.c_size_t(n), _p(mp), _p(out), H, W, C, pool, stride,
+                                           batch, comm.ptr())
+    return out
+
+
+def fc_layer_backward(delta, fwd_in, w, b, batch, din, dout, fp, lr, comm=None):
+    """FCLayer::backward (FCLayer.cu:132-217): returns (deltas, new w, new b)."""
+    delta = _views(delta, np.uint64, batch * dout)
+    fwd_in = _views(fwd_in, np.uint64, batch * din)
+    w = _views(w, np.uint64, din * dout).copy()
+    b = _views(b, np.uint64, dout).copy()
+    out = np.empty((3, 2, batch * din), dtype=np.uint64)
+    comm = comm or Comm()
+    lib().or_fc_layer_backward_u64(_p(delta), _p(fwd_in), _p(w), _p(b), _p(out), batch, din, dout, fp, lr,
+                                   comm.ptr())
+    return out, w, b
+
+
+def cnn_layer_backward(delta, fwd_in, w, batch, H, W, Din, Dout, f, stride, pad, fp, lr, comm=None):
+    """CNNLayer::backward (CNNLayer.cu:114-193): returns (deltas, new w)."""
+    delta = _views(delta, np.uint64)
+    fwd_in = _views(fwd_in, np.uint64, batch * H * W * Din)
+    w = _views(w, np.uint64, Dout * f * f * Din).copy()
+    out = np.empty((3, 2, batch * H * W * Din), dtype=np.uint64)
+    comm = comm or Comm()
+    lib().or_cnn_layer_backward_u64(_p(delta), _p(fwd_in), _p(w), _p(out), batch, H, W, Din, Dout, f, stride, pad,
+                                    fp, lr, comm.ptr())
+    return out, w
+
+
+def reveal_softmax_grad(act, labels, batch, fp=FP_DEFAULT, comm=None):
+    """NeuralNetwork::_reveal_softmax_grad (NeuralNetwork.cu:207-267)."""
+    act = _views(act, np.uint64)
+    n = act.shape[2]
+    labels = _views(labels, np.uint64, n)
+    out = np.empty((3, 2, n), dtype=np.uint64)
+    comm = comm or Comm()
+    lib().or_reveal_softmax_grad_u64(_p(act), _p(labels), ctypes.c_size_t(n), batch, fp, _p(out), comm.ptr())
+    return out
+
+
 # ------------------------------------------------------------------- TPC
 # A TPC tensor of n elements is a numpy array of shape (2, n): [party A/B][element]
 # (src/mpc/TPC.h: one additive share per party).

@@ -228,6 +228,77 @@ extern "C" void or_truncate_cols_u8(const uint8_t* a, uint8_t* b, size_t rows, i
     truncate_cols<uint8_t>(a, b, rows, start_cols, end_cols);
 }
 
+// ------------------------------------------------------- training step (RSS)
+
+extern "C" void or_vector_expand_u64(const uint64_t* a, size_t n, uint64_t* b, size_t f) {
+    vector_expand<uint64_t>(a, n, b, f);
+}
+extern "C" void or_maxpool_row2im_u64(const uint64_t* rows, uint64_t* out, int imageHeight, int imageWidth, int f,
+                                      int Din, int batch, int stride) {
+    maxpool_row2im<uint64_t>(rows, out, imageHeight, imageWidth, f, Din, batch, stride);
+}
+extern "C" int or_relu_layer_backward_u64_u8(const uint64_t* delta, size_t n, const uint8_t* relu_prime,
+                                             uint64_t* deltas, uint64_t* comm) {
+    RSSV<uint64_t> D, O;
+    RSSV<uint8_t> B;
+    load(D, delta, n);
+    load(B, relu_prime, n);
+    CommIO io(comm);
+    relu_layer_backward<uint64_t, uint8_t>(D, B, O, io.c);
+    store(O, deltas);
+    return 0;
+}
+extern "C" int or_maxpool_layer_backward_u64_u8(const uint64_t* delta, size_t n, const uint8_t* max_prime,
+                                                uint64_t* deltas, int H, int W, int C, int pool, int stride, int batch,
+                                                uint64_t* comm) {
+    RSSV<uint64_t> D, O;
+    RSSV<uint8_t> B;
+    load(D, delta, n);
+    load(B, max_prime, n * (size_t)pool * pool);
+    CommIO io(comm);
+    maxpool_layer_backward<uint64_t, uint8_t>(D, B, O, H, W, C, pool, stride, batch, io.c);
+    store(O, deltas);
+    return 0;
+}
+extern "C" int or_fc_layer_backward_u64(const uint64_t* delta, const uint64_t* fwd_in, uint64_t* w, uint64_t* b,
+                                        uint64_t* deltas, int batch, int din, int dout, int fp, int lr, uint64_t* comm) {
+    RSSV<uint64_t> D, X, Wt, Bs, O;
+    load(D, delta, (size_t)batch * dout);
+    load(X, fwd_in, (size_t)batch * din);
+    load(Wt, w, (size_t)din * dout);
+    load(Bs, b, (size_t)dout);
+    CommIO io(comm);
+    fc_layer_backward<uint64_t>(D, X, Wt, Bs, O, batch, din, dout, fp, lr, io.c);
+    store(Wt, w);
+    store(Bs, b);
+    store(O, deltas);
+    return 0;
+}
+extern "C" int or_cnn_layer_backward_u64(const uint64_t* delta, const uint64_t* fwd_in, uint64_t* w, uint64_t* deltas,
+                                         int batch, int H, int W, int Din, int Dout, int f, int stride, int pad, int fp,
+                                         int lr, uint64_t* comm) {
+    const int P = (H + 2 * pad - f) / stride + 1, Q = (W + 2 * pad - f) / stride + 1;
+    RSSV<uint64_t> D, X, Wt, O;
+    load(D, delta, (size_t)batch * P * Q * Dout);
+    load(X, fwd_in, (size_t)batch * H * W * Din);
+    load(Wt, w, (size_t)Dout * f * f * Din);
+    CommIO io(comm);
+    cnn_layer_backward<uint64_t>(D, X, Wt, O, batch, H, W, Din, Dout, f, stride, pad, fp, lr, io.c);
+    store(Wt, w);
+    store(O, deltas);
+    return 0;
+}
+extern "C" int or_reveal_softmax_grad_u64(const uint64_t* act, const uint64_t* labels, size_t n, int batch, int fp,
+                                          uint64_t* deltas, uint64_t* comm) {
+    RSSV<uint64_t> A, L, O;
+    load(A, act, n);
+    load(L, labels, n);
+    CommIO io(comm);
+    rss_reveal_softmax_grad<uint64_t>(A, L, batch, fp, O, io.c);
+    store(O, deltas);
+    return 0;
+}
+
 // ------------------------------------------------------------------- TPC
 // A TPC tensor crosses as one flat array [party(2)][n].
 

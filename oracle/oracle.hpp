@@ -683,6 +683,143 @@ void maxpool_layer_forward(const RSSV<T>& in, RSSV<T>& act, RSSV<U>& maxPrime, i
 }
 
 
+// ---------------------------------------------------------- training step
+
+// vectorExpand (matrix.cuh:129-139): b[i * f + j] = a[i]
+template <typename T> void vector_expand(const T* a, size_t n, T* b, size_t f) {
+    for (size_t i = 0; i < n; i++)
+        for (size_t j = 0; j < f; j++) b[i * f + j] = a[i];
+}
+
+// maxpool_row2im (convolution.cuh:111-152): every window value is added
+// (atomicAdd) into its image position, with the (batch, x, y, channel)
+// indexing of maxpool_im2row.
+template <typename T>
+void maxpool_row2im(const T* rows, T* out, int imageHeight, int imageWidth, int f, int Din, int batch, int stride) {
+    const int wk = (imageWidth - f) / stride + 1, hk = (imageHeight - f) / stride + 1;
+    const size_t windows = (size_t)batch * Din * wk * hk;
+    for (size_t cw = 0; cw < windows; cw++)
+        for (int v = 0; v < f * f; v++) {
+            size_t b = cw / ((size_t)wk * hk * Din);
+            size_t rem = cw % ((size_t)wk * hk * Din);
+            int widx = (int)(rem / Din), ch = (int)(rem % Din);
+            int wcol = widx / hk, wrow = widx % hk;
+            int vcol = wcol * stride + v / f, vrow = wrow * stride + v % f;
+            size_t o = b * (size_t)imageHeight * imageWidth * Din + (size_t)vcol * imageHeight * Din + (size_t)vrow * Din + ch;
+            out[o] = (T)(out[o] + rows[cw * f * f + v]);
+        }
+}
+
+// ReLULayer::backward (ReLULayer.cu:90-124): deltas = selectShare(0, delta, reluPrime)
+template <typename T, typename U>
+void relu_layer_backward(const RSSV<T>& delta, const RSSV<U>& reluPrime, RSSV<T>& deltas, Comm& comm) {
+    RSSV<T> zeros(delta.n);
+    deltas.resize(delta.n);
+    rss_select_share<T, U>(zeros, whole(delta.n), delta, whole(delta.n), reluPrime, deltas, whole(delta.n), comm);
+}
+
+// MaxpoolLayer::backward (MaxpoolLayer.cu:133-185): expand the incoming delta
+// over each pool, keep it where maxPrime selects, scatter back with row2im.
+// The reference passes (imageWidth, imageHeight) into row2im's (imageHeight,
+// imageWidth) parameters; the swap is kept (it only matters for non-square
+// images).
+template <typename T, typename U>
+void maxpool_layer_backward(const RSSV<T>& delta, const RSSV<U>& maxPrime, RSSV<T>& deltas, int H, int W, int C,
+                            int pool, int stride, int batch, Comm& comm) {
+    const size_t f2 = (size_t)pool * pool;
+    RSSV<T> pools(maxPrime.n), zeros(maxPrime.n);
+    for (int p = 0; p < 3; p++)
+        for (int s = 0; s < 2; s++) vector_expand<T>(delta.v[p][s].data(), delta.n, pools.v[p][s].data(), f2);
+    rss_select_share<T, U>(zeros, whole(pools.n), pools, whole(pools.n), maxPrime, pools, whole(pools.n), comm);
+    deltas.resize((size_t)batch * H * W * C);
+    for (int p = 0; p < 3; p++)
+        for (int s = 0; s < 2; s++) maxpool_row2im<T>(pools.v[p][s].data(), deltas.v[p][s].data(), W, H, pool, C, batch, stride);
+}
+
+template <typename T> static void rss_sub_assign(RSSV<T>& a, const RSSV<T>& b) {
+    for (int p = 0; p < 3; p++)
+        for (int s = 0; s < 2; s++)
+            for (size_t i = 0; i < a.n; i++) a.v[p][s][i] = (T)(a.v[p][s][i] - b.v[p][s][i]);
+}
+
+// FCLayer::backward (FCLayer.cu:132-217): deltas with the weights before the
+// update, dW truncated by FP + lr, db by the reference's reduceSum call
+// (reduceRows = false, rows = outputDim, cols = batchSize) then / 2^lr.
+template <typename T>
+void fc_layer_backward(const RSSV<T>& delta, const RSSV<T>& fwdInput, RSSV<T>& W, RSSV<T>& b, RSSV<T>& deltas,
+                       int batch, int din, int dout, int fp, int lr, Comm& comm) {
+    rss_matmul<T>(delta, W, deltas, batch, din, dout, true, false, true, fp, comm);
+    RSSV<T> dW;
+    rss_matmul<T>(delta, fwdInput, dW, dout, din, batch, false, true, false, fp + lr, comm);
+    rss_sub_assign(W, dW);
+    RSSV<T> db(dout);
+    for (int p = 0; p < 3; p++)
+        for (int s = 0; s < 2; s++) reduce_sum<T>(delta.v[p][s].data(), db.v[p][s].data(), false, dout, batch);
+    T d = (T)((T)1 << lr);
+    rss_divide_public<T>(db, &d, false, comm);
+    rss_sub_assign(b, db);
+}
+
+// CNNLayer::backward (CNNLayer.cu:114-193): dgrad and wgrad convolutions
+// truncated by FP, dF / 2^lr, no bias.
+template <typename T>
+void cnn_layer_backward(const RSSV<T>& delta, const RSSV<T>& fwdInput, RSSV<T>& Wt, RSSV<T>& deltas, int batch, int H,
+                        int W, int Din, int Dout, int f, int stride, int pad, int fp, int lr, Comm& comm) {
+    rss_convolution<T>(delta, Wt, deltas, CONV_DGRAD, batch, H, W, f, Din, Dout, stride, pad, fp, comm);
+    RSSV<T> dF;
+    rss_convolution<T>(delta, fwdInput, dF, CONV_WGRAD, batch, H, W, f, Din, Dout, stride, pad, fp, comm);
+    T d = (T)((T)1 << lr);
+    rss_divide_public<T>(dF, &d, false, comm);
+    rss_sub_assign(Wt, dF);
+}
+
+// to_fixed_functor (util/functors.h:117-123) runs on the device: PTX
+// cvt.rzi.u64.f64 truncates toward zero and saturates, NaN -> 0.
+template <typename T> static inline T to_fixed_device(double x) {
+    if (std::isnan(x) || x <= 0.0) return (T)0;
+    if (x >= std::ldexp(1.0, (int)sizeof(T) * 8)) return std::numeric_limits<T>::max();
+    return (T)x;
+}
+
+// NeuralNetwork::_reveal_softmax_grad (NeuralNetwork.cu:207-267): each party
+// reveals the logits, takes the softmax in double on the host (exp per value,
+// row sums in index order), converts back to fixed point, and the deltas are
+// softmax (added like public data: party A shareA, party C shareB) minus the
+// labels, divided by the batch when LOG_MINI_BATCH = (int)log2(batch) > 1.
+template <typename T>
+void rss_reveal_softmax_grad(const RSSV<T>& act, const RSSV<T>& labels, int batch, int fp, RSSV<T>& deltas,
+                             Comm& comm) {
+    typedef typename std::make_signed<T>::type S;
+    const size_t n = act.n;
+    const size_t classes = n / (size_t)batch;
+    std::vector<T> rev[3];
+    rss_reconstruct(act, whole(n), rev, comm);
+    std::vector<T> sm[3];
+    for (int p = 0; p < 3; p++) {
+        std::vector<double> fa(n), sums(n / classes, 0.0);
+        for (size_t i = 0; i < n; i++) fa[i] = ((double)((S)rev[p][i])) / (double)(1 << fp);
+        for (size_t i = 0; i < n; i++) {
+            fa[i] = std::exp(fa[i]);
+            sums[i / classes] += fa[i];
+        }
+        for (size_t i = 0; i < n; i++) fa[i] /= sums[i / classes];
+        sm[p].resize(n);
+        for (size_t i = 0; i < n; i++) sm[p][i] = to_fixed_device<T>(fa[i] * (double)(1 << fp));
+    }
+    deltas.resize(n);
+    for (size_t i = 0; i < n; i++) {
+        deltas.v[PA][0][i] = sm[PA][i];
+        deltas.v[PC][1][i] = sm[PC][i];
+    }
+    rss_sub_assign(deltas, labels);
+    const int log_mb = (int)std::log2((double)batch);
+    if (log_mb > 1) {
+        T d = (T)((T)1 << log_mb);
+        rss_divide_public<T>(deltas, &d, false, comm);
+    }
+}
+
+
 // ========================================================================
 // TPC: 2-party additive sharing (src/mpc/TPC.h, TPC.inl). Each party holds
 // one share; x = x_A + x_B. Multiplications use the Beaver triples of

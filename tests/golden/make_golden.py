@@ -14,7 +14,9 @@ and writes:
                  parameters of each case are recorded next to them with the
                  line they come from;
 * layers.npz   — the fixture-driven layer tests (FC MNIST, SecureML forward
-                 chain, ReLU MNIST, maxpool MNIST, CNN MNIST) as float64 arrays.
+                 chain, ReLU MNIST, maxpool MNIST, CNN MNIST, the FC /
+                 maxpool / CNN MNIST backward cases, and the SecureML
+                 training step) as float64 arrays.
 
 Nothing under tests/ reads the reference tree at test time; only this
 generator does.
@@ -61,7 +63,7 @@ def _arrays(body: str, env: dict | None = None) -> dict:
     out = {}
     body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)  # block comments
     body = re.sub(r"//[^\n]*", "", body)  # line comments (commented-out variants)
-    pat = re.compile(r"(?:DeviceData<[^>]+>|Share|LAYER_TEST_SHARE<T>|std::vector<double>|RSS<uint8_t>)\s+"
+    pat = re.compile(r"(?:DeviceData<[^>]+>|Share|LAYER_TEST_SHARE<T>|std::vector<double>|RSS<uint8_t>)\s*"
                      r"(\w+)\s*(?:=\s*)?(?:\(\s*)?\{([^}]*)\}", re.S)
     for m in pat.finditer(body):
         name, items = m.group(1), m.group(2)
@@ -132,6 +134,12 @@ def main():
                  ("CNNForwardAllDims", {"H": 3, "W": 3, "Din": 2, "Dout": 2, "f": 3, "stride": 2, "pad": 1, "batch": 2})]:
         add(layer, "src/test/Layer.cu", t, p)
 
+    # Layer.cu backward inline cases
+    add(layer, "src/test/Layer.cu", "ReLUBackwardBasic", {"batch": 1})
+    add(layer, "src/test/Layer.cu", "MaxpoolBackwardBasic", {"H": 2, "W": 2, "C": 2, "pool": 2, "stride": 1, "batch": 2})
+    add(layer, "src/test/Layer.cu", "CNNBackwardBasic",
+        {"H": 3, "W": 3, "Din": 2, "Dout": 3, "f": 3, "stride": 2, "pad": 1, "batch": 2})
+
     with open(os.path.join(HERE, "kat.json"), "w") as f:
         json.dump(kat, f, indent=0, sort_keys=True)
 
@@ -156,6 +164,21 @@ def main():
         "cnn_mnist_weight": load("test_convlayer_weight", 3 * 9 * 2),
         "cnn_mnist_output": load("test_convlayer_output", 128 * 25 * 3),
     }
+    # FCBackwardMNIST (Layer.cu:118-180): 16 -> 10, batch 128, log_learning_rate 6
+    arrays["fc_bw_gradin"] = load("test_fclayer_gradin", 128 * 10)
+    arrays["fc_bw_gradout"] = load("test_fclayer_gradout", 128 * 16)
+    arrays["fc_bw_newweight"] = load("test_fclayer_newweight", 16 * 10)
+    arrays["fc_bw_newbias"] = load("test_fclayer_newbias", 10)
+    arrays["fc_bw_gradweight"] = load("test_fclayer_gradweight", 16 * 10)
+    arrays["fc_bw_gradbias"] = load("test_fclayer_gradbias", 10)
+    # MaxpoolBackwardMNIST (Layer.cu:379-417): 9x9x2, pool 3, stride 2, batch 128
+    arrays["maxpool_bw_gradin"] = load("test_maxpoollayer_gradin", 128 * 2 * 16)
+    arrays["maxpool_bw_gradout"] = load("test_maxpoollayer_gradout", 128 * 2 * 81)
+    # CNNBackwardMNIST (Layer.cu:772-836): 9x9x2 -> 3, f 3, stride 2, pad 1, batch 128
+    arrays["cnn_bw_gradin"] = load("test_convlayer_gradin", 128 * 25 * 3)
+    arrays["cnn_bw_gradout"] = load("test_convlayer_gradout", 128 * 81 * 2)
+    arrays["cnn_bw_newweight"] = load("test_convlayer_newweight", 3 * 9 * 2)
+    arrays["cnn_bw_gradweight"] = load("test_convlayer_gradweight", 3 * 9 * 2)
     # SecureML forward chain (Layer.cu:86-116 and files/test/secureml/*)
     arrays["secureml_input"] = load("secureml/input", 128 * 784)
     for i, (din, dout) in zip((0, 2, 4), ((784, 128), (128, 128), (128, 10))):
@@ -164,6 +187,18 @@ def main():
     for i in range(6):
         n = 128 * (10 if i >= 4 else 128)
         arrays[f"secureml_output{i}"] = load(f"secureml/outputlayer{i}", n)
+    # SecureML training step (files/test/secureml/*): labels, every layer's
+    # incoming gradient, and the updated parameters (a 4096-value slice of the
+    # 784 x 128 layer-0 weights keeps the fixture small)
+    arrays["secureml_labels"] = load("secureml/labels", 128 * 10)
+    for i in range(6):
+        n = 128 * (10 if i >= 4 else 128)
+        arrays[f"secureml_gradin{i}"] = load(f"secureml/gradin_layer{i}", n)
+    arrays["secureml_newweight0_head"] = load("secureml/newweight_layer0", 4096)
+    for i, (din, dout) in zip((2, 4), ((128, 128), (128, 10))):
+        arrays[f"secureml_newweight{i}"] = load(f"secureml/newweight_layer{i}", din * dout)
+    for i, dout in zip((0, 2, 4), (128, 128, 10)):
+        arrays[f"secureml_newbias{i}"] = load(f"secureml/newbias_layer{i}", dout)
     np.savez_compressed(os.path.join(HERE, "layers.npz"), **arrays)
     print("wrote", sorted(kat["cases"]), "and", sorted(arrays))
 

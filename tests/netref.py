@@ -1,4 +1,5 @@
-"""Layer-by-layer oracle composition of NeuralNetwork::forward (NeuralNetwork.cu:109-133).
+"""Layer-by-layer oracle composition of NeuralNetwork::forward and ::backward
+(NeuralNetwork.cu:109-148, :439-460).
 
 Used by the network parity tests and the CPU-baseline leg of bench.py: the
 same layer tuples as piranha_gb300.Network, evaluated with the CPU oracle.
@@ -17,11 +18,13 @@ def fc_forward(x, w, b, batch, din, dout, fp=26):
     return act
 
 
-def forward(layers, params, x, batch, fp=26, comm=None, keep=False):
-    """params[i] = (w, b) views (or None); returns the output (and every layer's output if keep)."""
+def forward(layers, params, x, batch, fp=26, comm=None, keep=False, bits=None):
+    """params[i] = (w, b) views (or None); returns the output (and every layer's output if keep).
+    bits, a list, receives each layer's derivative bits (reluPrime / maxPrime, None for FC / CNN)."""
     outs = []
     for L, prm in zip(layers, params):
         kind = L[0]
+        d = None
         if kind == "fc":
             x = fc_forward(x, prm[0], prm[1], batch, L[1], L[2], fp)
             if comm is not None:
@@ -33,15 +36,57 @@ def forward(layers, params, x, batch, fp=26, comm=None, keep=False):
             H, W, Din, Dout, f, s, pd = L[1:]
             x = orc.convolution(x, prm[0], orc.FPROP, batch, H, W, f, Din, Dout, s, pd, fp, comm)
         elif kind == "relu":
-            x, _ = orc.relu(x, comm=comm)
+            x, d = orc.relu(x, comm=comm)
         elif kind == "maxpool":
             H, W, C, pool, stride = L[1:]
-            x, _ = orc.maxpool_layer(x, H, W, C, pool, stride, batch, fp, comm=comm)
+            x, d = orc.maxpool_layer(x, H, W, C, pool, stride, batch, fp, comm=comm)
         else:
             raise ValueError(kind)
         if keep:
             outs.append(x)
+        if bits is not None:
+            bits.append(d)
     return (x, outs) if keep else x
+
+
+def backward(layers, params, x, outs, bits, labels, batch, fp=26, log_lr=5, comm=None):
+    """NeuralNetwork::backward (NeuralNetwork.cu:136-148, :439-460): the revealed
+    softmax gradient of the last activation, then every layer's backward from
+    the last to the first. Returns (updated params, each layer's deltas)."""
+    params = [None if p is None else (p[0].copy(), None if p[1] is None else p[1].copy()) for p in params]
+    deltas = [None] * len(layers)
+    delta = orc.reveal_softmax_grad(outs[-1], labels, batch, fp, comm)
+    for i in range(len(layers) - 1, -1, -1):
+        L = layers[i]
+        fwd_in = outs[i - 1] if i > 0 else x
+        kind = L[0]
+        if kind == "fc":
+            d, w, b = orc.fc_layer_backward(delta, fwd_in, params[i][0], params[i][1], batch, L[1], L[2], fp, log_lr,
+                                            comm)
+            params[i] = (w, b)
+        elif kind == "cnn":
+            H, W, Din, Dout, f, s, pd = L[1:]
+            d, w = orc.cnn_layer_backward(delta, fwd_in, params[i][0], batch, H, W, Din, Dout, f, s, pd, fp, log_lr,
+                                          comm)
+            params[i] = (w, None)
+        elif kind == "relu":
+            d = orc.relu_layer_backward(delta, bits[i], comm)
+        elif kind == "maxpool":
+            H, W, C, pool, stride = L[1:]
+            d = orc.maxpool_layer_backward(delta, bits[i], H, W, C, pool, stride, batch, comm)
+        else:
+            raise ValueError(kind)
+        deltas[i] = d
+        delta = d
+    return params, deltas
+
+
+def train_step(layers, params, x, labels, batch, fp=26, log_lr=5, comm=None):
+    """One forward + backward + SGD update (main.cu:314-330 for one iteration)."""
+    bits = []
+    out, outs = forward(layers, params, x, batch, fp, comm, keep=True, bits=bits)
+    new_params, deltas = backward(layers, params, x, outs, bits, labels, batch, fp, log_lr, comm)
+    return out, outs, new_params, deltas
 
 
 def vgg16_layers(maxpool=True):

@@ -518,6 +518,99 @@ def test_layer_secureml_chain(golden):
         assert_reveal(o, L[f"secureml_output{i}"], parties=(0,))
 
 
+# ------------------------------------------------ Layer.cu backward cases
+
+def test_layer_relu_backward_basic(golden):
+    a = golden[0]["ReLUBackwardBasic"]["arrays"]
+    _, d = orc.relu(enc_list(a["input"]))
+    assert_reveal(orc.relu_layer_backward(enc_list(a["delta"]), d), a["expected"])
+
+
+def test_layer_maxpool_backward_basic(golden):
+    c = golden[0]["MaxpoolBackwardBasic"]
+    p, a = c["params"], c["arrays"]
+    geo = (p["H"], p["W"], p["C"], p["pool"], p["stride"], p["batch"])
+    _, mp = orc.maxpool_layer(enc_list(a["inputImage"]), *geo)
+    assert_reveal(orc.maxpool_layer_backward(enc_list(a["gradin"]), mp, *geo), a["expected"])
+
+
+def test_layer_cnn_backward_basic(golden):
+    c = golden[0]["CNNBackwardBasic"]
+    p, a = c["params"], c["arrays"]
+    w, x = enc_list(a["weights"]), enc_list(a["input"])
+    act = orc.convolution(x, w, orc.FPROP, p["batch"], p["H"], p["W"], p["f"], p["Din"], p["Dout"], p["stride"],
+                          p["pad"], FP)
+    assert_reveal(act, a["expected_activations"])
+    d, _ = orc.cnn_layer_backward(enc_list(a["gradin"]), x, w, p["batch"], p["H"], p["W"], p["Din"], p["Dout"], p["f"],
+                                  p["stride"], p["pad"], FP, 5)
+    assert_reveal(d, a["gradout"])
+
+
+def test_layer_fc_backward_mnist(golden):
+    """FCBackwardMNIST (Layer.cu:118-180), log_learning_rate 6: the input
+    gradient, the updated weights and the updated biases (the bias gradient
+    goes through the reference's reduceSum(delta, db, false, outputDim,
+    batchSize), restated as is)."""
+    L = golden[1]
+    comm = orc.Comm()
+    d, w, b = orc.fc_layer_backward(orc.set_public(L["fc_bw_gradin"]), orc.set_public(L["fc_mnist_input"]),
+                                    orc.set_public(L["fc_mnist_weight"]), orc.set_public(L["fc_mnist_bias"]),
+                                    128, 16, 10, FP, 6, comm)
+    assert_reveal(d, L["fc_bw_gradout"], parties=(0, 2))
+    assert_reveal(w, L["fc_bw_newweight"], parties=(0, 2))
+    assert_reveal(b, L["fc_bw_newbias"], parties=(0, 2))
+    # delta matmul (128 x 16), dW matmul (10 x 16), db dividePublic (10)
+    assert comm.rounds == 3 and comm.tx == [(2 * 128 * 16 + 2 * 16 * 10 + 10) * 8] * 3
+
+
+def test_layer_maxpool_backward_mnist(golden):
+    L = golden[1]
+    _, mp = orc.maxpool_layer(orc.set_public(L["maxpool_mnist_input"]), 9, 9, 2, 3, 2, 128)
+    d = orc.maxpool_layer_backward(orc.set_public(L["maxpool_bw_gradin"]), mp, 9, 9, 2, 3, 2, 128)
+    assert_reveal(d, L["maxpool_bw_gradout"], parties=(0, 2))
+
+
+@pytest.mark.parametrize("log_lr", [5, 6])
+def test_layer_cnn_backward_mnist(golden, log_lr):
+    """CNNBackwardMNIST (Layer.cu:772-836). The test leaves log_learning_rate
+    at whatever the suite set before it (6 after FCBackwardMNIST, 5 alone);
+    the new weights match within eps for both."""
+    L = golden[1]
+    d, w = orc.cnn_layer_backward(orc.set_public(L["cnn_bw_gradin"]), orc.set_public(L["cnn_mnist_input"]),
+                                  orc.set_public(L["cnn_mnist_weight"]), 128, 9, 9, 2, 3, 3, 2, 1, FP, log_lr)
+    assert_reveal(d, L["cnn_bw_gradout"], parties=(0, 2))
+    assert_reveal(w, L["cnn_bw_newweight"], parties=(0, 2))
+
+
+def test_secureml_training_step(golden):
+    """One SecureML training iteration (files/test/secureml): forward, the
+    revealed softmax gradient (NeuralNetwork.cu:207-267), every layer's
+    backward; each layer's incoming gradient and the updated weights and
+    biases match the fixtures, whose update used learning rate 2^-9."""
+    from tests import netref
+
+    L = golden[1]
+    layers = netref.secureml_layers()
+    params = []
+    for li in (0, 2, 4):
+        params += [(orc.set_public(L[f"secureml_weight{li}"]), orc.set_public(L[f"secureml_bias{li}"])), None]
+    x = orc.set_public(L["secureml_input"])
+    labels = orc.set_public(L["secureml_labels"])
+    _, outs, newp, deltas = netref.train_step(layers, params, x, labels, 128, FP, 9)
+    for i in range(6):
+        assert_reveal(outs[i], L[f"secureml_output{i}"], parties=(0, 2))
+    softmax_delta = orc.reveal_softmax_grad(outs[-1], labels, 128, FP)
+    assert_reveal(softmax_delta, L["secureml_gradin5"], parties=(0, 2))
+    for i in range(5):
+        assert_reveal(deltas[i + 1], L[f"secureml_gradin{i}"], parties=(0, 2))
+    w0 = orc.decode(orc.reconstruct(newp[0][0])[0], FP)[:4096]
+    assert np.max(np.abs(w0 - L["secureml_newweight0_head"])) <= EPS
+    for li in (2, 4):
+        assert_reveal(newp[li][0], L[f"secureml_newweight{li}"], parties=(0, 2))
+    for li in (0, 2, 4):
+        assert_reveal(newp[li][1], L[f"secureml_newbias{li}"], parties=(0, 2))
+
+
 # --------------------------------------------------------- ring semantics
 
 def test_division_semantics():
