@@ -331,6 +331,36 @@ int pg_net_layer_times(pg_net *net, float *ms);
 /* device pointers (owned by the network) of layer i's output shares */
 int pg_net_layer_output(pg_net *net, int layer, uint64_t *const out[6], size_t *n);
 
+/* Training: one SGD iteration (src/main.cu:314-330) = forward, then
+ * NeuralNetwork::backward (NeuralNetwork.cu:136-148): the revealed softmax
+ * gradient (_reveal_softmax_grad :207-267: each party's logits revealed, the
+ * softmax taken in double on the host as the reference does, here as a
+ * stream-ordered host function), then every layer's backward from the last
+ * (FCLayer.cu:132-217, CNNLayer.cu:114-193, ReLULayer.cu:90-124,
+ * MaxpoolLayer.cu:133-185), each updating its weights with learning rate
+ * 2^-log_lr. Labels are RSS shares of the one-hot targets, out_n elements
+ * per share. Training buffers are allocated by the first training call,
+ * which must be eager (not inside a stream capture); needs fp <= 30. */
+int pg_net_train_setup(pg_net *net);
+int pg_net_train_step(pg_net *net, const uint64_t *const in[6], const uint64_t *const labels[6], int log_lr);
+/* backward only, after a forward on the shares in[] (layer 0's weight
+ * gradient needs them) */
+int pg_net_backward(pg_net *net, const uint64_t *const in[6], const uint64_t *const labels[6], int log_lr);
+/* the network's own label buffers ([6][out_n] contiguous) */
+int pg_net_label_shares(pg_net *net, uint64_t *out[6]);
+/* capture forward + backward on the network's own input and label buffers as
+ * one CUDA graph (after one eager step whose parameter updates are undone) */
+int pg_net_capture_train(pg_net *net, int log_lr);
+int pg_net_train_resident(pg_net *net);
+/* host buffers: in_host [6][in_n], labels_host [6][out_n]; out_host receives
+ * the forward's output shares [6][out_n]; replays the captured step if any */
+int pg_net_train_host(pg_net *net, const uint64_t *in_host, const uint64_t *labels_host, uint64_t *out_host,
+                      int log_lr);
+/* layer i's backward output (the gradient it passes on; layer -1 = the
+ * softmax gradient entering the last layer), and its parameter buffers */
+int pg_net_layer_delta(pg_net *net, int layer, uint64_t *out[6], size_t *n);
+int pg_net_layer_params(pg_net *net, int layer, uint64_t *w[6], uint64_t *b[6], size_t *w_n, size_t *b_n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -99,6 +99,15 @@ def _declare(lib):
         "pg_net_input_shares": [vp, _P6],
         "pg_net_layer_output": [vp, i, _P6, ctypes.POINTER(sz)],
         "pg_net_enable_timing": [vp, i],
+        "pg_net_train_setup": [vp],
+        "pg_net_train_step": [vp, _P6, _P6, i],
+        "pg_net_backward": [vp, _P6, _P6, i],
+        "pg_net_label_shares": [vp, _P6],
+        "pg_net_capture_train": [vp, i],
+        "pg_net_train_resident": [vp],
+        "pg_net_train_host": [vp, vp, vp, vp, i],
+        "pg_net_layer_delta": [vp, i, _P6, ctypes.POINTER(sz)],
+        "pg_net_layer_params": [vp, i, _P6, _P6, ctypes.POINTER(sz), ctypes.POINTER(sz)],
         "pg_device_errors": [vp, ctypes.POINTER(i)],
         "pg_tc_selftest": [vp, vp, vp, vp],
         "pg_net_layer_times": [vp, vp],
@@ -680,7 +689,8 @@ class gpu:
 # ------------------------------------------------------------------ network
 
 class Network:
-    """Secure-inference executor (NeuralNetwork::forward, NeuralNetwork.cu:109-133).
+    """Secure-inference and training executor (NeuralNetwork::forward and
+    ::backward, NeuralNetwork.cu:109-148).
 
     ``layers`` is a list of tuples: ("fc", din, dout), ("cnn", H, W, Din, Dout, f, stride, pad),
     ("relu", n_per_image), ("maxpool", H, W, C, pool, stride).
@@ -739,6 +749,46 @@ class Network:
         n = ctypes.c_size_t()
         self.ctx._check(lib().pg_net_layer_output(self._h, layer, arr, ctypes.byref(n)))
         return [int(x) for x in arr], int(n.value)
+
+    # ---------------------------------------------------------- training
+    # One SGD iteration = forward + NeuralNetwork::backward (NeuralNetwork.cu:136-148).
+
+    def train_step(self, x, labels, log_lr: int = 5):
+        """Forward on x, then the backward pass and parameter updates with
+        learning rate 2^-log_lr; labels are (3, 2, out_n) RSS shares."""
+        self.ctx._check(lib().pg_net_train_step(self._h, _p6(x), _p6(labels), int(log_lr)))
+
+    def backward(self, x, labels, log_lr: int = 5):
+        """The backward pass after a forward on x."""
+        self.ctx._check(lib().pg_net_backward(self._h, _p6(x), _p6(labels), int(log_lr)))
+
+    def label_buffers(self):
+        arr = _P6()
+        self.ctx._check(lib().pg_net_label_shares(self._h, arr))
+        return [int(x) for x in arr]
+
+    def capture_train(self, log_lr: int = 5):
+        self.ctx._check(lib().pg_net_capture_train(self._h, int(log_lr)))
+
+    def train_resident(self):
+        self.ctx._check(lib().pg_net_train_resident(self._h))
+
+    def train_host(self, in_host_ptr: int, labels_host_ptr: int, out_host_ptr: int, log_lr: int = 5):
+        self.ctx._check(lib().pg_net_train_host(self._h, ctypes.c_void_p(in_host_ptr), ctypes.c_void_p(labels_host_ptr),
+                                                ctypes.c_void_p(out_host_ptr), int(log_lr)))
+
+    def layer_delta_ptrs(self, layer: int):
+        """Layer i's backward output (layer -1: the softmax gradient)."""
+        arr = _P6()
+        n = ctypes.c_size_t()
+        self.ctx._check(lib().pg_net_layer_delta(self._h, layer, arr, ctypes.byref(n)))
+        return [int(x) for x in arr], int(n.value)
+
+    def layer_param_ptrs(self, layer: int):
+        w, b = _P6(), _P6()
+        wn, bn = ctypes.c_size_t(), ctypes.c_size_t()
+        self.ctx._check(lib().pg_net_layer_params(self._h, layer, w, b, ctypes.byref(wn), ctypes.byref(bn)))
+        return [int(x or 0) for x in w], int(wn.value), [int(x or 0) for x in b], int(bn.value)
 
     def close(self):
         # a network must be destroyed before its context (Context.close does this first)

@@ -1,11 +1,14 @@
-// pg_net.cu — network executor for secure inference: NeuralNetwork::forward
-// (src/nn/NeuralNetwork.cu:109-133) over FC / CNN / ReLU / Maxpool layers
-// (FCLayer.cu:78-130, CNNLayer.cu:81-115, ReLULayer.cu:51-88,
-// MaxpoolLayer.cu:52-131). All share buffers of all layers are allocated once
-// in one device arena at creation; a forward is a fixed sequence of fused
-// launches on the context stream, which pg_net_capture records as one CUDA
-// graph so that a replay costs one launch.
+// pg_net.cu — network executor: NeuralNetwork::forward (src/nn/NeuralNetwork.cu:109-133)
+// and ::backward (:136-148, :207-267, :439-460) over FC / CNN / ReLU / Maxpool
+// layers (FCLayer.cu:78-217, CNNLayer.cu:81-193, ReLULayer.cu:51-124,
+// MaxpoolLayer.cu:52-185). All share buffers of all layers are allocated once
+// in one device arena at creation (the training buffers in a second one, on
+// first use); a forward or a training step is a fixed sequence of fused
+// launches on the context stream, which pg_net_capture / pg_net_capture_train
+// record as one CUDA graph so that a replay costs one launch.
+#include <cmath>
 #include <cstring>
+#include <limits>
 #include <vector>
 
 #include "pg_common.cuh"
@@ -20,6 +23,13 @@ int rss_conv(Ctx *, const T *const *, const T *const *, T *const *, int, int, in
 template <typename T, typename U> int rss_relu(Ctx *, const T *const *, size_t, T *const *, U *const *);
 template <typename T, typename U>
 int rss_maxpool_layer(Ctx *, const T *const *, T *const *, U *const *, int, int, int, int, int, int, int);
+template <typename T, typename U>
+int rss_select(Ctx *, const T *const *, const T *const *, const U *const *, T *const *, size_t);
+template <typename T> int rss_reconstruct(Ctx *, const T *const *, size_t, T *const *);
+template <typename T> int rss_divide_public(Ctx *, T *const *, size_t, T, const T *);
+int reduce_sum_u64(Ctx *, const uint64_t *, uint64_t *, int, int, int);
+int limb3_rss_matmul_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *,
+                         const uint64_t *const *, int, int, int, int, int, int, int);
 }  // namespace pg
 
 using namespace pg;
@@ -30,6 +40,7 @@ struct NetLayer {
     size_t in_n, out_n, w_n, b_n, d_n;  // elements per share buffer (activations include the batch)
     uint64_t *w[6], *b[6], *out[6];
     uint8_t *d[6];
+    uint64_t *delta[6];  // backward: the gradient this layer passes to the previous one (in_n)
     // limb tensor-core form (FC and CNN layers): plan, split-K, packed weights
     lt::Plan plan;
     int split, cps;
@@ -57,6 +68,27 @@ struct pg_net {
     void *limb_arena = nullptr;
     uint8_t *limb_image = nullptr;
     uint64_t *limb_partial = nullptr;
+    // Training (allocated by the first training call, which is eager):
+    struct Train {
+        void *arena = nullptr;
+        uint64_t *labels[6];   // label shares [6][out_n], contiguous
+        uint64_t *sdelta[6];   // the softmax gradient [6][out_n]
+        uint64_t *rev[3];      // each party's reveal of the logits
+        uint64_t *sm[3];       // each party's softmax, fixed point
+        uint64_t *h_rev = nullptr, *h_sm = nullptr;  // pinned host copies [3][out_n]
+        uint64_t *dW[6], *db[6];  // FC / CNN parameter gradients
+        uint64_t *pools[6];       // maxpool: incoming gradient expanded over each window
+        uint64_t *zeros;          // shared zero operand of selectShare
+        uint64_t *backup;         // parameter snapshot around the capture's eager run
+        size_t backup_bytes = 0;
+        // host softmax job (stable address: a graph host node points at it)
+        size_t n = 0;
+        int batch = 0, fp = 0;
+    } tr;
+    cudaGraph_t graph_train = nullptr;
+    cudaGraphExec_t exec_train = nullptr;
+    uint64_t comm_per_train[9] = {0};
+    uint64_t launches_per_train = 0;
 };
 
 // Plans, buffer sizes and weight packing of the limb form.
@@ -170,6 +202,316 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
     return PG_OK;
 }
 
+// ------------------------------------------------------------- training
+
+namespace {
+
+__global__ void softmax_delta_kernel(Sh6<uint64_t> out, const uint64_t *smA, const uint64_t *smC, CSh6<uint64_t> lab,
+                                     size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        // deltas = 0; deltas += softmax (party A shareA, party C shareB); deltas -= labels
+        out.p[0][i] = smA[i] - lab.p[0][i];
+        out.p[1][i] = 0 - lab.p[1][i];
+        out.p[2][i] = 0 - lab.p[2][i];
+        out.p[3][i] = 0 - lab.p[3][i];
+        out.p[4][i] = 0 - lab.p[4][i];
+        out.p[5][i] = smC[i] - lab.p[5][i];
+    }
+}
+
+__global__ void sub6_kernel(Sh6<uint64_t> a, CSh6<uint64_t> b, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+#pragma unroll
+        for (int k = 0; k < 6; k++) a.p[k][i] -= b.p[k][i];
+}
+
+// vectorExpand (matrix.cuh:129-139) of every share: out[j] = in[j / f2]
+__global__ void expand6_kernel(CSh6<uint64_t> in, Sh6<uint64_t> out, size_t n_out, int f2) {
+    for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n_out; j += (size_t)gridDim.x * blockDim.x)
+#pragma unroll
+        for (int k = 0; k < 6; k++) out.p[k][j] = in.p[k][j / f2];
+}
+
+// maxpool_row2im (convolution.cuh:111-152) of every share: window values are
+// added into their image positions ((batch, x, y, channel) indexing)
+__global__ void row2im6_kernel(CSh6<uint64_t> rows, Sh6<uint64_t> out, int imageHeight, int imageWidth, int f, int Din,
+                               int stride, size_t windows) {
+    const int wk = (imageWidth - f) / stride + 1, hk = (imageHeight - f) / stride + 1;
+    const size_t total = windows * f * f;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t cw = e / (f * f);
+        const int v = (int)(e - cw * f * f);
+        const size_t per_img = (size_t)wk * hk * Din;
+        const size_t b = cw / per_img, rem = cw - b * per_img;
+        const int widx = (int)(rem / Din), ch = (int)(rem % Din);
+        const int vcol = (widx / hk) * stride + v / f, vrow = (widx % hk) * stride + v % f;
+        const size_t o = b * (size_t)imageHeight * imageWidth * Din + (size_t)vcol * imageHeight * Din +
+                         (size_t)vrow * Din + ch;
+#pragma unroll
+        for (int k = 0; k < 6; k++)
+            atomicAdd((unsigned long long *)&out.p[k][o], (unsigned long long)rows.p[k][e]);
+    }
+}
+
+// to_fixed_functor (util/functors.h:117-123) runs on the device in the
+// reference: truncation toward zero, saturating, NaN -> 0 (cvt.rzi.u64.f64).
+inline uint64_t to_fixed_u64(double x) {
+    if (std::isnan(x) || x <= 0.0) return 0;
+    if (x >= 18446744073709551616.0) return std::numeric_limits<uint64_t>::max();
+    return (uint64_t)x;
+}
+
+// The host step of _reveal_softmax_grad (NeuralNetwork.cu:212-254): per party,
+// the revealed logits to double, exp, row sums in index order, divide, back to
+// fixed point. The reference runs this loop on the host as well. Runs as a
+// stream-ordered host function between the reveal's copy-out and the
+// softmax's copy-in, so that it can be part of a captured graph.
+void CUDART_CB softmax_host(void *arg) {
+    pg_net *net = (pg_net *)arg;
+    const size_t n = net->tr.n, batch = (size_t)net->tr.batch, classes = n / batch;
+    const double scale = (double)(1 << net->tr.fp);
+    std::vector<double> fa(n), sums(n / classes);
+    for (int p = 0; p < 3; p++) {
+        const uint64_t *rev = net->tr.h_rev + p * n;
+        uint64_t *sm = net->tr.h_sm + p * n;
+        std::fill(sums.begin(), sums.end(), 0.0);
+        for (size_t i = 0; i < n; i++) fa[i] = ((double)(int64_t)rev[i]) / scale;
+        for (size_t i = 0; i < n; i++) {
+            fa[i] = std::exp(fa[i]);
+            sums[i / classes] += fa[i];
+        }
+        for (size_t i = 0; i < n; i++) fa[i] /= sums[i / classes];
+        for (size_t i = 0; i < n; i++) sm[i] = to_fixed_u64(fa[i] * scale);
+    }
+}
+
+unsigned blocks_for(Ctx *c, size_t n) {
+    const int sms = c->sm_count > 0 ? c->sm_count : 148;
+    size_t b = (n + 255) / 256;
+    if (b > (size_t)sms * 8) b = (size_t)sms * 8;
+    return (unsigned)(b ? b : 1);
+}
+
+template <typename P> CSh6<uint64_t> c6(P const *a) {
+    CSh6<uint64_t> r;
+    for (int k = 0; k < 6; k++) r.p[k] = a[k];
+    return r;
+}
+Sh6<uint64_t> m6(uint64_t *const *a) {
+    Sh6<uint64_t> r;
+    for (int k = 0; k < 6; k++) r.p[k] = a[k];
+    return r;
+}
+
+int sub6(Ctx *c, uint64_t *const *a, const uint64_t *const *b, size_t n) {
+    if (!n) return PG_OK;
+    sub6_kernel<<<blocks_for(c, n), 256, 0, c->stream>>>(m6(a), c6(b), n);
+    c->launches++;
+    return launch_status(c, "sub6_kernel");
+}
+
+int log_mini_batch(int batch) {  // (int)log2(MINI_BATCH_SIZE), util/model.cu:39
+    int t = 0;
+    while ((2ll << t) <= batch) t++;
+    return t;
+}
+
+}  // namespace
+
+// Training buffers: per-layer gradients, labels, the softmax step, the
+// parameter-gradient scratch, and a parameter snapshot for capture.
+static int net_train_setup(pg_net *net) {
+    if (net->tr.arena) return PG_OK;
+    Ctx *c = net->ctx;
+    if (net->fp > 30) return set_error(c, PG_ERR_UNSUPPORTED, "training needs FLOAT_PRECISION <= 30 (got %d)", net->fp);
+    if (net->out_n % net->batch) return set_error(c, PG_ERR_SIZE, "output size is not a multiple of the batch");
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    PG_CHECK_CUDA(c, cudaStreamIsCapturing(c->stream, &cs));
+    if (cs != cudaStreamCaptureStatusNone)
+        return set_error(c, PG_ERR_INVALID_ARG, "training buffers must be set up by an eager step first");
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    size_t max_w = 0, max_b = 0, max_d = 0, max_sel = 0, params = 0;
+    for (auto &L : net->layers) {
+        max_w = L.w_n > max_w ? L.w_n : max_w;
+        max_b = L.b_n > max_b ? L.b_n : max_b;
+        max_d = L.type == PG_LAYER_MAXPOOL && L.d_n > max_d ? L.d_n : max_d;
+        const size_t sel = L.type == PG_LAYER_MAXPOOL ? L.d_n : L.type == PG_LAYER_RELU ? L.out_n : 0;
+        max_sel = sel > max_sel ? sel : max_sel;
+        params += 6 * (al(L.w_n * 8) + al(L.b_n * 8));
+    }
+    const size_t on = net->out_n;
+    size_t bytes = 2 * al(6 * on * 8) + 6 * al(on * 8);  // labels, sdelta, rev[3] + sm[3]
+    for (auto &L : net->layers) bytes += al(6 * L.in_n * 8);
+    bytes += 6 * (al(max_w * 8) + al(max_b * 8) + al(max_d * 8)) + al(max_sel * 8) + params;
+    if (cudaMalloc(&net->tr.arena, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        net->tr.arena = nullptr;
+        return set_error(c, PG_ERR_NO_MEMORY, "training buffers of %zu bytes", bytes);
+    }
+    if (cudaMallocHost(&net->tr.h_rev, 2 * 3 * on * 8) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(net->tr.arena);
+        net->tr.arena = nullptr;
+        net->tr.h_rev = nullptr;
+        return set_error(c, PG_ERR_NO_MEMORY, "pinned softmax buffers");
+    }
+    net->tr.h_sm = net->tr.h_rev + 3 * on;
+    PG_CHECK_CUDA(c, cudaMemsetAsync(net->tr.arena, 0, bytes, c->stream));
+    char *ptr = (char *)net->tr.arena;
+    for (int k = 0; k < 6; k++) net->tr.labels[k] = (uint64_t *)(ptr + k * on * 8);
+    ptr += al(6 * on * 8);
+    for (int k = 0; k < 6; k++) net->tr.sdelta[k] = (uint64_t *)(ptr + k * on * 8);
+    ptr += al(6 * on * 8);
+    for (int p = 0; p < 3; p++) { net->tr.rev[p] = (uint64_t *)ptr; ptr += al(on * 8); }
+    for (int p = 0; p < 3; p++) { net->tr.sm[p] = (uint64_t *)ptr; ptr += al(on * 8); }
+    for (auto &L : net->layers) {
+        for (int k = 0; k < 6; k++) L.delta[k] = (uint64_t *)(ptr + k * L.in_n * 8);
+        ptr += al(6 * L.in_n * 8);
+    }
+    for (int k = 0; k < 6; k++) { net->tr.dW[k] = (uint64_t *)ptr; ptr += al(max_w * 8); }
+    for (int k = 0; k < 6; k++) { net->tr.db[k] = (uint64_t *)ptr; ptr += al(max_b * 8); }
+    for (int k = 0; k < 6; k++) { net->tr.pools[k] = (uint64_t *)ptr; ptr += al(max_d * 8); }
+    net->tr.zeros = (uint64_t *)ptr;
+    ptr += al(max_sel * 8);
+    net->tr.backup = (uint64_t *)ptr;
+    net->tr.backup_bytes = params;
+    net->tr.n = on;
+    net->tr.batch = net->batch;
+    net->tr.fp = net->fp;
+    return PG_OK;
+}
+
+// Snapshot / restore of every weight and bias share (device to device).
+static int net_params_copy(pg_net *net, bool save) {
+    Ctx *c = net->ctx;
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    char *bk = (char *)net->tr.backup;
+    for (auto &L : net->layers)
+        for (int k = 0; k < 6; k++) {
+            if (L.w_n) {
+                PG_CHECK_CUDA(c, cudaMemcpyAsync(save ? (void *)bk : (void *)L.w[k], save ? (void *)L.w[k] : (void *)bk,
+                                                 L.w_n * 8, cudaMemcpyDeviceToDevice, c->stream));
+            }
+            bk += al(L.w_n * 8);
+            if (L.b_n) {
+                PG_CHECK_CUDA(c, cudaMemcpyAsync(save ? (void *)bk : (void *)L.b[k], save ? (void *)L.b[k] : (void *)bk,
+                                                 L.b_n * 8, cudaMemcpyDeviceToDevice, c->stream));
+            }
+            bk += al(L.b_n * 8);
+        }
+    if (!save && net->limb_arena)
+        for (auto &L : net->layers)
+            if (L.packB) {
+                int st = lt::run_pack(c, L.plan, (const uint64_t *const *)L.w, L.packB);
+                if (st) return st;
+            }
+    return PG_OK;
+}
+
+// _reveal_softmax_grad (NeuralNetwork.cu:207-267) into tr.sdelta.
+static int net_softmax_grad(pg_net *net, const uint64_t *const labels[6]) {
+    Ctx *c = net->ctx;
+    const size_t n = net->out_n;
+    NetLayer &last = net->layers.back();
+    int st = rss_reconstruct<uint64_t>(c, (const uint64_t *const *)last.out, n, net->tr.rev);
+    if (st) return st;
+    for (int p = 0; p < 3; p++)
+        PG_CHECK_CUDA(c, cudaMemcpyAsync(net->tr.h_rev + p * n, net->tr.rev[p], n * 8, cudaMemcpyDeviceToHost, c->stream));
+    PG_CHECK_CUDA(c, cudaLaunchHostFunc(c->stream, softmax_host, net));
+    for (int p = 0; p < 3; p++)
+        PG_CHECK_CUDA(c, cudaMemcpyAsync(net->tr.sm[p], net->tr.h_sm + p * n, n * 8, cudaMemcpyHostToDevice, c->stream));
+    softmax_delta_kernel<<<blocks_for(c, n), 256, 0, c->stream>>>(m6(net->tr.sdelta), net->tr.sm[0], net->tr.sm[2],
+                                                                  c6(labels), n);
+    c->launches++;
+    if ((st = launch_status(c, "softmax_delta_kernel"))) return st;
+    const int lmb = log_mini_batch(net->batch);
+    if (lmb > 1) st = rss_divide_public<uint64_t>(c, net->tr.sdelta, n, 1ull << lmb, nullptr);
+    return st;
+}
+
+static int share_gemm(Ctx *c, const uint64_t *const *a, const uint64_t *const *b, uint64_t *const *out, int M, int N,
+                      int K, int tA, int tB, int tC, int trunc) {
+    if (c->form == PG_FORM_LIMB_TC) return limb3_rss_matmul_u64(c, a, b, out, nullptr, M, N, K, tA, tB, tC, trunc);
+    return rss_matmul<uint64_t>(c, a, b, out, nullptr, M, N, K, tA, tB, tC, trunc);
+}
+
+// NeuralNetwork::_backward_pass (NeuralNetwork.cu:444-460): every layer's
+// backward from the last to the first, each updating its parameters.
+static int net_backward(pg_net *net, const uint64_t *const in[6], const uint64_t *const labels[6], int log_lr) {
+    Ctx *c = net->ctx;
+    if (log_lr < 0 || net->fp + log_lr > 62) return set_error(c, PG_ERR_INVALID_ARG, "bad log learning rate %d", log_lr);
+    int st = net_softmax_grad(net, labels);
+    if (st) return st;
+    const uint64_t *const *din = (const uint64_t *const *)net->tr.sdelta;
+    const uint64_t *zeros6[6];
+    for (int k = 0; k < 6; k++) zeros6[k] = net->tr.zeros;
+    const int B = net->batch;
+    for (int li = (int)net->layers.size() - 1; li >= 0; li--) {
+        NetLayer &L = net->layers[li];
+        const uint64_t *const *fwd_in = li ? (const uint64_t *const *)net->layers[li - 1].out : in;
+        switch (L.type) {
+            case PG_LAYER_FC: {  // FCLayer::backward (FCLayer.cu:132-217)
+                const int din_ = L.p[0], dout = L.p[1];
+                if ((st = share_gemm(c, din, (const uint64_t *const *)L.w, L.delta, B, din_, dout, 1, 0, 1, net->fp))) return st;
+                if ((st = share_gemm(c, din, fwd_in, net->tr.dW, dout, din_, B, 0, 1, 0, net->fp + log_lr))) return st;
+                if ((st = sub6(c, L.w, net->tr.dW, L.w_n))) return st;
+                for (int k = 0; k < 6; k++) {
+                    PG_CHECK_CUDA(c, cudaMemsetAsync(net->tr.db[k], 0, L.b_n * 8, c->stream));
+                    // reduceSum(delta, db, false, outputDim, batchSize), as the reference calls it
+                    if ((st = reduce_sum_u64(c, din[k], net->tr.db[k], 0, dout, B))) return st;
+                }
+                if ((st = rss_divide_public<uint64_t>(c, net->tr.db, L.b_n, 1ull << log_lr, nullptr))) return st;
+                if ((st = sub6(c, L.b, net->tr.db, L.b_n))) return st;
+                break;
+            }
+            case PG_LAYER_CNN: {  // CNNLayer::backward (CNNLayer.cu:114-193)
+                const int H = L.p[0], W = L.p[1], Din = L.p[2], Dout = L.p[3], f = L.p[4], s = L.p[5], pd = L.p[6];
+                if ((st = rss_conv<uint64_t>(c, din, (const uint64_t *const *)L.w, L.delta, PG_CONV_DGRAD, B, H, W, f, Din,
+                                             Dout, s, pd, net->fp)))
+                    return st;
+                if ((st = rss_conv<uint64_t>(c, din, fwd_in, net->tr.dW, PG_CONV_WGRAD, B, H, W, f, Din, Dout, s, pd,
+                                             net->fp)))
+                    return st;
+                if ((st = rss_divide_public<uint64_t>(c, net->tr.dW, L.w_n, 1ull << log_lr, nullptr))) return st;
+                if ((st = sub6(c, L.w, net->tr.dW, L.w_n))) return st;
+                break;
+            }
+            case PG_LAYER_RELU:  // ReLULayer::backward (ReLULayer.cu:90-124)
+                st = rss_select<uint64_t, uint8_t>(c, zeros6, din, (const uint8_t *const *)L.d, L.delta, L.in_n);
+                if (st) return st;
+                break;
+            case PG_LAYER_MAXPOOL: {  // MaxpoolLayer::backward (MaxpoolLayer.cu:133-185)
+                const int H = L.p[0], W = L.p[1], C = L.p[2], f = L.p[3], s = L.p[4];
+                expand6_kernel<<<blocks_for(c, L.d_n), 256, 0, c->stream>>>(c6(din), m6(net->tr.pools), L.d_n, f * f);
+                c->launches++;
+                if ((st = launch_status(c, "expand6_kernel"))) return st;
+                st = rss_select<uint64_t, uint8_t>(c, zeros6, (const uint64_t *const *)net->tr.pools,
+                                                   (const uint8_t *const *)L.d, net->tr.pools, L.d_n);
+                if (st) return st;
+                PG_CHECK_CUDA(c, cudaMemsetAsync(L.delta[0], 0, 6 * L.in_n * 8, c->stream));
+                // row2im gets (imageWidth, imageHeight) in its (imageHeight, imageWidth) slots, as the reference passes them
+                const size_t windows = L.d_n / ((size_t)f * f);
+                row2im6_kernel<<<blocks_for(c, L.d_n), 256, 0, c->stream>>>(
+                    c6(net->tr.pools), m6(L.delta), W, H, f, C, s, windows);
+                c->launches++;
+                if ((st = launch_status(c, "row2im6_kernel"))) return st;
+                break;
+            }
+            default: return set_error(c, PG_ERR_INVALID_ARG, "bad layer type %d", L.type);
+        }
+        // the limb form keeps packed weights: repack the updated ones
+        if (net->limb_arena && L.packB && (st = lt::run_pack(c, L.plan, (const uint64_t *const *)L.w, L.packB))) return st;
+        din = (const uint64_t *const *)L.delta;
+    }
+    return PG_OK;
+}
+
+static int net_train(pg_net *net, const uint64_t *const in[6], const uint64_t *const labels[6], int log_lr) {
+    int st = net_run(net, in);
+    if (st) return st;
+    return net_backward(net, in, labels, log_lr);
+}
+
 extern "C" {
 
 int pg_net_create(pg_ctx *c, pg_net **out, const int *spec, int nlayers, int batch, int fp) {
@@ -264,9 +606,13 @@ int pg_net_destroy(pg_net *net) {
     for (auto e : net->ev) cudaEventDestroy(e);
     if (net->exec) cudaGraphExecDestroy(net->exec);
     if (net->graph) cudaGraphDestroy(net->graph);
-    if (net->arena || net->limb_arena) cudaStreamSynchronize(net->ctx->stream);
+    if (net->exec_train) cudaGraphExecDestroy(net->exec_train);
+    if (net->graph_train) cudaGraphDestroy(net->graph_train);
+    if (net->arena || net->limb_arena || net->tr.arena) cudaStreamSynchronize(net->ctx->stream);
     if (net->arena) cudaFree(net->arena);
     if (net->limb_arena) cudaFree(net->limb_arena);
+    if (net->tr.arena) cudaFree(net->tr.arena);
+    if (net->tr.h_rev) cudaFreeHost(net->tr.h_rev);
     delete net;
     return PG_OK;
 }
@@ -425,6 +771,146 @@ int pg_net_layer_output(pg_net *net, int layer, uint64_t *const out[6], size_t *
     if (out)
         for (int k = 0; k < 6; k++) ((uint64_t **)out)[k] = L.out[k];
     if (n) *n = L.out_n;
+    return PG_OK;
+}
+
+// ----------------------------------------------------------- training API
+
+int pg_net_train_setup(pg_net *net) {
+    if (!net) return PG_ERR_INVALID_ARG;
+    return net_train_setup(net);
+}
+
+int pg_net_label_shares(pg_net *net, uint64_t *out[6]) {
+    if (!net || !out) return PG_ERR_INVALID_ARG;
+    int st = net_train_setup(net);
+    if (st) return st;
+    for (int k = 0; k < 6; k++) out[k] = net->tr.labels[k];
+    return PG_OK;
+}
+
+int pg_net_backward(pg_net *net, const uint64_t *const in[6], const uint64_t *const labels[6], int log_lr) {
+    if (!net || !in || !labels) return PG_ERR_INVALID_ARG;
+    int st = net_train_setup(net);
+    if (st) return st;
+    return net_backward(net, in, labels, log_lr);
+}
+
+int pg_net_train_step(pg_net *net, const uint64_t *const in[6], const uint64_t *const labels[6], int log_lr) {
+    if (!net || !in || !labels) return PG_ERR_INVALID_ARG;
+    int st = net_train_setup(net);
+    if (st) return st;
+    return net_train(net, in, labels, log_lr);
+}
+
+int pg_net_capture_train(pg_net *net, int log_lr) {
+    if (!net) return PG_ERR_INVALID_ARG;
+    Ctx *c = net->ctx;
+    int st = net_train_setup(net);
+    if (st) return st;
+    if (net->exec_train) {
+        cudaGraphExecDestroy(net->exec_train);
+        net->exec_train = nullptr;
+    }
+    if (net->graph_train) {
+        cudaGraphDestroy(net->graph_train);
+        net->graph_train = nullptr;
+    }
+    const uint64_t *const *in = (const uint64_t *const *)net->in;
+    const uint64_t *const *lab = (const uint64_t *const *)net->tr.labels;
+    // One eager step first (it sizes the context scratch and sets up the
+    // limb-form buffers), with the parameters restored afterwards.
+    {
+        uint64_t comm_save[9];
+        memcpy(comm_save, c->comm, sizeof(comm_save));
+        uint64_t launches_save = c->launches.load();
+        int st0 = net_params_copy(net, true);
+        if (!st0) st0 = net_train(net, in, lab, log_lr);
+        if (!st0) st0 = net_params_copy(net, false);
+        memcpy(c->comm, comm_save, sizeof(comm_save));
+        c->launches = launches_save;
+        if (st0) return st0;
+        PG_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    cudaStream_t cap = nullptr, user = c->stream;
+    PG_CHECK_CUDA(c, cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaEvent_t ev = nullptr;
+    PG_CHECK_CUDA(c, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaEventRecord(ev, user);
+    cudaStreamWaitEvent(cap, ev, 0);
+    uint64_t comm_before[9];
+    memcpy(comm_before, c->comm, sizeof(comm_before));
+    uint64_t launches_before = c->launches.load();
+    c->stream = cap;
+    cudaError_t e0 = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    st = e0 == cudaSuccess ? net_train(net, in, lab, log_lr) : PG_ERR_CUDA;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = e0 == cudaSuccess ? cudaStreamEndCapture(cap, &g) : e0;
+    c->stream = user;
+    cudaStreamSynchronize(cap);
+    cudaStreamDestroy(cap);
+    cudaEventDestroy(ev);
+    for (int k = 0; k < 9; k++) net->comm_per_train[k] = c->comm[k] - comm_before[k];
+    memcpy(c->comm, comm_before, sizeof(comm_before));
+    uint64_t launched = c->launches.load() - launches_before;
+    c->launches = launches_before;
+    if (st) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return set_error(c, PG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    net->graph_train = g;
+    PG_CHECK_CUDA(c, cudaGraphInstantiate(&net->exec_train, g, 0));
+    net->launches_per_train = launched;
+    return PG_OK;
+}
+
+int pg_net_train_resident(pg_net *net) {
+    if (!net) return PG_ERR_INVALID_ARG;
+    Ctx *c = net->ctx;
+    if (!net->exec_train) return set_error(c, PG_ERR_INVALID_ARG, "no captured training step");
+    PG_CHECK_CUDA(c, cudaGraphLaunch(net->exec_train, c->stream));
+    for (int k = 0; k < 9; k++) c->comm[k] += net->comm_per_train[k];
+    c->launches += net->launches_per_train;
+    return PG_OK;
+}
+
+int pg_net_train_host(pg_net *net, const uint64_t *in_host, const uint64_t *labels_host, uint64_t *out_host,
+                      int log_lr) {
+    if (!net || !in_host || !labels_host || !out_host) return PG_ERR_INVALID_ARG;
+    Ctx *c = net->ctx;
+    int st = net_train_setup(net);
+    if (st) return st;
+    PG_CHECK_CUDA(c, cudaMemcpyAsync(net->in[0], in_host, 6 * net->in_n * 8, cudaMemcpyHostToDevice, c->stream));
+    PG_CHECK_CUDA(c, cudaMemcpyAsync(net->tr.labels[0], labels_host, 6 * net->out_n * 8, cudaMemcpyHostToDevice,
+                                     c->stream));
+    st = net->exec_train ? pg_net_train_resident(net)
+                         : net_train(net, (const uint64_t *const *)net->in, (const uint64_t *const *)net->tr.labels,
+                                     log_lr);
+    if (st) return st;
+    NetLayer &last = net->layers.back();
+    PG_CHECK_CUDA(c, cudaMemcpyAsync(out_host, last.out[0], 6 * net->out_n * 8, cudaMemcpyDeviceToHost, c->stream));
+    return PG_OK;
+}
+
+int pg_net_layer_delta(pg_net *net, int layer, uint64_t *out[6], size_t *n) {
+    if (!net || !out || layer < -1 || layer >= (int)net->layers.size()) return PG_ERR_INVALID_ARG;
+    if (!net->tr.arena) return set_error(net->ctx, PG_ERR_INVALID_ARG, "no training step has run");
+    // layer -1: the softmax gradient that enters the last layer
+    for (int k = 0; k < 6; k++) out[k] = layer < 0 ? net->tr.sdelta[k] : net->layers[layer].delta[k];
+    if (n) *n = layer < 0 ? net->out_n : net->layers[layer].in_n;
+    return PG_OK;
+}
+
+int pg_net_layer_params(pg_net *net, int layer, uint64_t *w[6], uint64_t *b[6], size_t *w_n, size_t *b_n) {
+    if (!net || layer < 0 || layer >= (int)net->layers.size()) return PG_ERR_INVALID_ARG;
+    NetLayer &L = net->layers[layer];
+    for (int k = 0; k < 6; k++) {
+        if (w) w[k] = L.w_n ? L.w[k] : nullptr;
+        if (b) b[k] = L.b_n ? L.b[k] : nullptr;
+    }
+    if (w_n) *w_n = L.w_n;
+    if (b_n) *b_n = L.b_n;
     return PG_OK;
 }
 

@@ -1,0 +1,196 @@
+"""Training-step parity: the GPU executor's forward + backward + SGD update
+against the oracle's restatement, bit for bit — every layer's outputs, every
+gradient passed between layers, the softmax gradient, and every updated
+weight and bias share — plus the message counters."""
+import numpy as np
+import pytest
+
+import oracle as orc
+from tests import netref
+from tests.test_gpu_network import _wrap_device, gather
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pg():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import piranha_gb300 as pg
+
+    pg.lib()
+    return pg
+
+
+def one_hot_labels(batch, classes, seed):
+    rng = np.random.default_rng(seed)
+    y = np.zeros((batch, classes))
+    y[np.arange(batch), rng.integers(0, classes, batch)] = 1.0
+    return orc.set_public(y.ravel())
+
+
+def make_net(pg, ctx, layers, params, batch):
+    net = pg.Network(ctx, layers, batch)
+    for i, prm in enumerate(params):
+        if prm is not None:
+            net.set_params(i, pg.to_device(prm[0]), pg.to_device(prm[1]) if prm[1] is not None else None)
+    return net
+
+
+def fill(ptrs, views):
+    """Copy (3, 2, n) views into a contiguous [6][n] device block."""
+    import torch
+
+    n = views.shape[2]
+    dst = _wrap_device(ptrs[0], 6 * n)
+    dst.copy_(torch.from_numpy(np.ascontiguousarray(views).reshape(-1).view(np.int64)).cuda())
+    torch.cuda.synchronize()
+
+
+def check_against_oracle(pg, net, layers, want_outs, want_params, want_deltas, want_softmax):
+    for i in range(len(layers)):
+        optrs, n = net.layer_output_ptrs(i)
+        assert np.array_equal(gather(pg, optrs, n), want_outs[i]), f"output of layer {i} {layers[i]}"
+    dptrs, n = net.layer_delta_ptrs(-1)
+    assert np.array_equal(gather(pg, dptrs, n), want_softmax), "softmax gradient"
+    for i in range(len(layers)):
+        dptrs, n = net.layer_delta_ptrs(i)
+        assert np.array_equal(gather(pg, dptrs, n), want_deltas[i]), f"gradient out of layer {i} {layers[i]}"
+        if want_params[i] is not None:
+            w, wn, b, bn = net.layer_param_ptrs(i)
+            assert np.array_equal(gather(pg, w, wn), want_params[i][0]), f"weights of layer {i}"
+            if want_params[i][1] is not None:
+                assert np.array_equal(gather(pg, b, bn), want_params[i][1]), f"bias of layer {i}"
+
+
+def oracle_step(layers, params, x, labels, batch, log_lr, comm=None):
+    bits = []
+    _, outs = netref.forward(layers, params, x, batch, keep=True, bits=bits, comm=comm)
+    softmax = orc.reveal_softmax_grad(outs[-1], labels, batch)
+    new_params, deltas = netref.backward(layers, params, x, outs, bits, labels, batch, log_lr=log_lr, comm=comm)
+    return outs, new_params, deltas, softmax
+
+
+@pytest.mark.parametrize("form", ["u64", "tc"])
+def test_secureml_fixture_training_step(pg, golden, form):
+    """One SGD iteration of the SecureML net on the reference's training
+    fixture (learning rate 2^-9), every share against the oracle."""
+    L = golden[1]
+    layers = netref.secureml_layers()
+    params = []
+    for li in (0, 2, 4):
+        params += [(orc.set_public(L[f"secureml_weight{li}"]), orc.set_public(L[f"secureml_bias{li}"])), None]
+    x = orc.set_public(L["secureml_input"])
+    labels = orc.set_public(L["secureml_labels"])
+    comm = orc.Comm()
+    outs, new_params, deltas, softmax = oracle_step(layers, params, x, labels, 128, 9)
+    ctx = pg.Context(0, form=pg.FORM_LIMB_TC if form == "tc" else pg.FORM_U64)
+    net = make_net(pg, ctx, layers, params, 128)
+    ctx.reset_comm()
+    net.train_step(pg.to_device(x), pg.to_device(labels), 9)
+    ctx.sync()
+    check_against_oracle(pg, net, layers, outs, new_params, deltas, softmax)
+    ctx.check_device_errors()
+    net.close()
+    ctx.close()
+
+
+def test_training_step_counters(pg):
+    layers = netref.secureml_layers()
+    params = netref.kaiming_uniform_params(layers, 3)
+    batch = 16
+    rng = np.random.default_rng(4)
+    x = orc.share_random(orc.encode(rng.uniform(0, 1, batch * 784)), seed=5)
+    labels = one_hot_labels(batch, 10, 6)
+    # the forward's FC layers are accounted by netref.forward itself
+    comm = orc.Comm()
+    oracle_step(layers, params, x, labels, batch, 5, comm)
+    ctx = pg.Context(0)
+    net = make_net(pg, ctx, layers, params, batch)
+    ctx.reset_comm()
+    net.train_step(pg.to_device(x), pg.to_device(labels), 5)
+    ctx.sync()
+    got = ctx.comm()
+    assert got["tx"] == comm.tx and got["rx"] == comm.rx and got["rounds"] == comm.rounds, (got, comm.tx, comm.rounds)
+    net.close()
+    ctx.close()
+
+
+@pytest.mark.parametrize("form", ["u64", "tc"])
+def test_lenet_training_step(pg, form):
+    """LeNet (files/models/lenet.json: conv-maxpool-relu x2, FC-relu-FC-relu)
+    at batch 8, log learning rate 5, random input shares."""
+    layers = netref.lenet_layers()
+    params = netref.kaiming_uniform_params(layers, 11)
+    batch = 8
+    rng = np.random.default_rng(12)
+    x = orc.share_random(orc.encode(rng.uniform(0, 1, batch * 784)), seed=13)
+    labels = one_hot_labels(batch, 10, 14)
+    outs, new_params, deltas, softmax = oracle_step(layers, params, x, labels, batch, 5)
+    ctx = pg.Context(0, form=pg.FORM_LIMB_TC if form == "tc" else pg.FORM_U64)
+    net = make_net(pg, ctx, layers, params, batch)
+    net.train_step(pg.to_device(x), pg.to_device(labels), 5)
+    ctx.sync()
+    check_against_oracle(pg, net, layers, outs, new_params, deltas, softmax)
+    ctx.check_device_errors()
+    net.close()
+    ctx.close()
+
+
+@pytest.mark.parametrize("form", ["u64", "tc"])
+def test_lenet_training_captured_two_steps(pg, form):
+    """The captured training step: the capture's eager warm-up leaves the
+    parameters as they were, and two graph replays are two SGD iterations."""
+    layers = netref.lenet_layers()
+    params = netref.kaiming_uniform_params(layers, 21)
+    batch = 4
+    rng = np.random.default_rng(22)
+    x = orc.share_random(orc.encode(rng.uniform(0, 1, batch * 784)), seed=23)
+    labels = one_hot_labels(batch, 10, 24)
+    _, p1, _, _ = oracle_step(layers, params, x, labels, batch, 6)
+    outs2, p2, deltas2, softmax2 = oracle_step(layers, p1, x, labels, batch, 6)
+    ctx = pg.Context(0, form=pg.FORM_LIMB_TC if form == "tc" else pg.FORM_U64)
+    net = make_net(pg, ctx, layers, params, batch)
+    net.train_step(pg.to_device(x), pg.to_device(labels), 6)  # sets up the training buffers eagerly
+    for i, prm in enumerate(params):  # back to the initial parameters
+        if prm is not None:
+            net.set_params(i, pg.to_device(prm[0]), pg.to_device(prm[1]) if prm[1] is not None else None)
+    fill(net.input_buffers(), x)
+    fill(net.label_buffers(), labels)
+    net.capture_train(6)
+    net.train_resident()
+    net.train_resident()
+    ctx.sync()
+    check_against_oracle(pg, net, layers, outs2, p2, deltas2, softmax2)
+    net.close()
+    ctx.close()
+
+
+def test_train_host_buffers(pg):
+    """pg_net_train_host: pinned host input and labels in, the forward's output
+    shares out, the parameters updated on the device."""
+    import torch
+
+    layers = netref.secureml_layers()
+    params = netref.kaiming_uniform_params(layers, 31)
+    batch = 32
+    rng = np.random.default_rng(32)
+    x = orc.share_random(orc.encode(rng.uniform(0, 1, batch * 784)), seed=33)
+    labels = one_hot_labels(batch, 10, 34)
+    outs, new_params, _, _ = oracle_step(layers, params, x, labels, batch, 7)
+    ctx = pg.Context(0)
+    net = make_net(pg, ctx, layers, params, batch)
+    xin = torch.from_numpy(np.ascontiguousarray(x).reshape(-1).view(np.int64)).pin_memory()
+    lin = torch.from_numpy(np.ascontiguousarray(labels).reshape(-1).view(np.int64)).pin_memory()
+    out = torch.empty(6 * net.out_n, dtype=torch.int64).pin_memory()
+    net.train_host(xin.data_ptr(), lin.data_ptr(), out.data_ptr(), 7)
+    ctx.sync()
+    assert np.array_equal(out.numpy().view(np.uint64).reshape(3, 2, -1), outs[-1])
+    for i, prm in enumerate(new_params):
+        if prm is not None:
+            w, wn, b, bn = net.layer_param_ptrs(i)
+            assert np.array_equal(gather(pg, w, wn), prm[0])
+            assert np.array_equal(gather(pg, b, bn), prm[1])
+    net.close()
+    ctx.close()
