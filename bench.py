@@ -1,12 +1,12 @@
 #!/usr/bin/env python
 """Benchmark: 3PC VGG16 secure inference (batch 128, uint64 shares, 26 fractional bits).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 
-Workload (one "step" = one secure forward of a batch): VGG16 of Piranha's
-files/models/vgg16-cifar10.json with its five averagepool layers replaced by
-2x2/2 maxpool, batch 128 of synthetic 32x32x3 images uniform in [0,1],
-fixed-point encoded with 26 fractional bits and shared among the three
+Default workload (one "step" = one secure forward of a batch): VGG16 of
+Piranha's files/models/vgg16-cifar10.json with its five averagepool layers
+replaced by 2x2/2 maxpool, batch 128 of synthetic 32x32x3 images uniform in
+[0,1], fixed-point encoded with 26 fractional bits and shared among the three
 simulated parties with seeded random masks; weights are seeded
 Kaiming-uniform loaded with Piranha's setPublic. All three parties run on one
 GPU; the whole forward is replayed from one CUDA graph.
@@ -16,6 +16,12 @@ a 256 MiB write that flushes L2; device time from CUDA events on the replay
 stream; wall clock bracketed by barrier + synchronize. `value` = images/s of
 the device-resident replays; `e2e` = the same through pg_net_forward_host with
 pinned host shares in and out (H2D + forward + D2H per step).
+
+Other workloads (--workload), each printing the same JSON line for its own metric:
+  secureml      3PC SecureML (784-128-128-10, ReLU after every FC) inference, batch 128, u64, FP 26
+  lenet-train   3PC LeNet training step (forward + backward + SGD, log learning rate 5), batch 128
+  secureml-2pc  2PC SecureML inference, batch 128, uint32 shares, FP 10
+  secureml-4pc  4PC SecureML inference, batch 128, uint32 shares, FP 10
 
 With --impl reference the line times Piranha's own arithmetic restated on the
 CPU (the oracle; the reference's GPU build cannot be compiled here) on a
@@ -30,7 +36,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np
@@ -38,12 +43,31 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+from piranha_gb300 import encode as enc  # noqa: E402
+from piranha_gb300 import nets  # noqa: E402
+
 BATCH = 128
-FP = 26
 SEED = 2024
-METRIC = "3PC VGG16 secure inference img/s"
-WORKLOAD = "vgg16-cifar10 (averagepool->maxpool 2x2/2), 3PC RSS, batch 128, uint64 shares, FP 26"
 LIMB_FLOPS_PER_RING_MAC = 72  # 36 8-bit limb pairs x 2 flops: exact u64 MAC on fp16 tensor cores
+
+WORKLOADS = {
+    "vgg16": {"metric": "3PC VGG16 secure inference img/s", "kind": "infer3", "fp": 26, "ring": "u64",
+              "desc": "vgg16-cifar10 (averagepool->maxpool 2x2/2), 3PC RSS, batch 128, uint64 shares, FP 26"},
+    "secureml": {"metric": "3PC SecureML secure inference img/s", "kind": "infer3", "fp": 26, "ring": "u64",
+                 "desc": "secureml 784-128-128-10 (ReLU after every FC), 3PC RSS, batch 128, uint64 shares, FP 26"},
+    "lenet-train": {"metric": "3PC LeNet training step img/s", "kind": "train3", "fp": 26, "ring": "u64",
+                    "log_lr": 5,
+                    "desc": "lenet (maxpool variant), 3PC RSS, batch 128, uint64 shares, FP 26, "
+                            "forward + revealed-softmax backward + SGD (log learning rate 5)"},
+    "secureml-2pc": {"metric": "2PC SecureML secure inference img/s", "kind": "fcnet", "parties": 2, "fp": 10,
+                     "ring": "u32",
+                     "desc": "secureml 784-128-128-10, 2PC (TPC), batch 128, uint32 shares, FP 10"},
+    "secureml-4pc": {"metric": "4PC SecureML secure inference img/s", "kind": "fcnet", "parties": 4, "fp": 10,
+                     "ring": "u32",
+                     "desc": "secureml 784-128-128-10, 4PC (FPC), batch 128, uint32 shares, FP 10"},
+}
+_LAYERS = {"vgg16": nets.vgg16, "secureml": nets.secureml, "lenet-train": nets.lenet,
+           "secureml-2pc": nets.secureml, "secureml-4pc": nets.secureml}
 
 
 def parse():
@@ -52,6 +76,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="vgg16", choices=sorted(WORKLOADS))
     ap.add_argument("--form", default="auto", choices=["auto", "u64", "tc"])
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU sample budget")
@@ -62,26 +87,52 @@ def parse():
 
 # ------------------------------------------------------------------ workload
 
-def vgg16_workload(batch, seed=SEED):
-    import oracle as orc
-    from tests import netref
-
-    layers = netref.vgg16_layers()
-    params = netref.kaiming_uniform_params(layers, seed, FP)
+def make_workload(name, batch, seed=SEED):
+    """Layers, setPublic-loaded seeded parameters, seeded input shares (and labels for training)."""
+    w = WORKLOADS[name]
+    layers = _LAYERS[name]()
+    fp, ring = w["fp"], w["ring"]
     rng = np.random.default_rng(seed + 1)
-    x = orc.share_random(orc.encode(rng.uniform(0, 1, batch * 3072), np.uint64, FP), np.uint64, seed=seed + 2)
-    return layers, params, x
+    vals = rng.uniform(0, 1, batch * nets.input_size(layers))
+    if w["kind"] == "fcnet":
+        setp = enc.tpc_set_public if w["parties"] == 2 else enc.fpc_set_public
+        prng = np.random.default_rng(seed)
+        params = []
+        for L in layers:
+            if L[0] == "fc":
+                din, dout = L[1], L[2]
+                wv = prng.uniform(-1, 1, din * dout) * np.sqrt(6.0 / din)
+                params.append((setp(wv, ring, fp), setp(np.full(dout, 0.01), ring, fp)))
+            else:
+                params.append(None)
+        return {"layers": layers, "params": params, "x": setp(vals, ring, fp), "labels": None}
+    params = nets.kaiming_uniform(layers, seed, fp)
+    x = enc.share_random(enc.encode(vals, ring, fp), ring, seed=seed + 2)
+    labels = None
+    if w["kind"] == "train3":
+        classes = np.random.default_rng(seed + 3).integers(0, 10, batch)
+        labels = enc.set_public(enc.one_hot(classes, 10), ring, fp)
+    return {"layers": layers, "params": params, "x": x, "labels": labels}
 
 
-def conv_ring_macs(layers, batch):
-    """Ring multiply-adds per conv layer of one forward (3 parties x concatenated K = 6 per plaintext MAC)."""
+def ring_macs(layers, batch):
+    """Ring multiply-adds per share-GEMM layer of one forward (3 parties x concatenated K = 6 per plaintext MAC)."""
     out = {}
     for i, L in enumerate(layers):
         if L[0] == "cnn":
             H, W, Din, Dout, f, s, p = L[1:]
             P, Q = (H + 2 * p - f) // s + 1, (W + 2 * p - f) // s + 1
             out[i] = 6 * batch * P * Q * Dout * f * f * Din
+        elif L[0] == "fc":
+            out[i] = 6 * batch * L[1] * L[2]
     return out
+
+
+def load_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        return {}
 
 
 # -------------------------------------------------------------------- clocks
@@ -131,32 +182,60 @@ class ClockSampler:
 
 # ------------------------------------------------------------ CPU baseline
 
-def cpu_baseline(layers, params, x_full, batch_full, budget_s):
+def cpu_baseline(name, wl, batch_full, budget_s):
     """Piranha's arithmetic restated on the CPU (the oracle), timed on a sample of the batch."""
     import oracle as orc
     from tests import netref
 
     orc.lib()
-    n_in = x_full.shape[2] // batch_full
+    w = WORKLOADS[name]
+    layers, params, x_full = wl["layers"], wl["params"], wl["x"]
+    n_in = nets.input_size(layers)
+    fp = w["fp"]
 
     def run(nimg):
-        x = np.ascontiguousarray(x_full[:, :, : nimg * n_in])
+        x = np.ascontiguousarray(x_full[..., : nimg * n_in])
         t0 = time.perf_counter()
-        netref.forward(layers, params, x, nimg, FP)
+        if w["kind"] == "infer3":
+            netref.forward(layers, params, x, nimg, fp)
+        elif w["kind"] == "train3":
+            lab = np.ascontiguousarray(wl["labels"][..., : nimg * 10])
+            netref.train_step(layers, params, x, lab, nimg, fp, w["log_lr"])
+        else:
+            mm = orc.tpc_matmul if w["parties"] == 2 else orc.fpc_matmul
+            relu = orc.tpc_relu if w["parties"] == 2 else orc.fpc_relu
+            cur = x
+            for L, prm in zip(layers, params):
+                if L[0] == "fc":
+                    cur = mm(cur, prm[0], nimg, L[2], L[1], 1, 1, 1, fp)
+                    cur = (cur.reshape(cur.shape[:-1] + (nimg, L[2])) + prm[1][..., None, :]).reshape(
+                        cur.shape).astype(cur.dtype)
+                else:
+                    cur, _ = relu(cur)
         return time.perf_counter() - t0
 
-    t1 = run(1)
-    imgs, secs = 1, t1
+    first = 2 if w["kind"] == "train3" else 1  # a training sample needs the batch division
+    t1 = run(first)
+    runs, secs = [first], t1
     if t1 < budget_s / 2:
-        n = max(1, min(batch_full, int((budget_s - t1) / max(t1, 1e-3))))
+        n = max(first, min(batch_full, int(first * (budget_s - t1) / max(t1, 1e-3))))
         secs += run(n)
-        imgs += n
+        runs.append(n)
+    imgs = sum(runs)
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return {"value": imgs / secs, "unit": "img/s", "cores": cores, "kind": "port",
-            "sample": f"{imgs} of the {batch_full} images of the batch ({secs:.1f} s), same weights and shares"}
+            "sample": f"runs of {' and '.join(map(str, runs))} images from the {batch_full}-image batch "
+                      f"({secs:.1f} s), same weights and shares"}
 
 
 # ------------------------------------------------------------------ GPU arm
+
+def _as_device_block(torch, dev, ptr, n):
+    class _A:
+        __cuda_array_interface__ = {"shape": (n,), "typestr": "<i8", "data": (ptr, False), "version": 3}
+
+    return torch.as_tensor(_A(), device=dev)
+
 
 def run_ours(args, rank, world, local_rank):
     import torch
@@ -167,15 +246,20 @@ def run_ours(args, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     stream = torch.cuda.Stream(device=dev)
     batch = args.batch
-    layers, params, x = vgg16_workload(batch)
-    macs = conv_ring_macs(layers, batch)
+    wl = make_workload(args.workload, batch)
+    kind = WORKLOADS[args.workload]["kind"]
+
+    if kind == "fcnet":
+        with torch.cuda.stream(stream):
+            return bench_fcnet(args, pg, torch, stream, dev, wl, batch, world), wl
 
     forms = {"u64": [pg.FORM_U64], "tc": [pg.FORM_LIMB_TC], "auto": [pg.FORM_LIMB_TC, pg.FORM_U64]}[args.form]
+    fn = bench_form if kind == "infer3" else bench_train
     result = None
     with torch.cuda.stream(stream):
         for form in forms:
             try:
-                result = bench_form(args, pg, torch, stream, dev, form, layers, params, x, macs, batch, world)
+                result = fn(args, pg, torch, stream, dev, form, wl, batch, world)
                 break
             except pg.PiranhaError as e:
                 if form == forms[-1]:
@@ -183,108 +267,120 @@ def run_ours(args, rank, world, local_rank):
                 print(f"[bench] form {form} unavailable: {e}", file=sys.stderr)
         if result and result["form"] == "limb_tc" and not args.no_compare:
             # the same workload on the plain 64-bit integer CUDA-core form, for the limb/u64 ratio
-            u = bench_form(args, pg, torch, stream, dev, pg.FORM_U64, layers, params, x, macs, batch, world)
+            u = fn(args, pg, torch, stream, dev, pg.FORM_U64, wl, batch, world)
             result["compare_u64"] = {"value": u["value"], "ms_per_step": u["ms_per_step"],
-                                     "conv_tflops_equiv": u["roofline"]["achieved"],
+                                     "gemm_tflops_equiv": u["roofline"]["achieved"],
                                      "limb_over_u64": result["value"] / u["value"]}
-    return result, (layers, params, x)
+    return result, wl
 
 
-def bench_form(args, pg, torch, stream, dev, form, layers, params, x, macs, batch, world):
-    ctx = pg.Context(dev.index, stream=stream, form=form)
-    net = pg.Network(ctx, layers, batch, FP)
-    for i, prm in enumerate(params):
+def _setup_net(pg, ctx, dev, wl, batch, fp):
+    net = pg.Network(ctx, wl["layers"], batch, fp)
+    for i, prm in enumerate(wl["params"]):
         if prm is not None:
             net.set_params(i, pg.to_device(prm[0], dev), pg.to_device(prm[1], dev) if prm[1] is not None else None)
-    net.enable_timing(True)
-    net.capture()
-    # inputs resident in HBM: the network's own input buffers
-    ptr0 = net.input_buffers()[0]
-    xin = pg.to_device(x, dev).reshape(-1)
+    return net
 
-    class _A:
-        __cuda_array_interface__ = {"shape": (6 * net.in_n,), "typestr": "<i8", "data": (ptr0, False), "version": 3}
 
-    torch.as_tensor(_A(), device=dev).copy_(xin)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    stream.synchronize()
-
-    for _ in range(args.warmup):
-        net.forward_resident()
-    stream.synchronize()
-
-    # ------------------------------------------------------------ timed
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    layer_ms = np.zeros(len(layers))
+def _timed(args, torch, stream, dev, world, step, flush, per_step=None):
+    """K timed steps with an L2 flush before each (outside the event pair)."""
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     sampler = ClockSampler(dev.index)
     sampler.start()
-    launches0 = ctx.kernel_launches()
-    comm0 = ctx.comm()
     wall0 = time.perf_counter()
     step_ms = []
     for k in range(args.steps):
-        flush.fill_(k & 0xFF)  # L2 flush, outside the event pair
-        ev[k][0].record(stream)
-        net.forward_resident()
-        ev[k][1].record(stream)
+        flush.fill_(k & 0xFF)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
         stream.synchronize()
-        step_ms.append(ev[k][0].elapsed_time(ev[k][1]))
-        layer_ms += np.array(net.layer_times_ms())
+        step_ms.append(e0.elapsed_time(e1))
+        if per_step:
+            per_step()
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     if world > 1:
         torch.distributed.barrier()
     clocks = sampler.stop()
-    launches = ctx.kernel_launches() - launches0
-    comm1 = ctx.comm()
-
     dev_s = sum(step_ms) / 1e3
     if world > 1:
         t = torch.tensor([dev_s, wall], device=dev, dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         dev_s, wall = float(t[0]), float(t[1])
-    value = world * batch * args.steps / dev_s
+    return dev_s, wall, clocks
 
-    # dominant kernel: the fused share-GEMM of the conv layers
-    conv_idx = sorted(macs)
-    conv_ms = float(sum(layer_ms[i] for i in conv_idx)) / args.steps
-    conv_macs = sum(macs.values())
-    achieved = conv_macs * LIMB_FLOPS_PER_RING_MAC / (conv_ms / 1e3) / 1e12
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except OSError:
-        pass
-    peak = peaks.get("bf16_tflops", 1900.0)
-    peak_note = "of measured" if "bf16_tflops" in peaks else "of fallback"
 
-    # -------------------------------------------------------------- e2e
-    in_host = torch.empty(6 * net.in_n, dtype=torch.int64, pin_memory=True)
-    in_host.copy_(xin.cpu())
-    out_host = torch.empty(6 * net.out_n, dtype=torch.int64, pin_memory=True)
+def _e2e(args, torch, stream, dev, world, step, flush):
     for _ in range(max(1, args.warmup)):
-        net.forward_host(in_host.data_ptr(), out_host.data_ptr())
+        step()
     stream.synchronize()
-    e2e_ms = []
+    ms = []
     for k in range(args.steps):
         flush.fill_(k & 0xFF)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        net.forward_host(in_host.data_ptr(), out_host.data_ptr())
+        step()
         e1.record(stream)
         stream.synchronize()
-        e2e_ms.append(e0.elapsed_time(e1))
-    e2e_s = sum(e2e_ms) / 1e3
+        ms.append(e0.elapsed_time(e1))
+    s = sum(ms) / 1e3
     if world > 1:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        t = torch.tensor([s], device=dev, dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t[0])
+        s = float(t[0])
+    return s
 
-    per_fwd_tx = (comm1["tx"][0] - comm0["tx"][0]) // args.steps
-    per_fwd_rounds = (comm1["rounds"] - comm0["rounds"]) // args.steps
+
+def bench_form(args, pg, torch, stream, dev, form, wl, batch, world):
+    """Secure inference through the network executor (one CUDA graph per forward)."""
+    fp = WORKLOADS[args.workload]["fp"]
+    layers = wl["layers"]
+    macs = ring_macs(layers, batch)
+    ctx = pg.Context(dev.index, stream=stream, form=form)
+    net = _setup_net(pg, ctx, dev, wl, batch, fp)
+    net.enable_timing(True)
+    net.capture()
+    xin = pg.to_device(wl["x"], dev).reshape(-1)
+    _as_device_block(torch, dev, net.input_buffers()[0], 6 * net.in_n).copy_(xin)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream.synchronize()
+    for _ in range(args.warmup):
+        net.forward_resident()
+    stream.synchronize()
+
+    layer_ms = np.zeros(len(layers))
+
+    def acc_layers():
+        layer_ms[:] += np.array(net.layer_times_ms())
+
+    launches0 = ctx.kernel_launches()
+    comm0 = ctx.comm()
+    dev_s, wall, clocks = _timed(args, torch, stream, dev, world, net.forward_resident, flush, acc_layers)
+    launches = ctx.kernel_launches() - launches0
+    comm1 = ctx.comm()
+    value = world * batch * args.steps / dev_s
+
+    # dominant kernel: the fused share-GEMM of the conv layers (FC layers when there are none)
+    gemm_idx = sorted(i for i in macs if layers[i][0] == "cnn") or sorted(macs)
+    gemm_ms = float(sum(layer_ms[i] for i in gemm_idx)) / args.steps
+    gemm_macs = sum(macs[i] for i in gemm_idx)
+    achieved = gemm_macs * LIMB_FLOPS_PER_RING_MAC / (gemm_ms / 1e3) / 1e12
+    peaks = load_peaks()
+    peak = peaks.get("bf16_tflops", 1900.0)
+    peak_note = "of measured" if "bf16_tflops" in peaks else "of fallback"
+    what = (f"share-GEMM implicit conv (all {len(gemm_idx)} convs)" if layers[gemm_idx[0]][0] == "cnn"
+            else f"share-GEMM FC layers ({len(gemm_idx)})")
+
+    in_host = torch.empty(6 * net.in_n, dtype=torch.int64, pin_memory=True)
+    in_host.copy_(xin.cpu())
+    out_host = torch.empty(6 * net.out_n, dtype=torch.int64, pin_memory=True)
+    e2e_s = _e2e(args, torch, stream, dev, world, lambda: net.forward_host(in_host.data_ptr(), out_host.data_ptr()),
+                 flush)
+
     out = {
         "form": "limb_tc" if form == pg.FORM_LIMB_TC else "u64",
         "value": value,
@@ -295,14 +391,147 @@ def bench_form(args, pg, torch, stream, dev, form, layers, params, x, macs, batc
         "gpu_launches": int(launches),
         "clocks": clocks,
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "kernel": "share-GEMM implicit conv (all 13 VGG16 convs)",
-                     "work": f"{LIMB_FLOPS_PER_RING_MAC} limb-tensor flops per ring MAC, {conv_macs:.4g} ring MACs/forward",
+                     "frac": achieved / peak, "traffic": None, "kernel": what,
+                     "work": f"{LIMB_FLOPS_PER_RING_MAC} limb-tensor flops per ring MAC, {gemm_macs:.4g} ring MACs/forward",
                      "peak_source": f"bf16_tflops {peak_note}"},
-        "comm_per_party_per_forward": {"tx_bytes": int(per_fwd_tx), "rounds": int(per_fwd_rounds)},
+        "comm_per_party_per_step": {"tx_bytes": int((comm1["tx"][0] - comm0["tx"][0]) // args.steps),
+                                    "rounds": int((comm1["rounds"] - comm0["rounds"]) // args.steps)},
         "layer_ms": [round(float(v) / args.steps, 4) for v in layer_ms],
     }
     net.close()
+    ctx.close()
+    return out
+
+
+def bench_train(args, pg, torch, stream, dev, form, wl, batch, world):
+    """One SGD iteration (forward + revealed-softmax backward + updates) per step, one CUDA graph."""
+    w = WORKLOADS[args.workload]
+    fp, lr = w["fp"], w["log_lr"]
+    layers = wl["layers"]
+    macs = ring_macs(layers, batch)
+    ctx = pg.Context(dev.index, stream=stream, form=form)
+    net = _setup_net(pg, ctx, dev, wl, batch, fp)
+    xin = pg.to_device(wl["x"], dev).reshape(-1)
+    lin = pg.to_device(wl["labels"], dev).reshape(-1)
+    _as_device_block(torch, dev, net.input_buffers()[0], 6 * net.in_n).copy_(xin)
+    _as_device_block(torch, dev, net.label_buffers()[0], 6 * net.out_n).copy_(lin)
+    stream.synchronize()
+    net.capture_train(lr)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        net.train_resident()
+    stream.synchronize()
+    launches0 = ctx.kernel_launches()
+    comm0 = ctx.comm()
+    dev_s, wall, clocks = _timed(args, torch, stream, dev, world, net.train_resident, flush)
+    launches = ctx.kernel_launches() - launches0
+    comm1 = ctx.comm()
+    value = world * batch * args.steps / dev_s
+    # forward share-GEMMs plus the backward's two per layer (input gradient, weight gradient)
+    total_macs = 3 * sum(macs.values())
+    achieved = total_macs * LIMB_FLOPS_PER_RING_MAC / (dev_s / args.steps) / 1e12
+    peaks = load_peaks()
+    peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops", 1700.0))
+    peak_note = "of measured" if peaks else "of fallback"
+
+    in_host = torch.empty(6 * net.in_n, dtype=torch.int64, pin_memory=True)
+    in_host.copy_(xin.cpu())
+    lab_host = torch.empty(6 * net.out_n, dtype=torch.int64, pin_memory=True)
+    lab_host.copy_(lin.cpu())
+    out_host = torch.empty(6 * net.out_n, dtype=torch.int64, pin_memory=True)
+    e2e_s = _e2e(args, torch, stream, dev, world,
+                 lambda: net.train_host(in_host.data_ptr(), lab_host.data_ptr(), out_host.data_ptr(), lr), flush)
+    out = {
+        "form": "limb_tc" if form == pg.FORM_LIMB_TC else "u64",
+        "value": value,
+        "ms_per_step": 1e3 * dev_s / args.steps,
+        "wall_s": wall,
+        "e2e": {"value": world * batch * args.steps / e2e_s, "unit": "img/s",
+                "h2d_bytes_per_step": 6 * (net.in_n + net.out_n) * 8, "d2h_bytes_per_step": 6 * net.out_n * 8},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "whole training step (share-GEMMs of forward, input and weight gradients)",
+                     "work": f"{LIMB_FLOPS_PER_RING_MAC} limb-tensor flops per ring MAC, {total_macs:.4g} ring MACs/step; "
+                             "time includes every non-GEMM launch, so frac is a lower bound",
+                     "peak_source": f"bf16_tflops_sustained {peak_note}"},
+        "comm_per_party_per_step": {"tx_bytes": int((comm1["tx"][0] - comm0["tx"][0]) // args.steps),
+                                    "rounds": int((comm1["rounds"] - comm0["rounds"]) // args.steps)},
+    }
+    net.close()
+    ctx.close()
+    return out
+
+
+def bench_fcnet(args, pg, torch, stream, dev, wl, batch, world):
+    """2PC / 4PC FC net: FCLayer::forward + ReLU per layer through the TPC / FPC entry points (eager launches)."""
+    w = WORKLOADS[args.workload]
+    fp, ring = w["fp"], w["ring"]
+    proto = pg.tpc if w["parties"] == 2 else pg.fpc
+    layers = wl["layers"]
+    ctx = pg.Context(dev.index, stream=stream)
+    tdt = torch.int32 if ring == "u32" else torch.int64
+
+    def dev_t(a):
+        return torch.from_numpy(np.ascontiguousarray(a).view(np.int32 if ring == "u32" else np.int64)).to(dev)
+
+    x = dev_t(wl["x"])
+    prm = [None if p is None else (dev_t(p[0]), dev_t(p[1])) for p in wl["params"]]
+    bufs = []
+    for L in layers:
+        n = batch * (L[2] if L[0] == "fc" else L[1])
+        bufs.append((proto.empty(n, ring, dev), proto.zeros(n, "u8", dev) if L[0] == "relu" else None))
+
+    def forward(inp):
+        cur = inp
+        for L, p, (o, d) in zip(layers, prm, bufs):
+            if L[0] == "fc":
+                proto.fc_forward(ctx, cur, p[0], p[1], o, batch, L[1], L[2], fp)
+            else:
+                proto.ReLU(ctx, cur, o, d)
+            cur = o
+        return cur
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        forward(x)
+    stream.synchronize()
+    launches0 = ctx.kernel_launches()
+    comm0 = ctx.comm(w["parties"])
+    dev_s, wall, clocks = _timed(args, torch, stream, dev, world, lambda: forward(x), flush)
+    launches = ctx.kernel_launches() - launches0
+    comm1 = ctx.comm(w["parties"])
+    value = world * batch * args.steps / dev_s
+    macs = sum(batch * L[1] * L[2] for L in layers if L[0] == "fc")
+
+    x_host = torch.empty(x.shape, dtype=tdt, pin_memory=True)
+    x_host.copy_(x.cpu())
+    y_host = torch.empty(bufs[-1][0].shape, dtype=tdt, pin_memory=True)
+
+    def e2e_step():
+        xd = x_host.to(dev, non_blocking=True)
+        y = forward(xd)
+        y_host.copy_(y, non_blocking=True)
+
+    e2e_s = _e2e(args, torch, stream, dev, world, e2e_step, flush)
+    elt = 4 if ring == "u32" else 8
+    out = {
+        "form": "tpc" if w["parties"] == 2 else "fpc",
+        "value": value,
+        "ms_per_step": 1e3 * dev_s / args.steps,
+        "wall_s": wall,
+        "e2e": {"value": world * batch * args.steps / e2e_s, "unit": "img/s",
+                "h2d_bytes_per_step": int(x.numel()) * elt, "d2h_bytes_per_step": int(bufs[-1][0].numel()) * elt},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "roofline": {"bound": "launch", "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None,
+                     "kernel": "per-layer protocol launches",
+                     "work": f"{macs:.4g} plaintext MACs per forward in {len(layers)} layers: far too little to "
+                             "load the tensor cores or HBM, so the step is launch-bound"},
+        "comm_per_party_per_step": {"tx_bytes": [int((a - b) // args.steps) for a, b in zip(comm1["tx"], comm0["tx"])],
+                                    "rounds": int((comm1["rounds"] - comm0["rounds"]) // args.steps)},
+    }
     ctx.close()
     return out
 
@@ -312,16 +541,18 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    w = WORKLOADS[args.workload]
+    dtype = w["ring"]
 
     if args.impl == "reference":
         if rank != 0:
             return
-        layers, params, x = vgg16_workload(args.batch)
-        cb = cpu_baseline(layers, params, x, args.batch, args.cpu_seconds)
-        line = {"metric": METRIC, "value": cb["value"], "unit": "img/s", "impl": "reference", "n_gpus": args.gpus,
+        wl = make_workload(args.workload, args.batch)
+        cb = cpu_baseline(args.workload, wl, args.batch, args.cpu_seconds)
+        line = {"metric": w["metric"], "value": cb["value"], "unit": "img/s", "impl": "reference", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.batch / cb["value"],
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-                "data": "synthetic", "config": {"workload": WORKLOAD, "global_batch": args.batch,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+                "data": "synthetic", "config": {"workload": w["desc"], "global_batch": args.batch,
                                                 "parallelism": "replicas"},
                 "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "img/s", "h2d_bytes_per_step": 0,
                                             "d2h_bytes_per_step": 0},
@@ -339,19 +570,20 @@ def main():
         return
     cb = None
     if world == 1 and not args.no_cpu_baseline:
-        cb = cpu_baseline(*wl, args.batch, args.cpu_seconds)
+        cb = cpu_baseline(args.workload, wl, args.batch, args.cpu_seconds)
     line = {
-        "metric": METRIC, "value": res["value"], "unit": "img/s", "n_gpus": world, "steps": args.steps,
+        "metric": w["metric"], "value": res["value"], "unit": "img/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "global_batch": args.batch * world, "parallelism": "replicas",
+        "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+        "config": {"workload": w["desc"], "global_batch": args.batch * world, "parallelism": "replicas",
                    "form": res["form"], "l2": "256 MiB write between timed steps",
-                   "graph": "one CUDA graph per forward"},
+                   "graph": "eager launches" if w["kind"] == "fcnet" else "one CUDA graph per step"},
         "e2e": res["e2e"], "gpu_launches": res["gpu_launches"], "clocks": res["clocks"],
         "roofline": res["roofline"], "cpu_baseline": cb,
-        "comm_per_party_per_forward": res["comm_per_party_per_forward"],
-        "layer_ms": res["layer_ms"],
+        "comm_per_party_per_step": res["comm_per_party_per_step"],
     }
+    if "layer_ms" in res:
+        line["layer_ms"] = res["layer_ms"]
     if "compare_u64" in res:
         line["compare_u64_form"] = res["compare_u64"]
     print(json.dumps(line))

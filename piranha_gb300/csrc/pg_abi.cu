@@ -30,23 +30,29 @@ int launch_status(Ctx *c, const char *what) {
 
 int *device_error_word(Ctx *c) { return c->dev_err; }
 
-void *scratch(Ctx *c, size_t bytes) {
-    if (bytes <= c->scratch_bytes) return c->scratch;
-    if (c->scratch) {
+// A grow-only device buffer of the context (grows with cudaMalloc, which a
+// stream capture does not allow: capture after an eager run has sized it).
+static void *grow(Ctx *c, void *&buf, size_t &have, size_t bytes, const char *what) {
+    if (bytes <= have) return buf;
+    if (buf) {
         cudaStreamSynchronize(c->stream);
-        cudaFree(c->scratch);
-        c->scratch = nullptr;
-        c->scratch_bytes = 0;
+        cudaFree(buf);
+        buf = nullptr;
+        have = 0;
     }
     size_t want = bytes + (bytes >> 3);
-    if (cudaMalloc(&c->scratch, want) != cudaSuccess) {
+    if (cudaMalloc(&buf, want) != cudaSuccess) {
         cudaGetLastError();
-        set_error(c, PG_ERR_NO_MEMORY, "scratch allocation of %zu bytes failed", want);
+        buf = nullptr;
+        set_error(c, PG_ERR_NO_MEMORY, "%s allocation of %zu bytes failed", what, want);
         return nullptr;
     }
-    c->scratch_bytes = want;
-    return c->scratch;
+    have = want;
+    return buf;
 }
+
+void *scratch(Ctx *c, size_t bytes) { return grow(c, c->scratch, c->scratch_bytes, bytes, "scratch"); }
+void *gemm_partial(Ctx *c, size_t bytes) { return grow(c, c->partial, c->partial_bytes, bytes, "split-K buffer"); }
 
 // kernels in other translation units
 template <typename T>
@@ -114,6 +120,7 @@ int pg_ctx_destroy(pg_ctx *c) {
     CTX_OR_FAIL(c);
     cudaStreamSynchronize(c->stream);
     if (c->scratch) cudaFree(c->scratch);
+    if (c->partial) cudaFree(c->partial);
     if (c->dev_err) cudaFree(c->dev_err);
     delete c;
     return PG_OK;

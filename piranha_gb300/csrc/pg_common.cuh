@@ -28,6 +28,10 @@ struct Ctx {
     // scratch owned by the context (grown on demand, freed at destroy)
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
+    // split-K partial sums of the CUDA-core ring GEMM (separate from scratch,
+    // which callers of that GEMM may be using for its operands)
+    void *partial = nullptr;
+    size_t partial_bytes = 0;
     int sm_count = 0;
     int *dev_err = nullptr;  // device word that bounded waits set on timeout
 };
@@ -45,6 +49,7 @@ int set_error(Ctx *c, int code, const char *fmt, ...);
 int launch_status(Ctx *c, const char *what);
 
 void *scratch(Ctx *c, size_t bytes);  // nullptr on failure (error set)
+void *gemm_partial(Ctx *c, size_t bytes);  // the split-K buffer; nullptr on failure (error set)
 
 // ---------------------------------------------------------- communication
 

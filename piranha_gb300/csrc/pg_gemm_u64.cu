@@ -55,6 +55,11 @@ template <typename T> struct GemmArgs {
     T d;
     int dshift;
     int x0;  // EPI_FPC: the output share that holds component x0 (-1: none)
+    // split-K: CTA z runs k-steps [z * steps_per_split, (z + 1) * steps_per_split) of the
+    // concatenated (segment, k) range and adds its sums into partial (mod 2^w, exact);
+    // ring_epilogue_kernel then applies the epilogue. partial == nullptr: no split.
+    T *partial;
+    int steps_per_split;
 };
 
 constexpr int BM = 128, BN = 64, BK = 16, NT = 256, TM = 8, TN = 4;
@@ -124,6 +129,40 @@ template <typename T, int KIND> struct Loader {
     static constexpr bool b_kfast = (KIND == K_FPROP);
 };
 
+template <int KIND, typename T> __device__ __forceinline__ size_t out_index(const GemmArgs<T> &g, int m, int n) {
+    return (KIND == K_GEMM && !g.tC) ? (size_t)m + (size_t)n * g.M : (size_t)m * g.N + n;
+}
+
+__device__ __forceinline__ void atomic_add_ring(uint64_t *p, uint64_t v) {
+    atomicAdd((unsigned long long *)p, (unsigned long long)v);
+}
+__device__ __forceinline__ void atomic_add_ring(uint32_t *p, uint32_t v) { atomicAdd((unsigned int *)p, v); }
+
+// Output of one ring element z of the contraction at output index idx, column n.
+template <typename T> __device__ __forceinline__ void apply_epilogue(const GemmArgs<T> &g, size_t idx, int n, T z) {
+    if (g.epi == EPI_RAW) {
+        g.c_raw[idx] = z;
+    } else if (g.epi == EPI_FPC) {
+        // FPC dividePublic at one party: its reveal minus d, divided, plus r = 1 in x0
+        T v = (T)(1 + div_public<T>((T)(z - g.d), g.d, g.dshift));
+#pragma unroll
+        for (int ps = 0; ps < 3; ps++) {
+            T base = ps == g.x0 ? v : (T)0;
+            if (g.bias[ps]) base = (T)(base + g.bias[ps][n]);
+            g.out[ps][idx] = base;
+        }
+    } else {
+        // dividePublic3out3: reveal sum_p z_p - d, divide, r = 1 at A.shareA / C.shareB
+        T v = (T)(1 + div_public<T>((T)(z - g.d), g.d, g.dshift));
+#pragma unroll
+        for (int ps = 0; ps < 6; ps++) {
+            T base = (ps == 0 || ps == 5) ? v : (T)0;
+            if (g.bias[ps]) base = (T)(base + g.bias[ps][n]);
+            g.out[ps][idx] = base;
+        }
+    }
+}
+
 template <typename T, int KIND>
 __global__ void __launch_bounds__(NT) ring_gemm_kernel(const GemmArgs<T> g) {
     __shared__ T As[2][BK][BM + APAD];
@@ -142,9 +181,13 @@ __global__ void __launch_bounds__(NT) ring_gemm_kernel(const GemmArgs<T> g) {
 
     T ra[BM * BK / NT], rb[BN * BK / NT];
     const int ksteps = (g.K + BK - 1) / BK;
-    const int total = ksteps * g.nseg;
+    const int all_steps = ksteps * g.nseg;
+    const int first = g.partial ? (int)blockIdx.z * g.steps_per_split : 0;
+    const int last = g.partial ? min(all_steps, first + g.steps_per_split) : all_steps;
+    const int total = last > first ? last - first : 0;
 
-    auto gload = [&](int step) {
+    auto gload = [&](int local_step) {
+        const int step = first + local_step;
         int seg = step / ksteps, k0 = (step - seg * ksteps) * BK;
         const T *a = g.a[seg];
 #pragma unroll
@@ -209,30 +252,20 @@ __global__ void __launch_bounds__(NT) ring_gemm_kernel(const GemmArgs<T> g) {
         for (int j = 0; j < TN; j++) {
             int n = n0 + tn * TN + j;
             if (n >= g.N) continue;
-            size_t idx = (KIND == K_GEMM && !g.tC) ? (size_t)m + (size_t)n * g.M : (size_t)m * g.N + n;
-            T z = acc[i][j];
-            if (g.epi == EPI_RAW) {
-                g.c_raw[idx] = z;
-            } else if (g.epi == EPI_FPC) {
-                // FPC dividePublic at one party: its reveal minus d, divided, plus r = 1 in x0
-                T v = (T)(1 + div_public<T>((T)(z - g.d), g.d, g.dshift));
-#pragma unroll
-                for (int ps = 0; ps < 3; ps++) {
-                    T base = ps == g.x0 ? v : (T)0;
-                    if (g.bias[ps]) base = (T)(base + g.bias[ps][n]);
-                    g.out[ps][idx] = base;
-                }
-            } else {
-                // dividePublic3out3: reveal sum_p z_p - d, divide, r = 1 at A.shareA / C.shareB
-                T v = (T)(1 + div_public<T>((T)(z - g.d), g.d, g.dshift));
-#pragma unroll
-                for (int ps = 0; ps < 6; ps++) {
-                    T base = (ps == 0 || ps == 5) ? v : (T)0;
-                    if (g.bias[ps]) base = (T)(base + g.bias[ps][n]);
-                    g.out[ps][idx] = base;
-                }
-            }
+            const size_t idx = out_index<KIND>(g, m, n);
+            if (g.partial) atomic_add_ring(&g.partial[idx], acc[i][j]);
+            else apply_epilogue(g, idx, n, acc[i][j]);
         }
+    }
+}
+
+// The epilogue of split-K GEMMs, after all splits have added into partial.
+template <typename T, int KIND> __global__ void ring_epilogue_kernel(const GemmArgs<T> g) {
+    const size_t mn = (size_t)g.M * g.N;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < mn; e += (size_t)gridDim.x * blockDim.x) {
+        const int m = (int)(e / g.N), n = (int)(e - (size_t)m * g.N);
+        const size_t idx = out_index<KIND>(g, m, n);
+        apply_epilogue(g, idx, n, g.partial[idx]);
     }
 }
 
@@ -248,17 +281,50 @@ template <typename T> static void setup_conv(GemmArgs<T> &g, int op, int N, int 
     else { g.M = K; g.N = R * S * C; g.K = N * P * Q; }
 }
 
+template <typename T, int KIND> static void launch_kind(Ctx *c, dim3 grid, const GemmArgs<T> &g) {
+    ring_gemm_kernel<T, KIND><<<grid, NT, 0, c->stream>>>(g);
+    if (g.partial) {
+        const size_t mn = (size_t)g.M * g.N;
+        const int sms = c->sm_count > 0 ? c->sm_count : 148;
+        size_t blocks = (mn + 255) / 256;
+        if (blocks > (size_t)sms * 8) blocks = (size_t)sms * 8;
+        ring_epilogue_kernel<T, KIND><<<(unsigned)blocks, 256, 0, c->stream>>>(g);
+    }
+}
+
 template <typename T> static int launch_gemm(Ctx *c, GemmArgs<T> &g, int kind) {
     if (g.M <= 0 || g.N <= 0 || g.K < 0) return set_error(c, PG_ERR_SIZE, "ring gemm: bad sizes M=%d N=%d K=%d", g.M, g.N, g.K);
     dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM);
     if (grid.y > 65535) return set_error(c, PG_ERR_UNSUPPORTED, "ring gemm: M=%d too large", g.M);
-    switch (kind) {
-        case K_GEMM: ring_gemm_kernel<T, K_GEMM><<<grid, NT, 0, c->stream>>>(g); break;
-        case K_FPROP: ring_gemm_kernel<T, K_FPROP><<<grid, NT, 0, c->stream>>>(g); break;
-        case K_DGRAD: ring_gemm_kernel<T, K_DGRAD><<<grid, NT, 0, c->stream>>>(g); break;
-        default: ring_gemm_kernel<T, K_WGRAD><<<grid, NT, 0, c->stream>>>(g); break;
+    // Split K when the output tiles cannot fill the GPU (small M x N, long K:
+    // weight gradients, narrow layers): about two CTAs per SM, at least four
+    // k-steps each.
+    const int sms = c->sm_count > 0 ? c->sm_count : 148;
+    const long long tiles = (long long)grid.x * grid.y;
+    const int all_steps = ((g.K + BK - 1) / BK) * g.nseg;
+    g.partial = nullptr;
+    g.steps_per_split = 0;
+    if (tiles < sms && all_steps >= 8) {
+        long long split = (2LL * sms + tiles - 1) / tiles;
+        if (split > all_steps / 4) split = all_steps / 4;
+        if (split > 65535) split = 65535;
+        if (split >= 2) {
+            const int per = (int)((all_steps + split - 1) / split);
+            grid.z = (unsigned)((all_steps + per - 1) / per);
+            const size_t bytes = (size_t)g.M * g.N * sizeof(T);
+            g.partial = (T *)gemm_partial(c, bytes);
+            if (!g.partial) return PG_ERR_NO_MEMORY;
+            g.steps_per_split = per;
+            PG_CHECK_CUDA(c, cudaMemsetAsync(g.partial, 0, bytes, c->stream));
+        }
     }
-    c->launches++;
+    switch (kind) {
+        case K_GEMM: launch_kind<T, K_GEMM>(c, grid, g); break;
+        case K_FPROP: launch_kind<T, K_FPROP>(c, grid, g); break;
+        case K_DGRAD: launch_kind<T, K_DGRAD>(c, grid, g); break;
+        default: launch_kind<T, K_WGRAD>(c, grid, g); break;
+    }
+    c->launches += g.partial ? 2 : 1;
     return launch_status(c, "ring_gemm_kernel");
 }
 

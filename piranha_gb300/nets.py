@@ -1,0 +1,72 @@
+"""The reference's model configurations (files/models/*.json) as layer
+tuples for ``piranha_gb300.Network``, and seeded synthetic parameters.
+
+Layer tuples: ("fc", din, dout), ("cnn", H, W, Din, Dout, f, stride, pad),
+("relu", n_per_image), ("maxpool", H, W, C, pool, stride).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import encode as _enc
+
+
+def secureml():
+    """files/models/secureml.json: 784-128-128-10 with ReLU after every FC."""
+    return [("fc", 784, 128), ("relu", 128), ("fc", 128, 128), ("relu", 128), ("fc", 128, 10), ("relu", 10)]
+
+
+def lenet():
+    """files/models/lenet.json (maxpool variant)."""
+    return [("cnn", 28, 28, 1, 20, 5, 1, 0), ("maxpool", 24, 24, 20, 2, 2), ("relu", 2880),
+            ("cnn", 12, 12, 20, 50, 5, 1, 0), ("maxpool", 8, 8, 50, 2, 2), ("relu", 800),
+            ("fc", 800, 500), ("relu", 500), ("fc", 500, 10), ("relu", 10)]
+
+
+def vgg16(maxpool: bool = True):
+    """files/models/vgg16-cifar10.json with each averagepool replaced by a 2x2/2 maxpool."""
+    if not maxpool:
+        raise ValueError("only the maxpool variant is built")
+    L = []
+    hw, c = 32, 3
+    for width, reps in [(64, 2), (128, 2), (256, 3), (512, 3), (512, 3)]:
+        for r in range(reps):
+            L.append(("cnn", hw, hw, c, width, 3, 1, 1))
+            c = width
+            if r < reps - 1:
+                L.append(("relu", hw * hw * c))
+        L.append(("maxpool", hw, hw, c, 2, 2))
+        hw //= 2
+        L.append(("relu", hw * hw * c))
+    L += [("fc", 512, 256), ("relu", 256), ("fc", 256, 256), ("relu", 256), ("fc", 256, 10), ("relu", 10)]
+    return L
+
+
+def input_size(layers):
+    L = layers[0]
+    if L[0] == "fc":
+        return L[1]
+    if L[0] == "cnn":
+        return L[1] * L[2] * L[3]
+    if L[0] == "relu":
+        return L[1]
+    return L[1] * L[2] * L[3]
+
+
+def kaiming_uniform(layers, seed: int, fp: int = 26, ring: str = "u64"):
+    """Seeded Kaiming-uniform weights (bound sqrt(6 / fan_in)), FC bias 0.01,
+    loaded with setPublic; None for layers without parameters."""
+    rng = np.random.default_rng(seed)
+    params = []
+    for L in layers:
+        if L[0] == "fc":
+            din, dout = L[1], L[2]
+            w = rng.uniform(-1, 1, din * dout) * np.sqrt(6.0 / din)
+            params.append((_enc.set_public(w, ring, fp), _enc.set_public(np.full(dout, 0.01), ring, fp)))
+        elif L[0] == "cnn":
+            Din, Dout, f = L[3], L[4], L[5]
+            w = rng.uniform(-1, 1, Dout * f * f * Din) * np.sqrt(6.0 / (f * f * Din))
+            params.append((_enc.set_public(w, ring, fp), None))
+        else:
+            params.append(None)
+    return params
