@@ -22,6 +22,7 @@ Other workloads (--workload), each printing the same JSON line for its own metri
   lenet-train   3PC LeNet training step (forward + backward + SGD, log learning rate 5), batch 128
   secureml-2pc  2PC SecureML inference, batch 128, uint32 shares, FP 10
   secureml-4pc  4PC SecureML inference, batch 128, uint32 shares, FP 10
+  stream        512 requests of batch 1..64, SecureML or VGG16, served in order; p50/p99 latency
 
 With --impl reference the line times Piranha's own arithmetic restated on the
 CPU (the oracle; the reference's GPU build cannot be compiled here) on a
@@ -49,6 +50,10 @@ from piranha_gb300 import nets  # noqa: E402
 BATCH = 128
 SEED = 2024
 LIMB_FLOPS_PER_RING_MAC = 72  # 36 8-bit limb pairs x 2 flops: exact u64 MAC on fp16 tensor cores
+# DRAM bytes read + written by the 13 limb_tma_kernel launches of one VGG16
+# batch-128 forward, from the ncu capture summarised in
+# profiles/limb_tma_kernel_vgg16_b128_dram.md (the command is given there)
+VGG16_B128_LIMB_TRAFFIC = 5_565_221_120
 
 WORKLOADS = {
     "vgg16": {"metric": "3PC VGG16 secure inference img/s", "kind": "infer3", "fp": 26, "ring": "u64",
@@ -65,9 +70,13 @@ WORKLOADS = {
     "secureml-4pc": {"metric": "4PC SecureML secure inference img/s", "kind": "fcnet", "parties": 4, "fp": 10,
                      "ring": "u32",
                      "desc": "secureml 784-128-128-10, 4PC (FPC), batch 128, uint32 shares, FP 10"},
+    "stream": {"metric": "3PC batched request stream img/s", "kind": "stream", "fp": 26, "ring": "u64",
+               "requests": 512, "max_batch": 64,
+               "desc": "512 requests, batch uniform in 1..64, SecureML or VGG16 (even odds), 3PC RSS, uint64 "
+                       "shares, FP 26; each request runs on a captured network of the next power-of-two batch"},
 }
 _LAYERS = {"vgg16": nets.vgg16, "secureml": nets.secureml, "lenet-train": nets.lenet,
-           "secureml-2pc": nets.secureml, "secureml-4pc": nets.secureml}
+           "secureml-2pc": nets.secureml, "secureml-4pc": nets.secureml, "stream": nets.vgg16}
 
 
 def parse():
@@ -113,6 +122,21 @@ def make_workload(name, batch, seed=SEED):
         classes = np.random.default_rng(seed + 3).integers(0, 10, batch)
         labels = enc.set_public(enc.one_hot(classes, 10), ring, fp)
     return {"layers": layers, "params": params, "x": x, "labels": labels}
+
+
+def make_stream(seed=SEED):
+    """Seeded requests: (model, batch, input shares); one parameter set per model."""
+    w = WORKLOADS["stream"]
+    rng = np.random.default_rng(seed + 7)
+    models = {"secureml": nets.secureml(), "vgg16": nets.vgg16()}
+    params = {m: nets.kaiming_uniform(L, seed, w["fp"]) for m, L in models.items()}
+    reqs = []
+    for r in range(w["requests"]):
+        m = "secureml" if rng.integers(0, 2) == 0 else "vgg16"
+        b = int(rng.integers(1, w["max_batch"] + 1))
+        vals = rng.uniform(0, 1, b * nets.input_size(models[m]))
+        reqs.append((m, b, enc.share_random(enc.encode(vals, "u64", w["fp"]), "u64", seed=seed + 100 + r)))
+    return models, params, reqs
 
 
 def ring_macs(layers, batch):
@@ -182,12 +206,40 @@ class ClockSampler:
 
 # ------------------------------------------------------------ CPU baseline
 
+def cpu_baseline_stream(wl, budget_s):
+    """The oracle's time per image of each model (SecureML on its first
+    request, VGG16 on one image of its first), applied to the stream's mix."""
+    import oracle as orc
+    from tests import netref
+
+    orc.lib()
+    models, params, reqs = wl
+    fp = WORKLOADS["stream"]["fp"]
+    per_img = {}
+    for m in models:
+        _, b, x = next(r for r in reqs if r[0] == m)
+        nimg = b if m == "secureml" else 1
+        n_in = nets.input_size(models[m])
+        t0 = time.perf_counter()
+        netref.forward(models[m], params[m], np.ascontiguousarray(x[..., : nimg * n_in]), nimg, fp)
+        per_img[m] = (time.perf_counter() - t0) / nimg
+    imgs = sum(b for _, b, _ in reqs)
+    est = sum(b * per_img[m] for m, b, _ in reqs)
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": imgs / est, "unit": "img/s", "cores": cores, "kind": "port",
+            "sample": "seconds per image measured on " +
+                      ", ".join(f"{m} ({v:.3g} s/img)" for m, v in per_img.items()) +
+                      f", applied to the stream's {imgs} images"}
+
+
 def cpu_baseline(name, wl, batch_full, budget_s):
     """Piranha's arithmetic restated on the CPU (the oracle), timed on a sample of the batch."""
     import oracle as orc
     from tests import netref
 
     orc.lib()
+    if name == "stream":
+        return cpu_baseline_stream(wl, budget_s)
     w = WORKLOADS[name]
     layers, params, x_full = wl["layers"], wl["params"], wl["x"]
     n_in = nets.input_size(layers)
@@ -246,8 +298,12 @@ def run_ours(args, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     stream = torch.cuda.Stream(device=dev)
     batch = args.batch
-    wl = make_workload(args.workload, batch)
     kind = WORKLOADS[args.workload]["kind"]
+    if kind == "stream":
+        wl = make_stream()
+        with torch.cuda.stream(stream):
+            return bench_stream(args, pg, torch, stream, dev, wl, world), wl
+    wl = make_workload(args.workload, batch)
 
     if kind == "fcnet":
         with torch.cuda.stream(stream):
@@ -381,6 +437,9 @@ def bench_form(args, pg, torch, stream, dev, form, wl, batch, world):
     e2e_s = _e2e(args, torch, stream, dev, world, lambda: net.forward_host(in_host.data_ptr(), out_host.data_ptr()),
                  flush)
 
+    traffic = None
+    if args.workload == "vgg16" and batch == BATCH and form == pg.FORM_LIMB_TC:
+        traffic = VGG16_B128_LIMB_TRAFFIC
     out = {
         "form": "limb_tc" if form == pg.FORM_LIMB_TC else "u64",
         "value": value,
@@ -391,7 +450,9 @@ def bench_form(args, pg, torch, stream, dev, form, wl, batch, world):
         "gpu_launches": int(launches),
         "clocks": clocks,
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None, "kernel": what,
+                     "frac": achieved / peak, "traffic": traffic,
+                     "traffic_unit": "DRAM bytes per forward over the conv launches (ncu)" if traffic else None,
+                     "kernel": what,
                      "work": f"{LIMB_FLOPS_PER_RING_MAC} limb-tensor flops per ring MAC, {gemm_macs:.4g} ring MACs/forward",
                      "peak_source": f"bf16_tflops {peak_note}"},
         "comm_per_party_per_step": {"tx_bytes": int((comm1["tx"][0] - comm0["tx"][0]) // args.steps),
@@ -536,6 +597,111 @@ def bench_fcnet(args, pg, torch, stream, dev, wl, batch, world):
     return out
 
 
+def bench_stream(args, pg, torch, stream, dev, wl, world):
+    """The request stream, served in arrival order on one stream: per request
+    its shares go into the input buffers of the captured network of the next
+    power-of-two batch (rows past the request's batch keep what an earlier
+    request left there; every layer works image by image, so they do not
+    touch the request's rows), the graph
+    replays, and the request's output rows come back. Latency is a request's
+    CUDA-event time from the start of its input copy to the end of its output
+    copy. The stream runs args.warmup times untimed, then once timed per pass:
+    a device-resident pass (inputs staged in HBM beforehand) and an end-to-end
+    pass (pinned host shares in and out)."""
+    models, params, reqs = wl
+    fp = WORKLOADS["stream"]["fp"]
+    form = pg.FORM_U64 if args.form == "u64" else pg.FORM_LIMB_TC
+    ctx = pg.Context(dev.index, stream=stream, form=form)
+    nets_ = {}
+
+    def bucket(b):
+        p = 1
+        while p < b:
+            p *= 2
+        return p
+
+    for m, b, _ in reqs:
+        key = (m, bucket(b))
+        if key in nets_:
+            continue
+        net = pg.Network(ctx, models[m], key[1], fp)
+        for i, prm in enumerate(params[m]):
+            if prm is not None:
+                net.set_params(i, pg.to_device(prm[0], dev), pg.to_device(prm[1], dev) if prm[1] is not None else None)
+        net.capture()
+        ptr_in = net.input_buffers()[0]
+        optrs, on = net.layer_output_ptrs(len(models[m]) - 1)
+        nets_[key] = (net, _as_device_block(torch, dev, ptr_in, 6 * net.in_n).view(6, net.in_n),
+                      _as_device_block(torch, dev, optrs[0], 6 * on).view(6, on))
+    for net, inb, _ in nets_.values():
+        inb.zero_()
+    stream.synchronize()
+
+    per_img_in = {m: nets.input_size(L) for m, L in models.items()}
+    per_img_out = 10
+    dev_in = [torch.from_numpy(np.ascontiguousarray(x).reshape(6, -1).view(np.int64)).to(dev) for _, _, x in reqs]
+    host_in = [t.cpu().pin_memory() for t in dev_in]
+    host_out = [torch.empty((6, b * per_img_out), dtype=torch.int64, pin_memory=True) for _, b, _ in reqs]
+
+    def serve(resident):
+        lat = []
+        evs = []
+        for r, (m, b, _) in enumerate(reqs):
+            net, inb, outb = nets_[(m, bucket(b))]
+            n_in = b * per_img_in[m]
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            src = dev_in[r] if resident else host_in[r]
+            inb[:, :n_in].copy_(src, non_blocking=True)
+            net.forward_resident()
+            if not resident:
+                host_out[r].copy_(outb[:, :b * per_img_out], non_blocking=True)
+            e1.record(stream)
+            evs.append((e0, e1))
+        stream.synchronize()
+        for e0, e1 in evs:
+            lat.append(e0.elapsed_time(e1))
+        return lat
+
+    for _ in range(max(1, args.warmup)):
+        serve(True)
+    launches0 = ctx.kernel_launches()
+    sampler = ClockSampler(dev.index)
+    sampler.start()
+    wall0 = time.perf_counter()
+    lat_res = serve(True)
+    wall = time.perf_counter() - wall0
+    clocks = sampler.stop()
+    launches = ctx.kernel_launches() - launches0
+    lat_e2e = serve(False)
+    imgs = sum(b for _, b, _ in reqs)
+    dev_s, e2e_s = sum(lat_res) / 1e3, sum(lat_e2e) / 1e3
+    pct = lambda v, q: float(np.percentile(np.array(v), q))  # noqa: E731
+    out = {
+        "form": "limb_tc" if form == pg.FORM_LIMB_TC else "u64",
+        "value": world * imgs / dev_s,
+        "ms_per_step": 1e3 * dev_s / len(reqs),
+        "wall_s": wall,
+        "e2e": {"value": world * imgs / e2e_s, "unit": "img/s",
+                "h2d_bytes_per_step": int(sum(t.numel() * 8 for t in host_in) / len(reqs)),
+                "d2h_bytes_per_step": int(sum(t.numel() * 8 for t in host_out) / len(reqs))},
+        "latency_ms": {"resident": {"p50": pct(lat_res, 50), "p99": pct(lat_res, 99), "max": max(lat_res)},
+                       "e2e": {"p50": pct(lat_e2e, 50), "p99": pct(lat_e2e, 99), "max": max(lat_e2e)}},
+        "requests": len(reqs), "images": imgs,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "roofline": {"bound": "tensor", "achieved": None, "peak": None, "unit": "TFLOP/s", "frac": None,
+                     "traffic": None, "kernel": "see the vgg16 and secureml workloads",
+                     "work": "mixed request sizes; the per-model lines carry the kernel fractions"},
+        "comm_per_party_per_step": None,
+        "networks": sorted(f"{m}@{b}" for m, b in nets_),
+    }
+    for net, _, _ in nets_.values():
+        net.close()
+    ctx.close()
+    return out
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -547,7 +713,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        wl = make_workload(args.workload, args.batch)
+        wl = make_stream() if w["kind"] == "stream" else make_workload(args.workload, args.batch)
         cb = cpu_baseline(args.workload, wl, args.batch, args.cpu_seconds)
         line = {"metric": w["metric"], "value": cb["value"], "unit": "img/s", "impl": "reference", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.batch / cb["value"],
@@ -584,6 +750,9 @@ def main():
     }
     if "layer_ms" in res:
         line["layer_ms"] = res["layer_ms"]
+    for k in ("latency_ms", "requests", "images", "networks"):
+        if k in res:
+            line[k] = res[k]
     if "compare_u64" in res:
         line["compare_u64_form"] = res["compare_u64"]
     print(json.dumps(line))
