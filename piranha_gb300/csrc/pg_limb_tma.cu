@@ -19,8 +19,9 @@
 // image_kernel as an image of digit planes in global memory,
 //   img[seg][plane][C/8][pixel][8]  (fp16),
 // so that for a tile of output pixels and one conv tap, the 16 channels of a
-// K block are one 4-D tensor-map box: (8 channels x Wt pixels, as one
-// contiguous line of 16*Wt bytes) x Ht rows x Nt images x 2 channel groups.
+// K block in all eight digit planes are one 5-D tensor-map box: (8 channels
+// x Wt pixels, as one contiguous line of 16*Wt bytes) x Ht rows x Nt images
+// x 2 channel groups x 8 planes, one copy per stage.
 // A tap is a shift of the box (16 bytes per pixel along the line), and
 // padding is the box running out of bounds. The GEMM case reads lines of 32
 // consecutive image rows instead. B (weights, with
@@ -267,12 +268,13 @@ __global__ void pack_kernel(const __grid_constant__ PackArgs pa) {
 
 // ------------------------------------------------------------- GEMM kernel
 
-__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
-                                            uint32_t bar) {
+// One 5-D box: all eight digit planes of a stage's A tile in one copy.
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            int c4, uint32_t bar) {
     asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
-        "[%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
         : "memory");
 }
 
@@ -285,21 +287,23 @@ __device__ __forceinline__ void flag_error(Smem &sm, const Args &g, int code) {
 // digit plane i < 4 the B planes j = 0..3-i are adjacent in shared memory and
 // their products go to the adjacent accumulators of diagonals i..3, so one
 // MMA with N = 64 (4 - i) covers them. i = 0 writes all four accumulators.
-__device__ __forceinline__ void issue_lo(uint32_t acc, uint64_t adesc, uint64_t bdesc, bool first_stage) {
+__device__ __forceinline__ void issue_lo(uint32_t acc, uint64_t adesc, uint32_t aplane16, uint64_t bdesc,
+                                         bool first_stage) {
 #pragma unroll
     for (int i = 0; i < 4; i++)
-        tc::mma_f16(acc + (uint32_t)(i * BN), adesc + (uint64_t)((i * A_PLANE_BYTES) >> 4), bdesc,
+        tc::mma_f16(acc + (uint32_t)(i * BN), adesc + (uint64_t)(i * aplane16), bdesc,
                     tc::idesc_f16_f32(BM, BN * (4 - i)), (!first_stage || i > 0) ? 1u : 0u);
 }
 
 // The MMAs of one stage for the high diagonals 4-7 (columns 256-511): for A
 // plane i the B planes j = max(0, 4-i)..7-i, one MMA each (8 per stage).
-__device__ __forceinline__ void issue_hi(uint32_t acc, uint64_t adesc, uint64_t bdesc, bool first_stage) {
+__device__ __forceinline__ void issue_hi(uint32_t acc, uint64_t adesc, uint32_t aplane16, uint64_t bdesc,
+                                         bool first_stage) {
 #pragma unroll
     for (int i = 0; i < 8; i++) {
         const int jlo = 4 - i > 0 ? 4 - i : 0;
         const int cnt = 8 - i < 4 ? 8 - i : 4;
-        tc::mma_f16(acc + (uint32_t)((i + jlo) * BN), adesc + (uint64_t)((i * A_PLANE_BYTES) >> 4),
+        tc::mma_f16(acc + (uint32_t)((i + jlo) * BN), adesc + (uint64_t)(i * aplane16),
                     bdesc + (uint64_t)((jlo * B_PLANE_BYTES) >> 4), tc::idesc_f16_f32(BM, BN * cnt),
                     (!first_stage || i > 0) ? 1u : 0u);
     }
@@ -342,38 +346,54 @@ __device__ __forceinline__ int lo_chunks(int nst) {
     return nst <= 0 ? 0 : nst <= LO_FIRST ? 1 : 1 + (nst - LO_FIRST + CHUNK_STAGES_LO - 1) / CHUNK_STAGES_LO;
 }
 
-// 32 columns of one output row: store the slice's partial Z, or apply
-// dividePublic3out3 and write the six output shares (+ bias shares).
-__device__ __forceinline__ void finish32(const Args &g, int z, long long m, int nbase, const uint64_t (&zs)[32]) {
-    const int ncols = g.N - nbase < 32 ? g.N - nbase : 32;
-    if (!g.direct) {
-        uint64_t *dst = g.partial + ((long long)z * g.M + m) * g.N + nbase;
+// The tile's output, staged in shared memory once the accumulators are all
+// drained (the stage ring is free then: every MMA has completed, so every
+// load it read has landed). Each epilogue thread puts its row's 32 values
+// (Z, or 1 + (Z - d) / d for a direct output) into STG[row][col]; then the 256
+// epilogue threads write each output share as whole row segments (a warp
+// stores 32 consecutive columns of one row, or 32 consecutive rows of one
+// column for a column-major GEMM output), adding the bias shares.
+constexpr int STG_PITCH = BN + 1;  // u64 per staged row: two-way bank conflicts at most
+static_assert(BM * STG_PITCH * 8 + BM * 8 <= STAGES * STAGE_BYTES, "the staged tile must fit in the stage ring");
+static_assert(NTHREADS - W_EPI0 * 32 == 256, "eight epilogue warps");
+
+__device__ __forceinline__ void named_bar_epilogue() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+__device__ __forceinline__ void stage_row(const Args &g, uint64_t *stg, long long *mrow, int row, int colh,
+                                          long long m, const uint64_t (&zs)[32]) {
+    if (colh == 0) mrow[row] = m;
 #pragma unroll
-        for (int j = 0; j < 32; j++)
-            if (j < ncols) dst[j] = zs[j];
+    for (int j = 0; j < 32; j++) {
+        const uint64_t v = g.direct ? 1 + div_public<uint64_t>(zs[j] - g.d, g.d, g.dshift) : zs[j];
+        stg[row * STG_PITCH + colh * 32 + j] = v;
+    }
+}
+
+__device__ __forceinline__ void store_tile(const Args &g, int z, const uint64_t *stg, const long long *mrow, int te) {
+    const int nbase = blockIdx.x * BN;
+    const int ncols = g.N - nbase < BN ? g.N - nbase : BN;
+    if (!g.direct) {
+        for (int e = te; e < BM * BN; e += 256) {
+            const int r = e >> 6, c = e & (BN - 1);
+            const long long m = mrow[r];
+            if (m >= 0 && c < ncols) g.partial[((long long)z * g.M + m) * g.N + nbase + c] = stg[r * STG_PITCH + c];
+        }
         return;
     }
-#pragma unroll
-    for (int j8 = 0; j8 < 32; j8 += 8) {
-        uint64_t v[8];
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            v[j] = 1 + div_public<uint64_t>(zs[j8 + j] - g.d, g.d, g.dshift);
-        }
 #pragma unroll 1
-        for (int ps = 0; ps < 6; ps++) {
-            uint64_t *o = g.out[ps];
-            const uint64_t *b = g.bias[ps];
-            const bool val = (ps == 0 || ps == 5);
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                if (j8 + j < ncols) {
-                    const int n = nbase + j8 + j;
-                    uint64_t base = val ? v[j] : 0;
-                    if (b) base += b[n];
-                    o[g.colmajor ? m + (long long)n * g.M : m * g.N + n] = base;
-                }
-            }
+    for (int ps = 0; ps < 6; ps++) {
+        uint64_t *o = g.out[ps];
+        const uint64_t *b = g.bias[ps];
+        const bool val = (ps == 0 || ps == 5);
+        for (int e = te; e < BM * BN; e += 256) {
+            const int r = g.colmajor ? (e & (BM - 1)) : (e >> 6);
+            const int c = g.colmajor ? (e >> 7) : (e & (BN - 1));
+            const long long m = mrow[r];
+            if (m < 0 || c >= ncols) continue;
+            const int n = nbase + c;
+            uint64_t v = val ? stg[r * STG_PITCH + c] : 0;
+            if (b) v += b[n];
+            o[g.colmajor ? m + (long long)n * g.M : m * g.N + n] = v;
         }
     }
 }
@@ -447,8 +467,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 const int x = g.rows_mode ? 0 : 8 * (w0 + sx - g.pad);
                 const int y = g.rows_mode ? n0 >> 5 : h0 + r - g.pad;
                 const int zc = g.rows_mode ? 0 : n0;
-                for (int i = 0; i < 8; i++)
-                    tma_load_4d(dst + i * A_PLANE_BYTES, &tmA, x, y, zc, (seg * 8 + i) * g.C8 + 2 * cb, bar);
+                tma_load_5d(dst, &tmA, x, y, zc, 2 * cb, seg * 8, bar);
                 const uint8_t *src = g.packB + ((size_t)gst * g.ntiles_n + blockIdx.x) * B_STAGE_BYTES;
                 tc::bulk_g2s(dst + 8 * A_PLANE_BYTES, src, B_STAGE_BYTES, bar);
                 issued = git + 1;
@@ -468,6 +487,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const uint32_t s0 = tc::smem_u32(sm.stage[0]);
             const uint64_t adesc0 = tc::smem_desc(s0, g.a_box_bytes / 2, 128);  // K chunks one box half apart
             const uint64_t bdesc0 = tc::smem_desc(s0 + 8 * A_PLANE_BYTES, 128, 256);
+            // digit planes follow each other at one box (the 5-D copy packs them): rows past R of a
+            // plane are the next plane's, and land in output rows the epilogue does not store
+            const uint32_t aplane16 = g.a_box_bytes >> 4;
             // Two cursors over the stage ring, one per accumulator group. A group
             // at a chunk boundary waits for the epilogue to drain it while the
             // other group runs on over the stages already loaded; a stage is
@@ -492,8 +514,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     if (!tc::mbar_try_wait(tc::smem_u32(&sm.full[t % STAGES]), (uint32_t)(t / STAGES) & 1)) continue;
                     tc::tc_fence_after();
                     const uint64_t off = (uint64_t)(((t % STAGES) * STAGE_BYTES) >> 4);
-                    if (gi == 0) issue_lo(tmem, adesc0 + off, bdesc0 + off, t == cstart[0]);
-                    else issue_hi(tmem, adesc0 + off, bdesc0 + off, t == cstart[1]);
+                    if (gi == 0) issue_lo(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart[0]);
+                    else issue_hi(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart[1]);
                     cur[gi] = t + 1;
                     prog = true;
                     if (cur[gi] == cend[gi]) {
@@ -561,17 +583,22 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             tc::mbar_arrive(tc::smem_u32(&sm.acc_empty[gi]));
             done_ch[gi]++;
         }
-        if (!sm.abort && row < g.R) {
+        // output row of this thread's accumulator lane (-1: padding or past the image)
+        long long m = -1;
+        if (row < g.R) {
             const int wh = g.Wt * g.Ht;
             const int nn = row / wh, rem = row - nn * wh;
             const int hh = rem / g.Wt, ww = rem - hh * g.Wt;
             const int n = n0 + nn, h = h0 + hh, w = w0 + ww;
-            if (n < g.Nimg && h < g.P && w < g.Q) {
-                const long long m = ((long long)n * g.P + h) * g.Q + w;
-                const int nbase = blockIdx.x * BN + colh * 32;
-                if (nbase < g.N) finish32(g, z, m, nbase, zs);
-            }
+            if (n < g.Nimg && h < g.P && w < g.Q) m = ((long long)n * g.P + h) * g.Q + w;
         }
+        // every epilogue warp reaches both barriers (the drain loop only ever breaks out)
+        uint64_t *stg = reinterpret_cast<uint64_t *>(sm.stage[0]);
+        long long *mrow = reinterpret_cast<long long *>(stg + BM * STG_PITCH);
+        tc::fence_proxy_async_smem();
+        stage_row(g, stg, mrow, row, colh, sm.abort ? -1 : m, zs);
+        named_bar_epilogue();
+        if (!sm.abort) store_tile(g, z, stg, mrow, threadIdx.x - W_EPI0 * 32);
     }
     tc::tc_fence_before();
     __syncthreads();
@@ -862,21 +889,27 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
     // image dims (innermost first): a line of pixels x 8 channels, rows, images,
     // (segment, plane, channel group of 8)
     alignas(64) CUtensorMap tm;
-    cuuint64_t dims[4];
-    cuuint64_t strides[3];
-    cuuint32_t box[4];
-    const cuuint64_t plane_stride = (cuuint64_t)p.pixels_alloc * 16;
+    cuuint64_t dims[5];
+    cuuint64_t strides[4];
+    cuuint32_t box[5];
+    const cuuint64_t plane_stride = (cuuint64_t)p.pixels_alloc * 16;  // bytes between channel groups
+    const cuuint64_t C8 = (cuuint64_t)(p.C / 8);
     if (p.implicit) {
-        dims[0] = 8 * (cuuint64_t)p.Wimg; dims[1] = p.Himg; dims[2] = p.Nimg; dims[3] = 48 * (cuuint64_t)(p.C / 8);
+        dims[0] = 8 * (cuuint64_t)p.Wimg; dims[1] = p.Himg; dims[2] = p.Nimg;
         strides[0] = (cuuint64_t)p.Wimg * 16; strides[1] = (cuuint64_t)p.Himg * p.Wimg * 16; strides[2] = plane_stride;
-        box[0] = 8 * p.Wt; box[1] = p.Ht; box[2] = p.Nt; box[3] = 2;
+        box[0] = 8 * p.Wt; box[1] = p.Ht; box[2] = p.Nt;
     } else {
-        dims[0] = 256; dims[1] = p.pixels_alloc / 32; dims[2] = 1; dims[3] = 48 * (cuuint64_t)(p.C / 8);
+        dims[0] = 256; dims[1] = p.pixels_alloc / 32; dims[2] = 1;
         strides[0] = 512; strides[1] = plane_stride; strides[2] = plane_stride;
-        box[0] = 256; box[1] = p.Nt / 32; box[2] = 1; box[3] = 2;
+        box[0] = 256; box[1] = p.Nt / 32; box[2] = 1;
     }
-    const cuuint32_t estr[4] = {1, 1, 1, 1};
-    CUresult r = enc(&tm, CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, const_cast<void *>(image), dims, strides, box, estr,
+    // dims 3 and 4: the channel group of 8 (two per K block) and the (segment, digit plane) index;
+    // one box covers the eight planes of a segment
+    dims[3] = C8; dims[4] = 48;
+    strides[3] = C8 * plane_stride;
+    box[3] = 2; box[4] = 8;
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    CUresult r = enc(&tm, CU_TENSOR_MAP_DATA_TYPE_UINT16, 5, const_cast<void *>(image), dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_error(c, PG_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
