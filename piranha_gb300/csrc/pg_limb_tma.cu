@@ -312,33 +312,40 @@ __device__ __forceinline__ void issue_hi(uint32_t acc, uint64_t adesc, uint32_t 
 __device__ __forceinline__ int f2i(uint32_t x) { return __float2int_rz(__uint_as_float(x)); }
 
 // Move accumulators into the running 64-bit sums of this thread's 32
-// columns, one accumulator at a time. Low group: diagonals 0-3 in full 64-bit
-// precision. High group: diagonals 4-7 (shift >= 32) only into the high word.
-__device__ __forceinline__ void drain_lo(uint32_t taddr, uint64_t (&acc)[32]) {
+// columns. Low group: diagonals 0-3 in full 64-bit precision. High group:
+// diagonals 4-7 (shift >= 32) only into the high word. The next
+// accumulator's tensor-memory load is in flight while the current one is
+// folded in (tcgen05.wait::ld waits for all of a thread's loads, so each
+// wait covers exactly the one load issued since the previous wait).
+__device__ __forceinline__ void fold_lo(int a, const uint32_t (&r)[32], uint64_t (&acc)[32]) {
 #pragma unroll
-    for (int a = 0; a < 4; a++) {
-        uint32_t r[32];
-        tc::tmem_ld32(taddr + (uint32_t)(a * BN), r);
-        tc::tmem_wait_ld();
-#pragma unroll
-        for (int j = 0; j < 32; j++) {
-            // acc += D * 2^(8a) as one widening multiply-add
-            const int32_t dv = f2i(r[j]);
-            uint64_t t;
-            asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(t) : "r"(dv), "r"(1 << (8 * a)), "l"(acc[j]));
-            acc[j] = t;
-        }
+    for (int j = 0; j < 32; j++) {
+        // acc += D * 2^(8a) as one widening multiply-add
+        const int32_t dv = f2i(r[j]);
+        uint64_t t;
+        asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(t) : "r"(dv), "r"(1 << (8 * a)), "l"(acc[j]));
+        acc[j] = t;
     }
 }
-__device__ __forceinline__ void drain_hi(uint32_t taddr, uint64_t (&acc)[32]) {
+__device__ __forceinline__ void fold_hi(int a, const uint32_t (&r)[32], uint64_t (&acc)[32]) {
 #pragma unroll
-    for (int a = 4; a < 8; a++) {
-        uint32_t r[32];
-        tc::tmem_ld32(taddr + (uint32_t)(a * BN), r);
-        tc::tmem_wait_ld();
-#pragma unroll
-        for (int j = 0; j < 32; j++) acc[j] += (uint64_t)((uint32_t)f2i(r[j]) << (8 * (a - 4))) << 32;
-    }
+    for (int j = 0; j < 32; j++) acc[j] += (uint64_t)((uint32_t)f2i(r[j]) << (8 * (a - 4))) << 32;
+}
+template <bool HI> __device__ __forceinline__ void drain(uint32_t taddr, uint64_t (&acc)[32]) {
+    constexpr int a0 = HI ? 4 : 0;
+    uint32_t r0[32], r1[32];
+    tc::tmem_ld32(taddr + (uint32_t)(a0 * BN), r0);
+    tc::tmem_wait_ld();
+    tc::tmem_ld32(taddr + (uint32_t)((a0 + 1) * BN), r1);
+    if (HI) fold_hi(a0, r0, acc); else fold_lo(a0, r0, acc);
+    tc::tmem_wait_ld();
+    tc::tmem_ld32(taddr + (uint32_t)((a0 + 2) * BN), r0);
+    if (HI) fold_hi(a0 + 1, r1, acc); else fold_lo(a0 + 1, r1, acc);
+    tc::tmem_wait_ld();
+    tc::tmem_ld32(taddr + (uint32_t)((a0 + 3) * BN), r1);
+    if (HI) fold_hi(a0 + 2, r0, acc); else fold_lo(a0 + 2, r0, acc);
+    tc::tmem_wait_ld();
+    if (HI) fold_hi(a0 + 3, r1, acc); else fold_lo(a0 + 3, r1, acc);
 }
 
 // number of low-group chunks of a K' range of nst stages
@@ -493,7 +500,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             // Two cursors over the stage ring, one per accumulator group. A group
             // at a chunk boundary waits for the epilogue to drain it while the
             // other group runs on over the stages already loaded; a stage is
-            // released once both groups have issued their MMAs for it.
+            // released once both groups have issued their MMAs for it. The
+            // barriers are polled with test_wait, which never suspends the
+            // thread, so one group's wait does not hold back the other's MMAs.
             int cur[2] = {0, 0};           // next stage per group (0 low, 1 high)
             int cstart[2] = {0, 0};        // first stage of the group's current chunk
             int cend[2] = {nst < LO_FIRST ? nst : LO_FIRST, nst < CHUNK_STAGES ? nst : CHUNK_STAGES};
@@ -508,11 +517,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     const int t = cur[gi];
                     if (t >= nst) continue;
                     if (!drained[gi]) {
-                        if (!tc::mbar_try_wait(tc::smem_u32(&sm.acc_empty[gi]), (uint32_t)(chunk[gi] - 1) & 1)) continue;
+                        if (!tc::mbar_test_wait(tc::smem_u32(&sm.acc_empty[gi]), (uint32_t)(chunk[gi] - 1) & 1)) continue;
+                        // the epilogue's tensor-memory loads of these accumulators come before our MMAs
+                        tc::tc_fence_after();
                         drained[gi] = true;
                     }
-                    if (!tc::mbar_try_wait(tc::smem_u32(&sm.full[t % STAGES]), (uint32_t)(t / STAGES) & 1)) continue;
-                    tc::tc_fence_after();
+                    // stage data: the barrier's complete_tx orders the TMA writes before the MMAs
+                    if (!tc::mbar_test_wait(tc::smem_u32(&sm.full[t % STAGES]), (uint32_t)(t / STAGES) & 1)) continue;
                     const uint64_t off = (uint64_t)(((t % STAGES) * STAGE_BYTES) >> 4);
                     if (gi == 0) issue_lo(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart[0]);
                     else issue_hi(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart[1]);
@@ -562,8 +573,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         uint64_t t_idle = 0;
         while (done_ch[0] < nch[0] || done_ch[1] < nch[1]) {
             int gi = -1;
-            if (done_ch[1] < nch[1] && tc::mbar_try_wait(tc::smem_u32(&sm.acc_full[1]), (uint32_t)done_ch[1] & 1)) gi = 1;
-            else if (done_ch[0] < nch[0] && tc::mbar_try_wait(tc::smem_u32(&sm.acc_full[0]), (uint32_t)done_ch[0] & 1))
+            if (done_ch[1] < nch[1] && tc::mbar_test_wait(tc::smem_u32(&sm.acc_full[1]), (uint32_t)done_ch[1] & 1)) gi = 1;
+            else if (done_ch[0] < nch[0] && tc::mbar_test_wait(tc::smem_u32(&sm.acc_full[0]), (uint32_t)done_ch[0] & 1))
                 gi = 0;
             if (gi < 0) {
                 if (sm.abort) break;
@@ -577,8 +588,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             t_idle = 0;
             tc::tc_fence_after();
-            if (gi == 0) drain_lo(taddr, zs);
-            else drain_hi(taddr, zs);
+            if (gi == 0) drain<false>(taddr, zs);
+            else drain<true>(taddr, zs);
             tc::tc_fence_before();
             tc::mbar_arrive(tc::smem_u32(&sm.acc_empty[gi]));
             done_ch[gi]++;
