@@ -154,6 +154,17 @@ int pg_rss_maxpool_layer_u64_u8(pg_ctx *ctx, const uint64_t *const in[6], uint64
                                 uint8_t *const maxprime[6], int H, int W, int C, int pool, int stride, int batch,
                                 int fp);
 
+/* AveragepoolLayer::forward (src/nn/AveragepoolLayer.cu:58-81): the sum of
+ * each pool window (averagepool_im2row, src/gpu/convolution.cuh:340-374, with
+ * its kernel's width/height swap) and dividePublic by pool^2; and ::backward
+ * (:88-117): averagepool_expand_delta (convolution.cuh:195-208) then / pool^2.
+ * in/deltas are batch x H x W x C, out/delta the pooled shape. The backward
+ * needs non-overlapping pools (stride >= pool): the reference's expansion
+ * writes past the gradient buffer otherwise, here PG_ERR_UNSUPPORTED. */
+int pg_rss_avgpool_layer_u64(pg_ctx *ctx, const uint64_t *const in[6], uint64_t *const out[6], int H, int W, int C,
+                             int pool, int stride, int batch);
+int pg_rss_avgpool_backward_u64(pg_ctx *ctx, const uint64_t *const delta[6], uint64_t *const deltas[6], int H, int W,
+                                int C, int pool, int stride, int batch);
 /* ------------------------------------------------------- glue kernels
  * elementVectorAdd (src/gpu/matrix.cuh:75-84), reduceSum (:109-126),
  * truncate_cols (:141-154), bitexpand (src/gpu/bitwise.cuh:10-21),
@@ -299,6 +310,7 @@ int pg_rss_matmul_u64_noalloc(pg_ctx *ctx, const uint64_t *const a[6], const uin
 #define PG_LAYER_CNN 2     /* p = {H, W, Din, Dout, f, stride, pad} */
 #define PG_LAYER_RELU 3    /* p = {n per image} */
 #define PG_LAYER_MAXPOOL 4 /* p = {H, W, C, pool, stride} */
+#define PG_LAYER_AVGPOOL 5 /* p = {H, W, C, pool, stride} */
 
 typedef struct pg_net pg_net;
 /* spec: nlayers records of 8 ints {type, p0..p6}. Weight/bias shares are

@@ -414,6 +414,26 @@ def maxpool_row2im(rows, out, image_height, image_width, f, Din, batch, stride):
     return out
 
 
+def avgpool_layer(x, H, W, C, pool, stride, batch, comm=None):
+    """AveragepoolLayer::forward (AveragepoolLayer.cu:58-81) for RSS."""
+    x = _views(x, np.uint64, batch * H * W * C)
+    oh, ow = (H - pool) // stride + 1, (W - pool) // stride + 1
+    out = np.empty((3, 2, batch * oh * ow * C), dtype=np.uint64)
+    comm = comm or Comm()
+    lib().or_avgpool_layer_forward_u64(_p(x), _p(out), H, W, C, pool, stride, batch, comm.ptr())
+    return out
+
+
+def avgpool_layer_backward(delta, H, W, C, pool, batch, comm=None):
+    """AveragepoolLayer::backward (AveragepoolLayer.cu:88-117)."""
+    delta = _views(delta, np.uint64)
+    out = np.empty((3, 2, batch * H * W * C), dtype=np.uint64)
+    comm = comm or Comm()
+    lib().or_avgpool_layer_backward_u64(_p(delta), ctypes.c_size_t(delta.shape[2]), _p(out), H, W, C, pool, batch,
+                                        comm.ptr())
+    return out
+
+
 def relu_layer_backward(delta, relu_prime, comm=None):
     """ReLULayer::backward (ReLULayer.cu:90-124)."""
     delta = _views(delta, np.uint64)

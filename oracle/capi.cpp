@@ -260,6 +260,24 @@ extern "C" int or_maxpool_layer_backward_u64_u8(const uint64_t* delta, size_t n,
     store(O, deltas);
     return 0;
 }
+extern "C" int or_avgpool_layer_forward_u64(const uint64_t* in, uint64_t* out, int H, int W, int C, int pool,
+                                            int stride, int batch, uint64_t* comm) {
+    RSSV<uint64_t> A, O;
+    load(A, in, (size_t)batch * H * W * C);
+    CommIO io(comm);
+    avgpool_layer_forward<uint64_t>(A, O, H, W, C, pool, stride, batch, io.c);
+    store(O, out);
+    return 0;
+}
+extern "C" int or_avgpool_layer_backward_u64(const uint64_t* delta, size_t n, uint64_t* deltas, int H, int W, int C,
+                                             int pool, int batch, uint64_t* comm) {
+    RSSV<uint64_t> D, O;
+    load(D, delta, n);
+    CommIO io(comm);
+    avgpool_layer_backward<uint64_t>(D, O, H, W, C, pool, batch, io.c);
+    store(O, deltas);
+    return 0;
+}
 extern "C" int or_fc_layer_backward_u64(const uint64_t* delta, const uint64_t* fwd_in, uint64_t* w, uint64_t* b,
                                         uint64_t* deltas, int batch, int din, int dout, int fp, int lr, uint64_t* comm) {
     RSSV<uint64_t> D, X, Wt, Bs, O;

@@ -736,6 +736,56 @@ void maxpool_layer_backward(const RSSV<T>& delta, const RSSV<U>& maxPrime, RSSV<
         for (int s = 0; s < 2; s++) maxpool_row2im<T>(pools.v[p][s].data(), deltas.v[p][s].data(), W, H, pool, C, batch, stride);
 }
 
+// AveragepoolLayer::forward (AveragepoolLayer.cu:58-81): averagepool_im2row
+// (convolution.cuh:340-374, which hands the kernel of :56-107 its width and
+// height swapped), reduceSum of each window, dividePublic by pool^2. Window
+// positions out of the image are skipped by that kernel; with padding 0 and
+// whole windows there are none.
+template <typename T>
+void avgpool_layer_forward(const RSSV<T>& in, RSSV<T>& act, int H, int W, int C, int pool, int stride, int batch,
+                           Comm& comm) {
+    const int kW = H, kH = W;  // the kernel's imageWidth / imageHeight
+    const int wk = (kW - pool) / stride + 1, hk = (kH - pool) / stride + 1;
+    const size_t n_out = (size_t)batch * wk * hk * C;
+    act.resize(n_out);
+    for (int p = 0; p < 3; p++)
+        for (int s = 0; s < 2; s++)
+            for (size_t e = 0; e < n_out; e++) {
+                const size_t b = e / ((size_t)wk * hk * C), rem = e % ((size_t)wk * hk * C);
+                const int win = (int)(rem / C), ch = (int)(rem % C);
+                const int base_col = (win / hk) * stride, base_row = (win % hk) * stride;
+                T acc = 0;
+                for (int c = 0; c < pool; c++)
+                    for (int r = 0; r < pool; r++) {
+                        const int y = base_row + r, x = base_col + c;
+                        if (y < 0 || y >= kH || x < 0 || x >= kW) continue;
+                        acc = (T)(acc + in.v[p][s][b * (size_t)kH * kW * C + (size_t)x * kH * C + (size_t)y * C + ch]);
+                    }
+                act.v[p][s][e] = acc;
+            }
+    T d = (T)(pool * pool);
+    rss_divide_public<T>(act, &d, false, comm);
+}
+
+// AveragepoolLayer::backward (AveragepoolLayer.cu:88-117) with
+// averagepool_expand_delta (convolution.cuh:195-208): delta element i is
+// copied to slots (i / C) * C * pool^2 + i % C + k * C, k < pool^2, of the
+// zeroed input gradient (the input layout for a global pool), then / pool^2.
+template <typename T>
+void avgpool_layer_backward(const RSSV<T>& delta, RSSV<T>& deltas, int H, int W, int C, int pool, int batch,
+                            Comm& comm) {
+    const int f2 = pool * pool;
+    deltas.resize((size_t)batch * H * W * C);
+    for (int p = 0; p < 3; p++)
+        for (int s = 0; s < 2; s++)
+            for (size_t i = 0; i < delta.n; i++) {
+                const size_t b = i / C, ch = i % C;
+                for (size_t j = b * C * f2 + ch; j < (b + 1) * C * f2; j += C) deltas.v[p][s][j] = delta.v[p][s][i];
+            }
+    T d = (T)f2;
+    rss_divide_public<T>(deltas, &d, false, comm);
+}
+
 template <typename T> static void rss_sub_assign(RSSV<T>& a, const RSSV<T>& b) {
     for (int p = 0; p < 3; p++)
         for (int s = 0; s < 2; s++)

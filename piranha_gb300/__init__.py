@@ -28,7 +28,7 @@ from . import build as _build
 PG_OK = 0
 FORM_U64, FORM_LIMB_TC = 0, 1
 FPROP, DGRAD, WGRAD = 0, 1, 2
-LAYER_FC, LAYER_CNN, LAYER_RELU, LAYER_MAXPOOL = 1, 2, 3, 4
+LAYER_FC, LAYER_CNN, LAYER_RELU, LAYER_MAXPOOL, LAYER_AVGPOOL = 1, 2, 3, 4, 5
 FLOAT_PRECISION = 26
 
 _lib = None
@@ -83,6 +83,8 @@ def _declare(lib):
         "pg_rss_maxpool_u64_u8": [vp, _P6, sz, i, _P6, _P6],
         "pg_rss_maxpool_u64_u64": [vp, _P6, sz, i, _P6, _P6],
         "pg_rss_maxpool_layer_u64_u8": [vp, _P6, _P6, _P6, i, i, i, i, i, i, i],
+        "pg_rss_avgpool_layer_u64": [vp, _P6, _P6, i, i, i, i, i, i],
+        "pg_rss_avgpool_backward_u64": [vp, _P6, _P6, i, i, i, i, i, i],
         "pg_element_vector_add_u64": [vp, vp, vp, i, i, i],
         "pg_reduce_sum_u64": [vp, vp, vp, i, i, i],
         "pg_truncate_cols_u8": [vp, vp, vp, sz, i, i],
@@ -400,6 +402,18 @@ def maxpool(ctx: Context, input, result, dresult, k):
     return result, dresult
 
 
+def avgpool_layer(ctx: Context, input, out, H, W, C, pool, stride, batch):
+    """AveragepoolLayer::forward (AveragepoolLayer.cu:58-81)."""
+    ctx._check(lib().pg_rss_avgpool_layer_u64(ctx.handle, _p6(input), _p6(out), H, W, C, pool, stride, batch))
+    return out
+
+
+def avgpool_backward(ctx: Context, delta, deltas, H, W, C, pool, stride, batch):
+    """AveragepoolLayer::backward (AveragepoolLayer.cu:88-117)."""
+    ctx._check(lib().pg_rss_avgpool_backward_u64(ctx.handle, _p6(delta), _p6(deltas), H, W, C, pool, stride, batch))
+    return deltas
+
+
 def maxpool_layer(ctx: Context, input, out, maxprime, H, W, C, pool, stride, batch, fp=FLOAT_PRECISION):
     """MaxpoolLayer::forward (MaxpoolLayer.cu:52-131)."""
     ctx._check(lib().pg_rss_maxpool_layer_u64_u8(ctx.handle, _p6(input), _p6(out), _p6(maxprime), H, W, C, pool,
@@ -693,10 +707,11 @@ class Network:
     ::backward, NeuralNetwork.cu:109-148).
 
     ``layers`` is a list of tuples: ("fc", din, dout), ("cnn", H, W, Din, Dout, f, stride, pad),
-    ("relu", n_per_image), ("maxpool", H, W, C, pool, stride).
+    ("relu", n_per_image), ("maxpool", H, W, C, pool, stride), ("avgpool", H, W, C, pool, stride).
     """
 
-    _CODES = {"fc": LAYER_FC, "cnn": LAYER_CNN, "relu": LAYER_RELU, "maxpool": LAYER_MAXPOOL}
+    _CODES = {"fc": LAYER_FC, "cnn": LAYER_CNN, "relu": LAYER_RELU, "maxpool": LAYER_MAXPOOL,
+              "avgpool": LAYER_AVGPOOL}
 
     def __init__(self, ctx: Context, layers, batch: int, fp: int = FLOAT_PRECISION):
         self.ctx = ctx

@@ -70,6 +70,10 @@ int rss_select(Ctx *, const T *const *, const T *const *, const U *const *, T *c
 template <typename T, typename U> int rss_maxpool(Ctx *, const T *const *, size_t, int, T *const *, U *const *);
 template <typename T, typename U>
 int rss_maxpool_layer(Ctx *, const T *const *, T *const *, U *const *, int, int, int, int, int, int, int);
+template <typename T>
+int rss_avgpool_layer(Ctx *, const T *const *, T *const *, int, int, int, int, int, int);
+template <typename T>
+int rss_avgpool_backward(Ctx *, const T *const *, T *const *, int, int, int, int, int, int);
 template <typename T> int rss_reconstruct(Ctx *, const T *const *, size_t, T *const *);
 template <typename T> int rss_reshare(Ctx *, const T *const *, size_t, T *const *);
 template <typename T, bool AND> int rss_mul(Ctx *, T *const *, const T *const *, size_t);
@@ -300,6 +304,16 @@ int pg_rss_maxpool_layer_u64_u8(pg_ctx *c, const uint64_t *const in[6], uint64_t
                                 int fp) {
     CTX_OR_FAIL(c);
     return rss_maxpool_layer<uint64_t, uint8_t>(c, in, out, maxprime, H, W, C, pool, stride, batch, fp);
+}
+int pg_rss_avgpool_layer_u64(pg_ctx *c, const uint64_t *const in[6], uint64_t *const out[6], int H, int W, int C,
+                             int pool, int stride, int batch) {
+    CTX_OR_FAIL(c);
+    return rss_avgpool_layer<uint64_t>(c, in, out, H, W, C, pool, stride, batch);
+}
+int pg_rss_avgpool_backward_u64(pg_ctx *c, const uint64_t *const delta[6], uint64_t *const deltas[6], int H, int W,
+                                int C, int pool, int stride, int batch) {
+    CTX_OR_FAIL(c);
+    return rss_avgpool_backward<uint64_t>(c, delta, deltas, H, W, C, pool, stride, batch);
 }
 int pg_element_vector_add_u64(pg_ctx *c, uint64_t *a, const uint64_t *b, int rowwise, int rows, int cols) {
     CTX_OR_FAIL(c);

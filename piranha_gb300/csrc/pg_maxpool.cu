@@ -201,6 +201,99 @@ int rss_maxpool_layer(Ctx *c, const T *const in[6], T *const out[6], U *const ma
     return PG_OK;
 }
 
+// ------------------------------------------------------------ averagepool
+
+template <typename T> int rss_divide_public(Ctx *, T *const *, size_t, T, const T *);
+
+// AveragepoolLayer::forward (AveragepoolLayer.cu:58-81): each window summed
+// per share, in the (batch, window, channel) order of averagepool_im2row
+// (convolution.cuh:340-374), whose kernel (:56-107) gets the image's width and
+// height swapped (kW = H, kH = W here); window positions outside the image are
+// skipped, as that kernel skips them.
+template <typename T>
+__global__ void avgpool_sum_kernel(CSh6<T> in, Sh6<T> out, int kW, int kH, int C, int pool, int stride, int wk,
+                                   int hk, size_t n_out) {
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n_out; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t per_img = (size_t)wk * hk * C;
+        const size_t b = e / per_img, rem = e - b * per_img;
+        const int win = (int)(rem / C), ch = (int)(rem - (size_t)win * C);
+        const int base_col = (win / hk) * stride, base_row = (win % hk) * stride;
+        T acc[6] = {0, 0, 0, 0, 0, 0};
+        for (int cc = 0; cc < pool; cc++)
+            for (int r = 0; r < pool; r++) {
+                const int y = base_row + r, x = base_col + cc;
+                if (y < 0 || y >= kH || x < 0 || x >= kW) continue;
+                const size_t src = b * (size_t)kH * kW * C + (size_t)x * kH * C + (size_t)y * C + ch;
+#pragma unroll
+                for (int k = 0; k < 6; k++) acc[k] = (T)(acc[k] + in.p[k][src]);
+            }
+#pragma unroll
+        for (int k = 0; k < 6; k++) out.p[k][e] = acc[k];
+    }
+}
+
+// averagepool_expand_delta (convolution.cuh:195-208): delta element i goes to
+// slots (i / C) * C * f2 + i % C + j * C, j < f2, of the input gradient.
+template <typename T> __global__ void avgpool_expand_kernel(CSh6<T> in, Sh6<T> out, size_t n, int C, int f2) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t b = i / C, ch = i - b * C;
+        const size_t first = b * (size_t)C * f2 + ch;
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            const T v = in.p[k][i];
+            for (int j = 0; j < f2; j++) out.p[k][first + (size_t)j * C] = v;
+        }
+    }
+}
+
+template <typename T>
+int rss_avgpool_layer(Ctx *c, const T *const in[6], T *const out[6], int H, int W, int C, int pool, int stride,
+                      int batch) {
+    CSh6<T> a;
+    Sh6<T> o;
+    if (!load6(a, in) || !load6(o, out)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    if (H <= 0 || W <= 0 || C <= 0 || pool <= 0 || stride <= 0 || batch <= 0 || pool > H || pool > W)
+        return set_error(c, PG_ERR_SIZE, "averagepool layer: bad geometry");
+    const int kW = H, kH = W;
+    const int wk = (kW - pool) / stride + 1, hk = (kH - pool) / stride + 1;
+    const size_t n_out = (size_t)batch * wk * hk * C;
+    avgpool_sum_kernel<T><<<pool_grid(c, n_out), 128, 0, c->stream>>>(a, o, kW, kH, C, pool, stride, wk, hk, n_out);
+    c->launches++;
+    int st = launch_status(c, "avgpool_sum_kernel");
+    if (st) return st;
+    return rss_divide_public<T>(c, out, n_out, (T)(pool * pool), nullptr);
+}
+
+// AveragepoolLayer::backward (AveragepoolLayer.cu:88-117): deltas zeroed, the
+// incoming gradient expanded, then dividePublic by pool^2. The expansion
+// writes delta_n * pool^2 = batch * H * W * C slots when the pools tile the
+// image (stride == pool), as the reference's layer sizes assume.
+template <typename T>
+int rss_avgpool_backward(Ctx *c, const T *const delta[6], T *const deltas[6], int H, int W, int C, int pool,
+                         int stride, int batch) {
+    CSh6<T> a;
+    Sh6<T> o;
+    if (!load6(a, delta) || !load6(o, deltas)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    if (H <= 0 || W <= 0 || C <= 0 || pool <= 0 || stride <= 0 || batch <= 0 || pool > H || pool > W)
+        return set_error(c, PG_ERR_SIZE, "averagepool layer: bad geometry");
+    const size_t n_in = (size_t)batch * H * W * C;
+    const size_t n_delta = (size_t)batch * ((H - pool) / stride + 1) * ((W - pool) / stride + 1) * C;
+    if (n_delta * (size_t)pool * pool > n_in)
+        return set_error(c, PG_ERR_UNSUPPORTED, "averagepool backward: overlapping pools (stride %d < pool %d)", stride,
+                         pool);
+    for (int k = 0; k < 6; k++) PG_CHECK_CUDA(c, cudaMemsetAsync(deltas[k], 0, n_in * sizeof(T), c->stream));
+    avgpool_expand_kernel<T><<<pool_grid(c, n_delta), 128, 0, c->stream>>>(a, o, n_delta, C, pool * pool);
+    c->launches++;
+    int st = launch_status(c, "avgpool_expand_kernel");
+    if (st) return st;
+    return rss_divide_public<T>(c, deltas, n_in, (T)(pool * pool), nullptr);
+}
+
+template int rss_avgpool_layer<uint64_t>(Ctx *, const uint64_t *const *, uint64_t *const *, int, int, int, int, int,
+                                         int);
+template int rss_avgpool_backward<uint64_t>(Ctx *, const uint64_t *const *, uint64_t *const *, int, int, int, int,
+                                            int, int);
+
 template int rss_maxpool<uint64_t, uint8_t>(Ctx *, const uint64_t *const *, size_t, int, uint64_t *const *,
                                             uint8_t *const *);
 template int rss_maxpool<uint64_t, uint64_t>(Ctx *, const uint64_t *const *, size_t, int, uint64_t *const *,

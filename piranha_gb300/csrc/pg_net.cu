@@ -25,6 +25,10 @@ template <typename T, typename U>
 int rss_maxpool_layer(Ctx *, const T *const *, T *const *, U *const *, int, int, int, int, int, int, int);
 template <typename T, typename U>
 int rss_select(Ctx *, const T *const *, const T *const *, const U *const *, T *const *, size_t);
+template <typename T>
+int rss_avgpool_layer(Ctx *, const T *const *, T *const *, int, int, int, int, int, int);
+template <typename T>
+int rss_avgpool_backward(Ctx *, const T *const *, T *const *, int, int, int, int, int, int);
 template <typename T> int rss_reconstruct(Ctx *, const T *const *, size_t, T *const *);
 template <typename T> int rss_divide_public(Ctx *, T *const *, size_t, T, const T *);
 int reduce_sum_u64(Ctx *, const uint64_t *, uint64_t *, int, int, int);
@@ -192,6 +196,9 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
             case PG_LAYER_MAXPOOL:
                 st = rss_maxpool_layer<uint64_t, uint8_t>(c, cur, L.out, L.d, L.p[0], L.p[1], L.p[2], L.p[3], L.p[4],
                                                           net->batch, net->fp);
+                break;
+            case PG_LAYER_AVGPOOL:
+                st = rss_avgpool_layer<uint64_t>(c, cur, L.out, L.p[0], L.p[1], L.p[2], L.p[3], L.p[4], net->batch);
                 break;
             default: st = set_error(c, PG_ERR_INVALID_ARG, "bad layer type %d", L.type);
         }
@@ -497,6 +504,10 @@ static int net_backward(pg_net *net, const uint64_t *const in[6], const uint64_t
                 if ((st = launch_status(c, "row2im6_kernel"))) return st;
                 break;
             }
+            case PG_LAYER_AVGPOOL:  // AveragepoolLayer::backward (AveragepoolLayer.cu:88-117)
+                st = rss_avgpool_backward<uint64_t>(c, din, L.delta, L.p[0], L.p[1], L.p[2], L.p[3], L.p[4], B);
+                if (st) return st;
+                break;
             default: return set_error(c, PG_ERR_INVALID_ARG, "bad layer type %d", L.type);
         }
         // the limb form keeps packed weights: repack the updated ones
@@ -551,7 +562,8 @@ int pg_net_create(pg_ctx *c, pg_net **out, const int *spec, int nlayers, int bat
                 L.in_n = L.out_n = (size_t)batch * L.p[0];
                 L.d_n = L.out_n;
                 break;
-            case PG_LAYER_MAXPOOL: {
+            case PG_LAYER_MAXPOOL:
+            case PG_LAYER_AVGPOOL: {
                 int H = L.p[0], W = L.p[1], C = L.p[2], f = L.p[3], s = L.p[4];
                 if (f <= 0 || s <= 0 || f > H || f > W) {
                     delete net;
@@ -559,7 +571,7 @@ int pg_net_create(pg_ctx *c, pg_net **out, const int *spec, int nlayers, int bat
                 }
                 L.in_n = (size_t)batch * H * W * C;
                 L.out_n = (size_t)batch * ((H - f) / s + 1) * ((W - f) / s + 1) * C;
-                L.d_n = L.out_n * f * f;
+                L.d_n = L.type == PG_LAYER_MAXPOOL ? L.out_n * f * f : 0;
                 break;
             }
             default: delete net; return set_error(c, PG_ERR_INVALID_ARG, "layer %d: bad type %d", i, L.type);

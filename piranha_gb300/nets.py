@@ -2,7 +2,8 @@
 tuples for ``piranha_gb300.Network``, and seeded synthetic parameters.
 
 Layer tuples: ("fc", din, dout), ("cnn", H, W, Din, Dout, f, stride, pad),
-("relu", n_per_image), ("maxpool", H, W, C, pool, stride).
+("relu", n_per_image), ("maxpool", H, W, C, pool, stride),
+("avgpool", H, W, C, pool, stride).
 """
 from __future__ import annotations
 
@@ -24,9 +25,10 @@ def lenet():
 
 
 def vgg16(maxpool: bool = True):
-    """files/models/vgg16-cifar10.json with each averagepool replaced by a 2x2/2 maxpool."""
-    if not maxpool:
-        raise ValueError("only the maxpool variant is built")
+    """files/models/vgg16-cifar10.json; maxpool=True replaces each of its five
+    2x2/2 averagepool layers by a maxpool (the secure-inference benchmark's
+    network), maxpool=False keeps them."""
+    pool = "maxpool" if maxpool else "avgpool"
     L = []
     hw, c = 32, 3
     for width, reps in [(64, 2), (128, 2), (256, 3), (512, 3), (512, 3)]:
@@ -35,7 +37,7 @@ def vgg16(maxpool: bool = True):
             c = width
             if r < reps - 1:
                 L.append(("relu", hw * hw * c))
-        L.append(("maxpool", hw, hw, c, 2, 2))
+        L.append((pool, hw, hw, c, 2, 2))
         hw //= 2
         L.append(("relu", hw * hw * c))
     L += [("fc", 512, 256), ("relu", 256), ("fc", 256, 256), ("relu", 256), ("fc", 256, 10), ("relu", 10)]

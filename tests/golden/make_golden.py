@@ -137,6 +137,8 @@ def main():
     # Layer.cu backward inline cases
     add(layer, "src/test/Layer.cu", "ReLUBackwardBasic", {"batch": 1})
     add(layer, "src/test/Layer.cu", "MaxpoolBackwardBasic", {"H": 2, "W": 2, "C": 2, "pool": 2, "stride": 1, "batch": 2})
+    add(layer, "src/test/Layer.cu", "AveragepoolForwardBasic", {"H": 2, "W": 2, "C": 2, "pool": 2, "stride": 1, "batch": 2})
+    add(layer, "src/test/Layer.cu", "AveragepoolBackwardBasic", {"H": 2, "W": 2, "C": 2, "pool": 2, "stride": 1, "batch": 2})
     add(layer, "src/test/Layer.cu", "CNNBackwardBasic",
         {"H": 3, "W": 3, "Din": 2, "Dout": 3, "f": 3, "stride": 2, "pad": 1, "batch": 2})
 

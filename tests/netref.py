@@ -40,6 +40,9 @@ def forward(layers, params, x, batch, fp=26, comm=None, keep=False, bits=None):
         elif kind == "maxpool":
             H, W, C, pool, stride = L[1:]
             x, d = orc.maxpool_layer(x, H, W, C, pool, stride, batch, fp, comm=comm)
+        elif kind == "avgpool":
+            H, W, C, pool, stride = L[1:]
+            x = orc.avgpool_layer(x, H, W, C, pool, stride, batch, comm=comm)
         else:
             raise ValueError(kind)
         if keep:
@@ -74,6 +77,9 @@ def backward(layers, params, x, outs, bits, labels, batch, fp=26, log_lr=5, comm
         elif kind == "maxpool":
             H, W, C, pool, stride = L[1:]
             d = orc.maxpool_layer_backward(delta, bits[i], H, W, C, pool, stride, batch, comm)
+        elif kind == "avgpool":
+            H, W, C, pool, stride = L[1:]
+            d = orc.avgpool_layer_backward(delta, H, W, C, pool, batch, comm)
         else:
             raise ValueError(kind)
         deltas[i] = d
@@ -90,7 +96,7 @@ def train_step(layers, params, x, labels, batch, fp=26, log_lr=5, comm=None):
 
 
 def vgg16_layers(maxpool=True):
-    """VGG16 of files/models/vgg16-cifar10.json with each averagepool replaced by a 2x2/2 maxpool."""
+    """VGG16 of files/models/vgg16-cifar10.json; maxpool=True replaces each averagepool by a 2x2/2 maxpool."""
     L = []
     hw, c = 32, 3
     blocks = [(64, 2), (128, 2), (256, 3), (512, 3), (512, 3)]
@@ -100,7 +106,7 @@ def vgg16_layers(maxpool=True):
             c = width
             if r < reps - 1:
                 L.append(("relu", hw * hw * c))
-        L.append(("maxpool", hw, hw, c, 2, 2))
+        L.append(("maxpool" if maxpool else "avgpool", hw, hw, c, 2, 2))
         hw //= 2
         L.append(("relu", hw * hw * c))
     L += [("fc", 512, 256), ("relu", 256), ("fc", 256, 256), ("relu", 256), ("fc", 256, 10), ("relu", 10)]

@@ -534,6 +534,22 @@ def test_layer_maxpool_backward_basic(golden):
     assert_reveal(orc.maxpool_layer_backward(enc_list(a["gradin"]), mp, *geo), a["expected"])
 
 
+def test_layer_avgpool_forward_basic(golden):
+    c = golden[0]["AveragepoolForwardBasic"]
+    p, a = c["params"], c["arrays"]
+    out = orc.avgpool_layer(enc_list(a["inputImage"]), p["H"], p["W"], p["C"], p["pool"], p["stride"], p["batch"])
+    assert_reveal(out, a["expected"])
+
+
+def test_layer_avgpool_backward_basic(golden):
+    c = golden[0]["AveragepoolBackwardBasic"]
+    p, a = c["params"], c["arrays"]
+    comm = orc.Comm()
+    d = orc.avgpool_layer_backward(enc_list(a["gradin"]), p["H"], p["W"], p["C"], p["pool"], p["batch"], comm)
+    assert_reveal(d, a["expected"])
+    assert comm.rounds == 1 and comm.tx == [16 * 8] * 3  # the dividePublic of the 16 input gradients
+
+
 def test_layer_cnn_backward_basic(golden):
     c = golden[0]["CNNBackwardBasic"]
     p, a = c["params"], c["arrays"]
