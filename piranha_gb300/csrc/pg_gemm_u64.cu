@@ -62,8 +62,21 @@ template <typename T> struct GemmArgs {
     int steps_per_split;
 };
 
-constexpr int BM = 128, BN = 64, BK = 16, NT = 256, TM = 8, TN = 4;
+constexpr int BK = 16, NT = 256;
 constexpr int APAD = 2, BPAD = 2;
+
+// CTA tile shapes: BM x BN outputs, TM x TN per thread, (BM/TM) x (BN/TN) = NT
+// threads. Wide is the default; Thin serves narrow outputs (N <= 8: the input
+// gradient of a convolution with few input channels), Small serves small
+// M x N with a long K (weight gradients), where a 128 x 64 tile would be
+// mostly idle.
+template <int BM_, int BN_, int TM_, int TN_> struct Tile {
+    static constexpr int BM = BM_, BN = BN_, TM = TM_, TN = TN_;
+    static_assert((BM / TM) * (BN / TN) == NT, "one output block per thread");
+};
+using Wide = Tile<128, 64, 8, 4>;
+using Thin = Tile<128, 8, 4, 1>;
+using Small = Tile<32, 32, 2, 2>;
 
 // Which index of a loaded element varies fastest across threads.
 template <int KIND> struct Layout {
@@ -163,8 +176,10 @@ template <typename T> __device__ __forceinline__ void apply_epilogue(const GemmA
     }
 }
 
-template <typename T, int KIND>
+template <typename T, int KIND, class TL>
 __global__ void __launch_bounds__(NT) ring_gemm_kernel(const GemmArgs<T> g) {
+    constexpr int BM = TL::BM, BN = TL::BN, TM = TL::TM, TN = TL::TN;
+    constexpr int NA = (BM * BK + NT - 1) / NT, NB = (BN * BK + NT - 1) / NT;  // loads per thread
     __shared__ T As[2][BK][BM + APAD];
     __shared__ T Bs[2][BK][BN + BPAD];
     using L = Loader<T, KIND>;
@@ -179,7 +194,7 @@ __global__ void __launch_bounds__(NT) ring_gemm_kernel(const GemmArgs<T> g) {
 #pragma unroll
         for (int j = 0; j < TN; j++) acc[i][j] = 0;
 
-    T ra[BM * BK / NT], rb[BN * BK / NT];
+    T ra[NA], rb[NB];
     const int ksteps = (g.K + BK - 1) / BK;
     const int all_steps = ksteps * g.nseg;
     const int first = g.partial ? (int)blockIdx.z * g.steps_per_split : 0;
@@ -191,28 +206,32 @@ __global__ void __launch_bounds__(NT) ring_gemm_kernel(const GemmArgs<T> g) {
         int seg = step / ksteps, k0 = (step - seg * ksteps) * BK;
         const T *a = g.a[seg];
 #pragma unroll
-        for (int i = 0; i < BM * BK / NT; i++) {
+        for (int i = 0; i < NA; i++) {
             int e = tid + i * NT;
+            if (NA * NT > BM * BK && e >= BM * BK) break;
             int mm = a_mfast ? (e % BM) : (e / BK), kk = a_mfast ? (e / BM) : (e % BK);
             ra[i] = L::load_a(g, a, m0 + mm, k0 + kk);
         }
 #pragma unroll
-        for (int i = 0; i < BN * BK / NT; i++) {
+        for (int i = 0; i < NB; i++) {
             int e = tid + i * NT;
+            if (NB * NT > BN * BK && e >= BN * BK) break;
             int kk = b_kfast ? (e % BK) : (e / BN), nn = b_kfast ? (e / BK) : (e % BN);
             rb[i] = L::load_b(g, seg, k0 + kk, n0 + nn);
         }
     };
     auto sstore = [&](int buf) {
 #pragma unroll
-        for (int i = 0; i < BM * BK / NT; i++) {
+        for (int i = 0; i < NA; i++) {
             int e = tid + i * NT;
+            if (NA * NT > BM * BK && e >= BM * BK) break;
             int mm = a_mfast ? (e % BM) : (e / BK), kk = a_mfast ? (e / BM) : (e % BK);
             As[buf][kk][mm] = ra[i];
         }
 #pragma unroll
-        for (int i = 0; i < BN * BK / NT; i++) {
+        for (int i = 0; i < NB; i++) {
             int e = tid + i * NT;
+            if (NB * NT > BN * BK && e >= BN * BK) break;
             int kk = b_kfast ? (e % BK) : (e / BN), nn = b_kfast ? (e / BK) : (e % BN);
             Bs[buf][kk][nn] = rb[i];
         }
@@ -281,8 +300,8 @@ template <typename T> static void setup_conv(GemmArgs<T> &g, int op, int N, int 
     else { g.M = K; g.N = R * S * C; g.K = N * P * Q; }
 }
 
-template <typename T, int KIND> static void launch_kind(Ctx *c, dim3 grid, const GemmArgs<T> &g) {
-    ring_gemm_kernel<T, KIND><<<grid, NT, 0, c->stream>>>(g);
+template <typename T, int KIND, class TL> static void launch_kind(Ctx *c, dim3 grid, const GemmArgs<T> &g) {
+    ring_gemm_kernel<T, KIND, TL><<<grid, NT, 0, c->stream>>>(g);
     if (g.partial) {
         const size_t mn = (size_t)g.M * g.N;
         const int sms = c->sm_count > 0 ? c->sm_count : 148;
@@ -292,9 +311,24 @@ template <typename T, int KIND> static void launch_kind(Ctx *c, dim3 grid, const
     }
 }
 
+template <typename T, class TL> static void launch_tile(Ctx *c, dim3 grid, const GemmArgs<T> &g, int kind) {
+    switch (kind) {
+        case K_GEMM: launch_kind<T, K_GEMM, TL>(c, grid, g); break;
+        case K_FPROP: launch_kind<T, K_FPROP, TL>(c, grid, g); break;
+        case K_DGRAD: launch_kind<T, K_DGRAD, TL>(c, grid, g); break;
+        default: launch_kind<T, K_WGRAD, TL>(c, grid, g); break;
+    }
+}
+
 template <typename T> static int launch_gemm(Ctx *c, GemmArgs<T> &g, int kind) {
     if (g.M <= 0 || g.N <= 0 || g.K < 0) return set_error(c, PG_ERR_SIZE, "ring gemm: bad sizes M=%d N=%d K=%d", g.M, g.N, g.K);
-    dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM);
+    // tile shape: Thin for N <= 8, Small when a Wide tile would be less than half used
+    int shape = 0, bm = Wide::BM, bn = Wide::BN;
+    const double wide_use = (double)g.M * g.N /
+                            ((double)((g.M + Wide::BM - 1) / Wide::BM) * Wide::BM * ((g.N + Wide::BN - 1) / Wide::BN) * Wide::BN);
+    if (g.N <= Thin::BN) { shape = 1; bm = Thin::BM; bn = Thin::BN; }
+    else if (wide_use < 0.5) { shape = 2; bm = Small::BM; bn = Small::BN; }
+    dim3 grid((g.N + bn - 1) / bn, (g.M + bm - 1) / bm);
     if (grid.y > 65535) return set_error(c, PG_ERR_UNSUPPORTED, "ring gemm: M=%d too large", g.M);
     // Split K when the output tiles cannot fill the GPU (small M x N, long K:
     // weight gradients, narrow layers): about two CTAs per SM, at least four
@@ -318,12 +352,9 @@ template <typename T> static int launch_gemm(Ctx *c, GemmArgs<T> &g, int kind) {
             PG_CHECK_CUDA(c, cudaMemsetAsync(g.partial, 0, bytes, c->stream));
         }
     }
-    switch (kind) {
-        case K_GEMM: launch_kind<T, K_GEMM>(c, grid, g); break;
-        case K_FPROP: launch_kind<T, K_FPROP>(c, grid, g); break;
-        case K_DGRAD: launch_kind<T, K_DGRAD>(c, grid, g); break;
-        default: launch_kind<T, K_WGRAD>(c, grid, g); break;
-    }
+    if (shape == 1) launch_tile<T, Thin>(c, grid, g, kind);
+    else if (shape == 2) launch_tile<T, Small>(c, grid, g, kind);
+    else launch_tile<T, Wide>(c, grid, g, kind);
     c->launches += g.partial ? 2 : 1;
     return launch_status(c, "ring_gemm_kernel");
 }
