@@ -82,6 +82,7 @@ struct Args {
     int rows_mode;  // 1: the image holds one row per output row (GEMM, im2col)
     int ntiles_n, total_stages, chunks_per_split;
     int direct, colmajor;
+    int zeros_kept;  // the four zero output shares already hold 0: write only value / bias shares
     uint32_t a_box_bytes;  // bytes of one digit plane of a stage (16 * 2 * Wt * Ht * Nt)
     const uint8_t *packB;
     uint64_t *partial;
@@ -392,6 +393,7 @@ __device__ __forceinline__ void store_tile(const Args &g, int z, const uint64_t 
         uint64_t *o = g.out[ps];
         const uint64_t *b = g.bias[ps];
         const bool val = (ps == 0 || ps == 5);
+        if (!val && !b && g.zeros_kept) continue;
         for (int e = te; e < BM * BN; e += 256) {
             const int r = g.colmajor ? (e & (BM - 1)) : (e >> 6);
             const int c = g.colmajor ? (e >> 7) : (e & (BN - 1));
@@ -632,7 +634,9 @@ __global__ void reduce_kernel(const __grid_constant__ Args g, int nsplit) {
         const uint64_t vv = 1 + div_public<uint64_t>(zv - g.d, g.d, g.dshift);
 #pragma unroll
         for (int ps = 0; ps < 6; ps++) {
-            uint64_t base = (ps == 0 || ps == 5) ? vv : 0;
+            const bool val = (ps == 0 || ps == 5);
+            if (!val && !g.bias[ps] && g.zeros_kept) continue;
+            uint64_t base = val ? vv : 0;
             if (g.bias[ps]) base += g.bias[ps][n];
             g.out[ps][idx] = base;
         }
@@ -886,7 +890,7 @@ int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB) {
 }
 
 int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial, int split, int cps,
-             uint64_t *const out[6], const uint64_t *const bias[6], int trunc) {
+             uint64_t *const out[6], const uint64_t *const bias[6], int trunc, bool zeros_kept) {
     {
         int st = prepare_device(c);
         if (st) return st;
@@ -936,6 +940,7 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
     g.chunks_per_split = cps;
     g.direct = split > 1 ? 0 : 1;
     g.colmajor = p.colmajor;
+    g.zeros_kept = zeros_kept ? 1 : 0;
     g.a_box_bytes = 32u * (uint32_t)p.R;
     g.packB = (const uint8_t *)packB;
     g.partial = partial;

@@ -37,8 +37,12 @@ size_t partial_bytes(const Plan &p, int split);
 // A shares -> digit-plane image; weight shares -> packed stage images; then the GEMM (+ split-K reduction)
 int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image);
 int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB);
+// zeros_kept: the four output shares that dividePublic3out3 leaves at 0 (all
+// but party A's shareA and party C's shareB) already hold 0 and are only
+// written where a bias share is added (the network's zeroed arena)
 int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial, int split,
-             int chunks_per_split, uint64_t *const out[6], const uint64_t *const bias[6], int trunc);
+             int chunks_per_split, uint64_t *const out[6], const uint64_t *const bias[6], int trunc,
+             bool zeros_kept = false);
 
 }  // namespace lt
 }  // namespace pg

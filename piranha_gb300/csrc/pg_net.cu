@@ -143,8 +143,12 @@ static int net_limb_layer(pg_net *net, NetLayer &L, const uint64_t *const *in) {
     int st = lt::run_image(c, L.plan, in, net->limb_image);
     if (st) return st;
     const uint64_t *const *bias = L.b_n ? (const uint64_t *const *)L.b : nullptr;
+    // The arena is zeroed when the network is created and a layer's output
+    // buffers are written by that layer alone, so without a bias the four
+    // shares that dividePublic3out3 leaves at 0 stay 0: write only the two
+    // value shares.
     st = lt::run_gemm(c, L.plan, net->limb_image, L.packB, L.split > 1 ? net->limb_partial : nullptr, L.split, L.cps,
-                      L.out, bias, net->fp);
+                      L.out, bias, net->fp, bias == nullptr);
     if (st) return st;
     const uint64_t n_out = (uint64_t)L.plan.M * L.plan.N;
     comm_msg(c, 2 * n_out * 8, 2 * n_out * 8);
