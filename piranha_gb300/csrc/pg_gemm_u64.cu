@@ -69,7 +69,8 @@ constexpr int APAD = 2, BPAD = 2;
 // threads. Wide is the default; Thin serves narrow outputs (N <= 8: the input
 // gradient of a convolution with few input channels), Small serves small
 // M x N with a long K (weight gradients), where a 128 x 64 tile would be
-// mostly idle.
+// mostly idle. Col serves a single output column (the input gradient of a
+// convolution over one-channel images), one output per thread.
 template <int BM_, int BN_, int TM_, int TN_> struct Tile {
     static constexpr int BM = BM_, BN = BN_, TM = TM_, TN = TN_;
     static_assert((BM / TM) * (BN / TN) == NT, "one output block per thread");
@@ -77,6 +78,7 @@ template <int BM_, int BN_, int TM_, int TN_> struct Tile {
 using Wide = Tile<128, 64, 8, 4>;
 using Thin = Tile<128, 8, 4, 1>;
 using Small = Tile<32, 32, 2, 2>;
+using Col = Tile<256, 1, 1, 1>;
 
 // Which index of a loaded element varies fastest across threads.
 template <int KIND> struct Layout {
@@ -322,11 +324,12 @@ template <typename T, class TL> static void launch_tile(Ctx *c, dim3 grid, const
 
 template <typename T> static int launch_gemm(Ctx *c, GemmArgs<T> &g, int kind) {
     if (g.M <= 0 || g.N <= 0 || g.K < 0) return set_error(c, PG_ERR_SIZE, "ring gemm: bad sizes M=%d N=%d K=%d", g.M, g.N, g.K);
-    // tile shape: Thin for N <= 8, Small when a Wide tile would be less than half used
+    // tile shape: Col for N = 1, Thin for N <= 8, Small when a Wide tile would be less than half used
     int shape = 0, bm = Wide::BM, bn = Wide::BN;
     const double wide_use = (double)g.M * g.N /
                             ((double)((g.M + Wide::BM - 1) / Wide::BM) * Wide::BM * ((g.N + Wide::BN - 1) / Wide::BN) * Wide::BN);
-    if (g.N <= Thin::BN) { shape = 1; bm = Thin::BM; bn = Thin::BN; }
+    if (g.N == 1) { shape = 3; bm = Col::BM; bn = Col::BN; }
+    else if (g.N <= Thin::BN) { shape = 1; bm = Thin::BM; bn = Thin::BN; }
     else if (wide_use < 0.5) { shape = 2; bm = Small::BM; bn = Small::BN; }
     dim3 grid((g.N + bn - 1) / bn, (g.M + bm - 1) / bm);
     if (grid.y > 65535) return set_error(c, PG_ERR_UNSUPPORTED, "ring gemm: M=%d too large", g.M);
@@ -354,6 +357,7 @@ template <typename T> static int launch_gemm(Ctx *c, GemmArgs<T> &g, int kind) {
     }
     if (shape == 1) launch_tile<T, Thin>(c, grid, g, kind);
     else if (shape == 2) launch_tile<T, Small>(c, grid, g, kind);
+    else if (shape == 3) launch_tile<T, Col>(c, grid, g, kind);
     else launch_tile<T, Wide>(c, grid, g, kind);
     c->launches += g.partial ? 2 : 1;
     return launch_status(c, "ring_gemm_kernel");

@@ -86,6 +86,7 @@ struct Args {
     uint32_t a_box_bytes;  // bytes of one digit plane of a stage (16 * 2 * Wt * Ht * Nt)
     const uint8_t *packB;
     uint64_t *partial;
+    uint64_t *raw;  // non-null: write the untruncated Z (row-major M x N) here instead of output shares
     uint64_t *out[6];
     const uint64_t *bias[6];
     uint64_t d;
@@ -141,7 +142,7 @@ __device__ __forceinline__ void digits8(const uint64_t (&v)[8], uint4 (&pl)[NPL]
 
 // ------------------------------------------------------------ image kernel
 
-enum { SRC_ROWS = 0, SRC_COLS = 1, SRC_IM2COL = 2 };
+enum { SRC_ROWS = 0, SRC_COLS = 1, SRC_IM2COL = 2, SRC_WGRAD = 3 };
 
 struct ImageArgs {
     const uint64_t *a[6];
@@ -186,6 +187,32 @@ __global__ void image_kernel(const __grid_constant__ ImageArgs ia) {
 #pragma unroll
                 for (int i = 0; i < 8; i++)
                     if (k0 + i < ia.Kreal) v[i] = __ldg(src + i);
+            }
+        } else if (ia.mode == SRC_WGRAD) {
+            // weight gradient: row pix = (r, s, c) of the filter, K index k =
+            // (n, p, q) of an output pixel, value = the forward input at
+            // (n, p*stride - pad + r, q*stride - pad + s, c)
+            const int c = (int)(pix % ia.Din);
+            const int rs = (int)(pix / ia.Din);
+            const int s = rs % ia.f, r = rs / ia.f;
+            int q = k0 % ia.Q;
+            const int np = k0 / ia.Q;
+            int p = np % ia.P;
+            long long n = np / ia.P;
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                if (k0 + i < ia.Kreal) {
+                    const int h = p * ia.stride - ia.pad + r, w = q * ia.stride - ia.pad + s;
+                    if (h >= 0 && h < ia.H && w >= 0 && w < ia.W)
+                        v[i] = __ldg(a + ((n * ia.H + h) * ia.W + w) * (long long)ia.Din + c);
+                }
+                if (++q == ia.Q) {
+                    q = 0;
+                    if (++p == ia.P) {
+                        p = 0;
+                        ++n;
+                    }
+                }
             }
         } else if (ia.mode == SRC_COLS) {
 #pragma unroll
@@ -628,6 +655,10 @@ __global__ void reduce_kernel(const __grid_constant__ Args g, int nsplit) {
          e += (long long)gridDim.x * blockDim.x) {
         uint64_t zv = 0;
         for (int s = 0; s < nsplit; s++) zv += g.partial[(long long)s * total + e];
+        if (g.raw) {
+            g.raw[e] = zv;
+            continue;
+        }
         const long long m = e / g.N;
         const int n = (int)(e - m * g.N);
         const long long idx = g.colmajor ? m + (long long)n * g.M : e;
@@ -640,6 +671,51 @@ __global__ void reduce_kernel(const __grid_constant__ Args g, int nsplit) {
             if (g.bias[ps]) base += g.bias[ps][n];
             g.out[ps][idx] = base;
         }
+    }
+}
+
+// ------------------------------------------------------ input gradient
+
+struct Col2ImArgs {
+    const uint64_t *cols;  // [n][p][q][r][s][c]: untruncated Z of dY x W per output pixel and tap
+    uint64_t *out[6];
+    long long total;       // batch * H * W * Din
+    int H, W, Din, f, stride, pad, P, Q;
+    uint64_t d;
+    int dshift;
+};
+
+// The input gradient of a convolution (CNNLayer backward, dL/dX): Z at
+// (n, h, w, c) is the sum of the per-tap products cols[(n, p, q)][(r, s, c)]
+// over the taps with p * stride = h + pad - r, q * stride = w + pad - s; then
+// dividePublic3out3 (r = 1 at party A's shareA and party C's shareB).
+__global__ void col2im_kernel(const __grid_constant__ Col2ImArgs ca) {
+    const long long fd = (long long)ca.f * ca.f * ca.Din;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ca.total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(e % ca.Din);
+        long long t = e / ca.Din;
+        const int w = (int)(t % ca.W);
+        t /= ca.W;
+        const int h = (int)(t % ca.H);
+        const long long n = t / ca.H;
+        uint64_t z = 0;
+        for (int r = 0; r < ca.f; r++) {
+            const int ph = h + ca.pad - r;
+            if (ph < 0 || ph % ca.stride) continue;
+            const int p = ph / ca.stride;
+            if (p >= ca.P) continue;
+            for (int s = 0; s < ca.f; s++) {
+                const int qw = w + ca.pad - s;
+                if (qw < 0 || qw % ca.stride) continue;
+                const int q = qw / ca.stride;
+                if (q >= ca.Q) continue;
+                z += __ldg(ca.cols + ((n * ca.P + p) * ca.Q + q) * fd + (r * ca.f + s) * ca.Din + c);
+            }
+        }
+        const uint64_t v = 1 + div_public<uint64_t>(z - ca.d, ca.d, ca.dshift);
+#pragma unroll
+        for (int ps = 0; ps < 6; ps++) ca.out[ps][e] = (ps == 0 || ps == 5) ? v : 0;
     }
 }
 
@@ -826,6 +902,35 @@ int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout
     return PG_OK;
 }
 
+int plan_wgrad(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad) {
+    memset(&p, 0, sizeof(p));
+    if (batch <= 0 || H <= 0 || W <= 0 || f <= 0 || Din <= 0 || Dout <= 0 || stride <= 0 || pad < 0 ||
+        H + 2 * pad < f || W + 2 * pad < f)
+        return set_error(c, PG_ERR_SIZE, "convolution: bad geometry");
+    const int P = (H + 2 * pad - f) / stride + 1, Q = (W + 2 * pad - f) / stride + 1;
+    const long long K = (long long)batch * P * Q;
+    if (K > (1ll << 30)) return set_error(c, PG_ERR_UNSUPPORTED, "weight gradient over %lld output pixels", K);
+    // rows (r, s, c) of the filter, K = output pixels (n, p, q): the image is the
+    // transposed im2col gather of the forward input, the packed operand the
+    // output gradient dY[pixel][Dout], the output dW[Dout][r][s][c] column-major
+    p.implicit = 0;
+    p.M = f * f * Din;
+    p.N = Dout;
+    p.Kreal = (int)K;
+    p.C = (p.Kreal + BK - 1) / BK * BK;
+    p.pixels = p.M;
+    p.src_mode = SRC_WGRAD;
+    p.tB_kn = 1;
+    p.colmajor = 1;
+    p.H = H; p.W = W; p.Din = Din; p.stride = stride;
+    p.cf = f; p.cpad = pad; p.cP = P; p.cQ = Q;
+    p.f = 1; p.pad = 0;
+    p.Wimg = 1; p.Himg = 1; p.Nimg = p.M;
+    p.P = 1; p.Q = 1;
+    finish_plan(p);
+    return PG_OK;
+}
+
 void choose_split(const Plan &p, int sms, int &split, int &cps) {
     const int total_stages = 6 * p.kblocks;
     const int chunks = (total_stages + CHUNK_STAGES - 1) / CHUNK_STAGES;
@@ -890,7 +995,7 @@ int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB) {
 }
 
 int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial, int split, int cps,
-             uint64_t *const out[6], const uint64_t *const bias[6], int trunc, bool zeros_kept) {
+             uint64_t *const out[6], const uint64_t *const bias[6], int trunc, bool zeros_kept, uint64_t *raw) {
     {
         int st = prepare_device(c);
         if (st) return st;
@@ -938,14 +1043,15 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
     g.ntiles_n = p.ntiles_n;
     g.total_stages = 6 * p.kblocks;
     g.chunks_per_split = cps;
-    g.direct = split > 1 ? 0 : 1;
+    g.direct = (split > 1 || raw) ? 0 : 1;
     g.colmajor = p.colmajor;
     g.zeros_kept = zeros_kept ? 1 : 0;
     g.a_box_bytes = 32u * (uint32_t)p.R;
     g.packB = (const uint8_t *)packB;
-    g.partial = partial;
+    g.partial = raw && split <= 1 ? raw : partial;
+    g.raw = raw;
     for (int i = 0; i < 6; i++) {
-        g.out[i] = out[i];
+        g.out[i] = raw ? nullptr : out[i];
         g.bias[i] = bias ? bias[i] : nullptr;
     }
     g.d = 1ull << trunc;
@@ -1004,21 +1110,71 @@ int limb3_rss_matmul_u64(Ctx *c, const uint64_t *const a[6], const uint64_t *con
     return run_with_scratch(c, p, a, b, out, bias, trunc);
 }
 
-template <typename T>
-int rss_conv(Ctx *, const T *const *, const T *const *, T *const *, int, int, int, int, int, int, int, int, int, int);
-
 int limb3_rss_conv_u64(Ctx *c, const uint64_t *const A[6], const uint64_t *const B[6], uint64_t *const C[6], int op,
                        int batch, int H, int W, int f, int Din, int Dout, int stride, int pad, int trunc) {
-    if (op != PG_CONV_FPROP)  // the data-gradient and weight-gradient convolutions run on the integer CUDA cores
-        return rss_conv<uint64_t>(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc);
     CSh6<uint64_t> ca, cb;
     Sh6<uint64_t> co;
     if (!load6(ca, A) || !load6(cb, B) || !load6(co, C)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
     if (trunc < 0 || trunc > 63) return set_error(c, PG_ERR_INVALID_ARG, "bad truncation %d", trunc);
+    if (op < 0 || op > 2) return set_error(c, PG_ERR_INVALID_ARG, "bad conv operator %d", op);
     lt::Plan p;
-    int st = lt::plan_conv(c, p, batch, H, W, f, Din, Dout, stride, pad);
-    if (st) return st;
-    return run_with_scratch(c, p, A, B, C, nullptr, trunc);
+    int st;
+    if (op == PG_CONV_FPROP) {
+        if ((st = lt::plan_conv(c, p, batch, H, W, f, Din, Dout, stride, pad))) return st;
+        return run_with_scratch(c, p, A, B, C, nullptr, trunc);
+    }
+    if (op == PG_CONV_WGRAD) {
+        // dW[Dout][r][s][c] = sum over output pixels of dY x im2col(X): A is
+        // dY, B the forward input; the GEMM takes the forward input as its row
+        // operand (the sum over the three parties of x_p0 (y_p0 + y_p1) + x_p1
+        // y_p0 does not change when x and y trade places)
+        if ((st = lt::plan_wgrad(c, p, batch, H, W, f, Din, Dout, stride, pad))) return st;
+        return run_with_scratch(c, p, B, A, C, nullptr, trunc);
+    }
+    // dX = col2im(dY x W): the per-tap products of every output pixel as one
+    // GEMM (M = output pixels, N = f * f * Din, K = Dout), kept as untruncated
+    // Z, then summed into the input pixels and truncated once
+    if (batch <= 0 || H <= 0 || W <= 0 || f <= 0 || Din <= 0 || Dout <= 0 || stride <= 0 || pad < 0 ||
+        H + 2 * pad < f || W + 2 * pad < f)
+        return set_error(c, PG_ERR_SIZE, "convolution: bad geometry");
+    const int P = (H + 2 * pad - f) / stride + 1, Q = (W + 2 * pad - f) / stride + 1;
+    const long long Mcols = (long long)batch * P * Q;
+    if (Mcols > (1ll << 30) || (long long)f * f * Din > (1ll << 30))
+        return set_error(c, PG_ERR_UNSUPPORTED, "input gradient of %lld output pixels", Mcols);
+    if ((st = lt::plan_gemm(c, p, (int)Mcols, f * f * Din, Dout, 1, 1, 1))) return st;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    int split, cps;
+    lt::choose_split(p, c->sm_count > 0 ? c->sm_count : 148, split, cps);
+    const size_t ib = al(p.image_bytes), pb = al(p.packB_bytes), qb = al(lt::partial_bytes(p, split));
+    const size_t cb_bytes = al((size_t)p.M * p.N * 8);
+    uint8_t *scr = (uint8_t *)scratch(c, ib + pb + qb + cb_bytes);
+    if (!scr) return PG_ERR_NO_MEMORY;
+    uint64_t *cols = (uint64_t *)(scr + ib + pb + qb);
+    if ((st = lt::run_image(c, p, A, scr))) return st;
+    if ((st = lt::run_pack(c, p, B, scr + ib))) return st;
+    if ((st = lt::run_gemm(c, p, scr, scr + ib, split > 1 ? (uint64_t *)(scr + ib + pb) : nullptr, split, cps, C,
+                           nullptr, trunc, false, cols)))
+        return st;
+    lt::Col2ImArgs a2;
+    memset(&a2, 0, sizeof(a2));
+    a2.cols = cols;
+    for (int i = 0; i < 6; i++) a2.out[i] = C[i];
+    a2.total = (long long)batch * H * W * Din;
+    a2.H = H; a2.W = W; a2.Din = Din; a2.f = f; a2.stride = stride; a2.pad = pad; a2.P = P; a2.Q = Q;
+    a2.d = 1ull << trunc;
+    a2.dshift = pow2_shift<uint64_t>(a2.d);
+    {
+        const int sms = c->sm_count > 0 ? c->sm_count : 148;
+        long long blocks = (a2.total + 255) / 256;
+        if (blocks > (long long)sms * 16) blocks = (long long)sms * 16;
+        lt::col2im_kernel<<<(unsigned)blocks, 256, 0, c->stream>>>(a2);
+        c->launches++;
+        if ((st = launch_status(c, "col2im_kernel"))) return st;
+    }
+    const uint64_t n_out = (uint64_t)a2.total;
+    comm_msg(c, 2 * n_out * 8, 2 * n_out * 8);
+    comm_round(c);
+    return PG_OK;
 }
 
 int limb_prepare_current_device(Ctx *c) { return lt::prepare_device(c); }

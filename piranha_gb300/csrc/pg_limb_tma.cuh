@@ -32,6 +32,8 @@ struct Plan {
 int prepare_device(Ctx *c);  // once per device, with it current (no allocation)
 int plan_gemm(Ctx *c, Plan &p, int M, int N, int K, int tA, int tB, int tC);
 int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad);
+// the weight gradient of that convolution as a GEMM over the output pixels
+int plan_wgrad(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad);
 void choose_split(const Plan &p, int sms, int &split, int &chunks_per_split);
 size_t partial_bytes(const Plan &p, int split);
 // A shares -> digit-plane image; weight shares -> packed stage images; then the GEMM (+ split-K reduction)
@@ -39,10 +41,11 @@ int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image);
 int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB);
 // zeros_kept: the four output shares that dividePublic3out3 leaves at 0 (all
 // but party A's shareA and party C's shareB) already hold 0 and are only
-// written where a bias share is added (the network's zeroed arena)
+// written where a bias share is added (the network's zeroed arena).
+// raw: write the untruncated Z (M x N, row-major) there instead of shares.
 int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial, int split,
              int chunks_per_split, uint64_t *const out[6], const uint64_t *const bias[6], int trunc,
-             bool zeros_kept = false);
+             bool zeros_kept = false, uint64_t *raw = nullptr);
 
 }  // namespace lt
 }  // namespace pg

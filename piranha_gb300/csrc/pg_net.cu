@@ -34,6 +34,8 @@ template <typename T> int rss_divide_public(Ctx *, T *const *, size_t, T, const 
 int reduce_sum_u64(Ctx *, const uint64_t *, uint64_t *, int, int, int);
 int limb3_rss_matmul_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *,
                          const uint64_t *const *, int, int, int, int, int, int, int);
+int limb3_rss_conv_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *, int, int, int, int,
+                       int, int, int, int, int, int);
 }  // namespace pg
 
 using namespace pg;
@@ -446,6 +448,12 @@ static int share_gemm(Ctx *c, const uint64_t *const *a, const uint64_t *const *b
     return rss_matmul<uint64_t>(c, a, b, out, nullptr, M, N, K, tA, tB, tC, trunc);
 }
 
+static int share_conv(Ctx *c, const uint64_t *const *a, const uint64_t *const *b, uint64_t *const *out, int op,
+                      int B, int H, int W, int f, int Din, int Dout, int s, int pd, int trunc) {
+    if (c->form == PG_FORM_LIMB_TC) return limb3_rss_conv_u64(c, a, b, out, op, B, H, W, f, Din, Dout, s, pd, trunc);
+    return rss_conv<uint64_t>(c, a, b, out, op, B, H, W, f, Din, Dout, s, pd, trunc);
+}
+
 // NeuralNetwork::_backward_pass (NeuralNetwork.cu:444-460): every layer's
 // backward from the last to the first, each updating its parameters.
 static int net_backward(pg_net *net, const uint64_t *const in[6], const uint64_t *const labels[6], int log_lr) {
@@ -477,11 +485,11 @@ static int net_backward(pg_net *net, const uint64_t *const in[6], const uint64_t
             }
             case PG_LAYER_CNN: {  // CNNLayer::backward (CNNLayer.cu:114-193)
                 const int H = L.p[0], W = L.p[1], Din = L.p[2], Dout = L.p[3], f = L.p[4], s = L.p[5], pd = L.p[6];
-                if ((st = rss_conv<uint64_t>(c, din, (const uint64_t *const *)L.w, L.delta, PG_CONV_DGRAD, B, H, W, f, Din,
-                                             Dout, s, pd, net->fp)))
+                if ((st = share_conv(c, din, (const uint64_t *const *)L.w, L.delta, PG_CONV_DGRAD, B, H, W, f, Din, Dout,
+                                     s, pd, net->fp)))
                     return st;
-                if ((st = rss_conv<uint64_t>(c, din, fwd_in, net->tr.dW, PG_CONV_WGRAD, B, H, W, f, Din, Dout, s, pd,
-                                             net->fp)))
+                if ((st = share_conv(c, din, fwd_in, net->tr.dW, PG_CONV_WGRAD, B, H, W, f, Din, Dout, s, pd,
+                                     net->fp)))
                     return st;
                 if ((st = rss_divide_public<uint64_t>(c, net->tr.dW, L.w_n, 1ull << log_lr, nullptr))) return st;
                 if ((st = sub6(c, L.w, net->tr.dW, L.w_n))) return st;

@@ -127,6 +127,32 @@ def test_limb_conv(pg, ctx, batch, H, W, f, Din, Dout, stride, pad):
     assert np.array_equal(pg.to_host(C), want)
 
 
+@pytest.mark.parametrize("op", [orc.DGRAD, orc.WGRAD])
+@pytest.mark.parametrize("batch,H,W,f,Din,Dout,stride,pad", [
+    (3, 28, 28, 5, 1, 20, 1, 0),    # LeNet conv 1: one input channel
+    (4, 12, 12, 5, 20, 50, 1, 0),   # LeNet conv 2: odd channel counts
+    (2, 8, 8, 3, 64, 64, 1, 1),     # VGG-like, padded
+    (2, 9, 7, 3, 5, 7, 2, 1),       # strided, ragged
+    (1, 5, 5, 5, 3, 2, 1, 2),       # filter as wide as the padding allows
+])
+def test_limb_conv_backward(pg, ctx, op, batch, H, W, f, Din, Dout, stride, pad):
+    """Input gradient (dY x W into column products, then col2im and one
+    truncation) and weight gradient (the forward input's transposed im2col x
+    dY) against the oracle's dgrad / wgrad convolutions."""
+    P, Q = (H + 2 * pad - f) // stride + 1, (W + 2 * pad - f) // stride + 1
+    A = orc.random_views(batch * P * Q * Dout, U64, 17)
+    nb = Dout * f * f * Din if op == orc.DGRAD else batch * H * W * Din
+    B = orc.random_views(nb, U64, 18)
+    comm = orc.Comm()
+    want = orc.convolution(A, B, op, batch, H, W, f, Din, Dout, stride, pad, 26, comm)
+    C = pg.empty_shares(want.shape[2])
+    pg.convolution(ctx, pg.to_device(A), pg.to_device(B), C, op, batch, H, W, f, Din, Dout, stride, pad, 26)
+    ctx.check_device_errors()
+    assert np.array_equal(pg.to_host(C), want)
+    got = ctx.comm()
+    assert got["tx"] == comm.tx and got["rx"] == comm.rx and got["rounds"] == comm.rounds
+
+
 def test_limb_vgg16_forward(pg):
     from tests.test_gpu_network import run_net
 
