@@ -526,7 +526,8 @@ def bench_train(args, pg, torch, stream, dev, form, wl, batch, world):
 
 
 def bench_fcnet(args, pg, torch, stream, dev, wl, batch, world):
-    """2PC / 4PC FC net: FCLayer::forward + ReLU per layer through the TPC / FPC entry points (eager launches)."""
+    """2PC / 4PC FC net: FCLayer::forward + ReLU per layer through the TPC / FPC entry points, captured as one
+    CUDA graph (ctx.capture) after an eager forward."""
     w = WORKLOADS[args.workload]
     fp, ring = w["fp"], w["ring"]
     proto = pg.tpc if w["parties"] == 2 else pg.fpc
@@ -555,12 +556,16 @@ def bench_fcnet(args, pg, torch, stream, dev, wl, batch, world):
         return cur
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    # one eager forward sizes the context scratch, then the whole forward is one graph
+    forward(x)
+    with ctx.capture() as graph:
+        y = forward(x)
     for _ in range(args.warmup):
-        forward(x)
+        graph.launch()
     stream.synchronize()
     launches0 = ctx.kernel_launches()
     comm0 = ctx.comm(w["parties"])
-    dev_s, wall, clocks = _timed(args, torch, stream, dev, world, lambda: forward(x), flush)
+    dev_s, wall, clocks = _timed(args, torch, stream, dev, world, graph.launch, flush)
     launches = ctx.kernel_launches() - launches0
     comm1 = ctx.comm(w["parties"])
     value = world * batch * args.steps / dev_s
@@ -571,8 +576,8 @@ def bench_fcnet(args, pg, torch, stream, dev, wl, batch, world):
     y_host = torch.empty(bufs[-1][0].shape, dtype=tdt, pin_memory=True)
 
     def e2e_step():
-        xd = x_host.to(dev, non_blocking=True)
-        y = forward(xd)
+        x.copy_(x_host, non_blocking=True)
+        graph.launch()
         y_host.copy_(y, non_blocking=True)
 
     e2e_s = _e2e(args, torch, stream, dev, world, e2e_step, flush)
@@ -587,12 +592,13 @@ def bench_fcnet(args, pg, torch, stream, dev, wl, batch, world):
         "gpu_launches": int(launches),
         "clocks": clocks,
         "roofline": {"bound": "launch", "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None,
-                     "kernel": "per-layer protocol launches",
+                     "kernel": "per-layer protocol launches in one graph",
                      "work": f"{macs:.4g} plaintext MACs per forward in {len(layers)} layers: far too little to "
                              "load the tensor cores or HBM, so the step is launch-bound"},
         "comm_per_party_per_step": {"tx_bytes": [int((a - b) // args.steps) for a, b in zip(comm1["tx"], comm0["tx"])],
                                     "rounds": int((comm1["rounds"] - comm0["rounds"]) // args.steps)},
     }
+    graph.close()
     ctx.close()
     return out
 
@@ -743,7 +749,7 @@ def main():
         "vs_baseline": None, "dtype": dtype, "data": "synthetic",
         "config": {"workload": w["desc"], "global_batch": args.batch * world, "parallelism": "replicas",
                    "form": res["form"], "l2": "256 MiB write between timed steps",
-                   "graph": "eager launches" if w["kind"] == "fcnet" else "one CUDA graph per step"},
+                   "graph": "one CUDA graph per step"},
         "e2e": res["e2e"], "gpu_launches": res["gpu_launches"], "clocks": res["clocks"],
         "roofline": res["roofline"], "cpu_baseline": cb,
         "comm_per_party_per_step": res["comm_per_party_per_step"],

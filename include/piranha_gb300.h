@@ -70,6 +70,19 @@ uint64_t pg_kernel_launches(pg_ctx *ctx);
 /* synchronize, then report (and clear) the device error word that bounded
  * device-side waits set when they give up: PG_ERR_TIMEOUT with *code != 0 */
 int pg_device_errors(pg_ctx *ctx, int *code);
+/* Stream capture of any sequence of calls on ctx into one CUDA graph (the
+ * reference launches every kernel eagerly; this is the replacement for its
+ * per-op launch overhead). Run the same sequence eagerly once first: that
+ * sizes the context's scratch, which cannot be allocated inside a capture.
+ * Every pointer the calls received stays baked into the graph. Capture does no
+ * work and adds nothing to the counters; each launch adds the communication
+ * and kernel counts of the captured calls. A graph lives until
+ * pg_graph_destroy and must not outlive its context. */
+typedef struct pg_graph pg_graph;
+int pg_graph_begin(pg_ctx *ctx);
+int pg_graph_end(pg_ctx *ctx, pg_graph **out);
+int pg_graph_launch(pg_ctx *ctx, pg_graph *graph);
+int pg_graph_destroy(pg_graph *graph);
 /* diagnostic: one 128x64x16 tcgen05 MMA of fp16 operands (A 128x16 and B
  * 64x16 row-major halves), D = A * B^T as 128x64 fp32 row-major */
 int pg_tc_selftest(pg_ctx *ctx, const uint16_t *A, const uint16_t *B, float *D);

@@ -159,6 +159,10 @@ def _declare(lib):
     lib.pg_last_error.restype = ctypes.c_char_p
     lib.pg_kernel_launches.argtypes = [vp]
     lib.pg_kernel_launches.restype = ctypes.c_uint64
+    lib.pg_graph_begin.argtypes = [vp]
+    lib.pg_graph_end.argtypes = [vp, ctypes.POINTER(vp)]
+    lib.pg_graph_launch.argtypes = [vp, vp]
+    lib.pg_graph_destroy.argtypes = [vp]
     lib.pg_ctx_get_stream.argtypes = [vp]
     lib.pg_ctx_get_stream.restype = vp
     lib.pg_net_input_size.argtypes = [vp]
@@ -183,6 +187,51 @@ def library_path() -> str:
 
 
 # ------------------------------------------------------------------ context
+
+class Graph:
+    """pg_graph: a captured sequence of calls, replayed by launch()."""
+
+    def __init__(self, ctx: "Context"):
+        self.ctx = ctx
+        self._h = None
+
+    def launch(self):
+        if self._h is None:
+            raise PiranhaError("graph was not captured")
+        self.ctx._check(lib().pg_graph_launch(self.ctx.handle, self._h))
+
+    def close(self):
+        if self._h is not None:
+            lib().pg_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _Capture:
+    def __init__(self, ctx: "Context"):
+        self.ctx = ctx
+        self.graph = Graph(ctx)
+
+    def __enter__(self) -> Graph:
+        self.ctx._check(lib().pg_graph_begin(self.ctx.handle))
+        return self.graph
+
+    def __exit__(self, et, ev, tb):
+        h = ctypes.c_void_p()
+        st = lib().pg_graph_end(self.ctx.handle, ctypes.byref(h))
+        if et is not None:
+            if h.value:
+                lib().pg_graph_destroy(h)
+            return False
+        self.ctx._check(st)
+        self.graph._h = h
+        return False
+
 
 class Context:
     """pg_ctx: stream, implementation form and per-party comm counters."""
@@ -220,6 +269,13 @@ class Context:
 
     def sync(self):
         self._check(lib().pg_sync(self._h))
+
+    def capture(self) -> _Capture:
+        """``with ctx.capture() as g: ...`` records every call on this
+        context's stream (which must not be the legacy default stream) into a
+        CUDA graph; ``g.launch()`` replays it. Run the calls eagerly once
+        first so that the context's scratch is sized."""
+        return _Capture(self)
 
     def comm(self, parties=3):
         buf = (ctypes.c_uint64 * 9)()

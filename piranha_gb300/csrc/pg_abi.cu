@@ -32,15 +32,17 @@ int *device_error_word(Ctx *c) { return c->dev_err; }
 
 // A grow-only device buffer of the context (grows with cudaMalloc, which a
 // stream capture does not allow: capture after an eager run has sized it).
+// An outgrown buffer is retired, not freed: graphs captured earlier may still
+// read and write it.
 static void *grow(Ctx *c, void *&buf, size_t &have, size_t bytes, const char *what) {
     if (bytes <= have) return buf;
+    size_t want = bytes + (bytes >> 3);
     if (buf) {
-        cudaStreamSynchronize(c->stream);
-        cudaFree(buf);
+        if (want < 2 * have) want = 2 * have;  // geometric: the retired buffers sum to less than the live one
+        c->retired.push_back(buf);
         buf = nullptr;
         have = 0;
     }
-    size_t want = bytes + (bytes >> 3);
     if (cudaMalloc(&buf, want) != cudaSuccess) {
         cudaGetLastError();
         buf = nullptr;
@@ -125,6 +127,7 @@ int pg_ctx_destroy(pg_ctx *c) {
     cudaStreamSynchronize(c->stream);
     if (c->scratch) cudaFree(c->scratch);
     if (c->partial) cudaFree(c->partial);
+    for (void *p : c->retired) cudaFree(p);
     if (c->dev_err) cudaFree(c->dev_err);
     delete c;
     return PG_OK;
@@ -161,6 +164,81 @@ int pg_comm_reset(pg_ctx *c) {
     return PG_OK;
 }
 uint64_t pg_kernel_launches(pg_ctx *c) { return c ? c->launches.load() : 0; }
+
+}  // extern "C"
+
+struct pg_graph {
+    pg_ctx *owner = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t comm[9] = {0};  // counters added by one launch
+    uint64_t launches = 0;
+};
+
+extern "C" {
+
+int pg_graph_begin(pg_ctx *c) {
+    CTX_OR_FAIL(c);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    PG_CHECK_CUDA(c, cudaStreamIsCapturing(c->stream, &cs));
+    if (cs != cudaStreamCaptureStatusNone || c->capturing)
+        return set_error(c, PG_ERR_INVALID_ARG, "the context's stream is already capturing");
+    if (c->stream == nullptr)
+        return set_error(c, PG_ERR_INVALID_ARG, "capture needs a non-default stream (pg_ctx_set_stream)");
+    memcpy(c->capture_comm, c->comm, sizeof(c->comm));
+    c->capture_launches = c->launches.load();
+    PG_CHECK_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    c->capturing = true;
+    return PG_OK;
+}
+
+int pg_graph_end(pg_ctx *c, pg_graph **out) {
+    CTX_OR_FAIL(c);
+    if (!out) return set_error(c, PG_ERR_INVALID_ARG, "null graph pointer");
+    *out = nullptr;
+    if (!c->capturing) return set_error(c, PG_ERR_INVALID_ARG, "no capture in progress");
+    c->capturing = false;
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    pg_graph *g = new pg_graph;
+    g->owner = c;
+    for (int i = 0; i < 9; i++) g->comm[i] = c->comm[i] - c->capture_comm[i];
+    g->launches = c->launches.load() - c->capture_launches;
+    memcpy(c->comm, c->capture_comm, sizeof(c->comm));
+    c->launches.store(c->capture_launches);
+    if (e != cudaSuccess || !graph) {
+        cudaGetLastError();
+        if (graph) cudaGraphDestroy(graph);
+        delete g;
+        return set_error(c, PG_ERR_CUDA, "stream capture failed: %s (a call inside it allocated, synchronized or "
+                                         "failed; run the sequence eagerly once first)",
+                         cudaGetErrorString(e));
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&g->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+        cudaGetLastError();
+        delete g;
+        return set_error(c, PG_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(ei));
+    }
+    *out = g;
+    return PG_OK;
+}
+
+int pg_graph_launch(pg_ctx *c, pg_graph *g) {
+    CTX_OR_FAIL(c);
+    if (!g || g->owner != c) return set_error(c, PG_ERR_INVALID_ARG, "graph of another context");
+    PG_CHECK_CUDA(c, cudaGraphLaunch(g->exec, c->stream));
+    for (int i = 0; i < 9; i++) c->comm[i] += g->comm[i];
+    c->launches += g->launches;
+    return PG_OK;
+}
+
+int pg_graph_destroy(pg_graph *g) {
+    if (!g) return PG_ERR_INVALID_ARG;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    delete g;
+    return PG_OK;
+}
 
 int pg_device_errors(pg_ctx *c, int *out) {
     CTX_OR_FAIL(c);

@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "piranha_gb300.h"
 
@@ -34,6 +35,13 @@ struct Ctx {
     size_t partial_bytes = 0;
     int sm_count = 0;
     int *dev_err = nullptr;  // device word that bounded waits set on timeout
+    // buffers that scratch / partial outgrew: a captured graph may still
+    // point into them, so they are freed only with the context
+    std::vector<void *> retired;
+    // counters at pg_graph_begin (capture does no work: they are put back at the end)
+    uint64_t capture_comm[9] = {0};
+    uint64_t capture_launches = 0;
+    bool capturing = false;
 };
 
 int set_error(Ctx *c, int code, const char *fmt, ...);
