@@ -23,6 +23,8 @@ Other workloads (--workload), each printing the same JSON line for its own metri
   secureml-2pc  2PC SecureML inference, batch 128, uint32 shares, FP 10
   secureml-4pc  4PC SecureML inference, batch 128, uint32 shares, FP 10
   stream        512 requests of batch 1..64, SecureML or VGG16, served in order; p50/p99 latency
+  gemm          3PC share-GEMM M = N = K = 4096 with truncation by 2^26 (the matmul's dividePublic3out3
+                and reshare), uniform random uint64 shares; --sweep adds M = N = K in 512..8192
 
 With --impl reference the line times Piranha's own arithmetic restated on the
 CPU (the oracle; the reference's GPU build cannot be compiled here) on a
@@ -70,6 +72,10 @@ WORKLOADS = {
     "secureml-4pc": {"metric": "4PC SecureML secure inference img/s", "kind": "fcnet", "parties": 4, "fp": 10,
                      "ring": "u32",
                      "desc": "secureml 784-128-128-10, 4PC (FPC), batch 128, uint32 shares, FP 10"},
+    "gemm": {"metric": "3PC share-GEMM ring MAC/s", "kind": "gemm", "fp": 26, "ring": "u64", "M": 4096, "N": 4096,
+             "K": 4096, "unit": "ring-MAC/s",
+             "desc": "3PC RSS matmul M=N=K=4096 over Z_2^64 (uniform random shares), truncation by 2^26 and "
+                     "reshare; 6*M*N*K ring multiply-adds per step (3 parties x the concatenated K)"},
     "stream": {"metric": "3PC batched request stream img/s", "kind": "stream", "fp": 26, "ring": "u64",
                "requests": 512, "max_batch": 64,
                "desc": "512 requests, batch uniform in 1..64, SecureML or VGG16 (even odds), 3PC RSS, uint64 "
@@ -91,6 +97,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-u64-form comparison run")
+    ap.add_argument("--sweep", action="store_true", help="gemm: also time M = N = K in 512..8192 in both forms")
     return ap.parse_args()
 
 
@@ -122,6 +129,24 @@ def make_workload(name, batch, seed=SEED):
         classes = np.random.default_rng(seed + 3).integers(0, 10, batch)
         labels = enc.set_public(enc.one_hot(classes, 10), ring, fp)
     return {"layers": layers, "params": params, "x": x, "labels": labels}
+
+
+def make_gemm(seed=SEED):
+    """Uniform random uint64 share views of A (M x K) and B (K x N), row-major."""
+    w = WORKLOADS["gemm"]
+    M, N, K = w["M"], w["N"], w["K"]
+    rng = np.random.default_rng(seed + 11)
+    A = rng.integers(0, 2**64 - 1, size=(3, 2, M * K), dtype=np.uint64, endpoint=True)
+    B = rng.integers(0, 2**64 - 1, size=(3, 2, K * N), dtype=np.uint64, endpoint=True)
+    return {"A": A, "B": B, "M": M, "N": N, "K": K}
+
+
+def work_per_step(name, batch):
+    """Units of the workload's metric in one step: images, or ring MACs of the share-GEMM."""
+    w = WORKLOADS[name]
+    if w["kind"] == "gemm":
+        return 6 * w["M"] * w["N"] * w["K"]
+    return batch
 
 
 def make_stream(seed=SEED):
@@ -232,6 +257,33 @@ def cpu_baseline_stream(wl, budget_s):
                       f", applied to the stream's {imgs} images"}
 
 
+def cpu_baseline_gemm(wl, budget_s):
+    """The oracle's share matmul (OpenMP) on the first rows of A, extrapolated per ring MAC."""
+    import oracle as orc
+
+    M, N, K = wl["M"], wl["N"], wl["K"]
+    fp = WORKLOADS["gemm"]["fp"]
+
+    def run(rows):
+        a = np.ascontiguousarray(wl["A"][..., : rows * K])
+        t0 = time.perf_counter()
+        orc.matmul(a, wl["B"], rows, N, K, 1, 1, 1, fp)
+        return time.perf_counter() - t0
+
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    first = min(M, cores)  # one row per thread
+    t1 = run(first)
+    runs, secs = [first], t1
+    if t1 < budget_s / 2:
+        rows = max(1, min(M, int(first * (budget_s - t1) / max(t1, 1e-3)) // first * first))
+        secs += run(rows)
+        runs.append(rows)
+    macs = sum(6 * r * N * K for r in runs)
+    return {"value": macs / secs, "unit": "ring-MAC/s", "cores": cores, "kind": "port",
+            "sample": f"runs of {' and '.join(map(str, runs))} rows of the {M} x {N} x {K} share matmul "
+                      f"({secs:.1f} s), same shares"}
+
+
 def cpu_baseline(name, wl, batch_full, budget_s):
     """Piranha's arithmetic restated on the CPU (the oracle), timed on a sample of the batch."""
     import oracle as orc
@@ -240,6 +292,8 @@ def cpu_baseline(name, wl, batch_full, budget_s):
     orc.lib()
     if name == "stream":
         return cpu_baseline_stream(wl, budget_s)
+    if WORKLOADS[name]["kind"] == "gemm":
+        return cpu_baseline_gemm(wl, budget_s)
     w = WORKLOADS[name]
     layers, params, x_full = wl["layers"], wl["params"], wl["x"]
     n_in = nets.input_size(layers)
@@ -303,6 +357,10 @@ def run_ours(args, rank, world, local_rank):
         wl = make_stream()
         with torch.cuda.stream(stream):
             return bench_stream(args, pg, torch, stream, dev, wl, world), wl
+    if kind == "gemm":
+        wl = make_gemm()
+        with torch.cuda.stream(stream):
+            return bench_gemm(args, pg, torch, stream, dev, wl, world), wl
     wl = make_workload(args.workload, batch)
 
     if kind == "fcnet":
@@ -525,6 +583,104 @@ def bench_train(args, pg, torch, stream, dev, form, wl, batch, world):
     return out
 
 
+def _gemm_form(args, pg, torch, stream, dev, form, A, B, M, N, K, world, steps, warmup, e2e_host=None):
+    """One form of the share-GEMM: eager call (sizes the scratch), one captured
+    graph, warm-up and timed replays; optionally the end-to-end replays."""
+    fp = WORKLOADS["gemm"]["fp"]
+    ctx = pg.Context(dev.index, stream=stream, form=form)
+    C = pg.empty_shares(M * N, device=dev)
+    pg.matmul(ctx, A, B, C, M, N, K, 1, 1, 1, fp)
+    with ctx.capture() as graph:
+        pg.matmul(ctx, A, B, C, M, N, K, 1, 1, 1, fp)
+    for _ in range(warmup):
+        graph.launch()
+    stream.synchronize()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    sub_args = argparse.Namespace(**{**vars(args), "steps": steps})
+    launches0, comm0 = ctx.kernel_launches(), ctx.comm()
+    dev_s, wall, clocks = _timed(sub_args, torch, stream, dev, world, graph.launch, flush)
+    res = {"dev_s": dev_s, "wall": wall, "clocks": clocks, "launches": ctx.kernel_launches() - launches0,
+           "comm0": comm0, "comm1": ctx.comm()}
+    if e2e_host is not None:
+        a_h, b_h, c_h = e2e_host
+
+        def e2e_step():
+            A.copy_(a_h, non_blocking=True)
+            B.copy_(b_h, non_blocking=True)
+            graph.launch()
+            c_h.copy_(C, non_blocking=True)
+
+        res["e2e_s"] = _e2e(sub_args, torch, stream, dev, world, e2e_step, flush)
+    graph.close()
+    del C
+    ctx.close()
+    return res
+
+
+def bench_gemm(args, pg, torch, stream, dev, wl, world):
+    """3PC share-GEMM microbenchmark: pg.matmul (localMatMul over the concatenated K, dividePublic3out3 with
+    its reshare) at M = N = K = 4096, replayed from one CUDA graph; the limb tensor-core form, with the plain
+    u64 form beside it."""
+    M, N, K = wl["M"], wl["N"], wl["K"]
+    A = pg.to_device(wl["A"], dev)
+    B = pg.to_device(wl["B"], dev)
+    macs = 6 * M * N * K
+    a_h = torch.empty(A.shape, dtype=A.dtype, pin_memory=True)
+    b_h = torch.empty(B.shape, dtype=B.dtype, pin_memory=True)
+    a_h.copy_(A.cpu())
+    b_h.copy_(B.cpu())
+    c_h = torch.empty((3, 2, M * N), dtype=torch.int64, pin_memory=True)
+    form = pg.FORM_U64 if args.form == "u64" else pg.FORM_LIMB_TC
+    r = _gemm_form(args, pg, torch, stream, dev, form, A, B, M, N, K, world, args.steps, args.warmup,
+                   (a_h, b_h, c_h))
+    peaks = load_peaks()
+    peak = peaks.get("bf16_tflops")
+    achieved = LIMB_FLOPS_PER_RING_MAC * macs * args.steps / r["dev_s"] / 1e12
+    out = {
+        "form": "limb_tc" if form == pg.FORM_LIMB_TC else "u64",
+        "unit": "ring-MAC/s",
+        "value": world * macs * args.steps / r["dev_s"],
+        "ms_per_step": 1e3 * r["dev_s"] / args.steps,
+        "wall_s": r["wall"],
+        "e2e": {"value": world * macs * args.steps / r["e2e_s"], "unit": "ring-MAC/s",
+                "h2d_bytes_per_step": int(A.numel() + B.numel()) * 8, "d2h_bytes_per_step": int(c_h.numel()) * 8},
+        "gpu_launches": int(r["launches"]),
+        "clocks": r["clocks"],
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak else None, "traffic": None,
+                     "kernel": "share-GEMM (limb_tma_kernel with its operand image and packing launches)",
+                     "work": f"72 limb-tensor flops per ring MAC, {macs:.4g} ring MACs/step; the time includes "
+                             "the image and pack launches, so frac is a lower bound for the GEMM kernel",
+                     "peak_source": "bf16_tflops of measured" if peak else None},
+        "comm_per_party_per_step": {"tx_bytes": int((r["comm1"]["tx"][0] - r["comm0"]["tx"][0]) // args.steps),
+                                    "rounds": int((r["comm1"]["rounds"] - r["comm0"]["rounds"]) // args.steps)},
+        "config_extra": {"global_batch": None, "M": M, "N": N, "K": K, "truncation": 26,
+                         "data_size": "operands 805 MB per share tensor, larger than L2"},
+    }
+    if form == pg.FORM_LIMB_TC and not args.no_compare:
+        u = _gemm_form(args, pg, torch, stream, dev, pg.FORM_U64, A, B, M, N, K, world, max(2, args.steps // 4), 1)
+        uv = macs * max(2, args.steps // 4) / u["dev_s"]
+        out["compare_u64"] = {"value": uv, "ms_per_step": 1e3 * u["dev_s"] / max(2, args.steps // 4),
+                              "gemm_tflops_equiv": LIMB_FLOPS_PER_RING_MAC * uv / 1e12,
+                              "limb_over_u64": out["value"] / world / uv}
+    if args.sweep:
+        sweep = []
+        for n in (512, 1024, 2048, 4096, 8192):
+            As = torch.randint(-2**63, 2**63 - 1, (3, 2, n * n), dtype=torch.int64, device=dev)
+            Bs = torch.randint(-2**63, 2**63 - 1, (3, 2, n * n), dtype=torch.int64, device=dev)
+            row = {"M": n, "N": n, "K": n}
+            for name, fm in (("limb_tc", pg.FORM_LIMB_TC), ("u64", pg.FORM_U64)):
+                st = 3 if n <= 4096 or name == "limb_tc" else 2
+                rr = _gemm_form(args, pg, torch, stream, dev, fm, As, Bs, n, n, n, 1, st, 1)
+                row[name] = 6 * n ** 3 * st / rr["dev_s"]
+            row["limb_over_u64"] = row["limb_tc"] / row["u64"]
+            row["limb_tflops_equiv"] = LIMB_FLOPS_PER_RING_MAC * row["limb_tc"] / 1e12
+            sweep.append(row)
+            del As, Bs
+        out["sweep"] = sweep
+    return out
+
+
 def bench_fcnet(args, pg, torch, stream, dev, wl, batch, world):
     """2PC / 4PC FC net: FCLayer::forward + ReLU per layer through the TPC / FPC entry points, captured as one
     CUDA graph (ctx.capture) after an eager forward."""
@@ -719,14 +875,17 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        wl = make_stream() if w["kind"] == "stream" else make_workload(args.workload, args.batch)
+        wl = (make_stream() if w["kind"] == "stream" else make_gemm() if w["kind"] == "gemm"
+              else make_workload(args.workload, args.batch))
         cb = cpu_baseline(args.workload, wl, args.batch, args.cpu_seconds)
-        line = {"metric": w["metric"], "value": cb["value"], "unit": "img/s", "impl": "reference", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.batch / cb["value"],
+        unit = w.get("unit", "img/s")
+        line = {"metric": w["metric"], "value": cb["value"], "unit": unit, "impl": "reference", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * work_per_step(args.workload, args.batch) / cb["value"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
                 "data": "synthetic", "config": {"workload": w["desc"], "global_batch": args.batch,
                                                 "parallelism": "replicas"},
-                "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "img/s", "h2d_bytes_per_step": 0,
+                "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": unit, "h2d_bytes_per_step": 0,
                                             "d2h_bytes_per_step": 0},
                 "note": "Piranha's GPU build needs its un-vendored CUTLASS fork; this arm times the reference's "
                         "arithmetic restated on the host CPU"}
@@ -744,7 +903,8 @@ def main():
     if world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.workload, wl, args.batch, args.cpu_seconds)
     line = {
-        "metric": w["metric"], "value": res["value"], "unit": "img/s", "n_gpus": world, "steps": args.steps,
+        "metric": w["metric"], "value": res["value"], "unit": res.get("unit", "img/s"), "n_gpus": world,
+        "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": dtype, "data": "synthetic",
         "config": {"workload": w["desc"], "global_batch": args.batch * world, "parallelism": "replicas",
@@ -754,9 +914,10 @@ def main():
         "roofline": res["roofline"], "cpu_baseline": cb,
         "comm_per_party_per_step": res["comm_per_party_per_step"],
     }
+    line["config"].update(res.get("config_extra", {}))
     if "layer_ms" in res:
         line["layer_ms"] = res["layer_ms"]
-    for k in ("latency_ms", "requests", "images", "networks"):
+    for k in ("latency_ms", "requests", "images", "networks", "sweep"):
         if k in res:
             line[k] = res[k]
     if "compare_u64" in res:

@@ -246,6 +246,27 @@ template <typename T> void rss_divide_public_3of3(std::vector<T> (&z)[3], T d, R
 // is row-major when its transpose flag is set, column-major otherwise.
 template <typename T>
 void gemm(int M, int N, int K, const T* A, bool tA, const T* B, bool tB, T* C, bool tC) {
+    if (tB) {
+        // B row-major: accumulate whole rows of C (unit-stride over B's rows);
+        // the sums are the same mod 2^w in any order
+        #pragma omp parallel
+        {
+            std::vector<T> acc((size_t)N);
+            #pragma omp for schedule(static)
+            for (int m = 0; m < M; m++) {
+                std::fill(acc.begin(), acc.end(), (T)0);
+                for (int k = 0; k < K; k++) {
+                    const T a = tA ? A[(size_t)m * K + k] : A[m + (size_t)k * M];
+                    const T* brow = B + (size_t)k * N;
+                    for (int n = 0; n < N; n++) acc[n] = (T)(acc[n] + a * brow[n]);
+                }
+                for (int n = 0; n < N; n++) {
+                    if (tC) C[(size_t)m * N + n] = acc[n]; else C[m + (size_t)n * M] = acc[n];
+                }
+            }
+        }
+        return;
+    }
     #pragma omp parallel for schedule(static)
     for (int m = 0; m < M; m++) {
         for (int n = 0; n < N; n++) {
