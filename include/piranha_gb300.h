@@ -70,6 +70,12 @@ uint64_t pg_kernel_launches(pg_ctx *ctx);
 /* synchronize, then report (and clear) the device error word that bounded
  * device-side waits set when they give up: PG_ERR_TIMEOUT with *code != 0 */
 int pg_device_errors(pg_ctx *ctx, int *code);
+/* Host only: the reference's weight initialisation (FCLayer::initialize,
+ * src/nn/FCLayer.cu:31-47; CNNLayer::initialize, src/nn/CNNLayer.cu:36-50):
+ * n draws of std::normal_distribution<double>(0, std_dev) from
+ * std::default_random_engine(seed), the layer's seed being nn_seed + layer
+ * index (src/nn/NeuralNetwork.cu:32-48) and std_dev = sqrt(2 / fan_in). */
+int pg_reference_init_normal(double *out, size_t n, int seed, double std_dev);
 /* Stream capture of any sequence of calls on ctx into one CUDA graph (the
  * reference launches every kernel eagerly; this is the replacement for its
  * per-op launch overhead). Run the same sequence eagerly once first: that

@@ -159,6 +159,8 @@ def _declare(lib):
     lib.pg_last_error.restype = ctypes.c_char_p
     lib.pg_kernel_launches.argtypes = [vp]
     lib.pg_kernel_launches.restype = ctypes.c_uint64
+    lib.pg_reference_init_normal.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_size_t, ctypes.c_int,
+                                             ctypes.c_double]
     lib.pg_graph_begin.argtypes = [vp]
     lib.pg_graph_end.argtypes = [vp, ctypes.POINTER(vp)]
     lib.pg_graph_launch.argtypes = [vp, vp]

@@ -3,6 +3,7 @@
 // wrappers that forward to the templated kernels of the other translation
 // units.
 #include <cstring>
+#include <random>
 
 #include "pg_common.cuh"
 
@@ -247,6 +248,15 @@ int pg_device_errors(pg_ctx *c, int *out) {
     PG_CHECK_CUDA(c, cudaMemcpy(out, c->dev_err, sizeof(int), cudaMemcpyDeviceToHost));
     PG_CHECK_CUDA(c, cudaMemset(c->dev_err, 0, sizeof(int)));
     return *out ? set_error(c, PG_ERR_TIMEOUT, "device wait timed out (code 0x%x)", *out) : PG_OK;
+}
+
+int pg_reference_init_normal(double *out, size_t n, int seed, double std_dev) {
+    if (!out && n) return PG_ERR_INVALID_ARG;
+    if (!(std_dev >= 0.0)) return PG_ERR_INVALID_ARG;
+    std::default_random_engine generator(seed);
+    std::normal_distribution<double> distribution(0.0, std_dev);
+    for (size_t i = 0; i < n; i++) out[i] = distribution(generator);
+    return PG_OK;
 }
 
 int pg_tc_selftest(pg_ctx *c, const uint16_t *A, const uint16_t *B, float *D) {

@@ -55,6 +55,44 @@ def input_size(layers):
     return L[1] * L[2] * L[3]
 
 
+NN_SEED = 343934585  # nn_seed of the reference's config.json
+
+
+def reference_normal(n: int, seed: int, std_dev: float) -> np.ndarray:
+    """n draws of the reference's weight generator (std::default_random_engine
+    + std::normal_distribution<double>), computed by the library's host code."""
+    import ctypes
+
+    from . import lib
+
+    out = np.empty(n, dtype=np.float64)
+    st = lib().pg_reference_init_normal(out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n, int(seed),
+                                        float(std_dev))
+    if st != 0:
+        raise ValueError(f"pg_reference_init_normal status {st}")
+    return out
+
+
+def reference_init(layers, seed: int = NN_SEED, fp: int = 26, ring: str = "u64"):
+    """The reference's own initialisation (FCLayer.cu:31-47, CNNLayer.cu:36-50):
+    layer i draws from std::default_random_engine(seed + i) a normal with
+    standard deviation sqrt(2 / fan_in); FC biases 0.01; all loaded with
+    setPublic. None for layers without parameters."""
+    params = []
+    for i, L in enumerate(layers):
+        if L[0] == "fc":
+            din, dout = L[1], L[2]
+            w = reference_normal(din * dout, seed + i, float(np.sqrt(2.0 / din)))
+            params.append((_enc.set_public(w, ring, fp), _enc.set_public(np.full(dout, 0.01), ring, fp)))
+        elif L[0] == "cnn":
+            Din, Dout, f = L[3], L[4], L[5]
+            w = reference_normal(Dout * f * f * Din, seed + i, float(np.sqrt(2.0 / (f * f * Din))))
+            params.append((_enc.set_public(w, ring, fp), None))
+        else:
+            params.append(None)
+    return params
+
+
 def kaiming_uniform(layers, seed: int, fp: int = 26, ring: str = "u64"):
     """Seeded Kaiming-uniform weights (bound sqrt(6 / fan_in)), FC bias 0.01,
     loaded with setPublic; None for layers without parameters."""

@@ -46,3 +46,67 @@ def test_model_layers_and_params_match_test_reference(name):
             assert (a[1] is None) == (b[1] is None)
             if a[1] is not None:
                 assert np.array_equal(a[1], b[1])
+
+
+# The reference's weight generator, restated from the published algorithms of
+# the C++ standard library it runs on (libstdc++): minstd_rand0 (Park-Miller,
+# a = 16807, m = 2^31 - 1) as std::default_random_engine,
+# generate_canonical<double, 53> over two draws, and normal_distribution's
+# Marsaglia polar method, which returns the second variate of a pair first and
+# keeps the other for the next call.
+class _MinstdRand0:
+    M = 2147483647
+
+    def __init__(self, seed):
+        self.x = seed % self.M or 1
+
+    def __call__(self):
+        self.x = (16807 * self.x) % self.M
+        return self.x
+
+
+def _canonical(g):
+    r = float(2147483646)  # max - min + 1 with min = 1, max = m - 1
+    s = float(g() - 1) + float(g() - 1) * r
+    v = s / (r * r)
+    return v if v < 1.0 else np.nextafter(1.0, 0.0)
+
+
+def _normal_stream(seed, std_dev, n):
+    import math
+
+    g = _MinstdRand0(seed)
+    out, saved = [], None
+    while len(out) < n:
+        if saved is not None:
+            out.append(saved * std_dev)
+            saved = None
+            continue
+        while True:
+            x = 2.0 * _canonical(g) - 1.0
+            y = 2.0 * _canonical(g) - 1.0
+            r2 = x * x + y * y
+            if 0.0 < r2 <= 1.0:
+                break
+        mult = math.sqrt(-2.0 * math.log(r2) / r2)
+        saved = x * mult
+        out.append(y * mult * std_dev)
+    return np.array(out)
+
+
+@pytest.mark.parametrize("seed,std", [(nets.NN_SEED, float(np.sqrt(2.0 / 784))), (nets.NN_SEED + 4, 0.05), (1, 1.0)])
+def test_reference_init_normal_is_the_published_generator(seed, std):
+    got = nets.reference_normal(1001, seed, std)
+    want = _normal_stream(seed, std, 1001)
+    assert np.array_equal(got, want)
+
+
+def test_reference_init_layers():
+    layers = nets.secureml()
+    params = nets.reference_init(layers)
+    assert [p is None for p in params] == [False, True, False, True, False, True]
+    w0 = nets.reference_normal(784 * 128, nets.NN_SEED + 0, float(np.sqrt(2.0 / 784)))
+    assert np.array_equal(params[0][0], enc.set_public(w0))
+    assert np.array_equal(params[2][1], enc.set_public(np.full(128, 0.01)))
+    lp = nets.reference_init(nets.lenet())
+    assert lp[0][1] is None and lp[0][0].shape == (3, 2, 20 * 25)
