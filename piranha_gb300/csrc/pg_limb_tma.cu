@@ -257,18 +257,23 @@ __host__ __device__ __forceinline__ uint32_t b_off(int row, int kc) {
     return (uint32_t)((row >> 3) * 256 + kc * 128 + (row & 7) * 16);
 }
 
-// One thread per (segment, column, K block, chunk of 8). Segment 2p holds
-// y_p0 + y_p1 and segment 2p+1 holds y_p0 of party p.
+// One thread per (segment, K block, N tile, column, chunk of 8), with the
+// chunk and then the column varying fastest: a warp writes 512 contiguous
+// bytes of a digit plane (16 columns x both 8-element chunks) and reads runs
+// of consecutive columns (b[k * N + n]) or of consecutive k (b[n * K + k]).
+// Segment 2p holds y_p0 + y_p1 and segment 2p+1 holds y_p0 of party p.
 __global__ void pack_kernel(const __grid_constant__ PackArgs pa) {
-    const long long total = 6ll * pa.ntiles_n * BN * pa.kblocks * 2;
+    const long long total = 6ll * pa.kblocks * pa.ntiles_n * BN * 2;
     for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < total;
          u += (long long)gridDim.x * blockDim.x) {
         const int kc = (int)(u & 1);
-        long long t = u >> 1;
+        const int row = (int)((u >> 1) % BN);
+        long long t = (u >> 1) / BN;
+        const int nt = (int)(t % pa.ntiles_n);
+        t /= pa.ntiles_n;
         const int kb = (int)(t % pa.kblocks);
-        t /= pa.kblocks;
-        const int n = (int)(t % ((long long)pa.ntiles_n * BN));
-        const int seg = (int)(t / ((long long)pa.ntiles_n * BN));
+        const int seg = (int)(t / pa.kblocks);
+        const int n = nt * BN + row;
         const int p = seg >> 1;
         const int k0 = kb * BK + kc * 8;
         uint64_t v[8];
@@ -281,16 +286,16 @@ __global__ void pack_kernel(const __grid_constant__ PackArgs pa) {
                 const int k = k0 + i;
                 if (k < pa.Kreal) {
                     const long long idx = pa.kn ? (long long)k * pa.N + n : (long long)n * pa.Kreal + k;
-                    v[i] = b0[idx] + (b1 ? b1[idx] : 0);
+                    v[i] = __ldg(b0 + idx) + (b1 ? __ldg(b1 + idx) : 0);
                 }
             }
         }
         uint4 pl[8];
         digits8<8>(v, pl);
-        uint8_t *dst = pa.packB + (((long long)seg * pa.kblocks + kb) * pa.ntiles_n + n / BN) * B_STAGE_BYTES;
+        uint8_t *dst = pa.packB + (((long long)seg * pa.kblocks + kb) * pa.ntiles_n + nt) * B_STAGE_BYTES;
 #pragma unroll
         for (int i = 0; i < 8; i++)
-            *reinterpret_cast<uint4 *>(dst + i * B_PLANE_BYTES + b_off(n % BN, kc)) = pl[i];
+            *reinterpret_cast<uint4 *>(dst + i * B_PLANE_BYTES + b_off(row, kc)) = pl[i];
     }
 }
 
