@@ -59,6 +59,17 @@ int pg_ctx_set_stream(pg_ctx *ctx, void *cuda_stream);
 void *pg_ctx_get_stream(pg_ctx *ctx);
 int pg_ctx_set_form(pg_ctx *ctx, int form);
 int pg_ctx_get_form(pg_ctx *ctx);
+/* split-K of the limb-form GEMMs picked by timing the candidates on first use
+ * of each problem shape (default on; off = the heuristic, and the cache is
+ * cleared). Never tunes inside a stream capture. */
+int pg_ctx_set_autotune(pg_ctx *ctx, int on);
+/* Device share buffers, as the reference's share classes own them (RSS<T>:
+ * 6 buffers [party*2 + share], TPC<T>: 2, FPC<T>: 12 [party*3 + share];
+ * DeviceData.h:51-85): nbuf zeroed buffers of n elements of elem_bytes (1, 4
+ * or 8) each, 256-byte aligned, in one allocation that pg_free_shares(out[0])
+ * releases. */
+int pg_alloc_shares(pg_ctx *ctx, int nbuf, size_t n, int elem_bytes, void **out);
+int pg_free_shares(pg_ctx *ctx, void *first);
 const char *pg_last_error(pg_ctx *ctx);
 int pg_sync(pg_ctx *ctx);
 /* counters: out[0..3] = bytes sent by party 0..3, out[4..7] = bytes received,

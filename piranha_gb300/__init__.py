@@ -161,6 +161,9 @@ def _declare(lib):
     lib.pg_kernel_launches.restype = ctypes.c_uint64
     lib.pg_reference_init_normal.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_size_t, ctypes.c_int,
                                              ctypes.c_double]
+    lib.pg_ctx_set_autotune.argtypes = [vp, ctypes.c_int]
+    lib.pg_alloc_shares.argtypes = [vp, ctypes.c_int, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(vp)]
+    lib.pg_free_shares.argtypes = [vp, vp]
     lib.pg_graph_begin.argtypes = [vp]
     lib.pg_graph_end.argtypes = [vp, ctypes.POINTER(vp)]
     lib.pg_graph_launch.argtypes = [vp, vp]
@@ -271,6 +274,10 @@ class Context:
 
     def sync(self):
         self._check(lib().pg_sync(self._h))
+
+    def set_autotune(self, on: bool):
+        """Split-K of the limb-form GEMMs by timing (default on) or by the heuristic."""
+        self._check(lib().pg_ctx_set_autotune(self._h, 1 if on else 0))
 
     def capture(self) -> _Capture:
         """``with ctx.capture() as g: ...`` records every call on this

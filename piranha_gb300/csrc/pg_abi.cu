@@ -147,6 +147,36 @@ int pg_ctx_set_form(pg_ctx *c, int form) {
     return PG_OK;
 }
 int pg_ctx_get_form(pg_ctx *c) { return c ? c->form : -1; }
+int pg_ctx_set_autotune(pg_ctx *c, int on) {
+    CTX_OR_FAIL(c);
+    c->autotune = on ? 1 : 0;
+    if (!on) c->split_cache.clear();
+    return PG_OK;
+}
+
+int pg_alloc_shares(pg_ctx *c, int nbuf, size_t n, int elem_bytes, void **out) {
+    CTX_OR_FAIL(c);
+    if (!out || nbuf <= 0 || nbuf > 64 || (elem_bytes != 1 && elem_bytes != 4 && elem_bytes != 8))
+        return set_error(c, PG_ERR_INVALID_ARG, "alloc_shares: %d buffers of %d-byte elements", nbuf, elem_bytes);
+    for (int i = 0; i < nbuf; i++) out[i] = nullptr;
+    const size_t one = (n * (size_t)elem_bytes + 255) & ~(size_t)255;
+    void *base = nullptr;
+    if (cudaMalloc(&base, one * nbuf + (one == 0 ? 256 : 0)) != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(c, PG_ERR_NO_MEMORY, "alloc_shares of %zu bytes", one * nbuf);
+    }
+    PG_CHECK_CUDA(c, cudaMemsetAsync(base, 0, one * nbuf, c->stream));
+    for (int i = 0; i < nbuf; i++) out[i] = (char *)base + one * i;
+    return PG_OK;
+}
+
+int pg_free_shares(pg_ctx *c, void *first) {
+    CTX_OR_FAIL(c);
+    if (!first) return PG_OK;
+    PG_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    PG_CHECK_CUDA(c, cudaFree(first));
+    return PG_OK;
+}
 const char *pg_last_error(pg_ctx *c) { return c ? c->err.c_str() : "null context"; }
 int pg_sync(pg_ctx *c) {
     CTX_OR_FAIL(c);

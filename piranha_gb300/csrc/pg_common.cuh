@@ -11,6 +11,8 @@
 #include <cstdio>
 #include <mutex>
 #include <string>
+#include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include "piranha_gb300.h"
@@ -42,6 +44,10 @@ struct Ctx {
     uint64_t capture_comm[9] = {0};
     uint64_t capture_launches = 0;
     bool capturing = false;
+    // split-K autotuner of the limb GEMM: on/off, and the timed choice
+    // (split, chunks per split) per problem shape
+    int autotune = 1;
+    std::unordered_map<std::string, std::pair<int, int>> split_cache;
 };
 
 int set_error(Ctx *c, int code, const char *fmt, ...);

@@ -949,6 +949,119 @@ void choose_split(const Plan &p, int sms, int &split, int &cps) {
 
 size_t partial_bytes(const Plan &p, int split) { return split > 1 ? (size_t)split * p.M * p.N * 8 : 0; }
 
+// ---------------------------------------------------------- autotuner
+
+// Split-K candidates of a plan: the heuristic split, and 1, 2, 4, ... up to
+// the number of K chunks, 4x the heuristic and 64; each normalised so that
+// every split holds at least one chunk. Returns how many (at most 8).
+static int split_candidates(const Plan &p, int sms, int (&sp)[8], int (&cp)[8]) {
+    const int chunks = (6 * p.kblocks + CHUNK_STAGES - 1) / CHUNK_STAGES;
+    int h, hc;
+    choose_split(p, sms, h, hc);
+    int n = 0;
+    auto add = [&](int s) {
+        if (s < 1 || s > chunks || n >= 8) return;
+        const int c = (chunks + s - 1) / s;
+        const int s2 = (chunks + c - 1) / c;
+        for (int i = 0; i < n; i++)
+            if (sp[i] == s2) return;
+        sp[n] = s2;
+        cp[n] = c;
+        n++;
+    };
+    add(h);
+    const int cap = 4 * h < 64 ? 4 * h : 64;
+    for (int s = 1; s <= cap; s *= 2) add(s);
+    return n;
+}
+
+size_t tune_partial_bytes(const Plan &p, int sms) {
+    int sp[8], cp[8];
+    const int n = split_candidates(p, sms, sp, cp);
+    size_t b = 0;
+    for (int i = 0; i < n; i++) b = partial_bytes(p, sp[i]) > b ? partial_bytes(p, sp[i]) : b;
+    return b;
+}
+
+static std::string tune_key(const Plan &p);
+
+// the context's tuned choice for this shape, if any
+bool cached_split(Ctx *c, const Plan &p, int &split, int &cps) {
+    auto it = c->split_cache.find(tune_key(p));
+    if (it == c->split_cache.end()) return false;
+    split = it->second.first;
+    cps = it->second.second;
+    return true;
+}
+
+static std::string tune_key(const Plan &p) {
+    char k[256];
+    snprintf(k, sizeof(k), "%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d", p.implicit, p.src_mode, p.M, p.N, p.C, p.kblocks,
+             p.ntiles_n, p.tiles_m, p.Wt, p.Ht, p.Nt, p.f, p.colmajor);
+    return k;
+}
+
+// Picks split / cps for the plan: the context's cached choice for this shape,
+// else (autotuning on, no stream capture in progress) the fastest candidate
+// by CUDA-event time (one warm-up and two timed runs each, on the context's
+// stream, with the caller's operands and outputs: every candidate computes
+// the same result; another split must beat the heuristic one by 3 %), else
+// the heuristic. partial must hold
+// tune_partial_bytes(p) when tuning can run.
+int tune_split(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial,
+               uint64_t *const out[6], const uint64_t *const bias[6], int trunc, bool zeros_kept, uint64_t *raw,
+               int &split, int &cps) {
+    const int sms = c->sm_count > 0 ? c->sm_count : 148;
+    const std::string key = tune_key(p);
+    auto it = c->split_cache.find(key);
+    if (it != c->split_cache.end()) {
+        split = it->second.first;
+        cps = it->second.second;
+        return PG_OK;
+    }
+    choose_split(p, sms, split, cps);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    PG_CHECK_CUDA(c, cudaStreamIsCapturing(c->stream, &cs));
+    if (!c->autotune || cs != cudaStreamCaptureStatusNone) return PG_OK;
+    int sp[8], cp[8];
+    const int n = split_candidates(p, sms, sp, cp);
+    if (n <= 1) {
+        c->split_cache[key] = {split, cps};
+        return PG_OK;
+    }
+    cudaEvent_t e0, e1;
+    PG_CHECK_CUDA(c, cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return set_error(c, PG_ERR_CUDA, "cudaEventCreate failed");
+    }
+    float best = 0.f, href = -1.f;
+    int st = PG_OK;
+    for (int i = 0; i < n && st == PG_OK; i++) {
+        uint64_t *part = sp[i] > 1 ? partial : nullptr;
+        float ms = 0.f;
+        for (int r = 0; r < 3 && st == PG_OK; r++) {
+            if (r == 1 && cudaEventRecord(e0, c->stream) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event record");
+            if (!st) st = run_gemm(c, p, image, packB, part, sp[i], cp[i], out, bias, trunc, zeros_kept, raw);
+        }
+        if (!st && cudaEventRecord(e1, c->stream) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event record");
+        if (!st && cudaEventSynchronize(e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event synchronize");
+        if (!st && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event time");
+        // candidate 0 is the heuristic; another one must beat it by 3 %
+        if (!st && (i == 0 || ms < best * (best == href ? 0.97f : 1.f))) {
+            best = ms;
+            split = sp[i];
+            cps = cp[i];
+        }
+        if (i == 0) href = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) return st;
+    c->split_cache[key] = {split, cps};
+    return PG_OK;
+}
+
 int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image) {
     ImageArgs ia;
     memset(&ia, 0, sizeof(ia));
@@ -1088,15 +1201,15 @@ static int run_with_scratch(Ctx *c, const lt::Plan &p, const uint64_t *const a[6
                             uint64_t *const out[6], const uint64_t *const bias[6], int trunc) {
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     int split, cps;
-    lt::choose_split(p, c->sm_count > 0 ? c->sm_count : 148, split, cps);
-    const size_t ib = al(p.image_bytes), pb = al(p.packB_bytes), qb = al(lt::partial_bytes(p, split));
+    const size_t ib = al(p.image_bytes), pb = al(p.packB_bytes);
+    const size_t qb = al(lt::tune_partial_bytes(p, c->sm_count > 0 ? c->sm_count : 148));
     uint8_t *scr = (uint8_t *)scratch(c, ib + pb + qb);
     if (!scr) return PG_ERR_NO_MEMORY;
+    uint64_t *part = (uint64_t *)(scr + ib + pb);
     int st = lt::run_image(c, p, a, scr);
     if (!st) st = lt::run_pack(c, p, b, scr + ib);
-    if (!st)
-        st = lt::run_gemm(c, p, scr, scr + ib, split > 1 ? (uint64_t *)(scr + ib + pb) : nullptr, split, cps, out,
-                          bias, trunc);
+    if (!st) st = lt::tune_split(c, p, scr, scr + ib, part, out, bias, trunc, false, nullptr, split, cps);
+    if (!st) st = lt::run_gemm(c, p, scr, scr + ib, split > 1 ? part : nullptr, split, cps, out, bias, trunc);
     if (st) return st;
     comm_msg(c, 2ull * p.M * p.N * 8, 2ull * p.M * p.N * 8);
     comm_round(c);
@@ -1149,16 +1262,18 @@ int limb3_rss_conv_u64(Ctx *c, const uint64_t *const A[6], const uint64_t *const
     if ((st = lt::plan_gemm(c, p, (int)Mcols, f * f * Din, Dout, 1, 1, 1))) return st;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     int split, cps;
-    lt::choose_split(p, c->sm_count > 0 ? c->sm_count : 148, split, cps);
-    const size_t ib = al(p.image_bytes), pb = al(p.packB_bytes), qb = al(lt::partial_bytes(p, split));
+    const size_t ib = al(p.image_bytes), pb = al(p.packB_bytes);
+    const size_t qb = al(lt::tune_partial_bytes(p, c->sm_count > 0 ? c->sm_count : 148));
     const size_t cb_bytes = al((size_t)p.M * p.N * 8);
     uint8_t *scr = (uint8_t *)scratch(c, ib + pb + qb + cb_bytes);
     if (!scr) return PG_ERR_NO_MEMORY;
+    uint64_t *part = (uint64_t *)(scr + ib + pb);
     uint64_t *cols = (uint64_t *)(scr + ib + pb + qb);
     if ((st = lt::run_image(c, p, A, scr))) return st;
     if ((st = lt::run_pack(c, p, B, scr + ib))) return st;
-    if ((st = lt::run_gemm(c, p, scr, scr + ib, split > 1 ? (uint64_t *)(scr + ib + pb) : nullptr, split, cps, C,
-                           nullptr, trunc, false, cols)))
+    if ((st = lt::tune_split(c, p, scr, scr + ib, part, C, nullptr, trunc, false, cols, split, cps))) return st;
+    if ((st = lt::run_gemm(c, p, scr, scr + ib, split > 1 ? part : nullptr, split, cps, C, nullptr, trunc, false,
+                           cols)))
         return st;
     lt::Col2ImArgs a2;
     memset(&a2, 0, sizeof(a2));
@@ -1201,7 +1316,7 @@ int limb_rss_matmul_u64_fixed(Ctx *c, uint8_t *scr, size_t cap, const uint64_t *
     if (st) return st;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     int split, cps;
-    lt::choose_split(p, c->sm_count > 0 ? c->sm_count : 148, split, cps);
+    if (!lt::cached_split(c, p, split, cps)) lt::choose_split(p, c->sm_count > 0 ? c->sm_count : 148, split, cps);
     const size_t ib = al(p.image_bytes), pb = al(p.packB_bytes);
     if (ib + pb + al(lt::partial_bytes(p, split)) > cap) {
         split = 1;

@@ -36,6 +36,13 @@ int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout
 int plan_wgrad(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad);
 void choose_split(const Plan &p, int sms, int &split, int &chunks_per_split);
 size_t partial_bytes(const Plan &p, int split);
+// the split-K autotuner: partial bytes that every candidate fits in, and the
+// choice (cached per shape in the context; timed when the context allows)
+size_t tune_partial_bytes(const Plan &p, int sms);
+bool cached_split(Ctx *c, const Plan &p, int &split, int &chunks_per_split);
+int tune_split(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial,
+               uint64_t *const out[6], const uint64_t *const bias[6], int trunc, bool zeros_kept, uint64_t *raw,
+               int &split, int &chunks_per_split);
 // A shares -> digit-plane image; weight shares -> packed stage images; then the GEMM (+ split-K reduction)
 int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image);
 int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB);

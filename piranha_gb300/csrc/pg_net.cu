@@ -112,7 +112,7 @@ static int net_limb_setup(pg_net *net) {
         if (st) return st;
         lt::choose_split(L.plan, sms, L.split, L.cps);
         image = image > L.plan.image_bytes ? image : L.plan.image_bytes;
-        const size_t pb = lt::partial_bytes(L.plan, L.split);
+        const size_t pb = lt::tune_partial_bytes(L.plan, sms);
         partial = partial > pb ? partial : pb;
         packs += al(L.plan.packB_bytes);
     }
@@ -132,6 +132,17 @@ static int net_limb_setup(pg_net *net) {
         L.packB = ptr;
         ptr += al(L.plan.packB_bytes);
         int st = lt::run_pack(c, L.plan, (const uint64_t *const *)L.w, L.packB);
+        if (st) return st;
+    }
+    // split-K of every layer, timed on a zero image into the layer's own
+    // outputs (the forward overwrites them; without a bias only the value
+    // shares are written, so the zero shares stay 0)
+    PG_CHECK_CUDA(c, cudaMemsetAsync(net->limb_image, 0, al(image), c->stream));
+    for (auto &L : net->layers) {
+        if (L.type != PG_LAYER_FC && L.type != PG_LAYER_CNN) continue;
+        const uint64_t *const *bias = L.b_n ? (const uint64_t *const *)L.b : nullptr;
+        int st = lt::tune_split(c, L.plan, net->limb_image, L.packB, net->limb_partial, L.out, bias, net->fp,
+                                bias == nullptr, nullptr, L.split, L.cps);
         if (st) return st;
     }
     return PG_OK;

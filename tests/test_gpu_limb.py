@@ -166,3 +166,40 @@ def test_limb_vgg16_forward(pg):
     for i, (g, w) in enumerate(zip(got_outs, want_outs)):
         assert np.array_equal(g, w), f"layer {i} {layers[i]}"
     assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 64, 4096), (256, 200, 1000), (2, 10, 784)])
+def test_limb_split_autotune(pg, M, N, K):
+    """The split-K autotuner (timed candidates, cached per shape) and the
+    heuristic split give the same bits as the oracle."""
+    A = orc.random_views(M * K, U64, 41)
+    B = orc.random_views(K * N, U64, 42)
+    want = orc.matmul(A, B, M, N, K, 1, 1, 1, 26)
+    for tune in (True, False):
+        c = pg.Context(0, form=pg.FORM_LIMB_TC)
+        c.set_autotune(tune)
+        for _ in range(2):  # the second call uses the cached choice
+            C = pg.empty_shares(M * N)
+            pg.matmul(c, pg.to_device(A), pg.to_device(B), C, M, N, K, 1, 1, 1, 26)
+            c.check_device_errors()
+            assert np.array_equal(pg.to_host(C), want)
+        c.close()
+
+
+def test_alloc_shares(pg, ctx):
+    import torch
+
+    vp = ctypes.c_void_p
+    out = (vp * 6)()
+    ctx._check(pg.lib().pg_alloc_shares(ctx.handle, 6, 1000, 8, out))
+    ptrs = [out[i] for i in range(6)]
+    assert all(p % 256 == 0 for p in ptrs) and len(set(ptrs)) == 6
+    ctx.sync()
+
+    class _A:
+        def __init__(self, p):
+            self.__cuda_array_interface__ = {"shape": (1000,), "typestr": "<i8", "data": (p, False), "version": 3}
+
+    for p in ptrs:
+        assert int(torch.as_tensor(_A(p), device="cuda").abs().sum()) == 0
+    ctx._check(pg.lib().pg_free_shares(ctx.handle, vp(ptrs[0])))
