@@ -63,6 +63,12 @@ int pg_ctx_get_form(pg_ctx *ctx);
  * of each problem shape (default on; off = the heuristic, and the cache is
  * cleared). Never tunes inside a stream capture. */
 int pg_ctx_set_autotune(pg_ctx *ctx, int on);
+/* The tuned choices as a text file (first line "pg-tune <SM count>"; a file
+ * from a GPU with another SM count is refused). With the environment variable
+ * PG_TUNE_CACHE set to a path, every context loads it when created and
+ * merges its own choices into it when destroyed. */
+int pg_tune_load(pg_ctx *ctx, const char *path);
+int pg_tune_save(pg_ctx *ctx, const char *path);
 /* Device share buffers, as the reference's share classes own them (RSS<T>:
  * 6 buffers [party*2 + share], TPC<T>: 2, FPC<T>: 12 [party*3 + share];
  * DeviceData.h:51-85): nbuf zeroed buffers of n elements of elem_bytes (1, 4

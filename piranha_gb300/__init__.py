@@ -162,6 +162,8 @@ def _declare(lib):
     lib.pg_reference_init_normal.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_size_t, ctypes.c_int,
                                              ctypes.c_double]
     lib.pg_ctx_set_autotune.argtypes = [vp, ctypes.c_int]
+    lib.pg_tune_load.argtypes = [vp, ctypes.c_char_p]
+    lib.pg_tune_save.argtypes = [vp, ctypes.c_char_p]
     lib.pg_alloc_shares.argtypes = [vp, ctypes.c_int, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(vp)]
     lib.pg_free_shares.argtypes = [vp, vp]
     lib.pg_graph_begin.argtypes = [vp]
@@ -278,6 +280,12 @@ class Context:
     def set_autotune(self, on: bool):
         """Split-K of the limb-form GEMMs by timing (default on) or by the heuristic."""
         self._check(lib().pg_ctx_set_autotune(self._h, 1 if on else 0))
+
+    def tune_load(self, path: str):
+        self._check(lib().pg_tune_load(self._h, os.fsencode(path)))
+
+    def tune_save(self, path: str):
+        self._check(lib().pg_tune_save(self._h, os.fsencode(path)))
 
     def capture(self) -> _Capture:
         """``with ctx.capture() as g: ...`` records every call on this

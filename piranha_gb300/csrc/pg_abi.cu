@@ -2,6 +2,7 @@
 // context lifetime, status/error reporting, communication counters, and thin
 // wrappers that forward to the templated kernels of the other translation
 // units.
+#include <cstdlib>
 #include <cstring>
 #include <random>
 
@@ -102,6 +103,54 @@ using namespace pg;
 
 extern "C" {
 
+}  // extern "C"
+
+// Tuning cache file: a header line "pg-tune <SM count>", then one
+// "<shape key> <split> <chunks per split>" per line. A file written on a GPU
+// with another SM count is ignored.
+static int tune_load(pg::Ctx *c, const char *path, bool keep_own = false) {
+    FILE *f = fopen(path, "r");
+    if (!f) return PG_ERR_INVALID_ARG;
+    int sms = -1;
+    if (fscanf(f, "pg-tune %d", &sms) != 1 || sms != c->sm_count) {
+        fclose(f);
+        return PG_ERR_UNSUPPORTED;
+    }
+    char key[256];
+    int sp, cp;
+    while (fscanf(f, "%255s %d %d", key, &sp, &cp) == 3)
+        if (sp >= 1 && cp >= 1 && !(keep_own && c->split_cache.count(key))) c->split_cache[key] = {sp, cp};
+    fclose(f);
+    return PG_OK;
+}
+
+static int tune_save(pg::Ctx *c, const char *path) {
+    // merge with what the file already holds (another context may have written it)
+    tune_load(c, path, true);
+    FILE *f = fopen(path, "w");
+    if (!f) return PG_ERR_INVALID_ARG;
+    fprintf(f, "pg-tune %d\n", c->sm_count);
+    for (const auto &e : c->split_cache) fprintf(f, "%s %d %d\n", e.first.c_str(), e.second.first, e.second.second);
+    fclose(f);
+    return PG_OK;
+}
+
+extern "C" {
+
+int pg_tune_load(pg_ctx *c, const char *path) {
+    CTX_OR_FAIL(c);
+    if (!path) return set_error(c, PG_ERR_INVALID_ARG, "null path");
+    const int st = tune_load(c, path);
+    return st ? set_error(c, st, "cannot read a tuning cache for %d SMs from %s", c->sm_count, path) : PG_OK;
+}
+
+int pg_tune_save(pg_ctx *c, const char *path) {
+    CTX_OR_FAIL(c);
+    if (!path) return set_error(c, PG_ERR_INVALID_ARG, "null path");
+    const int st = tune_save(c, path);
+    return st ? set_error(c, st, "cannot write the tuning cache %s", path) : PG_OK;
+}
+
 int pg_ctx_create(pg_ctx **out, int device) {
     if (!out) return PG_ERR_INVALID_ARG;
     *out = nullptr;
@@ -119,6 +168,7 @@ int pg_ctx_create(pg_ctx **out, int device) {
         delete c;
         return PG_ERR_CUDA;
     }
+    if (const char *tc = getenv("PG_TUNE_CACHE")) tune_load(c, tc);
     *out = c;
     return PG_OK;
 }
@@ -126,6 +176,8 @@ int pg_ctx_create(pg_ctx **out, int device) {
 int pg_ctx_destroy(pg_ctx *c) {
     CTX_OR_FAIL(c);
     cudaStreamSynchronize(c->stream);
+    if (const char *tc = getenv("PG_TUNE_CACHE"))
+        if (!c->split_cache.empty()) tune_save(c, tc);
     if (c->scratch) cudaFree(c->scratch);
     if (c->partial) cudaFree(c->partial);
     for (void *p : c->retired) cudaFree(p);

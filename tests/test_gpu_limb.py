@@ -203,3 +203,31 @@ def test_alloc_shares(pg, ctx):
     for p in ptrs:
         assert int(torch.as_tensor(_A(p), device="cuda").abs().sum()) == 0
     ctx._check(pg.lib().pg_free_shares(ctx.handle, vp(ptrs[0])))
+
+
+def test_tune_cache_round_trip(pg, tmp_path):
+    """Tuned split-K choices saved to a file and loaded into another context,
+    which then reuses them (same bits)."""
+    M, N, K = 128, 64, 2048
+    A = orc.random_views(M * K, U64, 51)
+    B = orc.random_views(K * N, U64, 52)
+    want = orc.matmul(A, B, M, N, K, 1, 1, 1, 26)
+    path = str(tmp_path / "tune.txt")
+    c1 = pg.Context(0, form=pg.FORM_LIMB_TC)
+    C = pg.empty_shares(M * N)
+    pg.matmul(c1, pg.to_device(A), pg.to_device(B), C, M, N, K, 1, 1, 1, 26)
+    c1.tune_save(path)
+    c1.close()
+    lines = open(path).read().split("\n")
+    assert lines[0].startswith("pg-tune ") and len([x for x in lines[1:] if x.strip()]) >= 1
+    c2 = pg.Context(0, form=pg.FORM_LIMB_TC)
+    c2.tune_load(path)
+    C2 = pg.empty_shares(M * N)
+    pg.matmul(c2, pg.to_device(A), pg.to_device(B), C2, M, N, K, 1, 1, 1, 26)
+    c2.check_device_errors()
+    assert np.array_equal(pg.to_host(C2), want) and np.array_equal(pg.to_host(C), want)
+    with open(path, "w") as f:
+        f.write("pg-tune 1\n")
+    with pytest.raises(pg.PiranhaError):
+        c2.tune_load(path)
+    c2.close()
