@@ -51,6 +51,7 @@ from piranha_gb300 import nets  # noqa: E402
 
 BATCH = 128
 SEED = 2024
+STREAM_BUCKETS = (1, 2, 4, 8, 12, 16, 24, 32, 40, 48, 56, 64)  # batch sizes of the stream's captured networks
 LIMB_FLOPS_PER_RING_MAC = 72  # 36 8-bit limb pairs x 2 flops: exact u64 MAC on fp16 tensor cores
 # DRAM bytes read + written by the 13 limb_tma_kernel launches of one VGG16
 # batch-128 forward, from the ncu capture summarised in
@@ -79,7 +80,8 @@ WORKLOADS = {
     "stream": {"metric": "3PC batched request stream img/s", "kind": "stream", "fp": 26, "ring": "u64",
                "requests": 512, "max_batch": 64,
                "desc": "512 requests, batch uniform in 1..64, SecureML or VGG16 (even odds), 3PC RSS, uint64 "
-                       "shares, FP 26; each request runs on a captured network of the next power-of-two batch"},
+                       "shares, FP 26; each request runs on a captured network of the smallest batch bucket "
+                       "(1, 2, 4, 8, 12, 16, 24, ..., 64) that holds it"},
 }
 _LAYERS = {"vgg16": nets.vgg16, "secureml": nets.secureml, "lenet-train": nets.lenet,
            "secureml-2pc": nets.secureml, "secureml-4pc": nets.secureml, "stream": nets.vgg16}
@@ -98,6 +100,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-u64-form comparison run")
     ap.add_argument("--sweep", action="store_true", help="gemm: also time M = N = K in 512..8192 in both forms")
+    ap.add_argument("--no-autotune", action="store_true", help="split-K by the heuristic instead of by timing")
     return ap.parse_args()
 
 
@@ -455,6 +458,7 @@ def bench_form(args, pg, torch, stream, dev, form, wl, batch, world):
     layers = wl["layers"]
     macs = ring_macs(layers, batch)
     ctx = pg.Context(dev.index, stream=stream, form=form)
+    ctx.set_autotune(not args.no_autotune)
     net = _setup_net(pg, ctx, dev, wl, batch, fp)
     net.enable_timing(True)
     net.capture()
@@ -529,6 +533,7 @@ def bench_train(args, pg, torch, stream, dev, form, wl, batch, world):
     layers = wl["layers"]
     macs = ring_macs(layers, batch)
     ctx = pg.Context(dev.index, stream=stream, form=form)
+    ctx.set_autotune(not args.no_autotune)
     net = _setup_net(pg, ctx, dev, wl, batch, fp)
     xin = pg.to_device(wl["x"], dev).reshape(-1)
     lin = pg.to_device(wl["labels"], dev).reshape(-1)
@@ -588,6 +593,7 @@ def _gemm_form(args, pg, torch, stream, dev, form, A, B, M, N, K, world, steps, 
     graph, warm-up and timed replays; optionally the end-to-end replays."""
     fp = WORKLOADS["gemm"]["fp"]
     ctx = pg.Context(dev.index, stream=stream, form=form)
+    ctx.set_autotune(not args.no_autotune)
     C = pg.empty_shares(M * N, device=dev)
     pg.matmul(ctx, A, B, C, M, N, K, 1, 1, 1, fp)
     with ctx.capture() as graph:
@@ -761,8 +767,9 @@ def bench_fcnet(args, pg, torch, stream, dev, wl, batch, world):
 
 def bench_stream(args, pg, torch, stream, dev, wl, world):
     """The request stream, served in arrival order on one stream: per request
-    its shares go into the input buffers of the captured network of the next
-    power-of-two batch (rows past the request's batch keep what an earlier
+    its shares go into the input buffers of the captured network of the
+    smallest batch bucket that holds it (1, 2, 4, 8, then steps of 8 up to 64
+    with 12 besides: at most 1/3 of a replay is padding; rows past the request's batch keep what an earlier
     request left there; every layer works image by image, so they do not
     touch the request's rows), the graph
     replays, and the request's output rows come back. Latency is a request's
@@ -774,13 +781,11 @@ def bench_stream(args, pg, torch, stream, dev, wl, world):
     fp = WORKLOADS["stream"]["fp"]
     form = pg.FORM_U64 if args.form == "u64" else pg.FORM_LIMB_TC
     ctx = pg.Context(dev.index, stream=stream, form=form)
+    ctx.set_autotune(not args.no_autotune)
     nets_ = {}
 
     def bucket(b):
-        p = 1
-        while p < b:
-            p *= 2
-        return p
+        return next(x for x in STREAM_BUCKETS if x >= b)
 
     for m, b, _ in reqs:
         key = (m, bucket(b))

@@ -1003,7 +1003,8 @@ static std::string tune_key(const Plan &p) {
 
 // Picks split / cps for the plan: the context's cached choice for this shape,
 // else (autotuning on, no stream capture in progress) the fastest candidate
-// by CUDA-event time (one warm-up and two timed runs each, on the context's
+// by CUDA-event time (one warm-up and two timed runs each — more for runs
+// under a quarter millisecond — on the context's
 // stream, with the caller's operands and outputs: every candidate computes
 // the same result; another split must beat the heuristic one by 3 %), else
 // the heuristic. partial must hold
@@ -1040,13 +1041,26 @@ int tune_split(Ctx *c, const Plan &p, const void *image, const void *packB, uint
     for (int i = 0; i < n && st == PG_OK; i++) {
         uint64_t *part = sp[i] > 1 ? partial : nullptr;
         float ms = 0.f;
-        for (int r = 0; r < 3 && st == PG_OK; r++) {
-            if (r == 1 && cudaEventRecord(e0, c->stream) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event record");
-            if (!st) st = run_gemm(c, p, image, packB, part, sp[i], cp[i], out, bias, trunc, zeros_kept, raw);
+        // one warm-up run, then 2 timed runs; short runs are timed again over
+        // enough repetitions to fill about half a millisecond
+        int reps = 2;
+        for (int pass = 0; pass < 2 && st == PG_OK; pass++) {
+            for (int r = pass ? 1 : 0; r <= reps && st == PG_OK; r++) {
+                if (r == 1 && cudaEventRecord(e0, c->stream) != cudaSuccess)
+                    st = set_error(c, PG_ERR_CUDA, "event record");
+                if (!st) st = run_gemm(c, p, image, packB, part, sp[i], cp[i], out, bias, trunc, zeros_kept, raw);
+            }
+            if (!st && cudaEventRecord(e1, c->stream) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event record");
+            if (!st && cudaEventSynchronize(e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event synchronize");
+            if (!st && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event time");
+            if (st) break;
+            ms /= (float)reps;
+            if (pass == 0) {
+                if (ms * reps >= 0.3f) break;
+                reps = (int)(0.5f / (ms > 1e-3f ? ms : 1e-3f)) + 1;
+                if (reps > 64) reps = 64;
+            }
         }
-        if (!st && cudaEventRecord(e1, c->stream) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event record");
-        if (!st && cudaEventSynchronize(e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event synchronize");
-        if (!st && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event time");
         // candidate 0 is the heuristic; another one must beat it by 3 %
         if (!st && (i == 0 || ms < best * (best == href ? 0.97f : 1.f))) {
             best = ms;
