@@ -155,6 +155,21 @@ int pg_rss_divide_public_u32(pg_ctx *ctx, uint32_t *const a[6], size_t n, uint32
 int pg_rss_reconstruct_u64(pg_ctx *ctx, const uint64_t *const a[6], size_t n, uint64_t *const out[3]);
 int pg_rss_reconstruct_u8(pg_ctx *ctx, const uint8_t *const a[6], size_t n, uint8_t *const out[3]);
 /* reshare (RSS.inl:1053-1074): out_p = (c_p, c_{next(p)}) */
+/* Counter-mode AES generator of AESObject (src/mpc/AESObject.cpp:9-91):
+ * block k = AES-256-ECB_key(LE64(k) || LE64(k)); out[j] = 64-bit lane (j & 1)
+ * of block counter + j / 2, i.e. the uint64 stream of getRandom from that
+ * counter. The key is the first 32 bytes of the reference's key file (its
+ * text up to the first NUL, zero-padded). Device output. */
+int pg_prg_fill_u64(pg_ctx *ctx, const uint8_t key[32], uint64_t counter, uint64_t *out, size_t n);
+/* Live resharing masks (the reference leaves rndMask = c, RSS.inl:1053-1074):
+ * keys = 3 x 32 bytes, key p shared by party p and party p+1; reshare, *= and
+ * &= then add alpha_p = G(key p) - G(key p-1) to party p's value (XOR of the
+ * low bits for u8 bit shares, full-width XOR for u64 &=), which sums to zero,
+ * drawing from one context counter that starts at `counter` and advances by
+ * ceil(n / 2) blocks per step. keys = NULL turns them off. The fused dReLU /
+ * ReLU / maxpool kernels and the GEMM epilogues keep the reference's masks. */
+int pg_prg_set_keys(pg_ctx *ctx, const uint8_t *keys, uint64_t counter);
+int pg_prg_counter(pg_ctx *ctx, uint64_t *counter);
 int pg_rss_reshare_u64(pg_ctx *ctx, const uint64_t *const c[3], size_t n, uint64_t *const out[6]);
 /* RSS *= RSS and RSS &= RSS (RSS.inl:284-345), in place on a */
 int pg_rss_mul_u64(pg_ctx *ctx, uint64_t *const a[6], const uint64_t *const b[6], size_t n);

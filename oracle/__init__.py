@@ -40,7 +40,7 @@ _CT = {np.uint64: ctypes.c_uint64, np.uint32: ctypes.c_uint32, np.uint8: ctypes.
 
 def build() -> str:
     """Compile the oracle with its Makefile (idempotent); return the .so path."""
-    srcs = [os.path.join(_HERE, f) for f in ("capi.cpp", "oracle.hpp")]
+    srcs = [os.path.join(_HERE, f) for f in ("capi.cpp", "oracle.hpp", "aes.hpp")]
     if os.path.exists(_LIB_PATH) and all(os.path.getmtime(_LIB_PATH) >= os.path.getmtime(s) for s in srcs):
         return _LIB_PATH
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
@@ -779,3 +779,35 @@ def fpc_maxpool(x, k, udtype=np.uint8, comm=None):
     getattr(lib(), f"or_fpc_maxpool_{_bits_suffix(dt, udtype)}")(_p(x), ctypes.c_size_t(n), k, _p(out), _p(dout),
                                                                  comm.ptr())
     return out, dout
+
+
+# ---------------------------------------------------------------- generator
+
+def aes256_encrypt(key: bytes, block: bytes) -> bytes:
+    """One AES-256 block (FIPS-197), restated byte by byte."""
+    assert len(key) == 32 and len(block) == 16
+    out = ctypes.create_string_buffer(16)
+    lib().or_aes256_encrypt(key, block, out)
+    return out.raw
+
+
+def prg_fill_u64(key: bytes, counter: int, n: int) -> np.ndarray:
+    """AESObject's uint64 stream from block `counter` (src/mpc/AESObject.cpp:40-91)."""
+    assert len(key) == 32
+    out = np.zeros(n, dtype=np.uint64)
+    lib().or_prg_fill_u64(key, ctypes.c_uint64(counter), _p(out), ctypes.c_size_t(n))
+    return out
+
+
+def prg_masks(keys, counter: int, n: int, xor: bool = False, bits: bool = False) -> np.ndarray:
+    """The resharing masks alpha_p = G(key p) - G(key p-1) (or XOR; low bit for
+    bit shares) of n elements from block `counter`, as (3, n)."""
+    g = [prg_fill_u64(k, counter, n) for k in keys]
+    out = np.zeros((3, n), dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        for p in range(3):
+            q = (p + 2) % 3
+            out[p] = (g[p] ^ g[q]) if xor else (g[p] - g[q])
+    if bits:
+        out &= np.uint64(1)
+    return out

@@ -4,6 +4,7 @@
 // [party(3)][share(2)][n]; per-party public data as [party(3)][n]. The comm
 // argument points at 9 uint64 counters {tx[4], rx[4], rounds} that each call
 // adds to (DeviceData.h:87-118 byte accounting, one round per protocol step).
+#include "aes.hpp"
 #include "oracle.hpp"
 
 using namespace oracle;
@@ -572,3 +573,11 @@ OR_FPC(uint8_t, u8)
 OR_FPC_BITS(uint64_t, uint8_t, u64_u8)
 OR_FPC_BITS(uint64_t, uint64_t, u64_u64)
 OR_FPC_BITS(uint32_t, uint8_t, u32_u8)
+
+// AESObject's counter-mode stream (aes.hpp) and one AES-256 block
+extern "C" void or_prg_fill_u64(const uint8_t* key, uint64_t ctr, uint64_t* out, size_t n) {
+    prg_fill_u64(key, ctr, out, n);
+}
+extern "C" void or_aes256_encrypt(const uint8_t* key, const uint8_t* in, uint8_t* out) {
+    aes256_encrypt_block(key, in, out);
+}

@@ -162,6 +162,9 @@ def _declare(lib):
     lib.pg_reference_init_normal.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_size_t, ctypes.c_int,
                                              ctypes.c_double]
     lib.pg_ctx_set_autotune.argtypes = [vp, ctypes.c_int]
+    lib.pg_prg_fill_u64.argtypes = [vp, ctypes.c_char_p, ctypes.c_uint64, vp, ctypes.c_size_t]
+    lib.pg_prg_set_keys.argtypes = [vp, ctypes.c_char_p, ctypes.c_uint64]
+    lib.pg_prg_counter.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
     lib.pg_tune_load.argtypes = [vp, ctypes.c_char_p]
     lib.pg_tune_save.argtypes = [vp, ctypes.c_char_p]
     lib.pg_alloc_shares.argtypes = [vp, ctypes.c_int, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(vp)]
@@ -286,6 +289,28 @@ class Context:
 
     def tune_save(self, path: str):
         self._check(lib().pg_tune_save(self._h, os.fsencode(path)))
+
+    def prg_fill(self, key: bytes, counter: int, out):
+        """The reference generator's uint64 stream from `counter` into a CUDA int64 tensor."""
+        if len(key) != 32:
+            raise ValueError("AES-256 key of 32 bytes")
+        self._check(lib().pg_prg_fill_u64(self._h, key, counter, ctypes.c_void_p(out.data_ptr()), out.numel()))
+        return out
+
+    def set_prg_keys(self, keys, counter: int = 0):
+        """Live resharing masks from three 32-byte pairwise keys (None: off)."""
+        if keys is None:
+            self._check(lib().pg_prg_set_keys(self._h, None, 0))
+            return
+        blob = b"".join(keys)
+        if len(keys) != 3 or len(blob) != 96:
+            raise ValueError("three 32-byte keys")
+        self._check(lib().pg_prg_set_keys(self._h, blob, counter))
+
+    def prg_counter(self) -> int:
+        v = ctypes.c_uint64()
+        self._check(lib().pg_prg_counter(self._h, ctypes.byref(v)))
+        return v.value
 
     def capture(self) -> _Capture:
         """``with ctx.capture() as g: ...`` records every call on this

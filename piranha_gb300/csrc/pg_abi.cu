@@ -59,6 +59,8 @@ void *scratch(Ctx *c, size_t bytes) { return grow(c, c->scratch, c->scratch_byte
 void *gemm_partial(Ctx *c, size_t bytes) { return grow(c, c->partial, c->partial_bytes, bytes, "split-K buffer"); }
 
 // kernels in other translation units
+int prg_fill_u64(Ctx *, const uint8_t *, uint64_t, uint64_t *, size_t);
+int prg_set_keys(Ctx *, const uint8_t *, uint64_t);
 template <typename T>
 int rss_matmul(Ctx *, const T *const *, const T *const *, T *const *, const T *const *, int, int, int, int, int, int,
                int);
@@ -409,6 +411,20 @@ int pg_rss_reconstruct_u64(pg_ctx *c, const uint64_t *const a[6], size_t n, uint
 int pg_rss_reconstruct_u8(pg_ctx *c, const uint8_t *const a[6], size_t n, uint8_t *const out[3]) {
     CTX_OR_FAIL(c);
     return rss_reconstruct<uint8_t>(c, a, n, out);
+}
+int pg_prg_fill_u64(pg_ctx *c, const uint8_t key[32], uint64_t counter, uint64_t *out, size_t n) {
+    CTX_OR_FAIL(c);
+    return prg_fill_u64(c, key, counter, out, n);
+}
+int pg_prg_set_keys(pg_ctx *c, const uint8_t *keys, uint64_t counter) {
+    CTX_OR_FAIL(c);
+    return prg_set_keys(c, keys, counter);
+}
+int pg_prg_counter(pg_ctx *c, uint64_t *out) {
+    CTX_OR_FAIL(c);
+    if (!out) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+    *out = c->prg_ctr;
+    return PG_OK;
 }
 int pg_rss_reshare_u64(pg_ctx *c, const uint64_t *const cin[3], size_t n, uint64_t *const out[6]) {
     CTX_OR_FAIL(c);

@@ -48,6 +48,11 @@ struct Ctx {
     // (split, chunks per split) per problem shape
     int autotune = 1;
     std::unordered_map<std::string, std::pair<int, int>> split_cache;
+    // AES counter-mode masks of the resharing steps (off: the reference's
+    // unfilled masks); round keys of the three pairwise keys and the next block
+    bool prg_on = false;
+    uint32_t prg_rk[3][60];
+    uint64_t prg_ctr = 0;
 };
 
 int set_error(Ctx *c, int code, const char *fmt, ...);

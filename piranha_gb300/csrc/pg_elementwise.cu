@@ -6,6 +6,9 @@
 
 namespace pg {
 
+template <typename T> int rss_reshare_prg(Ctx *, const T *const *, size_t, T *const *);
+template <typename T, bool AND> int rss_mul_prg(Ctx *, T *const *, const T *const *, size_t);
+
 static unsigned grid1(Ctx *c, size_t n, int threads = 256) {
     size_t b = (n + threads - 1) / threads;
     size_t cap = (size_t)(c->sm_count > 0 ? c->sm_count : 148) * 32;
@@ -172,6 +175,7 @@ template <typename T> int rss_reconstruct(Ctx *c, const T *const a[6], size_t n,
 }
 
 template <typename T> int rss_reshare(Ctx *c, const T *const cin[3], size_t n, T *const out[6]) {
+    if (c->prg_on) return rss_reshare_prg<T>(c, cin, n, out);
     Sh6<T> o;
     if (!cin || !cin[0] || !cin[1] || !cin[2] || !load6(o, out)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
     Pub3<T> ci{{(T *)cin[0], (T *)cin[1], (T *)cin[2]}};
@@ -187,6 +191,7 @@ template <typename T> int rss_reshare(Ctx *c, const T *const cin[3], size_t n, T
 }
 
 template <typename T, bool AND> int rss_mul(Ctx *c, T *const a[6], const T *const b[6], size_t n) {
+    if (c->prg_on) return rss_mul_prg<T, AND>(c, a, b, n);
     Sh6<T> ca;
     CSh6<T> cb;
     if (!load6(ca, a) || !load6(cb, b)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
