@@ -92,3 +92,12 @@ def one_hot(classes_per_row, n_classes: int) -> np.ndarray:
     y = np.zeros((len(classes_per_row), n_classes))
     y[np.arange(len(classes_per_row)), np.asarray(classes_per_row)] = 1.0
     return y.ravel()
+
+
+def aes_key_from_file(path) -> bytes:
+    """The 32-byte AES-256 key of a reference key file (AESObject::AESObject,
+    src/mpc/AESObject.cpp:9-34): the file's text up to its first NUL,
+    zero-padded (or cut) to 32 bytes."""
+    data = open(path, "rb").read()
+    data = data.split(b"\0", 1)[0]
+    return (data + bytes(32))[:32]

@@ -110,3 +110,13 @@ def test_reference_init_layers():
     assert np.array_equal(params[2][1], enc.set_public(np.full(128, 0.01)))
     lp = nets.reference_init(nets.lenet())
     assert lp[0][1] is None and lp[0][0].shape == (3, 2, 20 * 25)
+
+
+def test_aes_key_from_file(tmp_path):
+    f = tmp_path / "key"
+    f.write_bytes(b"short key\n")
+    assert enc.aes_key_from_file(f) == b"short key\n" + bytes(22)
+    f.write_bytes(b"k" * 40)
+    assert enc.aes_key_from_file(f) == b"k" * 32
+    f.write_bytes(b"abc\0def")
+    assert enc.aes_key_from_file(f) == b"abc" + bytes(29)
