@@ -56,7 +56,7 @@ LIMB_FLOPS_PER_RING_MAC = 72  # 36 8-bit limb pairs x 2 flops: exact u64 MAC on 
 # DRAM bytes read + written by the 13 limb_tma_kernel launches of one VGG16
 # batch-128 forward, from the ncu capture summarised in
 # profiles/limb_tma_kernel_vgg16_b128_dram.md (the command is given there)
-VGG16_B128_LIMB_TRAFFIC = 4_662_534_144
+VGG16_B128_LIMB_TRAFFIC = 4_803_831_040
 
 WORKLOADS = {
     "vgg16": {"metric": "3PC VGG16 secure inference img/s", "kind": "infer3", "fp": 26, "ring": "u64",
