@@ -399,6 +399,19 @@ def _setup_net(pg, ctx, dev, wl, batch, fp):
     return net
 
 
+def max_over_ranks(torch, dev, values):
+    """Every rank's timings replaced by their maximum over the ranks (the job
+    is as slow as its slowest replica)."""
+    t = torch.tensor(values, device=dev, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
+def aggregate(world, units_per_step, steps, seconds):
+    """Whole-job throughput: every replica's units over the slowest replica's time."""
+    return world * units_per_step * steps / seconds
+
+
 def _timed(args, torch, stream, dev, world, step, flush, per_step=None):
     """K timed steps with an L2 flush before each (outside the event pair)."""
     if world > 1:
@@ -425,9 +438,7 @@ def _timed(args, torch, stream, dev, world, step, flush, per_step=None):
     clocks = sampler.stop()
     dev_s = sum(step_ms) / 1e3
     if world > 1:
-        t = torch.tensor([dev_s, wall], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_s, wall = float(t[0]), float(t[1])
+        dev_s, wall = max_over_ranks(torch, dev, [dev_s, wall])
     return dev_s, wall, clocks
 
 
@@ -446,9 +457,7 @@ def _e2e(args, torch, stream, dev, world, step, flush):
         ms.append(e0.elapsed_time(e1))
     s = sum(ms) / 1e3
     if world > 1:
-        t = torch.tensor([s], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        s = float(t[0])
+        (s,) = max_over_ranks(torch, dev, [s])
     return s
 
 
@@ -480,7 +489,7 @@ def bench_form(args, pg, torch, stream, dev, form, wl, batch, world):
     dev_s, wall, clocks = _timed(args, torch, stream, dev, world, net.forward_resident, flush, acc_layers)
     launches = ctx.kernel_launches() - launches0
     comm1 = ctx.comm()
-    value = world * batch * args.steps / dev_s
+    value = aggregate(world, batch, args.steps, dev_s)
 
     # dominant kernel: the fused share-GEMM of the conv layers (FC layers when there are none)
     gemm_idx = sorted(i for i in macs if layers[i][0] == "cnn") or sorted(macs)
@@ -507,7 +516,7 @@ def bench_form(args, pg, torch, stream, dev, form, wl, batch, world):
         "value": value,
         "ms_per_step": 1e3 * dev_s / args.steps,
         "wall_s": wall,
-        "e2e": {"value": world * batch * args.steps / e2e_s, "unit": "img/s",
+        "e2e": {"value": aggregate(world, batch, args.steps, e2e_s), "unit": "img/s",
                 "h2d_bytes_per_step": 6 * net.in_n * 8, "d2h_bytes_per_step": 6 * net.out_n * 8},
         "gpu_launches": int(launches),
         "clocks": clocks,
@@ -550,7 +559,7 @@ def bench_train(args, pg, torch, stream, dev, form, wl, batch, world):
     dev_s, wall, clocks = _timed(args, torch, stream, dev, world, net.train_resident, flush)
     launches = ctx.kernel_launches() - launches0
     comm1 = ctx.comm()
-    value = world * batch * args.steps / dev_s
+    value = aggregate(world, batch, args.steps, dev_s)
     # forward share-GEMMs plus the backward's two per layer (input gradient, weight gradient)
     total_macs = 3 * sum(macs.values())
     achieved = total_macs * LIMB_FLOPS_PER_RING_MAC / (dev_s / args.steps) / 1e12
@@ -570,7 +579,7 @@ def bench_train(args, pg, torch, stream, dev, form, wl, batch, world):
         "value": value,
         "ms_per_step": 1e3 * dev_s / args.steps,
         "wall_s": wall,
-        "e2e": {"value": world * batch * args.steps / e2e_s, "unit": "img/s",
+        "e2e": {"value": aggregate(world, batch, args.steps, e2e_s), "unit": "img/s",
                 "h2d_bytes_per_step": 6 * (net.in_n + net.out_n) * 8, "d2h_bytes_per_step": 6 * net.out_n * 8},
         "gpu_launches": int(launches),
         "clocks": clocks,
@@ -645,10 +654,10 @@ def bench_gemm(args, pg, torch, stream, dev, wl, world):
     out = {
         "form": "limb_tc" if form == pg.FORM_LIMB_TC else "u64",
         "unit": "ring-MAC/s",
-        "value": world * macs * args.steps / r["dev_s"],
+        "value": aggregate(world, macs, args.steps, r["dev_s"]),
         "ms_per_step": 1e3 * r["dev_s"] / args.steps,
         "wall_s": r["wall"],
-        "e2e": {"value": world * macs * args.steps / r["e2e_s"], "unit": "ring-MAC/s",
+        "e2e": {"value": aggregate(world, macs, args.steps, r["e2e_s"]), "unit": "ring-MAC/s",
                 "h2d_bytes_per_step": int(A.numel() + B.numel()) * 8, "d2h_bytes_per_step": int(c_h.numel()) * 8},
         "gpu_launches": int(r["launches"]),
         "clocks": r["clocks"],
@@ -730,7 +739,7 @@ def bench_fcnet(args, pg, torch, stream, dev, wl, batch, world):
     dev_s, wall, clocks = _timed(args, torch, stream, dev, world, graph.launch, flush)
     launches = ctx.kernel_launches() - launches0
     comm1 = ctx.comm(w["parties"])
-    value = world * batch * args.steps / dev_s
+    value = aggregate(world, batch, args.steps, dev_s)
     macs = sum(batch * L[1] * L[2] for L in layers if L[0] == "fc")
 
     x_host = torch.empty(x.shape, dtype=tdt, pin_memory=True)
@@ -749,7 +758,7 @@ def bench_fcnet(args, pg, torch, stream, dev, wl, batch, world):
         "value": value,
         "ms_per_step": 1e3 * dev_s / args.steps,
         "wall_s": wall,
-        "e2e": {"value": world * batch * args.steps / e2e_s, "unit": "img/s",
+        "e2e": {"value": aggregate(world, batch, args.steps, e2e_s), "unit": "img/s",
                 "h2d_bytes_per_step": int(x.numel()) * elt, "d2h_bytes_per_step": int(bufs[-1][0].numel()) * elt},
         "gpu_launches": int(launches),
         "clocks": clocks,
@@ -846,10 +855,10 @@ def bench_stream(args, pg, torch, stream, dev, wl, world):
     pct = lambda v, q: float(np.percentile(np.array(v), q))  # noqa: E731
     out = {
         "form": "limb_tc" if form == pg.FORM_LIMB_TC else "u64",
-        "value": world * imgs / dev_s,
+        "value": aggregate(world, imgs, 1, dev_s),
         "ms_per_step": 1e3 * dev_s / len(reqs),
         "wall_s": wall,
-        "e2e": {"value": world * imgs / e2e_s, "unit": "img/s",
+        "e2e": {"value": aggregate(world, imgs, 1, e2e_s), "unit": "img/s",
                 "h2d_bytes_per_step": int(sum(t.numel() * 8 for t in host_in) / len(reqs)),
                 "d2h_bytes_per_step": int(sum(t.numel() * 8 for t in host_out) / len(reqs))},
         "latency_ms": {"resident": {"p50": pct(lat_res, 50), "p99": pct(lat_res, 99), "max": max(lat_res)},
