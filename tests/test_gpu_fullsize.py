@@ -1,0 +1,74 @@
+"""Parity at the benchmark's full sizes, through properties that do not need
+the oracle to finish the whole problem:
+
+* VGG16 (maxpool) 3PC inference at batch 128: the limb tensor-core form and
+  the plain u64 form, two independent implementations of the same ring
+  arithmetic, agree on every share of every layer's output; and the first
+  two images' logits equal the oracle's run of the same two images (every
+  layer works image by image);
+* the 4096^3 share-GEMM with truncation: both forms agree on every share,
+  and sampled rows equal the oracle's product of those rows.
+"""
+import numpy as np
+import pytest
+
+import oracle as orc
+from tests import netref
+from tests.test_gpu_network import run_net
+
+pytestmark = pytest.mark.gpu
+
+U64 = np.uint64
+
+
+@pytest.fixture(scope="module")
+def pg():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import piranha_gb300 as pg
+
+    pg.lib()
+    return pg
+
+
+def test_vgg16_batch128_forms_agree(pg):
+    from piranha_gb300 import encode as enc
+    from piranha_gb300 import nets
+
+    layers = nets.vgg16()
+    params = nets.kaiming_uniform(layers, 2024, 26)
+    batch = 128
+    rng = np.random.default_rng(7)
+    x = enc.share_random(enc.encode(rng.uniform(0, 1, batch * 3072)), seed=8)
+    got_tc, outs_tc, comm_tc = run_net(pg, layers, params, x, batch, capture=True, form=pg.FORM_LIMB_TC)
+    got_u64, outs_u64, comm_u64 = run_net(pg, layers, params, x, batch, capture=True, form=pg.FORM_U64)
+    for i, (a, b) in enumerate(zip(outs_tc, outs_u64)):
+        assert np.array_equal(a, b), f"layer {i} {layers[i]}"
+    assert np.array_equal(got_tc, got_u64)
+    assert comm_tc == comm_u64
+    # the first two images through the oracle
+    n_in = 3072
+    want = netref.forward(layers, params, np.ascontiguousarray(x[..., : 2 * n_in]), 2)
+    assert np.array_equal(got_tc[..., : 2 * 10], want)
+
+
+def test_gemm_4096_forms_agree(pg):
+    M = N = K = 4096
+    rng = np.random.default_rng(11)
+    A = rng.integers(0, 2**64 - 1, size=(3, 2, M * K), dtype=U64, endpoint=True)
+    B = rng.integers(0, 2**64 - 1, size=(3, 2, K * N), dtype=U64, endpoint=True)
+    out = {}
+    for form in (pg.FORM_LIMB_TC, pg.FORM_U64):
+        ctx = pg.Context(0, form=form)
+        C = pg.empty_shares(M * N)
+        pg.matmul(ctx, pg.to_device(A), pg.to_device(B), C, M, N, K, 1, 1, 1, 26)
+        ctx.check_device_errors()
+        out[form] = pg.to_host(C)
+        ctx.close()
+    assert np.array_equal(out[pg.FORM_LIMB_TC], out[pg.FORM_U64])
+    rows = [0, 1, 2047, 4095]
+    a_rows = np.ascontiguousarray(A.reshape(3, 2, M, K)[:, :, rows, :].reshape(3, 2, -1))
+    want = orc.matmul(a_rows, B, len(rows), N, K, 1, 1, 1, 26).reshape(3, 2, len(rows), N)
+    got = out[pg.FORM_LIMB_TC].reshape(3, 2, M, N)[:, :, rows, :]
+    assert np.array_equal(got, want)
