@@ -159,16 +159,22 @@ struct ImageArgs {
     uint4 *img;
 };
 
-// One thread per (segment, 8-channel group, pixel); consecutive threads take
-// consecutive pixels, so the plane stores are coalesced.
+// One thread per (segment, pair of 8-channel groups, pixel); consecutive
+// threads take consecutive pixels, so the plane stores are coalesced, and a
+// thread reads its 16 channels of a row as one whole 128-byte line (with one
+// group per thread each line was fetched twice from DRAM). C8 is even (the
+// image's channels are a multiple of 16).
 __global__ void image_kernel(const __grid_constant__ ImageArgs ia) {
-    const long long total = 6ll * ia.C8 * ia.pixels;
+    const int C16 = ia.C8 >> 1;
+    const long long total = 6ll * C16 * ia.pixels;
     for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < total;
-         u += (long long)gridDim.x * blockDim.x) {
+         u += (long long)gridDim.x * blockDim.x)
+#pragma unroll 1
+    for (int half = 0; half < 2; half++) {
         const long long pix = u % ia.pixels;
         const long long t = u / ia.pixels;
-        const int cb = (int)(t % ia.C8);
-        const int seg = (int)(t / ia.C8);
+        const int cb = 2 * (int)(t % C16) + half;
+        const int seg = (int)(t / C16);
         const uint64_t *a = ia.a[seg];
         const int k0 = cb * 8;
         uint64_t v[8];
@@ -1069,7 +1075,8 @@ int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image) {
     ia.H = p.H; ia.W = p.W; ia.Din = p.Din; ia.f = p.cf; ia.stride = p.stride; ia.pad = p.cpad;
     ia.P = p.cP; ia.Q = p.cQ;
     ia.img = (uint4 *)image;
-    const long long units = 6ll * ia.C8 * p.pixels_alloc;
+    if (ia.C8 & 1) return set_error(c, PG_ERR_INVALID_ARG, "image channels %d are not a multiple of 16", p.C);
+    const long long units = 6ll * (ia.C8 / 2) * p.pixels_alloc;
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
     long long blocks = (units + 255) / 256;
     if (blocks > (long long)sms * 32) blocks = (long long)sms * 32;
