@@ -47,6 +47,17 @@ extern "C" {
 #define PG_CONV_FPROP 0
 #define PG_CONV_DGRAD 1
 #define PG_CONV_WGRAD 2
+/* local RSS operators (pg_rss_local_u64) */
+#define PG_OP_ADD 0
+#define PG_OP_SUB 1
+#define PG_OP_MUL 2
+#define PG_OP_XOR 3
+#define PG_OP_AND 4
+#define PG_OP_SHR 5 /* arithmetic */
+#define PG_OP_SHL 6
+#define PG_RHS_SCALAR 0 /* one public value */
+#define PG_RHS_PUBLIC 1 /* a public device vector of n (DeviceData) */
+#define PG_RHS_SHARES 2 /* another share tensor (six buffers) */
 
 typedef struct pg_ctx pg_ctx;
 
@@ -171,6 +182,16 @@ int pg_prg_fill_u64(pg_ctx *ctx, const uint8_t key[32], uint64_t counter, uint64
 int pg_prg_set_keys(pg_ctx *ctx, const uint8_t *keys, uint64_t counter);
 int pg_prg_counter(pg_ctx *ctx, uint64_t *counter);
 int pg_rss_reshare_u64(pg_ctx *ctx, const uint64_t *const c[3], size_t n, uint64_t *const out[6]);
+/* The local (communication-free) operators of RSSBase (RSS.inl:168-345), in
+ * place on a: `a op= rhs` for rhs a public scalar (+ - * >>), a public device
+ * vector (+ - * ^ & >> <<) or another share tensor (+ - ^). Public + - ^ touch
+ * party A's shareA and party C's shareB only; * & and shifts touch every share;
+ * share-tensor + - ^ go share by share. >> is arithmetic (functors.cuh:48-70);
+ * shift amounts of 64 or more give all sign bits (>>) or 0 (<<). Other
+ * combinations return PG_ERR_UNSUPPORTED (RSS * RSS and & are pg_rss_mul_u64 /
+ * pg_rss_and_u64). */
+int pg_rss_local_u64(pg_ctx *ctx, int op, uint64_t *const a[6], size_t n, int rhs_kind, uint64_t scalar,
+                     const uint64_t *pub, const uint64_t *const shares[6]);
 /* RSS *= RSS and RSS &= RSS (RSS.inl:284-345), in place on a */
 int pg_rss_mul_u64(pg_ctx *ctx, uint64_t *const a[6], const uint64_t *const b[6], size_t n);
 int pg_rss_and_u64(pg_ctx *ctx, uint64_t *const a[6], const uint64_t *const b[6], size_t n);

@@ -29,6 +29,8 @@ PG_OK = 0
 FORM_U64, FORM_LIMB_TC = 0, 1
 FPROP, DGRAD, WGRAD = 0, 1, 2
 LAYER_FC, LAYER_CNN, LAYER_RELU, LAYER_MAXPOOL, LAYER_AVGPOOL = 1, 2, 3, 4, 5
+OP_ADD, OP_SUB, OP_MUL, OP_XOR, OP_AND, OP_SHR, OP_SHL = range(7)
+RHS_SCALAR, RHS_PUBLIC, RHS_SHARES = range(3)
 FLOAT_PRECISION = 26
 
 _lib = None
@@ -162,6 +164,7 @@ def _declare(lib):
     lib.pg_reference_init_normal.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_size_t, ctypes.c_int,
                                              ctypes.c_double]
     lib.pg_ctx_set_autotune.argtypes = [vp, ctypes.c_int]
+    lib.pg_rss_local_u64.argtypes = [vp, ctypes.c_int, vp, ctypes.c_size_t, ctypes.c_int, ctypes.c_uint64, vp, vp]
     lib.pg_prg_fill_u64.argtypes = [vp, ctypes.c_char_p, ctypes.c_uint64, vp, ctypes.c_size_t]
     lib.pg_prg_set_keys.argtypes = [vp, ctypes.c_char_p, ctypes.c_uint64]
     lib.pg_prg_counter.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
@@ -454,6 +457,23 @@ def reconstruct(ctx: Context, a, out=None):
 def reshare(ctx: Context, c, out):
     ctx._check(lib().pg_rss_reshare_u64(ctx.handle, _p3(c), c.shape[1], _p6(out)))
     return out
+
+
+def local_(ctx: Context, op: int, a, rhs):
+    """RSSBase's local operators (RSS.inl:168-345), in place on a (3, 2, n)
+    uint64 shares: rhs an int (public scalar), a CUDA (n,) tensor (public
+    vector, DeviceData) or (3, 2, n) shares. op is one of OP_ADD, OP_SUB,
+    OP_MUL, OP_XOR, OP_AND, OP_SHR (arithmetic), OP_SHL."""
+    n = a.shape[2]
+    torch = _torch()
+    if isinstance(rhs, torch.Tensor) and rhs.dim() == 3:
+        st = lib().pg_rss_local_u64(ctx.handle, op, _p6(a), n, RHS_SHARES, 0, None, _p6(rhs))
+    elif isinstance(rhs, torch.Tensor):
+        st = lib().pg_rss_local_u64(ctx.handle, op, _p6(a), n, RHS_PUBLIC, 0, ctypes.c_void_p(rhs.data_ptr()), None)
+    else:
+        st = lib().pg_rss_local_u64(ctx.handle, op, _p6(a), n, RHS_SCALAR, int(rhs) % (1 << 64), None, None)
+    ctx._check(st)
+    return a
 
 
 def mul_(ctx: Context, a, b):

@@ -286,6 +286,69 @@ int maxpool_im2row_u64(Ctx *c, const uint64_t *im, uint64_t *out, int H, int W, 
 
 template int rss_reconstruct<uint64_t>(Ctx *, const uint64_t *const *, size_t, uint64_t *const *);
 template int rss_reconstruct<uint8_t>(Ctx *, const uint8_t *const *, size_t, uint8_t *const *);
+// The local (communication-free) RSS operators, RSS.inl:168-345: a public
+// scalar or vector added / subtracted / XORed where the reference's setPublic
+// puts public values (party A's shareA, party C's shareB: slots 0 and 5), and
+// multiplied / ANDed / shifted into every share; a share tensor added,
+// subtracted or XORed share by share. Shifts are arithmetic to the right
+// (functors.cuh:48-70) and logical to the left, with amounts of 64 or more
+// giving what the shift instructions give: all sign bits, or 0.
+__device__ __forceinline__ uint64_t sar64(uint64_t x, uint64_t y) {
+    return y >= 64 ? ((int64_t)x < 0 ? ~0ull : 0ull) : (uint64_t)((int64_t)x >> y);
+}
+__device__ __forceinline__ uint64_t shl64(uint64_t x, uint64_t y) { return y >= 64 ? 0ull : x << y; }
+
+__global__ void local_kernel(Sh6<uint64_t> a, size_t n, int op, int kind, uint64_t scalar, const uint64_t *pub,
+                             CSh6<uint64_t> sh) {
+    GRID_STRIDE(i, n) {
+        const uint64_t pv = kind == PG_RHS_SCALAR ? scalar : kind == PG_RHS_PUBLIC ? pub[i] : 0;
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            const uint64_t r = kind == PG_RHS_SHARES ? sh.p[k][i] : pv;
+            const bool pub_slot = (k == 0 || k == 5);
+            uint64_t x = a.p[k][i];
+            switch (op) {
+                case PG_OP_ADD: if (kind == PG_RHS_SHARES || pub_slot) x += r; break;
+                case PG_OP_SUB: if (kind == PG_RHS_SHARES || pub_slot) x -= r; break;
+                case PG_OP_XOR: if (kind == PG_RHS_SHARES || pub_slot) x ^= r; break;
+                case PG_OP_MUL: x *= r; break;
+                case PG_OP_AND: x &= r; break;
+                case PG_OP_SHR: x = sar64(x, r); break;
+                default: x = shl64(x, r); break;
+            }
+            a.p[k][i] = x;
+        }
+    }
+}
+
+int rss_local_u64(Ctx *c, int op, uint64_t *const a[6], size_t n, int kind, uint64_t scalar, const uint64_t *pub,
+                  const uint64_t *const shares[6]) {
+    Sh6<uint64_t> ca;
+    CSh6<uint64_t> cs;
+    if (!load6(ca, a)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+    // the combinations the reference's RSS class defines
+    static const bool ok[3][7] = {
+        // ADD   SUB   MUL   XOR    AND    SHR   SHL
+        {true, true, true, false, false, true, false},   // public scalar (operator op=(const T))
+        {true, true, true, true, true, true, true},      // public vector (operator op=(const DeviceData &))
+        {true, true, false, true, false, false, false},  // shares (operator op=(const RSSBase &)); * and & are protocol steps
+    };
+    if (kind < 0 || kind > 2 || op < 0 || op > 6 || !ok[kind][op])
+        return set_error(c, PG_ERR_UNSUPPORTED, "no local RSS operator %d with right-hand side kind %d", op, kind);
+    if (kind == PG_RHS_PUBLIC && !pub && n) return set_error(c, PG_ERR_INVALID_ARG, "null public vector");
+    if (kind == PG_RHS_SHARES) {
+        if (!load6(cs, shares)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    } else {
+        for (int k = 0; k < 6; k++) cs.p[k] = nullptr;
+    }
+    if (n) {
+        local_kernel<<<grid1(c, n), 256, 0, c->stream>>>(ca, n, op, kind, scalar, pub, cs);
+        c->launches++;
+        return launch_status(c, "local_kernel");
+    }
+    return PG_OK;
+}
+
 template int rss_reshare<uint64_t>(Ctx *, const uint64_t *const *, size_t, uint64_t *const *);
 template int rss_mul<uint64_t, false>(Ctx *, uint64_t *const *, const uint64_t *const *, size_t);
 template int rss_mul<uint64_t, true>(Ctx *, uint64_t *const *, const uint64_t *const *, size_t);

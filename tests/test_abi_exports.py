@@ -64,6 +64,9 @@ def test_constants_match_python_mirror(pg):
     assert int(consts["PG_OK"]) == 0
     assert int(consts["PG_FORM_U64"]) == pg.FORM_U64
     assert int(consts["PG_FORM_LIMB_TC"]) == pg.FORM_LIMB_TC
+    for name in ("OP_ADD", "OP_SUB", "OP_MUL", "OP_XOR", "OP_AND", "OP_SHR", "OP_SHL", "RHS_SCALAR", "RHS_PUBLIC",
+                 "RHS_SHARES"):
+        assert int(consts["PG_" + name]) == getattr(pg, name)
     for name in ("PG_CONV_FPROP", "PG_CONV_DGRAD", "PG_CONV_WGRAD"):
         assert int(consts[name]) in (0, 1, 2)
 

@@ -426,3 +426,43 @@ def test_invalid_arguments_return_status(pg, ctx):
     pg.ReLU(ctx, pg.zeros_shares(10), out, pg.empty_shares(10, "u8"))
     ctx.sync()
     assert torch.count_nonzero(out).item() == 0
+
+
+# ------------------------------------------------------------ local operators
+
+@pytest.mark.parametrize("op,kind", [("add", "scalar"), ("sub", "scalar"), ("mul", "scalar"), ("shr", "scalar"),
+                                     ("add", "public"), ("sub", "public"), ("mul", "public"), ("xor", "public"),
+                                     ("and", "public"), ("shr", "public"), ("shl", "public"),
+                                     ("add", "shares"), ("sub", "shares"), ("xor", "shares")])
+def test_rss_local(pg, ctx, op, kind):
+    import torch
+
+    n = 5003
+    a = orc.random_views(n, U64, 60)
+    rng = np.random.default_rng(61)
+    if kind == "scalar":
+        rhs_np = int(rng.integers(0, 70)) if op == "shr" else int(rng.integers(0, 2**63))
+        rhs_dev = rhs_np
+    elif kind == "public":
+        rhs_np = rng.integers(0, 70, n, dtype=U64) if op in ("shr", "shl") else \
+            rng.integers(0, 2**64 - 1, n, dtype=U64, endpoint=True)
+        rhs_dev = torch.from_numpy(rhs_np.view(np.int64)).cuda()
+    else:
+        rhs_np = orc.random_views(n, U64, 62)
+        rhs_dev = dev(pg, rhs_np)
+    ops = {"add": pg.OP_ADD, "sub": pg.OP_SUB, "mul": pg.OP_MUL, "xor": pg.OP_XOR, "and": pg.OP_AND,
+           "shr": pg.OP_SHR, "shl": pg.OP_SHL}
+    da = dev(pg, a)
+    pg.local_(ctx, ops[op], da, rhs_dev)
+    ctx.sync()
+    assert np.array_equal(host(pg, da), orc.rss_local(op, a, rhs_np))
+    assert ctx.comm()["rounds"] == 0
+
+
+def test_rss_local_unsupported(pg, ctx):
+    a = dev(pg, orc.random_views(10, U64, 63))
+    for op in (pg.OP_MUL, pg.OP_AND):  # protocol steps, not local operators
+        with pytest.raises(pg.PiranhaError):
+            pg.local_(ctx, op, a, a)
+    with pytest.raises(pg.PiranhaError):
+        pg.local_(ctx, pg.OP_XOR, a, 5)

@@ -42,3 +42,4 @@ def test_masks_sum_to_zero():
     assert not (x[0] ^ x[1] ^ x[2]).any()
     b = orc.prg_masks(keys, 5, 1001, xor=True, bits=True)
     assert set(np.unique(b)) <= {0, 1} and not (b[0] ^ b[1] ^ b[2]).any()
+
