@@ -192,6 +192,13 @@ int pg_rss_reshare_u64(pg_ctx *ctx, const uint64_t *const c[3], size_t n, uint64
  * pg_rss_and_u64). */
 int pg_rss_local_u64(pg_ctx *ctx, int op, uint64_t *const a[6], size_t n, int rhs_kind, uint64_t scalar,
                      const uint64_t *pub, const uint64_t *const shares[6]);
+/* the same local operators of TPCBase (TPC.inl:146-240; public values at
+ * party A's share) and FPCBase (FPC.inl:187-300; public values in the x0
+ * component: party B's shareC, party C's shareB, party D's shareA) */
+int pg_tpc_local_u64(pg_ctx *ctx, int op, uint64_t *const a[2], size_t n, int rhs_kind, uint64_t scalar,
+                     const uint64_t *pub, const uint64_t *const shares[2]);
+int pg_fpc_local_u64(pg_ctx *ctx, int op, uint64_t *const a[12], size_t n, int rhs_kind, uint64_t scalar,
+                     const uint64_t *pub, const uint64_t *const shares[12]);
 /* RSS *= RSS and RSS &= RSS (RSS.inl:284-345), in place on a */
 int pg_rss_mul_u64(pg_ctx *ctx, uint64_t *const a[6], const uint64_t *const b[6], size_t n);
 int pg_rss_and_u64(pg_ctx *ctx, uint64_t *const a[6], const uint64_t *const b[6], size_t n);

@@ -815,43 +815,60 @@ def prg_masks(keys, counter: int, n: int, xor: bool = False, bits: bool = False)
 
 # ---------------------------------------------------------- local operators
 
+def _local(op, a, rhs, pub_rows):
+    a = np.array(a, dtype=np.uint64, copy=True)
+    shape = a.shape
+    n = shape[-1]
+    flat = a.reshape(-1, n)
+    if isinstance(rhs, (int, np.integer)):
+        kind, r = "scalar", np.full(n, int(rhs) % (1 << 64), dtype=np.uint64)
+    elif np.asarray(rhs).ndim == 1:
+        kind, r = "public", np.asarray(rhs, dtype=np.uint64)
+    else:
+        kind, r = "shares", np.asarray(rhs, dtype=np.uint64).reshape(-1, n)
+    with np.errstate(over="ignore"):
+        for k in range(flat.shape[0]):
+            x = flat[k]
+            y = r[k] if kind == "shares" else r
+            if op in ("add", "sub", "xor") and kind != "shares" and k not in pub_rows:
+                continue
+            if op == "add":
+                x = x + y
+            elif op == "sub":
+                x = x - y
+            elif op == "xor":
+                x = x ^ y
+            elif op == "mul":
+                x = x * y
+            elif op == "and":
+                x = x & y
+            elif op == "shr":
+                sx = x.view(np.int64)
+                x = np.where(y >= 64, np.where(sx < 0, np.uint64(2**64 - 1), np.uint64(0)),
+                             (sx >> np.minimum(y, 63).astype(np.int64)).view(np.uint64))
+            elif op == "shl":
+                x = np.where(y >= 64, np.uint64(0), x << np.minimum(y, np.uint64(63)))
+            flat[k] = x
+    return flat.reshape(shape)
+
+
 def rss_local(op, a, rhs):
     """RSSBase's local operators (src/mpc/RSS.inl:168-345) on (3, 2, n) uint64
     views: rhs an int (public scalar), an (n,) array (public DeviceData) or
     (3, 2, n) shares. Public + - ^ go to party A's shareA and party C's shareB;
     * & and shifts to every share; shares + - ^ share by share. >> is the
     arithmetic shift of functors.cuh:48-70; shifts of 64 or more saturate."""
-    a = np.array(a, dtype=np.uint64, copy=True)
-    if isinstance(rhs, (int, np.integer)):
-        kind, r = "scalar", np.full(a.shape[2], int(rhs) % (1 << 64), dtype=np.uint64)
-    elif np.asarray(rhs).ndim == 1:
-        kind, r = "public", np.asarray(rhs, dtype=np.uint64)
-    else:
-        kind, r = "shares", np.asarray(rhs, dtype=np.uint64)
-    with np.errstate(over="ignore"):
-        for p in range(3):
-            for s in range(2):
-                x = a[p, s]
-                y = r[p, s] if kind == "shares" else r
-                pub = (p, s) in ((0, 0), (2, 1))
-                if op in ("add", "sub", "xor") and kind != "shares" and not pub:
-                    continue
-                if op == "add":
-                    x = x + y
-                elif op == "sub":
-                    x = x - y
-                elif op == "xor":
-                    x = x ^ y
-                elif op == "mul":
-                    x = x * y
-                elif op == "and":
-                    x = x & y
-                elif op == "shr":
-                    sx = x.view(np.int64)
-                    big = y >= 64
-                    x = np.where(big, np.where(sx < 0, np.uint64(2**64 - 1), np.uint64(0)),
-                                 (sx >> np.minimum(y, 63).astype(np.int64)).view(np.uint64))
-                elif op == "shl":
-                    x = np.where(y >= 64, np.uint64(0), x << np.minimum(y, np.uint64(63)))
-                a[p, s] = x
-    return a
+    return _local(op, a, rhs, {0, 5})
+
+
+def tpc_local(op, a, rhs):
+    """TPCBase's local operators (src/mpc/TPC.inl:146-240) on (2, n) views:
+    public + - ^ at party A's share."""
+    return _local(op, a, rhs, {0})
+
+
+def fpc_local(op, a, rhs):
+    """FPCBase's local operators (src/mpc/FPC.inl:187-300) on (4, 3, n) views:
+    public + - ^ in the x0 component (party B's shareC, party C's shareB,
+    party D's shareA)."""
+    return _local(op, a, rhs, {5, 7, 9})

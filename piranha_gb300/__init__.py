@@ -165,6 +165,8 @@ def _declare(lib):
                                              ctypes.c_double]
     lib.pg_ctx_set_autotune.argtypes = [vp, ctypes.c_int]
     lib.pg_rss_local_u64.argtypes = [vp, ctypes.c_int, vp, ctypes.c_size_t, ctypes.c_int, ctypes.c_uint64, vp, vp]
+    lib.pg_tpc_local_u64.argtypes = [vp, ctypes.c_int, vp, ctypes.c_size_t, ctypes.c_int, ctypes.c_uint64, vp, vp]
+    lib.pg_fpc_local_u64.argtypes = [vp, ctypes.c_int, vp, ctypes.c_size_t, ctypes.c_int, ctypes.c_uint64, vp, vp]
     lib.pg_prg_fill_u64.argtypes = [vp, ctypes.c_char_p, ctypes.c_uint64, vp, ctypes.c_size_t]
     lib.pg_prg_set_keys.argtypes = [vp, ctypes.c_char_p, ctypes.c_uint64]
     lib.pg_prg_counter.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
@@ -611,6 +613,22 @@ class tpc:
         return out
 
     @staticmethod
+    def local_(ctx: Context, op: int, a, rhs):
+        """TPCBase's local operators (TPC.inl:146-240) in place on (2, n) uint64
+        shares; rhs as for piranha_gb300.local_ ((2, n) for shares)."""
+        n = a.shape[1]
+        torch = _torch()
+        if isinstance(rhs, torch.Tensor) and rhs.dim() == 2:
+            st = lib().pg_tpc_local_u64(ctx.handle, op, tpc._p2(a), n, RHS_SHARES, 0, None, tpc._p2(rhs))
+        elif isinstance(rhs, torch.Tensor):
+            st = lib().pg_tpc_local_u64(ctx.handle, op, tpc._p2(a), n, RHS_PUBLIC, 0, ctypes.c_void_p(rhs.data_ptr()),
+                                        None)
+        else:
+            st = lib().pg_tpc_local_u64(ctx.handle, op, tpc._p2(a), n, RHS_SCALAR, int(rhs) % (1 << 64), None, None)
+        ctx._check(st)
+        return a
+
+    @staticmethod
     def mul_(ctx: Context, a, b):
         """TPC *= TPC (TPC.inl:242-272), in place on a."""
         ctx._check(lib().pg_tpc_mul_u64(ctx.handle, tpc._p2(a), tpc._p2(b), a.shape[1]))
@@ -720,6 +738,22 @@ class fpc:
         fn = getattr(lib(), f"pg_fpc_reconstruct_{_ring(a)}")
         ctx._check(fn(ctx.handle, fpc._p12(a), a.shape[2], fpc._p4(out)))
         return out
+
+    @staticmethod
+    def local_(ctx: Context, op: int, a, rhs):
+        """FPCBase's local operators (FPC.inl:187-300) in place on (4, 3, n) uint64
+        shares; rhs as for piranha_gb300.local_ ((4, 3, n) for shares)."""
+        n = a.shape[2]
+        torch = _torch()
+        if isinstance(rhs, torch.Tensor) and rhs.dim() == 3:
+            st = lib().pg_fpc_local_u64(ctx.handle, op, fpc._p12(a), n, RHS_SHARES, 0, None, fpc._p12(rhs))
+        elif isinstance(rhs, torch.Tensor):
+            st = lib().pg_fpc_local_u64(ctx.handle, op, fpc._p12(a), n, RHS_PUBLIC, 0, ctypes.c_void_p(rhs.data_ptr()),
+                                        None)
+        else:
+            st = lib().pg_fpc_local_u64(ctx.handle, op, fpc._p12(a), n, RHS_SCALAR, int(rhs) % (1 << 64), None, None)
+        ctx._check(st)
+        return a
 
     @staticmethod
     def mul_(ctx: Context, a, b):

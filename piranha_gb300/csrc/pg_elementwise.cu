@@ -2,6 +2,8 @@
 // (reconstruct, reshare, *=, &=, dividePublic) and the reference's small glue
 // kernels (src/gpu/matrix.cuh, bitwise.cuh, convolution.cuh). Each kernel
 // reads every party's share slots once and writes every output slot once.
+#include <cstring>
+
 #include "pg_common.cuh"
 
 namespace pg {
@@ -298,55 +300,82 @@ __device__ __forceinline__ uint64_t sar64(uint64_t x, uint64_t y) {
 }
 __device__ __forceinline__ uint64_t shl64(uint64_t x, uint64_t y) { return y >= 64 ? 0ull : x << y; }
 
-__global__ void local_kernel(Sh6<uint64_t> a, size_t n, int op, int kind, uint64_t scalar, const uint64_t *pub,
-                             CSh6<uint64_t> sh) {
+struct LocalArgs {
+    uint64_t *a[12];
+    const uint64_t *sh[12];
+    int nbuf, pubmask;  // share buffers; bit k: buffer k holds the public component
+    int op, kind;
+    uint64_t scalar;
+    const uint64_t *pub;
+};
+
+__global__ void local_kernel(const __grid_constant__ LocalArgs g, size_t n) {
     GRID_STRIDE(i, n) {
-        const uint64_t pv = kind == PG_RHS_SCALAR ? scalar : kind == PG_RHS_PUBLIC ? pub[i] : 0;
-#pragma unroll
-        for (int k = 0; k < 6; k++) {
-            const uint64_t r = kind == PG_RHS_SHARES ? sh.p[k][i] : pv;
-            const bool pub_slot = (k == 0 || k == 5);
-            uint64_t x = a.p[k][i];
-            switch (op) {
-                case PG_OP_ADD: if (kind == PG_RHS_SHARES || pub_slot) x += r; break;
-                case PG_OP_SUB: if (kind == PG_RHS_SHARES || pub_slot) x -= r; break;
-                case PG_OP_XOR: if (kind == PG_RHS_SHARES || pub_slot) x ^= r; break;
+        const uint64_t pv = g.kind == PG_RHS_SCALAR ? g.scalar : g.kind == PG_RHS_PUBLIC ? g.pub[i] : 0;
+        for (int k = 0; k < g.nbuf; k++) {
+            const uint64_t r = g.kind == PG_RHS_SHARES ? g.sh[k][i] : pv;
+            const bool pub_slot = (g.pubmask >> k) & 1;
+            uint64_t x = g.a[k][i];
+            switch (g.op) {
+                case PG_OP_ADD: if (g.kind == PG_RHS_SHARES || pub_slot) x += r; break;
+                case PG_OP_SUB: if (g.kind == PG_RHS_SHARES || pub_slot) x -= r; break;
+                case PG_OP_XOR: if (g.kind == PG_RHS_SHARES || pub_slot) x ^= r; break;
                 case PG_OP_MUL: x *= r; break;
                 case PG_OP_AND: x &= r; break;
                 case PG_OP_SHR: x = sar64(x, r); break;
                 default: x = shl64(x, r); break;
             }
-            a.p[k][i] = x;
+            g.a[k][i] = x;
         }
     }
 }
 
-int rss_local_u64(Ctx *c, int op, uint64_t *const a[6], size_t n, int kind, uint64_t scalar, const uint64_t *pub,
-                  const uint64_t *const shares[6]) {
-    Sh6<uint64_t> ca;
-    CSh6<uint64_t> cs;
-    if (!load6(ca, a)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
-    // the combinations the reference's RSS class defines
+// nbuf = 6 (RSS: public at party A's shareA and party C's shareB), 2 (TPC:
+// party A's share, TPC.inl:146-214) or 12 (FPC: the x0 component, held as
+// party B's shareC, party C's shareB and party D's shareA, FPC.inl:187-272)
+int local_u64(Ctx *c, int nbuf, int op, uint64_t *const *a, size_t n, int kind, uint64_t scalar, const uint64_t *pub,
+              const uint64_t *const *shares) {
+    LocalArgs g;
+    memset(&g, 0, sizeof(g));
+    g.nbuf = nbuf;
+    g.pubmask = nbuf == 6 ? (1 << 0) | (1 << 5) : nbuf == 2 ? 1 : (1 << 5) | (1 << 7) | (1 << 9);
+    if (!a) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+    for (int k = 0; k < nbuf; k++) {
+        if (!a[k]) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+        g.a[k] = a[k];
+    }
+    // the combinations the reference's share classes define
     static const bool ok[3][7] = {
         // ADD   SUB   MUL   XOR    AND    SHR   SHL
         {true, true, true, false, false, true, false},   // public scalar (operator op=(const T))
         {true, true, true, true, true, true, true},      // public vector (operator op=(const DeviceData &))
-        {true, true, false, true, false, false, false},  // shares (operator op=(const RSSBase &)); * and & are protocol steps
+        {true, true, false, true, false, false, false},  // shares (operator op=(share class)); * & are protocol steps
     };
     if (kind < 0 || kind > 2 || op < 0 || op > 6 || !ok[kind][op])
-        return set_error(c, PG_ERR_UNSUPPORTED, "no local RSS operator %d with right-hand side kind %d", op, kind);
+        return set_error(c, PG_ERR_UNSUPPORTED, "no local operator %d with right-hand side kind %d", op, kind);
     if (kind == PG_RHS_PUBLIC && !pub && n) return set_error(c, PG_ERR_INVALID_ARG, "null public vector");
     if (kind == PG_RHS_SHARES) {
-        if (!load6(cs, shares)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
-    } else {
-        for (int k = 0; k < 6; k++) cs.p[k] = nullptr;
+        if (!shares) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+        for (int k = 0; k < nbuf; k++) {
+            if (!shares[k]) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+            g.sh[k] = shares[k];
+        }
     }
+    g.op = op;
+    g.kind = kind;
+    g.scalar = scalar;
+    g.pub = pub;
     if (n) {
-        local_kernel<<<grid1(c, n), 256, 0, c->stream>>>(ca, n, op, kind, scalar, pub, cs);
+        local_kernel<<<grid1(c, n), 256, 0, c->stream>>>(g, n);
         c->launches++;
         return launch_status(c, "local_kernel");
     }
     return PG_OK;
+}
+
+int rss_local_u64(Ctx *c, int op, uint64_t *const a[6], size_t n, int kind, uint64_t scalar, const uint64_t *pub,
+                  const uint64_t *const shares[6]) {
+    return local_u64(c, 6, op, a, n, kind, scalar, pub, shares);
 }
 
 template int rss_reshare<uint64_t>(Ctx *, const uint64_t *const *, size_t, uint64_t *const *);

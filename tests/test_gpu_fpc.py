@@ -327,3 +327,29 @@ def test_fpc_fc_net_u32_fp10(pg, ctx):
             ctx.sync()
             assert np.array_equal(host(r), want_r), f"relu {li}"
             cur_h, cur_d = want_r, r
+
+
+@pytest.mark.parametrize("op,kind", [("add", "scalar"), ("sub", "public"), ("xor", "public"), ("and", "public"),
+                                     ("shr", "public"), ("mul", "scalar"), ("sub", "shares"), ("xor", "shares")])
+def test_fpc_local(pg, ctx, op, kind):
+    import torch
+
+    n = 555
+    a = views(n, U64, 80)
+    rng = np.random.default_rng(81)
+    shift = op in ("shr", "shl")
+    if kind == "scalar":
+        r_np = int(rng.integers(0, 70)) if shift else int(rng.integers(0, 2**63))
+        r_dev = r_np
+    elif kind == "public":
+        r_np = rng.integers(0, 70, n, dtype=U64) if shift else rng.integers(0, 2**63, n, dtype=U64)
+        r_dev = torch.from_numpy(r_np.view(np.int64)).cuda()
+    else:
+        r_np = views(n, U64, 82)
+        r_dev = dev(r_np)
+    ops = {"add": pg.OP_ADD, "sub": pg.OP_SUB, "mul": pg.OP_MUL, "xor": pg.OP_XOR, "and": pg.OP_AND,
+           "shr": pg.OP_SHR}
+    da = dev(a)
+    pg.fpc.local_(ctx, ops[op], da, r_dev)
+    ctx.sync()
+    assert np.array_equal(host(da), orc.fpc_local(op, a, r_np))

@@ -246,3 +246,28 @@ def test_tpc_fc_net_u32_fp10(pg, ctx):
             ctx.sync()
             assert np.array_equal(host(r), want_r), f"relu {li}"
             cur_h, cur_d = want_r, r
+
+
+@pytest.mark.parametrize("op,kind", [("add", "scalar"), ("sub", "public"), ("xor", "public"), ("mul", "public"),
+                                     ("shr", "scalar"), ("shl", "public"), ("add", "shares"), ("xor", "shares")])
+def test_tpc_local(pg, ctx, op, kind):
+    import torch
+
+    n = 777
+    a = rnd(n, U64, 70)
+    rng = np.random.default_rng(71)
+    shift = op in ("shr", "shl")
+    if kind == "scalar":
+        r_np = int(rng.integers(0, 70)) if shift else int(rng.integers(0, 2**63))
+        r_dev = r_np
+    elif kind == "public":
+        r_np = rng.integers(0, 70, n, dtype=U64) if shift else rng.integers(0, 2**63, n, dtype=U64)
+        r_dev = torch.from_numpy(r_np.view(np.int64)).cuda()
+    else:
+        r_np = rnd(n, U64, 72)
+        r_dev = dev(r_np)
+    ops = {"add": pg.OP_ADD, "sub": pg.OP_SUB, "mul": pg.OP_MUL, "xor": pg.OP_XOR, "shr": pg.OP_SHR, "shl": pg.OP_SHL}
+    da = dev(a)
+    pg.tpc.local_(ctx, ops[op], da, r_dev)
+    ctx.sync()
+    assert np.array_equal(host(da), orc.tpc_local(op, a, r_np))

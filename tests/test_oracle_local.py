@@ -60,3 +60,20 @@ def test_rss_local_scalar_and_shares():
         assert np.array_equal(_rec(orc.rss_local("add", a, b))[0], x + y)
         assert np.array_equal(_rec(orc.rss_local("sub", a, b))[0], x - y)
         assert np.array_equal(_rec(orc.rss_local("mul", a, 3))[0], x * np.uint64(3))
+
+
+def test_tpc_fpc_local_public_add_reconstructs():
+    rng = np.random.default_rng(9)
+    n = 50
+    x = rng.integers(0, 2**63, n, dtype=np.uint64)
+    r = rng.integers(0, 2**63, n, dtype=np.uint64)
+    t = orc.tpc_local("add", np.stack([x, np.zeros(n, np.uint64)]), r)  # party A holds the public value
+    with np.errstate(over="ignore"):
+        assert np.array_equal(t[0] + t[1], x + r)
+    f = np.zeros((4, 3, n), dtype=np.uint64)
+    f[1, 2] = f[2, 1] = f[3, 0] = x  # setPublic(x)
+    g = orc.fpc_local("add", f, r)
+    with np.errstate(over="ignore"):
+        for p, s in ((1, 2), (2, 1), (3, 0)):
+            assert np.array_equal(g[p, s], x + r)
+        assert not g[0].any()
