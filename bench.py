@@ -20,6 +20,7 @@ pinned host shares in and out (H2D + forward + D2H per step).
 Other workloads (--workload), each printing the same JSON line for its own metric:
   secureml      3PC SecureML (784-128-128-10, ReLU after every FC) inference, batch 128, u64, FP 26
   lenet-train   3PC LeNet training step (forward + backward + SGD, log learning rate 5), batch 128
+  vgg16-train   3PC VGG16 training step (the reference's vgg16-cifar10 with averagepool), batch 128
   secureml-2pc  2PC SecureML inference, batch 128, uint32 shares, FP 10
   secureml-4pc  4PC SecureML inference, batch 128, uint32 shares, FP 10
   stream        512 requests of batch 1..64, SecureML or VGG16, served in order; p50/p99 latency
@@ -67,6 +68,10 @@ WORKLOADS = {
                     "log_lr": 5,
                     "desc": "lenet (maxpool variant), 3PC RSS, batch 128, uint64 shares, FP 26, "
                             "forward + revealed-softmax backward + SGD (log learning rate 5)"},
+    "vgg16-train": {"metric": "3PC VGG16 training step img/s", "kind": "train3", "fp": 26, "ring": "u64",
+                    "log_lr": 5,
+                    "desc": "vgg16-cifar10 as the reference trains it (five 2x2/2 averagepools), 3PC RSS, batch 128, "
+                            "uint64 shares, FP 26, forward + revealed-softmax backward + SGD (log learning rate 5)"},
     "secureml-2pc": {"metric": "2PC SecureML secure inference img/s", "kind": "fcnet", "parties": 2, "fp": 10,
                      "ring": "u32",
                      "desc": "secureml 784-128-128-10, 2PC (TPC), batch 128, uint32 shares, FP 10"},
@@ -84,6 +89,7 @@ WORKLOADS = {
                        "(1, 2, 4, 8, 12, 16, 24, ..., 64) that holds it"},
 }
 _LAYERS = {"vgg16": nets.vgg16, "secureml": nets.secureml, "lenet-train": nets.lenet,
+           "vgg16-train": lambda: nets.vgg16(maxpool=False),
            "secureml-2pc": nets.secureml, "secureml-4pc": nets.secureml, "stream": nets.vgg16}
 
 
