@@ -85,6 +85,7 @@ struct Args {
     int ntiles_n, total_stages, chunks_per_split;
     int direct, colmajor;
     int zeros_kept;  // the four zero output shares already hold 0: write only value / bias shares
+    int tma_out;     // the two value shares go out as tensor-map stores of the staged tile (see tma_store_4d)
     uint32_t a_box_bytes;  // bytes of one digit plane of a stage (16 * 2 * Wt * Ht * Nt)
     const uint8_t *packB;
     uint64_t *partial;
@@ -403,6 +404,8 @@ __device__ __forceinline__ int lo_chunks(int nst) {
 // column for a column-major GEMM output), adding the bias shares.
 constexpr int STG_PITCH = BN + 1;  // u64 per staged row: two-way bank conflicts at most
 static_assert(BM * STG_PITCH * 8 + BM * 8 <= STAGES * STAGE_BYTES, "the staged tile must fit in the stage ring");
+static_assert(BM * STG_PITCH * 8 + BM * 8 <= 2 * STAGE_BYTES && BM * BN * 8 <= 2 * STAGE_BYTES,
+              "the pitched tile fits in stages 0-1 and the dense one in stages 2-3");
 static_assert(NTHREADS - W_EPI0 * 32 - 32 == 256, "eight epilogue warps");
 
 __device__ __forceinline__ void named_bar_epilogue() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
@@ -447,8 +450,17 @@ __device__ __forceinline__ void store_tile(const Args &g, int z, const uint64_t 
     }
 }
 
+// One 4-D tensor-map store of a staged tile from shared memory (bulk group).
+__device__ __forceinline__ void tma_store_4d(const CUtensorMap *map, uint32_t src, int c0, int c1, int c2, int c3) {
+    asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%2, %3, %4, %5}], [%1];" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+                 "r"(src), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+                 : "memory");
+}
+
 __global__ void __launch_bounds__(NTHREADS, 1)
-    limb_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ Args gp) {
+    limb_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmOut0,
+                    const __grid_constant__ CUtensorMap tmOut5, const __grid_constant__ Args gp) {
     extern __shared__ uint8_t smem_raw[];
     const uint32_t pad = (1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u;
     Smem &sm = *reinterpret_cast<Smem *>(smem_raw + pad);
@@ -623,7 +635,29 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         tc::fence_proxy_async_smem();
         stage_row(g, stg, mrow, row, colh, sm.abort ? -1 : m, zs);
         named_bar_epilogue();
-        if (!sm.abort) store_tile(g, z, stg, mrow, threadIdx.x - W_EPI0 * 32);
+        if (!sm.abort && g.tma_out) {
+            // The tile's value (the same for party A's shareA and party C's
+            // shareB) repacked densely, row by row in the box's order (BN
+            // columns, then Wt, Ht, Nt), then stored by the tensor maps of the
+            // two value shares; the maps clip rows and columns past the tensor.
+            const int te = threadIdx.x - W_EPI0 * 32;
+            uint64_t *dense = reinterpret_cast<uint64_t *>(sm.stage[2]);
+            for (int e = te; e < g.R * BN; e += 256) dense[e] = stg[(e >> 6) * STG_PITCH + (e & (BN - 1))];
+            tc::fence_proxy_async_smem();
+            named_bar_epilogue();
+            if (te == 0) {
+                const int c0 = blockIdx.x * BN;
+                const int c1 = g.rows_mode ? n0 : w0, c2 = g.rows_mode ? 0 : h0, c3 = g.rows_mode ? 0 : n0;
+                const uint32_t src = tc::smem_u32(dense);
+                tma_store_4d(&tmOut0, src, c0, c1, c2, c3);
+                tma_store_4d(&tmOut5, src, c0, c1, c2, c3);
+                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                // the shared memory must stay valid until the stores have read it
+                asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+            }
+        } else if (!sm.abort) {
+            store_tile(g, z, stg, mrow, threadIdx.x - W_EPI0 * 32);
+        }
     }
     tc::tc_fence_before();
     __syncthreads();
@@ -1173,8 +1207,36 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
     g.dshift = pow2_shift<uint64_t>(g.d);
     g.err = device_error_word(c);
     if (split > 1 && !partial) return set_error(c, PG_ERR_INVALID_ARG, "split-K needs a partial buffer");
+    // value shares by tensor-map stores: the network's convolutions (no bias,
+    // zero shares kept, row-major output of an even width of at least one N tile)
+    alignas(64) CUtensorMap tmo[2];
+    memset(tmo, 0, sizeof(tmo));
+    g.tma_out = 0;
+    // (every box dimension within its tensor dimension, tile origins never negative)
+    if (g.direct && !raw && !p.colmajor && zeros_kept && !bias && p.N >= BN && p.N % 2 == 0 &&
+        (p.implicit || p.Nt <= p.M) && !((uintptr_t)out[0] & 15) && !((uintptr_t)out[5] & 15)) {
+        cuuint64_t od[4], os[3];
+        cuuint32_t ob[4];
+        const cuuint64_t rowb = (cuuint64_t)p.N * 8;
+        if (p.implicit) {
+            od[0] = p.N; od[1] = p.Q; od[2] = p.P; od[3] = p.Nimg;
+            os[0] = rowb; os[1] = rowb * p.Q; os[2] = rowb * p.Q * p.P;
+            ob[0] = BN; ob[1] = p.Wt; ob[2] = p.Ht; ob[3] = p.Nt;
+        } else {
+            od[0] = p.N; od[1] = p.M; od[2] = 1; od[3] = 1;
+            os[0] = rowb; os[1] = rowb * p.M; os[2] = rowb * p.M;
+            ob[0] = BN; ob[1] = p.Nt; ob[2] = 1; ob[3] = 1;
+        }
+        const cuuint32_t oe[4] = {1, 1, 1, 1};
+        bool ok = true;
+        for (int k = 0; k < 2 && ok; k++)
+            ok = enc(&tmo[k], CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, out[k ? 5 : 0], od, os, ob, oe,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+        if (ok) g.tma_out = 1;
+    }
     dim3 grid(p.ntiles_n, p.tiles_m, split);
-    limb_tma_kernel<<<grid, NTHREADS, smem_bytes(), c->stream>>>(tm, g);
+    limb_tma_kernel<<<grid, NTHREADS, smem_bytes(), c->stream>>>(tm, tmo[0], tmo[1], g);
     c->launches++;
     int st = launch_status(c, "limb_tma_kernel");
     if (st) return st;
