@@ -51,6 +51,7 @@ struct NetLayer {
     lt::Plan plan;
     int split, cps;
     uint8_t *packB;
+    int u64 = 0;  // the plain u64 form timed faster for this layer at set-up (small layers)
 };
 
 struct pg_net {
@@ -169,6 +170,64 @@ static int net_limb_layer(pg_net *net, NetLayer &L, const uint64_t *const *in) {
     return PG_OK;
 }
 
+// The same FC / CNN layer in the plain u64 form (FCLayer.cu:101-116,
+// CNNLayer.cu:95-99).
+static int net_u64_layer(pg_net *net, NetLayer &L, const uint64_t *const *in) {
+    Ctx *c = net->ctx;
+    if (L.type == PG_LAYER_FC) {
+        const uint64_t *const *bias = L.b_n ? (const uint64_t *const *)L.b : nullptr;
+        return rss_matmul<uint64_t>(c, in, (const uint64_t *const *)L.w, L.out, bias, net->batch, L.p[1], L.p[0], 1,
+                                    1, 1, net->fp);
+    }
+    return rss_conv<uint64_t>(c, in, (const uint64_t *const *)L.w, L.out, PG_CONV_FPROP, net->batch, L.p[0], L.p[1],
+                              L.p[4], L.p[2], L.p[3], L.p[5], L.p[6], net->fp);
+}
+
+// Per FC / CNN layer of a limb-form network, the form that runs it faster:
+// both are timed on the layer's own buffers (one warm-up, then three runs
+// each, CUDA events on the context's stream; the outputs are overwritten by
+// the first real forward), and the u64 form is kept only if it wins by 3 %.
+// Both compute the same bits. Communication and launch counters are restored.
+static int net_choose_forms(pg_net *net) {
+    Ctx *c = net->ctx;
+    if (!c->autotune) return PG_OK;
+    uint64_t comm0[9];
+    memcpy(comm0, c->comm, sizeof(comm0));
+    const uint64_t launches0 = c->launches.load();
+    cudaEvent_t e0, e1;
+    PG_CHECK_CUDA(c, cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return set_error(c, PG_ERR_CUDA, "cudaEventCreate failed");
+    }
+    int st = PG_OK;
+    for (size_t li = 0; li < net->layers.size() && !st; li++) {
+        NetLayer &L = net->layers[li];
+        if (L.type != PG_LAYER_FC && L.type != PG_LAYER_CNN) continue;
+        const uint64_t *const *in = li ? (const uint64_t *const *)net->layers[li - 1].out
+                                       : (const uint64_t *const *)net->in;
+        float ms[2] = {0.f, 0.f};
+        for (int form = 0; form < 2 && !st; form++) {
+            for (int r = 0; r < 4 && !st; r++) {
+                if (r == 1 && cudaEventRecord(e0, c->stream) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
+                if (!st) st = form ? net_u64_layer(net, L, in) : net_limb_layer(net, L, in);
+            }
+            if (!st && cudaEventRecord(e1, c->stream) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
+            if (!st && cudaEventSynchronize(e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
+            if (!st && cudaEventElapsedTime(&ms[form], e0, e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
+        }
+        if (!st) L.u64 = ms[1] < 0.97f * ms[0];
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    // the zero shares of a limb layer's output stay 0 only if the u64 runs did
+    // not leave values there: the u64 form writes every share, with the same
+    // zeros, so they are still 0
+    memcpy(c->comm, comm0, sizeof(comm0));
+    c->launches.store(launches0);
+    return st;
+}
+
 // Per-layer timing events: inside a stream capture they must be external
 // event nodes so that graph replays record them; outside, a plain record.
 static int record_event(Ctx *c, cudaEvent_t e) {
@@ -188,6 +247,7 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
         if (cs != cudaStreamCaptureStatusNone)
             return set_error(c, PG_ERR_INVALID_ARG, "limb-form buffers must be set up by an eager forward first");
         int st = net_limb_setup(net);
+        if (!st) st = net_choose_forms(net);
         if (st) return st;
     }
     for (size_t li = 0; li < net->layers.size(); li++) {
@@ -198,14 +258,14 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
             case PG_LAYER_FC: {
                 const uint64_t *const *bias = L.b_n ? (const uint64_t *const *)L.b : nullptr;
                 st = c->form == PG_FORM_LIMB_TC
-                         ? net_limb_layer(net, L, cur)
+                         ? (L.u64 ? net_u64_layer(net, L, cur) : net_limb_layer(net, L, cur))
                          : rss_matmul<uint64_t>(c, cur, (const uint64_t *const *)L.w, L.out, bias, net->batch, L.p[1],
                                                 L.p[0], 1, 1, 1, net->fp);
                 break;
             }
             case PG_LAYER_CNN:
                 st = c->form == PG_FORM_LIMB_TC
-                         ? net_limb_layer(net, L, cur)
+                         ? (L.u64 ? net_u64_layer(net, L, cur) : net_limb_layer(net, L, cur))
                          : rss_conv<uint64_t>(c, cur, (const uint64_t *const *)L.w, L.out, PG_CONV_FPROP, net->batch,
                                               L.p[0], L.p[1], L.p[4], L.p[2], L.p[3], L.p[5], L.p[6], net->fp);
                 break;
