@@ -54,6 +54,7 @@
 
 #include "pg_common.cuh"
 #include "pg_limb_tma.cuh"
+#include "pg_relu_value.cuh"
 #include "pg_tcgen05.cuh"
 
 namespace pg {
@@ -247,6 +248,82 @@ __global__ void image_kernel(const __grid_constant__ ImageArgs ia) {
         digits8<8>(v, pl);
 #pragma unroll
         for (int i = 0; i < 8; i++) ia.img[((long long)(seg * 8 + i) * ia.C8 + cb) * ia.pixels + pix] = pl[i];
+    }
+}
+
+// ReLU fused with the digit image of the convolution it feeds: a block of
+// 256 threads takes 16 pixels x 16 channels (one 128-byte line of each
+// share per pixel). Each thread runs the ReLU of one value (dReLU +
+// selectShare, RSS.inl:807-865, all three parties) and writes the layer's
+// shares and bit shares; then 192 threads turn the block's 16 pixels x 2
+// channel groups x 6 shares into the next convolution's fp16 digit planes,
+// consecutive threads on consecutive pixels. The image launch and its
+// re-read of the ReLU output are saved.
+struct ReluImageArgs {
+    const uint64_t *in[6];
+    uint64_t *out[6];
+    uint8_t *dout[6];
+    uint4 *img;
+    long long pixels, pixels_alloc;
+    int C8;
+};
+
+constexpr int RI_PIX = 16, RI_CH = 16, RI_PITCH = RI_PIX + 1;  // pitch 17: two-way bank conflicts at most
+
+__global__ void __launch_bounds__(256) relu_image_kernel(const __grid_constant__ ReluImageArgs a) {
+    __shared__ uint64_t zs[6][RI_CH][RI_PITCH];
+    const int C16 = a.C8 >> 1;
+    const long long C = 8ll * a.C8;
+    const long long ptiles = (a.pixels + RI_PIX - 1) / RI_PIX;
+    const long long tiles = ptiles * C16;
+    const int t = threadIdx.x;
+    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int cp = (int)(tile % C16);
+        const long long p0 = (tile / C16) * RI_PIX;
+        {
+            const int pl = t / RI_CH, ch = t % RI_CH;
+            const long long pix = p0 + pl;
+            uint64_t z[3][2];
+            if (pix < a.pixels) {
+                const long long idx = pix * C + cp * RI_CH + ch;
+                uint64_t x[3][2], zero[3][2];
+                uint8_t r[3][2];
+#pragma unroll
+                for (int k = 0; k < 6; k++) {
+                    x[k >> 1][k & 1] = __ldg(a.in[k] + idx);
+                    zero[k >> 1][k & 1] = 0;
+                }
+                drelu_value<uint64_t, uint8_t>(x, r);
+                select_value<uint64_t, uint8_t>(zero, x, r, z);
+#pragma unroll
+                for (int k = 0; k < 6; k++) {
+                    a.out[k][idx] = z[k >> 1][k & 1];
+                    if (a.dout[k]) a.dout[k][idx] = r[k >> 1][k & 1];
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 6; k++) z[k >> 1][k & 1] = 0;
+            }
+#pragma unroll
+            for (int k = 0; k < 6; k++) zs[k][ch][pl] = z[k >> 1][k & 1];
+        }
+        __syncthreads();
+        if (t < 6 * 2 * RI_PIX) {
+            const int seg = t / (2 * RI_PIX), half = (t / RI_PIX) & 1, pl = t % RI_PIX;
+            const long long pix = p0 + pl;
+            if (pix < a.pixels) {
+                uint64_t v[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) v[i] = zs[seg][half * 8 + i][pl];
+                uint4 plv[8];
+                digits8<8>(v, plv);
+                const int cb = 2 * cp + half;
+#pragma unroll
+                for (int i = 0; i < 8; i++)
+                    a.img[((long long)(seg * 8 + i) * a.C8 + cb) * a.pixels_alloc + pix] = plv[i];
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -1090,6 +1167,34 @@ int tune_split(Ctx *c, const Plan &p, const void *image, const void *packB, uint
     if (st) return st;
     c->split_cache[key] = {split, cps};
     return PG_OK;
+}
+
+bool relu_image_fits(const Plan &p, size_t n) {
+    return p.implicit && p.src_mode == SRC_ROWS && p.C == p.Kreal && p.C % 16 == 0 && p.ld == p.C &&
+           (size_t)p.pixels * p.C == n;
+}
+
+int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n, uint64_t *const out[6],
+                   uint8_t *const dout[6], void *image) {
+    if (!relu_image_fits(p, n)) return set_error(c, PG_ERR_INVALID_ARG, "relu/image geometry mismatch");
+    ReluImageArgs a;
+    memset(&a, 0, sizeof(a));
+    for (int k = 0; k < 6; k++) {
+        if (!in[k] || !out[k]) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+        a.in[k] = in[k];
+        a.out[k] = out[k];
+        a.dout[k] = dout ? dout[k] : nullptr;
+    }
+    a.img = (uint4 *)image;
+    a.pixels = p.pixels;
+    a.pixels_alloc = p.pixels_alloc;
+    a.C8 = p.C / 8;
+    const long long tiles = (long long)(a.C8 / 2) * ((p.pixels + RI_PIX - 1) / RI_PIX);
+    const int sms = c->sm_count > 0 ? c->sm_count : 148;
+    long long blocks = tiles < (long long)sms * 16 ? tiles : (long long)sms * 16;
+    relu_image_kernel<<<(unsigned)blocks, 256, 0, c->stream>>>(a);
+    c->launches++;
+    return launch_status(c, "relu_image_kernel");
 }
 
 int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image) {

@@ -46,6 +46,11 @@ int tune_split(Ctx *c, const Plan &p, const void *image, const void *packB, uint
 // A shares -> digit-plane image; weight shares -> packed stage images; then the GEMM (+ split-K reduction)
 int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image);
 int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB);
+// ReLU of n values fused with the digit image of the implicit convolution
+// (plan p) that takes them as input; relu_image_fits says whether it applies
+bool relu_image_fits(const Plan &p, size_t n);
+int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n, uint64_t *const out[6],
+                   uint8_t *const dout[6], void *image);
 // zeros_kept: the four output shares that dividePublic3out3 leaves at 0 (all
 // but party A's shareA and party C's shareB) already hold 0 and are only
 // written where a bias share is added (the network's zeroed arena).

@@ -36,6 +36,7 @@ int limb3_rss_matmul_u64(Ctx *, const uint64_t *const *, const uint64_t *const *
                          const uint64_t *const *, int, int, int, int, int, int, int);
 int limb3_rss_conv_u64(Ctx *, const uint64_t *const *, const uint64_t *const *, uint64_t *const *, int, int, int, int,
                        int, int, int, int, int, int);
+void count_relu_u64_u8(Ctx *, size_t);
 }  // namespace pg
 
 using namespace pg;
@@ -152,9 +153,9 @@ static int net_limb_setup(pg_net *net) {
 // One FC / CNN layer in the limb form: digit image of the input, GEMM over
 // the packed weights (+ split-K reduction), then the message accounting of
 // matmul / convolution (RSS.inl:517-538, :790-802).
-static int net_limb_layer(pg_net *net, NetLayer &L, const uint64_t *const *in) {
+static int net_limb_layer(pg_net *net, NetLayer &L, const uint64_t *const *in, bool image_ready = false) {
     Ctx *c = net->ctx;
-    int st = lt::run_image(c, L.plan, in, net->limb_image);
+    int st = image_ready ? PG_OK : lt::run_image(c, L.plan, in, net->limb_image);
     if (st) return st;
     const uint64_t *const *bias = L.b_n ? (const uint64_t *const *)L.b : nullptr;
     // The arena is zeroed when the network is created and a layer's output
@@ -250,9 +251,12 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
         if (!st) st = net_choose_forms(net);
         if (st) return st;
     }
+    bool ready_next = false;  // the previous ReLU wrote this layer's digit image
     for (size_t li = 0; li < net->layers.size(); li++) {
         NetLayer &L = net->layers[li];
         int st = PG_OK;
+        const bool image_ready = ready_next;
+        ready_next = false;
         if (!net->ev.empty() && (st = record_event(c, net->ev[2 * li]))) return st;
         switch (L.type) {
             case PG_LAYER_FC: {
@@ -265,11 +269,24 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
             }
             case PG_LAYER_CNN:
                 st = c->form == PG_FORM_LIMB_TC
-                         ? (L.u64 ? net_u64_layer(net, L, cur) : net_limb_layer(net, L, cur))
+                         ? (L.u64 ? net_u64_layer(net, L, cur) : net_limb_layer(net, L, cur, image_ready))
                          : rss_conv<uint64_t>(c, cur, (const uint64_t *const *)L.w, L.out, PG_CONV_FPROP, net->batch,
                                               L.p[0], L.p[1], L.p[4], L.p[2], L.p[3], L.p[5], L.p[6], net->fp);
                 break;
-            case PG_LAYER_RELU: st = rss_relu<uint64_t, uint8_t>(c, cur, L.in_n, L.out, L.d); break;
+            case PG_LAYER_RELU: {
+                // a ReLU that feeds a limb-form implicit convolution also writes
+                // that convolution's digit image (the layer outputs as before)
+                NetLayer *next = li + 1 < net->layers.size() ? &net->layers[li + 1] : nullptr;
+                if (c->form == PG_FORM_LIMB_TC && net->limb_arena && next && next->type == PG_LAYER_CNN &&
+                    !next->u64 && lt::relu_image_fits(next->plan, L.in_n)) {
+                    st = lt::run_relu_image(c, next->plan, cur, L.in_n, L.out, L.d, net->limb_image);
+                    if (!st) count_relu_u64_u8(c, L.in_n);
+                    ready_next = !st;
+                } else {
+                    st = rss_relu<uint64_t, uint8_t>(c, cur, L.in_n, L.out, L.d);
+                }
+                break;
+            }
             case PG_LAYER_MAXPOOL:
                 st = rss_maxpool_layer<uint64_t, uint8_t>(c, cur, L.out, L.d, L.p[0], L.p[1], L.p[2], L.p[3], L.p[4],
                                                           net->batch, net->fp);

@@ -131,6 +131,13 @@ int rss_select(Ctx *c, const T *const x[6], const T *const y[6], const U *const 
 
 template int rss_drelu<uint64_t, uint8_t>(Ctx *, const uint64_t *const *, size_t, uint8_t *const *);
 template int rss_drelu<uint64_t, uint64_t>(Ctx *, const uint64_t *const *, size_t, uint64_t *const *);
+// the messages of ReLU (dReLU + selectShare) on n uint64 values with uint8
+// bit shares, for kernels that fuse the ReLU into other work
+void count_relu_u64_u8(Ctx *c, size_t n) {
+    count_drelu<uint64_t, uint8_t>(c, n);
+    count_select<uint64_t, uint8_t>(c, n);
+}
+
 template int rss_relu<uint64_t, uint8_t>(Ctx *, const uint64_t *const *, size_t, uint64_t *const *, uint8_t *const *);
 template int rss_relu<uint64_t, uint64_t>(Ctx *, const uint64_t *const *, size_t, uint64_t *const *, uint64_t *const *);
 template int rss_relu<uint32_t, uint8_t>(Ctx *, const uint32_t *const *, size_t, uint32_t *const *, uint8_t *const *);
