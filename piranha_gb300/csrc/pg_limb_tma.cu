@@ -1078,6 +1078,8 @@ size_t tune_partial_bytes(const Plan &p, int sms) {
 
 static std::string tune_key(const Plan &p);
 
+std::string plan_key(const Plan &p) { return tune_key(p); }
+
 // the context's tuned choice for this shape, if any
 bool cached_split(Ctx *c, const Plan &p, int &split, int &cps) {
     auto it = c->split_cache.find(tune_key(p));

@@ -6,6 +6,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <string>
+
 namespace pg {
 struct Ctx;
 namespace lt {
@@ -40,6 +42,8 @@ size_t partial_bytes(const Plan &p, int split);
 // choice (cached per shape in the context; timed when the context allows)
 size_t tune_partial_bytes(const Plan &p, int sms);
 bool cached_split(Ctx *c, const Plan &p, int &split, int &chunks_per_split);
+// the shape key of a plan in the context's tuning cache
+std::string plan_key(const Plan &p);
 int tune_split(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial,
                uint64_t *const out[6], const uint64_t *const bias[6], int trunc, bool zeros_kept, uint64_t *raw,
                int &split, int &chunks_per_split);

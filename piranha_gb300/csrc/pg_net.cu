@@ -205,6 +205,14 @@ static int net_choose_forms(pg_net *net) {
     for (size_t li = 0; li < net->layers.size() && !st; li++) {
         NetLayer &L = net->layers[li];
         if (L.type != PG_LAYER_FC && L.type != PG_LAYER_CNN) continue;
+        // the choice is cached with the split-K choices (and so in a tuning
+        // cache file): 1 = limb form, 2 = u64 form
+        const std::string key = "form/" + std::to_string(L.type) + "/" + lt::plan_key(L.plan);
+        auto it = c->split_cache.find(key);
+        if (it != c->split_cache.end()) {
+            L.u64 = it->second.first == 2;
+            continue;
+        }
         const uint64_t *const *in = li ? (const uint64_t *const *)net->layers[li - 1].out
                                        : (const uint64_t *const *)net->in;
         float ms[2] = {0.f, 0.f};
@@ -217,7 +225,10 @@ static int net_choose_forms(pg_net *net) {
             if (!st && cudaEventSynchronize(e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
             if (!st && cudaEventElapsedTime(&ms[form], e0, e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
         }
-        if (!st) L.u64 = ms[1] < 0.97f * ms[0];
+        if (!st) {
+            L.u64 = ms[1] < 0.97f * ms[0];
+            c->split_cache[key] = {L.u64 ? 2 : 1, 1};
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
