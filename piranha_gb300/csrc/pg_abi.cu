@@ -389,7 +389,7 @@ int pg_rss_fc_forward_u64(pg_ctx *c, const uint64_t *const x[6], const uint64_t 
 int pg_rss_conv_u64(pg_ctx *c, const uint64_t *const A[6], const uint64_t *const B[6], uint64_t *const C[6], int op,
                     int batch, int H, int W, int f, int Din, int Dout, int stride, int pad, int trunc) {
     CTX_OR_FAIL(c);
-    if (c->form == PG_FORM_LIMB_TC && op == PG_CONV_FPROP)
+    if (c->form == PG_FORM_LIMB_TC)
         return limb3_rss_conv_u64(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc);
     return rss_conv<uint64_t>(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc);
 }

@@ -1382,8 +1382,9 @@ static int run_with_scratch(Ctx *c, const lt::Plan &p, const uint64_t *const a[6
     return PG_OK;
 }
 
-int limb3_rss_matmul_u64(Ctx *c, const uint64_t *const a[6], const uint64_t *const b[6], uint64_t *const out[6],
-                         const uint64_t *const bias[6], int M, int N, int K, int tA, int tB, int tC, int trunc) {
+static int limb3_rss_matmul_impl(Ctx *c, const uint64_t *const a[6], const uint64_t *const b[6],
+                                 uint64_t *const out[6], const uint64_t *const bias[6], int M, int N, int K, int tA,
+                                 int tB, int tC, int trunc) {
     CSh6<uint64_t> ca, cb;
     Sh6<uint64_t> co;
     if (!load6(ca, a) || !load6(cb, b) || !load6(co, out)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
@@ -1394,8 +1395,9 @@ int limb3_rss_matmul_u64(Ctx *c, const uint64_t *const a[6], const uint64_t *con
     return run_with_scratch(c, p, a, b, out, bias, trunc);
 }
 
-int limb3_rss_conv_u64(Ctx *c, const uint64_t *const A[6], const uint64_t *const B[6], uint64_t *const C[6], int op,
-                       int batch, int H, int W, int f, int Din, int Dout, int stride, int pad, int trunc) {
+static int limb3_rss_conv_impl(Ctx *c, const uint64_t *const A[6], const uint64_t *const B[6], uint64_t *const C[6],
+                               int op, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad,
+                               int trunc) {
     CSh6<uint64_t> ca, cb;
     Sh6<uint64_t> co;
     if (!load6(ca, A) || !load6(cb, B) || !load6(co, C)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
@@ -1461,6 +1463,78 @@ int limb3_rss_conv_u64(Ctx *c, const uint64_t *const A[6], const uint64_t *const
     comm_msg(c, 2 * n_out * 8, 2 * n_out * 8);
     comm_round(c);
     return PG_OK;
+}
+
+template <typename T>
+int rss_matmul(Ctx *, const T *const *, const T *const *, T *const *, const T *const *, int, int, int, int, int, int,
+               int);
+template <typename T>
+int rss_conv(Ctx *, const T *const *, const T *const *, T *const *, int, int, int, int, int, int, int, int, int, int);
+
+// The form of a standalone share-GEMM / convolution in the limb context: the
+// context's cached choice for the shape, else (autotuning on, no capture in
+// progress) the faster of the limb and the plain u64 form, timed on the
+// call's own operands (one warm-up and three runs each; both give the same
+// bits; counters restored), else the limb form. Small or narrow problems (a
+// weight gradient with 25 x 20 outputs, say) can run faster on the CUDA
+// cores. Cached as 1 (limb) or 2 (u64).
+template <typename FL, typename FU> static int run_picked(Ctx *c, const std::string &key, FL limb, FU u64) {
+    int choice = 1;
+    auto it = c->split_cache.find(key);
+    if (it != c->split_cache.end()) {
+        choice = it->second.first;
+    } else if (c->autotune) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        PG_CHECK_CUDA(c, cudaStreamIsCapturing(c->stream, &cs));
+        if (cs == cudaStreamCaptureStatusNone) {
+            uint64_t comm0[9];
+            memcpy(comm0, c->comm, sizeof(comm0));
+            const uint64_t launches0 = c->launches.load();
+            cudaEvent_t e0, e1;
+            PG_CHECK_CUDA(c, cudaEventCreate(&e0));
+            if (cudaEventCreate(&e1) != cudaSuccess) {
+                cudaEventDestroy(e0);
+                return set_error(c, PG_ERR_CUDA, "cudaEventCreate failed");
+            }
+            float ms[2] = {0.f, 0.f};
+            int st = PG_OK;
+            for (int f = 0; f < 2 && !st; f++) {
+                for (int r = 0; r < 4 && !st; r++) {
+                    if (r == 1 && cudaEventRecord(e0, c->stream) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
+                    if (!st) st = f ? u64() : limb();
+                }
+                if (!st && cudaEventRecord(e1, c->stream) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
+                if (!st && cudaEventSynchronize(e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
+                if (!st && cudaEventElapsedTime(&ms[f], e0, e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            memcpy(c->comm, comm0, sizeof(comm0));
+            c->launches.store(launches0);
+            if (st) return st;
+            choice = ms[1] < 0.97f * ms[0] ? 2 : 1;
+            c->split_cache[key] = {choice, 1};
+        }
+    }
+    return choice == 2 ? u64() : limb();
+}
+
+int limb3_rss_matmul_u64(Ctx *c, const uint64_t *const a[6], const uint64_t *const b[6], uint64_t *const out[6],
+                         const uint64_t *const bias[6], int M, int N, int K, int tA, int tB, int tC, int trunc) {
+    const std::string key = "sform/mm/" + std::to_string(M) + "/" + std::to_string(N) + "/" + std::to_string(K) +
+                            "/" + std::to_string(tA) + std::to_string(tB) + std::to_string(tC) + (bias ? "b" : "");
+    return run_picked(
+        c, key, [&] { return limb3_rss_matmul_impl(c, a, b, out, bias, M, N, K, tA, tB, tC, trunc); },
+        [&] { return rss_matmul<uint64_t>(c, a, b, out, bias, M, N, K, tA, tB, tC, trunc); });
+}
+
+int limb3_rss_conv_u64(Ctx *c, const uint64_t *const A[6], const uint64_t *const B[6], uint64_t *const C[6], int op,
+                       int batch, int H, int W, int f, int Din, int Dout, int stride, int pad, int trunc) {
+    char k[160];
+    snprintf(k, sizeof(k), "sform/conv/%d/%d/%d/%d/%d/%d/%d/%d/%d", op, batch, H, W, f, Din, Dout, stride, pad);
+    return run_picked(
+        c, k, [&] { return limb3_rss_conv_impl(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc); },
+        [&] { return rss_conv<uint64_t>(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc); });
 }
 
 int limb_prepare_current_device(Ctx *c) { return lt::prepare_device(c); }

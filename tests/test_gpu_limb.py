@@ -32,7 +32,10 @@ def pg():
 
 @pytest.fixture()
 def ctx(pg):
+    # no timing-based choices here: every call runs the limb kernel, with the
+    # heuristic split-K (the tuner has its own tests below)
     c = pg.Context(0, form=pg.FORM_LIMB_TC)
+    c.set_autotune(False)
     yield c
     c.check_device_errors()
     c.close()
@@ -231,3 +234,38 @@ def test_tune_cache_round_trip(pg, tmp_path):
     with pytest.raises(pg.PiranhaError):
         c2.tune_load(path)
     c2.close()
+
+
+def test_form_pick_same_bits(pg, tmp_path):
+    """With autotuning on, a standalone call runs in whichever form timed
+    faster for its shape (cached in the tuning file as sform/...): the bits
+    are those of the oracle either way."""
+    cases = [("conv", (orc.WGRAD, 4, 28, 28, 5, 1, 20, 1, 0)), ("conv", (orc.DGRAD, 4, 12, 12, 5, 20, 50, 1, 0)),
+             ("mm", (64, 10, 256))]
+    c = pg.Context(0, form=pg.FORM_LIMB_TC)
+    for kind, args in cases:
+        if kind == "conv":
+            op, batch, H, W, f, Din, Dout, stride, pad = args
+            P, Q = (H + 2 * pad - f) // stride + 1, (W + 2 * pad - f) // stride + 1
+            A = orc.random_views(batch * P * Q * Dout, U64, 91)
+            nb = Dout * f * f * Din if op == orc.DGRAD else batch * H * W * Din
+            B = orc.random_views(nb, U64, 92)
+            want = orc.convolution(A, B, op, batch, H, W, f, Din, Dout, stride, pad, 26)
+            for _ in range(2):
+                C = pg.empty_shares(want.shape[2])
+                pg.convolution(c, pg.to_device(A), pg.to_device(B), C, op, batch, H, W, f, Din, Dout, stride, pad, 26)
+                c.check_device_errors()
+                assert np.array_equal(pg.to_host(C), want)
+        else:
+            M, N, K = args
+            A, B = orc.random_views(M * K, U64, 93), orc.random_views(K * N, U64, 94)
+            want = orc.matmul(A, B, M, N, K, 1, 1, 1, 26)
+            for _ in range(2):
+                C = pg.empty_shares(M * N)
+                pg.matmul(c, pg.to_device(A), pg.to_device(B), C, M, N, K, 1, 1, 1, 26)
+                c.check_device_errors()
+                assert np.array_equal(pg.to_host(C), want)
+    path = str(tmp_path / "t.txt")
+    c.tune_save(path)
+    assert sum(1 for line in open(path) if line.startswith("sform/")) == 3
+    c.close()
