@@ -41,7 +41,9 @@ def test_vgg16_batch128_forms_agree(pg):
     batch = 128
     rng = np.random.default_rng(7)
     x = enc.share_random(enc.encode(rng.uniform(0, 1, batch * 3072)), seed=8)
-    got_tc, outs_tc, comm_tc = run_net(pg, layers, params, x, batch, capture=True, form=pg.FORM_LIMB_TC)
+    # with the tuner on, as the benchmark runs it (split-K and per-layer forms by timing)
+    got_tc, outs_tc, comm_tc = run_net(pg, layers, params, x, batch, capture=True, form=pg.FORM_LIMB_TC,
+                                       autotune=True)
     got_u64, outs_u64, comm_u64 = run_net(pg, layers, params, x, batch, capture=True, form=pg.FORM_U64)
     for i, (a, b) in enumerate(zip(outs_tc, outs_u64)):
         assert np.array_equal(a, b), f"layer {i} {layers[i]}"

@@ -29,8 +29,11 @@ def _wrap_device(ptr, n):
     return torch.as_tensor(_A(), device="cuda")
 
 
-def run_net(pg, layers, params, x, batch, capture=False, form=0):
+def run_net(pg, layers, params, x, batch, capture=False, form=0, autotune=False):
+    # autotune off by default: every FC / CNN layer of a limb-form network then
+    # runs the limb kernels (timing could pick the u64 form for small layers)
     ctx = pg.Context(0, form=form)
+    ctx.set_autotune(autotune)
     net = pg.Network(ctx, layers, batch)
     for i, prm in enumerate(params):
         if prm is not None:
@@ -191,6 +194,7 @@ def test_limb_weights_repacked_after_capture(pg):
     batch = 8
     x = orc.share_random(orc.encode(np.random.default_rng(43).uniform(0, 1, batch * 784)), seed=44)
     ctx = pg.Context(0, form=pg.FORM_LIMB_TC)
+    ctx.set_autotune(False)  # every layer in the limb form, so that its packed weights are what is tested
     net = pg.Network(ctx, layers, batch)
     for i, prm in enumerate(p1):
         if prm is not None:

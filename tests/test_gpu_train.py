@@ -86,6 +86,7 @@ def test_secureml_fixture_training_step(pg, golden, form):
     comm = orc.Comm()
     outs, new_params, deltas, softmax = oracle_step(layers, params, x, labels, 128, 9)
     ctx = pg.Context(0, form=pg.FORM_LIMB_TC if form == "tc" else pg.FORM_U64)
+    ctx.set_autotune(False)  # every share-GEMM / conv then runs in the form under test
     net = make_net(pg, ctx, layers, params, 128)
     ctx.reset_comm()
     net.train_step(pg.to_device(x), pg.to_device(labels), 9)
@@ -129,6 +130,7 @@ def test_lenet_training_step(pg, form):
     labels = one_hot_labels(batch, 10, 14)
     outs, new_params, deltas, softmax = oracle_step(layers, params, x, labels, batch, 5)
     ctx = pg.Context(0, form=pg.FORM_LIMB_TC if form == "tc" else pg.FORM_U64)
+    ctx.set_autotune(False)  # every share-GEMM / conv then runs in the form under test
     net = make_net(pg, ctx, layers, params, batch)
     net.train_step(pg.to_device(x), pg.to_device(labels), 5)
     ctx.sync()
@@ -151,6 +153,7 @@ def test_lenet_training_captured_two_steps(pg, form):
     _, p1, _, _ = oracle_step(layers, params, x, labels, batch, 6)
     outs2, p2, deltas2, softmax2 = oracle_step(layers, p1, x, labels, batch, 6)
     ctx = pg.Context(0, form=pg.FORM_LIMB_TC if form == "tc" else pg.FORM_U64)
+    ctx.set_autotune(False)  # every share-GEMM / conv then runs in the form under test
     net = make_net(pg, ctx, layers, params, batch)
     net.train_step(pg.to_device(x), pg.to_device(labels), 6)  # sets up the training buffers eagerly
     for i, prm in enumerate(params):  # back to the initial parameters
