@@ -575,6 +575,7 @@ template <typename T, typename U> void rss_relu(const RSSV<T>& in, RSSV<T>& out,
 // expandCompare (bitwise.cuh:66-92), in-bounds part
 template <typename U>
 void expand_compare(const std::vector<U>& b, const std::vector<U>& nb, std::vector<U>& expanded) {
+    if (b.empty()) return;  // bitwise.cuh:70 divides by b.size(): empty pool rows have nothing to expand
     size_t f = (expanded.size() / b.size()) / 2;
     for (size_t i = 0; i < b.size(); i++)
         for (size_t e = 0; e < 2 * f; e++) expanded[i * 2 * f + e] = e < f ? b[i] : nb[i];

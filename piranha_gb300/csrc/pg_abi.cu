@@ -399,7 +399,7 @@ int pg_rss_divide_public_u64(pg_ctx *c, uint64_t *const a[6], size_t n, uint64_t
 }
 int pg_rss_divide_public_vec_u64(pg_ctx *c, uint64_t *const a[6], size_t n, const uint64_t *d) {
     CTX_OR_FAIL(c);
-    if (!d) return set_error(c, PG_ERR_INVALID_ARG, "null denominators");
+    if (!d && n) return set_error(c, PG_ERR_INVALID_ARG, "null denominators");
     return rss_divide_public<uint64_t>(c, a, n, 0, d);
 }
 int pg_rss_divide_public_u32(pg_ctx *c, uint32_t *const a[6], size_t n, uint32_t d) {

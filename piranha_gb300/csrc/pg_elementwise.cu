@@ -163,7 +163,8 @@ __global__ void maxpool_im2row_kernel(const uint64_t *im, uint64_t *out, int H, 
 
 template <typename T> int rss_reconstruct(Ctx *c, const T *const a[6], size_t n, T *const out[3]) {
     CSh6<T> ca;
-    if (!load6(ca, a) || !out || !out[0] || !out[1] || !out[2]) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+    if (n && (!load6(ca, a) || !out || !out[0] || !out[1] || !out[2]))
+        return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
     Pub3<T> o{{out[0], out[1], out[2]}};
     if (n) {
         reconstruct_kernel<T><<<grid1(c, n), 256, 0, c->stream>>>(ca, n, o);
@@ -179,8 +180,10 @@ template <typename T> int rss_reconstruct(Ctx *c, const T *const a[6], size_t n,
 template <typename T> int rss_reshare(Ctx *c, const T *const cin[3], size_t n, T *const out[6]) {
     if (c->prg_on) return rss_reshare_prg<T>(c, cin, n, out);
     Sh6<T> o;
-    if (!cin || !cin[0] || !cin[1] || !cin[2] || !load6(o, out)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
-    Pub3<T> ci{{(T *)cin[0], (T *)cin[1], (T *)cin[2]}};
+    if (n && (!cin || !cin[0] || !cin[1] || !cin[2] || !load6(o, out)))
+        return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+    Pub3<T> ci{};
+    if (n) ci = Pub3<T>{{(T *)cin[0], (T *)cin[1], (T *)cin[2]}};
     if (n) {
         reshare_kernel<T><<<grid1(c, n), 256, 0, c->stream>>>(ci, n, o);
         c->launches++;
@@ -196,7 +199,7 @@ template <typename T, bool AND> int rss_mul(Ctx *c, T *const a[6], const T *cons
     if (c->prg_on) return rss_mul_prg<T, AND>(c, a, b, n);
     Sh6<T> ca;
     CSh6<T> cb;
-    if (!load6(ca, a) || !load6(cb, b)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+    if (n && (!load6(ca, a) || !load6(cb, b))) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
     if (n) {
         mul_kernel<T, AND><<<grid1(c, n), 256, 0, c->stream>>>(ca, cb, n);
         c->launches++;
@@ -210,7 +213,7 @@ template <typename T, bool AND> int rss_mul(Ctx *c, T *const a[6], const T *cons
 
 template <typename T> int rss_divide_public(Ctx *c, T *const a[6], size_t n, T d, const T *dvec) {
     Sh6<T> ca;
-    if (!load6(ca, a)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+    if (n && !load6(ca, a)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
     if (n) {
         divide_public_kernel<T><<<grid1(c, n), 256, 0, c->stream>>>(ca, n, d, pow2_shift<T>(d), dvec);
         c->launches++;
@@ -341,7 +344,7 @@ int local_u64(Ctx *c, int nbuf, int op, uint64_t *const *a, size_t n, int kind, 
     g.pubmask = nbuf == 6 ? (1 << 0) | (1 << 5) : nbuf == 2 ? 1 : (1 << 5) | (1 << 7) | (1 << 9);
     if (!a) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
     for (int k = 0; k < nbuf; k++) {
-        if (!a[k]) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+        if (n && !a[k]) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
         g.a[k] = a[k];
     }
     // the combinations the reference's share classes define
@@ -357,7 +360,7 @@ int local_u64(Ctx *c, int nbuf, int op, uint64_t *const *a, size_t n, int kind, 
     if (kind == PG_RHS_SHARES) {
         if (!shares) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
         for (int k = 0; k < nbuf; k++) {
-            if (!shares[k]) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+            if (n && !shares[k]) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
             g.sh[k] = shares[k];
         }
     }

@@ -463,9 +463,12 @@ int conv_u64(Ctx *c, const uint64_t *const A[12], const uint64_t *const B[12], u
 }
 
 template <typename T> int divide_public(Ctx *c, T *const a[12], size_t n, T d, const T *dvec) {
-    if (!ok12(a)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
     if (!dvec && d == 0) return set_error(c, PG_ERR_INVALID_ARG, "division by zero");
-    if (n == 0) return PG_OK;
+    if (n == 0) {  // no values: empty messages, the protocol's rounds still counted
+        reveal_comm(c, 0, sizeof(T));
+        return PG_OK;
+    }
+    if (!ok12(a)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
     divide_kernel<T><<<grid_for(c, n), 256, 0, c->stream>>>(cf<T>(a), mf<T>(a), n, d, dvec, pow2_shift<T>(d));
     c->launches++;
     int st = launch_status(c, "fpc divide_kernel");
@@ -475,8 +478,11 @@ template <typename T> int divide_public(Ctx *c, T *const a[12], size_t n, T d, c
 }
 
 template <typename T> int reconstruct(Ctx *c, const T *const a[12], size_t n, T *const out[4]) {
+    if (n == 0) {  // no values: empty messages, the protocol's rounds still counted
+        reveal_comm(c, 0, sizeof(T));
+        return PG_OK;
+    }
     if (!ok12(a) || !out || !out[0] || !out[1] || !out[2] || !out[3]) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
-    if (n == 0) return PG_OK;
     reconstruct_kernel<T><<<grid_for(c, n), 256, 0, c->stream>>>(cf<T>(a), out[0], out[1], out[2], out[3], n);
     c->launches++;
     int st = launch_status(c, "fpc reconstruct_kernel");
@@ -486,8 +492,11 @@ template <typename T> int reconstruct(Ctx *c, const T *const a[12], size_t n, T 
 }
 
 template <typename T, bool BOOL> int mul(Ctx *c, T *const a[12], const T *const b[12], size_t n) {
+    if (n == 0) {  // no values: empty messages, the protocol's rounds still counted
+        reshare_comm(c, 0, sizeof(T));
+        return PG_OK;
+    }
     if (!ok12(a) || !ok12(b)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
-    if (n == 0) return PG_OK;
     mul_kernel<T, BOOL><<<grid_for(c, n), 256, 0, c->stream>>>(mf<T>(a), cf<T>(b), n);
     c->launches++;
     int st = launch_status(c, "fpc mul_kernel");
@@ -497,8 +506,11 @@ template <typename T, bool BOOL> int mul(Ctx *c, T *const a[12], const T *const 
 }
 
 template <typename T, typename U> int drelu(Ctx *c, const T *const in[12], size_t n, U *const out[12]) {
+    if (n == 0) {  // no values: empty messages, the protocol's rounds still counted
+        drelu_comm<T, U>(c, 0);
+        return PG_OK;
+    }
     if (!ok12(in) || !ok12(out)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
-    if (n == 0) return PG_OK;
     drelu_kernel<T, U><<<grid_for(c, n), 256, 0, c->stream>>>(cf<T>(in), mf<U>(out), n);
     c->launches++;
     int st = launch_status(c, "fpc drelu_kernel");
@@ -509,8 +521,12 @@ template <typename T, typename U> int drelu(Ctx *c, const T *const in[12], size_
 
 template <typename T, typename U>
 int relu(Ctx *c, const T *const in[12], size_t n, T *const out[12], U *const dout[12]) {
+    if (n == 0) {  // no values: empty messages, the protocol's rounds still counted
+        drelu_comm<T, U>(c, 0);
+        select_comm<T, U>(c, 0);
+        return PG_OK;
+    }
     if (!ok12(in) || !ok12(out) || !ok12(dout)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
-    if (n == 0) return PG_OK;
     relu_kernel<T, U><<<grid_for(c, n), 256, 0, c->stream>>>(cf<T>(in), mf<T>(out), mf<U>(dout), n);
     c->launches++;
     int st = launch_status(c, "fpc relu_kernel");
@@ -522,8 +538,11 @@ int relu(Ctx *c, const T *const in[12], size_t n, T *const out[12], U *const dou
 
 template <typename T, typename U>
 int select_share(Ctx *c, const T *const x[12], const T *const y[12], const U *const b[12], T *const z[12], size_t n) {
+    if (n == 0) {  // no values: empty messages, the protocol's rounds still counted
+        select_comm<T, U>(c, 0);
+        return PG_OK;
+    }
     if (!ok12(x) || !ok12(y) || !ok12(b) || !ok12(z)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
-    if (n == 0) return PG_OK;
     select_kernel<T, U><<<grid_for(c, n), 256, 0, c->stream>>>(cf<T>(x), cf<T>(y), cf<U>(b), mf<T>(z), n);
     c->launches++;
     int st = launch_status(c, "fpc select_kernel");
@@ -534,7 +553,7 @@ int select_share(Ctx *c, const T *const x[12], const T *const y[12], const U *co
 
 template <typename T, typename U>
 int maxpool(Ctx *c, const T *const in[12], size_t n, int k, T *const out[12], U *const dout[12]) {
-    if (!ok12(in) || !ok12(out) || !ok12(dout)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+    if (n && (!ok12(in) || !ok12(out) || !ok12(dout))) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
     if (k < 2 || (k & (k - 1))) return set_error(c, PG_ERR_UNSUPPORTED, "maxpool rows of %d (a power of two >= 2)", k);
     if (n % (size_t)k) return set_error(c, PG_ERR_SIZE, "maxpool input %zu is not a multiple of %d", n, k);
     if (n == 0) return PG_OK;
@@ -606,7 +625,7 @@ int pg_fpc_divide_public_u64(pg_ctx *c, uint64_t *const a[12], size_t n, uint64_
 }
 int pg_fpc_divide_public_vec_u64(pg_ctx *c, uint64_t *const a[12], size_t n, const uint64_t *d) {
     FPC_CTX(c);
-    if (!d) return set_error(c, PG_ERR_INVALID_ARG, "null denominators");
+    if (!d && n) return set_error(c, PG_ERR_INVALID_ARG, "null denominators");
     return fpc::divide_public<uint64_t>(c, a, n, 0, d);
 }
 int pg_fpc_divide_public_u32(pg_ctx *c, uint32_t *const a[12], size_t n, uint32_t d) {

@@ -157,11 +157,11 @@ int rss_maxpool(Ctx *c, const T *const in[6], size_t n, int k, T *const out[6], 
     CSh6<T> a;
     Sh6<T> o;
     Sh6<U> d;
-    if (!load6(a, in) || !load6(o, out) || !load6(d, dout)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
     if (k != 4 && k != 16) return set_error(c, PG_ERR_UNSUPPORTED, "maxpool: k=%d (supported: 4, 16)", k);
     if (n % k) return set_error(c, PG_ERR_SIZE, "maxpool: n=%zu not a multiple of k=%d", n, k);
     size_t rows = n / k;
-    if (rows == 0) return PG_OK;
+    if (rows == 0) return PG_OK;  // the reference divides by the row count here (bitwise.cuh:70)
+    if (!load6(a, in) || !load6(o, out) || !load6(d, dout)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
     if (k == 4) maxpool_rows_kernel<T, U, 4><<<pool_grid(c, rows), 128, 0, c->stream>>>(a, rows, o, d);
     else maxpool_rows_kernel<T, U, 16><<<pool_grid(c, rows), 128, 0, c->stream>>>(a, rows, o, d);
     c->launches++;

@@ -286,9 +286,10 @@ int prg_set_keys(Ctx *c, const uint8_t *keys, uint64_t ctr) {
 
 template <typename T> int rss_reshare_prg(Ctx *c, const T *const cin[3], size_t n, T *const out[6]) {
     Sh6<T> o;
-    if (!cin || !cin[0] || !cin[1] || !cin[2] || !load6(o, out)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
-    Pub3<T> ci{{(T *)cin[0], (T *)cin[1], (T *)cin[2]}};
+    if (n && (!cin || !cin[0] || !cin[1] || !cin[2] || !load6(o, out)))
+        return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
     if (n) {
+        Pub3<T> ci{{(T *)cin[0], (T *)cin[1], (T *)cin[2]}};
         AesKeys k;
         memcpy(k.rk, c->prg_rk, sizeof(k.rk));
         reshare_prg_kernel<T><<<prg_grid(c, n), 256, 0, c->stream>>>(k, c->prg_ctr, ci, n, o);
@@ -305,7 +306,7 @@ template <typename T> int rss_reshare_prg(Ctx *c, const T *const cin[3], size_t 
 template <typename T, bool AND> int rss_mul_prg(Ctx *c, T *const a[6], const T *const b[6], size_t n) {
     Sh6<T> ca;
     CSh6<T> cb;
-    if (!load6(ca, a) || !load6(cb, b)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+    if (n && (!load6(ca, a) || !load6(cb, b))) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
     if (n) {
         AesKeys k;
         memcpy(k.rk, c->prg_rk, sizeof(k.rk));

@@ -86,8 +86,11 @@ template <typename T, typename U> void count_select(Ctx *c, size_t n) {
 template <typename T, typename U> int rss_drelu(Ctx *c, const T *const in[6], size_t n, U *const out[6]) {
     CSh6<T> a;
     Sh6<U> o;
+    if (n == 0) {  // no values: the protocol's messages are empty, its rounds still counted
+        count_drelu<T, U>(c, 0);
+        return PG_OK;
+    }
     if (!load6(a, in) || !load6(o, out)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
-    if (n == 0) return PG_OK;
     drelu_kernel<T, U><<<ew_grid(c, n), 256, 0, c->stream>>>(a, n, o);
     c->launches++;
     int st = launch_status(c, "drelu_kernel");
@@ -101,9 +104,13 @@ int rss_relu(Ctx *c, const T *const in[6], size_t n, T *const out[6], U *const d
     CSh6<T> a;
     Sh6<T> o;
     Sh6<U> d;
+    if (n == 0) {
+        count_drelu<T, U>(c, 0);
+        count_select<T, U>(c, 0);
+        return PG_OK;
+    }
     if (!load6(a, in) || !load6(o, out)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
     for (int i = 0; i < 6; i++) d.p[i] = dout ? dout[i] : nullptr;
-    if (n == 0) return PG_OK;
     relu_kernel<T, U><<<ew_grid(c, n), 256, 0, c->stream>>>(a, n, o, d);
     c->launches++;
     int st = launch_status(c, "relu_kernel");
@@ -118,9 +125,12 @@ int rss_select(Ctx *c, const T *const x[6], const T *const y[6], const U *const 
     CSh6<T> cx, cy;
     CSh6<U> cb;
     Sh6<T> cz;
+    if (n == 0) {
+        count_select<T, U>(c, 0);
+        return PG_OK;
+    }
     if (!load6(cx, x) || !load6(cy, y) || !load6(cb, b) || !load6(cz, z))
         return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
-    if (n == 0) return PG_OK;
     select_kernel<T, U><<<ew_grid(c, n), 256, 0, c->stream>>>(cx, cy, cb, n, cz);
     c->launches++;
     int st = launch_status(c, "select_kernel");

@@ -248,9 +248,12 @@ int conv_u64(Ctx *c, const uint64_t *const A[2], const uint64_t *const B[2], uin
 }
 
 template <typename T> int divide_public(Ctx *c, T *const a[2], size_t n, T d, const T *dvec) {
-    if (!ok2(a)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
     if (!dvec && d == 0) return set_error(c, PG_ERR_INVALID_ARG, "division by zero");
-    if (n == 0) return PG_OK;
+    if (n == 0) {  // no values: empty messages, the protocol's rounds still counted
+        reveal_comm(c, 0, sizeof(T));
+        return PG_OK;
+    }
+    if (!ok2(a)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
     divide_kernel<T><<<grid_for(c, n), 256, 0, c->stream>>>(a[0], a[1], a[0], a[1], n, d, dvec, pow2_of<T>(d),
                                                             nullptr, nullptr, 1, 1, 0);
     c->launches++;
@@ -261,8 +264,11 @@ template <typename T> int divide_public(Ctx *c, T *const a[2], size_t n, T d, co
 }
 
 template <typename T> int reconstruct(Ctx *c, const T *const a[2], size_t n, T *const out[2]) {
+    if (n == 0) {  // no values: empty messages, the protocol's rounds still counted
+        reveal_comm(c, 0, sizeof(T));
+        return PG_OK;
+    }
     if (!ok2(a) || !ok2(out)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
-    if (n == 0) return PG_OK;
     reconstruct_kernel<T><<<grid_for(c, n), 256, 0, c->stream>>>(a[0], a[1], out[0], out[1], n);
     c->launches++;
     int st = launch_status(c, "tpc reconstruct_kernel");
@@ -272,8 +278,12 @@ template <typename T> int reconstruct(Ctx *c, const T *const a[2], size_t n, T *
 }
 
 template <typename T> int mul(Ctx *c, T *const a[2], const T *const b[2], size_t n) {
+    if (n == 0) {  // no values: empty messages, the protocol's rounds still counted
+        reveal_comm(c, 0, sizeof(T));  // e = x + a
+        reveal_comm(c, 0, sizeof(T));  // f = y + b
+        return PG_OK;
+    }
     if (!ok2(a) || !ok2(b)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
-    if (n == 0) return PG_OK;
     mul_kernel<T><<<grid_for(c, n), 256, 0, c->stream>>>(a[0], a[1], b[0], b[1], n);
     c->launches++;
     int st = launch_status(c, "tpc mul_kernel");
@@ -293,8 +303,11 @@ template <typename T, typename U> static void drelu_comm(Ctx *c, uint64_t n) {
 }
 
 template <typename T, typename U> int drelu(Ctx *c, const T *const in[2], size_t n, U *const out[2]) {
+    if (n == 0) {  // no values: empty messages, the protocol's rounds still counted
+        drelu_comm<T, U>(c, 0);
+        return PG_OK;
+    }
     if (!ok2(in) || !ok2(out)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
-    if (n == 0) return PG_OK;
     drelu_kernel<T, U><<<grid_for(c, n), 256, 0, c->stream>>>(in[0], in[1], out[0], out[1], n);
     c->launches++;
     int st = launch_status(c, "tpc drelu_kernel");
@@ -311,8 +324,12 @@ template <typename T, typename U> static void select_comm(Ctx *c, uint64_t n) {
 
 template <typename T, typename U>
 int relu(Ctx *c, const T *const in[2], size_t n, T *const out[2], U *const dout[2]) {
+    if (n == 0) {  // no values: empty messages, the protocol's rounds still counted
+        drelu_comm<T, U>(c, 0);
+        select_comm<T, U>(c, 0);
+        return PG_OK;
+    }
     if (!ok2(in) || !ok2(out) || !ok2(dout)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
-    if (n == 0) return PG_OK;
     relu_kernel<T, U><<<grid_for(c, n), 256, 0, c->stream>>>(in[0], in[1], out[0], out[1], dout[0], dout[1], n);
     c->launches++;
     int st = launch_status(c, "tpc relu_kernel");
@@ -324,8 +341,11 @@ int relu(Ctx *c, const T *const in[2], size_t n, T *const out[2], U *const dout[
 
 template <typename T, typename U>
 int select_share(Ctx *c, const T *const x[2], const T *const y[2], const U *const b[2], T *const z[2], size_t n) {
+    if (n == 0) {  // no values: empty messages, the protocol's rounds still counted
+        select_comm<T, U>(c, 0);
+        return PG_OK;
+    }
     if (!ok2(x) || !ok2(y) || !ok2(b) || !ok2(z)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
-    if (n == 0) return PG_OK;
     select_kernel<T, U><<<grid_for(c, n), 256, 0, c->stream>>>(x[0], x[1], y[0], y[1], b[0], b[1], z[0], z[1], n);
     c->launches++;
     int st = launch_status(c, "tpc select_kernel");
@@ -336,7 +356,7 @@ int select_share(Ctx *c, const T *const x[2], const T *const y[2], const U *cons
 
 template <typename T, typename U>
 int maxpool(Ctx *c, const T *const in[2], size_t n, int k, T *const out[2], U *const dout[2]) {
-    if (!ok2(in) || !ok2(out) || !ok2(dout)) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+    if (n && (!ok2(in) || !ok2(out) || !ok2(dout))) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
     if (k != 4 && k != 16 && k != 2 && k != 8)
         return set_error(c, PG_ERR_UNSUPPORTED, "maxpool rows of %d (2, 4, 8 or 16 supported)", k);
     if (n % (size_t)k) return set_error(c, PG_ERR_SIZE, "maxpool input %zu is not a multiple of %d", n, k);
@@ -403,7 +423,7 @@ int pg_tpc_divide_public_u64(pg_ctx *c, uint64_t *const a[2], size_t n, uint64_t
 }
 int pg_tpc_divide_public_vec_u64(pg_ctx *c, uint64_t *const a[2], size_t n, const uint64_t *d) {
     TPC_CTX(c);
-    if (!d) return set_error(c, PG_ERR_INVALID_ARG, "null denominators");
+    if (!d && n) return set_error(c, PG_ERR_INVALID_ARG, "null denominators");
     return tpc::divide_public<uint64_t>(c, a, n, 0, d);
 }
 int pg_tpc_divide_public_u32(pg_ctx *c, uint32_t *const a[2], size_t n, uint32_t d) {

@@ -353,3 +353,27 @@ def test_fpc_local(pg, ctx, op, kind):
     pg.fpc.local_(ctx, ops[op], da, r_dev)
     ctx.sync()
     assert np.array_equal(host(da), orc.fpc_local(op, a, r_np))
+
+
+def test_fpc_empty_inputs(pg, ctx):
+    """Zero-length inputs: no launch, the oracle's rounds with empty messages."""
+    e = np.zeros((4, 3, 0), U64)
+    comm = orc.Comm(4)
+    a, b = pg.fpc.empty(0), pg.fpc.empty(0)
+    pg.fpc.reconstruct(ctx, a, dev(np.zeros((4, 0), U64)))
+    orc.fpc_reconstruct(e, comm)
+    pg.fpc.mul_(ctx, a, b)
+    orc.fpc_mul(e, e, comm)
+    pg.fpc.dividePublic(ctx, a, 3)
+    orc.fpc_divide_public(e.copy(), 3, comm)
+    pg.fpc.dReLU(ctx, a, pg.fpc.empty(0, "u8"))
+    orc.fpc_drelu(e, comm=comm)
+    pg.fpc.ReLU(ctx, a, pg.fpc.empty(0), pg.fpc.empty(0, "u8"))
+    orc.fpc_relu(e, comm=comm)
+    pg.fpc.selectShare(ctx, a, b, pg.fpc.empty(0, "u8"), pg.fpc.empty(0))
+    orc.fpc_select_share(e, e, np.zeros((4, 3, 0), U8), comm)
+    pg.fpc.local_(ctx, pg.OP_ADD, a, 5)
+    pg.fpc.maxpool(ctx, a, pg.fpc.empty(0), pg.fpc.empty(0, "u8"), 4)
+    ctx.sync()
+    check_comm(ctx, comm)
+    assert comm.rounds > 20

@@ -428,6 +428,47 @@ def test_invalid_arguments_return_status(pg, ctx):
     assert torch.count_nonzero(out).item() == 0
 
 
+def test_empty_inputs(pg, ctx):
+    """Zero-length inputs: every elementwise protocol step returns without a
+    launch, its messages empty and its rounds counted as the oracle counts them
+    (the reference sends its empty vectors). Empty CUDA tensors have null data
+    pointers, which a zero length allows."""
+    import torch
+
+    e, e8 = np.zeros((3, 2, 0), U64), np.zeros((3, 2, 0), U8)
+    comm = orc.Comm()
+    a, b = pg.empty_shares(0), pg.empty_shares(0)
+    assert pg.reconstruct(ctx, a).shape == (3, 0)
+    orc.reconstruct(e, comm)
+    pg.reshare(ctx, torch.empty((3, 0), dtype=torch.int64, device="cuda"), pg.empty_shares(0))
+    orc.reshare(np.zeros((3, 0), U64), comm)
+    pg.mul_(ctx, a, b)
+    orc.mul(e, e, comm)
+    pg.and_(ctx, a, b)
+    orc.and_(e, e, comm)
+    pg.and_(ctx, pg.empty_shares(0, "u8"), pg.empty_shares(0, "u8"))
+    orc.and_(e, e, comm)  # one round, no bytes, whatever the ring
+    pg.dividePublic(ctx, a, 3)
+    orc.divide_public(e.copy(), 3, comm)
+    pg.dividePublic(ctx, a, torch.empty(0, dtype=torch.int64, device="cuda"))
+    orc.divide_public(e.copy(), 3, comm)
+    pg.dReLU(ctx, a, pg.empty_shares(0, "u8"))
+    orc.drelu(e, comm=comm)
+    pg.ReLU(ctx, a, pg.empty_shares(0), pg.empty_shares(0, "u8"))
+    orc.relu(e, comm=comm)
+    pg.selectShare(ctx, a, b, pg.empty_shares(0, "u8"), pg.empty_shares(0))
+    orc.select_share(e, e, e8, comm)
+    for op in (pg.OP_ADD, pg.OP_XOR):
+        pg.local_(ctx, op, a, b)
+    pg.local_(ctx, pg.OP_MUL, a, 5)
+    # maxpool of no rows is a no-op (the reference divides by the row count)
+    pg.maxpool(ctx, a, pg.empty_shares(0), pg.empty_shares(0, "u8"), 4)
+    ctx.sync()
+    ctx.check_device_errors()
+    comm_equal(ctx, comm)
+    assert ctx.comm()["rounds"] > 20
+
+
 # ------------------------------------------------------------ local operators
 
 @pytest.mark.parametrize("op,kind", [("add", "scalar"), ("sub", "scalar"), ("mul", "scalar"), ("shr", "scalar"),

@@ -271,3 +271,27 @@ def test_tpc_local(pg, ctx, op, kind):
     pg.tpc.local_(ctx, ops[op], da, r_dev)
     ctx.sync()
     assert np.array_equal(host(da), orc.tpc_local(op, a, r_np))
+
+
+def test_tpc_empty_inputs(pg, ctx):
+    """Zero-length inputs: no launch, the oracle's rounds with empty messages."""
+    e = np.zeros((2, 0), U64)
+    comm = orc.Comm()
+    a, b = pg.tpc.empty(0), pg.tpc.empty(0)
+    pg.tpc.reconstruct(ctx, a, pg.tpc.empty(0))
+    orc.tpc_reconstruct(e, comm)
+    pg.tpc.mul_(ctx, a, b)
+    orc.tpc_mul(e, e, comm)
+    pg.tpc.dividePublic(ctx, a, 3)
+    orc.tpc_divide_public(e.copy(), 3, comm)
+    pg.tpc.dReLU(ctx, a, pg.tpc.empty(0, "u8"))
+    orc.tpc_drelu(e, comm=comm)
+    pg.tpc.ReLU(ctx, a, pg.tpc.empty(0), pg.tpc.empty(0, "u8"))
+    orc.tpc_relu(e, comm=comm)
+    pg.tpc.selectShare(ctx, a, b, pg.tpc.empty(0, "u8"), pg.tpc.empty(0))
+    orc.tpc_select_share(e, e, np.zeros((2, 0), U8), comm)
+    pg.tpc.local_(ctx, pg.OP_ADD, a, 5)
+    pg.tpc.maxpool(ctx, a, pg.tpc.empty(0), pg.tpc.empty(0, "u8"), 4)
+    ctx.sync()
+    check_comm(ctx, comm)
+    assert comm.rounds > 20
