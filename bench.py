@@ -209,10 +209,16 @@ class ClockSampler:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return
+        # the timed region starts once the sampler is up (its first line is
+        # written), so a short region is covered from its start; bounded at 3 s
+        t0 = time.time()
+        while time.time() - t0 < 3 and self.proc.poll() is None and os.path.getsize(self.path) == 0:
+            time.sleep(0.01)
 
     def stop(self):
         if not self.proc:

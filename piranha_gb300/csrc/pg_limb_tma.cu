@@ -450,7 +450,10 @@ __device__ __forceinline__ void fold_hi(int a, const uint32_t (&r)[32], uint64_t
 #pragma unroll
     for (int j = 0; j < 32; j++) acc[j] += (uint64_t)((uint32_t)f2i(r[j]) << (8 * (a - 4))) << 32;
 }
-template <bool HI> __device__ __forceinline__ void drain(uint32_t taddr, uint64_t (&acc)[32]) {
+// Tensor memory is handed back (the arrival on acc_empty) as soon as the last
+// load has landed, before the last fold: the MMA warp of the group waits only
+// for the loads and three folds.
+template <bool HI> __device__ __forceinline__ void drain(uint32_t taddr, uint64_t (&acc)[32], Smem &sm) {
     constexpr int a0 = HI ? 4 : 0;
     uint32_t r0[32], r1[32];
     tc::tmem_ld32(taddr + (uint32_t)(a0 * BN), r0);
@@ -464,6 +467,8 @@ template <bool HI> __device__ __forceinline__ void drain(uint32_t taddr, uint64_
     tc::tmem_ld32(taddr + (uint32_t)((a0 + 3) * BN), r1);
     if (HI) fold_hi(a0 + 2, r0, acc); else fold_lo(a0 + 2, r0, acc);
     tc::tmem_wait_ld();
+    tc::tc_fence_before();
+    tc::mbar_arrive(tc::smem_u32(&sm.acc_empty[HI ? 1 : 0]));
     if (HI) fold_hi(a0 + 3, r1, acc); else fold_lo(a0 + 3, r1, acc);
 }
 
@@ -691,10 +696,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             t_idle = 0;
             tc::tc_fence_after();
-            if (gi == 0) drain<false>(taddr, zs);
-            else drain<true>(taddr, zs);
-            tc::tc_fence_before();
-            tc::mbar_arrive(tc::smem_u32(&sm.acc_empty[gi]));
+            if (gi == 0) drain<false>(taddr, zs, sm);
+            else drain<true>(taddr, zs, sm);
             done_ch[gi]++;
         }
         // output row of this thread's accumulator lane (-1: padding or past the image)
