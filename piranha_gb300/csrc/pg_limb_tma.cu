@@ -451,24 +451,23 @@ __device__ __forceinline__ void fold_hi(int a, const uint32_t (&r)[32], uint64_t
     for (int j = 0; j < 32; j++) acc[j] += (uint64_t)((uint32_t)f2i(r[j]) << (8 * (a - 4))) << 32;
 }
 // Tensor memory is handed back (the arrival on acc_empty) as soon as the last
-// load has landed, before the last fold: the MMA warp of the group waits only
-// for the loads and three folds.
+// two loads have landed, before the last two folds: the MMA warp of the group
+// waits only for the loads and two folds. tcgen05.wait::ld waits for all of a
+// thread's loads, so the two buffers are refilled only after their folds.
 template <bool HI> __device__ __forceinline__ void drain(uint32_t taddr, uint64_t (&acc)[32], Smem &sm) {
     constexpr int a0 = HI ? 4 : 0;
     uint32_t r0[32], r1[32];
     tc::tmem_ld32(taddr + (uint32_t)(a0 * BN), r0);
-    tc::tmem_wait_ld();
     tc::tmem_ld32(taddr + (uint32_t)((a0 + 1) * BN), r1);
-    if (HI) fold_hi(a0, r0, acc); else fold_lo(a0, r0, acc);
     tc::tmem_wait_ld();
+    if (HI) fold_hi(a0, r0, acc); else fold_lo(a0, r0, acc);
     tc::tmem_ld32(taddr + (uint32_t)((a0 + 2) * BN), r0);
     if (HI) fold_hi(a0 + 1, r1, acc); else fold_lo(a0 + 1, r1, acc);
-    tc::tmem_wait_ld();
     tc::tmem_ld32(taddr + (uint32_t)((a0 + 3) * BN), r1);
-    if (HI) fold_hi(a0 + 2, r0, acc); else fold_lo(a0 + 2, r0, acc);
     tc::tmem_wait_ld();
     tc::tc_fence_before();
     tc::mbar_arrive(tc::smem_u32(&sm.acc_empty[HI ? 1 : 0]));
+    if (HI) fold_hi(a0 + 2, r0, acc); else fold_lo(a0 + 2, r0, acc);
     if (HI) fold_hi(a0 + 3, r1, acc); else fold_lo(a0 + 3, r1, acc);
 }
 
