@@ -450,13 +450,15 @@ __device__ __forceinline__ void fold_hi(int a, const uint32_t (&r)[32], uint64_t
 #pragma unroll
     for (int j = 0; j < 32; j++) acc[j] += (uint64_t)((uint32_t)f2i(r[j]) << (8 * (a - 4))) << 32;
 }
-// Tensor memory is handed back (the arrival on acc_empty) as soon as the last
-// two loads have landed, before the last two folds: the MMA warp of the group
-// waits only for the loads and two folds. tcgen05.wait::ld waits for all of a
-// thread's loads, so the two buffers are refilled only after their folds.
-template <bool HI> __device__ __forceinline__ void drain(uint32_t taddr, uint64_t (&acc)[32], Smem &sm) {
+// A drain in two parts: drain_head loads the group's four accumulators
+// through two register buffers and folds the first two; the caller then hands
+// tensor memory back (the arrival on acc_empty) and drain_tail folds the last
+// two from registers, so the MMA warp of the group waits only for the loads
+// and two folds. tcgen05.wait::ld waits for all of a thread's loads, so each
+// buffer is refilled only after its fold.
+template <bool HI> __device__ __forceinline__ void drain_head(uint32_t taddr, uint64_t (&acc)[32], uint32_t (&r0)[32],
+                                                             uint32_t (&r1)[32]) {
     constexpr int a0 = HI ? 4 : 0;
-    uint32_t r0[32], r1[32];
     tc::tmem_ld32(taddr + (uint32_t)(a0 * BN), r0);
     tc::tmem_ld32(taddr + (uint32_t)((a0 + 1) * BN), r1);
     tc::tmem_wait_ld();
@@ -465,8 +467,10 @@ template <bool HI> __device__ __forceinline__ void drain(uint32_t taddr, uint64_
     if (HI) fold_hi(a0 + 1, r1, acc); else fold_lo(a0 + 1, r1, acc);
     tc::tmem_ld32(taddr + (uint32_t)((a0 + 3) * BN), r1);
     tc::tmem_wait_ld();
-    tc::tc_fence_before();
-    tc::mbar_arrive(tc::smem_u32(&sm.acc_empty[HI ? 1 : 0]));
+}
+template <bool HI> __device__ __forceinline__ void drain_tail(uint64_t (&acc)[32], const uint32_t (&r0)[32],
+                                                             const uint32_t (&r1)[32]) {
+    constexpr int a0 = HI ? 4 : 0;
     if (HI) fold_hi(a0 + 2, r0, acc); else fold_lo(a0 + 2, r0, acc);
     if (HI) fold_hi(a0 + 3, r1, acc); else fold_lo(a0 + 3, r1, acc);
 }
@@ -695,8 +699,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             t_idle = 0;
             tc::tc_fence_after();
-            if (gi == 0) drain<false>(taddr, zs, sm);
-            else drain<true>(taddr, zs, sm);
+            uint32_t r0[32], r1[32];
+            if (gi == 0) drain_head<false>(taddr, zs, r0, r1);
+            else drain_head<true>(taddr, zs, r0, r1);
+            tc::tc_fence_before();
+            tc::mbar_arrive(tc::smem_u32(&sm.acc_empty[gi]));
+            if (gi == 0) drain_tail<false>(zs, r0, r1);
+            else drain_tail<true>(zs, r0, r1);
             done_ch[gi]++;
         }
         // output row of this thread's accumulator lane (-1: padding or past the image)
