@@ -17,6 +17,13 @@
  * DeviceData::transmit/receive (src/gpu/DeviceData.h:87-118) and
  * Profiler::add_comm_round (src/util/Profiler.cpp:95-99).
  *
+ * A length n = 0 is valid for the elementwise protocol steps (reconstruct,
+ * reshare, *=, &=, dividePublic, dReLU, ReLU, selectShare, maxpool, the local
+ * operators): nothing is launched, the share pointers may be null (an empty
+ * CUDA tensor has none), and the step's rounds are counted with empty
+ * messages, as the reference counts the rounds of its empty vectors.
+ * maxpool of no rows counts nothing (the reference divides by the row count).
+ *
  * Citations point at the Piranha (ucbrise/piranha) source each entry point
  * replaces; paths are relative to that project.
  */
