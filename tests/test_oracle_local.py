@@ -77,3 +77,19 @@ def test_tpc_fpc_local_public_add_reconstructs():
         for p, s in ((1, 2), (2, 1), (3, 0)):
             assert np.array_equal(g[p, s], x + r)
         assert not g[0].any()
+
+
+def test_empty_inputs_count_the_protocol_rounds():
+    """Zero-length inputs: empty outputs, no bytes, and the rounds of the
+    reference's call sequence on empty vectors (reconstruct 1, dReLU 1 + 12,
+    ReLU 15); maxpool of no rows returns without dividing by the row count."""
+    U64 = np.uint64
+    e = np.zeros((3, 2, 0), dtype=U64)
+    for fn, rounds in ((lambda c: orc.reconstruct(e, c), 1), (lambda c: orc.mul(e, e, c), 1),
+                       (lambda c: orc.drelu(e, comm=c), 13), (lambda c: orc.relu(e, comm=c), 15)):
+        c = orc.Comm()
+        fn(c)
+        assert c.rounds == rounds and c.tx == [0, 0, 0] and c.rx == [0, 0, 0]
+    c = orc.Comm()
+    out, d = orc.maxpool(e, 4, comm=c)
+    assert out.shape[-1] == 0 and d.shape[-1] == 0 and c.tx == [0, 0, 0]
