@@ -55,8 +55,9 @@ SEED = 2024
 STREAM_BUCKETS = (1, 2, 4, 8, 12, 16, 24, 32, 40, 48, 56, 64)  # batch sizes of the stream's captured networks
 LIMB_FLOPS_PER_RING_MAC = 72  # 36 8-bit limb pairs x 2 flops: exact u64 MAC on fp16 tensor cores
 # DRAM bytes read + written by the 13 limb_tma_kernel launches of one VGG16
-# batch-128 forward, from the ncu capture summarised in
-# profiles/limb_tma_kernel_vgg16_b128_dram.md (the command is given there)
+# batch-128 forward, from one ncu capture of dram__bytes_read.sum +
+# dram__bytes_write.sum over those launches (bench.py --steps 1 --warmup 1
+# under ncu with the plain run's tuning cache)
 VGG16_B128_LIMB_TRAFFIC = 4_803_831_040
 
 WORKLOADS = {
@@ -102,7 +103,9 @@ def parse():
     ap.add_argument("--workload", default="vgg16", choices=sorted(WORKLOADS))
     ap.add_argument("--form", default="auto", choices=["auto", "u64", "tc"])
     ap.add_argument("--batch", type=int, default=BATCH)
-    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU sample budget")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU sample budget of the cpu_baseline key")
+    ap.add_argument("--ref-seconds", type=float, default=120.0,
+                    help="--impl reference: bound on the timed CPU steps' total time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-u64-form comparison run")
     ap.add_argument("--sweep", action="store_true", help="gemm: also time M = N = K in 512..8192 in both forms")
@@ -250,7 +253,7 @@ def cpu_baseline_stream(wl, budget_s):
     """The oracle's time per image of each model (SecureML on its first
     request, VGG16 on one image of its first), applied to the stream's mix."""
     import oracle as orc
-    from tests import netref
+    from oracle import netref
 
     orc.lib()
     models, params, reqs = wl
@@ -302,7 +305,7 @@ def cpu_baseline_gemm(wl, budget_s):
 def cpu_baseline(name, wl, batch_full, budget_s):
     """Piranha's arithmetic restated on the CPU (the oracle), timed on a sample of the batch."""
     import oracle as orc
-    from tests import netref
+    from oracle import netref
 
     orc.lib()
     if name == "stream":
@@ -347,6 +350,130 @@ def cpu_baseline(name, wl, batch_full, budget_s):
     return {"value": imgs / secs, "unit": "img/s", "cores": cores, "kind": "port",
             "sample": f"runs of {' and '.join(map(str, runs))} images from the {batch_full}-image batch "
                       f"({secs:.1f} s), same weights and shares"}
+
+
+# ------------------------------------------------------- reference arm
+
+def reference_arm(args, name, wl):
+    """--impl reference: Piranha's arithmetic restated on the CPU (the oracle,
+    OpenMP over all host threads), timed step by step on the same workload.
+
+    A step processes `per_step` units of the workload (images; share-GEMM rows
+    for the gemm workload; the next request's images for the stream), taken in
+    order and cycling through the batch, so that the timed steps cover the
+    whole batch once when the time bound (--ref-seconds) allows it. Warm-up
+    steps process the smallest unit and give the time estimate that sizes
+    per_step. Every figure printed is measured, none extrapolated."""
+    import oracle as orc
+    from oracle import netref
+
+    orc.lib()
+    w = WORKLOADS[name]
+    kind = w["kind"]
+    fp = w["fp"]
+    if kind == "gemm":
+        M, N, K = wl["M"], wl["N"], wl["K"]
+        A4 = wl["A"].reshape(3, 2, M, K)
+        total, unit_work, smallest = M, 6 * N * K, min(M, os.cpu_count() or 1)
+
+        def run(k0, n):
+            rows = (k0 + np.arange(n)) % M
+            a = np.ascontiguousarray(A4[:, :, rows, :].reshape(3, 2, -1))
+            orc.matmul(a, wl["B"], n, N, K, 1, 1, 1, fp)
+            return n
+    elif kind == "stream":
+        models, params, reqs = wl
+        total, unit_work, smallest = sum(b for _, b, _ in reqs), 1, 1
+        state = {"req": 0}
+
+        def run(k0, n):
+            m, b, x = reqs[state["req"] % len(reqs)]
+            state["req"] += 1
+            nimg = min(b, n)
+            n_in = nets.input_size(models[m])
+            netref.forward(models[m], params[m], np.ascontiguousarray(x[..., : nimg * n_in]), nimg, fp)
+            return nimg
+    else:
+        layers, params, x_full = wl["layers"], wl["params"], wl["x"]
+        batch = args.batch
+        n_in = nets.input_size(layers)
+        total, unit_work = batch, 1
+        smallest = 2 if kind == "train3" else 1  # a training step divides by its batch size
+        xv = x_full.reshape(x_full.shape[:-1] + (batch, n_in))
+
+        def run(k0, n):
+            idx = (k0 + np.arange(n)) % batch
+            x = np.ascontiguousarray(xv[..., idx, :].reshape(x_full.shape[:-1] + (-1,)))
+            if kind == "infer3":
+                netref.forward(layers, params, x, n, fp)
+            elif kind == "train3":
+                lab = np.ascontiguousarray(wl["labels"].reshape(3, 2, batch, 10)[:, :, idx, :].reshape(3, 2, -1))
+                netref.train_step(layers, params, x, lab, n, fp, w["log_lr"])
+            else:
+                mm = orc.tpc_matmul if w["parties"] == 2 else orc.fpc_matmul
+                relu = orc.tpc_relu if w["parties"] == 2 else orc.fpc_relu
+                cur = x
+                for L, prm in zip(layers, params):
+                    if L[0] == "fc":
+                        cur = mm(cur, prm[0], n, L[2], L[1], 1, 1, 1, fp)
+                        cur = (cur.reshape(cur.shape[:-1] + (n, L[2])) + prm[1][..., None, :]).reshape(
+                            cur.shape).astype(cur.dtype)
+                    else:
+                        cur, _ = relu(cur)
+            return n
+
+    est = None
+    for i in range(max(1, args.warmup)):
+        t0 = time.perf_counter()
+        run(0, smallest)
+        if i == 0:
+            est = (time.perf_counter() - t0) / smallest
+    if name == "stream":
+        state["req"] = 0
+    steps = args.steps
+    by_time = int(args.ref_seconds / max(steps * est, 1e-9))
+    per_step = max(smallest, min(-(-total // steps), by_time))
+    secs, units, done = [], 0, 0
+    for k in range(steps):
+        t0 = time.perf_counter()
+        got = run(done, per_step)
+        secs.append(time.perf_counter() - t0)
+        done += got
+        units += got * unit_work
+    tot = sum(secs)
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    what = {"gemm": "share-GEMM rows", "stream": "images of the next request"}.get(kind, "images")
+    covered = "the whole batch once" if done >= total else f"{done} of {total}"
+    return {"value": units / tot, "ms_per_step": 1e3 * tot / steps, "units": units,
+            "cpu_baseline": {"value": units / tot, "unit": w.get("unit", "img/s"), "cores": cores, "kind": "port",
+                             "sample": f"{steps} timed steps of {per_step} {what} each ({covered}, {tot:.1f} s), "
+                                       f"after {max(1, args.warmup)} warm-up steps of {smallest}; same inputs "
+                                       "and weights as the GPU arm"}}
+
+
+def line_config(args, w, world):
+    """The `config` of both arms' JSON lines (the same dict in both)."""
+    cfg = {"workload": w["desc"], "global_batch": args.batch * world, "parallelism": "replicas",
+           "l2": "GPU arm: 256 MiB write between timed steps; CPU arm: none",
+           "graph": "GPU arm: one CUDA graph per step"}
+    if w["kind"] == "gemm":
+        cfg.update({"global_batch": None, "M": w["M"], "N": w["N"], "K": w["K"], "truncation": w["fp"],
+                    "data_size": f"operands {6 * w['M'] * w['K'] * 8 / 1e6:.0f} MB per share tensor, larger than L2"})
+    return cfg
+
+
+def tensor_rates(pg, dev):
+    """Sustained rates of the tensor-core instruction forms on this GPU (pg_tensor_rate)."""
+    ctx = pg.Context(dev.index)
+    out = {}
+    for key, form, iters in (("tcgen05_f16", pg.RATE_TC_F16, 100000), ("tcgen05_f8_e4m3", pg.RATE_TC_F8, 100000),
+                             ("mma_sync_s8", pg.RATE_MMA_S8, 20000), ("mma_sync_f16", pg.RATE_MMA_F16, 20000)):
+        r = ctx.tensor_rate(form, iters)
+        out[key] = round(r["tops"], 1)
+    ctx.close()
+    out["unit"] = "TOP/s (2 per multiply-add), one launch over every SM"
+    out["note"] = "tcgen05.mma kind::i8 is rejected by ptxas for sm_103a: mma.sync s8 is GB300's only INT8 tensor form"
+    return out
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -400,6 +527,8 @@ def run_ours(args, rank, world, local_rank):
             result["compare_u64"] = {"value": u["value"], "ms_per_step": u["ms_per_step"],
                                      "gemm_tflops_equiv": u["roofline"]["achieved"],
                                      "limb_over_u64": result["value"] / u["value"]}
+        if result and args.workload == "vgg16":
+            result["tensor_rates"] = tensor_rates(pg, dev)
     return result, wl
 
 
@@ -720,8 +849,6 @@ def bench_gemm(args, pg, torch, stream, dev, wl, world):
                      "peak_source": "bf16_tflops of measured" if peak else None},
         "comm_per_party_per_step": {"tx_bytes": int((r["comm1"]["tx"][0] - r["comm0"]["tx"][0]) // args.steps),
                                     "rounds": int((r["comm1"]["rounds"] - r["comm0"]["rounds"]) // args.steps)},
-        "config_extra": {"global_batch": None, "M": M, "N": N, "K": K, "truncation": 26,
-                         "data_size": "operands 805 MB per share tensor, larger than L2"},
     }
     if form == pg.FORM_LIMB_TC and not args.no_compare:
         u = _gemm_form(args, pg, torch, stream, dev, pg.FORM_U64, A, B, M, N, K, world, max(2, args.steps // 4), 1)
@@ -982,16 +1109,14 @@ def main():
             return
         wl = (make_stream() if w["kind"] == "stream" else make_gemm() if w["kind"] == "gemm"
               else make_workload(args.workload, args.batch))
-        cb = cpu_baseline(args.workload, wl, args.batch, args.cpu_seconds)
+        r = reference_arm(args, args.workload, wl)
         unit = w.get("unit", "img/s")
-        line = {"metric": w["metric"], "value": cb["value"], "unit": unit, "impl": "reference", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": 1e3 * work_per_step(args.workload, args.batch) / cb["value"],
+        line = {"metric": w["metric"], "value": r["value"], "unit": unit, "impl": "reference", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
-                "data": "synthetic", "config": {"workload": w["desc"], "global_batch": args.batch,
-                                                "parallelism": "replicas"},
-                "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": unit, "h2d_bytes_per_step": 0,
-                                            "d2h_bytes_per_step": 0},
+                "data": "synthetic", "config": line_config(args, w, 1),
+                "cpu_baseline": r["cpu_baseline"], "e2e": {"value": r["value"], "unit": unit,
+                                                           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                 "note": "Piranha's GPU build needs its un-vendored CUTLASS fork; this arm times the reference's "
                         "arithmetic restated on the host CPU"}
         print(json.dumps(line))
@@ -1012,14 +1137,11 @@ def main():
         "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": dtype, "data": "synthetic",
-        "config": {"workload": w["desc"], "global_batch": args.batch * world, "parallelism": "replicas",
-                   "form": res["form"], "l2": "256 MiB write between timed steps",
-                   "graph": "one CUDA graph per step"},
+        "config": line_config(args, w, world), "form": res["form"],
         "e2e": res["e2e"], "gpu_launches": res["gpu_launches"], "clocks": res["clocks"],
         "roofline": res["roofline"], "cpu_baseline": cb,
         "comm_per_party_per_step": res["comm_per_party_per_step"],
     }
-    line["config"].update(res.get("config_extra", {}))
     if "layer_ms" in res:
         line["layer_ms"] = res["layer_ms"]
     for k in ("latency_ms", "requests", "images", "networks", "sweep"):
@@ -1027,6 +1149,8 @@ def main():
             line[k] = res[k]
     if "compare_u64" in res:
         line["compare_u64_form"] = res["compare_u64"]
+    if "tensor_rates" in res:
+        line["tensor_rates"] = res["tensor_rates"]
     print(json.dumps(line))
 
 

@@ -75,6 +75,10 @@ int pg_ctx_create(pg_ctx **out, int device);
 int pg_ctx_destroy(pg_ctx *ctx);
 int pg_ctx_set_stream(pg_ctx *ctx, void *cuda_stream);
 void *pg_ctx_get_stream(pg_ctx *ctx);
+/* The form of the share-GEMMs and convolutions. A new context uses
+ * PG_FORM_LIMB_TC, in which (with autotuning on) the first call of each
+ * problem shape times both forms and keeps the faster one for that shape;
+ * PG_FORM_U64 sends every call to the CUDA-core kernels. */
 int pg_ctx_set_form(pg_ctx *ctx, int form);
 int pg_ctx_get_form(pg_ctx *ctx);
 /* split-K of the limb-form GEMMs picked by timing the candidates on first use
@@ -127,6 +131,19 @@ int pg_graph_destroy(pg_graph *graph);
 /* diagnostic: one 128x64x16 tcgen05 MMA of fp16 operands (A 128x16 and B
  * 64x16 row-major halves), D = A * B^T as 128x64 fp32 row-major */
 int pg_tc_selftest(pg_ctx *ctx, const uint16_t *A, const uint16_t *B, float *D);
+/* Measurement, no counterpart in the reference (whose GEMMs are CUDA-core
+ * SIMT): the sustained rate of one tensor-core instruction form on ctx's
+ * device, from one launch over every SM after a shorter warm-up launch.
+ * out[0] = tera-operations per second (2 per multiply-add), out[1] = SM
+ * cycles per instruction per issuing CTA (tcgen05) or warp (mma.sync),
+ * out[2] = the timed launch in ms. Synchronizes. tcgen05.mma kind::i8 does
+ * not exist for sm_103a (ptxas rejects it), so the only INT8 tensor form on a
+ * GB300 is the legacy mma.sync one. */
+#define PG_RATE_TC_F16 0  /* tcgen05.mma kind::f16, M=128 N=256 K=16, fp32 in tensor memory */
+#define PG_RATE_TC_F8 1   /* tcgen05.mma kind::f8f6f4 e4m3, M=128 N=256 K=32, fp32 */
+#define PG_RATE_MMA_S8 2  /* mma.sync m16n8k32 s8 x s8 -> s32 */
+#define PG_RATE_MMA_F16 3 /* mma.sync m16n8k16 f16 x f16 -> f32 */
+int pg_tensor_rate(pg_ctx *ctx, int form, int iters, double out[3]);
 
 /* -------------------------------------------- single-array ring kernels
  * gpu::gemm (src/gpu/gemm.cuh:102-112): C = A*B mod 2^w, A MxK, B KxN, C MxN;

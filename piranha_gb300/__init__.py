@@ -27,6 +27,7 @@ from . import build as _build
 
 PG_OK = 0
 FORM_U64, FORM_LIMB_TC = 0, 1
+RATE_TC_F16, RATE_TC_F8, RATE_MMA_S8, RATE_MMA_F16 = 0, 1, 2, 3
 FPROP, DGRAD, WGRAD = 0, 1, 2
 LAYER_FC, LAYER_CNN, LAYER_RELU, LAYER_MAXPOOL, LAYER_AVGPOOL = 1, 2, 3, 4, 5
 OP_ADD, OP_SUB, OP_MUL, OP_XOR, OP_AND, OP_SHR, OP_SHL = range(7)
@@ -114,6 +115,7 @@ def _declare(lib):
         "pg_net_layer_params": [vp, i, _P6, _P6, ctypes.POINTER(sz), ctypes.POINTER(sz)],
         "pg_device_errors": [vp, ctypes.POINTER(i)],
         "pg_tc_selftest": [vp, vp, vp, vp],
+        "pg_tensor_rate": [vp, i, i, vp],
         "pg_net_layer_times": [vp, vp],
         "pg_tpc_matmul_u64": [vp, _P2, _P2, _P2, i, i, i, i, i, i, i],
         "pg_tpc_matmul_u32": [vp, _P2, _P2, _P2, i, i, i, i, i, i, i],
@@ -251,7 +253,7 @@ class _Capture:
 class Context:
     """pg_ctx: stream, implementation form and per-party comm counters."""
 
-    def __init__(self, device: int = 0, stream=None, form: int = FORM_U64):
+    def __init__(self, device: int = 0, stream=None, form: int = FORM_LIMB_TC):
         import torch
 
         self.torch = torch
@@ -323,6 +325,13 @@ class Context:
         CUDA graph; ``g.launch()`` replays it. Run the calls eagerly once
         first so that the context's scratch is sized."""
         return _Capture(self)
+
+    def tensor_rate(self, form: int, iters: int = 200000) -> dict:
+        """Sustained rate of one tensor-core instruction form (RATE_TC_F16,
+        RATE_TC_F8, RATE_MMA_S8, RATE_MMA_F16) on this context's device."""
+        out = (ctypes.c_double * 3)()
+        self._check(lib().pg_tensor_rate(self._h, form, iters, out))
+        return {"tops": out[0], "cycles_per_inst": out[1], "ms": out[2]}
 
     def comm(self, parties=3):
         buf = (ctypes.c_uint64 * 9)()

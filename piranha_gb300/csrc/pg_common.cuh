@@ -24,7 +24,7 @@ namespace pg {
 struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
-    int form = PG_FORM_U64;
+    int form = PG_FORM_LIMB_TC;
     std::string err;
     uint64_t comm[9] = {0};
     std::atomic<uint64_t> launches{0};

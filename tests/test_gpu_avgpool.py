@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import oracle as orc
-from tests import netref
+from oracle import netref
 from tests.test_gpu_network import run_net
 from tests.test_gpu_train import check_against_oracle, make_net, one_hot_labels, oracle_step
 

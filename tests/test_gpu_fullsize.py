@@ -1,24 +1,34 @@
-"""Parity at the benchmark's full sizes, through properties that do not need
-the oracle to finish the whole problem:
+"""Parity at the benchmark configurations' full sizes.
 
-* VGG16 (maxpool) 3PC inference at batch 128: the limb tensor-core form and
-  the plain u64 form, two independent implementations of the same ring
-  arithmetic, agree on every share of every layer's output; and the first
-  two images' logits equal the oracle's run of the same two images (every
-  layer works image by image);
-* the 4096^3 share-GEMM with truncation: both forms agree on every share,
-  and sampled rows equal the oracle's product of those rows.
+* VGG16 (maxpool) 3PC inference at batch 128 and one LeNet training step at
+  batch 128: every layer's six output shares (and, for training, the softmax
+  gradient, every gradient passed between layers and every updated weight
+  and bias share) hash to the SHA-256 digests of the oracle's run of the same
+  inputs, stored in tests/golden/fullsize.json by tests/golden/make_fullsize.py;
+  the message counters are compared too. Both forms, with the tuner on as the
+  benchmark runs them.
+* The request stream's bucket path: a request of b images served on the
+  captured network of a larger batch bucket, whose other rows hold an earlier
+  request's data, gives the oracle's result for its b images.
+* Share-GEMMs with truncation at 512^3, 4096^3, 8192^3 and non-cubic shapes:
+  both forms agree on every share, and sampled rows equal the oracle's
+  product of those rows.
 """
+import json
+import os
+
 import numpy as np
 import pytest
 
 import oracle as orc
-from tests import netref
-from tests.test_gpu_network import run_net
+from oracle import netref
+from tests.golden import seeded
+from tests.test_gpu_network import _wrap_device, gather, run_net
 
 pytestmark = pytest.mark.gpu
 
 U64 = np.uint64
+HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 @pytest.fixture(scope="module")
@@ -32,45 +42,127 @@ def pg():
     return pg
 
 
-def test_vgg16_batch128_forms_agree(pg):
-    from piranha_gb300 import encode as enc
-    from piranha_gb300 import nets
-
-    layers = nets.vgg16()
-    params = nets.kaiming_uniform(layers, 2024, 26)
-    batch = 128
-    rng = np.random.default_rng(7)
-    x = enc.share_random(enc.encode(rng.uniform(0, 1, batch * 3072)), seed=8)
-    # with the tuner on, as the benchmark runs it (split-K and per-layer forms by timing)
-    got_tc, outs_tc, comm_tc = run_net(pg, layers, params, x, batch, capture=True, form=pg.FORM_LIMB_TC,
-                                       autotune=True)
-    got_u64, outs_u64, comm_u64 = run_net(pg, layers, params, x, batch, capture=True, form=pg.FORM_U64)
-    for i, (a, b) in enumerate(zip(outs_tc, outs_u64)):
-        assert np.array_equal(a, b), f"layer {i} {layers[i]}"
-    assert np.array_equal(got_tc, got_u64)
-    assert comm_tc == comm_u64
-    # the first two images through the oracle
-    n_in = 3072
-    want = netref.forward(layers, params, np.ascontiguousarray(x[..., : 2 * n_in]), 2)
-    assert np.array_equal(got_tc[..., : 2 * 10], want)
+@pytest.fixture(scope="module")
+def fixtures():
+    return json.load(open(os.path.join(HERE, "golden", "fullsize.json")))
 
 
-def test_gemm_4096_forms_agree(pg):
-    M = N = K = 4096
-    rng = np.random.default_rng(11)
-    A = rng.integers(0, 2**64 - 1, size=(3, 2, M * K), dtype=U64, endpoint=True)
-    B = rng.integers(0, 2**64 - 1, size=(3, 2, K * N), dtype=U64, endpoint=True)
+def _form(pg, name):
+    return pg.FORM_LIMB_TC if name == "tc" else pg.FORM_U64
+
+
+@pytest.mark.parametrize("form", ["tc", "u64"])
+def test_vgg16_batch128_equals_oracle_digests(pg, fixtures, form):
+    fx = fixtures["vgg16_b128"]
+    layers = netref.vgg16_layers(maxpool=True)
+    params = seeded.kaiming_uniform(layers, fx["seeds"]["weights"])
+    batch = fx["batch"]
+    x = seeded.images(fx["seeds"]["images"], batch * 3072)
+    assert seeded.digest(x) == fx["input"], "inputs differ from the fixture's"
+    assert [None if p is None else seeded.digest(p[0]) for p in params] == fx["params"]
+    _, outs, comm = run_net(pg, layers, params, x, batch, capture=True, form=_form(pg, form), autotune=True)
+    for i, o in enumerate(outs):
+        assert seeded.digest(o) == fx["layers"][i], f"layer {i} {layers[i]}"
+    assert {"tx": comm["tx"], "rx": comm["rx"], "rounds": comm["rounds"]} == fx["comm"]
+
+
+@pytest.mark.parametrize("form", ["tc", "u64"])
+def test_lenet_training_batch128_equals_oracle_digests(pg, fixtures, form):
+    from tests.test_gpu_train import make_net
+
+    fx = fixtures["lenet_train_b128"]
+    layers = netref.lenet_layers()
+    params = seeded.kaiming_uniform(layers, fx["seeds"]["weights"])
+    batch = fx["batch"]
+    x = seeded.images(fx["seeds"]["images"], batch * 784)
+    labels = seeded.labels(fx["seeds"]["labels"], batch)
+    assert seeded.digest(x) == fx["input"] and seeded.digest(labels) == fx["labels"]
+    ctx = pg.Context(0, form=_form(pg, form))
+    ctx.set_autotune(True)
+    net = make_net(pg, ctx, layers, params, batch)
+    ctx.reset_comm()
+    net.train_step(pg.to_device(x), pg.to_device(labels), fx["log_lr"])
+    ctx.sync()
+    ctx.check_device_errors()
+    for i in range(len(layers)):
+        optrs, n = net.layer_output_ptrs(i)
+        assert seeded.digest(gather(pg, optrs, n)) == fx["outputs"][i], f"output of layer {i} {layers[i]}"
+    dptrs, n = net.layer_delta_ptrs(-1)
+    assert seeded.digest(gather(pg, dptrs, n)) == fx["softmax"], "softmax gradient"
+    for i in range(len(layers)):
+        dptrs, n = net.layer_delta_ptrs(i)
+        assert seeded.digest(gather(pg, dptrs, n)) == fx["deltas"][i], f"gradient out of layer {i} {layers[i]}"
+        if fx["params"][i] is not None:
+            w, wn, b, bn = net.layer_param_ptrs(i)
+            assert seeded.digest(gather(pg, w, wn)) == fx["params"][i][0], f"weights of layer {i}"
+            if fx["params"][i][1] is not None:
+                assert seeded.digest(gather(pg, b, bn)) == fx["params"][i][1], f"bias of layer {i}"
+    comm = ctx.comm()
+    assert {"tx": comm["tx"], "rx": comm["rx"], "rounds": comm["rounds"]} == fx["comm"]
+    net.close()
+    ctx.close()
+
+
+@pytest.mark.parametrize("model,requests", [
+    ("secureml", [(64, 64), (37, 40), (1, 1), (5, 8)]),
+    ("vgg16", [(3, 4), (1, 2)]),
+])
+def test_stream_bucket_path_equals_oracle(pg, model, requests):
+    """Each (b, bucket): the request's b images go into the first rows of the
+    bucket network's input, whose remaining rows hold an earlier request's
+    images, as the benchmark's request stream serves them."""
+    import torch
+
+    layers = netref.vgg16_layers(maxpool=True) if model == "vgg16" else netref.secureml_layers()
+    params = seeded.kaiming_uniform(layers, 77)
+    n_img = 3072 if model == "vgg16" else 784
+    ctx = pg.Context(0, form=pg.FORM_LIMB_TC)
+    ctx.set_autotune(True)
+    for r, (b, bucket) in enumerate(requests):
+        net = pg.Network(ctx, layers, bucket)
+        for i, prm in enumerate(params):
+            if prm is not None:
+                net.set_params(i, pg.to_device(prm[0]), pg.to_device(prm[1]) if prm[1] is not None else None)
+        net.capture()
+        inb = _wrap_device(net.input_buffers()[0], 6 * net.in_n).view(6, net.in_n)
+        earlier = seeded.images(500 + r, bucket * n_img)
+        inb.copy_(pg.to_device(earlier).reshape(6, -1))
+        net.forward_resident()
+        x = seeded.images(600 + r, b * n_img)
+        inb[:, : b * n_img].copy_(pg.to_device(x).reshape(6, -1))
+        net.forward_resident()
+        ctx.sync()
+        optrs, on = net.layer_output_ptrs(len(layers) - 1)
+        got = gather(pg, optrs, on)[..., : b * 10]
+        want = netref.forward(layers, params, x, b)
+        assert np.array_equal(got, want), f"request {r}: b={b} on the {bucket}-image network"
+        net.close()
+    ctx.check_device_errors()
+    ctx.close()
+    torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("M,N,K", [(512, 512, 512), (4096, 4096, 4096), (8192, 8192, 8192), (1024, 8192, 2048),
+                                   (8192, 512, 4096), (3000, 1000, 777)])
+def test_gemm_forms_agree_and_sampled_rows_equal_oracle(pg, M, N, K):
+    import torch
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(M * 31 + N * 7 + K)
+    A = torch.randint(-2**63, 2**63 - 1, (3, 2, M * K), dtype=torch.int64, device="cuda", generator=g)
+    B = torch.randint(-2**63, 2**63 - 1, (3, 2, K * N), dtype=torch.int64, device="cuda", generator=g)
     out = {}
     for form in (pg.FORM_LIMB_TC, pg.FORM_U64):
         ctx = pg.Context(0, form=form)
+        ctx.set_autotune(False)  # the form under test for every shape
         C = pg.empty_shares(M * N)
-        pg.matmul(ctx, pg.to_device(A), pg.to_device(B), C, M, N, K, 1, 1, 1, 26)
+        pg.matmul(ctx, A, B, C, M, N, K, 1, 1, 1, 26)
         ctx.check_device_errors()
-        out[form] = pg.to_host(C)
+        out[form] = C
         ctx.close()
-    assert np.array_equal(out[pg.FORM_LIMB_TC], out[pg.FORM_U64])
-    rows = [0, 1, 2047, 4095]
-    a_rows = np.ascontiguousarray(A.reshape(3, 2, M, K)[:, :, rows, :].reshape(3, 2, -1))
-    want = orc.matmul(a_rows, B, len(rows), N, K, 1, 1, 1, 26).reshape(3, 2, len(rows), N)
-    got = out[pg.FORM_LIMB_TC].reshape(3, 2, M, N)[:, :, rows, :]
+    assert torch.equal(out[pg.FORM_LIMB_TC], out[pg.FORM_U64])
+    rows = sorted({0, 1, M // 2, M - 1})
+    a_rows = pg.to_host(A.view(3, 2, M, K)[:, :, rows, :].reshape(3, 2, -1).contiguous())
+    want = orc.matmul(a_rows, pg.to_host(B), len(rows), N, K, 1, 1, 1, 26).reshape(3, 2, len(rows), N)
+    got = pg.to_host(out[pg.FORM_LIMB_TC].view(3, 2, M, N)[:, :, rows, :].contiguous())
     assert np.array_equal(got, want)

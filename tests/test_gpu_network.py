@@ -3,7 +3,7 @@ import numpy as np
 import pytest
 
 import oracle as orc
-from tests import netref
+from oracle import netref
 
 pytestmark = pytest.mark.gpu
 

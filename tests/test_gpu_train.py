@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import oracle as orc
-from tests import netref
+from oracle import netref
 from tests.test_gpu_network import _wrap_device, gather
 
 pytestmark = pytest.mark.gpu

@@ -6,7 +6,7 @@ import pytest
 import oracle as orc
 from piranha_gb300 import encode as enc
 from piranha_gb300 import nets
-from tests import netref
+from oracle import netref
 
 
 @pytest.mark.parametrize("ring,dt", [("u64", np.uint64), ("u32", np.uint32)])

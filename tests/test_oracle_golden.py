@@ -603,7 +603,7 @@ def test_secureml_training_step(golden):
     revealed softmax gradient (NeuralNetwork.cu:207-267), every layer's
     backward; each layer's incoming gradient and the updated weights and
     biases match the fixtures, whose update used learning rate 2^-9."""
-    from tests import netref
+    from oracle import netref
 
     L = golden[1]
     layers = netref.secureml_layers()
