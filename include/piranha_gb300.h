@@ -62,6 +62,8 @@ extern "C" {
 #define PG_OP_AND 4
 #define PG_OP_SHR 5 /* arithmetic */
 #define PG_OP_SHL 6
+#define PG_OP_DIV 7 /* DeviceData operator/= only (through double, functors.cuh:33-45,94-105) */
+#define PG_OP_SET 8 /* DeviceData fill only */
 #define PG_RHS_SCALAR 0 /* one public value */
 #define PG_RHS_PUBLIC 1 /* a public device vector of n (DeviceData) */
 #define PG_RHS_SHARES 2 /* another share tensor (six buffers) */
@@ -214,6 +216,13 @@ int pg_rss_reshare_u64(pg_ctx *ctx, const uint64_t *const c[3], size_t n, uint64
  * shift amounts of 64 or more give all sign bits (>>) or 0 (<<). Other
  * combinations return PG_ERR_UNSUPPORTED (RSS * RSS and & are pg_rss_mul_u64 /
  * pg_rss_and_u64). */
+/* DeviceData<uint64_t>'s own elementwise operators on one device array
+ * (src/gpu/DeviceData.h:131-277, src/gpu/functors.cuh:1-117): a op= rhs for
+ * op in ADD SUB MUL DIV XOR AND SHR SHL with rhs a scalar (PG_RHS_SCALAR) or
+ * a device vector of n (PG_RHS_PUBLIC), and fill (PG_OP_SET, scalar). DIV is
+ * the reference's division through double; SHR is arithmetic. */
+int pg_device_op_u64(pg_ctx *ctx, int op, uint64_t *a, size_t n, int rhs_kind, uint64_t scalar,
+                     const uint64_t *rhs);
 int pg_rss_local_u64(pg_ctx *ctx, int op, uint64_t *const a[6], size_t n, int rhs_kind, uint64_t scalar,
                      const uint64_t *pub, const uint64_t *const shares[6]);
 /* the same local operators of TPCBase (TPC.inl:146-240; public values at
@@ -386,17 +395,22 @@ int pg_fpc_maxpool_u64_u8(pg_ctx *ctx, const uint64_t *const in[12], size_t n, i
  * out-of-memory halfway through a request. pg_rss_matmul_u64 grows the
  * context's scratch with cudaMalloc/cudaFree; this call allocates nothing and
  * takes its scratch from one fixed device array of PG_NOALLOC_SCRATCH_BYTES,
- * which the CUDA runtime reserves when it loads the library module that holds
- * it.
+ * which the CUDA runtime reserves on a device when it loads the library module
+ * that holds it: at the first call on that device under the default lazy
+ * module loading, or for every device the process uses, called or not, under
+ * CUDA_MODULE_LOADING=EAGER. It stays reserved until the process exits.
  *  - The first call on a device does set-up (finds the array's address, sets
  *    the kernel's shared-memory limit and looks up the tensor-map encoder)
  *    and needs the context's device current. Make it before any stream
- *    capture on that device.
+ *    capture on that device. Later calls look the address up again (no
+ *    allocation) and repeat the set-up if a device reset moved the array.
  *  - The scratch need is 96 * K16 * M32 bytes for the digit image of a plus
  *    96 * K16 * N64 bytes for the packed weights (K16, M32, N64 = K, M, N
- *    rounded up to 16, 32, 64), plus split-K partial sums when they fit too;
- *    K = M = N = 1024 fits. A problem that does not fit returns PG_ERR_SIZE;
- *    pg_last_error gives the need and the limit.
+ *    rounded up to 16, 32, 64); K = M = N = 1024 fits. A problem that does not
+ *    fit returns PG_ERR_SIZE; pg_last_error gives the need and the limit.
+ *    Split-K partial sums (8 * split * M * N bytes, rounded up to 256) are used
+ *    only when they fit beside those; otherwise the call runs unsplit, which
+ *    is slow for few output tiles and a long K.
  *  - All calls on a device, from every context and thread, share the one
  *    array. Calls that can run at the same time on the device (streams with
  *    no ordering between them) corrupt each other's results: order them on

@@ -30,7 +30,7 @@ FORM_U64, FORM_LIMB_TC = 0, 1
 RATE_TC_F16, RATE_TC_F8, RATE_MMA_S8, RATE_MMA_F16 = 0, 1, 2, 3
 FPROP, DGRAD, WGRAD = 0, 1, 2
 LAYER_FC, LAYER_CNN, LAYER_RELU, LAYER_MAXPOOL, LAYER_AVGPOOL = 1, 2, 3, 4, 5
-OP_ADD, OP_SUB, OP_MUL, OP_XOR, OP_AND, OP_SHR, OP_SHL = range(7)
+OP_ADD, OP_SUB, OP_MUL, OP_XOR, OP_AND, OP_SHR, OP_SHL, OP_DIV, OP_SET = range(9)
 RHS_SCALAR, RHS_PUBLIC, RHS_SHARES = range(3)
 FLOAT_PRECISION = 26
 
@@ -116,6 +116,7 @@ def _declare(lib):
         "pg_device_errors": [vp, ctypes.POINTER(i)],
         "pg_tc_selftest": [vp, vp, vp, vp],
         "pg_tensor_rate": [vp, i, i, vp],
+        "pg_device_op_u64": [vp, i, vp, sz, i, u64, vp],
         "pg_net_layer_times": [vp, vp],
         "pg_tpc_matmul_u64": [vp, _P2, _P2, _P2, i, i, i, i, i, i, i],
         "pg_tpc_matmul_u32": [vp, _P2, _P2, _P2, i, i, i, i, i, i, i],
@@ -468,6 +469,24 @@ def reconstruct(ctx: Context, a, out=None):
 def reshare(ctx: Context, c, out):
     ctx._check(lib().pg_rss_reshare_u64(ctx.handle, _p3(c), c.shape[1], _p6(out)))
     return out
+
+
+def device_op_(ctx: Context, op: int, a, rhs):
+    """DeviceData<uint64_t>'s own operators (DeviceData.h:131-277,
+    functors.cuh) in place on one CUDA int64 tensor a: rhs an int (scalar) or
+    a tensor of a's size. op is one of OP_ADD, OP_SUB, OP_MUL, OP_DIV (through
+    double), OP_XOR, OP_AND, OP_SHR (arithmetic), OP_SHL, or OP_SET (fill)."""
+    torch = _torch()
+    if isinstance(rhs, torch.Tensor):
+        if rhs.numel() != a.numel():
+            raise PiranhaError("device_op_: sizes differ")
+        st = lib().pg_device_op_u64(ctx.handle, op, ctypes.c_void_p(a.data_ptr()), a.numel(), RHS_PUBLIC, 0,
+                                    ctypes.c_void_p(rhs.data_ptr()))
+    else:
+        st = lib().pg_device_op_u64(ctx.handle, op, ctypes.c_void_p(a.data_ptr()), a.numel(), RHS_SCALAR,
+                                    int(rhs) % (1 << 64), None)
+    ctx._check(st)
+    return a
 
 
 def local_(ctx: Context, op: int, a, rhs):

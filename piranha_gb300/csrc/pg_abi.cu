@@ -63,6 +63,7 @@ int prg_fill_u64(Ctx *, const uint8_t *, uint64_t, uint64_t *, size_t);
 int prg_set_keys(Ctx *, const uint8_t *, uint64_t);
 int rss_local_u64(Ctx *, int, uint64_t *const *, size_t, int, uint64_t, const uint64_t *, const uint64_t *const *);
 int local_u64(Ctx *, int, int, uint64_t *const *, size_t, int, uint64_t, const uint64_t *, const uint64_t *const *);
+int device_op_u64(Ctx *, int, uint64_t *, size_t, int, uint64_t, const uint64_t *);
 template <typename T>
 int rss_matmul(Ctx *, const T *const *, const T *const *, T *const *, const T *const *, int, int, int, int, int, int,
                int);
@@ -432,6 +433,10 @@ int pg_rss_local_u64(pg_ctx *c, int op, uint64_t *const a[6], size_t n, int kind
                      const uint64_t *pub, const uint64_t *const shares[6]) {
     CTX_OR_FAIL(c);
     return rss_local_u64(c, op, a, n, kind, scalar, pub, shares);
+}
+int pg_device_op_u64(pg_ctx *c, int op, uint64_t *a, size_t n, int kind, uint64_t scalar, const uint64_t *rhs) {
+    CTX_OR_FAIL(c);
+    return device_op_u64(c, op, a, n, kind, scalar, rhs);
 }
 int pg_tpc_local_u64(pg_ctx *c, int op, uint64_t *const a[2], size_t n, int kind, uint64_t scalar,
                      const uint64_t *pub, const uint64_t *const shares[2]) {

@@ -170,6 +170,12 @@ __device__ __forceinline__ uint32_t div_general(uint32_t x, uint32_t d) {
 template <typename T> __device__ __forceinline__ T div_public(T x, T d, int t) {
     return t >= 0 ? div_pow2(x, t) : div_general(x, d);
 }
+// device-side: log2 of d when d is a power of two in the integer-path range, else -1
+template <typename T> __device__ __forceinline__ int pow2_shift_dev(T d) {
+    if (d == 0 || (d & (d - 1))) return -1;
+    const int t = (int)(sizeof(T) * 8) - 1 - (sizeof(T) == 8 ? __clzll((long long)d) : __clz((int)d));
+    return t <= (int)(sizeof(T) * 8 - 2) ? t : -1;
+}
 // host-side: log2 of d when d is a power of two in the integer-path range
 template <typename T> inline int pow2_shift(T d) {
     if (d == 0 || (d & (d - 1))) return -1;

@@ -381,6 +381,44 @@ int rss_local_u64(Ctx *c, int op, uint64_t *const a[6], size_t n, int kind, uint
     return local_u64(c, 6, op, a, n, kind, scalar, pub, shares);
 }
 
+// DeviceData's own operators (src/gpu/DeviceData.h:131-277 with the functors
+// of src/gpu/functors.cuh:1-117) on one array: a op= scalar or a op= vector
+// for + - * / ^ & >> <<, and fill. Division is the reference's through double
+// (div_public: exact integers for powers of two, device double otherwise).
+template <typename T>
+__global__ void device_op_kernel(T *a, size_t n, int op, T scalar, const T *vec, int shift) {
+    GRID_STRIDE(i, n) {
+        const T r = vec ? vec[i] : scalar;
+        T x = a[i];
+        switch (op) {
+            case PG_OP_ADD: x += r; break;
+            case PG_OP_SUB: x -= r; break;
+            case PG_OP_MUL: x *= r; break;
+            case PG_OP_XOR: x ^= r; break;
+            case PG_OP_AND: x &= r; break;
+            case PG_OP_SHR: x = sar64(x, r); break;
+            case PG_OP_SHL: x = shl64(x, r); break;
+            case PG_OP_DIV: x = div_public<T>(x, r, vec ? pow2_shift_dev(r) : shift); break;
+            default: x = r; break;  // PG_OP_SET
+        }
+        a[i] = x;
+    }
+}
+
+int device_op_u64(Ctx *c, int op, uint64_t *a, size_t n, int kind, uint64_t scalar, const uint64_t *vec) {
+    if (op < 0 || op > PG_OP_SET) return set_error(c, PG_ERR_UNSUPPORTED, "no DeviceData operator %d", op);
+    if (kind != PG_RHS_SCALAR && kind != PG_RHS_PUBLIC)
+        return set_error(c, PG_ERR_UNSUPPORTED, "DeviceData operators take a scalar or a vector");
+    if (n && (!a || (kind == PG_RHS_PUBLIC && !vec))) return set_error(c, PG_ERR_INVALID_ARG, "null pointer");
+    if (op == PG_OP_SET && kind != PG_RHS_SCALAR) return set_error(c, PG_ERR_UNSUPPORTED, "fill takes a scalar");
+    if (!n) return PG_OK;
+    device_op_kernel<uint64_t><<<grid1(c, n), 256, 0, c->stream>>>(a, n, op, scalar,
+                                                                   kind == PG_RHS_PUBLIC ? vec : nullptr,
+                                                                   pow2_shift<uint64_t>(scalar));
+    c->launches++;
+    return launch_status(c, "device_op_kernel");
+}
+
 template int rss_reshare<uint64_t>(Ctx *, const uint64_t *const *, size_t, uint64_t *const *);
 template int rss_mul<uint64_t, false>(Ctx *, uint64_t *const *, const uint64_t *const *, size_t);
 template int rss_mul<uint64_t, true>(Ctx *, uint64_t *const *, const uint64_t *const *, size_t);

@@ -903,12 +903,12 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn(Ctx *c) {
 
 // Once per device (with it current): the GEMM kernel's shared-memory limit
 // and the tensor-map encoder.
-int prepare_device(Ctx *c) {
+int prepare_device(Ctx *c, bool again) {
     static std::mutex mu;
     static bool done[64];
     std::lock_guard<std::mutex> lock(mu);
     if (c->device < 0 || c->device >= 64) return set_error(c, PG_ERR_UNSUPPORTED, "device ordinal %d", c->device);
-    if (!done[c->device]) {
+    if (!done[c->device] || again) {
         PG_CHECK_CUDA(c, cudaFuncSetAttribute(limb_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)smem_bytes()));
         if (!encode_fn(c)) return PG_ERR_CUDA;
@@ -1548,7 +1548,7 @@ int limb3_rss_conv_u64(Ctx *c, const uint64_t *const A[6], const uint64_t *const
         [&] { return rss_conv<uint64_t>(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc); });
 }
 
-int limb_prepare_current_device(Ctx *c) { return lt::prepare_device(c); }
+int limb_prepare_current_device(Ctx *c, bool again) { return lt::prepare_device(c, again); }
 
 // limb3_rss_matmul_u64 without a bias, with every scratch byte taken from
 // [scr, scr + cap): the digit image of A, the packed weights, and the split-K

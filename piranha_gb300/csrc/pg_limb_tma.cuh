@@ -31,7 +31,7 @@ struct Plan {
     size_t image_bytes, packB_bytes;
 };
 
-int prepare_device(Ctx *c);  // once per device, with it current (no allocation)
+int prepare_device(Ctx *c, bool again = false);  // once per device (again: repeat it), with it current (no allocation)
 int plan_gemm(Ctx *c, Plan &p, int M, int N, int K, int tA, int tB, int tC);
 int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad);
 // the weight gradient of that convolution as a GEMM over the output pixels

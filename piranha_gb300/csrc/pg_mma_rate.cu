@@ -173,9 +173,19 @@ extern "C" int pg_tensor_rate(pg_ctx *c, int form, int iters, double *out) {
         return set_error(c, PG_ERR_NO_MEMORY, "tensor_rate: buffers");
     }
     int st = PG_OK;
+    // tcgen05 forms: an unused dynamic shared-memory reservation keeps one CTA
+    // (one 512-column tensor-memory allocation) per SM
+    const int pad_smem = tc ? 160 * 1024 : 0;
+    if (tc && (cudaFuncSetAttribute(rate::tc_rate_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad_smem) !=
+                   cudaSuccess ||
+               cudaFuncSetAttribute(rate::tc_rate_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, pad_smem) !=
+                   cudaSuccess)) {
+        cudaGetLastError();
+        st = set_error(c, PG_ERR_CUDA, "tensor_rate: shared-memory limit");
+    }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     float ms = 0.f;
-    if (cudaMemsetAsync(io, 0x35, 64 * sizeof(uint32_t), c->stream) != cudaSuccess ||
+    if (st == PG_OK && cudaMemsetAsync(io, 0x35, 64 * sizeof(uint32_t), c->stream) != cudaSuccess ||
         cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
         st = set_error(c, PG_ERR_CUDA, "tensor_rate: set-up");
     }
@@ -183,8 +193,8 @@ extern "C" int pg_tensor_rate(pg_ctx *c, int form, int iters, double *out) {
         const int n = rep == 0 ? (iters / 8 > 0 ? iters / 8 : 1) : iters;
         cudaEventRecord(e0, c->stream);
         switch (form) {
-            case PG_RATE_TC_F16: rate::tc_rate_kernel<0><<<blocks, threads, 0, c->stream>>>(n, cyc, c->dev_err); break;
-            case PG_RATE_TC_F8: rate::tc_rate_kernel<1><<<blocks, threads, 0, c->stream>>>(n, cyc, c->dev_err); break;
+            case PG_RATE_TC_F16: rate::tc_rate_kernel<0><<<blocks, threads, pad_smem, c->stream>>>(n, cyc, c->dev_err); break;
+            case PG_RATE_TC_F8: rate::tc_rate_kernel<1><<<blocks, threads, pad_smem, c->stream>>>(n, cyc, c->dev_err); break;
             case PG_RATE_MMA_S8:
                 rate::mma_sync_rate_kernel<1><<<blocks, threads, 0, c->stream>>>(n, io, io + 64, cyc);
                 break;

@@ -3,8 +3,15 @@ fixed device array) against pg_rss_matmul_u64, bit for bit, through the C ABI.
 
 The file name sorts last, so in a full run these calls come after every other
 test has used the library in the same process; it passes on its own as well.
+One test runs the calls in a child process whose CUDA allocation functions
+are wrapped by a small counting library (LD_PRELOAD), so that an allocation
+freed again inside a call is seen too.
 """
 import ctypes
+import json
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -119,3 +126,101 @@ def test_noalloc_any_k(pg, ctx):
     ctx._check(_noalloc(pg, ctx, pg.to_device(a), pg.to_device(b), out, M, N, K, 1, 1, 1, 20))
     ctx.check_device_errors()
     assert np.array_equal(pg.to_host(out), orc.matmul(a, b, M, N, K, 1, 1, 1, 20))
+
+
+_COUNTER_C = r"""
+#define _GNU_SOURCE
+#include <dlfcn.h>
+#include <stddef.h>
+static long n_calls;
+long pg_test_alloc_calls(void) { return __atomic_load_n(&n_calls, __ATOMIC_SEQ_CST); }
+void pg_test_alloc_reset(void) { __atomic_store_n(&n_calls, 0, __ATOMIC_SEQ_CST); }
+#define COUNT() __atomic_add_fetch(&n_calls, 1, __ATOMIC_SEQ_CST)
+#define REAL(name, type) static type real; if (!real) real = (type)dlsym(RTLD_NEXT, name)
+typedef int (*f_pp_sz)(void **, size_t);
+typedef int (*f_p)(void *);
+typedef int (*f_pp_sz_s)(void **, size_t, void *);
+typedef int (*f_p_s)(void *, void *);
+typedef int (*f_pp_sz_u)(void **, size_t, unsigned);
+typedef int (*f_pitch)(void **, size_t *, size_t, size_t);
+int cudaMalloc(void **p, size_t n) { REAL("cudaMalloc", f_pp_sz); COUNT(); return real(p, n); }
+int cudaFree(void *p) { REAL("cudaFree", f_p); COUNT(); return real(p); }
+int cudaMallocAsync(void **p, size_t n, void *s) { REAL("cudaMallocAsync", f_pp_sz_s); COUNT(); return real(p, n, s); }
+int cudaFreeAsync(void *p, void *s) { REAL("cudaFreeAsync", f_p_s); COUNT(); return real(p, s); }
+int cudaMallocHost(void **p, size_t n) { REAL("cudaMallocHost", f_pp_sz); COUNT(); return real(p, n); }
+int cudaFreeHost(void *p) { REAL("cudaFreeHost", f_p); COUNT(); return real(p); }
+int cudaHostAlloc(void **p, size_t n, unsigned f) { REAL("cudaHostAlloc", f_pp_sz_u); COUNT(); return real(p, n, f); }
+int cudaMallocManaged(void **p, size_t n, unsigned f) { REAL("cudaMallocManaged", f_pp_sz_u); COUNT(); return real(p, n, f); }
+int cudaMallocPitch(void **p, size_t *pitch, size_t w, size_t h) { REAL("cudaMallocPitch", f_pitch); COUNT(); return real(p, pitch, w, h); }
+"""
+
+_CHILD = r"""
+import ctypes, json, sys
+import numpy as np
+import torch
+sys.path.insert(0, sys.argv[2])
+import piranha_gb300 as pg
+counter = ctypes.CDLL(sys.argv[1])
+P6 = ctypes.c_void_p * 6
+fn = pg.lib().pg_rss_matmul_u64_noalloc
+fn.argtypes = [ctypes.c_void_p, P6, P6, P6] + [ctypes.c_int] * 7
+p6 = lambda t: P6(*[t[p, s].data_ptr() for p in range(3) for s in range(2)])
+cases = [(256, 192, 512, 1, 1, 1, 26), (64, 128, 1024, 1, 0, 1, 20)]
+g = torch.Generator(device="cuda")
+g.manual_seed(5)
+ins = [(torch.randint(-2**63, 2**63 - 1, (3, 2, M * K), dtype=torch.int64, device="cuda", generator=g),
+        torch.randint(-2**63, 2**63 - 1, (3, 2, K * N), dtype=torch.int64, device="cuda", generator=g))
+       for (M, N, K, *_) in cases]
+outs = [pg.empty_shares(M * N) for (M, N, *_) in cases]
+ctx = pg.Context(0, form=pg.FORM_LIMB_TC)
+want = []
+for (M, N, K, tA, tB, tC, t), (a, b) in zip(cases, ins):
+    w = pg.empty_shares(M * N)
+    pg.matmul(ctx, a, b, w, M, N, K, tA, tB, tC, t)
+    want.append(w)
+(M, N, K, tA, tB, tC, t), (a, b) = cases[0], ins[0]
+ctx._check(fn(ctx.handle, p6(a), p6(b), p6(outs[0]), M, N, K, tA, tB, tC, t))  # set-up call
+ctx.sync()
+ctx2 = pg.Context(0, form=pg.FORM_LIMB_TC)
+ctx2.set_autotune(False)
+w2 = pg.empty_shares(96 * 80)
+a2 = ins[0][0][..., : 96 * 512].contiguous()
+b2 = ins[0][1][..., : 512 * 80].contiguous()
+torch.cuda.synchronize()
+counter.pg_test_alloc_reset()
+for (M, N, K, tA, tB, tC, t), (a, b), o in zip(cases, ins, outs):
+    ctx._check(fn(ctx.handle, p6(a), p6(b), p6(o), M, N, K, tA, tB, tC, t))
+ctx.sync()
+noalloc_calls = counter.pg_test_alloc_calls()
+counter.pg_test_alloc_reset()
+# the detector itself: a regular call on a fresh context grows its scratch
+pg.matmul(ctx2, a2, b2, w2, 96, 80, 512, 1, 1, 1, 26)
+ctx2.sync()
+regular_calls = counter.pg_test_alloc_calls()
+ctx.check_device_errors()
+equal = all(torch.equal(o, w) for o, w in zip(outs, want))
+print(json.dumps({"noalloc": noalloc_calls, "regular": regular_calls, "equal": equal}))
+"""
+
+
+def test_noalloc_calls_no_allocation_function(pg, tmp_path):
+    """Two calls in a row (after the set-up call) reach no CUDA allocation or
+    free function at all, while a regular call on a fresh context does."""
+    import shutil
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler for the allocation counter")
+    src = tmp_path / "count_alloc.c"
+    src.write_text(_COUNTER_C)
+    so = tmp_path / "libcount_alloc.so"
+    subprocess.run([cc, "-shared", "-fPIC", "-O1", "-o", str(so), str(src), "-ldl"], check=True)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, LD_PRELOAD=str(so))
+    r = subprocess.run([sys.executable, "-c", _CHILD, str(so), root], env=env, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    assert res["equal"], res
+    assert res["regular"] > 0, res  # the counter sees the regular path's scratch growth
+    assert res["noalloc"] == 0, res
