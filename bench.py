@@ -83,6 +83,11 @@ WORKLOADS = {
              "K": 4096, "unit": "ring-MAC/s",
              "desc": "3PC RSS matmul M=N=K=4096 over Z_2^64 (uniform random shares), truncation by 2^26 and "
                      "reshare; 6*M*N*K ring multiply-adds per step (3 parties x the concatenated K)"},
+    "conv": {"metric": "3PC share-convolution ring MAC/s", "kind": "conv", "fp": 26, "ring": "u64",
+             "unit": "ring-MAC/s",
+             "desc": "3PC RSS convolution (fprop) of one VGG16-shaped layer (--conv-shape H,W,Din,Dout,f,stride,pad; "
+                     "default 32,32,64,64,3,1,1), uniform random uint64 shares, truncation by 2^26; "
+                     "6*batch*P*Q*Dout*f*f*Din ring multiply-adds per step"},
     "stream": {"metric": "3PC batched request stream img/s", "kind": "stream", "fp": 26, "ring": "u64",
                "requests": 512, "max_batch": 64,
                "desc": "512 requests, batch uniform in 1..64, SecureML or VGG16 (even odds), 3PC RSS, uint64 "
@@ -110,6 +115,7 @@ def parse():
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-u64-form comparison run")
     ap.add_argument("--sweep", action="store_true", help="gemm: also time M = N = K in 512..8192 in both forms")
     ap.add_argument("--no-autotune", action="store_true", help="split-K by the heuristic instead of by timing")
+    ap.add_argument("--conv-shape", default="32,32,64,64,3,1,1", help="conv: H,W,Din,Dout,f,stride,pad")
     return ap.parse_args()
 
 
@@ -151,6 +157,28 @@ def make_gemm(seed=SEED):
     A = rng.integers(0, 2**64 - 1, size=(3, 2, M * K), dtype=np.uint64, endpoint=True)
     B = rng.integers(0, 2**64 - 1, size=(3, 2, K * N), dtype=np.uint64, endpoint=True)
     return {"A": A, "B": B, "M": M, "N": N, "K": K}
+
+
+def conv_geometry(args):
+    H, W, Din, Dout, f, st, pd = (int(x) for x in args.conv_shape.split(","))
+    P, Q = (H + 2 * pd - f) // st + 1, (W + 2 * pd - f) // st + 1
+    return {"H": H, "W": W, "Din": Din, "Dout": Dout, "f": f, "stride": st, "pad": pd, "P": P, "Q": Q,
+            "batch": args.batch}
+
+
+def make_conv(args, seed=SEED):
+    """Uniform random uint64 share views of the layer's input (NHWC) and filters (KRSC)."""
+    g = conv_geometry(args)
+    rng = np.random.default_rng(seed + 13)
+    X = rng.integers(0, 2**64 - 1, size=(3, 2, g["batch"] * g["H"] * g["W"] * g["Din"]), dtype=np.uint64,
+                     endpoint=True)
+    F = rng.integers(0, 2**64 - 1, size=(3, 2, g["Dout"] * g["f"] * g["f"] * g["Din"]), dtype=np.uint64,
+                     endpoint=True)
+    return {**g, "X": X, "F": F}
+
+
+def conv_macs(g):
+    return 6 * g["batch"] * g["P"] * g["Q"] * g["Dout"] * g["f"] * g["f"] * g["Din"]
 
 
 def work_per_step(name, batch):
@@ -312,6 +340,16 @@ def cpu_baseline(name, wl, batch_full, budget_s):
         return cpu_baseline_stream(wl, budget_s)
     if WORKLOADS[name]["kind"] == "gemm":
         return cpu_baseline_gemm(wl, budget_s)
+    if WORKLOADS[name]["kind"] == "conv":
+        g = wl
+        n_img_in = g["H"] * g["W"] * g["Din"]
+        t0 = time.perf_counter()
+        orc.convolution(np.ascontiguousarray(g["X"][..., :n_img_in]), g["F"], orc.FPROP, 1, g["H"], g["W"], g["f"],
+                        g["Din"], g["Dout"], g["stride"], g["pad"], WORKLOADS[name]["fp"])
+        secs = time.perf_counter() - t0
+        cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+        return {"value": conv_macs(g) / g["batch"] / secs, "unit": "ring-MAC/s", "cores": cores, "kind": "port",
+                "sample": f"one image of the {g['batch']}-image batch ({secs:.2f} s), same shares"}
     w = WORKLOADS[name]
     layers, params, x_full = wl["layers"], wl["params"], wl["x"]
     n_in = nets.input_size(layers)
@@ -381,6 +419,18 @@ def reference_arm(args, name, wl):
             a = np.ascontiguousarray(A4[:, :, rows, :].reshape(3, 2, -1))
             orc.matmul(a, wl["B"], n, N, K, 1, 1, 1, fp)
             return n
+    elif kind == "conv":
+        g = wl
+        n_img_in = g["H"] * g["W"] * g["Din"]
+        X4 = g["X"].reshape(3, 2, g["batch"], n_img_in)
+        total, unit_work, smallest = g["batch"], conv_macs(g) // g["batch"], 1
+
+        def run(k0, n):
+            idx = (k0 + np.arange(n)) % g["batch"]
+            x = np.ascontiguousarray(X4[:, :, idx, :].reshape(3, 2, -1))
+            orc.convolution(x, g["F"], orc.FPROP, n, g["H"], g["W"], g["f"], g["Din"], g["Dout"], g["stride"],
+                            g["pad"], fp)
+            return n
     elif kind == "stream":
         models, params, reqs = wl
         total, unit_work, smallest = sum(b for _, b, _ in reqs), 1, 1
@@ -442,7 +492,8 @@ def reference_arm(args, name, wl):
         units += got * unit_work
     tot = sum(secs)
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    what = {"gemm": "share-GEMM rows", "stream": "images of the next request"}.get(kind, "images")
+    what = {"gemm": "share-GEMM rows", "stream": "images of the next request", "conv": "images of the batch"}.get(
+        kind, "images")
     covered = "the whole batch once" if done >= total else f"{done} of {total}"
     return {"value": units / tot, "ms_per_step": 1e3 * tot / steps, "units": units,
             "cpu_baseline": {"value": units / tot, "unit": w.get("unit", "img/s"), "cores": cores, "kind": "port",
@@ -459,6 +510,10 @@ def line_config(args, w, world):
     if w["kind"] == "gemm":
         cfg.update({"global_batch": None, "M": w["M"], "N": w["N"], "K": w["K"], "truncation": w["fp"],
                     "data_size": f"operands {6 * w['M'] * w['K'] * 8 / 1e6:.0f} MB per share tensor, larger than L2"})
+    if w["kind"] == "conv":
+        g = conv_geometry(args)
+        cfg.update({"conv": {k: g[k] for k in ("H", "W", "Din", "Dout", "f", "stride", "pad")}, "truncation": w["fp"],
+                    "data_size": f"input shares {48 * g['batch'] * g['H'] * g['W'] * g['Din'] / 1e6:.0f} MB"})
     return cfg
 
 
@@ -503,6 +558,10 @@ def run_ours(args, rank, world, local_rank):
         wl = make_gemm()
         with torch.cuda.stream(stream):
             return bench_gemm(args, pg, torch, stream, dev, wl, world), wl
+    if kind == "conv":
+        wl = make_conv(args)
+        with torch.cuda.stream(stream):
+            return bench_conv(args, pg, torch, stream, dev, wl, world), wl
     wl = make_workload(args.workload, batch)
 
     if kind == "fcnet":
@@ -738,16 +797,20 @@ def bench_train(args, pg, torch, stream, dev, form, wl, batch, world):
     return out
 
 
-def _gemm_form(args, pg, torch, stream, dev, form, A, B, M, N, K, world, steps, warmup, e2e_host=None):
-    """One form of the share-GEMM: eager call (sizes the scratch), one captured
-    graph, warm-up and timed replays; optionally the end-to-end replays."""
+def _gemm_form(args, pg, torch, stream, dev, form, A, B, M, N, K, world, steps, warmup, e2e_host=None, op=None):
+    """One form of the share-GEMM (or of `op(ctx, A, B, C)` with an M x N
+    output): eager call (sizes the scratch), one captured graph, warm-up and
+    timed replays; optionally the end-to-end replays."""
     fp = WORKLOADS["gemm"]["fp"]
+    if op is None:
+        def op(ctx, a, b, c):
+            pg.matmul(ctx, a, b, c, M, N, K, 1, 1, 1, fp)
     ctx = pg.Context(dev.index, stream=stream, form=form)
     ctx.set_autotune(not args.no_autotune)
     C = pg.empty_shares(M * N, device=dev)
-    pg.matmul(ctx, A, B, C, M, N, K, 1, 1, 1, fp)
+    op(ctx, A, B, C)
     with ctx.capture() as graph:
-        pg.matmul(ctx, A, B, C, M, N, K, 1, 1, 1, fp)
+        op(ctx, A, B, C)
     for _ in range(warmup):
         graph.launch()
     stream.synchronize()
@@ -765,9 +828,9 @@ def _gemm_form(args, pg, torch, stream, dev, form, A, B, M, N, K, world, steps, 
         a_h, b_h, c_h = e2e_host
         A2, B2 = A.clone(), B.clone()
         C2 = pg.empty_shares(M * N, device=dev)
-        pg.matmul(ctx, A2, B2, C2, M, N, K, 1, 1, 1, fp)
+        op(ctx, A2, B2, C2)
         with ctx.capture() as graph2:
-            pg.matmul(ctx, A2, B2, C2, M, N, K, 1, 1, 1, fp)
+            op(ctx, A2, B2, C2)
         sets = [(A, B, C, graph), (A2, B2, C2, graph2)]
         up, down = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
 
@@ -871,6 +934,60 @@ def bench_gemm(args, pg, torch, stream, dev, wl, world):
             sweep.append(row)
             del As, Bs
         out["sweep"] = sweep
+    return out
+
+
+def bench_conv(args, pg, torch, stream, dev, wl, world):
+    """One RSS convolution layer (fprop with truncation by 2^26), replayed from
+    one CUDA graph, in the form --form picks (the limb form by default, with
+    the u64 form beside it)."""
+    g = wl
+    X = pg.to_device(g["X"], dev)
+    F = pg.to_device(g["F"], dev)
+    macs = conv_macs(g)
+    n_out = g["batch"] * g["P"] * g["Q"] * g["Dout"]
+    x_h = torch.empty(X.shape, dtype=X.dtype, pin_memory=True)
+    f_h = torch.empty(F.shape, dtype=F.dtype, pin_memory=True)
+    x_h.copy_(X.cpu())
+    f_h.copy_(F.cpu())
+    c_h = torch.empty((3, 2, n_out), dtype=torch.int64, pin_memory=True)
+
+    def op(ctx, a, b, c):
+        pg.convolution(ctx, a, b, c, pg.FPROP, g["batch"], g["H"], g["W"], g["f"], g["Din"], g["Dout"], g["stride"],
+                       g["pad"], 26)
+
+    form = pg.FORM_U64 if args.form == "u64" else pg.FORM_LIMB_TC
+    r = _gemm_form(args, pg, torch, stream, dev, form, X, F, n_out, 1, 1, world, args.steps, args.warmup,
+                   (x_h, f_h, c_h), op=op)
+    peaks = load_peaks()
+    peak = peaks.get("bf16_tflops")
+    achieved = LIMB_FLOPS_PER_RING_MAC * macs * args.steps / r["dev_s"] / 1e12
+    out = {
+        "form": "limb_tc" if form == pg.FORM_LIMB_TC else "u64",
+        "unit": "ring-MAC/s",
+        "value": aggregate(world, macs, args.steps, r["dev_s"]),
+        "ms_per_step": 1e3 * r["dev_s"] / args.steps,
+        "wall_s": r["wall"],
+        "e2e": {"value": aggregate(world, macs, args.steps, r["e2e_s"]), "unit": "ring-MAC/s", "pipelined": True,
+                "h2d_bytes_per_step": int(X.numel() + F.numel()) * 8, "d2h_bytes_per_step": int(c_h.numel()) * 8},
+        "gpu_launches": int(r["launches"]),
+        "clocks": r["clocks"],
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak else None, "traffic": None,
+                     "kernel": "share-conv (the form's GEMM kernel with its operand image, packing and reduce "
+                               "launches)",
+                     "work": f"72 limb-tensor flops per ring MAC, {macs:.4g} ring MACs/step",
+                     "peak_source": "bf16_tflops of measured" if peak else None},
+        "comm_per_party_per_step": {"tx_bytes": int((r["comm1"]["tx"][0] - r["comm0"]["tx"][0]) // args.steps),
+                                    "rounds": int((r["comm1"]["rounds"] - r["comm0"]["rounds"]) // args.steps)},
+    }
+    if form == pg.FORM_LIMB_TC and not args.no_compare:
+        st = max(2, args.steps // 4)
+        u = _gemm_form(args, pg, torch, stream, dev, pg.FORM_U64, X, F, n_out, 1, 1, world, st, 1, op=op)
+        uv = macs * st / u["dev_s"]
+        out["compare_u64"] = {"value": uv, "ms_per_step": 1e3 * u["dev_s"] / st,
+                              "gemm_tflops_equiv": LIMB_FLOPS_PER_RING_MAC * uv / 1e12,
+                              "limb_over_u64": out["value"] / world / uv}
     return out
 
 
@@ -1108,7 +1225,7 @@ def main():
         if rank != 0:
             return
         wl = (make_stream() if w["kind"] == "stream" else make_gemm() if w["kind"] == "gemm"
-              else make_workload(args.workload, args.batch))
+              else make_conv(args) if w["kind"] == "conv" else make_workload(args.workload, args.batch))
         r = reference_arm(args, args.workload, wl)
         unit = w.get("unit", "img/s")
         line = {"metric": w["metric"], "value": r["value"], "unit": unit, "impl": "reference", "n_gpus": args.gpus,

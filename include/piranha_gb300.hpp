@@ -93,8 +93,6 @@ template <typename T> inline T encode(double v, bool fixed = true) {
     return (T)(uint64_t)(int64_t)x;
 }
 
-template <typename T> struct is_ring : std::integral_constant<bool, std::is_same<T, uint64_t>::value> {};
-
 }  // namespace piranha_gb300
 
 /* ------------------------------------------------------------- DeviceData */
@@ -177,7 +175,6 @@ template <typename T> class DeviceData {
 
   private:
     DeviceData &apply(int op, int kind, T scalar, const T *vec) {
-        static_assert(sizeof(T) > 0, "");
         if (!std::is_same<T, uint64_t>::value)
             throw piranha_gb300::Error(PG_ERR_UNSUPPORTED, "DeviceData operators are built for uint64_t");
         piranha_gb300::check(pg_device_op_u64(piranha_gb300::context(), op, (uint64_t *)ptr_, n_, kind,
@@ -593,8 +590,8 @@ inline void maxpool_im2row(SharePart<uint64_t> im, SharePart<uint64_t> output, i
                                                     (uint64_t)(int64_t)pad_val));
 }
 
-/* truncate_cols (matrix.cuh:383-396): columns [start_cols, end_cols) of each
- * row of a, into b */
+/* truncate_cols (matrix.cuh:383-396): a holds rows of start_cols columns;
+ * the first end_cols columns of each row go to b */
 inline void truncate_cols(const DeviceData<uint8_t> *a, DeviceData<uint8_t> *b, size_t rows, size_t start_cols,
                           size_t end_cols) {
     piranha_gb300::check(pg_truncate_cols_u8(piranha_gb300::context(), a->data(), b->data(), rows, (int)start_cols,

@@ -13,6 +13,7 @@
 // six share buffers of each result tensor, for tests/test_gpu_cpp_layer.py to
 // compare with the expected values and with the oracle.
 #include <cstdio>
+#include <iomanip>
 #include <iostream>
 #include <map>
 #include <sstream>
@@ -160,7 +161,7 @@ static void run(const Case &k) {
         maxpool(pools, result, expandedMaxPrime, expandedPoolSize);
         for (int share = 0; share < Share::numShares(); share++)
             gpu::truncate_cols(expandedMaxPrime.getShare(share), dresult.getShare(share),
-                               pools.size() / expandedPoolSize, 0, 9);
+                               pools.size() / expandedPoolSize, expandedPoolSize, 9);
         print_revealed(n, "result", result, true);
         print_revealed(n, "dresult", dresult, false);
         print_shares(n, "result", result);
@@ -191,6 +192,7 @@ static void run(const Case &k) {
 }
 
 int main() {
+    std::cout << std::setprecision(17);
     std::string line;
     Case k;
     int status = 0;
