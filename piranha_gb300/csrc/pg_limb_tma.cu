@@ -49,6 +49,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -82,9 +83,11 @@ struct Args {
     int M, N;
     int kblocks, cblocks, C8, f, pad;
     int Wt, Ht, Nt, R, tiles_w, tiles_h, P, Q, Nimg;
+    int Himg, Wimg;
     int rows_mode;  // 1: the image holds one row per output row (GEMM, im2col)
     int ntiles_n, total_stages, chunks_per_split;
     int direct, colmajor;
+    int posmajor;  // tiles by output position (Plan::posmajor); H, W: input extents then
     int zeros_kept;  // the four zero output shares already hold 0: write only value / bias shares
     int tma_out;     // the two value shares go out as tensor-map stores of the staged tile (see tma_store_4d)
     uint32_t a_box_bytes;  // bytes of one digit plane of a stage (16 * 2 * Wt * Ht * Nt)
@@ -158,6 +161,8 @@ struct ImageArgs {
     long long ld;      // ROWS: row stride; COLS: column stride
     int vec;           // ROWS: rows are 16-byte aligned and Kreal is a multiple of 8
     int H, W, Din, f, stride, pad, P, Q;
+    long long bi_n, bi_hw;  // ROWS, batch-innermost image: image row (h * W + w) * bi_n + n holds source row
+                            // n * bi_hw + h * W + w (bi_n = 0: image row = source row)
     uint4 *img;
 };
 
@@ -185,7 +190,8 @@ __global__ void image_kernel(const __grid_constant__ ImageArgs ia) {
         if (pix >= ia.pixels_src) {
             // zero row padding the image to whole lines
         } else if (ia.mode == SRC_ROWS) {
-            const uint64_t *src = a + pix * ia.ld + k0;
+            const long long srow = ia.bi_n ? (pix % ia.bi_n) * ia.bi_hw + pix / ia.bi_n : pix;
+            const uint64_t *src = a + srow * ia.ld + k0;
             if (ia.vec && k0 < ia.Kreal) {
 #pragma unroll
                 for (int i = 0; i < 4; i++) {
@@ -266,6 +272,7 @@ struct ReluImageArgs {
     uint4 *img;
     long long pixels, pixels_alloc;
     int C8;
+    long long bi_n, bi_hw;  // batch-innermost image (see ImageArgs); 0: image pixel = NHWC pixel
 };
 
 constexpr int RI_PIX = 16, RI_CH = 16, RI_PITCH = RI_PIX + 1;  // pitch 17: two-way bank conflicts at most
@@ -285,7 +292,8 @@ __global__ void __launch_bounds__(256) relu_image_kernel(const __grid_constant__
             const long long pix = p0 + pl;
             uint64_t z[3][2];
             if (pix < a.pixels) {
-                const long long idx = pix * C + cp * RI_CH + ch;
+                const long long src = a.bi_n ? (pix % a.bi_n) * a.bi_hw + pix / a.bi_n : pix;
+                const long long idx = src * C + cp * RI_CH + ch;
                 uint64_t x[3][2], zero[3][2];
                 uint8_t r[3][2];
 #pragma unroll
@@ -579,14 +587,34 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     tc::tc_fence_after();
     const Args &g = sm.args;
     const uint32_t tmem = sm.tmem_base;
-    const int stage_begin = z * g.chunks_per_split * CHUNK_STAGES;
-    int stage_end = stage_begin + g.chunks_per_split * CHUNK_STAGES;
-    if (stage_end > g.total_stages) stage_end = g.total_stages;
-    const int nst = stage_end > stage_begin ? stage_end - stage_begin : 0;
     // output-pixel rectangle of this tile
     const int tw = blockIdx.y % g.tiles_w, t2 = blockIdx.y / g.tiles_w;
     const int th = t2 % g.tiles_h, tn = t2 / g.tiles_h;
     const int w0 = tw * g.Wt, h0 = th * g.Ht, n0 = tn * g.Nt;
+    // Position-major tiles (output pixel (h0, w0) of Nt images) run only the
+    // taps inside the input: rows r_lo..r_lo+nr-1, columns s_lo..s_lo+ns-1 of
+    // the filter. Their K' range (6 segments x taps x channel blocks) is split
+    // evenly over the grid's z slices.
+    int r_lo = 0, s_lo = 0, ns = 1, tile_stages = g.total_stages;
+    if (g.posmajor) {
+        r_lo = g.pad - h0 > 0 ? g.pad - h0 : 0;
+        const int r_hi = g.Himg - 1 + g.pad - h0 < g.f - 1 ? g.Himg - 1 + g.pad - h0 : g.f - 1;
+        s_lo = g.pad - w0 > 0 ? g.pad - w0 : 0;
+        const int s_hi = g.Wimg - 1 + g.pad - w0 < g.f - 1 ? g.Wimg - 1 + g.pad - w0 : g.f - 1;
+        ns = s_hi - s_lo + 1;
+        tile_stages = 6 * (r_hi - r_lo + 1) * ns * g.cblocks;
+    }
+    int stage_begin, stage_end;
+    if (g.posmajor) {
+        const int per = (tile_stages + (int)gridDim.z - 1) / (int)gridDim.z;
+        stage_begin = z * per;
+        stage_end = stage_begin + per;
+    } else {
+        stage_begin = z * g.chunks_per_split * CHUNK_STAGES;
+        stage_end = stage_begin + g.chunks_per_split * CHUNK_STAGES;
+    }
+    if (stage_end > tile_stages) stage_end = tile_stages;
+    const int nst = stage_end > stage_begin ? stage_end - stage_begin : 0;
 
     if (warp == W_PROD) {
         // ------------------------------------------------ TMA + bulk copies
@@ -602,17 +630,36 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     ok = false;
                     break;
                 }
-                const int gst = stage_begin + git;
-                const int seg = gst / g.kblocks, kb = gst - seg * g.kblocks;
-                const int tap = kb / g.cblocks, cb = kb - tap * g.cblocks;
-                const int r = tap / g.f, sx = tap - r * g.f;
+                int gst = stage_begin + git;
+                int seg, tap, cb, x, y, zc;
+                if (g.posmajor) {
+                    // compacted K' index (segment, inside tap, channel block) -> the packed stage
+                    const int per_seg = tile_stages / 6;
+                    seg = gst / per_seg;
+                    const int kb = gst - seg * per_seg;
+                    const int ti = kb / g.cblocks;
+                    cb = kb - ti * g.cblocks;
+                    const int r = r_lo + ti / ns, sx = s_lo + ti % ns;
+                    tap = r * g.f + sx;
+                    gst = seg * g.kblocks + tap * g.cblocks + cb;
+                    // 32-row line of the batch-innermost image: pixel (h * W + w) * Nimg + n0
+                    x = 0;
+                    y = (int)((((long long)(h0 + r - g.pad) * g.Wimg + (w0 + sx - g.pad)) * g.Nimg + n0) >> 5);
+                    zc = 0;
+                } else {
+                    seg = gst / g.kblocks;
+                    const int kb = gst - seg * g.kblocks;
+                    tap = kb / g.cblocks;
+                    cb = kb - tap * g.cblocks;
+                    const int r = tap / g.f, sx = tap - r * g.f;
+                    // line offset (16 bytes per pixel, so always 16-byte aligned), row, image
+                    x = g.rows_mode ? 0 : 8 * (w0 + sx - g.pad);
+                    y = g.rows_mode ? n0 >> 5 : h0 + r - g.pad;
+                    zc = g.rows_mode ? 0 : n0;
+                }
                 const uint32_t bar = tc::smem_u32(&sm.full[s]);
                 tc::mbar_arrive_expect_tx(bar, 8 * g.a_box_bytes + B_STAGE_BYTES);
                 const uint32_t dst = tc::smem_u32(sm.stage[s]);
-                // line offset (16 bytes per pixel, so always 16-byte aligned), row, image
-                const int x = g.rows_mode ? 0 : 8 * (w0 + sx - g.pad);
-                const int y = g.rows_mode ? n0 >> 5 : h0 + r - g.pad;
-                const int zc = g.rows_mode ? 0 : n0;
                 tma_load_5d(dst, &tmA, x, y, zc, 2 * cb, seg * 8, bar);
                 const uint8_t *src = g.packB + ((size_t)gst * g.ntiles_n + blockIdx.x) * B_STAGE_BYTES;
                 tc::bulk_g2s(dst + 8 * A_PLANE_BYTES, src, B_STAGE_BYTES, bar);
@@ -632,7 +679,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         // Each group's issuer blocks on its own barriers only: the drain wait
         // at its chunk starts and the stage data. (One thread interleaving both
         // groups, polling both sets of barriers, issued 12-17 % slower.)
-        if (lane == 0) {
+        if (lane == 0 && nst > 0) {
             const int gi = warp == W_MMA ? 0 : 1;
             const uint32_t s0 = tc::smem_u32(sm.stage[0]);
             const uint64_t adesc0 = tc::smem_desc(s0, g.a_box_bytes / 2, 128);
@@ -918,7 +965,14 @@ int prepare_device(Ctx *c, bool again) {
 }
 
 static void tile_geometry(Plan &p) {
-    if (!p.implicit) {
+    if (p.posmajor) {
+        // one output position of BM images per tile
+        p.Wt = 1;
+        p.Ht = 1;
+        p.Nt = BM;
+        p.tiles_w = p.Q;
+        p.tiles_h = p.P;
+    } else if (!p.implicit) {
         // rows of the image, 32 per tensor-map line
         p.Wt = 1;
         p.Ht = 1;
@@ -971,6 +1025,18 @@ int plan_gemm(Ctx *c, Plan &p, int M, int N, int K, int tA, int tB, int tC) {
     return PG_OK;
 }
 
+// Output positions per image up to which a same convolution is tiled by
+// position (8 x 8 and smaller); PG_POSMAJOR=0 in the environment turns the
+// position-major tiles off (every implicit convolution then uses rectangles).
+constexpr int POSMAJOR_MAX_PIXELS = 64;
+static bool posmajor_enabled() {
+    static const bool on = [] {
+        const char *e = getenv("PG_POSMAJOR");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad) {
     memset(&p, 0, sizeof(p));
     if (batch <= 0 || H <= 0 || W <= 0 || f <= 0 || Din <= 0 || Dout <= 0 || stride <= 0 || pad < 0 ||
@@ -993,6 +1059,12 @@ int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout
         p.f = f; p.pad = pad;
         p.Wimg = W; p.Himg = H; p.Nimg = batch;
         p.P = P; p.Q = Q;
+        // Small "same" convolutions of a batch of whole 128-image tiles run by
+        // output position: a rectangle tile of a 4x4 or 2x2 image spends most
+        // of its taps on the zero padding (5/9 of them at 2x2), which a tile
+        // of one output position over 128 images skips.
+        p.posmajor = posmajor_enabled() && batch % BM == 0 && P == H && Q == W && 2 * pad + 1 == f &&
+                     P * Q <= POSMAJOR_MAX_PIXELS;
     } else {
         // explicit: the image holds the im2col rows (K = f*f*Din padded to 16)
         p.implicit = 0;
@@ -1102,8 +1174,8 @@ bool cached_split(Ctx *c, const Plan &p, int &split, int &cps) {
 
 static std::string tune_key(const Plan &p) {
     char k[256];
-    snprintf(k, sizeof(k), "%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d", p.implicit, p.src_mode, p.M, p.N, p.C, p.kblocks,
-             p.ntiles_n, p.tiles_m, p.Wt, p.Ht, p.Nt, p.f, p.colmajor);
+    snprintf(k, sizeof(k), "%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d%s", p.implicit, p.src_mode, p.M, p.N, p.C,
+             p.kblocks, p.ntiles_n, p.tiles_m, p.Wt, p.Ht, p.Nt, p.f, p.colmajor, p.posmajor ? "/pos" : "");
     return k;
 }
 
@@ -1202,6 +1274,8 @@ int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n,
     a.pixels = p.pixels;
     a.pixels_alloc = p.pixels_alloc;
     a.C8 = p.C / 8;
+    a.bi_n = p.posmajor ? p.Nimg : 0;
+    a.bi_hw = (long long)p.Himg * p.Wimg;
     const long long tiles = (long long)(a.C8 / 2) * ((p.pixels + RI_PIX - 1) / RI_PIX);
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
     long long blocks = tiles < (long long)sms * 16 ? tiles : (long long)sms * 16;
@@ -1228,6 +1302,8 @@ int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image) {
     ia.vec = vec && p.Kreal % 8 == 0;
     ia.H = p.H; ia.W = p.W; ia.Din = p.Din; ia.f = p.cf; ia.stride = p.stride; ia.pad = p.cpad;
     ia.P = p.cP; ia.Q = p.cQ;
+    ia.bi_n = p.posmajor ? p.Nimg : 0;
+    ia.bi_hw = (long long)p.Himg * p.Wimg;
     ia.img = (uint4 *)image;
     if (ia.C8 & 1) return set_error(c, PG_ERR_INVALID_ARG, "image channels %d are not a multiple of 16", p.C);
     const long long units = 6ll * (ia.C8 / 2) * p.pixels_alloc;
@@ -1281,7 +1357,7 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
     cuuint32_t box[5];
     const cuuint64_t plane_stride = (cuuint64_t)p.pixels_alloc * 16;  // bytes between channel groups
     const cuuint64_t C8 = (cuuint64_t)(p.C / 8);
-    if (p.implicit) {
+    if (p.implicit && !p.posmajor) {
         dims[0] = 8 * (cuuint64_t)p.Wimg; dims[1] = p.Himg; dims[2] = p.Nimg;
         strides[0] = (cuuint64_t)p.Wimg * 16; strides[1] = (cuuint64_t)p.Himg * p.Wimg * 16; strides[2] = plane_stride;
         box[0] = 8 * p.Wt; box[1] = p.Ht; box[2] = p.Nt;
@@ -1306,7 +1382,9 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
     g.kblocks = p.kblocks; g.cblocks = p.cblocks; g.C8 = p.C / 8; g.f = p.f; g.pad = p.pad;
     g.Wt = p.Wt; g.Ht = p.Ht; g.Nt = p.Nt; g.R = p.R; g.tiles_w = p.tiles_w; g.tiles_h = p.tiles_h;
     g.rows_mode = !p.implicit;
+    g.posmajor = p.posmajor;
     g.P = p.P; g.Q = p.Q; g.Nimg = p.Nimg;
+    g.Himg = p.Himg; g.Wimg = p.Wimg;
     g.ntiles_n = p.ntiles_n;
     g.total_stages = 6 * p.kblocks;
     g.chunks_per_split = cps;

@@ -28,6 +28,9 @@ struct Plan {
     int Wt, Ht, Nt, R, tiles_w, tiles_h, tiles_m;  // output-pixel rectangle of a tile, rows used
     int tB_kn;          // weights as b[k * N + n] (1) or b[n * Kb + k] (0)
     int colmajor;       // output column-major (GEMM with tC = 0)
+    int posmajor;       // implicit convolution tiled by output position: a tile is one output pixel (p, q) of
+                        // 128 images, the image is stored batch-innermost (pixel (h * W + w) * Nimg + n), and
+                        // the tile runs only the taps that fall inside the input (no zero-padding taps)
     size_t image_bytes, packB_bytes;
 };
 
