@@ -220,16 +220,18 @@ def ring_macs(layers, batch):
 def executed_ring_macs(layers, batch):
     """Ring multiply-adds the limb kernels execute per share-GEMM layer: the
     dense count, except for the convolutions the library tiles by output
-    position (stride 1, same padding, at most 64 output positions, batch a
+    position (stride 1, same padding, at most 64 output positions or the
+    PG_POSMAJOR limit, batch a
     multiple of 128, channels a multiple of 16), which run only the taps
     inside the input: (sum over output rows of the valid filter rows) x (the
     same over columns) taps instead of P * Q * f * f."""
     out = ring_macs(layers, batch)
+    limit = int(os.environ.get("PG_POSMAJOR") or 64)  # the library's position-major limit
     for i, L in enumerate(layers):
         if L[0] != "cnn":
             continue
         H, W, Din, Dout, f, s, p = L[1:]
-        if s == 1 and 2 * p + 1 == f and H * W <= 64 and batch % 128 == 0 and Din % 16 == 0:
+        if s == 1 and 2 * p + 1 == f and H * W <= limit and batch % 128 == 0 and Din % 16 == 0:
             rows = sum(min(f - 1, H - 1 + p - h) - max(0, p - h) + 1 for h in range(H))
             cols = sum(min(f - 1, W - 1 + p - w) - max(0, p - w) + 1 for w in range(W))
             out[i] = 6 * batch * rows * cols * Dout * Din

@@ -1026,15 +1026,15 @@ int plan_gemm(Ctx *c, Plan &p, int M, int N, int K, int tA, int tB, int tC) {
 }
 
 // Output positions per image up to which a same convolution is tiled by
-// position (8 x 8 and smaller); PG_POSMAJOR=0 in the environment turns the
-// position-major tiles off (every implicit convolution then uses rectangles).
-constexpr int POSMAJOR_MAX_PIXELS = 64;
-static bool posmajor_enabled() {
-    static const bool on = [] {
+// position: 64 (8 x 8 and smaller) unless the environment variable
+// PG_POSMAJOR gives another limit; PG_POSMAJOR=0 turns the position-major
+// tiles off (every implicit convolution then uses rectangles).
+static int posmajor_max_pixels() {
+    static const int lim = [] {
         const char *e = getenv("PG_POSMAJOR");
-        return !(e && e[0] == '0');
+        return e && *e ? atoi(e) : 64;
     }();
-    return on;
+    return lim;
 }
 
 int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad) {
@@ -1063,8 +1063,7 @@ int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout
         // output position: a rectangle tile of a 4x4 or 2x2 image spends most
         // of its taps on the zero padding (5/9 of them at 2x2), which a tile
         // of one output position over 128 images skips.
-        p.posmajor = posmajor_enabled() && batch % BM == 0 && P == H && Q == W && 2 * pad + 1 == f &&
-                     P * Q <= POSMAJOR_MAX_PIXELS;
+        p.posmajor = batch % BM == 0 && P == H && Q == W && 2 * pad + 1 == f && P * Q <= posmajor_max_pixels();
     } else {
         // explicit: the image holds the im2col rows (K = f*f*Din padded to 16)
         p.implicit = 0;
