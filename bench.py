@@ -220,13 +220,13 @@ def ring_macs(layers, batch):
 def executed_ring_macs(layers, batch):
     """Ring multiply-adds the limb kernels execute per share-GEMM layer: the
     dense count, except for the convolutions the library tiles by output
-    position (stride 1, same padding, at most 64 output positions or the
+    position (stride 1, same padding, at most 1024 output positions or the
     PG_POSMAJOR limit, batch a
     multiple of 128, channels a multiple of 16), which run only the taps
     inside the input: (sum over output rows of the valid filter rows) x (the
     same over columns) taps instead of P * Q * f * f."""
     out = ring_macs(layers, batch)
-    limit = int(os.environ.get("PG_POSMAJOR") or 64)  # the library's position-major limit
+    limit = int(os.environ.get("PG_POSMAJOR") or 1024)  # the library's position-major limit
     for i, L in enumerate(layers):
         if L[0] != "cnn":
             continue

@@ -1026,13 +1026,15 @@ int plan_gemm(Ctx *c, Plan &p, int M, int N, int K, int tA, int tB, int tC) {
 }
 
 // Output positions per image up to which a same convolution is tiled by
-// position: 64 (8 x 8 and smaller) unless the environment variable
-// PG_POSMAJOR gives another limit; PG_POSMAJOR=0 turns the position-major
-// tiles off (every implicit convolution then uses rectangles).
+// position: 1024 (32 x 32 and smaller; measured on VGG16 at batch 128, the
+// 2x2 to 8x8 layers gain 16-58 %, 16x16 3-7 %, 32x32 1 %) unless the
+// environment variable PG_POSMAJOR gives another limit; PG_POSMAJOR=0 turns
+// the position-major tiles off (every implicit convolution then uses
+// rectangles).
 static int posmajor_max_pixels() {
     static const int lim = [] {
         const char *e = getenv("PG_POSMAJOR");
-        return e && *e ? atoi(e) : 64;
+        return e && *e ? atoi(e) : 1024;
     }();
     return lim;
 }

@@ -1,5 +1,5 @@
 """Position-major tiles of the limb convolution (same convolutions of at most
-64 output positions per image, batch a multiple of 128): a tile is one output
+1024 output positions per image, batch a multiple of 128): a tile is one output
 pixel of 128 images and runs only the taps that fall inside the input. Every
 share against the oracle, bit for bit, at the shapes of VGG16's small layers
 and at ragged ones (non-square images, 5x5 filters, output channels that are
