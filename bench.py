@@ -52,7 +52,6 @@ from piranha_gb300 import nets  # noqa: E402
 
 BATCH = 128
 SEED = 2024
-STREAM_BUCKETS = (1, 2, 4, 8, 12, 16, 24, 32, 40, 48, 56, 64)  # batch sizes of the stream's captured networks
 LIMB_FLOPS_PER_RING_MAC = 72  # 36 8-bit limb pairs x 2 flops: exact u64 MAC on fp16 tensor cores
 # DRAM bytes read + written by the 13 limb_tma_kernel launches of one VGG16
 # batch-128 forward, from one ncu capture of dram__bytes_read.sum +
@@ -91,8 +90,9 @@ WORKLOADS = {
     "stream": {"metric": "3PC batched request stream img/s", "kind": "stream", "fp": 26, "ring": "u64",
                "requests": 512, "max_batch": 64,
                "desc": "512 requests, batch uniform in 1..64, SecureML or VGG16 (even odds), 3PC RSS, uint64 "
-                       "shares, FP 26; each request runs on a captured network of the smallest batch bucket "
-                       "(1, 2, 4, 8, 12, 16, 24, ..., 64) that holds it"},
+                       "shares, FP 26; waiting requests of one model are packed (up to 128 images) into one "
+                       "replay of the captured network of the smallest batch bucket (1, 2, 4, 6, 8, 12, 16, 24, "
+                       "..., 64, 80, 96, 112, 128) that holds them"},
 }
 _LAYERS = {"vgg16": nets.vgg16, "secureml": nets.secureml, "lenet-train": nets.lenet,
            "vgg16-train": lambda: nets.vgg16(maxpool=False),
@@ -116,6 +116,7 @@ def parse():
     ap.add_argument("--sweep", action="store_true", help="gemm: also time M = N = K in 512..8192 in both forms")
     ap.add_argument("--no-autotune", action="store_true", help="split-K by the heuristic instead of by timing")
     ap.add_argument("--conv-shape", default="32,32,64,64,3,1,1", help="conv: H,W,Din,Dout,f,stride,pad")
+    ap.add_argument("--no-pack", action="store_true", help="stream: one request per replay")
     return ap.parse_args()
 
 
@@ -1099,101 +1100,79 @@ def bench_fcnet(args, pg, torch, stream, dev, wl, batch, world):
 
 
 def bench_stream(args, pg, torch, stream, dev, wl, world):
-    """The request stream, served in arrival order on one stream: per request
-    its shares go into the input buffers of the captured network of the
-    smallest batch bucket that holds it (1, 2, 4, 8, then steps of 8 up to 64
-    with 12 besides: at most 1/3 of a replay is padding; rows past the request's batch keep what an earlier
-    request left there; every layer works image by image, so they do not
-    touch the request's rows), the graph
-    replays, and the request's output rows come back. Latency is a request's
-    CUDA-event time from the start of its input copy to the end of its output
-    copy. The stream runs args.warmup times untimed, then once timed per pass:
-    a device-resident pass (inputs staged in HBM beforehand) and an end-to-end
-    pass (pinned host shares in and out), each request alone on the stream;
-    the end-to-end throughput comes from a third, pipelined pass in which the
-    next request's input copy overlaps the current forward."""
+    """The request stream, served in arrival order on one stream by
+    piranha_gb300.stream: waiting requests of the same model are packed into
+    one replay of the captured network of the smallest batch bucket that holds
+    them (the oldest waiting request opens a pack, the next 16 waiting
+    requests of its model join it while it stays within 128 images; --no-pack
+    serves each request alone). A pack's latency is its CUDA-event time from
+    the start of its input copies to the end of its output copies; every
+    request of a pack has that latency. The stream runs args.warmup times
+    untimed, then once timed per pass: a device-resident pass (inputs staged
+    in HBM beforehand) and an end-to-end pass (pinned host shares in and out),
+    each pack alone on the stream; the end-to-end throughput comes from a
+    third, pipelined pass in which the next pack's input copies overlap the
+    current forward."""
+    from piranha_gb300 import stream as st
+
     models, params, reqs = wl
     fp = WORKLOADS["stream"]["fp"]
     form = pg.FORM_U64 if args.form == "u64" else pg.FORM_LIMB_TC
     ctx = pg.Context(dev.index, stream=stream, form=form)
     ctx.set_autotune(not args.no_autotune)
-    nets_ = {}
-
-    def bucket(b):
-        return next(x for x in STREAM_BUCKETS if x >= b)
-
-    for m, b, _ in reqs:
-        key = (m, bucket(b))
-        if key in nets_:
-            continue
-        net = pg.Network(ctx, models[m], key[1], fp)
-        for i, prm in enumerate(params[m]):
-            if prm is not None:
-                net.set_params(i, pg.to_device(prm[0], dev), pg.to_device(prm[1], dev) if prm[1] is not None else None)
-        net.capture()
-        ptr_in = net.input_buffers()[0]
-        optrs, on = net.layer_output_ptrs(len(models[m]) - 1)
-        nets_[key] = (net, _as_device_block(torch, dev, ptr_in, 6 * net.in_n).view(6, net.in_n),
-                      _as_device_block(torch, dev, optrs[0], 6 * on).view(6, on))
-    for net, inb, _ in nets_.values():
-        inb.zero_()
+    server = st.StreamServer(pg, ctx, {m: (models[m], params[m]) for m in models}, fp, dev)
+    packs = st.plan_packs([(m, b) for m, b, _ in reqs], cap=128, lookahead=0 if args.no_pack else 16)
+    for p in packs:
+        server.network(p.model, p.bucket)
     stream.synchronize()
 
-    per_img_in = {m: nets.input_size(L) for m, L in models.items()}
     per_img_out = 10
     dev_in = [torch.from_numpy(np.ascontiguousarray(x).reshape(6, -1).view(np.int64)).to(dev) for _, _, x in reqs]
     host_in = [t.cpu().pin_memory() for t in dev_in]
+    dev_out = [torch.empty((6, b * per_img_out), dtype=torch.int64, device=dev) for _, b, _ in reqs]
     host_out = [torch.empty((6, b * per_img_out), dtype=torch.int64, pin_memory=True) for _, b, _ in reqs]
 
     def serve(resident):
-        lat = []
         evs = []
-        for r, (m, b, _) in enumerate(reqs):
-            net, inb, outb = nets_[(m, bucket(b))]
-            n_in = b * per_img_in[m]
+        for p in packs:
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            src = dev_in[r] if resident else host_in[r]
-            inb[:, :n_in].copy_(src, non_blocking=True)
-            net.forward_resident()
-            if not resident:
-                host_out[r].copy_(outb[:, :b * per_img_out], non_blocking=True)
+            server.serve(p, dev_in if resident else host_in, dev_out if resident else host_out)
             e1.record(stream)
-            evs.append((e0, e1))
+            evs.append((p, e0, e1))
         stream.synchronize()
-        for e0, e1 in evs:
-            lat.append(e0.elapsed_time(e1))
-        return lat
+        lat = []
+        for p, e0, e1 in evs:
+            lat += [e0.elapsed_time(e1)] * len(p.requests)
+        return lat, sum(e0.elapsed_time(e1) for _, e0, e1 in evs) / 1e3
 
     copy_stream = torch.cuda.Stream(device=dev)
+    staged = {}
 
     def serve_pipelined():
-        """End-to-end throughput with the next request's host-to-device copy
-        on a second stream, overlapping the current request's forward (one
-        request ahead at most); returns the seconds from the first copy to
-        the last output copy."""
+        """End-to-end throughput: the next pack's host-to-device copies run on a
+        second stream (into staging buffers) while the current pack computes;
+        returns the seconds from the first copy to the last output copy."""
         t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        copied = [torch.cuda.Event() for _ in reqs]
-        started = [torch.cuda.Event() for _ in reqs]
+        copied = [torch.cuda.Event() for _ in packs]
+        started = [torch.cuda.Event() for _ in packs]
         t0.record(copy_stream)
 
-        def h2d(r):
-            if r > 0:
-                copy_stream.wait_event(started[r - 1])
+        def h2d(k):
+            if k > 0:
+                copy_stream.wait_event(started[k - 1])
             with torch.cuda.stream(copy_stream):
-                dev_in[r].copy_(host_in[r], non_blocking=True)
-            copied[r].record(copy_stream)
+                for r in packs[k].requests:
+                    dev_in[r].copy_(host_in[r], non_blocking=True)
+            copied[k].record(copy_stream)
 
         h2d(0)
-        for r, (m, b, _) in enumerate(reqs):
-            net, inb, outb = nets_[(m, bucket(b))]
-            stream.wait_event(copied[r])
-            started[r].record(stream)
-            if r + 1 < len(reqs):
-                h2d(r + 1)
-            inb[:, :b * per_img_in[m]].copy_(dev_in[r], non_blocking=True)
-            net.forward_resident()
-            host_out[r].copy_(outb[:, :b * per_img_out], non_blocking=True)
+        for k, p in enumerate(packs):
+            stream.wait_event(copied[k])
+            started[k].record(stream)
+            if k + 1 < len(packs):
+                h2d(k + 1)
+            server.serve(p, dev_in, host_out)
         t1.record(stream)
         stream.synchronize()
         copy_stream.synchronize()
@@ -1205,39 +1184,39 @@ def bench_stream(args, pg, torch, stream, dev, wl, world):
     sampler = ClockSampler(dev.index)
     sampler.start()
     wall0 = time.perf_counter()
-    lat_res = serve(True)
+    lat_res, dev_s = serve(True)
     wall = time.perf_counter() - wall0
     clocks = sampler.stop()
     launches = ctx.kernel_launches() - launches0
-    lat_e2e = serve(False)
+    lat_e2e, _ = serve(False)
     serve_pipelined()
     e2e_s = serve_pipelined()
     imgs = sum(b for _, b, _ in reqs)
-    dev_s = sum(lat_res) / 1e3
     pct = lambda v, q: float(np.percentile(np.array(v), q))  # noqa: E731
     out = {
         "form": "limb_tc" if form == pg.FORM_LIMB_TC else "u64",
         "value": aggregate(world, imgs, 1, dev_s),
-        "ms_per_step": 1e3 * dev_s / len(reqs),
+        "ms_per_step": 1e3 * dev_s / len(packs),
         "wall_s": wall,
         "e2e": {"value": aggregate(world, imgs, 1, e2e_s), "unit": "img/s",
-                "h2d_bytes_per_step": int(sum(t.numel() * 8 for t in host_in) / len(reqs)),
-                "d2h_bytes_per_step": int(sum(t.numel() * 8 for t in host_out) / len(reqs))},
+                "h2d_bytes_per_step": int(sum(t.numel() * 8 for t in host_in) / len(packs)),
+                "d2h_bytes_per_step": int(sum(t.numel() * 8 for t in host_out) / len(packs))},
         "latency_ms": {"resident": {"p50": pct(lat_res, 50), "p99": pct(lat_res, 99), "max": max(lat_res)},
                        "e2e": {"p50": pct(lat_e2e, 50), "p99": pct(lat_e2e, 99), "max": max(lat_e2e)},
-                       "note": "per request, alone on the stream (input copy to output copy); the e2e "
-                               "throughput overlaps the next request's input copy with the current forward"},
-        "requests": len(reqs), "images": imgs,
+                       "note": "per request: its pack's time alone on the stream (input copies to output copies); "
+                               "the e2e throughput overlaps the next pack's input copies with the current forward"},
+        "requests": len(reqs), "images": imgs, "replays": len(packs),
+        "packing": "none (one request per replay)" if args.no_pack else
+                   "same-model requests within the next 16 waiting ones, up to 128 images per replay",
         "gpu_launches": int(launches),
         "clocks": clocks,
         "roofline": {"bound": "tensor", "achieved": None, "peak": None, "unit": "TFLOP/s", "frac": None,
                      "traffic": None, "kernel": "see the vgg16 and secureml workloads",
                      "work": "mixed request sizes; the per-model lines carry the kernel fractions"},
         "comm_per_party_per_step": None,
-        "networks": sorted(f"{m}@{b}" for m, b in nets_),
+        "networks": sorted(f"{m}@{b}" for m, b in server.nets),
     }
-    for net, _, _ in nets_.values():
-        net.close()
+    server.close()
     ctx.close()
     return out
 
@@ -1290,7 +1269,7 @@ def main():
     }
     if "layer_ms" in res:
         line["layer_ms"] = res["layer_ms"]
-    for k in ("latency_ms", "requests", "images", "networks", "sweep"):
+    for k in ("latency_ms", "requests", "images", "replays", "packing", "networks", "sweep"):
         if k in res:
             line[k] = res[k]
     if "compare_u64" in res:

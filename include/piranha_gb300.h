@@ -130,6 +130,16 @@ int pg_graph_begin(pg_ctx *ctx);
 int pg_graph_end(pg_ctx *ctx, pg_graph **out);
 int pg_graph_launch(pg_ctx *ctx, pg_graph *graph);
 int pg_graph_destroy(pg_graph *graph);
+/* Failure detection, no counterpart in the reference (whose socket errors
+ * print and whose error() exits, src/util/connect.h:44-55, util.cu:18-21).
+ * wait_ns bounds every device-side wait of the limb tensor-core kernels
+ * (default 2 s; 0 restores it): a wait that runs out makes the kernel set the
+ * device error word, stop issuing, wait (bounded) for its own copies and MMAs,
+ * free its tensor memory and return, and pg_device_errors then reports
+ * PG_ERR_TIMEOUT; the context stays usable. withhold_stage >= 0 is a
+ * diagnostic for testing that path: the limb GEMM's producer issues no copies
+ * for that K stage of each CTA, so its consumers' waits run out (-1 is off). */
+int pg_ctx_set_wait_limit(pg_ctx *ctx, uint64_t wait_ns, int withhold_stage);
 /* diagnostic: one 128x64x16 tcgen05 MMA of fp16 operands (A 128x16 and B
  * 64x16 row-major halves), D = A * B^T as 128x64 fp32 row-major */
 int pg_tc_selftest(pg_ctx *ctx, const uint16_t *A, const uint16_t *B, float *D);

@@ -117,6 +117,7 @@ def _declare(lib):
         "pg_tc_selftest": [vp, vp, vp, vp],
         "pg_tensor_rate": [vp, i, i, vp],
         "pg_device_op_u64": [vp, i, vp, sz, i, u64, vp],
+        "pg_ctx_set_wait_limit": [vp, u64, i],
         "pg_net_layer_times": [vp, vp],
         "pg_tpc_matmul_u64": [vp, _P2, _P2, _P2, i, i, i, i, i, i, i],
         "pg_tpc_matmul_u32": [vp, _P2, _P2, _P2, i, i, i, i, i, i, i],
@@ -326,6 +327,11 @@ class Context:
         CUDA graph; ``g.launch()`` replays it. Run the calls eagerly once
         first so that the context's scratch is sized."""
         return _Capture(self)
+
+    def set_wait_limit(self, wait_ns: int = 0, withhold_stage: int = -1):
+        """Bound on the limb kernels' device-side waits (0: the default 2 s) and
+        the diagnostic K stage whose copies the producer withholds (-1: none)."""
+        self._check(lib().pg_ctx_set_wait_limit(self._h, int(wait_ns), int(withhold_stage)))
 
     def tensor_rate(self, form: int, iters: int = 200000) -> dict:
         """Sustained rate of one tensor-core instruction form (RATE_TC_F16,

@@ -204,6 +204,13 @@ int pg_ctx_set_form(pg_ctx *c, int form) {
     return PG_OK;
 }
 int pg_ctx_get_form(pg_ctx *c) { return c ? c->form : -1; }
+int pg_ctx_set_wait_limit(pg_ctx *c, uint64_t wait_ns, int withhold_stage) {
+    CTX_OR_FAIL(c);
+    if (withhold_stage < -1) return set_error(c, PG_ERR_INVALID_ARG, "withhold stage %d", withhold_stage);
+    c->wait_ns = wait_ns ? wait_ns : 2000000000ull;
+    c->withhold_stage = withhold_stage;
+    return PG_OK;
+}
 int pg_ctx_set_autotune(pg_ctx *c, int on) {
     CTX_OR_FAIL(c);
     c->autotune = on ? 1 : 0;

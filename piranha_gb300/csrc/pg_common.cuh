@@ -53,6 +53,10 @@ struct Ctx {
     bool prg_on = false;
     uint32_t prg_rk[3][60];
     uint64_t prg_ctr = 0;
+    // bound on every device-side wait of the limb kernels, and the diagnostic
+    // stage whose copies the limb GEMM's producer withholds (-1: none)
+    uint64_t wait_ns = 2000000000ull;
+    int withhold_stage = -1;
 };
 
 int set_error(Ctx *c, int code, const char *fmt, ...);

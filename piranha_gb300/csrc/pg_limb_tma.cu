@@ -77,7 +77,7 @@ constexpr int NTHREADS = 352;
 constexpr int W_PROD = 0, W_MMA = 1, W_EPI0 = 2, W_MMA2 = 10;
 constexpr uint32_t TMEM_COLS = 512;  // 8 diagonals x 64 columns
 constexpr uint64_t DIGIT_OFFSET = 0x8080808080808080ull;
-constexpr uint64_t WAIT_NS = 2000000000ull;  // 2 s bound on any single wait
+constexpr uint64_t WAIT_NS = 2000000000ull;  // 2 s bound on any single wait (the context can set a shorter one)
 
 struct Args {
     int M, N;
@@ -99,6 +99,8 @@ struct Args {
     uint64_t d;
     int dshift;
     int *err;
+    uint64_t wait_ns;  // bound on every wait of the kernel
+    int withhold;      // diagnostic: K stage (of each CTA's range) whose copies the producer never issues; -1: none
 };
 
 struct __align__(16) Smem {
@@ -587,6 +589,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     tc::tc_fence_after();
     const Args &g = sm.args;
     const uint32_t tmem = sm.tmem_base;
+    const uint64_t wait_ns = g.wait_ns;
     // output-pixel rectangle of this tile
     const int tw = blockIdx.y % g.tiles_w, t2 = blockIdx.y / g.tiles_w;
     const int th = t2 % g.tiles_h, tn = t2 / g.tiles_h;
@@ -625,7 +628,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             for (int git = 0; git < nst; git++) {
                 const int s = git % STAGES;
                 const uint32_t ph = (uint32_t)(git / STAGES) & 1;
-                if (!tc::mbar_wait(tc::smem_u32(&sm.empty[s]), ph ^ 1, &sm.abort, WAIT_NS)) {
+                if (!tc::mbar_wait(tc::smem_u32(&sm.empty[s]), ph ^ 1, &sm.abort, wait_ns)) {
                     flag_error(sm, g, 0x100 + s);
                     ok = false;
                     break;
@@ -657,20 +660,21 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     y = g.rows_mode ? n0 >> 5 : h0 + r - g.pad;
                     zc = g.rows_mode ? 0 : n0;
                 }
+                issued = git + 1;
+                if (git == g.withhold) continue;  // diagnostic: this stage's data never arrives
                 const uint32_t bar = tc::smem_u32(&sm.full[s]);
                 tc::mbar_arrive_expect_tx(bar, 8 * g.a_box_bytes + B_STAGE_BYTES);
                 const uint32_t dst = tc::smem_u32(sm.stage[s]);
                 tma_load_5d(dst, &tmA, x, y, zc, 2 * cb, seg * 8, bar);
                 const uint8_t *src = g.packB + ((size_t)gst * g.ntiles_n + blockIdx.x) * B_STAGE_BYTES;
                 tc::bulk_g2s(dst + 8 * A_PLANE_BYTES, src, B_STAGE_BYTES, bar);
-                issued = git + 1;
             }
             if (!ok) {
                 // wait (bounded, not cut short by the abort flag) for the copies still in flight
                 const int from = issued - STAGES > 0 ? issued - STAGES : 0;
                 for (int git = from; git < issued; git++)
                     tc::mbar_wait(tc::smem_u32(&sm.full[git % STAGES]), (uint32_t)(git / STAGES) & 1, &sm.never,
-                                  WAIT_NS);
+                                  wait_ns);
             }
         }
         __syncwarp();
@@ -690,13 +694,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             int cend = gi == 0 ? (nst < LO_FIRST ? nst : LO_FIRST) : (nst < CHUNK_STAGES ? nst : CHUNK_STAGES);
             for (int t = 0; t < nst; t++) {
                 if (t == cstart && chunk > 0) {
-                    if (!tc::mbar_wait(tc::smem_u32(&sm.acc_empty[gi]), (uint32_t)(chunk - 1) & 1, &sm.abort, WAIT_NS)) {
+                    if (!tc::mbar_wait(tc::smem_u32(&sm.acc_empty[gi]), (uint32_t)(chunk - 1) & 1, &sm.abort, wait_ns)) {
                         flag_error(sm, g, 0x300 + gi);
                         break;
                     }
                     tc::tc_fence_after();
                 }
-                if (!tc::mbar_wait(tc::smem_u32(&sm.full[t % STAGES]), (uint32_t)(t / STAGES) & 1, &sm.abort, WAIT_NS)) {
+                if (!tc::mbar_wait(tc::smem_u32(&sm.full[t % STAGES]), (uint32_t)(t / STAGES) & 1, &sm.abort, wait_ns)) {
                     flag_error(sm, g, 0x310 + gi);
                     break;
                 }
@@ -713,7 +717,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 }
             }
             tc::mma_commit(tc::smem_u32(&sm.done));
-            if (!tc::mbar_wait(tc::smem_u32(&sm.done), 0, &sm.never, WAIT_NS) && g.err) atomicCAS(g.err, 0, 0x400);
+            if (!tc::mbar_wait(tc::smem_u32(&sm.done), 0, &sm.never, wait_ns) && g.err) atomicCAS(g.err, 0, 0x400);
         }
         __syncwarp();
     } else {
@@ -738,7 +742,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 if (sm.abort) break;
                 const uint64_t now = tc::globaltimer();
                 if (t_idle == 0) t_idle = now;
-                else if (now - t_idle > WAIT_NS) {
+                else if (now - t_idle > wait_ns) {
                     flag_error(sm, g, 0x500);
                     break;
                 }
@@ -1403,6 +1407,8 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
     g.d = 1ull << trunc;
     g.dshift = pow2_shift<uint64_t>(g.d);
     g.err = device_error_word(c);
+    g.wait_ns = c->wait_ns;
+    g.withhold = c->withhold_stage;
     if (split > 1 && !partial) return set_error(c, PG_ERR_INVALID_ARG, "split-K needs a partial buffer");
     // value shares by tensor-map stores: the network's convolutions (no bias,
     // zero shares kept, row-major output of an even width of at least one N tile)

@@ -9,7 +9,8 @@
   benchmark runs them.
 * The request stream's bucket path: a request of b images served on the
   captured network of a larger batch bucket, whose other rows hold an earlier
-  request's data, gives the oracle's result for its b images.
+  request's data, gives the oracle's result for its b images; and requests
+  packed into one replay (piranha_gb300.stream) each get their own result.
 * Share-GEMMs with truncation at 512^3, 4096^3, 8192^3 and non-cubic shapes:
   both forms agree on every share, and sampled rows equal the oracle's
   product of those rows.
@@ -166,3 +167,33 @@ def test_gemm_forms_agree_and_sampled_rows_equal_oracle(pg, M, N, K):
     want = orc.matmul(a_rows, pg.to_host(B), len(rows), N, K, 1, 1, 1, 26).reshape(3, 2, len(rows), N)
     got = pg.to_host(out[pg.FORM_LIMB_TC].view(3, 2, M, N)[:, :, rows, :].contiguous())
     assert np.array_equal(got, want)
+
+
+def test_stream_packed_replays_equal_oracle(pg):
+    """Requests of one model packed into one replay (StreamServer): each
+    request's output rows equal the oracle's result for that request alone."""
+    import torch
+
+    from piranha_gb300 import stream as st
+
+    models = {"secureml": netref.secureml_layers(), "vgg16": netref.vgg16_layers(maxpool=True)}
+    params = {m: seeded.kaiming_uniform(L, 91 if m == "vgg16" else 92) for m, L in models.items()}
+    n_in = {"secureml": 784, "vgg16": 3072}
+    reqs = [("secureml", 5), ("vgg16", 2), ("secureml", 17), ("secureml", 9), ("vgg16", 3), ("secureml", 64)]
+    packs = st.plan_packs(reqs, cap=128, lookahead=16)
+    assert [p.requests for p in packs] == [[0, 2, 3, 5], [1, 4]]
+    ctx = pg.Context(0, form=pg.FORM_LIMB_TC)
+    server = st.StreamServer(pg, ctx, {m: (models[m], params[m]) for m in models})
+    for rnd in range(2):
+        xs = [seeded.images(700 + 10 * rnd + r, b * n_in[m]) for r, (m, b) in enumerate(reqs)]
+        ins = [pg.to_device(x).reshape(6, -1) for x in xs]
+        outs = [torch.empty((6, b * 10), dtype=torch.int64, device="cuda") for _, b in reqs]
+        for p in packs:
+            server.serve(p, ins, outs)
+        ctx.sync()
+        for r, (m, b) in enumerate(reqs):
+            want = netref.forward(models[m], params[m], xs[r], b)
+            assert np.array_equal(pg.to_host(outs[r]).reshape(3, 2, -1), want), f"round {rnd} request {r}"
+    ctx.check_device_errors()
+    server.close()
+    ctx.close()
