@@ -82,7 +82,7 @@ class StreamServer:
         self.ctx = ctx
         self.models = models
         self.fp = fp
-        self.device = device
+        self.device = device if device is not None else "cuda"
         self.nets = {}
         self.n_in = {m: _input_size(L) for m, (L, _) in models.items()}
         self.n_out = {m: _output_size(L) for m, (L, _) in models.items()}
