@@ -1,9 +1,9 @@
 """Regenerate the golden fixtures in this directory from the Piranha sources.
 
-Run in a checkout that has the reference tree mounted (default path below, or
-pass it as the first argument):
+Run with the Piranha source tree as the first argument (or in the
+environment variable PIRANHA_SRC):
 
-    python tests/golden/make_golden.py [/path/to/piranha]
+    python tests/golden/make_golden.py /path/to/piranha
 
 It reads Piranha's own known-answer tests as text (src/test/GPU.cu,
 src/test/Func.cu, src/test/Layer.cu) and its layer fixtures (files/test/*),
@@ -31,7 +31,7 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PIRANHA_SRC", "")
 
 _SAFE = re.compile(r"^[0-9a-fA-FxX\s\.\+\-\*/<>\(\)e]+$")
 
@@ -79,6 +79,8 @@ def _arrays(body: str, env: dict | None = None) -> dict:
 
 
 def main():
+    if not REF or not os.path.isdir(os.path.join(REF, "src", "test")):
+        sys.exit("usage: make_golden.py /path/to/piranha (or set PIRANHA_SRC)")
     gpu = open(os.path.join(REF, "src/test/GPU.cu")).read()
     func = open(os.path.join(REF, "src/test/Func.cu")).read()
     layer = open(os.path.join(REF, "src/test/Layer.cu")).read()
