@@ -218,21 +218,18 @@ def ring_macs(layers, batch):
     return out
 
 
-def executed_ring_macs(layers, batch):
+def executed_ring_macs(layers, batch, posmajor):
     """Ring multiply-adds the limb kernels execute per share-GEMM layer: the
-    dense count, except for the convolutions the library tiles by output
-    position (stride 1, same padding, at most 1024 output positions or the
-    PG_POSMAJOR limit, batch a
-    multiple of 128, channels a multiple of 16), which run only the taps
-    inside the input: (sum over output rows of the valid filter rows) x (the
-    same over columns) taps instead of P * Q * f * f."""
+    dense count, except for the convolutions the network runs with
+    position-major tiles (posmajor[i], from pg_net_layer_plan), which run only
+    the taps inside the input: (sum over output rows of the valid filter
+    rows) x (the same over columns) taps instead of P * Q * f * f."""
     out = ring_macs(layers, batch)
-    limit = int(os.environ.get("PG_POSMAJOR") or 1024)  # the library's position-major limit
     for i, L in enumerate(layers):
         if L[0] != "cnn":
             continue
         H, W, Din, Dout, f, s, p = L[1:]
-        if s == 1 and 2 * p + 1 == f and H * W <= limit and batch % 128 == 0 and Din % 16 == 0:
+        if posmajor[i]:
             rows = sum(min(f - 1, H - 1 + p - h) - max(0, p - h) + 1 for h in range(H))
             cols = sum(min(f - 1, W - 1 + p - w) - max(0, p - w) + 1 for w in range(W))
             out[i] = 6 * batch * rows * cols * Dout * Din
@@ -718,7 +715,8 @@ def bench_form(args, pg, torch, stream, dev, form, wl, batch, world):
     gemm_ms = float(sum(layer_ms[i] for i in gemm_idx)) / args.steps
     gemm_macs = sum(macs[i] for i in gemm_idx)
     achieved = gemm_macs * LIMB_FLOPS_PER_RING_MAC / (gemm_ms / 1e3) / 1e12
-    exe = executed_ring_macs(layers, batch) if form == pg.FORM_LIMB_TC else macs
+    plans = [net.layer_plan(i) for i in range(len(layers))]
+    exe = executed_ring_macs(layers, batch, [p["form"] == 1 and p["posmajor"] for p in plans])
     exe_macs = sum(exe[i] for i in gemm_idx)
     executed = exe_macs * LIMB_FLOPS_PER_RING_MAC / (gemm_ms / 1e3) / 1e12
     peaks = load_peaks()
@@ -759,6 +757,8 @@ def bench_form(args, pg, torch, stream, dev, form, wl, batch, world):
         "comm_per_party_per_step": {"tx_bytes": int((comm1["tx"][0] - comm0["tx"][0]) // args.steps),
                                     "rounds": int((comm1["rounds"] - comm0["rounds"]) // args.steps)},
         "layer_ms": [round(float(v) / args.steps, 4) for v in layer_ms],
+        "layer_plans": ["" if p["form"] == 0 else "u64" if p["form"] == 2 else
+                        ("pos" if p["posmajor"] else "rect") + f"/split{p['split']}" for p in plans],
     }
     net.close()
     ctx.close()
@@ -1269,6 +1269,8 @@ def main():
     }
     if "layer_ms" in res:
         line["layer_ms"] = res["layer_ms"]
+    if "layer_plans" in res:
+        line["layer_plans"] = res["layer_plans"]
     for k in ("latency_ms", "requests", "images", "replays", "packing", "networks", "sweep"):
         if k in res:
             line[k] = res[k]

@@ -469,6 +469,11 @@ int pg_net_enable_timing(pg_net *net, int on);
 int pg_net_layer_times(pg_net *net, float *ms);
 /* device pointers (owned by the network) of layer i's output shares */
 int pg_net_layer_output(pg_net *net, int layer, uint64_t *const out[6], size_t *n);
+/* how FC / CNN layer i runs (no counterpart in the reference): out[0] = 1
+ * limb tensor-core form, 2 plain u64 form; out[1] = 1 if its tiles are
+ * position-major; out[2] = split-K; out[3] = tiles per split. Valid after the
+ * first forward (which sets the network up); zeros for other layers. */
+int pg_net_layer_plan(pg_net *net, int layer, int out[4]);
 
 /* Training: one SGD iteration (src/main.cu:314-330) = forward, then
  * NeuralNetwork::backward (NeuralNetwork.cu:136-148): the revealed softmax

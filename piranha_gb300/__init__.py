@@ -118,6 +118,7 @@ def _declare(lib):
         "pg_tensor_rate": [vp, i, i, vp],
         "pg_device_op_u64": [vp, i, vp, sz, i, u64, vp],
         "pg_ctx_set_wait_limit": [vp, u64, i],
+        "pg_net_layer_plan": [vp, i, vp],
         "pg_net_layer_times": [vp, vp],
         "pg_tpc_matmul_u64": [vp, _P2, _P2, _P2, i, i, i, i, i, i, i],
         "pg_tpc_matmul_u32": [vp, _P2, _P2, _P2, i, i, i, i, i, i, i],
@@ -950,6 +951,13 @@ class Network:
         n = ctypes.c_size_t()
         self.ctx._check(lib().pg_net_layer_output(self._h, layer, arr, ctypes.byref(n)))
         return [int(x) for x in arr], int(n.value)
+
+    def layer_plan(self, layer: int) -> dict:
+        """How FC / CNN layer `layer` runs (after the first forward): form
+        (1 limb, 2 u64, 0 other layers), position-major tiles, split-K, tiles."""
+        arr = (ctypes.c_int * 4)()
+        self.ctx._check(lib().pg_net_layer_plan(self._h, layer, arr))
+        return {"form": arr[0], "posmajor": arr[1], "split": arr[2], "tiles": arr[3]}
 
     # ---------------------------------------------------------- training
     # One SGD iteration = forward + NeuralNetwork::backward (NeuralNetwork.cu:136-148).

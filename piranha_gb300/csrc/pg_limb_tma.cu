@@ -1043,7 +1043,8 @@ static int posmajor_max_pixels() {
     return lim;
 }
 
-int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad) {
+int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad,
+              bool posmajor_ok) {
     memset(&p, 0, sizeof(p));
     if (batch <= 0 || H <= 0 || W <= 0 || f <= 0 || Din <= 0 || Dout <= 0 || stride <= 0 || pad < 0 ||
         H + 2 * pad < f || W + 2 * pad < f)
@@ -1069,7 +1070,8 @@ int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout
         // output position: a rectangle tile of a 4x4 or 2x2 image spends most
         // of its taps on the zero padding (5/9 of them at 2x2), which a tile
         // of one output position over 128 images skips.
-        p.posmajor = batch % BM == 0 && P == H && Q == W && 2 * pad + 1 == f && P * Q <= posmajor_max_pixels();
+        p.posmajor = posmajor_ok && batch % BM == 0 && P == H && Q == W && 2 * pad + 1 == f &&
+                     P * Q <= posmajor_max_pixels();
     } else {
         // explicit: the image holds the im2col rows (K = f*f*Din padded to 16)
         p.implicit = 0;

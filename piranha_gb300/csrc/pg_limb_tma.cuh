@@ -36,7 +36,9 @@ struct Plan {
 
 int prepare_device(Ctx *c, bool again = false);  // once per device (again: repeat it), with it current (no allocation)
 int plan_gemm(Ctx *c, Plan &p, int M, int N, int K, int tA, int tB, int tC);
-int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad);
+// posmajor_ok = false: rectangle tiles even where position-major ones apply
+int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad,
+              bool posmajor_ok = true);
 // the weight gradient of that convolution as a GEMM over the output pixels
 int plan_wgrad(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad);
 void choose_split(const Plan &p, int sms, int &split, int &chunks_per_split);

@@ -50,6 +50,8 @@ struct NetLayer {
     uint64_t *delta[6];  // backward: the gradient this layer passes to the previous one (in_n)
     // limb tensor-core form (FC and CNN layers): plan, split-K, packed weights
     lt::Plan plan;
+    lt::Plan alt;      // a position-major convolution's rectangle-tile plan, timed against it at set-up
+    bool has_alt = false;
     int split, cps;
     uint8_t *packB;
     int u64 = 0;  // the plain u64 form timed faster for this layer at set-up (small layers)
@@ -99,6 +101,66 @@ struct pg_net {
     uint64_t launches_per_train = 0;
 };
 
+// The tile shape of a convolution that position-major tiles apply to: the
+// position-major plan (one output pixel of 128 images per tile, only the
+// taps inside the input) and the rectangle plan (128 pixels of one or more
+// images per tile, every tap), each with its own tuned split-K, timed on the
+// zero image into the layer's outputs (one warm-up, three timed runs each);
+// the rectangle plan is kept only if it wins by 3 %. The choice is cached
+// with the split-K choices (1 = rectangle, 2 = position-major). The next
+// layer's fused ReLU writes the image in the chosen plan's layout. Without
+// autotuning the position-major plan stays.
+static int net_choose_tiles(pg_net *net, NetLayer &L, const uint64_t *const *bias) {
+    Ctx *c = net->ctx;
+    const std::string key = "tile/" + lt::plan_key(L.alt);
+    int choice = 2;
+    auto it = c->split_cache.find(key);
+    if (it != c->split_cache.end()) {
+        choice = it->second.first;
+    } else if (c->autotune) {
+        int split[2] = {L.split, 0}, cps[2] = {L.cps, 0};
+        int st = lt::tune_split(c, L.alt, net->limb_image, L.packB, net->limb_partial, L.out, bias, net->fp,
+                                bias == nullptr, nullptr, split[1], cps[1]);
+        if (st) return st;
+        cudaEvent_t e0, e1;
+        PG_CHECK_CUDA(c, cudaEventCreate(&e0));
+        if (cudaEventCreate(&e1) != cudaSuccess) {
+            cudaEventDestroy(e0);
+            return set_error(c, PG_ERR_CUDA, "cudaEventCreate failed");
+        }
+        float ms[2] = {0.f, 0.f};
+        for (int v = 0; v < 2 && !st; v++) {
+            const lt::Plan &p = v ? L.alt : L.plan;
+            for (int r = 0; r < 4 && !st; r++) {
+                if (r == 1 && cudaEventRecord(e0, c->stream) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
+                if (!st)
+                    st = lt::run_gemm(c, p, net->limb_image, L.packB, split[v] > 1 ? net->limb_partial : nullptr,
+                                      split[v], cps[v], L.out, bias, net->fp, bias == nullptr);
+            }
+            if (!st && cudaEventRecord(e1, c->stream) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
+            if (!st && cudaEventSynchronize(e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
+            if (!st && cudaEventElapsedTime(&ms[v], e0, e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (st) return st;
+        choice = ms[1] < 0.97f * ms[0] ? 1 : 2;
+        c->split_cache[key] = {choice, 1};
+    }
+    if (choice == 1) {
+        L.plan = L.alt;
+        int sp, cp;
+        if (lt::cached_split(c, L.plan, sp, cp)) {
+            L.split = sp;
+            L.cps = cp;
+        } else {
+            lt::choose_split(L.plan, c->sm_count > 0 ? c->sm_count : 148, L.split, L.cps);
+        }
+    }
+    L.has_alt = false;
+    return PG_OK;
+}
+
 // Plans, buffer sizes and weight packing of the limb form.
 static int net_limb_setup(pg_net *net) {
     Ctx *c = net->ctx;
@@ -108,13 +170,25 @@ static int net_limb_setup(pg_net *net) {
     for (auto &L : net->layers) {
         int st = PG_OK;
         if (L.type == PG_LAYER_FC) st = lt::plan_gemm(c, L.plan, net->batch, L.p[1], L.p[0], 1, 1, 1);
-        else if (L.type == PG_LAYER_CNN)
+        else if (L.type == PG_LAYER_CNN) {
             st = lt::plan_conv(c, L.plan, net->batch, L.p[0], L.p[1], L.p[4], L.p[2], L.p[3], L.p[5], L.p[6]);
-        else continue;
+            L.has_alt = false;
+            if (!st && L.plan.posmajor) {
+                st = lt::plan_conv(c, L.alt, net->batch, L.p[0], L.p[1], L.p[4], L.p[2], L.p[3], L.p[5], L.p[6],
+                                   false);
+                L.has_alt = st == PG_OK;
+            }
+        } else continue;
         if (st) return st;
         lt::choose_split(L.plan, sms, L.split, L.cps);
         image = image > L.plan.image_bytes ? image : L.plan.image_bytes;
-        const size_t pb = lt::tune_partial_bytes(L.plan, sms);
+        size_t pb = lt::tune_partial_bytes(L.plan, sms);
+        if (L.has_alt) {
+            // the same packed weights and image size; its own split-K candidates
+            image = image > L.alt.image_bytes ? image : L.alt.image_bytes;
+            const size_t pa = lt::tune_partial_bytes(L.alt, sms);
+            pb = pb > pa ? pb : pa;
+        }
         partial = partial > pb ? partial : pb;
         packs += al(L.plan.packB_bytes);
     }
@@ -146,6 +220,7 @@ static int net_limb_setup(pg_net *net) {
         int st = lt::tune_split(c, L.plan, net->limb_image, L.packB, net->limb_partial, L.out, bias, net->fp,
                                 bias == nullptr, nullptr, L.split, L.cps);
         if (st) return st;
+        if (L.has_alt && (st = net_choose_tiles(net, L, bias))) return st;
     }
     return PG_OK;
 }
@@ -894,6 +969,21 @@ int pg_net_layer_output(pg_net *net, int layer, uint64_t *const out[6], size_t *
     if (out)
         for (int k = 0; k < 6; k++) ((uint64_t **)out)[k] = L.out[k];
     if (n) *n = L.out_n;
+    return PG_OK;
+}
+
+int pg_net_layer_plan(pg_net *net, int layer, int out[4]) {
+    if (!net || !out || layer < 0 || layer >= (int)net->layers.size()) return PG_ERR_INVALID_ARG;
+    NetLayer &L = net->layers[layer];
+    for (int k = 0; k < 4; k++) out[k] = 0;
+    if ((L.type == PG_LAYER_FC || L.type == PG_LAYER_CNN) && net->limb_arena) {
+        out[0] = L.u64 ? 2 : 1;
+        out[1] = L.plan.posmajor;
+        out[2] = L.split;
+        out[3] = L.plan.tiles_m * L.plan.ntiles_n;
+    } else if (L.type == PG_LAYER_FC || L.type == PG_LAYER_CNN) {
+        out[0] = 2;
+    }
     return PG_OK;
 }
 
