@@ -88,6 +88,8 @@ struct Args {
     int ntiles_n, total_stages, chunks_per_split;
     int direct, colmajor;
     int posmajor;  // tiles by output position (Plan::posmajor); H, W: input extents then
+    int wgt;       // implicit weight gradient (Plan::wgt): a tile is 128 input channels of one filter tap
+    int cdim, nb16;  // wgt: input channels, images / 16
     int zeros_kept;  // the four zero output shares already hold 0: write only value / bias shares
     int tma_out;     // the two value shares go out as tensor-map stores of the staged tile (see tma_store_4d)
     uint32_t a_box_bytes;  // bytes of one digit plane of a stage (16 * 2 * Wt * Ht * Nt)
@@ -151,7 +153,7 @@ __device__ __forceinline__ void digits8(const uint64_t (&v)[8], uint4 (&pl)[NPL]
 
 // ------------------------------------------------------------ image kernel
 
-enum { SRC_ROWS = 0, SRC_COLS = 1, SRC_IM2COL = 2, SRC_WGRAD = 3 };
+enum { SRC_ROWS = 0, SRC_COLS = 1, SRC_IM2COL = 2, SRC_WGRAD = 3, SRC_WGRAD_T = 4 };
 
 struct ImageArgs {
     const uint64_t *a[6];
@@ -259,6 +261,41 @@ __global__ void image_kernel(const __grid_constant__ ImageArgs ia) {
     }
 }
 
+// The digit image of the implicit weight gradient: the forward input X
+// (NHWC, batch x HW pixels x C channels) as img[seg][plane][pixel][n / 8][c][n % 8],
+// so that 8 consecutive images of one channel are one 16-byte core row and a
+// filter tap is a shift of the pixel coordinate. One thread per (segment,
+// pixel, 8-image block, channel): consecutive threads take consecutive
+// channels (coalesced reads of each image's row, coalesced 16-byte writes).
+struct WgtImageArgs {
+    const uint64_t *a[6];
+    long long hw, nb8, cdim;  // cdim: image channels (>= the input's, zero past it)
+    int din;                  // the input's channels
+    uint4 *img;
+};
+
+__global__ void wgt_image_kernel(const __grid_constant__ WgtImageArgs ia) {
+    const long long per_seg = ia.hw * ia.nb8 * ia.cdim;
+    const long long total = 6 * per_seg;
+    for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < total;
+         u += (long long)gridDim.x * blockDim.x) {
+        const long long c = u % ia.cdim;
+        long long t = u / ia.cdim;
+        const long long nb = t % ia.nb8;
+        t /= ia.nb8;
+        const long long pix = t % ia.hw;
+        const int seg = (int)(t / ia.hw);
+        const uint64_t *a = ia.a[seg];
+        uint64_t v[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) v[i] = c < ia.din ? __ldg(a + ((nb * 8 + i) * ia.hw + pix) * ia.din + c) : 0;
+        uint4 pl[8];
+        digits8<8>(v, pl);
+#pragma unroll
+        for (int i = 0; i < 8; i++) ia.img[(long long)(seg * 8 + i) * per_seg + (pix * ia.nb8 + nb) * ia.cdim + c] = pl[i];
+    }
+}
+
 // ReLU fused with the digit image of the convolution it feeds: a block of
 // 256 threads takes 16 pixels x 16 channels (one 128-byte line of each
 // share per pixel). Each thread runs the ReLU of one value (dReLU +
@@ -343,6 +380,8 @@ struct PackArgs {
     const uint64_t *b[6];
     int N, Kreal, kblocks, ntiles_n;
     int kn;  // 1: b[k * N + n]; 0: b[n * Kreal + k]
+    long long wg_pq;  // > 0: K index k = pixel * wg_batch + image of b = dY[image][pixel][n] (wg_pq pixels)
+    int wg_batch;
     uint8_t *packB;
 };
 
@@ -381,7 +420,8 @@ __global__ void pack_kernel(const __grid_constant__ PackArgs pa) {
             for (int i = 0; i < 8; i++) {
                 const int k = k0 + i;
                 if (k < pa.Kreal) {
-                    const long long idx = pa.kn ? (long long)k * pa.N + n : (long long)n * pa.Kreal + k;
+                    long long idx = pa.kn ? (long long)k * pa.N + n : (long long)n * pa.Kreal + k;
+                    if (pa.wg_pq) idx = ((long long)(k % pa.wg_batch) * pa.wg_pq + k / pa.wg_batch) * pa.N + n;
                     v[i] = __ldg(b0 + idx) + (b1 ? __ldg(b1 + idx) : 0);
                 }
             }
@@ -599,7 +639,19 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // the filter. Their K' range (6 segments x taps x channel blocks) is split
     // evenly over the grid's z slices.
     int r_lo = 0, s_lo = 0, ns = 1, tile_stages = g.total_stages;
-    if (g.posmajor) {
+    if (g.wgt) {
+        // Weight gradient of filter tap (r, s) = blockIdx.y / tiles_w for input
+        // channels tw * 128 ...: K runs over the output pixels (p, q) whose
+        // input pixel (p + r - pad, q + s - pad) is inside the image (rows
+        // r_lo..., columns s_lo..s_lo+ns-1) and 16 images per stage.
+        const int tap = t2, r = tap / g.f, sx = tap - r * g.f;
+        r_lo = g.pad - r > 0 ? g.pad - r : 0;
+        const int p_hi = g.Himg - 1 + g.pad - r < g.P - 1 ? g.Himg - 1 + g.pad - r : g.P - 1;
+        s_lo = g.pad - sx > 0 ? g.pad - sx : 0;
+        const int q_hi = g.Wimg - 1 + g.pad - sx < g.Q - 1 ? g.Wimg - 1 + g.pad - sx : g.Q - 1;
+        ns = q_hi - s_lo + 1;
+        tile_stages = (p_hi >= r_lo && ns > 0) ? 6 * (p_hi - r_lo + 1) * ns * g.nb16 : 0;
+    } else if (g.posmajor) {
         r_lo = g.pad - h0 > 0 ? g.pad - h0 : 0;
         const int r_hi = g.Himg - 1 + g.pad - h0 < g.f - 1 ? g.Himg - 1 + g.pad - h0 : g.f - 1;
         s_lo = g.pad - w0 > 0 ? g.pad - w0 : 0;
@@ -608,7 +660,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         tile_stages = 6 * (r_hi - r_lo + 1) * ns * g.cblocks;
     }
     int stage_begin, stage_end;
-    if (g.posmajor) {
+    if (g.posmajor || g.wgt) {
         const int per = (tile_stages + (int)gridDim.z - 1) / (int)gridDim.z;
         stage_begin = z * per;
         stage_end = stage_begin + per;
@@ -634,8 +686,23 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     break;
                 }
                 int gst = stage_begin + git;
-                int seg, tap, cb, x, y, zc;
-                if (g.posmajor) {
+                int seg, tap, cb, x, y, zc, c3;
+                if (g.wgt) {
+                    // (segment, valid output pixel, 16-image block) -> the packed dY stage
+                    const int per_seg = tile_stages / 6;
+                    seg = gst / per_seg;
+                    const int rem = gst - seg * per_seg;
+                    const int pi = rem / g.nb16, nb = rem - pi * g.nb16;
+                    const int pp = r_lo + pi / ns, qq = s_lo + pi % ns;
+                    const int r = t2 / g.f, sx = t2 - r * g.f;
+                    gst = seg * g.kblocks + (pp * g.Q + qq) * g.nb16 + nb;
+                    // box: 8 images x 128 channels x 2 image blocks at input pixel (h, w), 8 planes
+                    x = 0;
+                    y = tw * BM;
+                    zc = 2 * nb;
+                    c3 = (pp + r - g.pad) * g.Wimg + (qq + sx - g.pad);
+                    tap = cb = 0;
+                } else if (g.posmajor) {
                     // compacted K' index (segment, inside tap, channel block) -> the packed stage
                     const int per_seg = tile_stages / 6;
                     seg = gst / per_seg;
@@ -649,6 +716,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     x = 0;
                     y = (int)((((long long)(h0 + r - g.pad) * g.Wimg + (w0 + sx - g.pad)) * g.Nimg + n0) >> 5);
                     zc = 0;
+                    c3 = 2 * cb;
                 } else {
                     seg = gst / g.kblocks;
                     const int kb = gst - seg * g.kblocks;
@@ -659,13 +727,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     x = g.rows_mode ? 0 : 8 * (w0 + sx - g.pad);
                     y = g.rows_mode ? n0 >> 5 : h0 + r - g.pad;
                     zc = g.rows_mode ? 0 : n0;
+                    c3 = 2 * cb;
                 }
+                (void)tap;
                 issued = git + 1;
                 if (git == g.withhold) continue;  // diagnostic: this stage's data never arrives
                 const uint32_t bar = tc::smem_u32(&sm.full[s]);
                 tc::mbar_arrive_expect_tx(bar, 8 * g.a_box_bytes + B_STAGE_BYTES);
                 const uint32_t dst = tc::smem_u32(sm.stage[s]);
-                tma_load_5d(dst, &tmA, x, y, zc, 2 * cb, seg * 8, bar);
+                tma_load_5d(dst, &tmA, x, y, zc, c3, seg * 8, bar);
                 const uint8_t *src = g.packB + ((size_t)gst * g.ntiles_n + blockIdx.x) * B_STAGE_BYTES;
                 tc::bulk_g2s(dst + 8 * A_PLANE_BYTES, src, B_STAGE_BYTES, bar);
             }
@@ -761,7 +831,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
         // output row of this thread's accumulator lane (-1: padding or past the image)
         long long m = -1;
-        if (row < g.R) {
+        if (g.wgt) {
+            // row = input channel tw * 128 + row of filter tap t2: output row (r, s, c)
+            const int ch = tw * BM + row;
+            if (ch < g.cdim) m = (long long)t2 * g.cdim + ch;
+        } else if (row < g.R) {
             const int wh = g.Wt * g.Ht;
             const int nn = row / wh, rem = row - nn * wh;
             const int hh = rem / g.Wt, ww = rem - hh * g.Wt;
@@ -1029,6 +1103,16 @@ int plan_gemm(Ctx *c, Plan &p, int M, int N, int K, int tA, int tB, int tC) {
     return PG_OK;
 }
 
+// The implicit weight gradient (Plan::wgt) is used wherever it applies
+// (stride 1, a multiple of 16 images) unless PG_WGT=0 in the environment.
+static bool wgt_enabled() {
+    static const bool on = [] {
+        const char *e = getenv("PG_WGT");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 // Output positions per image up to which a same convolution is tiled by
 // position: 1024 (32 x 32 and smaller; measured on VGG16 at batch 128, the
 // 2x2 to 8x8 layers gain 16-58 %, 16x16 3-7 %, 32x32 1 %) unless the
@@ -1096,6 +1180,37 @@ int plan_wgrad(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dou
     const int P = (H + 2 * pad - f) / stride + 1, Q = (W + 2 * pad - f) / stride + 1;
     const long long K = (long long)batch * P * Q;
     if (K > (1ll << 30)) return set_error(c, PG_ERR_UNSUPPORTED, "weight gradient over %lld output pixels", K);
+    if (stride == 1 && batch % 16 == 0 && wgt_enabled()) {
+        // implicit: rows (tap, c) from one image of the forward input, taps as
+        // shifts of its pixel coordinate, K = valid output pixels x images
+        p.wgt = 1;
+        p.implicit = 0;
+        p.M = f * f * Din;
+        p.N = Dout;
+        p.Kreal = (int)K;
+        p.C = (int)K;  // K' per segment (a multiple of 16)
+        p.src_mode = SRC_WGRAD_T;
+        p.tB_kn = 1;
+        p.colmajor = 1;
+        p.H = H; p.W = W; p.Din = Din; p.stride = 1;
+        p.f = f; p.pad = pad; p.P = P; p.Q = Q;
+        p.Himg = H; p.Wimg = W; p.Nimg = batch;
+        p.kblocks = (int)(K / BK);
+        p.cblocks = 0;
+        p.ntiles_n = (Dout + BN - 1) / BN;
+        p.pixels = (long long)H * W * batch;
+        p.pixels_alloc = p.pixels;
+        // image channels: Din, or Din rounded up to 8 below one 128-row tile, so
+        // that the tensor-map box (min(128, that) rows) stays inside the tensor
+        p.C8 = Din >= BM ? Din : (Din + 7) / 8 * 8;
+        p.image_bytes = 96ull * (size_t)p.pixels * (size_t)p.C8;
+        p.packB_bytes = (size_t)6 * p.kblocks * p.ntiles_n * B_STAGE_BYTES;
+        p.Wt = 1; p.Ht = 1; p.Nt = BM; p.R = p.C8 < BM ? p.C8 : BM;
+        p.tiles_w = (Din + BM - 1) / BM;
+        p.tiles_h = f * f;
+        p.tiles_m = p.tiles_w * p.tiles_h;
+        return PG_OK;
+    }
     // rows (r, s, c) of the filter, K = output pixels (n, p, q): the image is the
     // transposed im2col gather of the forward input, the packed operand the
     // output gradient dY[pixel][Dout], the output dW[Dout][r][s][c] column-major
@@ -1182,7 +1297,8 @@ bool cached_split(Ctx *c, const Plan &p, int &split, int &cps) {
 static std::string tune_key(const Plan &p) {
     char k[256];
     snprintf(k, sizeof(k), "%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d%s", p.implicit, p.src_mode, p.M, p.N, p.C,
-             p.kblocks, p.ntiles_n, p.tiles_m, p.Wt, p.Ht, p.Nt, p.f, p.colmajor, p.posmajor ? "/pos" : "");
+             p.kblocks, p.ntiles_n, p.tiles_m, p.Wt, p.Ht, p.Nt, p.f, p.colmajor,
+             p.posmajor ? "/pos" : p.wgt ? "/wgt" : "");
     return k;
 }
 
@@ -1292,6 +1408,26 @@ int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n,
 }
 
 int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image) {
+    if (p.wgt) {
+        WgtImageArgs wa;
+        memset(&wa, 0, sizeof(wa));
+        for (int i = 0; i < 6; i++) {
+            if (!a[i]) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+            wa.a[i] = a[i];
+        }
+        wa.hw = (long long)p.Himg * p.Wimg;
+        wa.nb8 = p.Nimg / 8;
+        wa.cdim = p.C8;  // the image's channels
+        wa.din = p.Din;
+        wa.img = (uint4 *)image;
+        const long long units = 6 * wa.hw * wa.nb8 * wa.cdim;
+        const int sms = c->sm_count > 0 ? c->sm_count : 148;
+        long long blocks = (units + 255) / 256;
+        if (blocks > (long long)sms * 32) blocks = (long long)sms * 32;
+        wgt_image_kernel<<<(unsigned)blocks, 256, 0, c->stream>>>(wa);
+        c->launches++;
+        return launch_status(c, "wgt_image_kernel");
+    }
     ImageArgs ia;
     memset(&ia, 0, sizeof(ia));
     bool vec = p.src_mode == SRC_ROWS && p.ld % 2 == 0;
@@ -1334,6 +1470,8 @@ int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB) {
     pa.kblocks = p.kblocks;
     pa.ntiles_n = p.ntiles_n;
     pa.kn = p.tB_kn;
+    pa.wg_pq = p.wgt ? (long long)p.P * p.Q : 0;
+    pa.wg_batch = p.Nimg;
     pa.packB = (uint8_t *)packB;
     const long long units = 6ll * p.ntiles_n * BN * p.kblocks * 2;
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
@@ -1364,7 +1502,13 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
     cuuint32_t box[5];
     const cuuint64_t plane_stride = (cuuint64_t)p.pixels_alloc * 16;  // bytes between channel groups
     const cuuint64_t C8 = (cuuint64_t)(p.C / 8);
-    if (p.implicit && !p.posmajor) {
+    if (p.wgt) {
+        // [seg*8 + plane][pixel][n / 8][c][n % 8]: 8 images, 128 channels, 2 image blocks, one pixel, 8 planes
+        const cuuint64_t nb8 = (cuuint64_t)p.Nimg / 8, cd = (cuuint64_t)p.C8, hw = (cuuint64_t)p.Himg * p.Wimg;
+        dims[0] = 8; dims[1] = cd; dims[2] = nb8; dims[3] = hw; dims[4] = 48;
+        strides[0] = 16; strides[1] = cd * 16; strides[2] = nb8 * cd * 16; strides[3] = hw * nb8 * cd * 16;
+        box[0] = 8; box[1] = (cuuint32_t)p.R; box[2] = 2; box[3] = 1; box[4] = 8;
+    } else if (p.implicit && !p.posmajor) {
         dims[0] = 8 * (cuuint64_t)p.Wimg; dims[1] = p.Himg; dims[2] = p.Nimg;
         strides[0] = (cuuint64_t)p.Wimg * 16; strides[1] = (cuuint64_t)p.Himg * p.Wimg * 16; strides[2] = plane_stride;
         box[0] = 8 * p.Wt; box[1] = p.Ht; box[2] = p.Nt;
@@ -1375,9 +1519,11 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
     }
     // dims 3 and 4: the channel group of 8 (two per K block) and the (segment, digit plane) index;
     // one box covers the eight planes of a segment
-    dims[3] = C8; dims[4] = 48;
-    strides[3] = C8 * plane_stride;
-    box[3] = 2; box[4] = 8;
+    if (!p.wgt) {
+        dims[3] = C8; dims[4] = 48;
+        strides[3] = C8 * plane_stride;
+        box[3] = 2; box[4] = 8;
+    }
     const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
     CUresult r = enc(&tm, CU_TENSOR_MAP_DATA_TYPE_UINT16, 5, const_cast<void *>(image), dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -1390,6 +1536,9 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
     g.Wt = p.Wt; g.Ht = p.Ht; g.Nt = p.Nt; g.R = p.R; g.tiles_w = p.tiles_w; g.tiles_h = p.tiles_h;
     g.rows_mode = !p.implicit;
     g.posmajor = p.posmajor;
+    g.wgt = p.wgt;
+    g.cdim = p.Din;
+    g.nb16 = p.Nimg / 16;
     g.P = p.P; g.Q = p.Q; g.Nimg = p.Nimg;
     g.Himg = p.Himg; g.Wimg = p.Wimg;
     g.ntiles_n = p.ntiles_n;

@@ -31,6 +31,10 @@ struct Plan {
     int posmajor;       // implicit convolution tiled by output position: a tile is one output pixel (p, q) of
                         // 128 images, the image is stored batch-innermost (pixel (h * W + w) * Nimg + n), and
                         // the tile runs only the taps that fall inside the input (no zero-padding taps)
+    int C8;             // wgt: image channels (Din, or Din rounded up to 8 when below 128)
+    int wgt;            // implicit weight gradient: rows (tap, c), K = output pixels x images (16 per stage);
+                        // the image is the forward input as [seg][plane][h * W + w][n / 8][c][n % 8], a tile
+                        // is 128 channels of one tap and runs only the output pixels whose tap lands inside
     size_t image_bytes, packB_bytes;
 };
 
