@@ -50,6 +50,8 @@
 #include <cuda_fp16.h>
 
 #include <cstdlib>
+#include <functional>
+#include <vector>
 #include <cstring>
 #include <mutex>
 
@@ -1172,7 +1174,10 @@ int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout
     return PG_OK;
 }
 
-int plan_wgrad(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad) {
+bool wgrad_implicit_applies(int batch, int stride) { return stride == 1 && batch % 16 == 0 && wgt_enabled(); }
+
+int plan_wgrad(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad,
+               bool implicit_ok) {
     memset(&p, 0, sizeof(p));
     if (batch <= 0 || H <= 0 || W <= 0 || f <= 0 || Din <= 0 || Dout <= 0 || stride <= 0 || pad < 0 ||
         H + 2 * pad < f || W + 2 * pad < f)
@@ -1180,7 +1185,7 @@ int plan_wgrad(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dou
     const int P = (H + 2 * pad - f) / stride + 1, Q = (W + 2 * pad - f) / stride + 1;
     const long long K = (long long)batch * P * Q;
     if (K > (1ll << 30)) return set_error(c, PG_ERR_UNSUPPORTED, "weight gradient over %lld output pixels", K);
-    if (stride == 1 && batch % 16 == 0 && wgt_enabled()) {
+    if (implicit_ok && wgrad_implicit_applies(batch, stride)) {
         // implicit: rows (tap, c) from one image of the forward input, taps as
         // shifts of its pixel coordinate, K = valid output pixels x images
         p.wgt = 1;
@@ -1644,7 +1649,7 @@ static int limb3_rss_matmul_impl(Ctx *c, const uint64_t *const a[6], const uint6
 
 static int limb3_rss_conv_impl(Ctx *c, const uint64_t *const A[6], const uint64_t *const B[6], uint64_t *const C[6],
                                int op, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad,
-                               int trunc) {
+                               int trunc, bool wgrad_implicit) {
     CSh6<uint64_t> ca, cb;
     Sh6<uint64_t> co;
     if (!load6(ca, A) || !load6(cb, B) || !load6(co, C)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
@@ -1661,7 +1666,7 @@ static int limb3_rss_conv_impl(Ctx *c, const uint64_t *const A[6], const uint64_
         // dY, B the forward input; the GEMM takes the forward input as its row
         // operand (the sum over the three parties of x_p0 (y_p0 + y_p1) + x_p1
         // y_p0 does not change when x and y trade places)
-        if ((st = lt::plan_wgrad(c, p, batch, H, W, f, Din, Dout, stride, pad))) return st;
+        if ((st = lt::plan_wgrad(c, p, batch, H, W, f, Din, Dout, stride, pad, wgrad_implicit))) return st;
         return run_with_scratch(c, p, B, A, C, nullptr, trunc);
     }
     // dX = col2im(dY x W): the per-tap products of every output pixel as one
@@ -1720,17 +1725,21 @@ int rss_conv(Ctx *, const T *const *, const T *const *, T *const *, int, int, in
 
 // The form of a standalone share-GEMM / convolution in the limb context: the
 // context's cached choice for the shape, else (autotuning on, no capture in
-// progress) the faster of the limb and the plain u64 form, timed on the
-// call's own operands (one warm-up and three runs each; both give the same
-// bits; counters restored), else the limb form. Small or narrow problems (a
-// weight gradient with 25 x 20 outputs, say) can run faster on the CUDA
-// cores. Cached as 1 (limb) or 2 (u64).
-template <typename FL, typename FU> static int run_picked(Ctx *c, const std::string &key, FL limb, FU u64) {
-    int choice = 1;
+// progress) the fastest of the candidates, timed on the call's own operands
+// (one warm-up and three runs each; all give the same bits; counters
+// restored), else the first candidate. Candidates: the limb form, the plain
+// u64 form, and for a weight gradient the limb form with the explicit
+// transposed-im2col image besides the implicit one. Small or narrow problems
+// (a weight gradient with 25 x 20 outputs, say) can run faster on the CUDA
+// cores, and the implicit weight gradient fills only Din of a tile's 128 rows.
+// Cached as 1 + the candidate's index.
+static int run_picked(Ctx *c, const std::string &key, const std::vector<std::function<int()>> &cand) {
+    int choice = 0;
     auto it = c->split_cache.find(key);
     if (it != c->split_cache.end()) {
-        choice = it->second.first;
-    } else if (c->autotune) {
+        choice = it->second.first - 1;
+        if (choice < 0 || choice >= (int)cand.size()) choice = 0;
+    } else if (c->autotune && cand.size() > 1) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         PG_CHECK_CUDA(c, cudaStreamIsCapturing(c->stream, &cs));
         if (cs == cudaStreamCaptureStatusNone) {
@@ -1743,12 +1752,12 @@ template <typename FL, typename FU> static int run_picked(Ctx *c, const std::str
                 cudaEventDestroy(e0);
                 return set_error(c, PG_ERR_CUDA, "cudaEventCreate failed");
             }
-            float ms[2] = {0.f, 0.f};
+            std::vector<float> ms(cand.size(), 0.f);
             int st = PG_OK;
-            for (int f = 0; f < 2 && !st; f++) {
+            for (size_t f = 0; f < cand.size() && !st; f++) {
                 for (int r = 0; r < 4 && !st; r++) {
                     if (r == 1 && cudaEventRecord(e0, c->stream) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
-                    if (!st) st = f ? u64() : limb();
+                    if (!st) st = cand[f]();
                 }
                 if (!st && cudaEventRecord(e1, c->stream) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
                 if (!st && cudaEventSynchronize(e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event");
@@ -1759,29 +1768,39 @@ template <typename FL, typename FU> static int run_picked(Ctx *c, const std::str
             memcpy(c->comm, comm0, sizeof(comm0));
             c->launches.store(launches0);
             if (st) return st;
-            choice = ms[1] < 0.97f * ms[0] ? 2 : 1;
-            c->split_cache[key] = {choice, 1};
+            // another candidate must beat the first by 3 %
+            float best = ms[0];
+            for (size_t f = 1; f < cand.size(); f++)
+                if (ms[f] < 0.97f * ms[0] && ms[f] < best) {
+                    best = ms[f];
+                    choice = (int)f;
+                }
+            c->split_cache[key] = {choice + 1, 1};
         }
     }
-    return choice == 2 ? u64() : limb();
+    return cand[choice]();
 }
 
 int limb3_rss_matmul_u64(Ctx *c, const uint64_t *const a[6], const uint64_t *const b[6], uint64_t *const out[6],
                          const uint64_t *const bias[6], int M, int N, int K, int tA, int tB, int tC, int trunc) {
     const std::string key = "sform/mm/" + std::to_string(M) + "/" + std::to_string(N) + "/" + std::to_string(K) +
                             "/" + std::to_string(tA) + std::to_string(tB) + std::to_string(tC) + (bias ? "b" : "");
-    return run_picked(
-        c, key, [&] { return limb3_rss_matmul_impl(c, a, b, out, bias, M, N, K, tA, tB, tC, trunc); },
-        [&] { return rss_matmul<uint64_t>(c, a, b, out, bias, M, N, K, tA, tB, tC, trunc); });
+    return run_picked(c, key,
+                      {[&] { return limb3_rss_matmul_impl(c, a, b, out, bias, M, N, K, tA, tB, tC, trunc); },
+                       [&] { return rss_matmul<uint64_t>(c, a, b, out, bias, M, N, K, tA, tB, tC, trunc); }});
 }
 
 int limb3_rss_conv_u64(Ctx *c, const uint64_t *const A[6], const uint64_t *const B[6], uint64_t *const C[6], int op,
                        int batch, int H, int W, int f, int Din, int Dout, int stride, int pad, int trunc) {
     char k[160];
     snprintf(k, sizeof(k), "sform/conv/%d/%d/%d/%d/%d/%d/%d/%d/%d", op, batch, H, W, f, Din, Dout, stride, pad);
-    return run_picked(
-        c, k, [&] { return limb3_rss_conv_impl(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc); },
-        [&] { return rss_conv<uint64_t>(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc); });
+    std::vector<std::function<int()>> cand = {
+        [&] { return limb3_rss_conv_impl(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc, true); },
+        [&] { return rss_conv<uint64_t>(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc); }};
+    if (op == PG_CONV_WGRAD && lt::wgrad_implicit_applies(batch, stride))
+        cand.push_back(
+            [&] { return limb3_rss_conv_impl(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc, false); });
+    return run_picked(c, k, cand);
 }
 
 int limb_prepare_current_device(Ctx *c, bool again) { return lt::prepare_device(c, again); }

@@ -44,7 +44,11 @@ int plan_gemm(Ctx *c, Plan &p, int M, int N, int K, int tA, int tB, int tC);
 int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad,
               bool posmajor_ok = true);
 // the weight gradient of that convolution as a GEMM over the output pixels
-int plan_wgrad(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad);
+// implicit_ok = false: the explicit transposed-im2col image even where the implicit form applies
+int plan_wgrad(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad,
+               bool implicit_ok = true);
+// whether the implicit weight gradient applies (stride 1, a multiple of 16 images)
+bool wgrad_implicit_applies(int batch, int stride);
 void choose_split(const Plan &p, int sms, int &split, int &chunks_per_split);
 size_t partial_bytes(const Plan &p, int split);
 // the split-K autotuner: partial bytes that every candidate fits in, and the
