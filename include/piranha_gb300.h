@@ -505,6 +505,71 @@ int pg_net_train_host(pg_net *net, const uint64_t *in_host, const uint64_t *labe
 int pg_net_layer_delta(pg_net *net, int layer, uint64_t *out[6], size_t *n);
 int pg_net_layer_params(pg_net *net, int layer, uint64_t *w[6], uint64_t *b[6], size_t *w_n, size_t *b_n);
 
+/* ----------------------------------------------------- party mode (TCP)
+ * One party per process, parties on separate hosts (or processes), messages
+ * over TCP exactly as the reference sends them: per ordered pair of parties
+ * three connections (NUMCONNECTIONS, src/util/basicSockets.h:35), the
+ * receiving party listening on base_port + sender * num_parties + receiver
+ * (initializeCommunication, src/util/connect.cu:109-123, base 32000 there),
+ * set up in the reference's serial order (initializeCommunicationSerial,
+ * :64-80), TCP_NODELAY, and every message the raw bytes of the vector on the
+ * first connection, with no header (sendVector / receiveVector,
+ * src/util/connect.h:41-55). A reference party process can be a peer.
+ * Unlike the reference, which prints and carries on (or waits forever),
+ * every call returns a status: a peer that does not connect, a receive that
+ * stays short of its length (PG_ERR_TIMEOUT after timeout_ms), a peer that
+ * closes its connection (PG_ERR_COMM). */
+#define PG_ERR_COMM 7          /* a party message was lost, cut short or duplicated */
+typedef struct pg_party pg_party;
+int pg_party_create(pg_party **out, int party, int num_parties, const char *const *hosts, int base_port,
+                    int timeout_ms);
+int pg_party_destroy(pg_party *p);
+/* the last error's text; pg_party_last_error(NULL) gives that of this
+ * thread's last failed pg_party_create */
+const char *pg_party_last_error(pg_party *p);
+/* sendVector / receiveVector of bytes of host memory */
+int pg_party_send(pg_party *p, int to, const void *data, size_t bytes);
+int pg_party_recv(pg_party *p, int from, void *data, size_t bytes);
+/* DeviceData::transmit + receive + join (src/gpu/DeviceData.h:87-129): bytes
+ * of device memory sent to `to` while bytes_in are received from `from` (a
+ * sending thread beside the receiving one, as the reference overlaps them),
+ * through pinned host staging, ordered on ctx's stream; to or from may be -1 */
+int pg_party_exchange(pg_party *p, pg_ctx *ctx, int to, const void *dev_out, size_t bytes_out, int from,
+                      void *dev_in, size_t bytes_in);
+/* the party's counters, with the reference's accounting (comm_profiler bytes
+ * per transmit / receive, one round per protocol step): out[0..n-1] bytes
+ * sent to each party, out[n..2n-1] bytes received from each, out[2n] rounds */
+int pg_party_counters(pg_party *p, uint64_t *out);
+/* End-of-step check (no counterpart in the reference): every pair of
+ * parties swaps its byte counters on the second connection and compares
+ * them, and no data may be left unread on the first; PG_ERR_COMM names the
+ * peer and the numbers when a message was lost, duplicated or cut short. */
+int pg_party_check(pg_party *p);
+/* Host-side fault injection for testing the detection: the nth send from now
+ * (n >= 1) is dropped (counted, not written), duplicated (written twice) or
+ * truncated (half written); PG_FAULT_NONE clears it. */
+#define PG_FAULT_NONE 0
+#define PG_FAULT_DROP 1
+#define PG_FAULT_DUPLICATE 2
+#define PG_FAULT_TRUNCATE 3
+int pg_party_inject(pg_party *p, int kind, int nth);
+/* RSS protocol steps of this party alone, on its two device share buffers
+ * sh[0] = shareA, sh[1] = shareB (RSS.h:74-75), with the reference's messages
+ * and accounting:
+ *  - reconstruct (RSS.inl:457-479): shareA to the next party, the previous
+ *    party's shareA received, out = shareA + shareB + received;
+ *  - reshare (RSS.inl:1052-1074): out[0] = c sent to the previous party,
+ *    out[1] received from the next;
+ *  - matmul (RSS.inl:481-540): localMatMul (three gpu::gemm, :1096-1110),
+ *    dividePublic3out3 (:1076-1094: r' = 2^trunc taken off at party A,
+ *    reconstruct3out3 :1019-1050 with the next and the previous party, the
+ *    division through double, r = 1 and the quotient added at party A's
+ *    shareA and party C's shareB). */
+int pg_party_rss_reconstruct_u64(pg_party *p, pg_ctx *ctx, const uint64_t *const sh[2], size_t n, uint64_t *out);
+int pg_party_rss_reshare_u64(pg_party *p, pg_ctx *ctx, const uint64_t *c, size_t n, uint64_t *const out[2]);
+int pg_party_rss_matmul_u64(pg_party *p, pg_ctx *ctx, const uint64_t *const a[2], const uint64_t *const b[2],
+                            uint64_t *const c[2], int M, int N, int K, int tA, int tB, int tC, int trunc);
+
 #ifdef __cplusplus
 }
 #endif

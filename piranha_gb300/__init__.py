@@ -119,6 +119,17 @@ def _declare(lib):
         "pg_device_op_u64": [vp, i, vp, sz, i, u64, vp],
         "pg_ctx_set_wait_limit": [vp, u64, i],
         "pg_net_layer_plan": [vp, i, vp],
+        "pg_party_create": [ctypes.POINTER(vp), i, i, vp, i, i],
+        "pg_party_destroy": [vp],
+        "pg_party_send": [vp, i, vp, sz],
+        "pg_party_recv": [vp, i, vp, sz],
+        "pg_party_exchange": [vp, vp, i, vp, sz, i, vp, sz],
+        "pg_party_counters": [vp, vp],
+        "pg_party_check": [vp],
+        "pg_party_inject": [vp, i, i],
+        "pg_party_rss_reconstruct_u64": [vp, vp, vp, sz, vp],
+        "pg_party_rss_reshare_u64": [vp, vp, vp, sz, vp],
+        "pg_party_rss_matmul_u64": [vp, vp, vp, vp, vp, i, i, i, i, i, i, i],
         "pg_net_layer_times": [vp, vp],
         "pg_tpc_matmul_u64": [vp, _P2, _P2, _P2, i, i, i, i, i, i, i],
         "pg_tpc_matmul_u32": [vp, _P2, _P2, _P2, i, i, i, i, i, i, i],
@@ -164,6 +175,8 @@ def _declare(lib):
         fn.restype = ctypes.c_int
     lib.pg_last_error.argtypes = [vp]
     lib.pg_last_error.restype = ctypes.c_char_p
+    lib.pg_party_last_error.argtypes = [vp]
+    lib.pg_party_last_error.restype = ctypes.c_char_p
     lib.pg_kernel_launches.argtypes = [vp]
     lib.pg_kernel_launches.restype = ctypes.c_uint64
     lib.pg_reference_init_normal.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_size_t, ctypes.c_int,
