@@ -25,7 +25,8 @@ Other workloads (--workload), each printing the same JSON line for its own metri
   secureml-4pc  4PC SecureML inference, batch 128, uint32 shares, FP 10
   stream        512 requests of batch 1..64, SecureML or VGG16, served in order; p50/p99 latency
   gemm          3PC share-GEMM M = N = K = 4096 with truncation by 2^26 (the matmul's dividePublic3out3
-                and reshare), uniform random uint64 shares; --sweep adds M = N = K in 512..8192
+                and reshare), uniform random uint64 shares; --sweep adds M = N = K in 512..8192 and five
+                non-cubic (M, N, K) in that range
 
 With --impl reference the line times Piranha's own arithmetic restated on the
 CPU (the oracle; the reference's GPU build cannot be compiled here) on a
@@ -113,7 +114,7 @@ def parse():
                     help="--impl reference: bound on the timed CPU steps' total time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-u64-form comparison run")
-    ap.add_argument("--sweep", action="store_true", help="gemm: also time M = N = K in 512..8192 in both forms")
+    ap.add_argument("--sweep", action="store_true", help="gemm: also time M = N = K in 512..8192 and five non-cubic shapes in both forms")
     ap.add_argument("--no-autotune", action="store_true", help="split-K by the heuristic instead of by timing")
     ap.add_argument("--conv-shape", default="32,32,64,64,3,1,1", help="conv: H,W,Din,Dout,f,stride,pad")
     ap.add_argument("--no-pack", action="store_true", help="stream: one request per replay")
@@ -951,14 +952,17 @@ def bench_gemm(args, pg, torch, stream, dev, wl, world):
                               "limb_over_u64": out["value"] / world / uv}
     if args.sweep:
         sweep = []
-        for n in (512, 1024, 2048, 4096, 8192):
-            As = torch.randint(-2**63, 2**63 - 1, (3, 2, n * n), dtype=torch.int64, device=dev)
-            Bs = torch.randint(-2**63, 2**63 - 1, (3, 2, n * n), dtype=torch.int64, device=dev)
-            row = {"M": n, "N": n, "K": n}
+        shapes = [(n, n, n) for n in (512, 1024, 2048, 4096, 8192)] + [
+            (1024, 8192, 2048), (8192, 512, 4096), (2048, 2048, 8192), (8192, 8192, 512), (512, 4096, 8192)]
+        for sM, sN, sK in shapes:
+            As = torch.randint(-2**63, 2**63 - 1, (3, 2, sM * sK), dtype=torch.int64, device=dev)
+            Bs = torch.randint(-2**63, 2**63 - 1, (3, 2, sK * sN), dtype=torch.int64, device=dev)
+            row = {"M": sM, "N": sN, "K": sK}
+            work = 6 * sM * sN * sK
             for name, fm in (("limb_tc", pg.FORM_LIMB_TC), ("u64", pg.FORM_U64)):
-                st = 3 if n <= 4096 or name == "limb_tc" else 2
-                rr = _gemm_form(args, pg, torch, stream, dev, fm, As, Bs, n, n, n, 1, st, 1)
-                row[name] = 6 * n ** 3 * st / rr["dev_s"]
+                st = 3 if work <= 6 * 4096 ** 3 or name == "limb_tc" else 2
+                rr = _gemm_form(args, pg, torch, stream, dev, fm, As, Bs, sM, sN, sK, 1, st, 1)
+                row[name] = work * st / rr["dev_s"]
             row["limb_over_u64"] = row["limb_tc"] / row["u64"]
             row["limb_tflops_equiv"] = LIMB_FLOPS_PER_RING_MAC * row["limb_tc"] / 1e12
             sweep.append(row)
