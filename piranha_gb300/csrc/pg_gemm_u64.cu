@@ -62,7 +62,7 @@ template <typename T> struct GemmArgs {
     int steps_per_split;
 };
 
-constexpr int BK = 16, NT = 256;
+constexpr int BK = 8, NT = 256;
 constexpr int APAD = 2, BPAD = 2;
 
 // CTA tile shapes: BM x BN outputs, TM x TN per thread, (BM/TM) x (BN/TN) = NT
@@ -179,7 +179,7 @@ template <typename T> __device__ __forceinline__ void apply_epilogue(const GemmA
 }
 
 template <typename T, int KIND, class TL>
-__global__ void __launch_bounds__(NT) ring_gemm_kernel(const GemmArgs<T> g) {
+__global__ void __launch_bounds__(NT, 2) ring_gemm_kernel(const GemmArgs<T> g) {
     constexpr int BM = TL::BM, BN = TL::BN, TM = TL::TM, TN = TL::TN;
     constexpr int NA = (BM * BK + NT - 1) / NT, NB = (BN * BK + NT - 1) / NT;  // loads per thread
     __shared__ T As[2][BK][BM + APAD];
@@ -334,15 +334,15 @@ template <typename T> static int launch_gemm(Ctx *c, GemmArgs<T> &g, int kind) {
     dim3 grid((g.N + bn - 1) / bn, (g.M + bm - 1) / bm);
     if (grid.y > 65535) return set_error(c, PG_ERR_UNSUPPORTED, "ring gemm: M=%d too large", g.M);
     // Split K when the output tiles cannot fill the GPU (small M x N, long K:
-    // weight gradients, narrow layers): about two CTAs per SM, at least four
-    // k-steps each.
+    // weight gradients, narrow layers): about four CTAs per SM (two resident),
+    // at least four k-steps each.
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
     const long long tiles = (long long)grid.x * grid.y;
     const int all_steps = ((g.K + BK - 1) / BK) * g.nseg;
     g.partial = nullptr;
     g.steps_per_split = 0;
     if (tiles < sms && all_steps >= 8) {
-        long long split = (2LL * sms + tiles - 1) / tiles;
+        long long split = (4LL * sms + tiles - 1) / tiles;
         if (split > all_steps / 4) split = all_steps / 4;
         if (split > 65535) split = 65535;
         if (split >= 2) {
