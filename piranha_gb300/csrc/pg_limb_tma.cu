@@ -33,11 +33,12 @@
 // src/mpc/RSS.inl:1097-1110; localFprop :614-639); the epilogue truncates
 // Z = sum_p z_p with dividePublic3out3 (:1077-1094).
 //
-// Roles (352 threads): warp 0 issues the TMA and bulk copies of each stage,
+// Roles (384 threads): warp 0 issues the TMA and bulk copies of each stage,
 // warp 1 owns tensor memory and one lane issues the MMAs of diagonals 0-3,
-// one lane of warp 10 issues those of diagonals 4-7, warps 2-9 drain the
-// accumulators (two warps per 32-lane quarter, 32 columns each) and run the
-// epilogue. Each output tile makes one pass over K' with all eight digit
+// one lane of warp 2 issues those of diagonals 4-7, warp 3 is spare, warps
+// 4-11 drain the accumulators (two warps per 32-lane quarter, 32 columns
+// each) and run the epilogue; warpgroup 0 hands most of its registers to
+// them (setmaxnreg). Each output tile makes one pass over K' with all eight digit
 // diagonals in tensor memory (8 x 64 columns) in two groups, diagonals 0-3
 // and 4-7, whose drains into 64-bit registers are staggered: while the
 // epilogue drains one group, the other group's MMA warp runs ahead over the
@@ -75,8 +76,23 @@ constexpr int A_PLANE_BYTES = BM * BK * 2;                      // 4096
 constexpr int B_PLANE_BYTES = BN * BK * 2;                      // 2048
 constexpr int B_STAGE_BYTES = 8 * B_PLANE_BYTES;                // 16384
 constexpr int STAGE_BYTES = 8 * A_PLANE_BYTES + B_STAGE_BYTES;  // 49152
-constexpr int NTHREADS = 352;
-constexpr int W_PROD = 0, W_MMA = 1, W_EPI0 = 2, W_MMA2 = 10;
+// Warp roles: warpgroup 0 = the copy producer, the two MMA issuers and one
+// spare warp; warpgroups 1-2 = the eight drain / epilogue warps (warp w reads
+// tensor-memory lanes 32 * (w % 4), so each lane quarter has two of them).
+constexpr int NTHREADS = 384;
+constexpr int W_PROD = 0, W_MMA = 1, W_MMA2 = 2, W_EPI0 = 4;
+// Register split (setmaxnreg): the block is launched at REGS_LAUNCH per thread
+// (the most that 3 warps on each SM sub-partition allow); warpgroup 0 gives
+// registers back down to REGS_CTRL and the epilogue warpgroups take them up to
+// REGS_EPI, enough to hold a group's four accumulators (4 x 32 values) beside
+// the 32 running 64-bit sums, so that tensor memory is handed back to the
+// MMA warp before any of them is converted. The split must add up to the
+// launch's registers, or the increase would wait forever; the host checks the
+// kernel's register count against REGS_LAUNCH before the first launch.
+constexpr int REGS_LAUNCH = 168, REGS_CTRL = 56, REGS_EPI = 224;
+static_assert(4 * 32 * REGS_CTRL + 8 * 32 * REGS_EPI <= NTHREADS * REGS_LAUNCH, "register split over the launch");
+static_assert(3 * REGS_LAUNCH * 32 <= 16384 && REGS_CTRL + 2 * REGS_EPI <= 512,
+              "three warps per sub-partition at launch; one control and two epilogue warps after the split");
 constexpr uint32_t TMEM_COLS = 512;  // 8 diagonals x 64 columns
 constexpr uint64_t DIGIT_OFFSET = 0x8080808080808080ull;
 constexpr uint64_t WAIT_NS = 2000000000ull;  // 2 s bound on any single wait (the context can set a shorter one)
@@ -502,29 +518,29 @@ __device__ __forceinline__ void fold_hi(int a, const uint32_t (&r)[32], uint64_t
 #pragma unroll
     for (int j = 0; j < 32; j++) acc[j] += (uint64_t)((uint32_t)f2i(r[j]) << (8 * (a - 4))) << 32;
 }
-// A drain in two parts: drain_head loads the group's four accumulators
-// through two register buffers and folds the first two; the caller then hands
-// tensor memory back (the arrival on acc_empty) and drain_tail folds the last
-// two from registers, so the MMA warp of the group waits only for the loads
-// and two folds. tcgen05.wait::ld waits for all of a thread's loads, so each
-// buffer is refilled only after its fold.
-template <bool HI> __device__ __forceinline__ void drain_head(uint32_t taddr, uint64_t (&acc)[32], uint32_t (&r0)[32],
-                                                             uint32_t (&r1)[32]) {
+// The whole drain of a group with the four accumulators in registers: load,
+// wait, hand tensor memory back to the group's MMA warp, then fold all four.
+template <bool HI> __device__ __forceinline__ void drain4(uint32_t taddr, uint64_t (&acc)[32], uint32_t bar_empty) {
     constexpr int a0 = HI ? 4 : 0;
+    uint32_t r0[32], r1[32], r2[32], r3[32];
     tc::tmem_ld32(taddr + (uint32_t)(a0 * BN), r0);
     tc::tmem_ld32(taddr + (uint32_t)((a0 + 1) * BN), r1);
+    tc::tmem_ld32(taddr + (uint32_t)((a0 + 2) * BN), r2);
+    tc::tmem_ld32(taddr + (uint32_t)((a0 + 3) * BN), r3);
     tc::tmem_wait_ld();
-    if (HI) fold_hi(a0, r0, acc); else fold_lo(a0, r0, acc);
-    tc::tmem_ld32(taddr + (uint32_t)((a0 + 2) * BN), r0);
-    if (HI) fold_hi(a0 + 1, r1, acc); else fold_lo(a0 + 1, r1, acc);
-    tc::tmem_ld32(taddr + (uint32_t)((a0 + 3) * BN), r1);
-    tc::tmem_wait_ld();
-}
-template <bool HI> __device__ __forceinline__ void drain_tail(uint64_t (&acc)[32], const uint32_t (&r0)[32],
-                                                             const uint32_t (&r1)[32]) {
-    constexpr int a0 = HI ? 4 : 0;
-    if (HI) fold_hi(a0 + 2, r0, acc); else fold_lo(a0 + 2, r0, acc);
-    if (HI) fold_hi(a0 + 3, r1, acc); else fold_lo(a0 + 3, r1, acc);
+    tc::tc_fence_before();
+    tc::mbar_arrive(bar_empty);
+    if (HI) {
+        fold_hi(a0, r0, acc);
+        fold_hi(a0 + 1, r1, acc);
+        fold_hi(a0 + 2, r2, acc);
+        fold_hi(a0 + 3, r3, acc);
+    } else {
+        fold_lo(a0, r0, acc);
+        fold_lo(a0 + 1, r1, acc);
+        fold_lo(a0 + 2, r2, acc);
+        fold_lo(a0 + 3, r3, acc);
+    }
 }
 
 // number of low-group chunks of a K' range of nst stages
@@ -543,7 +559,7 @@ constexpr int STG_PITCH = BN + 1;  // u64 per staged row: two-way bank conflicts
 static_assert(BM * STG_PITCH * 8 + BM * 8 <= STAGES * STAGE_BYTES, "the staged tile must fit in the stage ring");
 static_assert(BM * STG_PITCH * 8 + BM * 8 <= 2 * STAGE_BYTES && BM * BN * 8 <= 2 * STAGE_BYTES,
               "the pitched tile fits in stages 0-1 and the dense one in stages 2-3");
-static_assert(NTHREADS - W_EPI0 * 32 - 32 == 256, "eight epilogue warps");
+static_assert(NTHREADS - W_EPI0 * 32 == 256, "eight epilogue warps");
 
 __device__ __forceinline__ void named_bar_epilogue() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
 
@@ -673,6 +689,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     if (stage_end > tile_stages) stage_end = tile_stages;
     const int nst = stage_end > stage_begin ? stage_end - stage_begin : 0;
 
+    if (warp < W_EPI0) {
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(REGS_CTRL));
     if (warp == W_PROD) {
         // ------------------------------------------------ TMA + bulk copies
         if (lane == 0) {
@@ -792,7 +810,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             if (!tc::mbar_wait(tc::smem_u32(&sm.done), 0, &sm.never, wait_ns) && g.err) atomicCAS(g.err, 0, 0x400);
         }
         __syncwarp();
+    }
     } else {
+        asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(REGS_EPI));
         // -------------------------------------------------------- epilogue
         const int q = warp & 3;
         const int colh = (warp - W_EPI0) >> 2;
@@ -822,13 +842,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             t_idle = 0;
             tc::tc_fence_after();
-            uint32_t r0[32], r1[32];
-            if (gi == 0) drain_head<false>(taddr, zs, r0, r1);
-            else drain_head<true>(taddr, zs, r0, r1);
-            tc::tc_fence_before();
-            tc::mbar_arrive(tc::smem_u32(&sm.acc_empty[gi]));
-            if (gi == 0) drain_tail<false>(zs, r0, r1);
-            else drain_tail<true>(zs, r0, r1);
+            if (gi == 0) drain4<false>(taddr, zs, tc::smem_u32(&sm.acc_empty[0]));
+            else drain4<true>(taddr, zs, tc::smem_u32(&sm.acc_empty[1]));
             done_ch[gi]++;
         }
         // output row of this thread's accumulator lane (-1: padding or past the image)
@@ -1038,6 +1053,13 @@ int prepare_device(Ctx *c, bool again) {
     if (!done[c->device] || again) {
         PG_CHECK_CUDA(c, cudaFuncSetAttribute(limb_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)smem_bytes()));
+        // the register split inside the kernel assumes this launch size
+        cudaFuncAttributes fa;
+        PG_CHECK_CUDA(c, cudaFuncGetAttributes(&fa, limb_tma_kernel));
+        if (fa.numRegs != REGS_LAUNCH || fa.maxThreadsPerBlock < NTHREADS)
+            return set_error(c, PG_ERR_UNSUPPORTED,
+                             "limb_tma_kernel built with %d registers per thread (%d threads); its register split "
+                             "needs %d", fa.numRegs, fa.maxThreadsPerBlock, REGS_LAUNCH);
         if (!encode_fn(c)) return PG_ERR_CUDA;
         done[c->device] = true;
     }
