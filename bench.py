@@ -58,7 +58,7 @@ LIMB_FLOPS_PER_RING_MAC = 72  # 36 8-bit limb pairs x 2 flops: exact u64 MAC on 
 # batch-128 forward, from one ncu capture of dram__bytes_read.sum +
 # dram__bytes_write.sum over those launches (bench.py --steps 1 --warmup 1
 # under ncu with the plain run's tuning cache)
-VGG16_B128_LIMB_TRAFFIC = 5_074_737_152
+VGG16_B128_LIMB_TRAFFIC = 5_525_633_792
 
 WORKLOADS = {
     "vgg16": {"metric": "3PC VGG16 secure inference img/s", "kind": "infer3", "fp": 26, "ring": "u64",
@@ -92,8 +92,8 @@ WORKLOADS = {
                "requests": 512, "max_batch": 64,
                "desc": "512 requests, batch uniform in 1..64, SecureML or VGG16 (even odds), 3PC RSS, uint64 "
                        "shares, FP 26; waiting requests of one model are packed (up to 128 images) into one "
-                       "replay of the captured network of the smallest batch bucket (1, 2, 4, 6, 8, 12, 16, 24, "
-                       "..., 64, 80, 96, 112, 128) that holds them"},
+                       "replay of a captured network whose batch bucket (1, 2, 4, 6, 8, 12, 16, 24, ..., 64, 80, "
+                       "96, 112, 128) holds them: the smallest, or a larger one of the model that replays faster"},
 }
 _LAYERS = {"vgg16": nets.vgg16, "secureml": nets.secureml, "lenet-train": nets.lenet,
            "vgg16-train": lambda: nets.vgg16(maxpool=False),
@@ -1106,8 +1106,9 @@ def bench_fcnet(args, pg, torch, stream, dev, wl, batch, world):
 def bench_stream(args, pg, torch, stream, dev, wl, world):
     """The request stream, served in arrival order on one stream by
     piranha_gb300.stream: waiting requests of the same model are packed into
-    one replay of the captured network of the smallest batch bucket that holds
-    them (the oldest waiting request opens a pack, the next 16 waiting
+    one replay of a captured network whose batch bucket holds them: the
+    smallest such bucket, or a larger bucket of the same model whose replay
+    timed faster (the oldest waiting request opens a pack, the next 16 waiting
     requests of its model join it while it stays within 128 images; --no-pack
     serves each request alone). A pack's latency is its CUDA-event time from
     the start of its input copies to the end of its output copies; every
@@ -1129,6 +1130,11 @@ def bench_stream(args, pg, torch, stream, dev, wl, world):
     for p in packs:
         server.network(p.model, p.bucket)
     stream.synchronize()
+    moved = 0
+    if not args.no_autotune:
+        tuned = server.tune_buckets(packs)
+        moved = sum(a.bucket != b.bucket for a, b in zip(packs, tuned))
+        packs = tuned
 
     per_img_out = 10
     dev_in = [torch.from_numpy(np.ascontiguousarray(x).reshape(6, -1).view(np.int64)).to(dev) for _, _, x in reqs]
@@ -1219,6 +1225,10 @@ def bench_stream(args, pg, torch, stream, dev, wl, world):
                      "work": "mixed request sizes; the per-model lines carry the kernel fractions"},
         "comm_per_party_per_step": None,
         "networks": sorted(f"{m}@{b}" for m, b in server.nets),
+        "bucket_choice": {"moved_to_a_larger_bucket": int(moved),
+                          "replay_ms": {f"{m}@{b}": round(1e3 * t, 4) for (m, b), t in sorted(server.times.items())},
+                          "rule": "a pack runs on the fastest timed network of its model that holds it (a larger "
+                                  "bucket only when at least 3 % faster); --no-autotune keeps the smallest bucket"},
     }
     server.close()
     ctx.close()
@@ -1275,7 +1285,7 @@ def main():
         line["layer_ms"] = res["layer_ms"]
     if "layer_plans" in res:
         line["layer_plans"] = res["layer_plans"]
-    for k in ("latency_ms", "requests", "images", "replays", "packing", "networks", "sweep"):
+    for k in ("latency_ms", "requests", "images", "replays", "packing", "networks", "bucket_choice", "sweep"):
         if k in res:
             line[k] = res[k]
     if "compare_u64" in res:

@@ -290,6 +290,103 @@ template <typename T, int KIND> __global__ void ring_epilogue_kernel(const GemmA
     }
 }
 
+// Weight gradients with few outputs and a long K (LeNet's first
+// convolution: 20 filters x 25 taps over 128 x 24 x 24 output pixels): each
+// thread owns a 4 x 4 block of (filter, tap) outputs and one of `phases`
+// interleaved slices of the CTA's (segment, pixel) range, with the input
+// offsets of its four taps fixed for the whole run, so the gather costs one
+// add and a bounds test per value. The CTA's phases are summed in shared
+// memory and added into the split-K partial sums with one 64/32-bit atomic
+// per output (exact mod 2^w); ring_epilogue_kernel then applies the
+// epilogue. A = dY[k][m] (m = filter), B = X gathered at tap n = (r, s, c).
+constexpr int WS_OB = 4, WS_TB = 4, WS_THREADS = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(WS_THREADS, 2) wgrad_small_kernel(const GemmArgs<T> g, int phases, long long per_cta) {
+    __shared__ T red[WS_THREADS][WS_OB * WS_TB + 1];
+    const int ob_n = (g.M + WS_OB - 1) / WS_OB, tb_n = (g.N + WS_TB - 1) / WS_TB;
+    const int lbs = ob_n * tb_n;
+    const int tid = threadIdx.x;
+    const int lb = tid % lbs, phase = tid / lbs;
+    const int o0 = (lb / tb_n) * WS_OB, t0 = (lb % tb_n) * WS_TB;
+    T acc[WS_OB][WS_TB];
+#pragma unroll
+    for (int i = 0; i < WS_OB; i++)
+#pragma unroll
+        for (int j = 0; j < WS_TB; j++) acc[i][j] = 0;
+    if (phase < phases) {
+        // this thread's taps: input offset relative to the output pixel's corner, and (r, s) for the bounds
+        long long toff[WS_TB];
+        int tr[WS_TB], ts[WS_TB];
+        bool tval[WS_TB];
+#pragma unroll
+        for (int j = 0; j < WS_TB; j++) {
+            const int t = t0 + j;
+            tval[j] = t < g.N;
+            const int tt = tval[j] ? t : 0;
+            const int rs = tt / g.cc, c = tt - rs * g.cc;
+            tr[j] = rs / g.cs - g.pad;
+            ts[j] = rs % g.cs - g.pad;
+            toff[j] = ((long long)tr[j] * g.cw + ts[j]) * g.cc + c;
+        }
+        const long long ksz = g.K;
+        const long long begin = (long long)blockIdx.x * per_cta;
+        long long end = begin + per_cta;
+        const long long all = ksz * g.nseg;
+        if (end > all) end = all;
+        for (int seg = (int)(begin / ksz); seg < g.nseg && (long long)seg * ksz < end; seg++) {
+        const long long s0 = (long long)seg * ksz;
+        const uint32_t klo = (uint32_t)((begin > s0 ? begin : s0) - s0);
+        const uint32_t khi = (uint32_t)((end < s0 + ksz ? end : s0 + ksz) - s0);
+        const T *a = g.a[seg], *b0 = g.b0[seg], *b1 = g.b1[seg];
+        for (uint32_t k = klo + (uint32_t)phase; k < khi; k += (uint32_t)phases) {
+            const uint32_t nq = g.dQ.div(k), q = k - nq * g.cq;
+            const uint32_t n = g.dP.div(nq), p = nq - n * g.cp;
+            const int hb = (int)p * g.stride, wb = (int)q * g.stride;
+            const long long base = (((long long)n * g.ch + hb) * g.cw + wb) * g.cc;
+            T av[WS_OB], bv[WS_TB];
+#pragma unroll
+            for (int i = 0; i < WS_OB; i++) av[i] = o0 + i < g.M ? a[(size_t)k * g.ck + o0 + i] : (T)0;
+#pragma unroll
+            for (int j = 0; j < WS_TB; j++) {
+                const int h = hb + tr[j], w = wb + ts[j];
+                T v = 0;
+                if (tval[j] && h >= 0 && h < g.ch && w >= 0 && w < g.cw) {
+                    v = b0[base + toff[j]];
+                    if (b1) v = (T)(v + b1[base + toff[j]]);
+                }
+                bv[j] = v;
+            }
+#pragma unroll
+            for (int i = 0; i < WS_OB; i++)
+#pragma unroll
+                for (int j = 0; j < WS_TB; j++) acc[i][j] = (T)(acc[i][j] + av[i] * bv[j]);
+        }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < WS_OB; i++)
+#pragma unroll
+        for (int j = 0; j < WS_TB; j++) red[tid][i * WS_TB + j] = acc[i][j];
+    __syncthreads();
+    // thread e < lbs * 16 sums output e % 16 of lane block e / 16 over the phases
+    for (int e = tid; e < lbs * WS_OB * WS_TB; e += WS_THREADS) {
+        const int blk = e / (WS_OB * WS_TB), w = e - blk * (WS_OB * WS_TB);
+        const int m = (blk / tb_n) * WS_OB + w / WS_TB, nn = (blk % tb_n) * WS_TB + w % WS_TB;
+        if (m >= g.M || nn >= g.N) continue;
+        T sum = 0;
+        for (int ph = 0; ph < phases; ph++) sum = (T)(sum + red[ph * lbs + blk][w]);
+        atomic_add_ring(&g.partial[out_index<K_WGRAD>(g, m, nn)], sum);
+    }
+}
+
+// whether wgrad_small_kernel serves a weight gradient: at least two phases
+// of lane blocks per CTA and a K long enough to spread over the GPU
+template <typename T> static bool wgrad_small_applies(const GemmArgs<T> &g) {
+    const long long lbs = (long long)((g.M + WS_OB - 1) / WS_OB) * ((g.N + WS_TB - 1) / WS_TB);
+    return 2 * lbs <= WS_THREADS && (long long)g.K * g.nseg >= 16384 && g.K < (1LL << 31);
+}
+
 template <typename T> static void setup_conv(GemmArgs<T> &g, int op, int N, int H, int W, int C, int K, int R,
                                             int S, int pad, int stride) {
     int P = (H + 2 * pad - R) / stride + 1, Q = (W + 2 * pad - S) / stride + 1;
@@ -324,6 +421,29 @@ template <typename T, class TL> static void launch_tile(Ctx *c, dim3 grid, const
 
 template <typename T> static int launch_gemm(Ctx *c, GemmArgs<T> &g, int kind) {
     if (g.M <= 0 || g.N <= 0 || g.K < 0) return set_error(c, PG_ERR_SIZE, "ring gemm: bad sizes M=%d N=%d K=%d", g.M, g.N, g.K);
+    if (kind == K_WGRAD && wgrad_small_applies(g)) {
+        const int sms = c->sm_count > 0 ? c->sm_count : 148;
+        const int lbs = ((g.M + WS_OB - 1) / WS_OB) * ((g.N + WS_TB - 1) / WS_TB);
+        const int phases = WS_THREADS / lbs;
+        const long long all = (long long)g.K * g.nseg;
+        long long ctas = 4LL * sms;
+        const long long min_per = 64LL * phases;  // at least 64 pixels per phase
+        if (ctas * min_per > all) ctas = (all + min_per - 1) / min_per;
+        if (ctas < 1) ctas = 1;
+        const long long per = (all + ctas - 1) / ctas;
+        ctas = (all + per - 1) / per;
+        const size_t bytes = (size_t)g.M * g.N * sizeof(T);
+        g.partial = (T *)gemm_partial(c, bytes);
+        if (!g.partial) return PG_ERR_NO_MEMORY;
+        g.steps_per_split = 0;
+        PG_CHECK_CUDA(c, cudaMemsetAsync(g.partial, 0, bytes, c->stream));
+        wgrad_small_kernel<T><<<(unsigned)ctas, WS_THREADS, 0, c->stream>>>(g, phases, per);
+        size_t blocks = (bytes / sizeof(T) + 255) / 256;
+        if (blocks > (size_t)sms * 8) blocks = (size_t)sms * 8;
+        ring_epilogue_kernel<T, K_WGRAD><<<(unsigned)blocks, 256, 0, c->stream>>>(g);
+        c->launches += 2;
+        return launch_status(c, "wgrad_small_kernel");
+    }
     // tile shape: Col for N = 1, Thin for N <= 8, Small when a Wide tile would be less than half used
     int shape = 0, bm = Wide::BM, bn = Wide::BN;
     const double wide_use = (double)g.M * g.N /

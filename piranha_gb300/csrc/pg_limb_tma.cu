@@ -400,6 +400,7 @@ struct PackArgs {
     int kn;  // 1: b[k * N + n]; 0: b[n * Kreal + k]
     long long wg_pq;  // > 0: K index k = pixel * wg_batch + image of b = dY[image][pixel][n] (wg_pq pixels)
     int wg_batch;
+    int cpad, creal;  // cpad > 0: K index k = tap * cpad + c of the channel-padded image, b's k = tap * creal + c
     uint8_t *packB;
 };
 
@@ -436,7 +437,11 @@ __global__ void pack_kernel(const __grid_constant__ PackArgs pa) {
             const uint64_t *b0 = pa.b[2 * p], *b1 = (seg & 1) ? nullptr : pa.b[2 * p + 1];
 #pragma unroll
             for (int i = 0; i < 8; i++) {
-                const int k = k0 + i;
+                int k = k0 + i;
+                if (pa.cpad) {
+                    const int tap = k / pa.cpad, ch = k - tap * pa.cpad;
+                    k = ch < pa.creal ? tap * pa.creal + ch : pa.Kreal;  // padding channels: 0
+                }
                 if (k < pa.Kreal) {
                     long long idx = pa.kn ? (long long)k * pa.N + n : (long long)n * pa.Kreal + k;
                     if (pa.wg_pq) idx = ((long long)(k % pa.wg_batch) * pa.wg_pq + k / pa.wg_batch) * pa.N + n;
@@ -1143,6 +1148,20 @@ static bool wgt_enabled() {
 // environment variable PG_POSMAJOR gives another limit; PG_POSMAJOR=0 turns
 // the position-major tiles off (every implicit convolution then uses
 // rectangles).
+// Implicit convolutions over input channels that are not a multiple of 16
+// pad the image's channels with zeros up to the next multiple (PG_CPAD=0
+// turns this off), when that adds at most 60 % to the tensor work: LeNet's
+// second convolution (20 -> 32 channels) then reads a 57 MB digit image
+// instead of a 403 MB im2col image.
+static bool cpad_enabled() {
+    static int v = -1;
+    if (v < 0) {
+        const char *e = getenv("PG_CPAD");
+        v = (e && e[0] == '0') ? 0 : 1;
+    }
+    return v == 1;
+}
+
 static int posmajor_max_pixels() {
     static const int lim = [] {
         const char *e = getenv("PG_POSMAJOR");
@@ -1163,11 +1182,14 @@ int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout
     p.tB_kn = 0;  // KRSC filters: b[n * f*f*Din + k]
     p.colmajor = 0;
     p.H = H; p.W = W; p.Din = Din; p.stride = stride;
-    if (stride == 1 && Din % BK == 0 && Q <= BM && P <= H && Q <= W) {
-        // implicit: the image is the activation tensor itself, taps are box shifts
+    const int Cpad = (Din + BK - 1) / BK * BK;
+    const bool padded = Din % BK != 0 && 5 * Cpad <= 8 * Din && cpad_enabled();
+    if (stride == 1 && (Din % BK == 0 || padded) && Q <= BM && P <= H && Q <= W) {
+        // implicit: the image is the activation tensor itself (channels zero-padded
+        // to Cpad), taps are box shifts
         p.implicit = 1;
         p.Kreal = Din;
-        p.C = Din;
+        p.C = Cpad;
         p.pixels = (long long)batch * H * W;
         p.src_mode = SRC_ROWS;
         p.ld = Din;
@@ -1499,6 +1521,10 @@ int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB) {
     pa.kn = p.tB_kn;
     pa.wg_pq = p.wgt ? (long long)p.P * p.Q : 0;
     pa.wg_batch = p.Nimg;
+    if (p.implicit && !p.wgt && p.C != p.Din) {
+        pa.cpad = p.C;
+        pa.creal = p.Din;
+    }
     pa.packB = (uint8_t *)packB;
     const long long units = 6ll * p.ntiles_n * BN * p.kblocks * 2;
     const int sms = c->sm_count > 0 ? c->sm_count : 148;

@@ -16,6 +16,10 @@ them.
 * ``StreamServer`` keeps one captured network per (model, bucket), copies a
   pack's input shares into the first rows of the bucket network's input
   buffers, replays its graph and hands out each request's output rows.
+* ``StreamServer.tune_buckets`` times each captured network once and moves a
+  pack to a larger bucket of its model when that one replays faster (VGG16
+  at 128 images runs position-major convolution tiles, which need a multiple
+  of 128 images; at 112 it runs rectangle tiles and takes longer).
 """
 from __future__ import annotations
 
@@ -40,6 +44,20 @@ class Pack:
     requests: list  # request indices, in arrival order
     images: int     # total images
     bucket: int     # batch of the network that serves it
+
+
+def choose_bucket(times: dict, bucket: int, margin: float = 0.03) -> int:
+    """times: {bucket: replay seconds} of one model's captured networks. The
+    bucket a pack that fits ``bucket`` is served on: the fastest of ``bucket``
+    and the larger timed buckets, a larger one only when it is at least
+    ``margin`` faster."""
+    best, t_best = bucket, times.get(bucket)
+    if t_best is None:
+        return bucket
+    for b in sorted(times):
+        if b > bucket and times[b] < t_best * (1.0 - margin):
+            best, t_best = b, times[b]
+    return best
 
 
 def plan_packs(requests, cap: int = 128, lookahead: int = 16, buckets=BUCKETS):
@@ -86,6 +104,35 @@ class StreamServer:
         self.nets = {}
         self.n_in = {m: _input_size(L) for m, (L, _) in models.items()}
         self.n_out = {m: _output_size(L) for m, (L, _) in models.items()}
+        self.times = {}  # (model, bucket) -> seconds per replay
+
+    def replay_seconds(self, model: str, bucket: int, reps: int = 3) -> float:
+        """Seconds per replay of the (model, bucket) network, timed once on the
+        host around ``reps`` replays after one warm-up (the stream synchronised
+        on both sides)."""
+        import time
+
+        key = (model, bucket)
+        if key not in self.times:
+            net, _, _ = self.network(model, bucket)
+            net.forward_resident()
+            self.ctx.sync()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                net.forward_resident()
+            self.ctx.sync()
+            self.times[key] = (time.perf_counter() - t0) / reps
+        return self.times[key]
+
+    def tune_buckets(self, packs):
+        """The packs with each one's bucket replaced by the fastest captured
+        bucket of its model that holds it (choose_bucket over the buckets the
+        packs already use, so no further network is captured)."""
+        used = {}
+        for p in packs:
+            used.setdefault(p.model, set()).add(p.bucket)
+        times = {m: {b: self.replay_seconds(m, b) for b in bs} for m, bs in used.items()}
+        return [Pack(p.model, p.requests, p.images, choose_bucket(times[p.model], p.bucket)) for p in packs]
 
     def network(self, model: str, bucket: int):
         """(net, input view (6, in_n), output view (6, out_n)) of the captured network."""

@@ -126,6 +126,21 @@ def test_fpc_convolution(pg, ctx, op):
     check_comm(ctx, comm)
 
 
+def test_fpc_wgrad_small_output(pg, ctx):
+    """A weight gradient with few outputs and a long K (the u64 form's
+    small-output kernel over the 4PC party segments)."""
+    batch, H, W, f, Din, Dout, stride, pad = 64, 20, 20, 5, 1, 8, 1, 0
+    P = Q = H - f + 1
+    A, B = views(batch * P * Q * Dout, U64, 18), views(batch * H * W * Din, U64, 19)
+    comm = orc.Comm(4)
+    want = orc.fpc_convolution(A, B, orc.WGRAD, batch, H, W, f, Din, Dout, stride, pad, 20, comm)
+    C = pg.fpc.empty(want.shape[2])
+    pg.fpc.convolution(ctx, dev(A), dev(B), C, orc.WGRAD, batch, H, W, f, Din, Dout, stride, pad, 20)
+    ctx.sync()
+    assert np.array_equal(host(C), want)
+    check_comm(ctx, comm)
+
+
 def test_fpc_convolution_strided(pg, ctx):
     batch, H, W, f, Din, Dout, stride, pad = 3, 9, 7, 3, 2, 5, 2, 1
     P = (H + 2 * pad - f) // stride + 1

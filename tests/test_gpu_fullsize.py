@@ -197,3 +197,37 @@ def test_stream_packed_replays_equal_oracle(pg):
     ctx.check_device_errors()
     server.close()
     ctx.close()
+
+
+def test_stream_pack_on_a_larger_bucket_equals_oracle(pg):
+    """A pack served on a larger bucket than the smallest that holds it (what
+    StreamServer.tune_buckets does when the larger network replays faster)
+    gives each request the oracle's result; tune_buckets never picks a
+    bucket smaller than the pack."""
+    import torch
+
+    from piranha_gb300 import stream as st
+
+    layers = netref.secureml_layers()
+    params = seeded.kaiming_uniform(layers, 93)
+    reqs = [("secureml", 5), ("secureml", 17), ("secureml", 9), ("secureml", 100)]
+    packs = st.plan_packs(reqs, cap=128, lookahead=16)
+    assert [(p.requests, p.bucket) for p in packs] == [([0, 1, 2], 32), ([3], 112)]
+    ctx = pg.Context(0, form=pg.FORM_LIMB_TC)
+    server = st.StreamServer(pg, ctx, {"secureml": (layers, params)})
+    tuned = server.tune_buckets(packs)
+    assert all(t.bucket >= t.images and t.bucket in (32, 112) for t in tuned)
+    moved = [st.Pack(p.model, p.requests, p.images, 112) for p in packs]
+    xs = [seeded.images(800 + r, b * 784) for r, (_, b) in enumerate(reqs)]
+    ins = [pg.to_device(x).reshape(6, -1) for x in xs]
+    for plan in (tuned, moved):
+        outs = [torch.empty((6, b * 10), dtype=torch.int64, device="cuda") for _, b in reqs]
+        for p in plan:
+            server.serve(p, ins, outs)
+        ctx.sync()
+        for r, (_, b) in enumerate(reqs):
+            want = netref.forward(layers, params, xs[r], b)
+            assert np.array_equal(pg.to_host(outs[r]).reshape(3, 2, -1), want), f"request {r}"
+    ctx.check_device_errors()
+    server.close()
+    ctx.close()

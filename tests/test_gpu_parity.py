@@ -206,6 +206,49 @@ def test_rss_conv_random_views(pg, ctx, op, batch, H, W, f, Din, Dout, stride, p
     comm_equal(ctx, comm)
 
 
+@pytest.mark.parametrize("batch,H,W,f,Din,Dout,stride,pad", [(4, 12, 12, 5, 20, 50, 1, 0), (3, 9, 7, 3, 10, 70, 1, 1),
+                                                             (128, 4, 4, 3, 20, 24, 1, 1)])
+def test_rss_fprop_padded_channels_limb_form(pg, batch, H, W, f, Din, Dout, stride, pad):
+    """Implicit limb-form convolutions over input channels that are not a
+    multiple of 16 (the image's channels zero-padded to 32 or 16; the last
+    case on position-major tiles), with the form fixed to the limb kernel."""
+    ctx = pg.Context(0, form=pg.FORM_LIMB_TC)
+    ctx.set_autotune(False)
+    A = orc.random_views(batch * H * W * Din, U64, 42)
+    B = orc.random_views(Dout * f * f * Din, U64, 43)
+    comm = orc.Comm()
+    want = orc.convolution(A, B, orc.FPROP, batch, H, W, f, Din, Dout, stride, pad, 26, comm)
+    C = pg.empty_shares(want.shape[2])
+    pg.convolution(ctx, dev(pg, A), dev(pg, B), C, orc.FPROP, batch, H, W, f, Din, Dout, stride, pad, 26)
+    ctx.sync()
+    assert np.array_equal(host(pg, C), want)
+    comm_equal(ctx, comm)
+    ctx.check_device_errors()
+    ctx.close()
+
+
+@pytest.mark.parametrize("batch,H,W,f,Din,Dout,stride,pad", [(8, 28, 28, 5, 1, 20, 1, 0), (64, 17, 17, 3, 3, 6, 2, 1),
+                                                             (40, 10, 10, 3, 2, 30, 1, 1)])
+def test_rss_wgrad_small_output_u64_form(pg, batch, H, W, f, Din, Dout, stride, pad):
+    """Weight gradients with few outputs and a long K (LeNet's first
+    convolution at batch 8; a strided, padded one; one with 30 filters) run the
+    u64 form's small-output kernel: every share equal to the oracle's."""
+    ctx = pg.Context(0, form=pg.FORM_U64)
+    P, Q = (H + 2 * pad - f) // stride + 1, (W + 2 * pad - f) // stride + 1
+    assert 6 * batch * P * Q >= 16384
+    A = orc.random_views(batch * P * Q * Dout, U64, 40)
+    B = orc.random_views(batch * H * W * Din, U64, 41)
+    comm = orc.Comm()
+    want = orc.convolution(A, B, orc.WGRAD, batch, H, W, f, Din, Dout, stride, pad, 26, comm)
+    C = pg.empty_shares(want.shape[2])
+    pg.convolution(ctx, dev(pg, A), dev(pg, B), C, orc.WGRAD, batch, H, W, f, Din, Dout, stride, pad, 26)
+    ctx.sync()
+    assert np.array_equal(host(pg, C), want)
+    comm_equal(ctx, comm)
+    ctx.check_device_errors()
+    ctx.close()
+
+
 # ------------------------------------------------------------- elementwise ops
 
 @pytest.mark.parametrize("n", [1, 1000, 65537])

@@ -101,6 +101,21 @@ def test_tpc_convolution(pg, ctx, op):
     check_comm(ctx, comm)
 
 
+def test_tpc_wgrad_small_output(pg, ctx):
+    """A weight gradient with few outputs and a long K (the u64 form's
+    small-output kernel over the 2PC segments)."""
+    batch, H, W, f, Din, Dout, stride, pad = 64, 20, 20, 5, 1, 8, 1, 0
+    P = Q = H - f + 1
+    A, B = rnd(batch * P * Q * Dout, U64, 16), rnd(batch * H * W * Din, U64, 17)
+    comm = orc.Comm()
+    want = orc.tpc_convolution(A, B, orc.WGRAD, batch, H, W, f, Din, Dout, stride, pad, 20, comm)
+    C = pg.tpc.empty(want.shape[1])
+    pg.tpc.convolution(ctx, dev(A), dev(B), C, orc.WGRAD, batch, H, W, f, Din, Dout, stride, pad, 20)
+    ctx.sync()
+    assert np.array_equal(host(C), want)
+    check_comm(ctx, comm)
+
+
 @pytest.mark.parametrize("d", [1 << 26, 3, 1000])
 def test_tpc_divide_public(pg, ctx, d):
     a = rnd(999, U64, 8)

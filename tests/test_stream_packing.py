@@ -39,3 +39,17 @@ def test_buckets_pad_at_most_a_third():
     for b in range(1, 129):
         k = stream.bucket_for(b)
         assert k >= b and (k - b) <= max(1, k // 3)
+
+
+def test_choose_bucket_takes_a_faster_larger_bucket():
+    # 112 images replay slower than 128 (rectangle vs position-major tiles)
+    times = {64: 5.9e-3, 112: 11.0e-3, 128: 10.3e-3}
+    assert stream.choose_bucket(times, 112) == 128
+    assert stream.choose_bucket(times, 64) == 64       # a larger bucket that is slower is not taken
+    assert stream.choose_bucket(times, 128) == 128
+    # within the 3 % margin the pack stays on its own bucket
+    assert stream.choose_bucket({112: 10.5e-3, 128: 10.3e-3}, 112) == 112
+    # an untimed bucket is kept
+    assert stream.choose_bucket({128: 1.0}, 96) == 96
+    # never a smaller bucket
+    assert stream.choose_bucket({16: 1e-4, 32: 1.0}, 32) == 32
