@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(WS_THREADS, 2) wgrad_small_kernel(const GemmAr
         for (int j = 0; j < WS_TB; j++) acc[i][j] = 0;
     if (phase < phases) {
         // this thread's taps: input offset relative to the output pixel's corner, and (r, s) for the bounds
-        long long toff[WS_TB];
+        int toff[WS_TB];
         int tr[WS_TB], ts[WS_TB];
         bool tval[WS_TB];
 #pragma unroll
@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(WS_THREADS, 2) wgrad_small_kernel(const GemmAr
             const int rs = tt / g.cc, c = tt - rs * g.cc;
             tr[j] = rs / g.cs - g.pad;
             ts[j] = rs % g.cs - g.pad;
-            toff[j] = ((long long)tr[j] * g.cw + ts[j]) * g.cc + c;
+            toff[j] = (tr[j] * g.cw + ts[j]) * g.cc + c;
         }
         const long long ksz = g.K;
         const long long begin = (long long)blockIdx.x * per_cta;
@@ -339,28 +339,44 @@ __global__ void __launch_bounds__(WS_THREADS, 2) wgrad_small_kernel(const GemmAr
         const uint32_t klo = (uint32_t)((begin > s0 ? begin : s0) - s0);
         const uint32_t khi = (uint32_t)((end < s0 + ksz ? end : s0 + ksz) - s0);
         const T *a = g.a[seg], *b0 = g.b0[seg], *b1 = g.b1[seg];
-        for (uint32_t k = klo + (uint32_t)phase; k < khi; k += (uint32_t)phases) {
+        // the operands of output pixel k (dY row, gathered taps); two pixels per
+        // iteration, all loads issued before either block of multiply-adds
+        auto load = [&](uint32_t k, T (&av)[WS_OB], T (&bv)[WS_TB]) {
             const uint32_t nq = g.dQ.div(k), q = k - nq * g.cq;
             const uint32_t n = g.dP.div(nq), p = nq - n * g.cp;
             const int hb = (int)p * g.stride, wb = (int)q * g.stride;
             const long long base = (((long long)n * g.ch + hb) * g.cw + wb) * g.cc;
-            T av[WS_OB], bv[WS_TB];
 #pragma unroll
-            for (int i = 0; i < WS_OB; i++) av[i] = o0 + i < g.M ? a[(size_t)k * g.ck + o0 + i] : (T)0;
+            for (int i = 0; i < WS_OB; i++) av[i] = o0 + i < g.M ? __ldg(a + (size_t)k * g.ck + o0 + i) : (T)0;
 #pragma unroll
             for (int j = 0; j < WS_TB; j++) {
                 const int h = hb + tr[j], w = wb + ts[j];
                 T v = 0;
                 if (tval[j] && h >= 0 && h < g.ch && w >= 0 && w < g.cw) {
-                    v = b0[base + toff[j]];
-                    if (b1) v = (T)(v + b1[base + toff[j]]);
+                    v = __ldg(b0 + base + toff[j]);
+                    if (b1) v = (T)(v + __ldg(b1 + base + toff[j]));
                 }
                 bv[j] = v;
             }
+        };
+        auto mac = [&](const T (&av)[WS_OB], const T (&bv)[WS_TB]) {
 #pragma unroll
             for (int i = 0; i < WS_OB; i++)
 #pragma unroll
                 for (int j = 0; j < WS_TB; j++) acc[i][j] = (T)(acc[i][j] + av[i] * bv[j]);
+        };
+        uint32_t k = klo + (uint32_t)phase;
+        for (; k + (uint32_t)phases < khi; k += 2u * (uint32_t)phases) {
+            T av0[WS_OB], bv0[WS_TB], av1[WS_OB], bv1[WS_TB];
+            load(k, av0, bv0);
+            load(k + (uint32_t)phases, av1, bv1);
+            mac(av0, bv0);
+            mac(av1, bv1);
+        }
+        if (k < khi) {
+            T av0[WS_OB], bv0[WS_TB];
+            load(k, av0, bv0);
+            mac(av0, bv0);
         }
         }
     }
