@@ -1142,26 +1142,25 @@ static bool wgt_enabled() {
     return on;
 }
 
-// Output positions per image up to which a same convolution is tiled by
-// position: 1024 (32 x 32 and smaller; measured on VGG16 at batch 128, the
-// 2x2 to 8x8 layers gain 16-58 %, 16x16 3-7 %, 32x32 1 %) unless the
-// environment variable PG_POSMAJOR gives another limit; PG_POSMAJOR=0 turns
-// the position-major tiles off (every implicit convolution then uses
-// rectangles).
 // Implicit convolutions over input channels that are not a multiple of 16
 // pad the image's channels with zeros up to the next multiple (PG_CPAD=0
 // turns this off), when that adds at most 60 % to the tensor work: LeNet's
 // second convolution (20 -> 32 channels) then reads a 57 MB digit image
 // instead of a 403 MB im2col image.
 static bool cpad_enabled() {
-    static int v = -1;
-    if (v < 0) {
+    static const bool on = [] {
         const char *e = getenv("PG_CPAD");
-        v = (e && e[0] == '0') ? 0 : 1;
-    }
-    return v == 1;
+        return !(e && e[0] == '0');
+    }();
+    return on;
 }
 
+// Output positions per image up to which a same convolution is tiled by
+// position: 1024 (32 x 32 and smaller; measured on VGG16 at batch 128, the
+// 2x2 to 8x8 layers gain 16-58 %, 16x16 3-7 %, 32x32 1 %) unless the
+// environment variable PG_POSMAJOR gives another limit; PG_POSMAJOR=0 turns
+// the position-major tiles off (every implicit convolution then uses
+// rectangles).
 static int posmajor_max_pixels() {
     static const int lim = [] {
         const char *e = getenv("PG_POSMAJOR");
