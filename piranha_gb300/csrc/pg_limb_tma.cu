@@ -261,15 +261,26 @@ __global__ void image_kernel(const __grid_constant__ ImageArgs ia) {
             const long long np = pix / ia.Q;
             const int p = (int)(np % ia.P);
             const long long n = np / ia.P;
+            // k = (r * f + s) * Din + c, split once and then carried
+            int c = k0 % ia.Din;
+            const int rs = k0 / ia.Din;
+            int s = rs % ia.f, r = rs / ia.f;
+            const int h0 = p * ia.stride - ia.pad, w0 = q * ia.stride - ia.pad;
+            const uint64_t *img0 = a + n * ia.H * ia.W * (long long)ia.Din;
 #pragma unroll
             for (int i = 0; i < 8; i++) {
-                const int k = k0 + i;
-                if (k >= ia.Kreal) continue;
-                const int c = k % ia.Din, rs = k / ia.Din;
-                const int s = rs % ia.f, r = rs / ia.f;
-                const int h = p * ia.stride - ia.pad + r, w = q * ia.stride - ia.pad + s;
-                if (h < 0 || h >= ia.H || w < 0 || w >= ia.W) continue;
-                v[i] = __ldg(a + ((n * ia.H + h) * ia.W + w) * (long long)ia.Din + c);
+                if (k0 + i < ia.Kreal) {
+                    const int h = h0 + r, w = w0 + s;
+                    if (h >= 0 && h < ia.H && w >= 0 && w < ia.W)
+                        v[i] = __ldg(img0 + ((long long)h * ia.W + w) * ia.Din + c);
+                }
+                if (++c == ia.Din) {
+                    c = 0;
+                    if (++s == ia.f) {
+                        s = 0;
+                        ++r;
+                    }
+                }
             }
         }
         uint4 pl[8];
