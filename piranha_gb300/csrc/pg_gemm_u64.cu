@@ -10,6 +10,8 @@
 // reconstruct3out3 (:1020-1050) reveals. The epilogue then applies
 // dividePublic3out3 (:1077-1094) and writes all six output shares (plus the
 // FC bias shares of FCLayer.cu:110-116 when given).
+#include <mutex>
+
 #include "pg_common.cuh"
 
 namespace pg {
@@ -396,6 +398,119 @@ __global__ void __launch_bounds__(WS_THREADS, 2) wgrad_small_kernel(const GemmAr
     }
 }
 
+// The same weight gradients, staged through shared memory by output row:
+// each phase of the CTA takes one output row (segment, image n, row p) at a
+// time and its threads copy the row's dY values (Q x Dout) and the f input
+// rows it touches (zero-padded to W + 2 pad columns, b0 + b1 summed) into the
+// phase's slice of shared memory; then every thread runs its 4 x 4 block of
+// (filter, tap) outputs over the row's Q pixels with pointer increments only.
+// Phases run their rows independently (one named barrier each).
+template <typename T>
+__global__ void __launch_bounds__(WS_THREADS, 2) wgrad_rows_kernel(const GemmArgs<T> g, int phases, int rows_per_cta, int rpr) {
+    extern __shared__ __align__(16) unsigned char ws_smem[];
+    T *sm = reinterpret_cast<T *>(ws_smem);
+    const int ob_n = (g.M + WS_OB - 1) / WS_OB, tb_n = (g.N + WS_TB - 1) / WS_TB;
+    const int lbs = ob_n * tb_n;
+    const int tid = threadIdx.x;
+    const int lb = tid % lbs, phase = tid / lbs;
+    const int o0 = (lb / tb_n) * WS_OB, t0 = (lb % tb_n) * WS_TB;
+    const int Wp = g.cw + 2 * g.pad;                 // staged input row length in pixels
+    const int xrow = Wp * g.cc;                      // values per staged input row
+    const int dy_vals = g.cq * g.ck, x_vals = g.cr * xrow;
+    const int slice = dy_vals + x_vals;
+    T acc[WS_OB][WS_TB];
+#pragma unroll
+    for (int i = 0; i < WS_OB; i++)
+#pragma unroll
+        for (int j = 0; j < WS_TB; j++) acc[i][j] = 0;
+    const bool active = phase < phases;
+    T *const slices = sm + (size_t)(active ? phase : 0) * rpr * slice;  // this phase's rpr row slices
+    // this thread's taps inside the staged rows
+    int toff[WS_TB];
+#pragma unroll
+    for (int j = 0; j < WS_TB; j++) {
+        const int t = t0 + j < g.N ? t0 + j : 0;
+        const int rs = t / g.cc, c = t - rs * g.cc;
+        toff[j] = (rs / g.cs) * xrow + (rs % g.cs) * g.cc + c;
+    }
+    const int pt = phase * lbs;  // first thread of the phase
+    const long long per_img = (long long)g.cn * g.cp;
+    const long long rows = (long long)g.nseg * per_img;
+    const long long r0 = (long long)blockIdx.x * rows_per_cta;
+    // every thread runs the same number of rounds (rpr rows per phase each,
+    // staged together so their loads overlap), so the two CTA-wide barriers of
+    // a round are reached by all threads
+    const int per_round = phases * rpr;
+    const int rounds = (rows_per_cta + per_round - 1) / per_round;
+    for (int rnd = 0; rnd < rounds; rnd++) {
+      for (int ri = 0; ri < rpr; ri++) {
+        const long long row = r0 + ((long long)rnd * phases + phase) * rpr + ri;
+        const bool have = active && row < r0 + rows_per_cta && row < rows;
+        T *dys = slices + (size_t)ri * slice, *xs = dys + dy_vals;
+        const T *a = nullptr;
+        if (have) {
+            const int seg = (int)(row / per_img);
+            const int np = (int)(row - (long long)seg * per_img);
+            const int n = np / g.cp, p = np - n * g.cp;
+            a = g.a[seg];
+            const T *b0 = g.b0[seg], *b1 = g.b1[seg];
+            // stage dY[n][p][*][*] and the input rows p*stride - pad + r, r < f
+            const T *dyg = a + ((size_t)n * g.cp + p) * g.cq * g.ck;
+#pragma unroll 4
+            for (int e = tid - pt; e < dy_vals; e += lbs) dys[e] = dyg[e];
+#pragma unroll 4
+            for (int e = tid - pt; e < x_vals; e += lbs) {
+                const int r = e / xrow, rem = e - r * xrow;
+                const int wp = rem / g.cc, c = rem - wp * g.cc;
+                const int h = p * g.stride - g.pad + r, w = wp - g.pad;
+                T v = 0;
+                if (h >= 0 && h < g.ch && w >= 0 && w < g.cw) {
+                    const size_t idx = (((size_t)n * g.ch + h) * g.cw + w) * g.cc + c;
+                    v = b0[idx];
+                    if (b1) v = (T)(v + b1[idx]);
+                }
+                xs[e] = v;
+            }
+        }
+      }
+        __syncthreads();
+      for (int ri = 0; ri < rpr; ri++) {
+        const long long row = r0 + ((long long)rnd * phases + phase) * rpr + ri;
+        const int q_n = active && row < r0 + rows_per_cta && row < rows ? g.cq : 0;
+        const T *dys = slices + (size_t)ri * slice, *xs = dys + dy_vals;
+        const T *dp = dys + o0, *xp = xs;
+        const int xstep = g.stride * g.cc;
+        for (int q = 0; q < q_n; q++, dp += g.ck, xp += xstep) {
+            T av[WS_OB], bv[WS_TB];
+#pragma unroll
+            for (int i = 0; i < WS_OB; i++) av[i] = o0 + i < g.M ? dp[i] : (T)0;
+#pragma unroll
+            for (int j = 0; j < WS_TB; j++) bv[j] = t0 + j < g.N ? xp[toff[j]] : (T)0;
+#pragma unroll
+            for (int i = 0; i < WS_OB; i++)
+#pragma unroll
+                for (int j = 0; j < WS_TB; j++) acc[i][j] = (T)(acc[i][j] + av[i] * bv[j]);
+        }
+      }
+        __syncthreads();
+    }
+    __syncthreads();
+    T (*red)[WS_OB * WS_TB + 1] = reinterpret_cast<T (*)[WS_OB * WS_TB + 1]>(sm);
+#pragma unroll
+    for (int i = 0; i < WS_OB; i++)
+#pragma unroll
+        for (int j = 0; j < WS_TB; j++) red[tid][i * WS_TB + j] = acc[i][j];
+    __syncthreads();
+    for (int e = tid; e < lbs * WS_OB * WS_TB; e += WS_THREADS) {
+        const int blk = e / (WS_OB * WS_TB), w = e - blk * (WS_OB * WS_TB);
+        const int m = (blk / tb_n) * WS_OB + w / WS_TB, nn = (blk % tb_n) * WS_TB + w % WS_TB;
+        if (m >= g.M || nn >= g.N) continue;
+        T sum = 0;
+        for (int ph = 0; ph < phases; ph++) sum = (T)(sum + red[ph * lbs + blk][w]);
+        atomic_add_ring(&g.partial[out_index<K_WGRAD>(g, m, nn)], sum);
+    }
+}
+
 // whether wgrad_small_kernel serves a weight gradient: at least two phases
 // of lane blocks per CTA and a K long enough to spread over the GPU
 template <typename T> static bool wgrad_small_applies(const GemmArgs<T> &g) {
@@ -440,6 +555,49 @@ template <typename T> static int launch_gemm(Ctx *c, GemmArgs<T> &g, int kind) {
     if (kind == K_WGRAD && wgrad_small_applies(g)) {
         const int sms = c->sm_count > 0 ? c->sm_count : 148;
         const int lbs = ((g.M + WS_OB - 1) / WS_OB) * ((g.N + WS_TB - 1) / WS_TB);
+        // staged by output row when a phase's slice (one row of dY and the f
+        // input rows it touches) fits: at most 96 KB per CTA, two CTAs per SM
+        const long long slice = (long long)g.cq * g.ck + (long long)g.cr * (g.cw + 2 * g.pad) * g.cc;
+        const long long red_bytes = (long long)WS_THREADS * (WS_OB * WS_TB + 1) * sizeof(T);
+        int row_phases = WS_THREADS / lbs;
+        while (row_phases > 0 && row_phases * slice * (long long)sizeof(T) > 96 * 1024) row_phases--;
+        if (row_phases >= 1 && slice * sizeof(T) <= 96 * 1024) {
+            // one output row per phase and round (two rows per round measured
+            // 0.5 % slower on LeNet's training step)
+            const int rpr = 1;
+            const long long rows = (long long)g.nseg * g.cn * g.cp;
+            const long long per_round = (long long)row_phases * rpr;
+            // one wave of resident CTAs (two per SM), each a whole number of rounds
+            const long long slots = 2LL * sms;
+            long long per = (rows + slots - 1) / slots;
+            per = (per + per_round - 1) / per_round * per_round;
+            const long long ctas = (rows + per - 1) / per;
+            const long long stage = per_round * slice * (long long)sizeof(T);
+            const long long smem = stage > red_bytes ? stage : red_bytes;
+            const size_t bytes = (size_t)g.M * g.N * sizeof(T);
+            g.partial = (T *)gemm_partial(c, bytes);
+            if (!g.partial) return PG_ERR_NO_MEMORY;
+            g.steps_per_split = 0;
+            if (smem > 48 * 1024) {
+                // once per device: the kernel's shared-memory limit (never inside a stream capture)
+                static std::mutex mu;
+                static bool done[64];
+                std::lock_guard<std::mutex> lock(mu);
+                if (c->device < 0 || c->device >= 64) return set_error(c, PG_ERR_UNSUPPORTED, "device %d", c->device);
+                if (!done[c->device]) {
+                    PG_CHECK_CUDA(c, cudaFuncSetAttribute(wgrad_rows_kernel<T>,
+                                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+                    done[c->device] = true;
+                }
+            }
+            PG_CHECK_CUDA(c, cudaMemsetAsync(g.partial, 0, bytes, c->stream));
+            wgrad_rows_kernel<T><<<(unsigned)ctas, WS_THREADS, (size_t)smem, c->stream>>>(g, row_phases, (int)per, rpr);
+            size_t blocks = (bytes / sizeof(T) + 255) / 256;
+            if (blocks > (size_t)sms * 8) blocks = (size_t)sms * 8;
+            ring_epilogue_kernel<T, K_WGRAD><<<(unsigned)blocks, 256, 0, c->stream>>>(g);
+            c->launches += 2;
+            return launch_status(c, "wgrad_rows_kernel");
+        }
         const int phases = WS_THREADS / lbs;
         const long long all = (long long)g.K * g.nseg;
         long long ctas = 4LL * sms;

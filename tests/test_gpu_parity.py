@@ -228,11 +228,13 @@ def test_rss_fprop_padded_channels_limb_form(pg, batch, H, W, f, Din, Dout, stri
 
 
 @pytest.mark.parametrize("batch,H,W,f,Din,Dout,stride,pad", [(8, 28, 28, 5, 1, 20, 1, 0), (64, 17, 17, 3, 3, 6, 2, 1),
-                                                             (40, 10, 10, 3, 2, 30, 1, 1)])
+                                                             (40, 10, 10, 3, 2, 30, 1, 1), (2, 3, 600, 3, 20, 4, 1, 1)])
 def test_rss_wgrad_small_output_u64_form(pg, batch, H, W, f, Din, Dout, stride, pad):
     """Weight gradients with few outputs and a long K (LeNet's first
     convolution at batch 8; a strided, padded one; one with 30 filters) run the
-    u64 form's small-output kernel: every share equal to the oracle's."""
+    u64 form's row-staged small-output kernel; the last case's input rows
+    (600 pixels x 20 channels) are too long to stage and take the gathering
+    kernel: every share equal to the oracle's."""
     ctx = pg.Context(0, form=pg.FORM_U64)
     P, Q = (H + 2 * pad - f) // stride + 1, (W + 2 * pad - f) // stride + 1
     assert 6 * batch * P * Q >= 16384
