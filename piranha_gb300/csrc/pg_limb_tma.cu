@@ -412,6 +412,7 @@ struct PackArgs {
     long long wg_pq;  // > 0: K index k = pixel * wg_batch + image of b = dY[image][pixel][n] (wg_pq pixels)
     int wg_batch;
     int cpad, creal;  // cpad > 0: K index k = tap * cpad + c of the channel-padded image, b's k = tap * creal + c
+    int flip_f;       // > 0: K index k = tap * cpad + kk (kk < creal), column n: b = W[kk][f-1-r][f-1-s][n], N = Din
     uint8_t *packB;
 };
 
@@ -449,6 +450,17 @@ __global__ void pack_kernel(const __grid_constant__ PackArgs pa) {
 #pragma unroll
             for (int i = 0; i < 8; i++) {
                 int k = k0 + i;
+                if (pa.flip_f) {
+                    const int tap = k / pa.cpad, kk = k - tap * pa.cpad;
+                    if (kk < pa.creal && tap < pa.flip_f * pa.flip_f) {
+                        const int r = tap / pa.flip_f, sx = tap - r * pa.flip_f;
+                        const long long idx =
+                            ((long long)(kk * pa.flip_f + (pa.flip_f - 1 - r)) * pa.flip_f + (pa.flip_f - 1 - sx)) *
+                                pa.N + n;
+                        v[i] = __ldg(b0 + idx) + (b1 ? __ldg(b1 + idx) : 0);
+                    }
+                    continue;
+                }
                 if (pa.cpad) {
                     const int tap = k / pa.cpad, ch = k - tap * pa.cpad;
                     k = ch < pa.creal ? tap * pa.creal + ch : pa.Kreal;  // padding channels: 0
@@ -1230,6 +1242,22 @@ int plan_conv(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout
 
 bool wgrad_implicit_applies(int batch, int stride) { return stride == 1 && batch % 16 == 0 && wgt_enabled(); }
 
+int plan_dgrad_flip(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad) {
+    memset(&p, 0, sizeof(p));
+    if (stride != 1 || pad < 0 || pad > f - 1 || H + 2 * pad < f || W + 2 * pad < f)
+        return set_error(c, PG_ERR_UNSUPPORTED, "flipped input gradient: stride %d, pad %d", stride, pad);
+    const int P = H + 2 * pad - f + 1, Q = W + 2 * pad - f + 1;
+    // dX[n][h][w][c] = sum over (r', s', k) of dY[n][h - (f-1-pad) + r'][w - (f-1-pad) + s'][k] W[k][f-1-r'][f-1-s'][c]
+    int st = plan_conv(c, p, batch, P, Q, f, Dout, Din, 1, f - 1 - pad);
+    if (st) return st;
+    if (!p.implicit || p.P != H || p.Q != W) {
+        memset(&p, 0, sizeof(p));
+        return set_error(c, PG_ERR_UNSUPPORTED, "flipped input gradient: not an implicit convolution");
+    }
+    p.flip_f = f;
+    return PG_OK;
+}
+
 int plan_wgrad(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad,
                bool implicit_ok) {
     memset(&p, 0, sizeof(p));
@@ -1357,7 +1385,7 @@ static std::string tune_key(const Plan &p) {
     char k[256];
     snprintf(k, sizeof(k), "%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d%s", p.implicit, p.src_mode, p.M, p.N, p.C,
              p.kblocks, p.ntiles_n, p.tiles_m, p.Wt, p.Ht, p.Nt, p.f, p.colmajor,
-             p.posmajor ? "/pos" : p.wgt ? "/wgt" : "");
+             p.posmajor ? (p.flip_f ? "/pos/flip" : "/pos") : p.wgt ? "/wgt" : p.flip_f ? "/flip" : "");
     return k;
 }
 
@@ -1531,7 +1559,11 @@ int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB) {
     pa.kn = p.tB_kn;
     pa.wg_pq = p.wgt ? (long long)p.P * p.Q : 0;
     pa.wg_batch = p.Nimg;
-    if (p.implicit && !p.wgt && p.C != p.Din) {
+    if (p.flip_f) {
+        pa.flip_f = p.flip_f;
+        pa.cpad = p.C;
+        pa.creal = p.Din;
+    } else if (p.implicit && !p.wgt && p.C != p.Din) {
         pa.cpad = p.C;
         pa.creal = p.Din;
     }
@@ -1858,6 +1890,21 @@ int limb3_rss_conv_u64(Ctx *c, const uint64_t *const A[6], const uint64_t *const
     if (op == PG_CONV_WGRAD && lt::wgrad_implicit_applies(batch, stride))
         cand.push_back(
             [&] { return limb3_rss_conv_impl(c, A, B, C, op, batch, H, W, f, Din, Dout, stride, pad, trunc, false); });
+    lt::Plan fp;
+    const std::string err0 = c->err;  // a flipped plan that does not apply is not an error of this call
+    const bool flip_ok = op == PG_CONV_DGRAD && lt::plan_dgrad_flip(c, fp, batch, H, W, f, Din, Dout, stride, pad) == PG_OK;
+    c->err = err0;
+    if (flip_ok) {
+        // the input gradient as a convolution of dY with the flipped filter (third candidate, timed like the others)
+        cand.push_back([&, fp] {
+            CSh6<uint64_t> ca, cb;
+            Sh6<uint64_t> co;
+            if (!load6(ca, A) || !load6(cb, B) || !load6(co, C))
+                return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+            if (trunc < 0 || trunc > 63) return set_error(c, PG_ERR_INVALID_ARG, "bad truncation %d", trunc);
+            return run_with_scratch(c, fp, A, B, C, nullptr, trunc);
+        });
+    }
     return run_picked(c, k, cand);
 }
 

@@ -32,6 +32,8 @@ struct Plan {
                         // 128 images, the image is stored batch-innermost (pixel (h * W + w) * Nimg + n), and
                         // the tile runs only the taps that fall inside the input (no zero-padding taps)
     int C8;             // wgt: image channels (Din, or Din rounded up to 8 when below 128)
+    int flip_f;         // > 0: the input gradient as a convolution of dY with the flipped filter (f x f, B = W[Dout]
+                        // [f][f][Din] read at tap (f-1-r, f-1-s) and transposed); 0: the weights as given
     int wgt;            // implicit weight gradient: rows (tap, c), K = output pixels x images (16 per stage);
                         // the image is the forward input as [seg][plane][h * W + w][n / 8][c][n % 8], a tile
                         // is 128 channels of one tap and runs only the output pixels whose tap lands inside
@@ -49,6 +51,9 @@ int plan_wgrad(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dou
                bool implicit_ok = true);
 // whether the implicit weight gradient applies (stride 1, a multiple of 16 images)
 bool wgrad_implicit_applies(int batch, int stride);
+// the input gradient of a stride-1 convolution as an implicit convolution of dY (P x Q x Dout, padded by
+// f - 1 - pad) with the flipped, transposed filter; PG_ERR_UNSUPPORTED where that is not an implicit plan
+int plan_dgrad_flip(Ctx *c, Plan &p, int batch, int H, int W, int f, int Din, int Dout, int stride, int pad);
 void choose_split(const Plan &p, int sms, int &split, int &chunks_per_split);
 size_t partial_bytes(const Plan &p, int split);
 // the split-K autotuner: partial bytes that every candidate fits in, and the

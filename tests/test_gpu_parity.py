@@ -227,6 +227,35 @@ def test_rss_fprop_padded_channels_limb_form(pg, batch, H, W, f, Din, Dout, stri
     ctx.close()
 
 
+@pytest.mark.parametrize("batch,H,W,f,Din,Dout,stride,pad", [(128, 4, 4, 3, 32, 48, 1, 1), (4, 10, 9, 3, 16, 24, 1, 1),
+                                                             (4, 12, 12, 5, 20, 50, 1, 0)])
+def test_rss_dgrad_flipped_filter_limb_form(pg, tmp_path, batch, H, W, f, Din, Dout, stride, pad):
+    """The input gradient as an implicit convolution of dY with the flipped,
+    transposed filter (the third form the set-up timing can pick; here forced
+    through a tuning-cache entry): position-major tiles at 128 images,
+    rectangle tiles below, and a valid convolution whose dY is padded by
+    f - 1 and whose 50 channels are zero-padded to 64."""
+    import torch
+
+    ctx = pg.Context(0, form=pg.FORM_LIMB_TC)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    cache = tmp_path / "tune.txt"
+    cache.write_text(f"pg-tune {sms}\nsform/conv/1/{batch}/{H}/{W}/{f}/{Din}/{Dout}/{stride}/{pad} 3 1\n")
+    ctx.tune_load(str(cache))
+    P, Q = (H + 2 * pad - f) // stride + 1, (W + 2 * pad - f) // stride + 1
+    A = orc.random_views(batch * P * Q * Dout, U64, 44)
+    B = orc.random_views(Dout * f * f * Din, U64, 45)
+    comm = orc.Comm()
+    want = orc.convolution(A, B, orc.DGRAD, batch, H, W, f, Din, Dout, stride, pad, 26, comm)
+    C = pg.empty_shares(want.shape[2])
+    pg.convolution(ctx, dev(pg, A), dev(pg, B), C, orc.DGRAD, batch, H, W, f, Din, Dout, stride, pad, 26)
+    ctx.sync()
+    assert np.array_equal(host(pg, C), want)
+    comm_equal(ctx, comm)
+    ctx.check_device_errors()
+    ctx.close()
+
+
 @pytest.mark.parametrize("batch,H,W,f,Din,Dout,stride,pad", [(8, 28, 28, 5, 1, 20, 1, 0), (64, 17, 17, 3, 3, 6, 2, 1),
                                                              (40, 10, 10, 3, 2, 30, 1, 1), (2, 3, 600, 3, 20, 4, 1, 1)])
 def test_rss_wgrad_small_output_u64_form(pg, batch, H, W, f, Din, Dout, stride, pad):
