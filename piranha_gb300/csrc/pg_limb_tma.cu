@@ -423,13 +423,14 @@ __host__ __device__ __forceinline__ uint32_t b_off(int row, int kc) {
     return (uint32_t)((row >> 3) * 256 + kc * 128 + (row & 7) * 16);
 }
 
-// One thread per (segment, K block, N tile, column, chunk of 8), with the
+// One thread per (party, K block, N tile, column, chunk of 8), with the
 // chunk and then the column varying fastest: a warp writes 512 contiguous
 // bytes of a digit plane (16 columns x both 8-element chunks) and reads runs
 // of consecutive columns (b[k * N + n]) or of consecutive k (b[n * K + k]).
-// Segment 2p holds y_p0 + y_p1 and segment 2p+1 holds y_p0 of party p.
+// Segment 2p holds y_p0 + y_p1 and segment 2p+1 holds y_p0 of party p; the
+// thread reads each of the party's two shares once and writes both segments.
 __global__ void pack_kernel(const __grid_constant__ PackArgs pa) {
-    const long long total = 6ll * pa.kblocks * pa.ntiles_n * BN * 2;
+    const long long total = 3ll * pa.kblocks * pa.ntiles_n * BN * 2;
     for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < total;
          u += (long long)gridDim.x * blockDim.x) {
         const int kc = (int)(u & 1);
@@ -438,43 +439,51 @@ __global__ void pack_kernel(const __grid_constant__ PackArgs pa) {
         const int nt = (int)(t % pa.ntiles_n);
         t /= pa.ntiles_n;
         const int kb = (int)(t % pa.kblocks);
-        const int seg = (int)(t / pa.kblocks);
+        const int p = (int)(t / pa.kblocks);
         const int n = nt * BN + row;
-        const int p = seg >> 1;
         const int k0 = kb * BK + kc * 8;
-        uint64_t v[8];
+        uint64_t v0[8], v1[8];  // y_p0, y_p1
 #pragma unroll
-        for (int i = 0; i < 8; i++) v[i] = 0;
+        for (int i = 0; i < 8; i++) v0[i] = v1[i] = 0;
         if (n < pa.N) {
-            const uint64_t *b0 = pa.b[2 * p], *b1 = (seg & 1) ? nullptr : pa.b[2 * p + 1];
+            const uint64_t *b0 = pa.b[2 * p], *b1 = pa.b[2 * p + 1];
 #pragma unroll
             for (int i = 0; i < 8; i++) {
                 int k = k0 + i;
+                long long idx = -1;
                 if (pa.flip_f) {
                     const int tap = k / pa.cpad, kk = k - tap * pa.cpad;
                     if (kk < pa.creal && tap < pa.flip_f * pa.flip_f) {
                         const int r = tap / pa.flip_f, sx = tap - r * pa.flip_f;
-                        const long long idx =
-                            ((long long)(kk * pa.flip_f + (pa.flip_f - 1 - r)) * pa.flip_f + (pa.flip_f - 1 - sx)) *
-                                pa.N + n;
-                        v[i] = __ldg(b0 + idx) + (b1 ? __ldg(b1 + idx) : 0);
+                        idx = ((long long)(kk * pa.flip_f + (pa.flip_f - 1 - r)) * pa.flip_f + (pa.flip_f - 1 - sx)) *
+                                  pa.N + n;
                     }
-                    continue;
+                } else {
+                    if (pa.cpad) {
+                        const int tap = k / pa.cpad, ch = k - tap * pa.cpad;
+                        k = ch < pa.creal ? tap * pa.creal + ch : pa.Kreal;  // padding channels: 0
+                    }
+                    if (k < pa.Kreal) {
+                        idx = pa.kn ? (long long)k * pa.N + n : (long long)n * pa.Kreal + k;
+                        if (pa.wg_pq) idx = ((long long)(k % pa.wg_batch) * pa.wg_pq + k / pa.wg_batch) * pa.N + n;
+                    }
                 }
-                if (pa.cpad) {
-                    const int tap = k / pa.cpad, ch = k - tap * pa.cpad;
-                    k = ch < pa.creal ? tap * pa.creal + ch : pa.Kreal;  // padding channels: 0
-                }
-                if (k < pa.Kreal) {
-                    long long idx = pa.kn ? (long long)k * pa.N + n : (long long)n * pa.Kreal + k;
-                    if (pa.wg_pq) idx = ((long long)(k % pa.wg_batch) * pa.wg_pq + k / pa.wg_batch) * pa.N + n;
-                    v[i] = __ldg(b0 + idx) + (b1 ? __ldg(b1 + idx) : 0);
+                if (idx >= 0) {
+                    v0[i] = __ldg(b0 + idx);
+                    v1[i] = __ldg(b1 + idx);
                 }
             }
         }
         uint4 pl[8];
-        digits8<8>(v, pl);
-        uint8_t *dst = pa.packB + (((long long)seg * pa.kblocks + kb) * pa.ntiles_n + nt) * B_STAGE_BYTES;
+#pragma unroll
+        for (int i = 0; i < 8; i++) v1[i] += v0[i];
+        digits8<8>(v1, pl);  // segment 2p: y_p0 + y_p1
+        uint8_t *dst = pa.packB + (((long long)(2 * p) * pa.kblocks + kb) * pa.ntiles_n + nt) * B_STAGE_BYTES;
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+            *reinterpret_cast<uint4 *>(dst + i * B_PLANE_BYTES + b_off(row, kc)) = pl[i];
+        digits8<8>(v0, pl);  // segment 2p + 1: y_p0
+        dst = pa.packB + (((long long)(2 * p + 1) * pa.kblocks + kb) * pa.ntiles_n + nt) * B_STAGE_BYTES;
 #pragma unroll
         for (int i = 0; i < 8; i++)
             *reinterpret_cast<uint4 *>(dst + i * B_PLANE_BYTES + b_off(row, kc)) = pl[i];
@@ -1568,7 +1577,7 @@ int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB) {
         pa.creal = p.Din;
     }
     pa.packB = (uint8_t *)packB;
-    const long long units = 6ll * p.ntiles_n * BN * p.kblocks * 2;
+    const long long units = 3ll * p.ntiles_n * BN * p.kblocks * 2;
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
     long long blocks = (units + 255) / 256;
     if (blocks > (long long)sms * 16) blocks = (long long)sms * 16;
