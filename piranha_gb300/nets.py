@@ -44,6 +44,63 @@ def vgg16(maxpool: bool = True):
     return L
 
 
+def from_model(doc: dict):
+    """Layer tuples of a model in the reference's model-file format (the JSON
+    of files/models/*.json: {"batch_size", "input_size", "num_classes",
+    "model": [{"layer": ...}, ...]}), read field by field as the reference's
+    loader reads them (src/util/model.cu:43-118: input_hw = (height, width),
+    only the first filter_hw / pool_hw entry). Returns (layers, meta) with meta
+    = {"name", "dataset", "batch_size", "input_size", "num_classes"}. Layer
+    normalisation ("ln") and residual blocks ("res") are outside this
+    library's layers and raise ValueError."""
+    layers = []
+    for i, l in enumerate(doc["model"]):
+        kind = l["layer"]
+        if kind == "fc":
+            layers.append(("fc", int(l["input_dim"]), int(l["output_dim"])))
+        elif kind == "relu":
+            layers.append(("relu", int(l["input_dim"])))
+        elif kind == "cnn":
+            H, W = (int(v) for v in l["input_hw"])
+            layers.append(("cnn", H, W, int(l["in_channels"]), int(l["out_channels"]), int(l["filter_hw"][0]),
+                           int(l["stride"]), int(l["padding"])))
+        elif kind in ("maxpool", "averagepool"):
+            H, W = (int(v) for v in l["input_hw"])
+            layers.append(("maxpool" if kind == "maxpool" else "avgpool", H, W, int(l["in_channels"]),
+                           int(l["pool_hw"][0]), int(l["stride"])))
+        else:
+            raise ValueError(f"layer {i}: {kind!r} is not one of this library's layers "
+                             "(fc, relu, cnn, maxpool, averagepool)")
+    meta = {k: doc.get(k) for k in ("name", "dataset", "batch_size", "input_size", "num_classes")}
+    return layers, meta
+
+
+def load_model(path: str):
+    """from_model of a model file (the reference's files/models/*.json format)."""
+    import json
+
+    with open(path) as f:
+        return from_model(json.load(f))
+
+
+def to_model(layers, batch_size: int = 128, name: str = "", dataset: str = "", num_classes: int = 10) -> dict:
+    """The reference's model-file dict of layer tuples (the inverse of from_model)."""
+    out = []
+    for L in layers:
+        if L[0] == "fc":
+            out.append({"layer": "fc", "input_dim": L[1], "output_dim": L[2]})
+        elif L[0] == "relu":
+            out.append({"layer": "relu", "input_dim": L[1]})
+        elif L[0] == "cnn":
+            out.append({"layer": "cnn", "input_hw": [L[1], L[2]], "in_channels": L[3], "out_channels": L[4],
+                        "filter_hw": [L[5], L[5]], "stride": L[6], "padding": L[7]})
+        else:
+            out.append({"layer": "maxpool" if L[0] == "maxpool" else "averagepool", "input_hw": [L[1], L[2]],
+                        "in_channels": L[3], "pool_hw": [L[4], L[4]], "stride": L[5]})
+    return {"name": name, "dataset": dataset, "batch_size": batch_size, "input_size": input_size(layers),
+            "num_classes": num_classes, "model": out}
+
+
 def input_size(layers):
     L = layers[0]
     if L[0] == "fc":

@@ -214,3 +214,27 @@ def test_limb_weights_repacked_after_capture(pg):
     ctx.check_device_errors()
     net.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("name", ["alexnet-cifar10", "minionn", "sarda", "lenet-norelu-avgpool"])
+@pytest.mark.parametrize("limb", [False, True])
+def test_reference_model_files_forward(pg, name, limb):
+    """Networks read from the reference's own model files (11x11 stride-4
+    and 5x5 convolutions, 3x3/2 and 2x2/1 average pools, 1x1 images, a
+    stride-2 2x2 convolution): every layer's shares equal the oracle's, in
+    the u64 and the limb form."""
+    import json
+    import os
+
+    models = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "models.json")))
+    layers = [tuple(L) for L in models[name]["layers"]]
+    params = netref.kaiming_uniform_params(layers, 51)
+    batch = 2
+    rng = np.random.default_rng(52)
+    x = orc.share_random(orc.encode(rng.uniform(0, 1, batch * models[name]["meta"]["input_size"])), seed=53)
+    want, want_outs = netref.forward(layers, params, x, batch, keep=True)
+    got, got_outs, _ = run_net(pg, layers, params, x, batch, form=pg.FORM_LIMB_TC if limb else pg.FORM_U64)
+    for i, (g, w) in enumerate(zip(got_outs, want_outs)):
+        assert np.array_equal(g, w), f"layer {i} {layers[i]}"
+    assert np.array_equal(got, want)
+
