@@ -429,8 +429,10 @@ def avgpool_layer_backward(delta, H, W, C, pool, batch, comm=None):
     delta = _views(delta, np.uint64)
     out = np.empty((3, 2, batch * H * W * C), dtype=np.uint64)
     comm = comm or Comm()
-    lib().or_avgpool_layer_backward_u64(_p(delta), ctypes.c_size_t(delta.shape[2]), _p(out), H, W, C, pool, batch,
-                                        comm.ptr())
+    if lib().or_avgpool_layer_backward_u64(_p(delta), ctypes.c_size_t(delta.shape[2]), _p(out), H, W, C, pool,
+                                           batch, comm.ptr()):
+        raise ValueError(f"averagepool backward: {delta.shape[2]} deltas x pool {pool}^2 exceed the "
+                         f"{batch * H * W * C}-element input gradient (overlapping pools)")
     return out
 
 

@@ -272,6 +272,9 @@ extern "C" int or_avgpool_layer_forward_u64(const uint64_t* in, uint64_t* out, i
 }
 extern "C" int or_avgpool_layer_backward_u64(const uint64_t* delta, size_t n, uint64_t* deltas, int H, int W, int C,
                                              int pool, int batch, uint64_t* comm) {
+    // the expansion writes n * pool^2 slots of the batch * H * W * C input
+    // gradient; overlapping pools (stride < pool) would write past it
+    if (n * (size_t)pool * pool > (size_t)batch * H * W * C) return 1;
     RSSV<uint64_t> D, O;
     load(D, delta, n);
     CommIO io(comm);

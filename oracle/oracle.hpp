@@ -793,6 +793,10 @@ void avgpool_layer_forward(const RSSV<T>& in, RSSV<T>& act, int H, int W, int C,
 // averagepool_expand_delta (convolution.cuh:195-208): delta element i is
 // copied to slots (i / C) * C * pool^2 + i % C + k * C, k < pool^2, of the
 // zeroed input gradient (the input layout for a global pool), then / pool^2.
+// The slots stay inside the input gradient only when delta.n * pool^2 <=
+// batch * H * W * C (pools that tile the image); the C entry point refuses
+// overlapping pools, for which the reference's kernel writes past its
+// buffer.
 template <typename T>
 void avgpool_layer_backward(const RSSV<T>& delta, RSSV<T>& deltas, int H, int W, int C, int pool, int batch,
                             Comm& comm) {

@@ -197,3 +197,100 @@ def test_train_host_buffers(pg):
             assert np.array_equal(gather(pg, b, bn), prm[1])
     net.close()
     ctx.close()
+
+
+def _model(name):
+    import json
+    import os
+
+    models = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "models.json")))
+    return models
+
+
+@pytest.mark.parametrize("name", ["minionn", "sarda", "lenet-norelu-avgpool"])
+@pytest.mark.parametrize("form", ["u64", "tc"])
+def test_reference_model_files_training_step(pg, name, form):
+    """Training steps of networks read from the reference's model files
+    (MiniONN, Sarda's 2x2 stride-2 convolution, LeNet with 2x2/2 average
+    pools) at batch 4: every output, gradient and updated parameter share
+    equals the oracle's."""
+    models = _model(name)
+    layers = [tuple(L) for L in models[name]["layers"]]
+    params = netref.kaiming_uniform_params(layers, 61)
+    batch = 4
+    rng = np.random.default_rng(62)
+    x = orc.share_random(orc.encode(rng.uniform(0, 1, batch * models[name]["meta"]["input_size"])), seed=63)
+    labels = one_hot_labels(batch, 10, 64)
+    outs, new_params, deltas, softmax = oracle_step(layers, params, x, labels, batch, 5)
+    ctx = pg.Context(0, form=pg.FORM_LIMB_TC if form == "tc" else pg.FORM_U64)
+    ctx.set_autotune(False)
+    net = make_net(pg, ctx, layers, params, batch)
+    net.train_step(pg.to_device(x), pg.to_device(labels), 5)
+    ctx.sync()
+    check_against_oracle(pg, net, layers, outs, new_params, deltas, softmax)
+    ctx.check_device_errors()
+    net.close()
+    ctx.close()
+
+
+def test_alexnet_training_refused_on_overlapping_average_pool(pg):
+    """AlexNet's first average pool overlaps (3x3, stride 2: 16 windows x 9 >
+    100 inputs). The reference's averagepool backward expands each delta into
+    pool^2 slots as for a pool that tiles the image and would write past its
+    input-gradient buffer; the library refuses the step with a status (before
+    any launch) and so does the oracle, while the forward runs."""
+    models = _model("alexnet-cifar10")
+    layers = [tuple(L) for L in models["alexnet-cifar10"]["layers"]]
+    params = netref.kaiming_uniform_params(layers, 81)
+    batch = 2
+    rng = np.random.default_rng(82)
+    x = orc.share_random(orc.encode(rng.uniform(0, 1, batch * 3072)), seed=83)
+    labels = one_hot_labels(batch, 10, 84)
+    with pytest.raises(ValueError, match="overlapping"):
+        oracle_step(layers, params, x, labels, batch, 5)
+    ctx = pg.Context(0, form=pg.FORM_U64)
+    ctx.set_autotune(False)
+    net = make_net(pg, ctx, layers, params, batch)
+    with pytest.raises(pg.PiranhaError, match="overlapping"):
+        net.train_step(pg.to_device(x), pg.to_device(labels), 5)
+    ctx.sync()
+    ctx.check_device_errors()
+    net.close()
+    # the context is still usable: a fresh network's forward equals the oracle's
+    net = make_net(pg, ctx, layers, params, batch)
+    out = pg.empty_shares(net.out_n)
+    net.forward(pg.to_device(x), out)
+    ctx.sync()
+    assert np.array_equal(pg.to_host(out).reshape(3, 2, -1), netref.forward(layers, params, x, batch))
+    net.close()
+    ctx.close()
+
+
+def test_training_step_flipped_input_gradient(pg, tmp_path):
+    """A training step whose convolutions' input gradients run as convolutions
+    of dY with the flipped filter (forced through tuning-cache entries), on
+    position-major tiles at 128 images: bit-exact against the oracle."""
+    import torch
+
+    layers = [("cnn", 8, 8, 16, 32, 3, 1, 1), ("relu", 2048), ("cnn", 8, 8, 32, 32, 3, 1, 1), ("relu", 2048),
+              ("fc", 2048, 10), ("relu", 10)]
+    params = netref.kaiming_uniform_params(layers, 71)
+    batch = 128
+    rng = np.random.default_rng(72)
+    x = orc.share_random(orc.encode(rng.uniform(0, 1, batch * 8 * 8 * 16)), seed=73)
+    labels = one_hot_labels(batch, 10, 74)
+    outs, new_params, deltas, softmax = oracle_step(layers, params, x, labels, batch, 5)
+    ctx = pg.Context(0, form=pg.FORM_LIMB_TC)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    cache = tmp_path / "tune.txt"
+    cache.write_text(f"pg-tune {sms}\nsform/conv/1/128/8/8/3/16/32/1/1 3 1\nsform/conv/1/128/8/8/3/32/32/1/1 3 1\n")
+    ctx.tune_load(str(cache))
+    ctx.set_autotune(False)
+    net = make_net(pg, ctx, layers, params, batch)
+    net.train_step(pg.to_device(x), pg.to_device(labels), 5)
+    ctx.sync()
+    check_against_oracle(pg, net, layers, outs, new_params, deltas, softmax)
+    ctx.check_device_errors()
+    net.close()
+    ctx.close()
+
