@@ -121,6 +121,7 @@ struct Args {
     int *err;
     uint64_t wait_ns;  // bound on every wait of the kernel
     int withhold;      // diagnostic: K stage (of each CTA's range) whose copies the producer never issues; -1: none
+    int lag;           // the low group's issuer issues stage t once the high group's has issued stage t + lag
 };
 
 struct __align__(16) Smem {
@@ -129,7 +130,8 @@ struct __align__(16) Smem {
     uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], done;  // [0] low group, [1] high group
     uint32_t tmem_base;
     int abort;
-    int never;  // stays 0: a wait that must not be cut short by the abort flag
+    int never;      // stays 0: a wait that must not be cut short by the abort flag
+    int hi_issued;  // stages whose MMAs the high group's issuer has issued
 };
 
 static size_t smem_bytes() { return sizeof(Smem) + 1024; }
@@ -507,6 +509,27 @@ __device__ __forceinline__ void flag_error(Smem &sm, const Args &g, int code) {
     if (g.err) atomicCAS(g.err, 0, code);
 }
 
+// The low group's issuer trails the high group's: it issues stage t only
+// once the high one has issued stage t + lag (both run one thread of
+// warpgroup 0). Then, while the high group waits for its accumulators to be
+// drained, the tensor pipe still holds the low group's MMAs of the stages
+// the high one has already passed, instead of running dry. A lag below the
+// ring depth cannot deadlock: the high issuer's stages up to t + lag are
+// loaded once the low one has released stage t + lag - STAGES < t. Bounded,
+// and cut short by the abort flag.
+__device__ __forceinline__ bool wait_issued(Smem &sm, int need, uint64_t limit_ns) {
+    const volatile int *hi = &sm.hi_issued;
+    if (*hi >= need) return true;
+    const uint64_t t0 = tc::globaltimer();
+    for (uint32_t it = 1;; it++) {
+        if (*hi >= need) return true;
+        if ((it & 63) == 0) {
+            if (*reinterpret_cast<volatile int *>(&sm.abort)) return false;
+            if (tc::globaltimer() - t0 > limit_ns) return false;
+        }
+    }
+}
+
 // The MMAs of one stage for the low diagonals 0-3 (columns 0-255): for A
 // digit plane i < 4 the B planes j = 0..3-i are adjacent in shared memory and
 // their products go to the adjacent accumulators of diagonals i..3, so one
@@ -673,6 +696,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         tc::mbar_init(tc::smem_u32(&sm.done), 2);
         sm.abort = 0;
         sm.never = 0;
+        sm.hi_issued = 0;
         tc::fence_mbar_init();
     }
     if (warp == W_MMA) {
@@ -832,10 +856,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     break;
                 }
                 tc::tc_fence_after();
+                if (gi == 0 && g.lag > 0 && !wait_issued(sm, t + g.lag < nst ? t + g.lag : nst, wait_ns)) {
+                    flag_error(sm, g, 0x320);
+                    break;
+                }
                 const uint64_t off = (uint64_t)(((t % STAGES) * STAGE_BYTES) >> 4);
                 if (gi == 0) issue_lo(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
                 else issue_hi(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
                 if (t < nst - STAGES) tc::mma_commit(tc::smem_u32(&sm.empty[t % STAGES]));
+                if (gi == 1) *reinterpret_cast<volatile int *>(&sm.hi_issued) = t + 1;
                 if (t + 1 == cend) {
                     tc::mma_commit(tc::smem_u32(&sm.acc_full[gi]));
                     chunk++;
@@ -1185,6 +1214,17 @@ static bool cpad_enabled() {
         return !(e && e[0] == '0');
     }();
     return on;
+}
+
+// Stages by which the low accumulator group's MMA issuer trails the high
+// group's (PG_LAG, 0..STAGES-1; 0 turns the lag off).
+static int issue_lag() {
+    static const int lag = [] {
+        const char *e = getenv("PG_LAG");
+        const int v = e && *e ? atoi(e) : 2;
+        return v < 0 ? 0 : v > STAGES - 1 ? STAGES - 1 : v;
+    }();
+    return lag;
 }
 
 // Output positions per image up to which a same convolution is tiled by
@@ -1664,6 +1704,7 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
     g.err = device_error_word(c);
     g.wait_ns = c->wait_ns;
     g.withhold = c->withhold_stage;
+    g.lag = issue_lag();
     if (split > 1 && !partial) return set_error(c, PG_ERR_INVALID_ARG, "split-K needs a partial buffer");
     // value shares by tensor-map stores: the network's convolutions (no bias,
     // zero shares kept, row-major output of an even width of at least one N tile)
