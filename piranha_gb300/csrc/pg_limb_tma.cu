@@ -122,6 +122,9 @@ struct Args {
     uint64_t wait_ns;  // bound on every wait of the kernel
     int withhold;      // diagnostic: K stage (of each CTA's range) whose copies the producer never issues; -1: none
     int lag;           // the low group's issuer issues stage t once the high group's has issued stage t + lag
+    int order;         // 1: narrow and wide MMAs interleaved within a group's stage (issue_lo / issue_hi)
+    int seg_block[6];  // digit-plane block of the image holding each K segment (the identity, or 0,1,1,2,2,0
+                       // for an image of a replicated sharing stored once per share)
 };
 
 struct __align__(16) Smem {
@@ -187,6 +190,8 @@ struct ImageArgs {
     int H, W, Din, f, stride, pad, P, Q;
     long long bi_n, bi_hw;  // ROWS, batch-innermost image: image row (h * W + w) * bi_n + n holds source row
                             // n * bi_hw + h * W + w (bi_n = 0: image row = source row)
+    int nseg;               // 6: a block per share buffer; 3: block b from party b's first share (a
+                            // replicated sharing stored once per share, run_image's shared flag)
     uint4 *img;
 };
 
@@ -197,7 +202,7 @@ struct ImageArgs {
 // image's channels are a multiple of 16).
 __global__ void image_kernel(const __grid_constant__ ImageArgs ia) {
     const int C16 = ia.C8 >> 1;
-    const long long total = 6ll * C16 * ia.pixels;
+    const long long total = (long long)ia.nseg * C16 * ia.pixels;
     for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < total;
          u += (long long)gridDim.x * blockDim.x)
 #pragma unroll 1
@@ -206,7 +211,7 @@ __global__ void image_kernel(const __grid_constant__ ImageArgs ia) {
         const long long t = u / ia.pixels;
         const int cb = 2 * (int)(t % C16) + half;
         const int seg = (int)(t / C16);
-        const uint64_t *a = ia.a[seg];
+        const uint64_t *a = ia.a[ia.nseg == 3 ? 2 * seg : seg];
         const int k0 = cb * 8;
         uint64_t v[8];
 #pragma unroll
@@ -343,6 +348,7 @@ struct ReluImageArgs {
     long long pixels, pixels_alloc;
     int C8;
     long long bi_n, bi_hw;  // batch-innermost image (see ImageArgs); 0: image pixel = NHWC pixel
+    int nseg;               // 6 or 3 plane blocks (see ImageArgs)
 };
 
 constexpr int RI_PIX = 16, RI_CH = 16, RI_PITCH = RI_PIX + 1;  // pitch 17: two-way bank conflicts at most
@@ -386,13 +392,14 @@ __global__ void __launch_bounds__(256) relu_image_kernel(const __grid_constant__
             for (int k = 0; k < 6; k++) zs[k][ch][pl] = z[k >> 1][k & 1];
         }
         __syncthreads();
-        if (t < 6 * 2 * RI_PIX) {
+        if (t < a.nseg * 2 * RI_PIX) {
             const int seg = t / (2 * RI_PIX), half = (t / RI_PIX) & 1, pl = t % RI_PIX;
+            const int sh = a.nseg == 3 ? 2 * seg : seg;
             const long long pix = p0 + pl;
             if (pix < a.pixels) {
                 uint64_t v[8];
 #pragma unroll
-                for (int i = 0; i < 8; i++) v[i] = zs[seg][half * 8 + i][pl];
+                for (int i = 0; i < 8; i++) v[i] = zs[sh][half * 8 + i][pl];
                 uint4 plv[8];
                 digits8<8>(v, plv);
                 const int cb = 2 * cp + half;
@@ -533,21 +540,34 @@ __device__ __forceinline__ bool wait_issued(Smem &sm, int need, uint64_t limit_n
 // The MMAs of one stage for the low diagonals 0-3 (columns 0-255): for A
 // digit plane i < 4 the B planes j = 0..3-i are adjacent in shared memory and
 // their products go to the adjacent accumulators of diagonals i..3, so one
-// MMA with N = 64 (4 - i) covers them. i = 0 writes all four accumulators.
+// MMA with N = 64 (4 - i) covers them. i = 0 writes all four accumulators,
+// so it comes first (it resets them at a chunk's first stage).
+// ORDER 1 issues the narrow MMAs between the wide ones (low: N = 256, 64,
+// 192, 128; high: 256, 64, 256, 128, 256, 192, 256, 256): a narrow MMA reads
+// more shared memory per tensor-pipe cycle than a wide one, and interleaved
+// they keep both busy (measured on the GB300: 1362 -> 1256 cycles per stage
+// for the stage mix without drains, 1574 -> 1525 with them).
+template <int ORDER>
 __device__ __forceinline__ void issue_lo(uint32_t acc, uint64_t adesc, uint32_t aplane16, uint64_t bdesc,
                                          bool first_stage) {
 #pragma unroll
-    for (int i = 0; i < 4; i++)
+    for (int ii = 0; ii < 4; ii++) {
+        const int i = ORDER ? (ii == 0 ? 0 : ii == 1 ? 3 : ii == 2 ? 1 : 2) : ii;
         tc::mma_f16(acc + (uint32_t)(i * BN), adesc + (uint64_t)(i * aplane16), bdesc,
                     tc::idesc_f16_f32(BM, BN * (4 - i)), (!first_stage || i > 0) ? 1u : 0u);
+    }
 }
 
 // The MMAs of one stage for the high diagonals 4-7 (columns 256-511): for A
 // plane i the B planes j = max(0, 4-i)..7-i, one MMA each (8 per stage).
+template <int ORDER>
 __device__ __forceinline__ void issue_hi(uint32_t acc, uint64_t adesc, uint32_t aplane16, uint64_t bdesc,
                                          bool first_stage) {
 #pragma unroll
-    for (int i = 0; i < 8; i++) {
+    for (int ii = 0; ii < 8; ii++) {
+        const int i = ORDER ? (ii == 0 ? 0 : ii == 1 ? 7 : ii == 2 ? 1 : ii == 3 ? 6 : ii == 4 ? 2 : ii == 5 ? 5
+                                                                                    : ii == 6 ? 3 : 4)
+                            : ii;
         const int jlo = 4 - i > 0 ? 4 - i : 0;
         const int cnt = 8 - i < 4 ? 8 - i : 4;
         tc::mma_f16(acc + (uint32_t)((i + jlo) * BN), adesc + (uint64_t)(i * aplane16),
@@ -816,7 +836,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 const uint32_t bar = tc::smem_u32(&sm.full[s]);
                 tc::mbar_arrive_expect_tx(bar, 8 * g.a_box_bytes + B_STAGE_BYTES);
                 const uint32_t dst = tc::smem_u32(sm.stage[s]);
-                tma_load_5d(dst, &tmA, x, y, zc, c3, seg * 8, bar);
+                tma_load_5d(dst, &tmA, x, y, zc, c3, g.seg_block[seg] * 8, bar);
                 const uint8_t *src = g.packB + ((size_t)gst * g.ntiles_n + blockIdx.x) * B_STAGE_BYTES;
                 tc::bulk_g2s(dst + 8 * A_PLANE_BYTES, src, B_STAGE_BYTES, bar);
             }
@@ -861,8 +881,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     break;
                 }
                 const uint64_t off = (uint64_t)(((t % STAGES) * STAGE_BYTES) >> 4);
-                if (gi == 0) issue_lo(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
-                else issue_hi(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
+                if (gi == 0) {
+                    if (g.order) issue_lo<1>(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
+                    else issue_lo<0>(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
+                } else {
+                    if (g.order) issue_hi<1>(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
+                    else issue_hi<0>(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
+                }
                 if (t < nst - STAGES) tc::mma_commit(tc::smem_u32(&sm.empty[t % STAGES]));
                 if (gi == 1) *reinterpret_cast<volatile int *>(&sm.hi_issued) = t + 1;
                 if (t + 1 == cend) {
@@ -1217,14 +1242,29 @@ static bool cpad_enabled() {
 }
 
 // Stages by which the low accumulator group's MMA issuer trails the high
-// group's (PG_LAG, 0..STAGES-1; 0 turns the lag off).
+// group's (PG_LAG, 0..STAGES-1; 0 turns the lag off). Measured on one GB300
+// with the same tuned plans (VGG16 b128 img/s, 4096^3 share-GEMM T
+// ring-MAC/s): order 0 lag 2 12.84k / 22.36 T, order 0 lag 1 12.91k /
+// 23.18 T, order 1 lag 2 12.99k / 22.60 T, order 1 lag 1 13.10k / 23.48 T.
+// On another, order 0: lag 0 12.06k, lag 1 12.99k, lag 2 12.98k, lag 3
+// 11.03k (a lag of the ring depth less one starves the low group).
 static int issue_lag() {
     static const int lag = [] {
         const char *e = getenv("PG_LAG");
-        const int v = e && *e ? atoi(e) : 2;
+        const int v = e && *e ? atoi(e) : 1;
         return v < 0 ? 0 : v > STAGES - 1 ? STAGES - 1 : v;
     }();
     return lag;
+}
+
+// MMA order within a group's stage (PG_ORDER: 1 interleaved, 0 by A plane;
+// measured with issue_lag).
+static int issue_order() {
+    static const int order = [] {
+        const char *e = getenv("PG_ORDER");
+        return e && *e == '0' ? 0 : 1;
+    }();
+    return order;
 }
 
 // Output positions per image up to which a same convolution is tiled by
@@ -1519,7 +1559,7 @@ bool relu_image_fits(const Plan &p, size_t n) {
 }
 
 int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n, uint64_t *const out[6],
-                   uint8_t *const dout[6], void *image) {
+                   uint8_t *const dout[6], void *image, bool shared) {
     if (!relu_image_fits(p, n)) return set_error(c, PG_ERR_INVALID_ARG, "relu/image geometry mismatch");
     ReluImageArgs a;
     memset(&a, 0, sizeof(a));
@@ -1535,6 +1575,7 @@ int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n,
     a.C8 = p.C / 8;
     a.bi_n = p.posmajor ? p.Nimg : 0;
     a.bi_hw = (long long)p.Himg * p.Wimg;
+    a.nseg = shared ? 3 : 6;
     const long long tiles = (long long)(a.C8 / 2) * ((p.pixels + RI_PIX - 1) / RI_PIX);
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
     long long blocks = tiles < (long long)sms * 16 ? tiles : (long long)sms * 16;
@@ -1543,7 +1584,8 @@ int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n,
     return launch_status(c, "relu_image_kernel");
 }
 
-int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image) {
+int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image, bool shared) {
+    if (shared && p.wgt) return set_error(c, PG_ERR_INVALID_ARG, "the weight-gradient image keeps six segments");
     if (p.wgt) {
         WgtImageArgs wa;
         memset(&wa, 0, sizeof(wa));
@@ -1583,9 +1625,10 @@ int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image) {
     ia.P = p.cP; ia.Q = p.cQ;
     ia.bi_n = p.posmajor ? p.Nimg : 0;
     ia.bi_hw = (long long)p.Himg * p.Wimg;
+    ia.nseg = shared ? 3 : 6;
     ia.img = (uint4 *)image;
     if (ia.C8 & 1) return set_error(c, PG_ERR_INVALID_ARG, "image channels %d are not a multiple of 16", p.C);
-    const long long units = 6ll * (ia.C8 / 2) * p.pixels_alloc;
+    const long long units = (long long)ia.nseg * (ia.C8 / 2) * p.pixels_alloc;
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
     long long blocks = (units + 255) / 256;
     if (blocks > (long long)sms * 32) blocks = (long long)sms * 32;
@@ -1627,7 +1670,9 @@ int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB) {
 }
 
 int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial, int split, int cps,
-             uint64_t *const out[6], const uint64_t *const bias[6], int trunc, bool zeros_kept, uint64_t *raw) {
+             uint64_t *const out[6], const uint64_t *const bias[6], int trunc, bool zeros_kept, uint64_t *raw,
+             bool shared) {
+    if (shared && p.wgt) return set_error(c, PG_ERR_INVALID_ARG, "the weight-gradient image keeps six segments");
     {
         int st = prepare_device(c);
         if (st) return st;
@@ -1705,6 +1750,8 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
     g.wait_ns = c->wait_ns;
     g.withhold = c->withhold_stage;
     g.lag = issue_lag();
+    g.order = issue_order();
+    for (int s = 0; s < 6; s++) g.seg_block[s] = shared ? ((s + 1) >> 1) % 3 : s;
     if (split > 1 && !partial) return set_error(c, PG_ERR_INVALID_ARG, "split-K needs a partial buffer");
     // value shares by tensor-map stores: the network's convolutions (no bias,
     // zero shares kept, row-major output of an even width of at least one N tile)

@@ -65,21 +65,25 @@ std::string plan_key(const Plan &p);
 int tune_split(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial,
                uint64_t *const out[6], const uint64_t *const bias[6], int trunc, bool zeros_kept, uint64_t *raw,
                int &split, int &chunks_per_split);
-// A shares -> digit-plane image; weight shares -> packed stage images; then the GEMM (+ split-K reduction)
-int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image);
+// A shares -> digit-plane image; weight shares -> packed stage images; then the GEMM (+ split-K reduction).
+// shared (run_image, run_relu_image, run_gemm): the six share buffers hold a replicated sharing (party p's
+// second share equals party p+1's first, bit for bit), so the image stores each of the three shares once
+// (block b = party b's first share) and the GEMM reads segment s (party s/2's share s%2) from block
+// ((s + 1) / 2) % 3; the image producer and the GEMM must agree on it.
+int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image, bool shared = false);
 int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB);
 // ReLU of n values fused with the digit image of the implicit convolution
 // (plan p) that takes them as input; relu_image_fits says whether it applies
 bool relu_image_fits(const Plan &p, size_t n);
 int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n, uint64_t *const out[6],
-                   uint8_t *const dout[6], void *image);
+                   uint8_t *const dout[6], void *image, bool shared = false);
 // zeros_kept: the four output shares that dividePublic3out3 leaves at 0 (all
 // but party A's shareA and party C's shareB) already hold 0 and are only
 // written where a bias share is added (the network's zeroed arena).
 // raw: write the untruncated Z (M x N, row-major) there instead of shares.
 int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial, int split,
              int chunks_per_split, uint64_t *const out[6], const uint64_t *const bias[6], int trunc,
-             bool zeros_kept = false, uint64_t *raw = nullptr);
+             bool zeros_kept = false, uint64_t *raw = nullptr, bool shared = false);
 
 }  // namespace lt
 }  // namespace pg

@@ -55,6 +55,7 @@ struct NetLayer {
     int split, cps;
     uint8_t *packB;
     int u64 = 0;  // the plain u64 form timed faster for this layer at set-up (small layers)
+    bool b_replicated = true;  // the bias shares are a replicated sharing (checked by pg_net_set_params)
 };
 
 struct pg_net {
@@ -228,9 +229,14 @@ static int net_limb_setup(pg_net *net) {
 // One FC / CNN layer in the limb form: digit image of the input, GEMM over
 // the packed weights (+ split-K reduction), then the message accounting of
 // matmul / convolution (RSS.inl:517-538, :790-802).
-static int net_limb_layer(pg_net *net, NetLayer &L, const uint64_t *const *in, bool image_ready = false) {
+// shared: the input's six buffers hold a replicated sharing (every layer
+// output of the network does: an FC / CNN output is [v, 0, 0, 0, 0, v], and
+// the ReLU, maxpool and averagepool steps keep a replicated sharing
+// replicated), so the digit image stores each of the three shares once.
+static int net_limb_layer(pg_net *net, NetLayer &L, const uint64_t *const *in, bool image_ready = false,
+                          bool shared = false) {
     Ctx *c = net->ctx;
-    int st = image_ready ? PG_OK : lt::run_image(c, L.plan, in, net->limb_image);
+    int st = image_ready ? PG_OK : lt::run_image(c, L.plan, in, net->limb_image, shared);
     if (st) return st;
     const uint64_t *const *bias = L.b_n ? (const uint64_t *const *)L.b : nullptr;
     // The arena is zeroed when the network is created and a layer's output
@@ -238,7 +244,7 @@ static int net_limb_layer(pg_net *net, NetLayer &L, const uint64_t *const *in, b
     // shares that dividePublic3out3 leaves at 0 stay 0: write only the two
     // value shares.
     st = lt::run_gemm(c, L.plan, net->limb_image, L.packB, L.split > 1 ? net->limb_partial : nullptr, L.split, L.cps,
-                      L.out, bias, net->fp, bias == nullptr);
+                      L.out, bias, net->fp, bias == nullptr, nullptr, shared);
     if (st) return st;
     const uint64_t n_out = (uint64_t)L.plan.M * L.plan.N;
     comm_msg(c, 2 * n_out * 8, 2 * n_out * 8);
@@ -338,6 +344,10 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
         if (st) return st;
     }
     bool ready_next = false;  // the previous ReLU wrote this layer's digit image
+    // The network's input is taken as six independent buffers; an FC / CNN
+    // output is a replicated sharing ([v, 0, 0, 0, 0, v] plus the bias shares,
+    // when those are replicated too), and the layers after it keep it so.
+    bool replicated = false;
     for (size_t li = 0; li < net->layers.size(); li++) {
         NetLayer &L = net->layers[li];
         int st = PG_OK;
@@ -348,14 +358,15 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
             case PG_LAYER_FC: {
                 const uint64_t *const *bias = L.b_n ? (const uint64_t *const *)L.b : nullptr;
                 st = c->form == PG_FORM_LIMB_TC
-                         ? (L.u64 ? net_u64_layer(net, L, cur) : net_limb_layer(net, L, cur))
+                         ? (L.u64 ? net_u64_layer(net, L, cur) : net_limb_layer(net, L, cur, false, replicated))
                          : rss_matmul<uint64_t>(c, cur, (const uint64_t *const *)L.w, L.out, bias, net->batch, L.p[1],
                                                 L.p[0], 1, 1, 1, net->fp);
                 break;
             }
             case PG_LAYER_CNN:
                 st = c->form == PG_FORM_LIMB_TC
-                         ? (L.u64 ? net_u64_layer(net, L, cur) : net_limb_layer(net, L, cur, image_ready))
+                         ? (L.u64 ? net_u64_layer(net, L, cur)
+                                  : net_limb_layer(net, L, cur, image_ready, replicated))
                          : rss_conv<uint64_t>(c, cur, (const uint64_t *const *)L.w, L.out, PG_CONV_FPROP, net->batch,
                                               L.p[0], L.p[1], L.p[4], L.p[2], L.p[3], L.p[5], L.p[6], net->fp);
                 break;
@@ -365,7 +376,7 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
                 NetLayer *next = li + 1 < net->layers.size() ? &net->layers[li + 1] : nullptr;
                 if (c->form == PG_FORM_LIMB_TC && net->limb_arena && next && next->type == PG_LAYER_CNN &&
                     !next->u64 && lt::relu_image_fits(next->plan, L.in_n)) {
-                    st = lt::run_relu_image(c, next->plan, cur, L.in_n, L.out, L.d, net->limb_image);
+                    st = lt::run_relu_image(c, next->plan, cur, L.in_n, L.out, L.d, net->limb_image, replicated);
                     if (!st) count_relu_u64_u8(c, L.in_n);
                     ready_next = !st;
                 } else {
@@ -384,6 +395,7 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
         }
         if (st) return st;
         if (!net->ev.empty() && (st = record_event(c, net->ev[2 * li + 1]))) return st;
+        if (L.type == PG_LAYER_FC || L.type == PG_LAYER_CNN) replicated = !L.b_n || L.b_replicated;
         cur = L.out;
     }
     return PG_OK;
@@ -824,9 +836,32 @@ int pg_net_set_params(pg_net *net, int layer, const uint64_t *const w[6], const 
         for (int k = 0; k < 6; k++)
             PG_CHECK_CUDA(c, cudaMemcpyAsync(L.w[k], w[k], L.w_n * 8, cudaMemcpyDeviceToDevice, c->stream));
     }
-    if (L.b_n && bias)
+    if (L.b_n && bias) {
         for (int k = 0; k < 6; k++)
             PG_CHECK_CUDA(c, cudaMemcpyAsync(L.b[k], bias[k], L.b_n * 8, cudaMemcpyDeviceToDevice, c->stream));
+        // whether the layer's outputs stay a replicated sharing: party p's
+        // second bias share equals party p+1's first
+        std::vector<uint64_t> hb(6 * L.b_n);
+        for (int k = 0; k < 6; k++)
+            PG_CHECK_CUDA(c, cudaMemcpyAsync(hb.data() + k * L.b_n, bias[k], L.b_n * 8, cudaMemcpyDeviceToHost,
+                                             c->stream));
+        PG_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+        bool rep = true;
+        for (int p = 0; p < 3 && rep; p++)
+            rep = memcmp(hb.data() + (2 * p + 1) * L.b_n, hb.data() + ((2 * p + 2) % 6) * L.b_n, L.b_n * 8) == 0;
+        if (rep != L.b_replicated) {
+            // captured steps chose their image layouts with the old flag
+            if (net->exec) cudaGraphExecDestroy(net->exec);
+            if (net->graph) cudaGraphDestroy(net->graph);
+            if (net->exec_train) cudaGraphExecDestroy(net->exec_train);
+            if (net->graph_train) cudaGraphDestroy(net->graph_train);
+            net->exec = nullptr;
+            net->graph = nullptr;
+            net->exec_train = nullptr;
+            net->graph_train = nullptr;
+        }
+        L.b_replicated = rep;
+    }
     // the limb form keeps the weights packed: repack this layer's
     if (net->limb_arena && L.packB) {
         int st = lt::run_pack(c, L.plan, (const uint64_t *const *)L.w, L.packB);

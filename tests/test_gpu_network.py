@@ -238,3 +238,30 @@ def test_reference_model_files_forward(pg, name, limb):
         assert np.array_equal(g, w), f"layer {i} {layers[i]}"
     assert np.array_equal(got, want)
 
+
+
+@pytest.mark.parametrize("replicated_bias", [False, True])
+def test_fc_fed_by_a_biased_fc(pg, replicated_bias):
+    """An FC layer whose input comes straight from a biased FC layer. With
+    the reference's setPublic bias (its PARTY_B fall-through leaves party B
+    holding (0, b), not a replicated sharing) the first layer's output is not
+    replicated, and the second layer's digit image keeps all six share
+    buffers; with a replicated bias it stores each share once. Both equal the
+    oracle's per-party computation, share for share."""
+    rng = np.random.default_rng(61)
+    layers = [("fc", 256, 128), ("fc", 128, 64), ("relu", 64), ("fc", 64, 32)]
+    params = []
+    for L in layers:
+        if L[0] != "fc":
+            params.append(None)
+            continue
+        w = rng.uniform(-1, 1, L[1] * L[2]) * np.sqrt(6.0 / L[1])
+        b = orc.set_public(rng.uniform(-0.1, 0.1, L[2]), ref_compat=not replicated_bias)
+        params.append((orc.set_public(w), b))
+    batch = 128
+    x = orc.share_random(orc.encode(rng.uniform(0, 1, batch * 256)), seed=62)
+    want, want_outs = netref.forward(layers, params, x, batch, keep=True)
+    got, got_outs, _ = run_net(pg, layers, params, x, batch, form=pg.FORM_LIMB_TC)
+    for i, (g, w) in enumerate(zip(got_outs, want_outs)):
+        assert np.array_equal(g, w), f"layer {i} {layers[i]}"
+    assert np.array_equal(got, want)
