@@ -1423,17 +1423,20 @@ size_t partial_bytes(const Plan &p, int split) { return split > 1 ? (size_t)spli
 
 // ---------------------------------------------------------- autotuner
 
-// Split-K candidates of a plan: the heuristic split, 1, 2, 3, 4, 6, 8, 12,
-// 16, and doublings up to 4x the heuristic (at most 64), none above the
-// number of K chunks; each normalised so that every split holds at least one
-// chunk. Returns how many (at most 12).
-static int split_candidates(const Plan &p, int sms, int (&sp)[12], int (&cp)[12]) {
+// Split-K candidates of a plan: the heuristic split, 1-8, 10, 12, 14, 16,
+// and doublings up to 4x the heuristic (at most 64), none above the number
+// of K chunks; each normalised so that every split holds at least one chunk.
+// The odd splits let a grid of tiles x split CTAs come closer to a whole
+// number of waves (4x4 x 512 channels: 128 tiles, 6 -> 5.05 waves, 7 -> 5.9).
+// Returns how many (at most MAX_SPLIT_CAND).
+constexpr int MAX_SPLIT_CAND = 16;
+static int split_candidates(const Plan &p, int sms, int (&sp)[MAX_SPLIT_CAND], int (&cp)[MAX_SPLIT_CAND]) {
     const int chunks = (6 * p.kblocks + CHUNK_STAGES - 1) / CHUNK_STAGES;
     int h, hc;
     choose_split(p, sms, h, hc);
     int n = 0;
     auto add = [&](int s) {
-        if (s < 1 || s > chunks || n >= 12) return;
+        if (s < 1 || s > chunks || n >= MAX_SPLIT_CAND) return;
         const int c = (chunks + s - 1) / s;
         const int s2 = (chunks + c - 1) / c;
         for (int i = 0; i < n; i++)
@@ -1443,14 +1446,14 @@ static int split_candidates(const Plan &p, int sms, int (&sp)[12], int (&cp)[12]
         n++;
     };
     add(h);
-    for (int s : {1, 2, 3, 4, 6, 8, 12, 16}) add(s);
+    for (int s : {1, 2, 3, 4, 5, 6, 7, 8, 10, 12, 14, 16}) add(s);
     const int cap = 4 * h < 64 ? 4 * h : 64;
     for (int s = 32; s <= cap; s *= 2) add(s);
     return n;
 }
 
 size_t tune_partial_bytes(const Plan &p, int sms) {
-    int sp[12], cp[12];
+    int sp[MAX_SPLIT_CAND], cp[MAX_SPLIT_CAND];
     const int n = split_candidates(p, sms, sp, cp);
     size_t b = 0;
     for (int i = 0; i < n; i++) b = partial_bytes(p, sp[i]) > b ? partial_bytes(p, sp[i]) : b;
@@ -1501,7 +1504,7 @@ int tune_split(Ctx *c, const Plan &p, const void *image, const void *packB, uint
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     PG_CHECK_CUDA(c, cudaStreamIsCapturing(c->stream, &cs));
     if (!c->autotune || cs != cudaStreamCaptureStatusNone) return PG_OK;
-    int sp[12], cp[12];
+    int sp[MAX_SPLIT_CAND], cp[MAX_SPLIT_CAND];
     const int n = split_candidates(p, sms, sp, cp);
     if (n <= 1) {
         c->split_cache[key] = {split, cps};
