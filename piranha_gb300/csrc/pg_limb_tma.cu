@@ -50,6 +50,8 @@
 #include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 
+#include <algorithm>
+#include <climits>
 #include <cstdlib>
 #include <functional>
 #include <vector>
@@ -104,6 +106,7 @@ struct Args {
     int Himg, Wimg;
     int rows_mode;  // 1: the image holds one row per output row (GEMM, im2col)
     int ntiles_n, total_stages, chunks_per_split;
+    int tiles_m, nsplit, n_items;  // row tiles; K' slices; work items (ntiles_n x tiles_m x nsplit)
     int direct, colmajor;
     int posmajor;  // tiles by output position (Plan::posmajor); H, W: input extents then
     int wgt;       // implicit weight gradient (Plan::wgt): a tile is 128 input channels of one filter tap
@@ -653,8 +656,8 @@ __device__ __forceinline__ void stage_row(const Args &g, uint64_t *stg, long lon
     }
 }
 
-__device__ __forceinline__ void store_tile(const Args &g, int z, const uint64_t *stg, const long long *mrow, int te) {
-    const int nbase = blockIdx.x * BN;
+__device__ __forceinline__ void store_tile(const Args &g, int z, int nbase, const uint64_t *stg, const long long *mrow,
+                                           int te) {
     const int ncols = g.N - nbase < BN ? g.N - nbase : BN;
     if (!g.direct) {
         for (int e = te; e < BM * BN; e += 256) {
@@ -691,9 +694,151 @@ __device__ __forceinline__ void tma_store_4d(const CUtensorMap *map, uint32_t sr
                  : "memory");
 }
 
+// One work item of the kernel: an output tile (N tile bx, row tile by) and
+// its K' slice z, with the tile's geometry and its stage range. Items are
+// numbered bx fastest, then by, then z; a CTA takes items blockIdx.x,
+// blockIdx.x + gridDim.x, ... (one item per CTA when the grid holds them
+// all, a loop over items when the grid is one CTA per SM).
+struct Item {
+    int bx, by, z;
+    int tw, t2, w0, h0, n0;
+    int r_lo, s_lo, ns, tile_stages, stage_begin, nst;
+};
+
+__host__ __device__ __forceinline__ void item_geometry(const Args &g, int item, Item &it) {
+    it.bx = item % g.ntiles_n;
+    const int rest = item / g.ntiles_n;
+    it.by = rest % g.tiles_m;
+    it.z = rest / g.tiles_m;
+    it.tw = it.by % g.tiles_w;
+    it.t2 = it.by / g.tiles_w;
+    const int th = it.t2 % g.tiles_h, tn = it.t2 / g.tiles_h;
+    it.w0 = it.tw * g.Wt;
+    it.h0 = th * g.Ht;
+    it.n0 = tn * g.Nt;
+    // Position-major tiles (output pixel (h0, w0) of Nt images) run only the
+    // taps inside the input: rows r_lo..r_lo+nr-1, columns s_lo..s_lo+ns-1 of
+    // the filter. Their K' range (6 segments x taps x channel blocks) is split
+    // evenly over the nsplit slices.
+    it.r_lo = 0;
+    it.s_lo = 0;
+    it.ns = 1;
+    it.tile_stages = g.total_stages;
+    if (g.wgt) {
+        // Weight gradient of filter tap (r, s) = t2 for input channels tw *
+        // 128 ...: K runs over the output pixels (p, q) whose input pixel
+        // (p + r - pad, q + s - pad) is inside the image (rows r_lo...,
+        // columns s_lo..s_lo+ns-1) and 16 images per stage.
+        const int tap = it.t2, r = tap / g.f, sx = tap - r * g.f;
+        it.r_lo = g.pad - r > 0 ? g.pad - r : 0;
+        const int p_hi = g.Himg - 1 + g.pad - r < g.P - 1 ? g.Himg - 1 + g.pad - r : g.P - 1;
+        it.s_lo = g.pad - sx > 0 ? g.pad - sx : 0;
+        const int q_hi = g.Wimg - 1 + g.pad - sx < g.Q - 1 ? g.Wimg - 1 + g.pad - sx : g.Q - 1;
+        it.ns = q_hi - it.s_lo + 1;
+        it.tile_stages = (p_hi >= it.r_lo && it.ns > 0) ? 6 * (p_hi - it.r_lo + 1) * it.ns * g.nb16 : 0;
+    } else if (g.posmajor) {
+        it.r_lo = g.pad - it.h0 > 0 ? g.pad - it.h0 : 0;
+        const int r_hi = g.Himg - 1 + g.pad - it.h0 < g.f - 1 ? g.Himg - 1 + g.pad - it.h0 : g.f - 1;
+        it.s_lo = g.pad - it.w0 > 0 ? g.pad - it.w0 : 0;
+        const int s_hi = g.Wimg - 1 + g.pad - it.w0 < g.f - 1 ? g.Wimg - 1 + g.pad - it.w0 : g.f - 1;
+        it.ns = s_hi - it.s_lo + 1;
+        it.tile_stages = 6 * (r_hi - it.r_lo + 1) * it.ns * g.cblocks;
+    }
+    int stage_end;
+    if (g.posmajor || g.wgt) {
+        const int per = (it.tile_stages + g.nsplit - 1) / g.nsplit;
+        it.stage_begin = it.z * per;
+        stage_end = it.stage_begin + per;
+    } else {
+        it.stage_begin = it.z * g.chunks_per_split * CHUNK_STAGES;
+        stage_end = it.stage_begin + g.chunks_per_split * CHUNK_STAGES;
+    }
+    if (stage_end > it.tile_stages) stage_end = it.tile_stages;
+    it.nst = stage_end > it.stage_begin ? stage_end - it.stage_begin : 0;
+}
+
+// The CTAs' item lists, balanced on the host: items taken longest first
+// (by stage count), each given to the CTA with the fewest stages so far, so
+// that position-major tiles of 4, 6 and 9 taps, split-K slices and
+// weight-gradient taps of different lengths even out across the CTAs (a
+// round-robin deal left some CTAs with more long tiles: the 8x8x256
+// convolutions of VGG16 1.10 -> 1.13 ms). CTA b runs order[start[b]] ..
+// order[start[b+1] - 1]; n == 0: round-robin (item b, b + gridDim.x, ...).
+constexpr int SCHED_MAX_CTAS = 256, SCHED_MAX_ITEMS = 8192;
+struct Sched {
+    int n;
+    uint16_t start[SCHED_MAX_CTAS + 1];
+    uint16_t order[SCHED_MAX_ITEMS];
+};
+
+// k-th item of this CTA, or -1
+__device__ __forceinline__ int cta_item(const Sched &sc, const Args &g, int k) {
+    if (sc.n) {
+        const int i = sc.start[blockIdx.x] + k;
+        return i < sc.start[blockIdx.x + 1] ? sc.order[i] : -1;
+    }
+    const long long item = blockIdx.x + (long long)k * gridDim.x;
+    return item < g.n_items ? (int)item : -1;
+}
+
+// The stage count of an item alone (for the MMA issuers, which need nothing else).
+__device__ __forceinline__ int item_nst(const Args &g, int item) {
+    Item it;
+    item_geometry(g, item, it);
+    return it.nst;
+}
+
+// A tile's output straight from the epilogue thread's registers (row m,
+// columns nb .. nb+31 of its half), while the stage ring already holds the
+// next item's operands: 16-byte stores of a row's consecutive columns where
+// the row is 16-byte aligned, one column per store for a column-major output
+// (the warp's 32 consecutive rows make those coalesced).
+__device__ __forceinline__ void put_row(uint64_t *dst, int ncols, const uint64_t (&v)[32], const uint64_t *b) {
+    if (!b && ncols == 32 && !((uintptr_t)dst & 15)) {
+#pragma unroll
+        for (int j = 0; j < 32; j += 2)
+            asm volatile("st.global.v2.u64 [%0], {%1, %2};" ::"l"(dst + j), "l"(v[j]), "l"(v[j + 1]) : "memory");
+        return;
+    }
+#pragma unroll
+    for (int j = 0; j < 32; j++)
+        if (j < ncols) dst[j] = v[j] + (b ? b[j] : 0);
+}
+
+__device__ __forceinline__ void store_row_direct(const Args &g, int z, long long m, int nb, uint64_t (&zs)[32]) {
+    const int ncols = g.N - nb < 32 ? g.N - nb : 32;
+    if (m < 0 || ncols <= 0) return;
+    if (!g.direct) {
+        put_row(g.partial + ((long long)z * g.M + m) * g.N + nb, ncols, zs, nullptr);
+        return;
+    }
+#pragma unroll
+    for (int j = 0; j < 32; j++) zs[j] = 1 + div_public<uint64_t>(zs[j] - g.d, g.d, g.dshift);
+#pragma unroll 1
+    for (int ps = 0; ps < 6; ps++) {
+        uint64_t *o = g.out[ps];
+        const uint64_t *b = g.bias[ps] ? g.bias[ps] + nb : nullptr;
+        const bool val = (ps == 0 || ps == 5);
+        if (!val && !b && g.zeros_kept) continue;
+        if (g.colmajor) {
+#pragma unroll
+            for (int j = 0; j < 32; j++)
+                if (j < ncols) o[m + (long long)(nb + j) * g.M] = (val ? zs[j] : 0) + (b ? b[j] : 0);
+        } else if (val) {
+            put_row(o + m * g.N + nb, ncols, zs, b);
+        } else {
+            uint64_t zero[32];
+#pragma unroll
+            for (int j = 0; j < 32; j++) zero[j] = 0;
+            put_row(o + m * g.N + nb, ncols, zero, b);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(NTHREADS, 1)
     limb_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmOut0,
-                    const __grid_constant__ CUtensorMap tmOut5, const __grid_constant__ Args gp) {
+                    const __grid_constant__ CUtensorMap tmOut5, const __grid_constant__ Args gp,
+                    const __grid_constant__ Sched sc) {
     extern __shared__ uint8_t smem_raw[];
     const uint32_t pad = (1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u;
     Smem &sm = *reinterpret_cast<Smem *>(smem_raw + pad);
@@ -703,7 +848,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         for (int i = threadIdx.x; i < (int)(sizeof(Args) / 4); i += blockDim.x) dst[i] = src[i];
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int z = blockIdx.z;
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
             tc::mbar_init(tc::smem_u32(&sm.full[s]), 1);
@@ -729,46 +873,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const Args &g = sm.args;
     const uint32_t tmem = sm.tmem_base;
     const uint64_t wait_ns = g.wait_ns;
-    // output-pixel rectangle of this tile
-    const int tw = blockIdx.y % g.tiles_w, t2 = blockIdx.y / g.tiles_w;
-    const int th = t2 % g.tiles_h, tn = t2 / g.tiles_h;
-    const int w0 = tw * g.Wt, h0 = th * g.Ht, n0 = tn * g.Nt;
-    // Position-major tiles (output pixel (h0, w0) of Nt images) run only the
-    // taps inside the input: rows r_lo..r_lo+nr-1, columns s_lo..s_lo+ns-1 of
-    // the filter. Their K' range (6 segments x taps x channel blocks) is split
-    // evenly over the grid's z slices.
-    int r_lo = 0, s_lo = 0, ns = 1, tile_stages = g.total_stages;
-    if (g.wgt) {
-        // Weight gradient of filter tap (r, s) = blockIdx.y / tiles_w for input
-        // channels tw * 128 ...: K runs over the output pixels (p, q) whose
-        // input pixel (p + r - pad, q + s - pad) is inside the image (rows
-        // r_lo..., columns s_lo..s_lo+ns-1) and 16 images per stage.
-        const int tap = t2, r = tap / g.f, sx = tap - r * g.f;
-        r_lo = g.pad - r > 0 ? g.pad - r : 0;
-        const int p_hi = g.Himg - 1 + g.pad - r < g.P - 1 ? g.Himg - 1 + g.pad - r : g.P - 1;
-        s_lo = g.pad - sx > 0 ? g.pad - sx : 0;
-        const int q_hi = g.Wimg - 1 + g.pad - sx < g.Q - 1 ? g.Wimg - 1 + g.pad - sx : g.Q - 1;
-        ns = q_hi - s_lo + 1;
-        tile_stages = (p_hi >= r_lo && ns > 0) ? 6 * (p_hi - r_lo + 1) * ns * g.nb16 : 0;
-    } else if (g.posmajor) {
-        r_lo = g.pad - h0 > 0 ? g.pad - h0 : 0;
-        const int r_hi = g.Himg - 1 + g.pad - h0 < g.f - 1 ? g.Himg - 1 + g.pad - h0 : g.f - 1;
-        s_lo = g.pad - w0 > 0 ? g.pad - w0 : 0;
-        const int s_hi = g.Wimg - 1 + g.pad - w0 < g.f - 1 ? g.Wimg - 1 + g.pad - w0 : g.f - 1;
-        ns = s_hi - s_lo + 1;
-        tile_stages = 6 * (r_hi - r_lo + 1) * ns * g.cblocks;
-    }
-    int stage_begin, stage_end;
-    if (g.posmajor || g.wgt) {
-        const int per = (tile_stages + (int)gridDim.z - 1) / (int)gridDim.z;
-        stage_begin = z * per;
-        stage_end = stage_begin + per;
-    } else {
-        stage_begin = z * g.chunks_per_split * CHUNK_STAGES;
-        stage_end = stage_begin + g.chunks_per_split * CHUNK_STAGES;
-    }
-    if (stage_end > tile_stages) stage_end = tile_stages;
-    const int nst = stage_end > stage_begin ? stage_end - stage_begin : 0;
 
     if (warp < W_EPI0) {
     asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(REGS_CTRL));
@@ -776,76 +880,77 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         // ------------------------------------------------ TMA + bulk copies
         if (lane == 0) {
             asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
-            int issued = 0;
+            int R = 0;  // ring position: stages issued by this CTA over its items
             bool ok = true;
-            for (int git = 0; git < nst; git++) {
-                const int s = git % STAGES;
-                const uint32_t ph = (uint32_t)(git / STAGES) & 1;
-                if (!tc::mbar_wait(tc::smem_u32(&sm.empty[s]), ph ^ 1, &sm.abort, wait_ns)) {
-                    flag_error(sm, g, 0x100 + s);
-                    ok = false;
-                    break;
+            for (int k = 0, item; ok && (item = cta_item(sc, g, k)) >= 0; k++) {
+                Item it;
+                item_geometry(g, item, it);
+                for (int git = 0; git < it.nst; git++) {
+                    const int s = R % STAGES;
+                    const uint32_t ph = (uint32_t)(R / STAGES) & 1;
+                    if (!tc::mbar_wait(tc::smem_u32(&sm.empty[s]), ph ^ 1, &sm.abort, wait_ns)) {
+                        flag_error(sm, g, 0x100 + s);
+                        ok = false;
+                        break;
+                    }
+                    int gst = it.stage_begin + git;
+                    int seg, x, y, zc, c3;
+                    if (g.wgt) {
+                        // (segment, valid output pixel, 16-image block) -> the packed dY stage
+                        const int per_seg = it.tile_stages / 6;
+                        seg = gst / per_seg;
+                        const int rem = gst - seg * per_seg;
+                        const int pi = rem / g.nb16, nb = rem - pi * g.nb16;
+                        const int pp = it.r_lo + pi / it.ns, qq = it.s_lo + pi % it.ns;
+                        const int r = it.t2 / g.f, sx = it.t2 - r * g.f;
+                        gst = seg * g.kblocks + (pp * g.Q + qq) * g.nb16 + nb;
+                        // box: 8 images x 128 channels x 2 image blocks at input pixel (h, w), 8 planes
+                        x = 0;
+                        y = it.tw * BM;
+                        zc = 2 * nb;
+                        c3 = (pp + r - g.pad) * g.Wimg + (qq + sx - g.pad);
+                    } else if (g.posmajor) {
+                        // compacted K' index (segment, inside tap, channel block) -> the packed stage
+                        const int per_seg = it.tile_stages / 6;
+                        seg = gst / per_seg;
+                        const int kb = gst - seg * per_seg;
+                        const int ti = kb / g.cblocks;
+                        const int cb = kb - ti * g.cblocks;
+                        const int r = it.r_lo + ti / it.ns, sx = it.s_lo + ti % it.ns;
+                        gst = seg * g.kblocks + (r * g.f + sx) * g.cblocks + cb;
+                        // 32-row line of the batch-innermost image: pixel (h * W + w) * Nimg + n0
+                        x = 0;
+                        y = (int)((((long long)(it.h0 + r - g.pad) * g.Wimg + (it.w0 + sx - g.pad)) * g.Nimg + it.n0) >>
+                                  5);
+                        zc = 0;
+                        c3 = 2 * cb;
+                    } else {
+                        seg = gst / g.kblocks;
+                        const int kb = gst - seg * g.kblocks;
+                        const int tap = kb / g.cblocks;
+                        const int cb = kb - tap * g.cblocks;
+                        const int r = tap / g.f, sx = tap - r * g.f;
+                        // line offset (16 bytes per pixel, so always 16-byte aligned), row, image
+                        x = g.rows_mode ? 0 : 8 * (it.w0 + sx - g.pad);
+                        y = g.rows_mode ? it.n0 >> 5 : it.h0 + r - g.pad;
+                        zc = g.rows_mode ? 0 : it.n0;
+                        c3 = 2 * cb;
+                    }
+                    const int this_R = R++;
+                    if (this_R == g.withhold) continue;  // diagnostic: this stage's data never arrives
+                    const uint32_t bar = tc::smem_u32(&sm.full[s]);
+                    tc::mbar_arrive_expect_tx(bar, 8 * g.a_box_bytes + B_STAGE_BYTES);
+                    const uint32_t dst = tc::smem_u32(sm.stage[s]);
+                    tma_load_5d(dst, &tmA, x, y, zc, c3, g.seg_block[seg] * 8, bar);
+                    const uint8_t *src = g.packB + ((size_t)gst * g.ntiles_n + it.bx) * B_STAGE_BYTES;
+                    tc::bulk_g2s(dst + 8 * A_PLANE_BYTES, src, B_STAGE_BYTES, bar);
                 }
-                int gst = stage_begin + git;
-                int seg, tap, cb, x, y, zc, c3;
-                if (g.wgt) {
-                    // (segment, valid output pixel, 16-image block) -> the packed dY stage
-                    const int per_seg = tile_stages / 6;
-                    seg = gst / per_seg;
-                    const int rem = gst - seg * per_seg;
-                    const int pi = rem / g.nb16, nb = rem - pi * g.nb16;
-                    const int pp = r_lo + pi / ns, qq = s_lo + pi % ns;
-                    const int r = t2 / g.f, sx = t2 - r * g.f;
-                    gst = seg * g.kblocks + (pp * g.Q + qq) * g.nb16 + nb;
-                    // box: 8 images x 128 channels x 2 image blocks at input pixel (h, w), 8 planes
-                    x = 0;
-                    y = tw * BM;
-                    zc = 2 * nb;
-                    c3 = (pp + r - g.pad) * g.Wimg + (qq + sx - g.pad);
-                    tap = cb = 0;
-                } else if (g.posmajor) {
-                    // compacted K' index (segment, inside tap, channel block) -> the packed stage
-                    const int per_seg = tile_stages / 6;
-                    seg = gst / per_seg;
-                    const int kb = gst - seg * per_seg;
-                    const int ti = kb / g.cblocks;
-                    cb = kb - ti * g.cblocks;
-                    const int r = r_lo + ti / ns, sx = s_lo + ti % ns;
-                    tap = r * g.f + sx;
-                    gst = seg * g.kblocks + tap * g.cblocks + cb;
-                    // 32-row line of the batch-innermost image: pixel (h * W + w) * Nimg + n0
-                    x = 0;
-                    y = (int)((((long long)(h0 + r - g.pad) * g.Wimg + (w0 + sx - g.pad)) * g.Nimg + n0) >> 5);
-                    zc = 0;
-                    c3 = 2 * cb;
-                } else {
-                    seg = gst / g.kblocks;
-                    const int kb = gst - seg * g.kblocks;
-                    tap = kb / g.cblocks;
-                    cb = kb - tap * g.cblocks;
-                    const int r = tap / g.f, sx = tap - r * g.f;
-                    // line offset (16 bytes per pixel, so always 16-byte aligned), row, image
-                    x = g.rows_mode ? 0 : 8 * (w0 + sx - g.pad);
-                    y = g.rows_mode ? n0 >> 5 : h0 + r - g.pad;
-                    zc = g.rows_mode ? 0 : n0;
-                    c3 = 2 * cb;
-                }
-                (void)tap;
-                issued = git + 1;
-                if (git == g.withhold) continue;  // diagnostic: this stage's data never arrives
-                const uint32_t bar = tc::smem_u32(&sm.full[s]);
-                tc::mbar_arrive_expect_tx(bar, 8 * g.a_box_bytes + B_STAGE_BYTES);
-                const uint32_t dst = tc::smem_u32(sm.stage[s]);
-                tma_load_5d(dst, &tmA, x, y, zc, c3, g.seg_block[seg] * 8, bar);
-                const uint8_t *src = g.packB + ((size_t)gst * g.ntiles_n + blockIdx.x) * B_STAGE_BYTES;
-                tc::bulk_g2s(dst + 8 * A_PLANE_BYTES, src, B_STAGE_BYTES, bar);
             }
             if (!ok) {
                 // wait (bounded, not cut short by the abort flag) for the copies still in flight
-                const int from = issued - STAGES > 0 ? issued - STAGES : 0;
-                for (int git = from; git < issued; git++)
-                    tc::mbar_wait(tc::smem_u32(&sm.full[git % STAGES]), (uint32_t)(git / STAGES) & 1, &sm.never,
-                                  wait_ns);
+                const int from = R - STAGES > 0 ? R - STAGES : 0;
+                for (int r = from; r < R; r++)
+                    tc::mbar_wait(tc::smem_u32(&sm.full[r % STAGES]), (uint32_t)(r / STAGES) & 1, &sm.never, wait_ns);
             }
         }
         __syncwarp();
@@ -854,51 +959,65 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         // Each group's issuer blocks on its own barriers only: the drain wait
         // at its chunk starts and the stage data. (One thread interleaving both
         // groups, polling both sets of barriers, issued 12-17 % slower.)
-        if (lane == 0 && nst > 0) {
+        if (lane == 0) {
             const int gi = warp == W_MMA ? 0 : 1;
             const uint32_t s0 = tc::smem_u32(sm.stage[0]);
             const uint64_t adesc0 = tc::smem_desc(s0, g.a_box_bytes / 2, 128);
             const uint64_t bdesc0 = tc::smem_desc(s0 + 8 * A_PLANE_BYTES, 128, 256);
             const uint32_t aplane16 = g.a_box_bytes >> 4;
             const int len = gi == 0 ? CHUNK_STAGES_LO : CHUNK_STAGES;
-            int chunk = 0, cstart = 0;
-            int cend = gi == 0 ? (nst < LO_FIRST ? nst : LO_FIRST) : (nst < CHUNK_STAGES ? nst : CHUNK_STAGES);
-            for (int t = 0; t < nst; t++) {
-                if (t == cstart && chunk > 0) {
-                    if (!tc::mbar_wait(tc::smem_u32(&sm.acc_empty[gi]), (uint32_t)(chunk - 1) & 1, &sm.abort, wait_ns)) {
-                        flag_error(sm, g, 0x300 + gi);
+            int R_total = 0;  // stages of all of this CTA's items
+            for (int k = 0, item; (item = cta_item(sc, g, k)) >= 0; k++) R_total += item_nst(g, item);
+            int R = 0, chunk = 0;  // ring position and chunks committed, over the items
+            bool ok = true;
+            for (int k = 0, item; ok && (item = cta_item(sc, g, k)) >= 0; k++) {
+                const int nst = item_nst(g, item);
+                int cstart = 0;
+                int cend = gi == 0 ? (nst < LO_FIRST ? nst : LO_FIRST) : (nst < CHUNK_STAGES ? nst : CHUNK_STAGES);
+                for (int t = 0; t < nst; t++, R++) {
+                    if (t == cstart && chunk > 0) {
+                        if (!tc::mbar_wait(tc::smem_u32(&sm.acc_empty[gi]), (uint32_t)(chunk - 1) & 1, &sm.abort,
+                                           wait_ns)) {
+                            flag_error(sm, g, 0x300 + gi);
+                            ok = false;
+                            break;
+                        }
+                        tc::tc_fence_after();
+                    }
+                    if (!tc::mbar_wait(tc::smem_u32(&sm.full[R % STAGES]), (uint32_t)(R / STAGES) & 1, &sm.abort,
+                                       wait_ns)) {
+                        flag_error(sm, g, 0x310 + gi);
+                        ok = false;
                         break;
                     }
                     tc::tc_fence_after();
-                }
-                if (!tc::mbar_wait(tc::smem_u32(&sm.full[t % STAGES]), (uint32_t)(t / STAGES) & 1, &sm.abort, wait_ns)) {
-                    flag_error(sm, g, 0x310 + gi);
-                    break;
-                }
-                tc::tc_fence_after();
-                if (gi == 0 && g.lag > 0 && !wait_issued(sm, t + g.lag < nst ? t + g.lag : nst, wait_ns)) {
-                    flag_error(sm, g, 0x320);
-                    break;
-                }
-                const uint64_t off = (uint64_t)(((t % STAGES) * STAGE_BYTES) >> 4);
-                if (gi == 0) {
-                    if (g.order) issue_lo<1>(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
-                    else issue_lo<0>(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
-                } else {
-                    if (g.order) issue_hi<1>(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
-                    else issue_hi<0>(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
-                }
-                if (t < nst - STAGES) tc::mma_commit(tc::smem_u32(&sm.empty[t % STAGES]));
-                if (gi == 1) *reinterpret_cast<volatile int *>(&sm.hi_issued) = t + 1;
-                if (t + 1 == cend) {
-                    tc::mma_commit(tc::smem_u32(&sm.acc_full[gi]));
-                    chunk++;
-                    cstart = t + 1;
-                    cend = nst < cstart + len ? nst : cstart + len;
+                    if (gi == 0 && g.lag > 0 && !wait_issued(sm, R + g.lag < R_total ? R + g.lag : R_total, wait_ns)) {
+                        flag_error(sm, g, 0x320);
+                        ok = false;
+                        break;
+                    }
+                    const uint64_t off = (uint64_t)(((R % STAGES) * STAGE_BYTES) >> 4);
+                    if (gi == 0) {
+                        if (g.order) issue_lo<1>(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
+                        else issue_lo<0>(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
+                    } else {
+                        if (g.order) issue_hi<1>(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
+                        else issue_hi<0>(tmem, adesc0 + off, aplane16, bdesc0 + off, t == cstart);
+                    }
+                    if (R < R_total - STAGES) tc::mma_commit(tc::smem_u32(&sm.empty[R % STAGES]));
+                    if (gi == 1) *reinterpret_cast<volatile int *>(&sm.hi_issued) = R + 1;
+                    if (t + 1 == cend) {
+                        tc::mma_commit(tc::smem_u32(&sm.acc_full[gi]));
+                        chunk++;
+                        cstart = t + 1;
+                        cend = nst < cstart + len ? nst : cstart + len;
+                    }
                 }
             }
-            tc::mma_commit(tc::smem_u32(&sm.done));
-            if (!tc::mbar_wait(tc::smem_u32(&sm.done), 0, &sm.never, wait_ns) && g.err) atomicCAS(g.err, 0, 0x400);
+            if (R_total > 0) {
+                tc::mma_commit(tc::smem_u32(&sm.done));
+                if (!tc::mbar_wait(tc::smem_u32(&sm.done), 0, &sm.never, wait_ns) && g.err) atomicCAS(g.err, 0, 0x400);
+            }
         }
         __syncwarp();
     }
@@ -908,76 +1027,98 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int q = warp & 3;
         const int colh = (warp - W_EPI0) >> 2;
         const int row = q * 32 + lane;
-        uint64_t zs[32];  // running Z of this thread's 32 columns
-#pragma unroll
-        for (int j = 0; j < 32; j++) zs[j] = 0;
         const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(colh * 32);
-        // drain each group's chunks in order, whichever group is ready first
-        const int nch[2] = {lo_chunks(nst), (nst + CHUNK_STAGES - 1) / CHUNK_STAGES};
-        int done_ch[2] = {0, 0};
-        uint64_t t_idle = 0;
-        while (done_ch[0] < nch[0] || done_ch[1] < nch[1]) {
-            int gi = -1;
-            if (done_ch[1] < nch[1] && tc::mbar_test_wait(tc::smem_u32(&sm.acc_full[1]), (uint32_t)done_ch[1] & 1)) gi = 1;
-            else if (done_ch[0] < nch[0] && tc::mbar_test_wait(tc::smem_u32(&sm.acc_full[0]), (uint32_t)done_ch[0] & 1))
-                gi = 0;
-            if (gi < 0) {
-                if (sm.abort) break;
-                const uint64_t now = tc::globaltimer();
-                if (t_idle == 0) t_idle = now;
-                else if (now - t_idle > wait_ns) {
-                    flag_error(sm, g, 0x500);
-                    break;
+        int drained[2] = {0, 0};  // chunks drained per group, over the items
+        for (int k = 0, item; (item = cta_item(sc, g, k)) >= 0; k++) {
+            Item it;
+            item_geometry(g, item, it);
+            const bool last = cta_item(sc, g, k + 1) < 0;
+            uint64_t zs[32];  // running Z of this thread's 32 columns
+#pragma unroll
+            for (int j = 0; j < 32; j++) zs[j] = 0;
+            // drain each group's chunks in order, whichever group is ready first
+            const int nch[2] = {lo_chunks(it.nst), (it.nst + CHUNK_STAGES - 1) / CHUNK_STAGES};
+            int done_ch[2] = {0, 0};
+            uint64_t t_idle = 0;
+            while (done_ch[0] < nch[0] || done_ch[1] < nch[1]) {
+                int gi = -1;
+                if (done_ch[1] < nch[1] && tc::mbar_test_wait(tc::smem_u32(&sm.acc_full[1]), (uint32_t)drained[1] & 1))
+                    gi = 1;
+                else if (done_ch[0] < nch[0] &&
+                         tc::mbar_test_wait(tc::smem_u32(&sm.acc_full[0]), (uint32_t)drained[0] & 1))
+                    gi = 0;
+                if (gi < 0) {
+                    if (sm.abort) break;
+                    const uint64_t now = tc::globaltimer();
+                    if (t_idle == 0) t_idle = now;
+                    else if (now - t_idle > wait_ns) {
+                        flag_error(sm, g, 0x500);
+                        break;
+                    }
+                    continue;
                 }
+                t_idle = 0;
+                tc::tc_fence_after();
+                if (gi == 0) drain4<false>(taddr, zs, tc::smem_u32(&sm.acc_empty[0]));
+                else drain4<true>(taddr, zs, tc::smem_u32(&sm.acc_empty[1]));
+                done_ch[gi]++;
+                drained[gi]++;
+            }
+            // output row of this thread's accumulator lane (-1: padding or past the image)
+            long long m = -1;
+            if (g.wgt) {
+                // row = input channel tw * 128 + row of filter tap t2: output row (r, s, c)
+                const int ch = it.tw * BM + row;
+                if (ch < g.cdim) m = (long long)it.t2 * g.cdim + ch;
+            } else if (row < g.R) {
+                const int wh = g.Wt * g.Ht;
+                const int nn = row / wh, rem = row - nn * wh;
+                const int hh = rem / g.Wt, ww = rem - hh * g.Wt;
+                const int n = it.n0 + nn, h = it.h0 + hh, w = it.w0 + ww;
+                if (n < g.Nimg && h < g.P && w < g.Q) m = ((long long)n * g.P + h) * g.Q + w;
+            }
+            if (!last) {
+                // the stage ring already holds the next item's operands; after
+                // an abort the items are still walked (without stores), so that
+                // every epilogue thread reaches the last item's barriers
+                if (!sm.abort) store_row_direct(g, it.z, m, it.bx * BN + colh * 32, zs);
                 continue;
             }
-            t_idle = 0;
-            tc::tc_fence_after();
-            if (gi == 0) drain4<false>(taddr, zs, tc::smem_u32(&sm.acc_empty[0]));
-            else drain4<true>(taddr, zs, tc::smem_u32(&sm.acc_empty[1]));
-            done_ch[gi]++;
-        }
-        // output row of this thread's accumulator lane (-1: padding or past the image)
-        long long m = -1;
-        if (g.wgt) {
-            // row = input channel tw * 128 + row of filter tap t2: output row (r, s, c)
-            const int ch = tw * BM + row;
-            if (ch < g.cdim) m = (long long)t2 * g.cdim + ch;
-        } else if (row < g.R) {
-            const int wh = g.Wt * g.Ht;
-            const int nn = row / wh, rem = row - nn * wh;
-            const int hh = rem / g.Wt, ww = rem - hh * g.Wt;
-            const int n = n0 + nn, h = h0 + hh, w = w0 + ww;
-            if (n < g.Nimg && h < g.P && w < g.Q) m = ((long long)n * g.P + h) * g.Q + w;
-        }
-        // every epilogue warp reaches both barriers (the drain loop only ever breaks out)
-        uint64_t *stg = reinterpret_cast<uint64_t *>(sm.stage[0]);
-        long long *mrow = reinterpret_cast<long long *>(stg + BM * STG_PITCH);
-        tc::fence_proxy_async_smem();
-        stage_row(g, stg, mrow, row, colh, sm.abort ? -1 : m, zs);
-        named_bar_epilogue();
-        if (!sm.abort && g.tma_out) {
-            // The tile's value (the same for party A's shareA and party C's
-            // shareB) repacked densely, row by row in the box's order (BN
-            // columns, then Wt, Ht, Nt), then stored by the tensor maps of the
-            // two value shares; the maps clip rows and columns past the tensor.
-            const int te = threadIdx.x - W_EPI0 * 32;
-            uint64_t *dense = reinterpret_cast<uint64_t *>(sm.stage[2]);
-            for (int e = te; e < g.R * BN; e += 256) dense[e] = stg[(e >> 6) * STG_PITCH + (e & (BN - 1))];
+            // The CTA's last item: every MMA has completed and no copy is
+            // pending, so the tile is staged in the stage ring and written as
+            // whole row segments or by tensor-map stores. Every epilogue warp
+            // reaches both barriers (the drain loop only ever breaks out, and
+            // no role sets the abort flag any more once the last item's
+            // chunks are drained).
+            uint64_t *stg = reinterpret_cast<uint64_t *>(sm.stage[0]);
+            long long *mrow = reinterpret_cast<long long *>(stg + BM * STG_PITCH);
             tc::fence_proxy_async_smem();
+            stage_row(g, stg, mrow, row, colh, sm.abort ? -1 : m, zs);
             named_bar_epilogue();
-            if (te == 0) {
-                const int c0 = blockIdx.x * BN;
-                const int c1 = g.rows_mode ? n0 : w0, c2 = g.rows_mode ? 0 : h0, c3 = g.rows_mode ? 0 : n0;
-                const uint32_t src = tc::smem_u32(dense);
-                tma_store_4d(&tmOut0, src, c0, c1, c2, c3);
-                tma_store_4d(&tmOut5, src, c0, c1, c2, c3);
-                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-                // the shared memory must stay valid until the stores have read it
-                asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+            if (!sm.abort && g.tma_out) {
+                // The tile's value (the same for party A's shareA and party C's
+                // shareB) repacked densely, row by row in the box's order (BN
+                // columns, then Wt, Ht, Nt), then stored by the tensor maps of the
+                // two value shares; the maps clip rows and columns past the tensor.
+                const int te = threadIdx.x - W_EPI0 * 32;
+                uint64_t *dense = reinterpret_cast<uint64_t *>(sm.stage[2]);
+                for (int e = te; e < g.R * BN; e += 256) dense[e] = stg[(e >> 6) * STG_PITCH + (e & (BN - 1))];
+                tc::fence_proxy_async_smem();
+                named_bar_epilogue();
+                if (te == 0) {
+                    const int c0 = it.bx * BN;
+                    const int c1 = g.rows_mode ? it.n0 : it.w0, c2 = g.rows_mode ? 0 : it.h0,
+                              c3 = g.rows_mode ? 0 : it.n0;
+                    const uint32_t src = tc::smem_u32(dense);
+                    tma_store_4d(&tmOut0, src, c0, c1, c2, c3);
+                    tma_store_4d(&tmOut5, src, c0, c1, c2, c3);
+                    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                    // the shared memory must stay valid until the stores have read it
+                    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                }
+            } else if (!sm.abort) {
+                store_tile(g, it.z, it.bx * BN, stg, mrow, threadIdx.x - W_EPI0 * 32);
             }
-        } else if (!sm.abort) {
-            store_tile(g, z, stg, mrow, threadIdx.x - W_EPI0 * 32);
         }
     }
     tc::tc_fence_before();
@@ -1255,6 +1396,63 @@ static int issue_lag() {
         return v < 0 ? 0 : v > STAGES - 1 ? STAGES - 1 : v;
     }();
     return lag;
+}
+
+// Longest-first balanced item lists of a grid of `ctas` CTAs (Sched); the
+// round-robin deal where the grid holds every item, or where the lists do
+// not fit the parameter's tables.
+static void build_schedule(const Args &g, int ctas, Sched &sc) {
+    static const bool on = [] {
+        const char *e = getenv("PG_SCHED");  // 0: round-robin deal
+        return !(e && *e == '0');
+    }();
+    sc.n = 0;
+    if (!on || ctas >= g.n_items || ctas > SCHED_MAX_CTAS || g.n_items > SCHED_MAX_ITEMS) return;
+    std::vector<std::pair<int, int>> len((size_t)g.n_items);  // (stages, item)
+    for (int i = 0; i < g.n_items; i++) {
+        Item it;
+        item_geometry(g, i, it);
+        len[(size_t)i] = {it.nst, i};
+    }
+    std::stable_sort(len.begin(), len.end(), [](const std::pair<int, int> &a, const std::pair<int, int> &b) {
+        return a.first > b.first;
+    });
+    std::vector<long long> load((size_t)ctas, 0);
+    std::vector<std::vector<int>> lists((size_t)ctas);
+    // least-loaded CTA first (a binary heap of (load, cta))
+    std::vector<std::pair<long long, int>> heap;
+    for (int b = 0; b < ctas; b++) heap.push_back({0, b});
+    auto cmp = [](const std::pair<long long, int> &a, const std::pair<long long, int> &b) {
+        return a.first != b.first ? a.first > b.first : a.second > b.second;
+    };
+    std::make_heap(heap.begin(), heap.end(), cmp);
+    for (const auto &e : len) {
+        std::pop_heap(heap.begin(), heap.end(), cmp);
+        auto &top = heap.back();
+        lists[(size_t)top.second].push_back(e.second);
+        top.first += e.first + 4;  // + a few stages' worth of per-item cost
+        std::push_heap(heap.begin(), heap.end(), cmp);
+    }
+    int pos = 0;
+    for (int b = 0; b < ctas; b++) {
+        sc.start[b] = (uint16_t)pos;
+        // a CTA's items in increasing index (neighbouring tiles share operands in L2)
+        std::sort(lists[(size_t)b].begin(), lists[(size_t)b].end());
+        for (int it : lists[(size_t)b]) sc.order[pos++] = (uint16_t)it;
+    }
+    sc.start[ctas] = (uint16_t)pos;
+    sc.n = 1;
+}
+
+// Grid of the limb GEMM (PG_PERSIST): 1 = one CTA per SM, each walking its
+// share of the work items (its tiles' output stores overlap the next tile's
+// copies and MMAs); 0 = one CTA per item.
+static bool persistent_grid() {
+    static const bool on = [] {
+        const char *e = getenv("PG_PERSIST");
+        return !(e && *e == '0');
+    }();
+    return on;
 }
 
 // MMA order within a group's stage (PG_ORDER: 1 interleaved, 0 by A plane;
@@ -1784,8 +1982,18 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
         if (ok) g.tma_out = 1;
     }
-    dim3 grid(p.ntiles_n, p.tiles_m, split);
-    limb_tma_kernel<<<grid, NTHREADS, smem_bytes(), c->stream>>>(tm, tmo[0], tmo[1], g);
+    g.tiles_m = p.tiles_m;
+    g.nsplit = split;
+    const long long items = (long long)p.ntiles_n * p.tiles_m * split;
+    if (items > INT_MAX) return set_error(c, PG_ERR_UNSUPPORTED, "%lld work items", items);
+    g.n_items = (int)items;
+    const int sms = c->sm_count > 0 ? c->sm_count : 148;
+    dim3 grid((unsigned)(persistent_grid() && items > sms ? sms : items));
+    static Sched sc;  // host staging of the kernel parameter (copied at launch)
+    static std::mutex sc_mu;
+    std::lock_guard<std::mutex> sc_lock(sc_mu);
+    build_schedule(g, (int)grid.x, sc);
+    limb_tma_kernel<<<grid, NTHREADS, smem_bytes(), c->stream>>>(tm, tmo[0], tmo[1], g, sc);
     c->launches++;
     int st = launch_status(c, "limb_tma_kernel");
     if (st) return st;
