@@ -48,6 +48,10 @@ struct Ctx {
     // (split, chunks per split) per problem shape
     int autotune = 1;
     std::unordered_map<std::string, std::pair<int, int>> split_cache;
+    // set by the network executor around a standalone share-GEMM / convolution
+    // call whose A (rep_a) or B (rep_b) share buffers hold a replicated sharing,
+    // so that the limb form's digit image of that operand stores each share once
+    bool rep_a = false, rep_b = false;
     // AES counter-mode masks of the resharing steps (off: the reference's
     // unfilled masks); round keys of the three pairwise keys and the next block
     bool prg_on = false;

@@ -310,12 +310,13 @@ struct WgtImageArgs {
     const uint64_t *a[6];
     long long hw, nb8, cdim;  // cdim: image channels (>= the input's, zero past it)
     int din;                  // the input's channels
+    int nseg;                 // 6 or 3 plane blocks (see ImageArgs)
     uint4 *img;
 };
 
 __global__ void wgt_image_kernel(const __grid_constant__ WgtImageArgs ia) {
     const long long per_seg = ia.hw * ia.nb8 * ia.cdim;
-    const long long total = 6 * per_seg;
+    const long long total = ia.nseg * per_seg;
     for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < total;
          u += (long long)gridDim.x * blockDim.x) {
         const long long c = u % ia.cdim;
@@ -324,7 +325,7 @@ __global__ void wgt_image_kernel(const __grid_constant__ WgtImageArgs ia) {
         t /= ia.nb8;
         const long long pix = t % ia.hw;
         const int seg = (int)(t / ia.hw);
-        const uint64_t *a = ia.a[seg];
+        const uint64_t *a = ia.a[ia.nseg == 3 ? 2 * seg : seg];
         uint64_t v[8];
 #pragma unroll
         for (int i = 0; i < 8; i++) v[i] = c < ia.din ? __ldg(a + ((nb * 8 + i) * ia.hw + pix) * ia.din + c) : 0;
@@ -1689,7 +1690,7 @@ static std::string tune_key(const Plan &p) {
 // tune_partial_bytes(p) when tuning can run.
 int tune_split(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial,
                uint64_t *const out[6], const uint64_t *const bias[6], int trunc, bool zeros_kept, uint64_t *raw,
-               int &split, int &cps) {
+               int &split, int &cps, bool shared) {
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
     const std::string key = tune_key(p);
     auto it = c->split_cache.find(key);
@@ -1726,7 +1727,8 @@ int tune_split(Ctx *c, const Plan &p, const void *image, const void *packB, uint
             for (int r = pass ? 1 : 0; r <= reps && st == PG_OK; r++) {
                 if (r == 1 && cudaEventRecord(e0, c->stream) != cudaSuccess)
                     st = set_error(c, PG_ERR_CUDA, "event record");
-                if (!st) st = run_gemm(c, p, image, packB, part, sp[i], cp[i], out, bias, trunc, zeros_kept, raw);
+                if (!st)
+                    st = run_gemm(c, p, image, packB, part, sp[i], cp[i], out, bias, trunc, zeros_kept, raw, shared);
             }
             if (!st && cudaEventRecord(e1, c->stream) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event record");
             if (!st && cudaEventSynchronize(e1) != cudaSuccess) st = set_error(c, PG_ERR_CUDA, "event synchronize");
@@ -1786,7 +1788,6 @@ int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n,
 }
 
 int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image, bool shared) {
-    if (shared && p.wgt) return set_error(c, PG_ERR_INVALID_ARG, "the weight-gradient image keeps six segments");
     if (p.wgt) {
         WgtImageArgs wa;
         memset(&wa, 0, sizeof(wa));
@@ -1798,8 +1799,9 @@ int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image, bo
         wa.nb8 = p.Nimg / 8;
         wa.cdim = p.C8;  // the image's channels
         wa.din = p.Din;
+        wa.nseg = shared ? 3 : 6;
         wa.img = (uint4 *)image;
-        const long long units = 6 * wa.hw * wa.nb8 * wa.cdim;
+        const long long units = wa.nseg * wa.hw * wa.nb8 * wa.cdim;
         const int sms = c->sm_count > 0 ? c->sm_count : 148;
         long long blocks = (units + 255) / 256;
         if (blocks > (long long)sms * 32) blocks = (long long)sms * 32;
@@ -1873,7 +1875,6 @@ int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB) {
 int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial, int split, int cps,
              uint64_t *const out[6], const uint64_t *const bias[6], int trunc, bool zeros_kept, uint64_t *raw,
              bool shared) {
-    if (shared && p.wgt) return set_error(c, PG_ERR_INVALID_ARG, "the weight-gradient image keeps six segments");
     {
         int st = prepare_device(c);
         if (st) return st;
@@ -2013,8 +2014,9 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
 
 // --------------------------------------------------- standalone entry points
 
+// shared: a's six buffers hold a replicated sharing (Ctx::rep_a / rep_b)
 static int run_with_scratch(Ctx *c, const lt::Plan &p, const uint64_t *const a[6], const uint64_t *const b[6],
-                            uint64_t *const out[6], const uint64_t *const bias[6], int trunc) {
+                            uint64_t *const out[6], const uint64_t *const bias[6], int trunc, bool shared = false) {
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     int split, cps;
     const size_t ib = al(p.image_bytes), pb = al(p.packB_bytes);
@@ -2022,10 +2024,12 @@ static int run_with_scratch(Ctx *c, const lt::Plan &p, const uint64_t *const a[6
     uint8_t *scr = (uint8_t *)scratch(c, ib + pb + qb);
     if (!scr) return PG_ERR_NO_MEMORY;
     uint64_t *part = (uint64_t *)(scr + ib + pb);
-    int st = lt::run_image(c, p, a, scr);
+    int st = lt::run_image(c, p, a, scr, shared);
     if (!st) st = lt::run_pack(c, p, b, scr + ib);
-    if (!st) st = lt::tune_split(c, p, scr, scr + ib, part, out, bias, trunc, false, nullptr, split, cps);
-    if (!st) st = lt::run_gemm(c, p, scr, scr + ib, split > 1 ? part : nullptr, split, cps, out, bias, trunc);
+    if (!st) st = lt::tune_split(c, p, scr, scr + ib, part, out, bias, trunc, false, nullptr, split, cps, shared);
+    if (!st)
+        st = lt::run_gemm(c, p, scr, scr + ib, split > 1 ? part : nullptr, split, cps, out, bias, trunc, false,
+                          nullptr, shared);
     if (st) return st;
     comm_msg(c, 2ull * p.M * p.N * 8, 2ull * p.M * p.N * 8);
     comm_round(c);
@@ -2042,7 +2046,7 @@ static int limb3_rss_matmul_impl(Ctx *c, const uint64_t *const a[6], const uint6
     lt::Plan p;
     int st = lt::plan_gemm(c, p, M, N, K, tA, tB, tC);
     if (st) return st;
-    return run_with_scratch(c, p, a, b, out, bias, trunc);
+    return run_with_scratch(c, p, a, b, out, bias, trunc, c->rep_a);
 }
 
 static int limb3_rss_conv_impl(Ctx *c, const uint64_t *const A[6], const uint64_t *const B[6], uint64_t *const C[6],
@@ -2057,7 +2061,7 @@ static int limb3_rss_conv_impl(Ctx *c, const uint64_t *const A[6], const uint64_
     int st;
     if (op == PG_CONV_FPROP) {
         if ((st = lt::plan_conv(c, p, batch, H, W, f, Din, Dout, stride, pad))) return st;
-        return run_with_scratch(c, p, A, B, C, nullptr, trunc);
+        return run_with_scratch(c, p, A, B, C, nullptr, trunc, c->rep_a);
     }
     if (op == PG_CONV_WGRAD) {
         // dW[Dout][r][s][c] = sum over output pixels of dY x im2col(X): A is
@@ -2065,7 +2069,7 @@ static int limb3_rss_conv_impl(Ctx *c, const uint64_t *const A[6], const uint64_
         // operand (the sum over the three parties of x_p0 (y_p0 + y_p1) + x_p1
         // y_p0 does not change when x and y trade places)
         if ((st = lt::plan_wgrad(c, p, batch, H, W, f, Din, Dout, stride, pad, wgrad_implicit))) return st;
-        return run_with_scratch(c, p, B, A, C, nullptr, trunc);
+        return run_with_scratch(c, p, B, A, C, nullptr, trunc, c->rep_b);
     }
     // dX = col2im(dY x W): the per-tap products of every output pixel as one
     // GEMM (M = output pixels, N = f * f * Din, K = Dout), kept as untruncated
@@ -2087,11 +2091,12 @@ static int limb3_rss_conv_impl(Ctx *c, const uint64_t *const A[6], const uint64_
     if (!scr) return PG_ERR_NO_MEMORY;
     uint64_t *part = (uint64_t *)(scr + ib + pb);
     uint64_t *cols = (uint64_t *)(scr + ib + pb + qb);
-    if ((st = lt::run_image(c, p, A, scr))) return st;
+    if ((st = lt::run_image(c, p, A, scr, c->rep_a))) return st;
     if ((st = lt::run_pack(c, p, B, scr + ib))) return st;
-    if ((st = lt::tune_split(c, p, scr, scr + ib, part, C, nullptr, trunc, false, cols, split, cps))) return st;
+    if ((st = lt::tune_split(c, p, scr, scr + ib, part, C, nullptr, trunc, false, cols, split, cps, c->rep_a)))
+        return st;
     if ((st = lt::run_gemm(c, p, scr, scr + ib, split > 1 ? part : nullptr, split, cps, C, nullptr, trunc, false,
-                           cols)))
+                           cols, c->rep_a)))
         return st;
     lt::Col2ImArgs a2;
     memset(&a2, 0, sizeof(a2));
@@ -2210,7 +2215,7 @@ int limb3_rss_conv_u64(Ctx *c, const uint64_t *const A[6], const uint64_t *const
             if (!load6(ca, A) || !load6(cb, B) || !load6(co, C))
                 return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
             if (trunc < 0 || trunc > 63) return set_error(c, PG_ERR_INVALID_ARG, "bad truncation %d", trunc);
-            return run_with_scratch(c, fp, A, B, C, nullptr, trunc);
+            return run_with_scratch(c, fp, A, B, C, nullptr, trunc, c->rep_a);
         });
     }
     return run_picked(c, k, cand);

@@ -64,7 +64,7 @@ bool cached_split(Ctx *c, const Plan &p, int &split, int &chunks_per_split);
 std::string plan_key(const Plan &p);
 int tune_split(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial,
                uint64_t *const out[6], const uint64_t *const bias[6], int trunc, bool zeros_kept, uint64_t *raw,
-               int &split, int &chunks_per_split);
+               int &split, int &chunks_per_split, bool shared = false);
 // A shares -> digit-plane image; weight shares -> packed stage images; then the GEMM (+ split-K reduction).
 // shared (run_image, run_relu_image, run_gemm): the six share buffers hold a replicated sharing (party p's
 // second share equals party p+1's first, bit for bit), so the image stores each of the three shares once

@@ -56,6 +56,7 @@ struct NetLayer {
     uint8_t *packB;
     int u64 = 0;  // the plain u64 form timed faster for this layer at set-up (small layers)
     bool b_replicated = true;  // the bias shares are a replicated sharing (checked by pg_net_set_params)
+    bool out_rep = false;      // the last forward left a replicated sharing in out (see net_run)
 };
 
 struct pg_net {
@@ -396,6 +397,7 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
         if (st) return st;
         if (!net->ev.empty() && (st = record_event(c, net->ev[2 * li + 1]))) return st;
         if (L.type == PG_LAYER_FC || L.type == PG_LAYER_CNN) replicated = !L.b_n || L.b_replicated;
+        L.out_rep = replicated;
         cur = L.out;
     }
     return PG_OK;
@@ -628,6 +630,18 @@ static int net_softmax_grad(pg_net *net, const uint64_t *const labels[6]) {
     return st;
 }
 
+// The standalone share-GEMM / convolution calls of the backward pass learn
+// through the context which of their operands hold a replicated sharing
+// (Ctx::rep_a, rep_b), for the limb form's digit images; cleared on return.
+struct RepOperands {
+    Ctx *c;
+    RepOperands(Ctx *c_, bool a, bool b) : c(c_) {
+        c->rep_a = a;
+        c->rep_b = b;
+    }
+    ~RepOperands() { c->rep_a = c->rep_b = false; }
+};
+
 static int share_gemm(Ctx *c, const uint64_t *const *a, const uint64_t *const *b, uint64_t *const *out, int M, int N,
                       int K, int tA, int tB, int tC, int trunc) {
     if (c->form == PG_FORM_LIMB_TC) return limb3_rss_matmul_u64(c, a, b, out, nullptr, M, N, K, tA, tB, tC, trunc);
@@ -648,17 +662,27 @@ static int net_backward(pg_net *net, const uint64_t *const in[6], const uint64_t
     int st = net_softmax_grad(net, labels);
     if (st) return st;
     const uint64_t *const *din = (const uint64_t *const *)net->tr.sdelta;
+    // the softmax delta takes the label shares as given; every FC / CNN
+    // input gradient is a replicated sharing ([v, 0, 0, 0, 0, v]), and the
+    // ReLU, maxpool and averagepool backward steps keep one replicated
+    bool din_rep = false;
     const uint64_t *zeros6[6];
     for (int k = 0; k < 6; k++) zeros6[k] = net->tr.zeros;
     const int B = net->batch;
     for (int li = (int)net->layers.size() - 1; li >= 0; li--) {
         NetLayer &L = net->layers[li];
         const uint64_t *const *fwd_in = li ? (const uint64_t *const *)net->layers[li - 1].out : in;
+        const bool fwd_rep = li ? net->layers[li - 1].out_rep : false;
         switch (L.type) {
             case PG_LAYER_FC: {  // FCLayer::backward (FCLayer.cu:132-217)
                 const int din_ = L.p[0], dout = L.p[1];
-                if ((st = share_gemm(c, din, (const uint64_t *const *)L.w, L.delta, B, din_, dout, 1, 0, 1, net->fp))) return st;
-                if ((st = share_gemm(c, din, fwd_in, net->tr.dW, dout, din_, B, 0, 1, 0, net->fp + log_lr))) return st;
+                {
+                    RepOperands rep(c, din_rep, fwd_rep);  // both GEMMs take the delta as their image operand
+                    if ((st = share_gemm(c, din, (const uint64_t *const *)L.w, L.delta, B, din_, dout, 1, 0, 1, net->fp)))
+                        return st;
+                    if ((st = share_gemm(c, din, fwd_in, net->tr.dW, dout, din_, B, 0, 1, 0, net->fp + log_lr)))
+                        return st;
+                }
                 if ((st = sub6(c, L.w, net->tr.dW, L.w_n))) return st;
                 for (int k = 0; k < 6; k++) {
                     PG_CHECK_CUDA(c, cudaMemsetAsync(net->tr.db[k], 0, L.b_n * 8, c->stream));
@@ -671,12 +695,16 @@ static int net_backward(pg_net *net, const uint64_t *const in[6], const uint64_t
             }
             case PG_LAYER_CNN: {  // CNNLayer::backward (CNNLayer.cu:114-193)
                 const int H = L.p[0], W = L.p[1], Din = L.p[2], Dout = L.p[3], f = L.p[4], s = L.p[5], pd = L.p[6];
-                if ((st = share_conv(c, din, (const uint64_t *const *)L.w, L.delta, PG_CONV_DGRAD, B, H, W, f, Din, Dout,
-                                     s, pd, net->fp)))
-                    return st;
-                if ((st = share_conv(c, din, fwd_in, net->tr.dW, PG_CONV_WGRAD, B, H, W, f, Din, Dout, s, pd,
-                                     net->fp)))
-                    return st;
+                {
+                    // the input gradient's image is dY; the weight gradient's the forward input
+                    RepOperands rep(c, din_rep, fwd_rep);
+                    if ((st = share_conv(c, din, (const uint64_t *const *)L.w, L.delta, PG_CONV_DGRAD, B, H, W, f, Din,
+                                         Dout, s, pd, net->fp)))
+                        return st;
+                    if ((st = share_conv(c, din, fwd_in, net->tr.dW, PG_CONV_WGRAD, B, H, W, f, Din, Dout, s, pd,
+                                         net->fp)))
+                        return st;
+                }
                 if ((st = rss_divide_public<uint64_t>(c, net->tr.dW, L.w_n, 1ull << log_lr, nullptr))) return st;
                 if ((st = sub6(c, L.w, net->tr.dW, L.w_n))) return st;
                 break;
@@ -711,6 +739,7 @@ static int net_backward(pg_net *net, const uint64_t *const in[6], const uint64_t
         // the limb form keeps packed weights: repack the updated ones
         if (net->limb_arena && L.packB && (st = lt::run_pack(c, L.plan, (const uint64_t *const *)L.w, L.packB))) return st;
         din = (const uint64_t *const *)L.delta;
+        if (L.type == PG_LAYER_FC || L.type == PG_LAYER_CNN) din_rep = true;
     }
     return PG_OK;
 }
