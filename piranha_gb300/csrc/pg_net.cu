@@ -420,6 +420,27 @@ __global__ void softmax_delta_kernel(Sh6<uint64_t> out, const uint64_t *smA, con
     }
 }
 
+// FCLayer::backward's bias gradient (FCLayer.cu:184-189: db zeroed, then
+// reduceSum(delta, db, false, outputDim, batchSize)) of all six shares in one
+// launch: db[k][c] = sum over i < len of delta[k][c * len + i], block (k, c)
+// per output.
+__global__ void bias_grad6_kernel(CSh6<uint64_t> d, Sh6<uint64_t> db, int outn, int len) {
+    __shared__ uint64_t red[256];
+    for (int blk = blockIdx.x; blk < 6 * outn; blk += gridDim.x) {
+        const int k = blk / outn, col = blk - k * outn;
+        uint64_t acc = 0;
+        for (int i = threadIdx.x; i < len; i += blockDim.x) acc += d.p[k][(size_t)len * col + i];
+        red[threadIdx.x] = acc;
+        __syncthreads();
+        for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+            if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) db.p[k][col] = red[0];
+        __syncthreads();
+    }
+}
+
 __global__ void sub6_kernel(Sh6<uint64_t> a, CSh6<uint64_t> b, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
 #pragma unroll
@@ -684,10 +705,13 @@ static int net_backward(pg_net *net, const uint64_t *const in[6], const uint64_t
                         return st;
                 }
                 if ((st = sub6(c, L.w, net->tr.dW, L.w_n))) return st;
-                for (int k = 0; k < 6; k++) {
-                    PG_CHECK_CUDA(c, cudaMemsetAsync(net->tr.db[k], 0, L.b_n * 8, c->stream));
-                    // reduceSum(delta, db, false, outputDim, batchSize), as the reference calls it
-                    if ((st = reduce_sum_u64(c, din[k], net->tr.db[k], 0, dout, B))) return st;
+                {
+                    // reduceSum(delta, db, false, outputDim, batchSize) into a zeroed db, as the
+                    // reference calls it, for the six shares at once
+                    const int blocks = 6 * dout < 4096 ? 6 * dout : 4096;
+                    bias_grad6_kernel<<<blocks, 256, 0, c->stream>>>(c6(din), m6(net->tr.db), dout, B);
+                    c->launches++;
+                    if ((st = launch_status(c, "bias_grad6_kernel"))) return st;
                 }
                 if ((st = rss_divide_public<uint64_t>(c, net->tr.db, L.b_n, 1ull << log_lr, nullptr))) return st;
                 if ((st = sub6(c, L.b, net->tr.db, L.b_n))) return st;
