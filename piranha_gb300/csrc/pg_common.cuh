@@ -52,6 +52,8 @@ struct Ctx {
     // call whose A (rep_a) or B (rep_b) share buffers hold a replicated sharing,
     // so that the limb form's digit image of that operand stores each share once
     bool rep_a = false, rep_b = false;
+    // the limb GEMM's schedule (MMA order, issue lag) of a tuner's timing run; -1: none
+    int lsched_order = -1, lsched_lag = -1;
     // AES counter-mode masks of the resharing steps (off: the reference's
     // unfilled masks); round keys of the three pairwise keys and the next block
     bool prg_on = false;
