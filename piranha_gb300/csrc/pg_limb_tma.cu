@@ -1484,6 +1484,16 @@ static bool schedule_from_env() {
     return set;
 }
 
+// CTAs of the persistent grid: one per SM, or fewer where PG_CTAS caps them
+// (the tests use a small cap to make every CTA walk many items)
+static int persistent_ctas(int sms) {
+    static const int cap = [] {
+        const char *e = getenv("PG_CTAS");
+        return e && *e ? atoi(e) : 0;
+    }();
+    return cap > 0 && cap < sms ? cap : sms;
+}
+
 // MMA order within a group's stage (PG_ORDER: 1 interleaved, 0 by A plane;
 // measured with issue_lag).
 static int issue_order() {
@@ -2051,7 +2061,8 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
     if (items > INT_MAX) return set_error(c, PG_ERR_UNSUPPORTED, "%lld work items", items);
     g.n_items = (int)items;
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
-    dim3 grid((unsigned)(persistent_grid() && items > sms ? sms : items));
+    const int ctas = persistent_ctas(sms);
+    dim3 grid((unsigned)(persistent_grid() && items > ctas ? ctas : items));
     static Sched sc;  // host staging of the kernel parameter (copied at launch)
     static std::mutex sc_mu;
     std::lock_guard<std::mutex> sc_lock(sc_mu);
