@@ -137,35 +137,6 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t adesc, uint64_
         : "memory");
 }
 
-// Variants that keep matrix A in the tensor core's collector buffer across
-// consecutive MMAs with the same A: FILL reads A and keeps it, USE reuses it,
-// LASTUSE reuses it and releases the buffer.
-enum CollectorA { COLL_NONE = 0, COLL_FILL = 1, COLL_USE = 2, COLL_LASTUSE = 3 };
-template <int COLL>
-__device__ __forceinline__ void mma_f16_c(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                          uint32_t accumulate) {
-    if (COLL == COLL_FILL)
-        asm volatile(
-            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-            "tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
-            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-            : "memory");
-    else if (COLL == COLL_USE)
-        asm volatile(
-            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-            "tcgen05.mma.cta_group::1.kind::f16.collector::a::use [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
-            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-            : "memory");
-    else if (COLL == COLL_LASTUSE)
-        asm volatile(
-            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-            "tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
-            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-            : "memory");
-    else
-        mma_f16(d_tmem, adesc, bdesc, idesc, accumulate);
-}
-
 // arrive on an mbarrier once all previously issued tcgen05 async ops of this thread complete
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
