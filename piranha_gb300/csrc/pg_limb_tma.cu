@@ -128,6 +128,7 @@ struct Args {
     int order;         // 1: narrow and wide MMAs interleaved within a group's stage (issue_lo / issue_hi)
     int seg_block[6];  // digit-plane block of the image holding each K segment (the identity, or 0,1,1,2,2,0
                        // for an image of a replicated sharing stored once per share)
+    const int *rep_flag;  // non-null: the blocks 0,1,1,2,2,0 when the device word is set (the image's layout)
 };
 
 struct __align__(16) Smem {
@@ -196,6 +197,7 @@ struct ImageArgs {
                             // n * bi_hw + h * W + w (bi_n = 0: image row = source row)
     int nseg;               // 6: a block per share buffer; 3: block b from party b's first share (a
                             // replicated sharing stored once per share, run_image's shared flag)
+    const int *rep_flag;    // non-null: 3 blocks when the device word is set (checked on the device)
     uint4 *img;
 };
 
@@ -206,7 +208,8 @@ struct ImageArgs {
 // image's channels are a multiple of 16).
 __global__ void image_kernel(const __grid_constant__ ImageArgs ia) {
     const int C16 = ia.C8 >> 1;
-    const long long total = (long long)ia.nseg * C16 * ia.pixels;
+    const int nseg = ia.rep_flag && *ia.rep_flag ? 3 : ia.nseg;
+    const long long total = (long long)nseg * C16 * ia.pixels;
     for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < total;
          u += (long long)gridDim.x * blockDim.x)
 #pragma unroll 1
@@ -215,7 +218,7 @@ __global__ void image_kernel(const __grid_constant__ ImageArgs ia) {
         const long long t = u / ia.pixels;
         const int cb = 2 * (int)(t % C16) + half;
         const int seg = (int)(t / C16);
-        const uint64_t *a = ia.a[ia.nseg == 3 ? 2 * seg : seg];
+        const uint64_t *a = ia.a[nseg == 3 ? 2 * seg : seg];
         const int k0 = cb * 8;
         uint64_t v[8];
 #pragma unroll
@@ -885,6 +888,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         // ------------------------------------------------ TMA + bulk copies
         if (lane == 0) {
             asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
+            const bool rep = g.rep_flag && *g.rep_flag;  // the image holds one block per share
             int R = 0;  // ring position: stages issued by this CTA over its items
             bool ok = true;
             for (int k = 0, item; ok && (item = cta_item(sc, g, k)) >= 0; k++) {
@@ -946,7 +950,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     const uint32_t bar = tc::smem_u32(&sm.full[s]);
                     tc::mbar_arrive_expect_tx(bar, 8 * g.a_box_bytes + B_STAGE_BYTES);
                     const uint32_t dst = tc::smem_u32(sm.stage[s]);
-                    tma_load_5d(dst, &tmA, x, y, zc, c3, g.seg_block[seg] * 8, bar);
+                    tma_load_5d(dst, &tmA, x, y, zc, c3, (rep ? ((seg + 1) >> 1) % 3 : g.seg_block[seg]) * 8, bar);
                     const uint8_t *src = g.packB + ((size_t)gst * g.ntiles_n + it.bx) * B_STAGE_BYTES;
                     tc::bulk_g2s(dst + 8 * A_PLANE_BYTES, src, B_STAGE_BYTES, bar);
                 }
@@ -1849,7 +1853,7 @@ int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n,
     return launch_status(c, "relu_image_kernel");
 }
 
-int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image, bool shared) {
+int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image, bool shared, const int *rep_flag) {
     if (p.wgt) {
         WgtImageArgs wa;
         memset(&wa, 0, sizeof(wa));
@@ -1891,6 +1895,7 @@ int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image, bo
     ia.bi_n = p.posmajor ? p.Nimg : 0;
     ia.bi_hw = (long long)p.Himg * p.Wimg;
     ia.nseg = shared ? 3 : 6;
+    ia.rep_flag = shared ? nullptr : rep_flag;
     ia.img = (uint4 *)image;
     if (ia.C8 & 1) return set_error(c, PG_ERR_INVALID_ARG, "image channels %d are not a multiple of 16", p.C);
     const long long units = (long long)ia.nseg * (ia.C8 / 2) * p.pixels_alloc;
@@ -1936,7 +1941,7 @@ int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB) {
 
 int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial, int split, int cps,
              uint64_t *const out[6], const uint64_t *const bias[6], int trunc, bool zeros_kept, uint64_t *raw,
-             bool shared) {
+             bool shared, const int *rep_flag) {
     {
         int st = prepare_device(c);
         if (st) return st;
@@ -2026,6 +2031,7 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
         }
     }
     for (int s = 0; s < 6; s++) g.seg_block[s] = shared ? ((s + 1) >> 1) % 3 : s;
+    g.rep_flag = (shared || p.wgt) ? nullptr : rep_flag;  // the weight-gradient image keeps six blocks
     if (split > 1 && !partial) return set_error(c, PG_ERR_INVALID_ARG, "split-K needs a partial buffer");
     // value shares by tensor-map stores: the network's convolutions (no bias,
     // zero shares kept, row-major output of an even width of at least one N tile)

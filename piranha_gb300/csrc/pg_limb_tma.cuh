@@ -70,7 +70,10 @@ int tune_split(Ctx *c, const Plan &p, const void *image, const void *packB, uint
 // second share equals party p+1's first, bit for bit), so the image stores each of the three shares once
 // (block b = party b's first share) and the GEMM reads segment s (party s/2's share s%2) from block
 // ((s + 1) / 2) % 3; the image producer and the GEMM must agree on it.
-int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image, bool shared = false);
+// rep_flag (run_image, run_gemm): a device word, set where a[]'s buffers hold a replicated sharing (checked on
+// the device by the caller); the image kernel and the GEMM then use the three-block layout
+int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image, bool shared = false,
+              const int *rep_flag = nullptr);
 int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB);
 // ReLU of n values fused with the digit image of the implicit convolution
 // (plan p) that takes them as input; relu_image_fits says whether it applies
@@ -83,7 +86,7 @@ int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n,
 // raw: write the untruncated Z (M x N, row-major) there instead of shares.
 int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64_t *partial, int split,
              int chunks_per_split, uint64_t *const out[6], const uint64_t *const bias[6], int trunc,
-             bool zeros_kept = false, uint64_t *raw = nullptr, bool shared = false);
+             bool zeros_kept = false, uint64_t *raw = nullptr, bool shared = false, const int *rep_flag = nullptr);
 
 }  // namespace lt
 }  // namespace pg

@@ -79,6 +79,7 @@ struct pg_net {
     // limb-form forward, which is always eager (capture runs one first).
     void *limb_arena = nullptr;
     uint8_t *limb_image = nullptr;
+    int *in_rep = nullptr;  // device word: the forward's input is a replicated sharing (checked each forward)
     uint64_t *limb_partial = nullptr;
     // Training (allocated by the first training call, which is eager):
     struct Train {
@@ -194,7 +195,7 @@ static int net_limb_setup(pg_net *net) {
         partial = partial > pb ? partial : pb;
         packs += al(L.plan.packB_bytes);
     }
-    const size_t bytes = al(image) + al(partial) + packs;
+    const size_t bytes = al(image) + al(partial) + packs + 256;
     if (cudaMalloc(&net->limb_arena, bytes) != cudaSuccess) {
         cudaGetLastError();
         net->limb_arena = nullptr;
@@ -205,6 +206,8 @@ static int net_limb_setup(pg_net *net) {
     ptr += al(image);
     net->limb_partial = partial ? (uint64_t *)ptr : nullptr;
     ptr += al(partial);
+    net->in_rep = (int *)ptr;
+    ptr += 256;
     for (auto &L : net->layers) {
         if (L.type != PG_LAYER_FC && L.type != PG_LAYER_CNN) continue;
         L.packB = ptr;
@@ -234,10 +237,12 @@ static int net_limb_setup(pg_net *net) {
 // output of the network does: an FC / CNN output is [v, 0, 0, 0, 0, v], and
 // the ReLU, maxpool and averagepool steps keep a replicated sharing
 // replicated), so the digit image stores each of the three shares once.
+// rep_flag: a device word that says whether in[] holds a replicated sharing
+// (the network's input, checked on the device each forward)
 static int net_limb_layer(pg_net *net, NetLayer &L, const uint64_t *const *in, bool image_ready = false,
-                          bool shared = false) {
+                          bool shared = false, const int *rep_flag = nullptr) {
     Ctx *c = net->ctx;
-    int st = image_ready ? PG_OK : lt::run_image(c, L.plan, in, net->limb_image, shared);
+    int st = image_ready ? PG_OK : lt::run_image(c, L.plan, in, net->limb_image, shared, rep_flag);
     if (st) return st;
     const uint64_t *const *bias = L.b_n ? (const uint64_t *const *)L.b : nullptr;
     // The arena is zeroed when the network is created and a layer's output
@@ -245,7 +250,7 @@ static int net_limb_layer(pg_net *net, NetLayer &L, const uint64_t *const *in, b
     // shares that dividePublic3out3 leaves at 0 stay 0: write only the two
     // value shares.
     st = lt::run_gemm(c, L.plan, net->limb_image, L.packB, L.split > 1 ? net->limb_partial : nullptr, L.split, L.cps,
-                      L.out, bias, net->fp, bias == nullptr, nullptr, shared);
+                      L.out, bias, net->fp, bias == nullptr, nullptr, shared, image_ready ? nullptr : rep_flag);
     if (st) return st;
     const uint64_t n_out = (uint64_t)L.plan.M * L.plan.N;
     comm_msg(c, 2 * n_out * 8, 2 * n_out * 8);
@@ -332,6 +337,8 @@ static int record_event(Ctx *c, cudaEvent_t e) {
     return PG_OK;
 }
 
+static int check_replicated(Ctx *c, const uint64_t *const in[6], size_t n, int *flag);
+
 static int net_run(pg_net *net, const uint64_t *const in[6]) {
     Ctx *c = net->ctx;
     const uint64_t *const *cur = in;
@@ -343,6 +350,16 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
         int st = net_limb_setup(net);
         if (!st) st = net_choose_forms(net);
         if (st) return st;
+    }
+    // Whether the caller's input is a replicated sharing is checked on the
+    // device (one read of the six buffers) where the first layer's digit image
+    // can use it: its image kernel and GEMM read the answer.
+    const int *in_rep = nullptr;
+    if (c->form == PG_FORM_LIMB_TC && net->in_rep && !net->layers.empty() &&
+        (net->layers[0].type == PG_LAYER_FC || net->layers[0].type == PG_LAYER_CNN) && !net->layers[0].u64) {
+        int st = check_replicated(c, in, net->in_n, net->in_rep);
+        if (st) return st;
+        in_rep = net->in_rep;
     }
     bool ready_next = false;  // the previous ReLU wrote this layer's digit image
     // The network's input is taken as six independent buffers; an FC / CNN
@@ -359,7 +376,8 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
             case PG_LAYER_FC: {
                 const uint64_t *const *bias = L.b_n ? (const uint64_t *const *)L.b : nullptr;
                 st = c->form == PG_FORM_LIMB_TC
-                         ? (L.u64 ? net_u64_layer(net, L, cur) : net_limb_layer(net, L, cur, false, replicated))
+                         ? (L.u64 ? net_u64_layer(net, L, cur)
+                                  : net_limb_layer(net, L, cur, false, replicated, li == 0 ? in_rep : nullptr))
                          : rss_matmul<uint64_t>(c, cur, (const uint64_t *const *)L.w, L.out, bias, net->batch, L.p[1],
                                                 L.p[0], 1, 1, 1, net->fp);
                 break;
@@ -367,7 +385,7 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
             case PG_LAYER_CNN:
                 st = c->form == PG_FORM_LIMB_TC
                          ? (L.u64 ? net_u64_layer(net, L, cur)
-                                  : net_limb_layer(net, L, cur, image_ready, replicated))
+                                  : net_limb_layer(net, L, cur, image_ready, replicated, li == 0 ? in_rep : nullptr))
                          : rss_conv<uint64_t>(c, cur, (const uint64_t *const *)L.w, L.out, PG_CONV_FPROP, net->batch,
                                               L.p[0], L.p[1], L.p[4], L.p[2], L.p[3], L.p[5], L.p[6], net->fp);
                 break;
@@ -439,6 +457,15 @@ __global__ void bias_grad6_kernel(CSh6<uint64_t> d, Sh6<uint64_t> db, int outn, 
         if (threadIdx.x == 0) db.p[k][col] = red[0];
         __syncthreads();
     }
+}
+
+// clears *flag where the six buffers are not a replicated sharing (party p's
+// second share differs from party p+1's first)
+__global__ void replicated6_kernel(CSh6<uint64_t> a, size_t n, int *flag) {
+    bool ok = true;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        ok &= (a.p[1][i] == a.p[2][i]) & (a.p[3][i] == a.p[4][i]) & (a.p[5][i] == a.p[0][i]);
+    if (!ok) *flag = 0;
 }
 
 __global__ void sub6_kernel(Sh6<uint64_t> a, CSh6<uint64_t> b, size_t n) {
@@ -539,6 +566,16 @@ int log_mini_batch(int batch) {  // (int)log2(MINI_BATCH_SIZE), util/model.cu:39
 }
 
 }  // namespace
+
+// *flag = whether in[]'s six buffers hold a replicated sharing (a set word,
+// cleared by the kernel on any mismatch)
+static int check_replicated(Ctx *c, const uint64_t *const in[6], size_t n, int *flag) {
+    PG_CHECK_CUDA(c, cudaMemsetAsync(flag, 1, sizeof(int), c->stream));
+    if (!n) return PG_OK;
+    replicated6_kernel<<<blocks_for(c, n), 256, 0, c->stream>>>(c6(in), n, flag);
+    c->launches++;
+    return launch_status(c, "replicated6_kernel");
+}
 
 // Training buffers: per-layer gradients, labels, the softmax step, the
 // parameter-gradient scratch, and a parameter snapshot for capture.

@@ -265,3 +265,42 @@ def test_fc_fed_by_a_biased_fc(pg, replicated_bias):
     for i, (g, w) in enumerate(zip(got_outs, want_outs)):
         assert np.array_equal(g, w), f"layer {i} {layers[i]}"
     assert np.array_equal(got, want)
+
+
+def test_input_replication_checked_on_the_device_per_replay(pg):
+    """The first layer's digit image stores each share once when the
+    network's input is a replicated sharing, and all six otherwise: the
+    check runs on the device in every forward, so one captured graph serves
+    both kinds of input. VGG16's first convolution (the im2col image) at
+    batch 2, replayed with a replicated input, a six-independent-buffer
+    input, then the replicated one again; every layer equals the oracle."""
+    import torch
+
+    layers = netref.vgg16_layers()
+    params = netref.kaiming_uniform_params(layers, 71)
+    batch = 2
+    rng = np.random.default_rng(72)
+    n_in = batch * 3072
+    rep = orc.share_random(orc.encode(rng.uniform(0, 1, n_in)), seed=73)
+    indep = rng.integers(0, 2**63, size=(3, 2, n_in), dtype=np.uint64)
+    ctx = pg.Context(0, form=pg.FORM_LIMB_TC)
+    ctx.set_autotune(False)
+    net = pg.Network(ctx, layers, batch)
+    for i, prm in enumerate(params):
+        if prm is not None:
+            net.set_params(i, pg.to_device(prm[0]), pg.to_device(prm[1]) if prm[1] is not None else None)
+    net.capture()
+    ptrs = net.input_buffers()
+    dst = _wrap_device(ptrs[0], 6 * net.in_n)
+    for x in (rep, indep, rep):
+        dst.copy_(pg.to_device(x).reshape(-1))
+        torch.cuda.synchronize()
+        net.forward_resident()
+        ctx.sync()
+        want, want_outs = netref.forward(layers, params, x, batch, keep=True)
+        for i in range(len(layers)):
+            optrs, n = net.layer_output_ptrs(i)
+            assert np.array_equal(gather(pg, optrs, n), want_outs[i]), f"layer {i} {layers[i]}"
+    ctx.check_device_errors()
+    net.close()
+    ctx.close()
