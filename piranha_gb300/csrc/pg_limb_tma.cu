@@ -43,9 +43,19 @@
 // and 4-7, whose drains into 64-bit registers are staggered: while the
 // epilogue drains one group, the other group's MMA warp runs ahead over the
 // stages already loaded. A stage is released when both MMA warps have
-// committed it (the empty barrier counts two arrivals). Every mbarrier wait
-// is bounded; on a timeout the kernel records an error word, stops issuing,
-// waits for its own copies and MMAs, and frees tensor memory.
+// committed it (the empty barrier counts two arrivals); the low group's
+// issuer trails the high group's by a stage (the issue lag). The grid is one
+// CTA per SM: each walks a host-balanced list of work items (an output tile
+// and its K' slice), with the ring and chunk counts running on across them,
+// and stores a tile's output from the epilogue registers while the next
+// tile's copies and MMAs run. Every mbarrier wait is bounded; on a timeout
+// the kernel records an error word, stops issuing, waits for its own copies
+// and MMAs, and frees tensor memory.
+//
+// Replicated sharings. Where the six share buffers hold one (party p's
+// second share equal to party p+1's first), the image stores each share once
+// (three blocks of digit planes) and segment s is read from block
+// ((s + 1) / 2) mod 3.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_fp16.h>
