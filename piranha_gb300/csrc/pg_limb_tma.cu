@@ -66,7 +66,9 @@
 #include <functional>
 #include <vector>
 #include <cstring>
+#include <memory>
 #include <mutex>
+#include <unordered_map>
 
 #include "pg_common.cuh"
 #include "pg_limb_tma.cuh"
@@ -2079,11 +2081,22 @@ int run_gemm(Ctx *c, const Plan &p, const void *image, const void *packB, uint64
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
     const int ctas = persistent_ctas(sms);
     dim3 grid((unsigned)(persistent_grid() && items > ctas ? ctas : items));
-    static Sched sc;  // host staging of the kernel parameter (copied at launch)
+    // the item lists depend only on the plan, the split and the grid: built once per
+    // shape (the kernel parameter is copied at launch)
+    static std::unordered_map<std::string, std::unique_ptr<Sched>> sc_cache;
     static std::mutex sc_mu;
     std::lock_guard<std::mutex> sc_lock(sc_mu);
-    build_schedule(g, (int)grid.x, sc);
-    limb_tma_kernel<<<grid, NTHREADS, smem_bytes(), c->stream>>>(tm, tmo[0], tmo[1], g, sc);
+    char sk[320];  // every field item_geometry reads, the split and the grid
+    snprintf(sk, sizeof(sk), "%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d", g.ntiles_n,
+             g.tiles_m, g.tiles_w, g.tiles_h, g.Wt, g.Ht, g.Nt, g.f, g.pad, g.Himg, g.Wimg, g.P, g.Q, g.cblocks, g.nb16,
+             g.kblocks, g.total_stages, g.chunks_per_split, g.wgt, g.posmajor, g.nsplit, g.n_items, (int)grid.x,
+             g.Nimg);
+    std::unique_ptr<Sched> &sc = sc_cache[sk];
+    if (!sc) {
+        sc.reset(new Sched);
+        build_schedule(g, (int)grid.x, *sc);
+    }
+    limb_tma_kernel<<<grid, NTHREADS, smem_bytes(), c->stream>>>(tm, tmo[0], tmo[1], g, *sc);
     c->launches++;
     int st = launch_status(c, "limb_tma_kernel");
     if (st) return st;
