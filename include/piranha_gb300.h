@@ -452,7 +452,13 @@ size_t pg_net_output_size(pg_net *net);
 /* forward on device-resident shares (six pointers each) */
 int pg_net_forward(pg_net *net, const uint64_t *const in[6], uint64_t *const out[6]);
 /* the same with host buffers: in_host/out_host are [6][n] contiguous
- * (pinned memory recommended); copies are on the context stream */
+ * (pinned memory recommended). Asynchronous: the host buffers must stay valid
+ * until the context stream is synchronised. Without a captured forward the
+ * copies are on the context stream; after pg_net_capture the input goes to
+ * one of two input buffer sets on a copy stream, each with its own graph, so
+ * that calls queued back to back overlap a call's input copy with the
+ * previous call's replay (the output copy follows each replay on the context
+ * stream) */
 int pg_net_forward_host(pg_net *net, const uint64_t *in_host, uint64_t *out_host);
 /* capture the forward (on the network's own input/output buffers) as a CUDA
  * graph, recorded on a private stream; later forwards replay it on the

@@ -69,6 +69,15 @@ struct pg_net {
     size_t in_n = 0, out_n = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    // pg_net_forward_host with a captured forward: a second input buffer set
+    // and its own captured graph, so that the next call's host-to-device copy
+    // (on the copy stream) overlaps the current replay
+    uint64_t *in_alt = nullptr;
+    cudaGraph_t graph_alt = nullptr;
+    cudaGraphExec_t exec_alt = nullptr;
+    cudaStream_t copy = nullptr;
+    cudaEvent_t in_ready[2] = {nullptr, nullptr}, in_free[2] = {nullptr, nullptr};
+    int slot = 0;
     uint64_t comm_per_fwd[9] = {0};  // accounting of one forward, replayed with the graph
     uint64_t launches_per_fwd = 0;
     std::vector<cudaEvent_t> ev;  // 2 per layer when per-layer timing is on (recorded into graphs too)
@@ -901,11 +910,32 @@ int pg_net_create(pg_ctx *c, pg_net **out, const int *spec, int nlayers, int bat
     return PG_OK;
 }
 
+// Work enqueued on the context stream that reads (or writes) the first input
+// buffer set: pg_net_forward_host's next copy into it waits for that.
+static void mark_in_used(pg_net *net) {
+    if (net->in_free[0]) cudaEventRecord(net->in_free[0], net->ctx->stream);
+}
+
+// the captured forward (both input buffer sets' graphs)
+static void drop_forward_graphs(pg_net *net) {
+    if (net->exec) cudaGraphExecDestroy(net->exec);
+    if (net->graph) cudaGraphDestroy(net->graph);
+    if (net->exec_alt) cudaGraphExecDestroy(net->exec_alt);
+    if (net->graph_alt) cudaGraphDestroy(net->graph_alt);
+    net->exec = net->exec_alt = nullptr;
+    net->graph = net->graph_alt = nullptr;
+}
+
 int pg_net_destroy(pg_net *net) {
     if (!net) return PG_ERR_INVALID_ARG;
     for (auto e : net->ev) cudaEventDestroy(e);
-    if (net->exec) cudaGraphExecDestroy(net->exec);
-    if (net->graph) cudaGraphDestroy(net->graph);
+    if (net->copy) cudaStreamSynchronize(net->copy);
+    drop_forward_graphs(net);
+    for (int s = 0; s < 2; s++) {
+        if (net->in_ready[s]) cudaEventDestroy(net->in_ready[s]);
+        if (net->in_free[s]) cudaEventDestroy(net->in_free[s]);
+    }
+    if (net->copy) cudaStreamDestroy(net->copy);
     if (net->exec_train) cudaGraphExecDestroy(net->exec_train);
     if (net->graph_train) cudaGraphDestroy(net->graph_train);
     if (net->arena || net->limb_arena || net->tr.arena) cudaStreamSynchronize(net->ctx->stream);
@@ -913,6 +943,7 @@ int pg_net_destroy(pg_net *net) {
     if (net->limb_arena) cudaFree(net->limb_arena);
     if (net->tr.arena) cudaFree(net->tr.arena);
     if (net->tr.h_rev) cudaFreeHost(net->tr.h_rev);
+    if (net->in_alt) cudaFree(net->in_alt);
     delete net;
     return PG_OK;
 }
@@ -941,12 +972,10 @@ int pg_net_set_params(pg_net *net, int layer, const uint64_t *const w[6], const 
             rep = memcmp(hb.data() + (2 * p + 1) * L.b_n, hb.data() + ((2 * p + 2) % 6) * L.b_n, L.b_n * 8) == 0;
         if (rep != L.b_replicated) {
             // captured steps chose their image layouts with the old flag
-            if (net->exec) cudaGraphExecDestroy(net->exec);
-            if (net->graph) cudaGraphDestroy(net->graph);
+            if (net->copy) cudaStreamSynchronize(net->copy);
+            drop_forward_graphs(net);
             if (net->exec_train) cudaGraphExecDestroy(net->exec_train);
             if (net->graph_train) cudaGraphDestroy(net->graph_train);
-            net->exec = nullptr;
-            net->graph = nullptr;
             net->exec_train = nullptr;
             net->graph_train = nullptr;
         }
@@ -969,6 +998,7 @@ int pg_net_forward(pg_net *net, const uint64_t *const in[6], uint64_t *const out
     if (!net || !in || !out) return PG_ERR_INVALID_ARG;
     Ctx *c = net->ctx;
     int st = net_run(net, in);
+    mark_in_used(net);
     if (st) return st;
     NetLayer &last = net->layers.back();
     for (int k = 0; k < 6; k++)
@@ -977,29 +1007,11 @@ int pg_net_forward(pg_net *net, const uint64_t *const in[6], uint64_t *const out
     return PG_OK;
 }
 
-int pg_net_capture(pg_net *net) {
-    if (!net) return PG_ERR_INVALID_ARG;
+// One forward captured as a graph reading the input buffers in[] (replays go
+// to the context stream); its accounting goes to comm_per_fwd /
+// launches_per_fwd.
+static int capture_forward(pg_net *net, const uint64_t *const in[6], cudaGraph_t &graph, cudaGraphExec_t &exec) {
     Ctx *c = net->ctx;
-    if (net->exec) {
-        cudaGraphExecDestroy(net->exec);
-        net->exec = nullptr;
-    }
-    if (net->graph) {
-        cudaGraphDestroy(net->graph);
-        net->graph = nullptr;
-    }
-    // One eager forward first: it sizes the context scratch (split-K
-    // partials), which cannot be allocated while a stream is capturing.
-    {
-        uint64_t comm_save[9];
-        memcpy(comm_save, c->comm, sizeof(comm_save));
-        uint64_t launches_save = c->launches.load();
-        int st0 = net_run(net, (const uint64_t *const *)net->in);
-        memcpy(c->comm, comm_save, sizeof(comm_save));
-        c->launches = launches_save;
-        if (st0) return st0;
-        PG_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
-    }
     // Capture on a private stream (the context stream may be the legacy
     // default stream, which cannot be captured); replays go to ctx->stream.
     cudaStream_t cap = nullptr, user = c->stream;
@@ -1013,7 +1025,7 @@ int pg_net_capture(pg_net *net) {
     uint64_t launches_before = c->launches.load();
     c->stream = cap;
     cudaError_t e0 = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-    int st = e0 == cudaSuccess ? net_run(net, (const uint64_t *const *)net->in) : PG_ERR_CUDA;
+    int st = e0 == cudaSuccess ? net_run(net, in) : PG_ERR_CUDA;
     cudaGraph_t g = nullptr;
     cudaError_t e = e0 == cudaSuccess ? cudaStreamEndCapture(cap, &g) : e0;
     c->stream = user;
@@ -1029,9 +1041,53 @@ int pg_net_capture(pg_net *net) {
         return st;
     }
     if (e != cudaSuccess) return set_error(c, PG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
-    net->graph = g;
-    PG_CHECK_CUDA(c, cudaGraphInstantiate(&net->exec, g, 0));
+    graph = g;
+    PG_CHECK_CUDA(c, cudaGraphInstantiate(&exec, g, 0));
     net->launches_per_fwd = launched;  // capture does not execute: replays add these
+    return PG_OK;
+}
+
+int pg_net_capture(pg_net *net) {
+    if (!net) return PG_ERR_INVALID_ARG;
+    Ctx *c = net->ctx;
+    if (net->copy) PG_CHECK_CUDA(c, cudaStreamSynchronize(net->copy));
+    drop_forward_graphs(net);
+    // One eager forward first: it sizes the context scratch (split-K
+    // partials), which cannot be allocated while a stream is capturing.
+    {
+        uint64_t comm_save[9];
+        memcpy(comm_save, c->comm, sizeof(comm_save));
+        uint64_t launches_save = c->launches.load();
+        int st0 = net_run(net, (const uint64_t *const *)net->in);
+        memcpy(c->comm, comm_save, sizeof(comm_save));
+        c->launches = launches_save;
+        if (st0) return st0;
+        PG_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    int st = capture_forward(net, (const uint64_t *const *)net->in, net->graph, net->exec);
+    if (st) return st;
+    // the second input buffer set of pg_net_forward_host and its graph; without
+    // them (no memory) the host forward replays the first graph
+    if (!net->in_alt && cudaMalloc(&net->in_alt, 6 * net->in_n * 8) != cudaSuccess) {
+        cudaGetLastError();
+        net->in_alt = nullptr;
+    }
+    if (net->in_alt && !net->copy) {
+        if (cudaStreamCreateWithFlags(&net->copy, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            net->copy = nullptr;
+        }
+        for (int s = 0; s < 2 && net->copy; s++)
+            if (cudaEventCreateWithFlags(&net->in_ready[s], cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&net->in_free[s], cudaEventDisableTiming) != cudaSuccess)
+                return set_error(c, PG_ERR_CUDA, "cudaEventCreate failed");
+    }
+    if (net->in_alt && net->copy) {
+        const uint64_t *alt[6];
+        for (int k = 0; k < 6; k++) alt[k] = net->in_alt + (size_t)k * net->in_n;
+        if ((st = capture_forward(net, alt, net->graph_alt, net->exec_alt))) return st;
+    }
+    net->slot = 0;
     return PG_OK;
 }
 
@@ -1041,14 +1097,36 @@ static int net_replay_or_run(pg_net *net) {
         PG_CHECK_CUDA(c, cudaGraphLaunch(net->exec, c->stream));
         for (int k = 0; k < 9; k++) c->comm[k] += net->comm_per_fwd[k];
         c->launches += net->launches_per_fwd;
+        mark_in_used(net);
         return PG_OK;
     }
-    return net_run(net, (const uint64_t *const *)net->in);
+    int st = net_run(net, (const uint64_t *const *)net->in);
+    mark_in_used(net);
+    return st;
 }
 
 int pg_net_forward_host(pg_net *net, const uint64_t *in_host, uint64_t *out_host) {
     if (!net || !in_host || !out_host) return PG_ERR_INVALID_ARG;
     Ctx *c = net->ctx;
+    if (net->exec && net->exec_alt) {
+        // Double-buffered: this call's input goes to one buffer set on the
+        // copy stream (once the replay that last read it has finished) while
+        // the previous call's replay still runs on the context stream.
+        const int s = net->slot;
+        net->slot ^= 1;
+        uint64_t *buf = s ? net->in_alt : net->in[0];
+        PG_CHECK_CUDA(c, cudaStreamWaitEvent(net->copy, net->in_free[s], 0));
+        PG_CHECK_CUDA(c, cudaMemcpyAsync(buf, in_host, 6 * net->in_n * 8, cudaMemcpyHostToDevice, net->copy));
+        PG_CHECK_CUDA(c, cudaEventRecord(net->in_ready[s], net->copy));
+        PG_CHECK_CUDA(c, cudaStreamWaitEvent(c->stream, net->in_ready[s], 0));
+        PG_CHECK_CUDA(c, cudaGraphLaunch(s ? net->exec_alt : net->exec, c->stream));
+        for (int k = 0; k < 9; k++) c->comm[k] += net->comm_per_fwd[k];
+        c->launches += net->launches_per_fwd;
+        PG_CHECK_CUDA(c, cudaEventRecord(net->in_free[s], c->stream));
+        NetLayer &last = net->layers.back();
+        PG_CHECK_CUDA(c, cudaMemcpyAsync(out_host, last.out[0], 6 * net->out_n * 8, cudaMemcpyDeviceToHost, c->stream));
+        return PG_OK;
+    }
     PG_CHECK_CUDA(c, cudaMemcpyAsync(net->in[0], in_host, 6 * net->in_n * 8, cudaMemcpyHostToDevice, c->stream));
     int st = net_replay_or_run(net);
     if (st) return st;
@@ -1210,6 +1288,7 @@ int pg_net_train_resident(pg_net *net) {
     PG_CHECK_CUDA(c, cudaGraphLaunch(net->exec_train, c->stream));
     for (int k = 0; k < 9; k++) c->comm[k] += net->comm_per_train[k];
     c->launches += net->launches_per_train;
+    mark_in_used(net);
     return PG_OK;
 }
 
@@ -1225,6 +1304,7 @@ int pg_net_train_host(pg_net *net, const uint64_t *in_host, const uint64_t *labe
     st = net->exec_train ? pg_net_train_resident(net)
                          : net_train(net, (const uint64_t *const *)net->in, (const uint64_t *const *)net->tr.labels,
                                      log_lr);
+    mark_in_used(net);
     if (st) return st;
     NetLayer &last = net->layers.back();
     PG_CHECK_CUDA(c, cudaMemcpyAsync(out_host, last.out[0], 6 * net->out_n * 8, cudaMemcpyDeviceToHost, c->stream));

@@ -304,3 +304,43 @@ def test_input_replication_checked_on_the_device_per_replay(pg):
     ctx.check_device_errors()
     net.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("form", ["u64", "tc"])
+def test_host_forwards_back_to_back_after_capture(pg, form):
+    """pg_net_forward_host after pg_net_capture: each call's input goes to
+    one of two input buffer sets on a copy stream while the previous call's
+    replay runs. Three calls with three different inputs, queued without a
+    synchronisation between them, then a device-resident replay and two
+    more host calls: every output equals the oracle's for its own input."""
+    import torch
+
+    layers = netref.lenet_layers()
+    params = netref.kaiming_uniform_params(layers, 81)
+    batch = 8
+    ctx = pg.Context(0, form=pg.FORM_LIMB_TC if form == "tc" else pg.FORM_U64)
+    ctx.set_autotune(False)
+    net = pg.Network(ctx, layers, batch)
+    for i, prm in enumerate(params):
+        if prm is not None:
+            net.set_params(i, pg.to_device(prm[0]), pg.to_device(prm[1]) if prm[1] is not None else None)
+    net.capture()
+    rng = np.random.default_rng(82)
+    xs = [orc.share_random(orc.encode(rng.uniform(0, 1, batch * 784)), seed=83 + k) for k in range(5)]
+    ins = [torch.from_numpy(x.reshape(-1).view(np.int64)).pin_memory() for x in xs]
+    outs = [torch.empty(6 * net.out_n, dtype=torch.int64).pin_memory() for _ in range(5)]
+    for k in range(3):
+        net.forward_host(ins[k].data_ptr(), outs[k].data_ptr())
+    # a replay of whatever the first buffer set holds, then two more host
+    # calls (the second one's copy into the first set waits for that replay)
+    net.forward_resident()
+    net.forward_host(ins[3].data_ptr(), outs[3].data_ptr())
+    net.forward_host(ins[4].data_ptr(), outs[4].data_ptr())
+    ctx.sync()
+    for k in range(5):
+        want = netref.forward(layers, params, xs[k], batch)
+        got = outs[k].numpy().view(np.uint64).reshape(3, 2, -1)
+        assert np.array_equal(got, want), f"call {k}"
+    ctx.check_device_errors()
+    net.close()
+    ctx.close()
