@@ -54,6 +54,10 @@ struct Ctx {
     bool rep_a = false, rep_b = false;
     // the limb GEMM's schedule (MMA order, issue lag) of a tuner's timing run; -1: none
     int lsched_order = -1, lsched_lag = -1;
+    // set by the network executor around a maxpool / ReLU layer whose input's
+    // shares 1-4 (party A's shareB, party B's two, party C's shareA) are known
+    // to be 0 (a bias-free FC / CNN output, [v, 0, 0, 0, 0, v]): those are not read
+    bool in_zero_mid = false;
     // AES counter-mode masks of the resharing steps (off: the reference's
     // unfilled masks); round keys of the three pairwise keys and the next block
     bool prg_on = false;

@@ -369,6 +369,7 @@ struct ReluImageArgs {
     int C8;
     long long bi_n, bi_hw;  // batch-innermost image (see ImageArgs); 0: image pixel = NHWC pixel
     int nseg;               // 6 or 3 plane blocks (see ImageArgs)
+    int zmid;               // shares 1-4 of the input are 0 (Ctx::in_zero_mid): not read
 };
 
 constexpr int RI_PIX = 16, RI_CH = 16, RI_PITCH = RI_PIX + 1;  // pitch 17: two-way bank conflicts at most
@@ -394,7 +395,7 @@ __global__ void __launch_bounds__(256) relu_image_kernel(const __grid_constant__
                 uint8_t r[3][2];
 #pragma unroll
                 for (int k = 0; k < 6; k++) {
-                    x[k >> 1][k & 1] = __ldg(a.in[k] + idx);
+                    x[k >> 1][k & 1] = (a.zmid && k > 0 && k < 5) ? 0 : __ldg(a.in[k] + idx);
                     zero[k >> 1][k & 1] = 0;
                 }
                 drelu_value<uint64_t, uint8_t>(x, r);
@@ -1857,6 +1858,7 @@ int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n,
     a.bi_n = p.posmajor ? p.Nimg : 0;
     a.bi_hw = (long long)p.Himg * p.Wimg;
     a.nseg = shared ? 3 : 6;
+    a.zmid = c->in_zero_mid ? 1 : 0;
     const long long tiles = (long long)(a.C8 / 2) * ((p.pixels + RI_PIX - 1) / RI_PIX);
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
     long long blocks = tiles < (long long)sms * 16 ? tiles : (long long)sms * 16;

@@ -99,7 +99,7 @@ struct PoolGeom {
 // row = (b * (wK*hK) + win) * C + ch, window elements gathered with the
 // (batch, x=col, y=row, channel) indexing of maxpool_im2row.
 template <typename T, typename U, int K>
-__global__ void maxpool_layer_kernel(CSh6<T> in, PoolGeom g, size_t rows, Sh6<T> out, Sh6<U> maxprime) {
+__global__ void maxpool_layer_kernel(CSh6<T> in, PoolGeom g, size_t rows, Sh6<T> out, Sh6<U> maxprime, int zmid) {
     const int pool = g.f * g.f;
     for (size_t row = blockIdx.x * (size_t)blockDim.x + threadIdx.x; row < rows;
          row += (size_t)gridDim.x * blockDim.x) {
@@ -117,7 +117,8 @@ __global__ void maxpool_layer_kernel(CSh6<T> in, PoolGeom g, size_t rows, Sh6<T>
                 size_t src = (size_t)b * g.H * g.W * g.C + (size_t)(baseCol + c) * g.H * g.C +
                              (size_t)(baseRow + r) * g.C + ch;
 #pragma unroll
-                for (int k = 0; k < 6; k++) v[i][k >> 1][k & 1] = in.p[k][src];
+                for (int k = 0; k < 6; k++)
+                    v[i][k >> 1][k & 1] = (zmid && k > 0 && k < 5) ? (T)0 : in.p[k][src];
             } else {
 #pragma unroll
                 for (int k = 0; k < 6; k++) v[i][k >> 1][k & 1] = (T)g.pad_val;  // stride_pad value
@@ -192,8 +193,10 @@ int rss_maxpool_layer(Ctx *c, const T *const in[6], T *const out[6], U *const ma
     g.hK = (H - pool) / stride + 1;
     g.pad_val = (uint64_t)(T)(int64_t)(-10 * (1 << fp));
     size_t rows = (size_t)batch * g.wK * g.hK * C;
-    if (padded == 4) maxpool_layer_kernel<T, U, 4><<<pool_grid(c, rows), 128, 0, c->stream>>>(a, g, rows, o, d);
-    else maxpool_layer_kernel<T, U, 16><<<pool_grid(c, rows), 128, 0, c->stream>>>(a, g, rows, o, d);
+    // in_zero_mid: the caller knows shares 1-4 of the input are 0 (they are not read)
+    const int zmid = c->in_zero_mid ? 1 : 0;
+    if (padded == 4) maxpool_layer_kernel<T, U, 4><<<pool_grid(c, rows), 128, 0, c->stream>>>(a, g, rows, o, d, zmid);
+    else maxpool_layer_kernel<T, U, 16><<<pool_grid(c, rows), 128, 0, c->stream>>>(a, g, rows, o, d, zmid);
     c->launches++;
     int st = launch_status(c, "maxpool_layer_kernel");
     if (st) return st;

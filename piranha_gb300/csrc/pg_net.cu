@@ -371,6 +371,7 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
         in_rep = net->in_rep;
     }
     bool ready_next = false;  // the previous ReLU wrote this layer's digit image
+    bool zero_mid = false;    // cur's shares 1-4 are 0 (the previous layer is a bias-free FC / CNN)
     // The network's input is taken as six independent buffers; an FC / CNN
     // output is a replicated sharing ([v, 0, 0, 0, 0, v] plus the bias shares,
     // when those are replicated too), and the layers after it keep it so.
@@ -404,7 +405,9 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
                 NetLayer *next = li + 1 < net->layers.size() ? &net->layers[li + 1] : nullptr;
                 if (c->form == PG_FORM_LIMB_TC && net->limb_arena && next && next->type == PG_LAYER_CNN &&
                     !next->u64 && lt::relu_image_fits(next->plan, L.in_n)) {
+                    c->in_zero_mid = zero_mid;
                     st = lt::run_relu_image(c, next->plan, cur, L.in_n, L.out, L.d, net->limb_image, replicated);
+                    c->in_zero_mid = false;
                     if (!st) count_relu_u64_u8(c, L.in_n);
                     ready_next = !st;
                 } else {
@@ -413,8 +416,10 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
                 break;
             }
             case PG_LAYER_MAXPOOL:
+                c->in_zero_mid = zero_mid;
                 st = rss_maxpool_layer<uint64_t, uint8_t>(c, cur, L.out, L.d, L.p[0], L.p[1], L.p[2], L.p[3], L.p[4],
                                                           net->batch, net->fp);
+                c->in_zero_mid = false;
                 break;
             case PG_LAYER_AVGPOOL:
                 st = rss_avgpool_layer<uint64_t>(c, cur, L.out, L.p[0], L.p[1], L.p[2], L.p[3], L.p[4], net->batch);
@@ -425,6 +430,10 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
         if (!net->ev.empty() && (st = record_event(c, net->ev[2 * li + 1]))) return st;
         if (L.type == PG_LAYER_FC || L.type == PG_LAYER_CNN) replicated = !L.b_n || L.b_replicated;
         L.out_rep = replicated;
+        // dividePublic3out3 leaves party A's shareB, party B's shares and party
+        // C's shareA at 0 (and the network never writes them), unless a bias
+        // share is added there
+        zero_mid = (L.type == PG_LAYER_FC || L.type == PG_LAYER_CNN) && !L.b_n;
         cur = L.out;
     }
     return PG_OK;
