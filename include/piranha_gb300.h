@@ -271,7 +271,9 @@ int pg_rss_maxpool_u64_u64(pg_ctx *ctx, const uint64_t *const in[6], size_t n, i
 /* MaxpoolLayer::forward (src/nn/MaxpoolLayer.cu:52-131): maxpool_im2row
  * windows (reference N,W,H,C indexing), power-of-two padding with
  * -10 * 2^fp, tournament, truncate_cols; one fused launch. out has
- * batch*P*Q*C values, maxprime batch*P*Q*C*pool*pool bit shares. */
+ * batch*P*Q*C values, maxprime batch*P*Q*C*pool*pool bit shares
+ * (maxprime == NULL: the bit shares, which only the backward reads, are
+ * not written). */
 int pg_rss_maxpool_layer_u64_u8(pg_ctx *ctx, const uint64_t *const in[6], uint64_t *const out[6],
                                 uint8_t *const maxprime[6], int H, int W, int C, int pool, int stride, int batch,
                                 int fp);
@@ -473,7 +475,13 @@ int pg_net_input_shares(pg_net *net, uint64_t *out[6]);
  * completed forward */
 int pg_net_enable_timing(pg_net *net, int on);
 int pg_net_layer_times(pg_net *net, float *ms);
-/* device pointers (owned by the network) of layer i's output shares */
+/* device pointers (owned by the network) of layer i's output shares.
+ * A forward before the training buffers exist (pg_net_train_setup, or any
+ * training call) is an inference forward: it writes no ReLU / maxpool bit
+ * shares, and a ReLU whose output feeds a limb-form convolution keeps that
+ * output only as the convolution's fp16 digit image (exact: the shares are
+ * the image's digits). This call then rebuilds the six shares from the image
+ * on the context stream and synchronises it before it returns. */
 int pg_net_layer_output(pg_net *net, int layer, uint64_t *const out[6], size_t *n);
 /* how FC / CNN layer i runs (no counterpart in the reference): out[0] = 1
  * limb tensor-core form, 2 plain u64 form; out[1] = 1 if its tiles are
@@ -494,7 +502,8 @@ int pg_net_layer_plan(pg_net *net, int layer, int out[4]);
 int pg_net_train_setup(pg_net *net);
 int pg_net_train_step(pg_net *net, const uint64_t *const in[6], const uint64_t *const labels[6], int log_lr);
 /* backward only, after a forward on the shares in[] (layer 0's weight
- * gradient needs them) */
+ * gradient needs them) that ran after pg_net_train_setup (an inference
+ * forward keeps no bit shares: PG_ERR_INVALID_ARG) */
 int pg_net_backward(pg_net *net, const uint64_t *const in[6], const uint64_t *const labels[6], int log_lr);
 /* the network's own label buffers ([6][out_n] contiguous) */
 int pg_net_label_shares(pg_net *net, uint64_t *out[6]);

@@ -359,7 +359,9 @@ __global__ void wgt_image_kernel(const __grid_constant__ WgtImageArgs ia) {
 // shares and bit shares; then 192 threads turn the block's 16 pixels x 2
 // channel groups x 6 shares into the next convolution's fp16 digit planes,
 // consecutive threads on consecutive pixels. The image launch and its
-// re-read of the ReLU output are saved.
+// re-read of the ReLU output are saved. With out[0] null the ReLU output is
+// kept in the digit image alone (image_decode_kernel restores the shares),
+// with dout[k] null bit share k is not written.
 struct ReluImageArgs {
     const uint64_t *in[6];
     uint64_t *out[6];
@@ -402,7 +404,7 @@ __global__ void __launch_bounds__(256) relu_image_kernel(const __grid_constant__
                 select_value<uint64_t, uint8_t>(zero, x, r, z);
 #pragma unroll
                 for (int k = 0; k < 6; k++) {
-                    a.out[k][idx] = z[k >> 1][k & 1];
+                    if (a.out[0]) a.out[k][idx] = z[k >> 1][k & 1];
                     if (a.dout[k]) a.dout[k][idx] = r[k >> 1][k & 1];
                 }
             } else {
@@ -430,6 +432,43 @@ __global__ void __launch_bounds__(256) relu_image_kernel(const __grid_constant__
             }
         }
         __syncthreads();
+    }
+}
+
+// The inverse of relu_image_kernel's image: the six u64 shares of every
+// (NHWC pixel, channel) value rebuilt from its eight fp16 digit planes,
+// v = sum_i (digit_i + 128) * 2^(8 i) - DIGIT_OFFSET. With three plane blocks
+// (a replicated sharing, block b = share 2b) share s is block ((s + 1) / 2) % 3.
+// One thread per (value, share); not on the forward's path (it serves reads
+// of a layer output that the forward kept as a digit image).
+struct ImageDecodeArgs {
+    const uint4 *img;
+    uint64_t *out[6];
+    long long pixels, pixels_alloc;
+    int C8, nseg;
+    long long bi_n, bi_hw;  // batch-innermost image (see ReluImageArgs)
+};
+
+__global__ void image_decode_kernel(const __grid_constant__ ImageDecodeArgs a) {
+    const long long C = 8ll * a.C8;
+    const long long total = 6 * a.pixels * C;
+    for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < total;
+         u += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(u / (a.pixels * C));
+        const long long idx = u - (long long)k * a.pixels * C;  // NHWC value index
+        const long long src = idx / C;
+        const int ch = (int)(idx - src * C);
+        const long long pix = a.bi_n ? (src % a.bi_hw) * a.bi_n + src / a.bi_hw : src;
+        const int seg = a.nseg == 3 ? ((k + 1) / 2) % 3 : k;
+        const __half *pl = reinterpret_cast<const __half *>(a.img);
+        uint64_t u64 = 0;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const long long at = (((long long)(seg * 8 + i) * a.C8 + ch / 8) * a.pixels_alloc + pix) * 8 + ch % 8;
+            const int digit = (int)__half2float(pl[at]);
+            u64 |= (uint64_t)(uint32_t)(digit + 128) << (8 * i);
+        }
+        a.out[k][idx] = u64 - DIGIT_OFFSET;
     }
 }
 
@@ -1846,9 +1885,9 @@ int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n,
     ReluImageArgs a;
     memset(&a, 0, sizeof(a));
     for (int k = 0; k < 6; k++) {
-        if (!in[k] || !out[k]) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+        if (!in[k] || (out && !out[k])) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
         a.in[k] = in[k];
-        a.out[k] = out[k];
+        a.out[k] = out ? out[k] : nullptr;
         a.dout[k] = dout ? dout[k] : nullptr;
     }
     a.img = (uint4 *)image;
@@ -1865,6 +1904,30 @@ int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n,
     relu_image_kernel<<<(unsigned)blocks, 256, 0, c->stream>>>(a);
     c->launches++;
     return launch_status(c, "relu_image_kernel");
+}
+
+int run_image_decode(Ctx *c, const Plan &p, const void *image, size_t n, uint64_t *const out[6], bool shared) {
+    if (!relu_image_fits(p, n) || !image) return set_error(c, PG_ERR_INVALID_ARG, "image decode: geometry mismatch");
+    ImageDecodeArgs a;
+    memset(&a, 0, sizeof(a));
+    for (int k = 0; k < 6; k++) {
+        if (!out[k]) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+        a.out[k] = out[k];
+    }
+    a.img = (const uint4 *)image;
+    a.pixels = p.pixels;
+    a.pixels_alloc = p.pixels_alloc;
+    a.C8 = p.C / 8;
+    a.nseg = shared ? 3 : 6;
+    a.bi_n = p.posmajor ? p.Nimg : 0;
+    a.bi_hw = (long long)p.Himg * p.Wimg;
+    const long long total = 6ll * (long long)n;
+    const int sms = c->sm_count > 0 ? c->sm_count : 148;
+    long long blocks = (total + 255) / 256;
+    if (blocks > (long long)sms * 16) blocks = (long long)sms * 16;
+    image_decode_kernel<<<(unsigned)blocks, 256, 0, c->stream>>>(a);
+    c->launches++;
+    return launch_status(c, "image_decode_kernel");
 }
 
 int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image, bool shared, const int *rep_flag) {

@@ -76,10 +76,14 @@ int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image, bo
               const int *rep_flag = nullptr);
 int run_pack(Ctx *c, const Plan &p, const uint64_t *const b[6], void *packB);
 // ReLU of n values fused with the digit image of the implicit convolution
-// (plan p) that takes them as input; relu_image_fits says whether it applies
+// (plan p) that takes them as input; relu_image_fits says whether it applies.
+// out == nullptr: the ReLU output is kept in the image alone; dout == nullptr:
+// no bit shares (an inference forward needs neither)
 bool relu_image_fits(const Plan &p, size_t n);
 int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n, uint64_t *const out[6],
                    uint8_t *const dout[6], void *image, bool shared = false);
+// the six u64 shares of the n values that run_relu_image left in image (plan p, the same shared)
+int run_image_decode(Ctx *c, const Plan &p, const void *image, size_t n, uint64_t *const out[6], bool shared);
 // zeros_kept: the four output shares that dividePublic3out3 leaves at 0 (all
 // but party A's shareA and party C's shareB) already hold 0 and are only
 // written where a bias share is added (the network's zeroed arena).

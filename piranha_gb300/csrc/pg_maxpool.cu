@@ -128,7 +128,8 @@ __global__ void maxpool_layer_kernel(CSh6<T> in, PoolGeom g, size_t rows, Sh6<T>
 #pragma unroll
         for (int k = 0; k < 6; k++) {
             out.p[k][row] = v[0][k >> 1][k & 1];
-            for (int i = 0; i < pool; i++) maxprime.p[k][row * pool + i] = dr[i][k >> 1][k & 1];
+            if (maxprime.p[k])
+                for (int i = 0; i < pool; i++) maxprime.p[k][row * pool + i] = dr[i][k >> 1][k & 1];
         }
     }
 }
@@ -178,7 +179,11 @@ int rss_maxpool_layer(Ctx *c, const T *const in[6], T *const out[6], U *const ma
     CSh6<T> a;
     Sh6<T> o;
     Sh6<U> d;
-    if (!load6(a, in) || !load6(o, out) || !load6(d, maxprime)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    // maxprime == nullptr: no argmax bit shares (an inference forward needs none)
+    if (!load6(a, in) || !load6(o, out)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    if (maxprime && !load6(d, maxprime)) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+    if (!maxprime)
+        for (int k = 0; k < 6; k++) d.p[k] = nullptr;
     if (H <= 0 || W <= 0 || C <= 0 || pool <= 0 || stride <= 0 || batch <= 0 || pool > H || pool > W)
         return set_error(c, PG_ERR_SIZE, "maxpool layer: bad geometry");
     // padded pool size pow(ceil(log2(pool^2)), 2) (MaxpoolLayer.cu:69)

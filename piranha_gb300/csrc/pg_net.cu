@@ -57,6 +57,15 @@ struct NetLayer {
     int u64 = 0;  // the plain u64 form timed faster for this layer at set-up (small layers)
     bool b_replicated = true;  // the bias shares are a replicated sharing (checked by pg_net_set_params)
     bool out_rep = false;      // the last forward left a replicated sharing in out (see net_run)
+    // A CNN layer after a ReLU: its own digit image, which that ReLU writes
+    // (relu_image) and which keeps the ReLU's output between forwards;
+    // held_shared: the image's three-block layout (a replicated sharing).
+    uint8_t *held = nullptr;
+    bool held_shared = false;
+    // A ReLU layer that writes the next layer's held image: an inference
+    // forward keeps its output there alone (out[] is rebuilt from the image
+    // when it is read); a training forward writes out[] too
+    bool out_held = false;
 };
 
 struct pg_net {
@@ -88,6 +97,11 @@ struct pg_net {
     // limb-form forward, which is always eager (capture runs one first).
     void *limb_arena = nullptr;
     uint8_t *limb_image = nullptr;
+    // The last forward that ran (eager or a replay) was an inference forward
+    // (no training buffers): the ReLU / maxpool bit shares were not written,
+    // nor the out[] of the ReLUs marked out_held. fwd_graph_held: the same
+    // for the captured forward graphs.
+    bool last_fwd_held = false, fwd_graph_held = false;
     int *in_rep = nullptr;  // device word: the forward's input is a replicated sharing (checked each forward)
     uint64_t *limb_partial = nullptr;
     // Training (allocated by the first training call, which is eager):
@@ -173,11 +187,23 @@ static int net_choose_tiles(pg_net *net, NetLayer &L, const uint64_t *const *bia
     return PG_OK;
 }
 
+// The digit image a CNN layer owns when the ReLU before it can write it
+// (either tile plan: the set-up timing picks one of them afterwards).
+static size_t held_bytes(pg_net *net, NetLayer &L) {
+    if (L.type != PG_LAYER_CNN) return 0;
+    const size_t li = (size_t)(&L - net->layers.data());
+    if (li == 0 || net->layers[li - 1].type != PG_LAYER_RELU) return 0;
+    const size_t n = net->layers[li - 1].in_n;
+    size_t b = lt::relu_image_fits(L.plan, n) ? L.plan.image_bytes : 0;
+    if (L.has_alt && lt::relu_image_fits(L.alt, n) && L.alt.image_bytes > b) b = L.alt.image_bytes;
+    return b;
+}
+
 // Plans, buffer sizes and weight packing of the limb form.
 static int net_limb_setup(pg_net *net) {
     Ctx *c = net->ctx;
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    size_t image = 0, partial = 0, packs = 0;
+    size_t image = 0, partial = 0, packs = 0, held = 0;
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
     for (auto &L : net->layers) {
         int st = PG_OK;
@@ -194,6 +220,7 @@ static int net_limb_setup(pg_net *net) {
         if (st) return st;
         lt::choose_split(L.plan, sms, L.split, L.cps);
         image = image > L.plan.image_bytes ? image : L.plan.image_bytes;
+        held += al(held_bytes(net, L));
         size_t pb = lt::tune_partial_bytes(L.plan, sms);
         if (L.has_alt) {
             // the same packed weights and image size; its own split-K candidates
@@ -204,7 +231,7 @@ static int net_limb_setup(pg_net *net) {
         partial = partial > pb ? partial : pb;
         packs += al(L.plan.packB_bytes);
     }
-    const size_t bytes = al(image) + al(partial) + packs + 256;
+    const size_t bytes = al(image) + al(partial) + packs + held + 256;
     if (cudaMalloc(&net->limb_arena, bytes) != cudaSuccess) {
         cudaGetLastError();
         net->limb_arena = nullptr;
@@ -223,6 +250,14 @@ static int net_limb_setup(pg_net *net) {
         ptr += al(L.plan.packB_bytes);
         int st = lt::run_pack(c, L.plan, (const uint64_t *const *)L.w, L.packB);
         if (st) return st;
+    }
+    for (auto &L : net->layers) {
+        const size_t hb = held_bytes(net, L);
+        if (!hb) continue;
+        L.held = ptr;
+        ptr += al(hb);
+        // rows past the activation stay 0 (the GEMM's last tile line reads them)
+        PG_CHECK_CUDA(c, cudaMemsetAsync(L.held, 0, al(hb), c->stream));
     }
     // split-K of every layer, timed on a zero image into the layer's own
     // outputs (the forward overwrites them; without a bias only the value
@@ -251,14 +286,16 @@ static int net_limb_setup(pg_net *net) {
 static int net_limb_layer(pg_net *net, NetLayer &L, const uint64_t *const *in, bool image_ready = false,
                           bool shared = false, const int *rep_flag = nullptr) {
     Ctx *c = net->ctx;
-    int st = image_ready ? PG_OK : lt::run_image(c, L.plan, in, net->limb_image, shared, rep_flag);
+    // the ReLU before it wrote the image into the layer's own buffer
+    uint8_t *const image = image_ready && L.held ? L.held : net->limb_image;
+    int st = image_ready ? PG_OK : lt::run_image(c, L.plan, in, image, shared, rep_flag);
     if (st) return st;
     const uint64_t *const *bias = L.b_n ? (const uint64_t *const *)L.b : nullptr;
     // The arena is zeroed when the network is created and a layer's output
     // buffers are written by that layer alone, so without a bias the four
     // shares that dividePublic3out3 leaves at 0 stay 0: write only the two
     // value shares.
-    st = lt::run_gemm(c, L.plan, net->limb_image, L.packB, L.split > 1 ? net->limb_partial : nullptr, L.split, L.cps,
+    st = lt::run_gemm(c, L.plan, image, L.packB, L.split > 1 ? net->limb_partial : nullptr, L.split, L.cps,
                       L.out, bias, net->fp, bias == nullptr, nullptr, shared, image_ready ? nullptr : rep_flag);
     if (st) return st;
     const uint64_t n_out = (uint64_t)L.plan.M * L.plan.N;
@@ -370,6 +407,10 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
         if (st) return st;
         in_rep = net->in_rep;
     }
+    // An inference forward (no training buffers, so no backward follows it)
+    // writes no bit shares, and a ReLU that writes the next convolution's
+    // digit image keeps its output there alone.
+    const bool hold = !net->tr.arena;
     bool ready_next = false;  // the previous ReLU wrote this layer's digit image
     bool zero_mid = false;    // cur's shares 1-4 are 0 (the previous layer is a bias-free FC / CNN)
     // The network's input is taken as six independent buffers; an FC / CNN
@@ -381,6 +422,7 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
         int st = PG_OK;
         const bool image_ready = ready_next;
         ready_next = false;
+        L.out_held = false;
         if (!net->ev.empty() && (st = record_event(c, net->ev[2 * li]))) return st;
         switch (L.type) {
             case PG_LAYER_FC: {
@@ -405,20 +447,24 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
                 NetLayer *next = li + 1 < net->layers.size() ? &net->layers[li + 1] : nullptr;
                 if (c->form == PG_FORM_LIMB_TC && net->limb_arena && next && next->type == PG_LAYER_CNN &&
                     !next->u64 && lt::relu_image_fits(next->plan, L.in_n)) {
+                    uint8_t *const image = next->held ? next->held : net->limb_image;
+                    L.out_held = next->held != nullptr;
                     c->in_zero_mid = zero_mid;
-                    st = lt::run_relu_image(c, next->plan, cur, L.in_n, L.out, L.d, net->limb_image, replicated);
+                    st = lt::run_relu_image(c, next->plan, cur, L.in_n, hold && L.out_held ? nullptr : L.out,
+                                            hold ? nullptr : L.d, image, replicated);
                     c->in_zero_mid = false;
                     if (!st) count_relu_u64_u8(c, L.in_n);
                     ready_next = !st;
+                    next->held_shared = replicated;
                 } else {
-                    st = rss_relu<uint64_t, uint8_t>(c, cur, L.in_n, L.out, L.d);
+                    st = rss_relu<uint64_t, uint8_t>(c, cur, L.in_n, L.out, hold ? nullptr : L.d);
                 }
                 break;
             }
             case PG_LAYER_MAXPOOL:
                 c->in_zero_mid = zero_mid;
-                st = rss_maxpool_layer<uint64_t, uint8_t>(c, cur, L.out, L.d, L.p[0], L.p[1], L.p[2], L.p[3], L.p[4],
-                                                          net->batch, net->fp);
+                st = rss_maxpool_layer<uint64_t, uint8_t>(c, cur, L.out, hold ? nullptr : L.d, L.p[0], L.p[1], L.p[2],
+                                                          L.p[3], L.p[4], net->batch, net->fp);
                 c->in_zero_mid = false;
                 break;
             case PG_LAYER_AVGPOOL:
@@ -436,6 +482,7 @@ static int net_run(pg_net *net, const uint64_t *const in[6]) {
         zero_mid = (L.type == PG_LAYER_FC || L.type == PG_LAYER_CNN) && !L.b_n;
         cur = L.out;
     }
+    net->last_fwd_held = hold;
     return PG_OK;
 }
 
@@ -1075,6 +1122,7 @@ int pg_net_capture(pg_net *net) {
     }
     int st = capture_forward(net, (const uint64_t *const *)net->in, net->graph, net->exec);
     if (st) return st;
+    net->fwd_graph_held = net->last_fwd_held;  // the captured forward's kind
     // the second input buffer set of pg_net_forward_host and its graph; without
     // them (no memory) the host forward replays the first graph
     if (!net->in_alt && cudaMalloc(&net->in_alt, 6 * net->in_n * 8) != cudaSuccess) {
@@ -1106,6 +1154,7 @@ static int net_replay_or_run(pg_net *net) {
         PG_CHECK_CUDA(c, cudaGraphLaunch(net->exec, c->stream));
         for (int k = 0; k < 9; k++) c->comm[k] += net->comm_per_fwd[k];
         c->launches += net->launches_per_fwd;
+        net->last_fwd_held = net->fwd_graph_held;
         mark_in_used(net);
         return PG_OK;
     }
@@ -1131,6 +1180,7 @@ int pg_net_forward_host(pg_net *net, const uint64_t *in_host, uint64_t *out_host
         PG_CHECK_CUDA(c, cudaGraphLaunch(s ? net->exec_alt : net->exec, c->stream));
         for (int k = 0; k < 9; k++) c->comm[k] += net->comm_per_fwd[k];
         c->launches += net->launches_per_fwd;
+        net->last_fwd_held = net->fwd_graph_held;
         PG_CHECK_CUDA(c, cudaEventRecord(net->in_free[s], c->stream));
         NetLayer &last = net->layers.back();
         PG_CHECK_CUDA(c, cudaMemcpyAsync(out_host, last.out[0], 6 * net->out_n * 8, cudaMemcpyDeviceToHost, c->stream));
@@ -1178,6 +1228,15 @@ int pg_net_layer_times(pg_net *net, float *ms) {
 int pg_net_layer_output(pg_net *net, int layer, uint64_t *const out[6], size_t *n) {
     if (!net || layer < 0 || layer >= (int)net->layers.size()) return PG_ERR_INVALID_ARG;
     NetLayer &L = net->layers[layer];
+    if (L.out_held && net->last_fwd_held && (size_t)layer + 1 < net->layers.size()) {
+        // the last (inference) forward kept this ReLU output in the next
+        // layer's digit image alone: rebuild the six shares from it
+        Ctx *c = net->ctx;
+        NetLayer &nx = net->layers[layer + 1];
+        int st = lt::run_image_decode(c, nx.plan, nx.held, L.out_n, L.out, nx.held_shared);
+        if (st) return st;
+        PG_CHECK_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
     if (out)
         for (int k = 0; k < 6; k++) ((uint64_t **)out)[k] = L.out[k];
     if (n) *n = L.out_n;
@@ -1216,6 +1275,11 @@ int pg_net_label_shares(pg_net *net, uint64_t *out[6]) {
 
 int pg_net_backward(pg_net *net, const uint64_t *const in[6], const uint64_t *const labels[6], int log_lr) {
     if (!net || !in || !labels) return PG_ERR_INVALID_ARG;
+    // the backward reads the forward's bit shares and layer outputs, which an
+    // inference forward does not keep
+    if (net->last_fwd_held)
+        return set_error(net->ctx, PG_ERR_INVALID_ARG,
+                         "the last forward was an inference forward: call pg_net_train_setup before the forward");
     int st = net_train_setup(net);
     if (st) return st;
     return net_backward(net, in, labels, log_lr);
@@ -1297,6 +1361,7 @@ int pg_net_train_resident(pg_net *net) {
     PG_CHECK_CUDA(c, cudaGraphLaunch(net->exec_train, c->stream));
     for (int k = 0; k < 9; k++) c->comm[k] += net->comm_per_train[k];
     c->launches += net->launches_per_train;
+    net->last_fwd_held = false;
     mark_in_used(net);
     return PG_OK;
 }

@@ -294,3 +294,48 @@ def test_training_step_flipped_input_gradient(pg, tmp_path):
     net.close()
     ctx.close()
 
+
+
+def test_inference_forward_keeps_relu_outputs_as_digit_images(pg):
+    """Before the training buffers exist a forward is an inference forward: a
+    ReLU that feeds a limb-form convolution keeps its output only as that
+    convolution's digit image, and reading the layer rebuilds the six shares
+    from the image. Every reading follows the last forward that ran: the
+    captured inference graph, an eager training step (which writes every
+    layer output), then the inference graph again with the updated weights.
+    A backward right after an inference forward is refused."""
+    layers = [("cnn", 8, 8, 16, 16, 3, 1, 1), ("relu", 1024), ("cnn", 8, 8, 16, 16, 3, 1, 1),
+              ("maxpool", 8, 8, 16, 2, 2), ("relu", 256), ("cnn", 4, 4, 16, 32, 3, 1, 1), ("relu", 512),
+              ("fc", 512, 10), ("relu", 10)]
+    params = netref.kaiming_uniform_params(layers, 61)
+    batch = 16
+    rng = np.random.default_rng(62)
+    x = orc.share_random(orc.encode(rng.uniform(0, 1, batch * 1024)), seed=63)
+    labels = one_hot_labels(batch, 10, 64)
+    ctx = pg.Context(0, form=pg.FORM_LIMB_TC)
+    ctx.set_autotune(False)  # every convolution in the limb form, so that the ReLUs write digit images
+    net = make_net(pg, ctx, layers, params, batch)
+    net.capture()
+    fill(net.input_buffers(), x)
+
+    def check_forward(prm, what):
+        _, want = netref.forward(layers, prm, x, batch, keep=True)
+        for i in range(len(layers)):
+            optrs, n = net.layer_output_ptrs(i)
+            assert np.array_equal(gather(pg, optrs, n), want[i]), f"{what}: output of layer {i} {layers[i]}"
+
+    net.forward_resident()
+    ctx.sync()
+    check_forward(params, "inference graph")
+    with pytest.raises(pg.PiranhaError):
+        net.backward(pg.to_device(x), pg.to_device(labels), 5)
+    outs, new_params, deltas, softmax = oracle_step(layers, params, x, labels, batch, 5)
+    net.train_step(pg.to_device(x), pg.to_device(labels), 5)
+    ctx.sync()
+    check_against_oracle(pg, net, layers, outs, new_params, deltas, softmax)
+    net.forward_resident()
+    ctx.sync()
+    check_forward(new_params, "inference graph after the training step")
+    ctx.check_device_errors()
+    net.close()
+    ctx.close()
