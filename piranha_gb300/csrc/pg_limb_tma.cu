@@ -376,6 +376,8 @@ struct ReluImageArgs {
 
 constexpr int RI_PIX = 16, RI_CH = 16, RI_PITCH = RI_PIX + 1;  // pitch 17: two-way bank conflicts at most
 
+// ZM: a.zmid (shares 1-4 of the input are 0, not read) as a compile-time fact
+template <bool ZM>
 __global__ void __launch_bounds__(256) relu_image_kernel(const __grid_constant__ ReluImageArgs a) {
     __shared__ uint64_t zs[6][RI_CH][RI_PITCH];
     const int C16 = a.C8 >> 1;
@@ -394,12 +396,12 @@ __global__ void __launch_bounds__(256) relu_image_kernel(const __grid_constant__
                 const long long src = a.bi_n ? (pix % a.bi_n) * a.bi_hw + pix / a.bi_n : pix;
                 const long long idx = src * C + cp * RI_CH + ch;
                 uint64_t x[3][2], zero[3][2];
-                uint8_t r[3][2];
 #pragma unroll
                 for (int k = 0; k < 6; k++) {
-                    x[k >> 1][k & 1] = (a.zmid && k > 0 && k < 5) ? 0 : __ldg(a.in[k] + idx);
+                    x[k >> 1][k & 1] = (ZM && k > 0 && k < 5) ? 0 : __ldg(a.in[k] + idx);
                     zero[k >> 1][k & 1] = 0;
                 }
+                uint8_t r[3][2];
                 drelu_value<uint64_t, uint8_t>(x, r);
                 select_value<uint64_t, uint8_t>(zero, x, r, z);
 #pragma unroll
@@ -1901,7 +1903,8 @@ int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n,
     const long long tiles = (long long)(a.C8 / 2) * ((p.pixels + RI_PIX - 1) / RI_PIX);
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
     long long blocks = tiles < (long long)sms * 16 ? tiles : (long long)sms * 16;
-    relu_image_kernel<<<(unsigned)blocks, 256, 0, c->stream>>>(a);
+    if (a.zmid) relu_image_kernel<true><<<(unsigned)blocks, 256, 0, c->stream>>>(a);
+    else relu_image_kernel<false><<<(unsigned)blocks, 256, 0, c->stream>>>(a);
     c->launches++;
     return launch_status(c, "relu_image_kernel");
 }

@@ -98,18 +98,16 @@ struct PoolGeom {
 // One thread per (image, window, channel) pool row in the reference's order:
 // row = (b * (wK*hK) + win) * C + ch, window elements gathered with the
 // (batch, x=col, y=row, channel) indexing of maxpool_im2row.
-template <typename T, typename U, int K>
-__global__ void maxpool_layer_kernel(CSh6<T> in, PoolGeom g, size_t rows, Sh6<T> out, Sh6<U> maxprime, int zmid) {
+// ZM: shares 1-4 of the input are 0 (Ctx::in_zero_mid) and are not read.
+template <typename T, typename U, int K, bool ZM>
+__global__ void maxpool_layer_kernel(CSh6<T> in, PoolGeom g, size_t rows, Sh6<T> out, Sh6<U> maxprime) {
     const int pool = g.f * g.f;
-    for (size_t row = blockIdx.x * (size_t)blockDim.x + threadIdx.x; row < rows;
-         row += (size_t)gridDim.x * blockDim.x) {
+    auto load = [&](size_t row, T (&v)[K][3][2]) {
         int ch = (int)(row % g.C);
         size_t t = row / g.C;
         int win = (int)(t % ((size_t)g.wK * g.hK));
         int b = (int)(t / ((size_t)g.wK * g.hK));
         int baseCol = (win / g.hK) * g.stride, baseRow = (win % g.hK) * g.stride;
-        T v[K][3][2];
-        U dr[K][3][2];
 #pragma unroll
         for (int i = 0; i < K; i++) {
             if (i < pool) {
@@ -118,12 +116,18 @@ __global__ void maxpool_layer_kernel(CSh6<T> in, PoolGeom g, size_t rows, Sh6<T>
                              (size_t)(baseRow + r) * g.C + ch;
 #pragma unroll
                 for (int k = 0; k < 6; k++)
-                    v[i][k >> 1][k & 1] = (zmid && k > 0 && k < 5) ? (T)0 : in.p[k][src];
+                    v[i][k >> 1][k & 1] = (ZM && k > 0 && k < 5) ? (T)0 : in.p[k][src];
             } else {
 #pragma unroll
                 for (int k = 0; k < 6; k++) v[i][k >> 1][k & 1] = (T)g.pad_val;  // stride_pad value
             }
         }
+    };
+    for (size_t row = blockIdx.x * (size_t)blockDim.x + threadIdx.x; row < rows;
+         row += (size_t)gridDim.x * blockDim.x) {
+        T v[K][3][2];
+        U dr[K][3][2];
+        load(row, v);
         tournament<T, U, K>(v, dr);
 #pragma unroll
         for (int k = 0; k < 6; k++) {
@@ -199,9 +203,14 @@ int rss_maxpool_layer(Ctx *c, const T *const in[6], T *const out[6], U *const ma
     g.pad_val = (uint64_t)(T)(int64_t)(-10 * (1 << fp));
     size_t rows = (size_t)batch * g.wK * g.hK * C;
     // in_zero_mid: the caller knows shares 1-4 of the input are 0 (they are not read)
-    const int zmid = c->in_zero_mid ? 1 : 0;
-    if (padded == 4) maxpool_layer_kernel<T, U, 4><<<pool_grid(c, rows), 128, 0, c->stream>>>(a, g, rows, o, d, zmid);
-    else maxpool_layer_kernel<T, U, 16><<<pool_grid(c, rows), 128, 0, c->stream>>>(a, g, rows, o, d, zmid);
+    const unsigned grid = pool_grid(c, rows);
+    if (padded == 4) {
+        if (c->in_zero_mid) maxpool_layer_kernel<T, U, 4, true><<<grid, 128, 0, c->stream>>>(a, g, rows, o, d);
+        else maxpool_layer_kernel<T, U, 4, false><<<grid, 128, 0, c->stream>>>(a, g, rows, o, d);
+    } else {
+        if (c->in_zero_mid) maxpool_layer_kernel<T, U, 16, true><<<grid, 128, 0, c->stream>>>(a, g, rows, o, d);
+        else maxpool_layer_kernel<T, U, 16, false><<<grid, 128, 0, c->stream>>>(a, g, rows, o, d);
+    }
     c->launches++;
     int st = launch_status(c, "maxpool_layer_kernel");
     if (st) return st;
