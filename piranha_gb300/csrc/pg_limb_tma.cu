@@ -380,21 +380,28 @@ constexpr int RI_PIX = 16, RI_CH = 16, RI_PITCH = RI_PIX + 1;  // pitch 17: two-
 template <bool ZM>
 __global__ void __launch_bounds__(256) relu_image_kernel(const __grid_constant__ ReluImageArgs a) {
     __shared__ uint64_t zs[6][RI_CH][RI_PITCH];
-    const int C16 = a.C8 >> 1;
-    const long long C = 8ll * a.C8;
-    const long long ptiles = (a.pixels + RI_PIX - 1) / RI_PIX;
-    const long long tiles = ptiles * C16;
+    // 32-bit tile and pixel arithmetic (relu_image_fits keeps both below 2^31)
+    const uint32_t C16 = (uint32_t)(a.C8 >> 1);
+    const uint64_t C = 8ull * a.C8;
+    const uint32_t pixels = (uint32_t)a.pixels;
+    const uint32_t tiles = (pixels + RI_PIX - 1) / RI_PIX * C16;
+    const uint32_t bi_n = (uint32_t)a.bi_n, bi_hw = (uint32_t)a.bi_hw;
     const int t = threadIdx.x;
-    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const int cp = (int)(tile % C16);
-        const long long p0 = (tile / C16) * RI_PIX;
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const uint32_t pt = tile / C16;
+        const uint32_t cp = tile - pt * C16;
+        const uint32_t p0 = pt * RI_PIX;
         {
             const int pl = t / RI_CH, ch = t % RI_CH;
-            const long long pix = p0 + pl;
+            const uint32_t pix = p0 + pl;
             uint64_t z[3][2];
-            if (pix < a.pixels) {
-                const long long src = a.bi_n ? (pix % a.bi_n) * a.bi_hw + pix / a.bi_n : pix;
-                const long long idx = src * C + cp * RI_CH + ch;
+            if (pix < pixels) {
+                uint32_t src = pix;
+                if (bi_n) {
+                    const uint32_t n = pix / bi_n;
+                    src = (pix - n * bi_n) * bi_hw + n;
+                }
+                const uint64_t idx = src * C + cp * RI_CH + ch;
                 uint64_t x[3][2], zero[3][2];
 #pragma unroll
                 for (int k = 0; k < 6; k++) {
@@ -420,8 +427,8 @@ __global__ void __launch_bounds__(256) relu_image_kernel(const __grid_constant__
         if (t < a.nseg * 2 * RI_PIX) {
             const int seg = t / (2 * RI_PIX), half = (t / RI_PIX) & 1, pl = t % RI_PIX;
             const int sh = a.nseg == 3 ? 2 * seg : seg;
-            const long long pix = p0 + pl;
-            if (pix < a.pixels) {
+            const uint32_t pix = p0 + pl;
+            if (pix < pixels) {
                 uint64_t v[8];
 #pragma unroll
                 for (int i = 0; i < 8; i++) v[i] = zs[sh][half * 8 + i][pl];
@@ -1877,8 +1884,10 @@ int tune_split(Ctx *c, const Plan &p, const void *image, const void *packB, uint
 }
 
 bool relu_image_fits(const Plan &p, size_t n) {
+    // the kernel's tile and pixel indices are 32-bit
+    const long long tiles = (p.pixels + RI_PIX - 1) / RI_PIX * (p.C / 16);
     return p.implicit && p.src_mode == SRC_ROWS && p.C == p.Kreal && p.C % 16 == 0 && p.ld == p.C &&
-           (size_t)p.pixels * p.C == n;
+           (size_t)p.pixels * p.C == n && p.pixels < (1ll << 31) && tiles < (1ll << 31);
 }
 
 int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n, uint64_t *const out[6],

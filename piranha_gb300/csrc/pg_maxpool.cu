@@ -99,14 +99,17 @@ struct PoolGeom {
 // row = (b * (wK*hK) + win) * C + ch, window elements gathered with the
 // (batch, x=col, y=row, channel) indexing of maxpool_im2row.
 // ZM: shares 1-4 of the input are 0 (Ctx::in_zero_mid) and are not read.
-template <typename T, typename U, int K, bool ZM>
-__global__ void maxpool_layer_kernel(CSh6<T> in, PoolGeom g, size_t rows, Sh6<T> out, Sh6<U> maxprime) {
+// I: the row index type (uint32_t below 2^32 rows: its divisions are a few
+// instructions where 64-bit ones are a long software sequence).
+template <typename T, typename U, int K, bool ZM, typename I>
+__global__ void maxpool_layer_kernel(CSh6<T> in, PoolGeom g, I rows, Sh6<T> out, Sh6<U> maxprime) {
     const int pool = g.f * g.f;
-    auto load = [&](size_t row, T (&v)[K][3][2]) {
-        int ch = (int)(row % g.C);
-        size_t t = row / g.C;
-        int win = (int)(t % ((size_t)g.wK * g.hK));
-        int b = (int)(t / ((size_t)g.wK * g.hK));
+    const I C = (I)g.C, wins = (I)g.wK * (I)g.hK;
+    auto load = [&](I row, T (&v)[K][3][2]) {
+        const I t = row / C;
+        const int ch = (int)(row - t * C);
+        const I b_ = t / wins;
+        const int win = (int)(t - b_ * wins), b = (int)b_;
         int baseCol = (win / g.hK) * g.stride, baseRow = (win % g.hK) * g.stride;
 #pragma unroll
         for (int i = 0; i < K; i++) {
@@ -123,8 +126,7 @@ __global__ void maxpool_layer_kernel(CSh6<T> in, PoolGeom g, size_t rows, Sh6<T>
             }
         }
     };
-    for (size_t row = blockIdx.x * (size_t)blockDim.x + threadIdx.x; row < rows;
-         row += (size_t)gridDim.x * blockDim.x) {
+    for (I row = blockIdx.x * (I)blockDim.x + threadIdx.x; row < rows; row += (I)gridDim.x * blockDim.x) {
         T v[K][3][2];
         U dr[K][3][2];
         load(row, v);
@@ -133,7 +135,7 @@ __global__ void maxpool_layer_kernel(CSh6<T> in, PoolGeom g, size_t rows, Sh6<T>
         for (int k = 0; k < 6; k++) {
             out.p[k][row] = v[0][k >> 1][k & 1];
             if (maxprime.p[k])
-                for (int i = 0; i < pool; i++) maxprime.p[k][row * pool + i] = dr[i][k >> 1][k & 1];
+                for (int i = 0; i < pool; i++) maxprime.p[k][(size_t)row * pool + i] = dr[i][k >> 1][k & 1];
         }
     }
 }
@@ -204,13 +206,20 @@ int rss_maxpool_layer(Ctx *c, const T *const in[6], T *const out[6], U *const ma
     size_t rows = (size_t)batch * g.wK * g.hK * C;
     // in_zero_mid: the caller knows shares 1-4 of the input are 0 (they are not read)
     const unsigned grid = pool_grid(c, rows);
+    // 32-bit rows while the last row index and the grid stride past it fit
+    const bool narrow = rows + (size_t)grid * 128 < (1ull << 32);
+    const uint32_t rows32 = (uint32_t)rows;
+#define PG_MAXPOOL_LAUNCH(KK, ZZ)                                                                      \
+    (narrow ? maxpool_layer_kernel<T, U, KK, ZZ, uint32_t><<<grid, 128, 0, c->stream>>>(a, g, rows32, o, d) \
+            : maxpool_layer_kernel<T, U, KK, ZZ, size_t><<<grid, 128, 0, c->stream>>>(a, g, rows, o, d))
     if (padded == 4) {
-        if (c->in_zero_mid) maxpool_layer_kernel<T, U, 4, true><<<grid, 128, 0, c->stream>>>(a, g, rows, o, d);
-        else maxpool_layer_kernel<T, U, 4, false><<<grid, 128, 0, c->stream>>>(a, g, rows, o, d);
+        if (c->in_zero_mid) PG_MAXPOOL_LAUNCH(4, true);
+        else PG_MAXPOOL_LAUNCH(4, false);
     } else {
-        if (c->in_zero_mid) maxpool_layer_kernel<T, U, 16, true><<<grid, 128, 0, c->stream>>>(a, g, rows, o, d);
-        else maxpool_layer_kernel<T, U, 16, false><<<grid, 128, 0, c->stream>>>(a, g, rows, o, d);
+        if (c->in_zero_mid) PG_MAXPOOL_LAUNCH(16, true);
+        else PG_MAXPOOL_LAUNCH(16, false);
     }
+#undef PG_MAXPOOL_LAUNCH
     c->launches++;
     int st = launch_status(c, "maxpool_layer_kernel");
     if (st) return st;
