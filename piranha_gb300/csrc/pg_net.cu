@@ -533,6 +533,21 @@ __global__ void replicated6_kernel(CSh6<uint64_t> a, size_t n, int *flag) {
     if (!ok) *flag = 0;
 }
 
+// The SGD step of a weight or bias buffer, w -= dividePublic(dw, d)
+// (CNNLayer.cu:192-193, FCLayer.cu:211,220), in one pass: dividePublic
+// (divide_public_kernel: r = 1, r' = d) leaves the shares [qA, 0, 0, 0, 0, qC],
+// so only shares 0 and 5 of w change. dw itself is left undivided.
+__global__ void sgd6_kernel(Sh6<uint64_t> w, CSh6<uint64_t> dw, size_t n, uint64_t d, int t) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const uint64_t s0 = dw.p[0][i] - d, s5 = dw.p[5][i] - d;
+        const uint64_t s2 = dw.p[2][i], s4 = dw.p[4][i];
+        const uint64_t rA = s0 + dw.p[1][i] + s4;  // party A: own two + C's shareA
+        const uint64_t rC = s4 + s5 + s2;          // party C: own two + B's shareA
+        w.p[0][i] -= 1 + div_public<uint64_t>(rA, d, t);
+        w.p[5][i] -= 1 + div_public<uint64_t>(rC, d, t);
+    }
+}
+
 __global__ void sub6_kernel(Sh6<uint64_t> a, CSh6<uint64_t> b, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
 #pragma unroll
@@ -622,6 +637,21 @@ int sub6(Ctx *c, uint64_t *const *a, const uint64_t *const *b, size_t n) {
     sub6_kernel<<<blocks_for(c, n), 256, 0, c->stream>>>(m6(a), c6(b), n);
     c->launches++;
     return launch_status(c, "sub6_kernel");
+}
+
+// w -= dividePublic(dw, 2^log_lr), with dividePublic's messages counted
+// (rss_divide_public)
+int sgd6(Ctx *c, uint64_t *const *w, const uint64_t *const *dw, size_t n, int log_lr) {
+    if (n) {
+        const uint64_t d = 1ull << log_lr;
+        sgd6_kernel<<<blocks_for(c, n), 256, 0, c->stream>>>(m6(w), c6(dw), n, d, pow2_shift<uint64_t>(d));
+        c->launches++;
+        int st = launch_status(c, "sgd6_kernel");
+        if (st) return st;
+    }
+    comm_msg(c, n * sizeof(uint64_t), n * sizeof(uint64_t));
+    comm_round(c);
+    return PG_OK;
 }
 
 int log_mini_batch(int batch) {  // (int)log2(MINI_BATCH_SIZE), util/model.cu:39
@@ -815,8 +845,7 @@ static int net_backward(pg_net *net, const uint64_t *const in[6], const uint64_t
                     c->launches++;
                     if ((st = launch_status(c, "bias_grad6_kernel"))) return st;
                 }
-                if ((st = rss_divide_public<uint64_t>(c, net->tr.db, L.b_n, 1ull << log_lr, nullptr))) return st;
-                if ((st = sub6(c, L.b, net->tr.db, L.b_n))) return st;
+                if ((st = sgd6(c, L.b, net->tr.db, L.b_n, log_lr))) return st;
                 break;
             }
             case PG_LAYER_CNN: {  // CNNLayer::backward (CNNLayer.cu:114-193)
@@ -831,8 +860,7 @@ static int net_backward(pg_net *net, const uint64_t *const in[6], const uint64_t
                                          net->fp)))
                         return st;
                 }
-                if ((st = rss_divide_public<uint64_t>(c, net->tr.dW, L.w_n, 1ull << log_lr, nullptr))) return st;
-                if ((st = sub6(c, L.w, net->tr.dW, L.w_n))) return st;
+                if ((st = sgd6(c, L.w, net->tr.dW, L.w_n, log_lr))) return st;
                 break;
             }
             case PG_LAYER_RELU:  // ReLULayer::backward (ReLULayer.cu:90-124)
