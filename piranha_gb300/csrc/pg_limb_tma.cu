@@ -376,9 +376,10 @@ struct ReluImageArgs {
 
 constexpr int RI_PIX = 16, RI_CH = 16, RI_PITCH = RI_PIX + 1;  // pitch 17: two-way bank conflicts at most
 
-// ZM: a.zmid (shares 1-4 of the input are 0, not read) as a compile-time fact
+// ZM: a.zmid (shares 1-4 of the input are 0, not read) as a compile-time fact;
+// at most 40 registers, so that six blocks of 256 threads fit on an SM
 template <bool ZM>
-__global__ void __launch_bounds__(256) relu_image_kernel(const __grid_constant__ ReluImageArgs a) {
+__global__ void __launch_bounds__(256, 6) relu_image_kernel(const __grid_constant__ ReluImageArgs a) {
     __shared__ uint64_t zs[6][RI_CH][RI_PITCH];
     // 32-bit tile and pixel arithmetic (relu_image_fits keeps both below 2^31)
     const uint32_t C16 = (uint32_t)(a.C8 >> 1);
