@@ -380,7 +380,10 @@ constexpr int RI_PIX = 16, RI_CH = 16, RI_PITCH = RI_PIX + 1;  // pitch 17: two-
 // at most 40 registers, so that six blocks of 256 threads fit on an SM
 template <bool ZM>
 __global__ void __launch_bounds__(256, 6) relu_image_kernel(const __grid_constant__ ReluImageArgs a) {
-    __shared__ uint64_t zs[6][RI_CH][RI_PITCH];
+    // two staging buffers, alternating by round: a round's ReLU writes one
+    // while nothing reads it (the other round's digit phase reads the other),
+    // so one barrier per tile suffices
+    __shared__ uint64_t zbuf[2][6][RI_CH][RI_PITCH];
     // 32-bit tile and pixel arithmetic (relu_image_fits keeps both below 2^31)
     const uint32_t C16 = (uint32_t)(a.C8 >> 1);
     const uint64_t C = 8ull * a.C8;
@@ -388,7 +391,9 @@ __global__ void __launch_bounds__(256, 6) relu_image_kernel(const __grid_constan
     const uint32_t tiles = (pixels + RI_PIX - 1) / RI_PIX * C16;
     const uint32_t bi_n = (uint32_t)a.bi_n, bi_hw = (uint32_t)a.bi_hw;
     const int t = threadIdx.x;
-    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    int round = 0;
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x, round ^= 1) {
+        uint64_t (*zs)[RI_CH][RI_PITCH] = zbuf[round];
         const uint32_t pt = tile / C16;
         const uint32_t cp = tile - pt * C16;
         const uint32_t p0 = pt * RI_PIX;
@@ -441,7 +446,9 @@ __global__ void __launch_bounds__(256, 6) relu_image_kernel(const __grid_constan
                     a.img[((long long)(seg * 8 + i) * a.C8 + cb) * a.pixels_alloc + pix] = plv[i];
             }
         }
-        __syncthreads();
+        // no barrier here: the next round writes the other buffer, and the
+        // round after it passes the next round's barrier first, which every
+        // thread reaches only after this digit phase
     }
 }
 
