@@ -58,7 +58,7 @@ LIMB_FLOPS_PER_RING_MAC = 72  # 36 8-bit limb pairs x 2 flops: exact u64 MAC on 
 # batch-128 forward, from one ncu capture of dram__bytes_read.sum +
 # dram__bytes_write.sum over those launches (bench.py --steps 1 --warmup 3
 # --form tc under ncu with the plain run's tuning cache)
-VGG16_B128_LIMB_TRAFFIC = 5_495_756_032
+VGG16_B128_LIMB_TRAFFIC = 5_513_132_544
 
 WORKLOADS = {
     "vgg16": {"metric": "3PC VGG16 secure inference img/s", "kind": "infer3", "fp": 26, "ring": "u64",
