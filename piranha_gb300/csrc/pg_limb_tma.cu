@@ -377,8 +377,12 @@ struct ReluImageArgs {
 constexpr int RI_PIX = 16, RI_CH = 16, RI_PITCH = RI_PIX + 1;  // pitch 17: two-way bank conflicts at most
 
 // ZM: a.zmid (shares 1-4 of the input are 0, not read) as a compile-time fact;
-// at most 40 registers, so that six blocks of 256 threads fit on an SM
-template <bool ZM>
+// RELU = false: no ReLU, the digit image of the input itself (run_image's
+// rows of a position-major image, whose consecutive image rows are rows of
+// different images: read here as whole 128-byte lines of a row), and with
+// three plane blocks only shares 0, 2 and 4 are read. At most 40 registers,
+// so that six blocks of 256 threads fit on an SM.
+template <bool ZM, bool RELU>
 __global__ void __launch_bounds__(256, 6) relu_image_kernel(const __grid_constant__ ReluImageArgs a) {
     // two staging buffers, alternating by round: a round's ReLU writes one
     // while nothing reads it (the other round's digit phase reads the other),
@@ -411,16 +415,22 @@ __global__ void __launch_bounds__(256, 6) relu_image_kernel(const __grid_constan
                 uint64_t x[3][2], zero[3][2];
 #pragma unroll
                 for (int k = 0; k < 6; k++) {
-                    x[k >> 1][k & 1] = (ZM && k > 0 && k < 5) ? 0 : __ldg(a.in[k] + idx);
+                    const bool skip = (ZM && k > 0 && k < 5) || (!RELU && a.nseg == 3 && (k & 1));
+                    x[k >> 1][k & 1] = skip ? 0 : __ldg(a.in[k] + idx);
                     zero[k >> 1][k & 1] = 0;
                 }
-                uint8_t r[3][2];
-                drelu_value<uint64_t, uint8_t>(x, r);
-                select_value<uint64_t, uint8_t>(zero, x, r, z);
+                if constexpr (RELU) {
+                    uint8_t r[3][2];
+                    drelu_value<uint64_t, uint8_t>(x, r);
+                    select_value<uint64_t, uint8_t>(zero, x, r, z);
 #pragma unroll
-                for (int k = 0; k < 6; k++) {
-                    if (a.out[0]) a.out[k][idx] = z[k >> 1][k & 1];
-                    if (a.dout[k]) a.dout[k][idx] = r[k >> 1][k & 1];
+                    for (int k = 0; k < 6; k++) {
+                        if (a.out[0]) a.out[k][idx] = z[k >> 1][k & 1];
+                        if (a.dout[k]) a.dout[k][idx] = r[k >> 1][k & 1];
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 6; k++) z[k >> 1][k & 1] = x[k >> 1][k & 1];
                 }
             } else {
 #pragma unroll
@@ -1920,8 +1930,8 @@ int run_relu_image(Ctx *c, const Plan &p, const uint64_t *const in[6], size_t n,
     const long long tiles = (long long)(a.C8 / 2) * ((p.pixels + RI_PIX - 1) / RI_PIX);
     const int sms = c->sm_count > 0 ? c->sm_count : 148;
     long long blocks = tiles < (long long)sms * 16 ? tiles : (long long)sms * 16;
-    if (a.zmid) relu_image_kernel<true><<<(unsigned)blocks, 256, 0, c->stream>>>(a);
-    else relu_image_kernel<false><<<(unsigned)blocks, 256, 0, c->stream>>>(a);
+    if (a.zmid) relu_image_kernel<true, true><<<(unsigned)blocks, 256, 0, c->stream>>>(a);
+    else relu_image_kernel<false, true><<<(unsigned)blocks, 256, 0, c->stream>>>(a);
     c->launches++;
     return launch_status(c, "relu_image_kernel");
 }
@@ -1971,6 +1981,31 @@ int run_image(Ctx *c, const Plan &p, const uint64_t *const a[6], void *image, bo
         wgt_image_kernel<<<(unsigned)blocks, 256, 0, c->stream>>>(wa);
         c->launches++;
         return launch_status(c, "wgt_image_kernel");
+    }
+    if (p.src_mode == SRC_ROWS && p.posmajor && !rep_flag && p.pixels_alloc == p.pixels &&
+        relu_image_fits(p, (size_t)p.pixels * p.C)) {
+        // a position-major image of whole rows: the staged kernel reads each
+        // source row as whole lines (the generic one below reads 64 bytes of
+        // rows one image apart per thread)
+        ReluImageArgs ra;
+        memset(&ra, 0, sizeof(ra));
+        for (int k = 0; k < 6; k++) {
+            if (!a[k]) return set_error(c, PG_ERR_INVALID_ARG, "null share pointer");
+            ra.in[k] = a[k];
+        }
+        ra.img = (uint4 *)image;
+        ra.pixels = p.pixels;
+        ra.pixels_alloc = p.pixels_alloc;
+        ra.C8 = p.C / 8;
+        ra.bi_n = p.Nimg;
+        ra.bi_hw = (long long)p.Himg * p.Wimg;
+        ra.nseg = shared ? 3 : 6;
+        const long long tiles = (long long)(ra.C8 / 2) * ((p.pixels + RI_PIX - 1) / RI_PIX);
+        const int sms = c->sm_count > 0 ? c->sm_count : 148;
+        const long long blocks = tiles < (long long)sms * 16 ? tiles : (long long)sms * 16;
+        relu_image_kernel<false, false><<<(unsigned)blocks, 256, 0, c->stream>>>(ra);
+        c->launches++;
+        return launch_status(c, "relu_image_kernel");
     }
     ImageArgs ia;
     memset(&ia, 0, sizeof(ia));
